@@ -1,0 +1,224 @@
+/*
+ * vca_gpu.h -- C-ABI of the GB300 cluster exact-diagonalization path of VCA.
+ *
+ * One process, one GPU, one global solver context (not thread-safe, not
+ * reentrant), one CUDA stream, synchronous return.  Every array argument is a
+ * HOST pointer in Fortran column-major order and is neither retained nor
+ * modified after return unless it is an output.  complex(8) arrays are passed
+ * as `double*` pointing at interleaved (re, im) pairs: the memory layout of a
+ * Fortran complex(c_double_complex) array and of a C99 double _Complex array.
+ *
+ * Reference interface replaced (paths inside QcmPlab/VCA):
+ *   vca_init_solver  VCA_MAIN.f90:51-76   (MPI form :79-115)
+ *   vca_solve        VCA_MAIN.f90:124-215 (MPI form :220-323)
+ *   vca_get_sft_potential   VCA_IO/get_sft_potential.f90:1-4
+ *   vca_gf_cluster   VCA_IO/gf_cluster.f90:1-88 (generic at VCA_IO.f90:38-62)
+ *   spHtimesV_p / cc_sparse_HxV  VCA_VARS_GLOBAL.f90:83-89,137
+ * Configuration mirrors the module variables of VCA_INPUT_VARS.f90:14-81 with
+ * the defaults of VCA_INPUT_VARS.f90:112-172 (vca_config_defaults).
+ *
+ * Status codes: 0 = OK, negative = error (vca_gpu_last_error gives the text).
+ */
+#ifndef VCA_GPU_H
+#define VCA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VCA_OK 0
+#define VCA_ERR_CONFIG (-1)      /* invalid or unsupported input variable     */
+#define VCA_ERR_SHAPE (-2)       /* array extents inconsistent with config    */
+#define VCA_ERR_STATE (-3)       /* call order: init missing, no solve yet    */
+#define VCA_ERR_CUDA (-4)        /* CUDA runtime error                        */
+#define VCA_ERR_TIMEOUT (-5)     /* a bounded device wait ran out             */
+#define VCA_ERR_UNSUPPORTED (-6) /* feature outside the implemented path      */
+#define VCA_ERR_NUMERIC (-7)     /* NaN/Inf input, zero-norm vector, breakdown */
+#define VCA_ERR_ALLOC (-8)       /* device memory exhausted                   */
+#define VCA_ERR_ARG (-9)         /* null pointer or out-of-range index        */
+
+#define VCA_LANC_ARPACK 0
+#define VCA_LANC_LANCZOS 1
+
+/*
+ * Input variables.  Field names, meanings and defaults follow
+ * VCA_INPUT_VARS.f90:14-81 / :112-172.  Integers are 32-bit, logicals are
+ * 0/1.  Fields after `verbose` have no counterpart in the reference: they fix
+ * what the reference leaves to SciFortran defaults (Lanczos stopping rule,
+ * start vector) or replaces (the adaptive QUADPACK integral becomes a fixed
+ * Gauss-Legendre rule).
+ */
+typedef struct vca_config {
+  int32_t Norb;      /* NORB       orbitals per cluster site (<= 5)          */
+  int32_t Nspin;     /* NSPIN      1 or 2                                   */
+  int32_t Nlat;      /* NLAT       cluster sites                            */
+  int32_t Nlat_bath; /* NLAT_BATH  bath "site" levels                       */
+  int32_t Norb_bath; /* NORB_BATH  bath "orb" levels                        */
+  int32_t pad0;
+  double Uloc[5];    /* ULOC       on-site interaction per orbital          */
+  double Ust;        /* UST        inter-orbital opposite-spin interaction  */
+  double Jh;         /* JH         Hund coupling (Ust-Jh parallel spins)    */
+  double Jx;         /* JX         parsed, not part of H (as reference)     */
+  double Jp;         /* JP         parsed, not part of H (as reference)     */
+  double xmu;        /* XMU        chemical potential                       */
+  double beta;       /* BETA       inverse temperature (IR cut-off at T=0)  */
+  double eps;        /* EPS        real-axis broadening                     */
+  double wini;       /* WINI       real-axis grid start                     */
+  double wfin;       /* WFIN       real-axis grid end                       */
+  int32_t hfmode;    /* HFMODE     U(n-1/2)(n-1/2) form                     */
+  int32_t hfshift;   /* HFSHIFT    bath half-filling shift                  */
+  int32_t Lmats;     /* LMATS      Matsubara frequencies                    */
+  int32_t Lreal;     /* LREAL      real-axis frequencies                    */
+  int32_t lanc_method;         /* LANC_METHOD  VCA_LANC_ARPACK | VCA_LANC_LANCZOS */
+  int32_t lanc_niter;          /* LANC_NITER                              */
+  int32_t lanc_ngfiter;        /* LANC_NGFITER  GF chain length           */
+  int32_t lanc_dim_threshold;  /* LANC_DIM_THRESHOLD  dense path below    */
+  int32_t lanc_nstates_sector; /* LANC_NSTATES_SECTOR                     */
+  int32_t lanc_nstates_total;  /* LANC_NSTATES_TOTAL  1 => T=0            */
+  double lanc_tolerance;       /* LANC_TOLERANCE                          */
+  double gs_threshold;         /* GS_THRESHOLD  GS degeneracy window      */
+  int32_t vca_gf_symmetric;    /* VCA_GF_SYMMETRIC  2-channel off-diag GF */
+  int32_t vca_sparse_H;        /* VCA_SPARSE_H  stored semantics (always) */
+  int32_t vca_twin;            /* VCA_TWIN                                */
+  int32_t vca_sectors;         /* VCA_SECTORS   restrict sector scan      */
+  int32_t vca_sectors_shift;   /* VCA_SECTORS_SHIFT                       */
+  int32_t verbose;             /* VERBOSE                                 */
+  /* ---- no counterpart in the reference ---------------------------------- */
+  int32_t omega_nodes;     /* Gauss-Legendre nodes on [0,inf) for Omega     */
+  int32_t gs_check_every;  /* Lanczos GS convergence test interval          */
+  double omega_scale;      /* map w = omega_scale * s/(1-s), s in (0,1)     */
+  double gs_residual_tol;  /* GS stop: |beta_{k+1} s_k| <= tol*max(1,|E|)   */
+  double gf_beta_tol;      /* GF chain stop: beta_{k+1} < tol (exhausted)   */
+  uint64_t start_seed;     /* seed of the deterministic Lanczos start vector */
+  int32_t reserved[8];
+} vca_config;
+
+/* Fill *cfg with the reference defaults (VCA_INPUT_VARS.f90:112-172) plus
+ * the build-specific defaults above. */
+void vca_config_defaults(vca_config* cfg);
+
+/*
+ * vca_init_solver replacement (VCA_MAIN.f90:51-76).  Validates the config,
+ * builds the sector tables (VCA_SETUP.f90:81-94,259-390), selects the GPU and
+ * creates the stream.  bath_h/bath_v are optional (both NULL = no bath, which
+ * sets Nlat_bath = Norb_bath = 0 as VCA_MAIN.f90:64-66 does); when given their
+ * shapes are (Nlat_bath,Nlat_bath,Nspin,Nspin,Norb_bath,Norb_bath) and
+ * (Nlat,Nlat_bath,Nspin,Nspin,Norb,Norb_bath).  A second call re-initialises.
+ */
+int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath_v);
+
+/*
+ * vca_solve replacement (VCA_MAIN.f90:124-215), T=0 path.
+ *   Hloc  (Nlat,Nlat,Nspin,Nspin,Norb,Norb)        complex, read-only
+ *   Hk    (Nlat,Nlat,Nspin,Nspin,Norb,Norb,Nk)     complex, read-only
+ *   bath_h/bath_v as in vca_gpu_init (NULL when the model has no bath)
+ *   omega_out  receives the SFT grand potential E_gs - Omega_int (may be NULL)
+ * Diagonalises every sector, builds the cluster Green's function chains and
+ * integrates the Potthoff functional on the imaginary axis.
+ */
+int vca_gpu_solve(const double* Hloc, const double* Hk, int64_t Nk,
+                  const double* bath_h, const double* bath_v, double* omega_out);
+
+/*
+ * Batched solve: B variational points in one call.  No counterpart in the
+ * reference (it replaces a driver loop of vca_solve calls, e.g.
+ * drivers/vca_hm_chain1d.f90:88-111).  Point b uses Hloc + b*stride_hloc
+ * complex elements, and bath_h/bath_v likewise (NULL = no bath); Hk is shared
+ * by all points.  omega_out[b] receives the SFT potential of point b.
+ */
+int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc,
+                        const double* Hk, int64_t Nk,
+                        const double* bath_h, int64_t stride_bath_h,
+                        const double* bath_v, int64_t stride_bath_v,
+                        double* omega_out);
+
+/* Results of the last vca_gpu_solve (VCA_IO/get_sft_potential.f90:1-4). */
+int vca_gpu_get_sft_potential(double* omega);
+/* Ground-state energy E_gs and Omega integral: sft = egs - omega_int. */
+int vca_gpu_get_energies(double* egs, double* omega_int);
+
+/*
+ * Cluster Green's function G'(z) at nz complex points (VCA_IO/gf_cluster.f90:
+ * 1-64, including the off-diagonal recombination :50-62).  gf_out has shape
+ * (Nlat,Nlat,Nspin,Nspin,Norb,Norb,nz), complex, spin-off-diagonal blocks 0.
+ */
+int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out);
+
+/*
+ * Matsubara / real-axis cluster Green's function on the reference grids
+ * wm = pi/beta*(2n-1), n=1..Lmats and wr = linspace(wini,wfin,Lreal)+i*eps
+ * (VCA_GF_SHARED.f90:43-56, accumulation VCA_GF_NORMAL.f90:1024-1031):
+ * shapes (Nlat,Nlat,Nspin,Nspin,Norb,Norb,Lmats|Lreal).
+ */
+int vca_gpu_get_gimp_matsubara(double* g_out);
+int vca_gpu_get_gimp_realaxis(double* g_out);
+
+/*
+ * Ground-state bookkeeping of the last solve (VCA_DIAG.f90:224-236,
+ * VCA_EIGENSPACE.f90:136-216): number of retained T=0 states, and per state
+ * its sector (1-based, as get_Sector) and energy.
+ */
+int vca_gpu_get_state_count(int32_t* nstates);
+int vca_gpu_get_state(int32_t istate, int32_t* isector, double* energy);
+/* Lowest eigenvalue found in every sector (Nsectors entries, 1-based order);
+ * sectors not scanned hold +inf. */
+int vca_gpu_get_sector_energies(double* e_out, int32_t n);
+
+/*
+ * Pole/weight table of one Green's function element, the GFmatrix of
+ * VCA_VARS_GLOBAL.f90:54-71 filled by VCA_GF_NORMAL.f90:970-1033:
+ * element (ilat,jlat,ispin,iorb,jorb) 1-based, state istate, channel ichan.
+ * *nexc receives the number of excitations; poles and weights (complex,
+ * capacity cap) receive them when cap >= *nexc.
+ */
+int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t iorb,
+                           int32_t jorb, int32_t istate, int32_t ichan, int32_t* nexc,
+                           double* poles, double* weights, int32_t cap);
+
+/* Omega integrand f(w) = (1/Lk) sum_k ln|det(1+(Delta+Hloc-Hk)G'(iw))|
+ * (VCA_OMEGA.f90:37-75) at nw real frequencies, from the last solve. */
+int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out);
+
+/* Release every device buffer and the stream. */
+int vca_gpu_finalize(void);
+
+/* Text of the last error (empty when none).  Returns the string length. */
+int vca_gpu_last_error(char* buf, int32_t len);
+
+/* ---- parity hooks on the H x v contract ------------------------------- */
+/*
+ * Sector information (VCA_SETUP.f90:404-458,660-695): 1-based isector,
+ * n_up, n_dw, DimUp, DimDw.  Needs vca_gpu_init only.
+ */
+int vca_gpu_sector_info(int32_t isector, int32_t* nup, int32_t* ndw, int64_t* dimup,
+                        int64_t* dimdw);
+/* Fock words of the up (spin=1) or down (spin=2) map of a sector, built on
+ * the GPU (build_sector, VCA_SETUP.f90:660-695): map[k] = word, k = 0..Dim-1. */
+int vca_gpu_sector_map(int32_t isector, int32_t spin, int64_t* map, int64_t cap);
+/*
+ * Load the one-body data of a solve point without solving: Hloc, bath_h,
+ * bath_v as in vca_gpu_solve.  Used before vca_gpu_hxv.
+ */
+int vca_gpu_set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath_v);
+/*
+ * Hv = H v on sector isector: the cc_sparse_HxV(Nloc,v,Hv) contract of
+ * VCA_VARS_GLOBAL.f90:83-89 with the stored semantics of
+ * VCA_HAMILTONIAN_SPARSE_HxV.f90:152-200.  v, hv: complex[dim] host arrays,
+ * index i = iup + (idw-1)*DimUp (1-based, VCA_SETUP.f90:505-518).
+ */
+int vca_gpu_hxv(int32_t isector, const double* v, double* hv);
+/* Same product on DEVICE buffers: v/hv are complex[dim] (is_complex=1) or
+ * real[dim] (is_complex=0, only for a real Hamiltonian), on the library stream. */
+int vca_gpu_hxv_device(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex);
+/* Run the H x v kernel `reps` times on device buffers and report the mean
+ * device time per product in milliseconds (CUDA events on the library stream). */
+int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex,
+                      int32_t reps, double* ms_per_call);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VCA_GPU_H */
