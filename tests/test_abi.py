@@ -1,0 +1,59 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol
+declared in include/vca_gpu.h, and its config defaults match the Python
+mirror of VCA_INPUT_VARS.f90 defaults."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from vca_gb300 import solver
+from vca_gb300.config import VcaConfig, default_config
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "vca_gpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void)\s+(vca_\w+)\s*\(", txt, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from vca_gb300 import build
+    build.build()
+    return solver.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(solver.EXPORTS) == syms
+
+
+def test_config_layout_and_defaults(lib):
+    c = solver.library_defaults()
+    d = default_config()
+    assert ctypes.sizeof(VcaConfig) == ctypes.sizeof(c)
+    assert c.as_dict() == d.as_dict()
+
+
+def test_init_without_gpu_reports_error(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    c = default_config(Nlat=2)
+    rc = lib.vca_gpu_init(ctypes.byref(c), None, None)
+    assert rc == -4
+    buf = ctypes.create_string_buffer(256)
+    lib.vca_gpu_last_error(buf, 256)
+    assert b"no CPU fallback" in buf.value
+
+
+def test_bad_config_rejected_on_host(lib):
+    c = default_config(Nlat=2, Nspin=3)
+    assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
+    c = default_config(Nlat=2, lanc_nstates_total=2)
+    assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -6

@@ -1,0 +1,123 @@
+"""GPU parity: the CUDA path through the C-ABI against the CPU oracle.
+
+Tolerances (from the parity targets of this path): Fock maps, sector tables
+and matrix-element signs bit-exact; H x v to 1e-13 relative; ground-state
+energies and Omega to 1e-10 relative; G'(i w) to 1e-8 absolute.
+"""
+import numpy as np
+import pytest
+
+from vca_gb300 import clusters
+from vca_gb300.solver import VcaSolver, VcaError
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-10
+G_TOL = 1e-8
+
+
+def _rng(seed=7):
+    return np.random.default_rng(seed)
+
+
+def _small_bath(nb=4, seed=11, **kw):
+    return clusters.square_bath(nb=nb, nk1=6, ngfiter=60, omega_nodes=256, seed=seed, **kw)
+
+
+POINTS = {
+    "chain4": lambda: clusters.chain1d(tprime=0.9, nlat=4, U=4.0, xmu=2.0, nk=16, ngfiter=100,
+                                       omega_nodes=256),
+    "square2x2_afm": lambda: clusters.square(nx=2, ny=2, U=8.0, xmu=4.0, maf=0.2, nspin=2, nkx=6,
+                                             nky=6, ngfiter=80, omega_nodes=256),
+    "bath2x2+4": lambda: _small_bath(),
+    "bhz_small": lambda: clusters.bhz(mass=2.2, delta=0.1, nk1=4, ngfiter=60, omega_nodes=256),
+}
+
+
+@pytest.fixture(scope="module", params=list(POINTS))
+def point(request):
+    return POINTS[request.param]()
+
+
+def test_sector_maps_bitexact(point):
+    s = VcaSolver(point.cfg, point.bath_h, point.bath_v)
+    o = Oracle.from_point(point)
+    assert s.Ns == o.Ns
+    for isec in range(1, o.Nsectors + 1):
+        assert s.sector_info(isec) == o.sector_info(isec)
+        for spin in (1, 2):
+            np.testing.assert_array_equal(s.sector_map(isec, spin), o.sector_map(isec, spin))
+
+
+def test_hxv_matches_oracle(point):
+    s = VcaSolver(point.cfg, point.bath_h, point.bath_v)
+    s.set_hamiltonian(point.Hloc, point.bath_h, point.bath_v)
+    o = Oracle.from_point(point)
+    rng = _rng()
+    worst = 0.0
+    for isec in range(1, o.Nsectors + 1):
+        d = o.dim(isec)
+        if d > 20000:
+            continue
+        v = rng.normal(size=d) + 1j * rng.normal(size=d)
+        ref = o.hxv(isec, v)
+        got = s.hxv(isec, v)
+        scale = max(1.0, np.abs(ref).max())
+        worst = max(worst, np.abs(got - ref).max() / scale)
+    assert worst < 1e-13, worst
+
+
+def test_solve_matches_oracle(point):
+    s = VcaSolver(point.cfg, point.bath_h, point.bath_v)
+    om = s.solve(point.Hloc, point.Hk, point.bath_h, point.bath_v)
+    o = Oracle.from_point(point)
+    ref, egs_ref, oi_ref = o.solve()
+    egs, oi = s.energies()
+    assert abs(egs - egs_ref) <= E_TOL * abs(egs_ref)
+    # every sector's lowest eigenvalue
+    se = s.sector_energies()
+    so = o.sector_energies()
+    np.testing.assert_allclose(se, so, rtol=E_TOL, atol=E_TOL)
+    # ground-state list
+    st = s.states()
+    so_states = []
+    k = 0
+    while True:
+        r = o.state(k) if k < 64 else None
+        if r is None or r[0] <= 0:
+            break
+        so_states.append(r[:2])
+        k += 1
+    assert [x[0] for x in st] == [x[0] for x in so_states]
+    np.testing.assert_allclose([x[1] for x in st], [x[1] for x in so_states], rtol=E_TOL)
+    assert abs(om - ref) <= E_TOL * abs(ref), (om, ref)
+    # cluster Green's function on the imaginary axis
+    z = 1j * np.array([0.05, 0.3, 1.0, 3.0, 10.0])
+    g = s.gf_cluster(z)
+    go = o.gf_cluster(z)
+    assert np.abs(g - go).max() < G_TOL, np.abs(g - go).max()
+
+
+def test_sum_kmesh_matches_oracle():
+    pt = POINTS["square2x2_afm"]()
+    s = VcaSolver(pt.cfg)
+    s.solve(pt.Hloc, pt.Hk)
+    o = Oracle.from_point(pt)
+    o.solve()
+    w = np.array([0.01, 0.5, 2.0, 40.0, 1e4])
+    f = s.sum_kmesh(w)
+    fo = np.array([o.sum_kmesh(x) for x in w])
+    np.testing.assert_allclose(f, fo, rtol=1e-10, atol=1e-12)
+
+
+def test_shape_errors_raise():
+    pt = POINTS["chain4"]()
+    s = VcaSolver(pt.cfg)
+    with pytest.raises(VcaError):
+        s.solve(pt.Hloc[:2], pt.Hk)
+    bad = pt.Hloc.copy()
+    bad[0, 0, 0, 0, 0, 0] = np.nan
+    with pytest.raises(VcaError) as ei:
+        s.solve(bad, pt.Hk)
+    assert ei.value.code == -7

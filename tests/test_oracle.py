@@ -1,0 +1,274 @@
+"""The oracle (CPU restatement) pinned against independent constructions.
+
+The reference has no tests or golden vectors and cannot be built here, so the
+oracle is checked against: an independent numpy construction of the sector
+Hamiltonian from the operator definitions, dense exact diagonalisation, the
+Hubbard-dimer and U=0 closed forms, and scipy's LAPACK / QUADPACK.
+"""
+import itertools
+
+import numpy as np
+import pytest
+import scipy.integrate
+import scipy.linalg
+
+from vca_gb300 import clusters
+from vca_gb300.clusters import nnn2lso
+from oracle import oracle as orc
+from oracle.oracle import Oracle
+
+
+# ---------------------------------------------------------------------------
+# independent numpy restatement of the operator algebra (small Ns only)
+# ---------------------------------------------------------------------------
+def words(ns, n):
+    return [w for w in range(1 << ns) if bin(w).count("1") == n]
+
+
+def one_word_sign(w, pos):  # pos 0-based: (-1)^(set bits below pos)
+    return -1.0 if bin(w & ((1 << pos) - 1)).count("1") % 2 else 1.0
+
+
+def spin_matrix_np(ns, n, A):
+    """H_sigma[target, source] = sum_{i!=j} A[i,j] c^dag_i c_j on words of popcount n."""
+    ws = words(ns, n)
+    idx = {w: k for k, w in enumerate(ws)}
+    H = np.zeros((len(ws), len(ws)), dtype=complex)
+    for s, w in enumerate(ws):
+        for i in range(ns):
+            for j in range(ns):
+                if i == j or A[i, j] == 0:
+                    continue
+                if (w >> j) & 1 and not (w >> i) & 1:
+                    sg1 = one_word_sign(w, j)
+                    k1 = w & ~(1 << j)
+                    sg2 = one_word_sign(k1, i)
+                    H[idx[k1 | (1 << i)], s] += A[i, j] * sg1 * sg2
+    return H
+
+
+def amplitude_matrix(pt, sidx):
+    c = pt.cfg
+    L = c.Nlat * c.Norb
+    ns = L + c.Nlat_bath * c.Norb_bath
+    A = np.zeros((ns, ns), dtype=complex)
+    for il, jl, io, jo in itertools.product(range(c.Nlat), range(c.Nlat), range(c.Norb), range(c.Norb)):
+        A[io + il * c.Norb, jo + jl * c.Norb] = pt.Hloc[il, jl, sidx, sidx, io, jo]
+    if pt.bath_h is not None:
+        for a, b, oa, ob in itertools.product(range(c.Nlat_bath), range(c.Nlat_bath), range(c.Norb_bath),
+                                              range(c.Norb_bath)):
+            A[L + a * c.Norb_bath + oa, L + b * c.Norb_bath + ob] = pt.bath_h[a, b, sidx, sidx, oa, ob]
+        for il, b, io, ob in itertools.product(range(c.Nlat), range(c.Nlat_bath), range(c.Norb),
+                                               range(c.Norb_bath)):
+            v = pt.bath_v[il, b, sidx, sidx, io, ob]
+            A[io + il * c.Norb, L + b * c.Norb_bath + ob] = v
+            A[L + b * c.Norb_bath + ob, io + il * c.Norb] = np.conj(v)
+    np.fill_diagonal(A, 0)
+    return A
+
+
+SMALL = {
+    "chain4": lambda: clusters.chain1d(tprime=0.9, nlat=4, U=4.0, xmu=2.0, nk=8, omega_nodes=128),
+    "square2x2": lambda: clusters.square(nx=2, ny=2, U=6.0, xmu=3.0, maf=0.15, nspin=2, nkx=4, nky=4,
+                                         omega_nodes=128),
+    "bath2+2": lambda: clusters.square_bath(nb=2, nk1=4, omega_nodes=128, ngfiter=50),
+    "bhz": lambda: clusters.bhz(nk1=2, omega_nodes=64, ngfiter=40),
+}
+
+
+@pytest.fixture(params=list(SMALL))
+def small(request):
+    return SMALL[request.param]()
+
+
+def test_sector_tables():
+    pt = clusters.chain1d(nlat=4, nk=2)
+    o = Oracle.from_point(pt)
+    assert o.Ns == 4 and o.Nsectors == 25
+    total = 0
+    for isec in range(1, 26):
+        nu, nd, du, dd = o.sector_info(isec)
+        assert isec == 1 + nd + nu * 5  # get_Sector (VCA_SETUP.f90:404-415)
+        assert du == orc.lib().orc_binomial(4, nu) and dd == orc.lib().orc_binomial(4, nd)
+        total += du * dd
+        assert o.cdg_sector(isec, 1) == (1 + nd + (nu + 1) * 5 if nu < 4 else 0)
+        assert o.c_sector(isec, 2) == (1 + (nd - 1) + nu * 5 if nd > 0 else 0)
+        np.testing.assert_array_equal(o.sector_map(isec, 1), words(4, nu))
+    assert total == 4 ** 4
+    for n in range(17):  # binomial through FP64 rounding is exact up to Ns=16
+        assert orc.lib().orc_binomial(16, n) == scipy.special.comb(16, n, exact=True)
+
+
+def test_spin_matrices_match_operator_algebra(small):
+    o = Oracle.from_point(small)
+    c = small.cfg
+    for isec in [1 + (o.Ns // 2) + (o.Ns // 2) * (o.Ns + 1), 1 + 1 + 2 * (o.Ns + 1)]:
+        nu, nd, du, dd = o.sector_info(isec)
+        for spin, n, sidx in ((1, nu, 0), (2, nd, c.Nspin - 1)):
+            r, cc, v = o.spin_matrix(isec, spin)
+            dim = du if spin == 1 else dd
+            H = np.zeros((dim, dim), dtype=complex)
+            np.add.at(H, (r, cc), v)
+            Hn = spin_matrix_np(o.Ns, n, amplitude_matrix(small, sidx))
+            np.testing.assert_array_equal(H, Hn)
+
+
+def test_dense_hermitian_and_hxv(small):
+    o = Oracle.from_point(small)
+    rng = np.random.default_rng(3)
+    for isec in range(1, o.Nsectors + 1):
+        d = o.dim(isec)
+        if d > 400:
+            continue
+        H = o.dense_h(isec)
+        np.testing.assert_allclose(H, H.conj().T, atol=1e-14)
+        v = rng.normal(size=d) + 1j * rng.normal(size=d)
+        np.testing.assert_allclose(o.hxv(isec, v), H @ v, atol=1e-12)
+
+
+def test_dimer_closed_form():
+    for U in (0.5, 3.0, 8.0):
+        # half filling (xmu = U/2): the N=2 singlet, E = (U - sqrt(U^2+16t^2))/2 - 2*xmu
+        pt = clusters.chain1d(tprime=1.0, nlat=2, U=U, xmu=U / 2, nk=2, omega_nodes=32)
+        o = Oracle.from_point(pt)
+        o.diagonalize()
+        assert abs(o.egs() - ((U - np.sqrt(U * U + 16)) / 2 - U)) < 1e-12
+
+
+def test_lanczos_gs_matches_lapack(small):
+    o = Oracle.from_point(small)
+    for isec in range(1, o.Nsectors + 1):
+        d = o.dim(isec)
+        if d < 2 or d > 600:
+            continue
+        w, V = np.linalg.eigh(o.dense_h(isec))
+        e, psi, it = o.lanczos_gs(isec)
+        assert abs(e - w[0]) < 1e-11 * max(1, abs(w[0]))
+        H = o.dense_h(isec)
+        assert np.linalg.norm(H @ psi - e * psi) < 1e-9
+
+
+def test_tql2_and_tridiagonal_lowest():
+    rng = np.random.default_rng(5)
+    for n in (1, 2, 7, 60, 200):
+        d = rng.normal(size=n)
+        e = np.r_[0.0, rng.normal(size=n - 1)]
+        w, z0, r = orc.tql2(d, e)
+        ww, V = scipy.linalg.eigh_tridiagonal(d, e[1:])
+        assert r == 0
+        np.testing.assert_allclose(w, ww, atol=1e-12)
+        np.testing.assert_allclose(z0 ** 2, V[0] ** 2, atol=1e-12)
+        th, s = orc.tri_lowest(d, e[1:])
+        assert abs(th - ww[0]) < 1e-12
+        assert min(np.linalg.norm(s - V[:, 0]), np.linalg.norm(s + V[:, 0])) < 1e-9
+
+
+def test_gauss_legendre_nodes():
+    for n in (8, 256, 4096):
+        x, w = orc.gauss_legendre01(n)
+        xr, wr = np.polynomial.legendre.leggauss(n)
+        np.testing.assert_allclose(x, 0.5 * (xr + 1), atol=1e-14)
+        # exact for monomials of degree < 2n (numpy's own weights drift ~1e-7 at n=4096)
+        for k in (0, 1, 7, n, 2 * n - 1):
+            assert abs((w * x ** k).sum() * (k + 1) - 1.0) < 1e-12
+
+
+def _exact_gf(o, pt, z, ispin=1):
+    """G_ij(z) by dense ED of the N+-1 sectors (T=0, one ground state)."""
+    c = pt.cfg
+    isec, e0, psi = o.state(0, with_vector=True)
+    nu, nd, du, dd = o.sector_info(isec)
+    L = c.Nlat * c.Norb
+    out = np.zeros((L, L, len(z)), dtype=complex)
+
+    def op_matrix(tsec, pos, dag):
+        # matrix of c^dag_pos (dag) or c_pos from isec to tsec on spin `ispin`
+        tnu, tnd, tdu, tdd = o.sector_info(tsec)
+        mu_s, md_s = words(o.Ns, nu), words(o.Ns, nd)
+        mu_t, md_t = words(o.Ns, tnu), words(o.Ns, tnd)
+        iu = {w: k for k, w in enumerate(mu_t)}
+        idd = {w: k for k, w in enumerate(md_t)}
+        M = np.zeros((tdu * tdd, du * dd))
+        for s in range(du * dd):
+            wu, wd = mu_s[s % du], md_s[s // du]
+            w = wu if ispin == 1 else wd
+            occ = (w >> pos) & 1
+            if occ == dag:
+                continue
+            sg = one_word_sign(w, pos)
+            w2 = w ^ (1 << pos)
+            t = (iu[w2] + idd[wd] * tdu) if ispin == 1 else (iu[wu] + idd[w2] * tdu)
+            M[t, s] = sg
+        return M
+
+    for dag, fsec in ((1, o.cdg_sector(isec, ispin)), (0, o.c_sector(isec, ispin))):
+        if not fsec:
+            continue
+        w, V = np.linalg.eigh(o.dense_h(fsec))
+        amps = []
+        for p in range(L):
+            amps.append(V.conj().T @ (op_matrix(fsec, p, dag) @ psi))
+        for i in range(L):
+            for j in range(L):
+                if dag:  # <c_i R c^dag_j>
+                    num = np.conj(amps[i]) * amps[j]
+                    out[i, j] += (num[None, :] / (z[:, None] - (w - e0)[None, :])).sum(1)
+                else:    # <c^dag_j R' c_i>
+                    num = np.conj(amps[j]) * amps[i]
+                    out[i, j] += (num[None, :] / (z[:, None] + (w - e0)[None, :])).sum(1)
+    return out
+
+
+def test_gf_poles_match_dense_resolvent():
+    pt = clusters.chain1d(tprime=0.8, nlat=4, U=4.0, xmu=2.0, nk=4, ngfiter=100, omega_nodes=64)
+    o = Oracle.from_point(pt)
+    o.diagonalize()
+    o.build_gf()
+    z = np.array([0.2j, 1.0j, 0.5 + 0.3j, 4.0j])
+    g = o.gf_cluster(z)
+    ge = _exact_gf(o, pt, z)
+    for i in range(4):
+        for j in range(4):
+            np.testing.assert_allclose(g[i, j, 0, 0, 0, 0], ge[i, j], atol=1e-10)
+
+
+def test_omega_u0_closed_form():
+    for pt, mu, sfac in (
+        (clusters.chain1d(tprime=1.0, nlat=4, U=0.0, xmu=0.3, nk=32, omega_nodes=512), 0.3, 2.0),
+        (clusters.square(nx=2, ny=2, U=0.0, xmu=0.37, nspin=2, nkx=4, nky=4, omega_nodes=512), 0.37, 1.0),
+    ):
+        o = Oracle.from_point(pt)
+        sft, egs, oi = o.solve()
+        Hk = nnn2lso(pt.Hk)
+        ex = sfac * np.mean([np.minimum(np.linalg.eigvalsh(Hk[:, :, k]) - mu, 0).sum() for k in range(pt.Nk)])
+        assert abs(sft - ex) < 1e-12 * abs(ex)
+
+
+def test_sum_kmesh_direct_formula():
+    pt = clusters.square_bath(nb=2, nk1=3, omega_nodes=64, ngfiter=40)
+    o = Oracle.from_point(pt)
+    o.diagonalize()
+    o.build_gf()
+    c = pt.cfg
+    for w in (0.1, 1.3, 25.0):
+        G = nnn2lso(o.gf_cluster(1j * w)[..., 0])
+        D = o.delta_bath(1j * w)
+        Hl = nnn2lso(pt.Hloc)
+        Hk = nnn2lso(pt.Hk)
+        f = np.mean([np.log(abs(np.linalg.det(np.eye(G.shape[0]) + (D + Hl - Hk[:, :, k]) @ G)))
+                     for k in range(pt.Nk)])
+        assert abs(o.sum_kmesh(w) - f) < 1e-12 * max(1, abs(f))
+        # Delta_bath = V (z + mu - h)^-1 V^dag (VCA_BATH_FUNCTIONS.f90:127-150)
+        h = nnn2lso(pt.bath_h)
+        V = pt.bath_v[:, :, 0, 0, 0, 0]
+        De = V @ np.linalg.inv((1j * w + c.xmu) * np.eye(h.shape[0]) - h) @ V.conj().T
+        np.testing.assert_allclose(D, De, atol=1e-13)
+
+
+def test_fixed_rule_against_qagi():
+    pt = clusters.chain1d(tprime=1.05, nlat=4, U=4.0, xmu=2.0, nk=16, omega_nodes=1024)
+    o = Oracle.from_point(pt)
+    sft, egs, oi = o.solve()
+    val, err = scipy.integrate.quad(o.sum_kmesh, 0.0, np.inf, epsabs=1e-13, epsrel=1e-13, limit=500)
+    oi_q = 2.0 * val / np.pi
+    assert abs(oi - oi_q) < 1e-10 * abs(egs), (oi, oi_q)

@@ -1,0 +1,1292 @@
+// vca_api.cu -- C-ABI entry points and host orchestration of the GB300
+// cluster-ED -> Lanczos Green's function -> Potthoff Omega path.
+//
+// The host side only sequences kernels, moves the caller's arrays across the
+// boundary and keeps scalar bookkeeping (sector order, the T=0 ground-state
+// list); every vector, matrix and reduction of the solve runs on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vca_gpu.h"
+#include "vca_kernels.cuh"
+
+using namespace vca;
+typedef std::complex<double> cd;
+
+namespace {
+
+std::string g_err;
+
+#define VFAIL(code, msg)   \
+  do {                     \
+    g_err = (msg);         \
+    return (code);         \
+  } while (0)
+#define CUCHK(x)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess) {                                                                \
+      g_err = std::string("CUDA error ") + cudaGetErrorString(e_) + " at " + #x;            \
+      return e_ == cudaErrorMemoryAllocation ? VCA_ERR_ALLOC : VCA_ERR_CUDA;                \
+    }                                                                                       \
+  } while (0)
+#define RCHK(x)            \
+  do {                     \
+    int r_ = (x);          \
+    if (r_ != VCA_OK) return r_; \
+  } while (0)
+
+// Device allocations owned by one stage of the context.
+struct Arena {
+  std::vector<void*> ptrs;
+  template <class T>
+  int alloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+      *p = nullptr;
+      g_err = std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed: " +
+              cudaGetErrorString(e);
+      cudaGetLastError();
+      return VCA_ERR_ALLOC;
+    }
+    ptrs.push_back(*p);
+    return VCA_OK;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+struct GState {
+  int sector;
+  double e;
+  void* vec;  // device, double (real model) or double2
+};
+
+struct ChainRec {
+  int elem;   // spin-diagonal element index (il,jl,is,io,jo)
+  int state;  // 0-based GS index
+  int chan;   // 1..4 as the reference's channel numbers
+};
+
+struct Ctx {
+  vca_config cfg{};
+  bool has_bath = false;
+  int Ns = 0, Nsectors = 0, N = 0, L = 0, Nb = 0;
+  cudaStream_t st = nullptr;
+  Arena basis, ham, states, gf, omega, work;
+  std::vector<int> dimn;
+  std::vector<int*> words;
+  int* d_iscratch = nullptr;
+  // Hamiltonian of the current point
+  bool ham_set = false, real_model = true;
+  std::vector<cd> Hloc, bath_h, bath_v;
+  std::vector<SpinSpace> sp[2];
+  int dwset = 0;  // spin table used by the down word (0 when Nspin == 1)
+  MixedDiag md{};
+  HopPair* d_pairs[2] = {nullptr, nullptr};
+  // results
+  bool solved = false;
+  std::vector<double> sector_e;
+  std::vector<GState> gs;
+  double egs = 0, zeta = 0, omega_int = 0, sft = 0;
+  std::vector<ChainRec> chains;
+  int ld = 0;
+  double* d_poles = nullptr;
+  double2* d_weights = nullptr;
+  int* d_nexc = nullptr;
+  int nelem = 0;
+  int* d_elem_ptr = nullptr;
+  int* d_elem_chain = nullptr;
+  // Hk and Omega
+  int64_t Nk = 0;
+  double2* d_Hk = nullptr;  // lso per k
+};
+Ctx* g = nullptr;
+
+inline int64_t binom_h(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  int64_t v = 1;
+  for (int t = 1; t <= k; t++) v = v * (n + 1 - t) / t;
+  return v;
+}
+inline int sec_nup(int isector) { return ((isector - 1) / (g->Ns + 1)) % (g->Ns + 1); }
+inline int sec_ndw(int isector) { return (isector - 1) % (g->Ns + 1); }
+inline int sec_of(int nup, int ndw) { return 1 + ndw + nup * (g->Ns + 1); }
+
+// column-major offsets of the caller's arrays
+inline int64_t idx_nnn(const vca_config& c, int il, int jl, int is, int js, int io, int jo) {
+  return il + (int64_t)c.Nlat * (jl + (int64_t)c.Nlat * (is + (int64_t)c.Nspin *
+         (js + (int64_t)c.Nspin * (io + (int64_t)c.Norb * jo))));
+}
+inline int64_t idx_bh(const vca_config& c, int il, int jl, int is, int js, int io, int jo) {
+  return il + (int64_t)c.Nlat_bath * (jl + (int64_t)c.Nlat_bath * (is + (int64_t)c.Nspin *
+         (js + (int64_t)c.Nspin * (io + (int64_t)c.Norb_bath * jo))));
+}
+inline int64_t idx_bv(const vca_config& c, int il, int jl, int is, int js, int io, int jo) {
+  return il + (int64_t)c.Nlat * (jl + (int64_t)c.Nlat_bath * (is + (int64_t)c.Nspin *
+         (js + (int64_t)c.Nspin * (io + (int64_t)c.Norb * jo))));
+}
+inline int elem_index(const vca_config& c, int il, int jl, int is, int io, int jo) {
+  return il + c.Nlat * (jl + c.Nlat * (is + c.Nspin * (io + c.Norb * jo)));
+}
+
+int check_finite(const double* p, size_t n, const char* what) {
+  for (size_t i = 0; i < n; i++)
+    if (!std::isfinite(p[i])) VFAIL(VCA_ERR_NUMERIC, std::string(what) + " holds NaN or Inf");
+  return VCA_OK;
+}
+
+size_t hloc_len(const vca_config& c) {
+  return (size_t)c.Nlat * c.Nlat * c.Nspin * c.Nspin * c.Norb * c.Norb;
+}
+size_t bh_len(const vca_config& c) {
+  return (size_t)c.Nlat_bath * c.Nlat_bath * c.Nspin * c.Nspin * c.Norb_bath * c.Norb_bath;
+}
+size_t bv_len(const vca_config& c) {
+  return (size_t)c.Nlat * c.Nlat_bath * c.Nspin * c.Nspin * c.Norb * c.Norb_bath;
+}
+
+SectorView view_of(int nup, int ndw) {
+  const SpinSpace& u = g->sp[0][nup];
+  const SpinSpace& d = g->sp[g->dwset][ndw];
+  SectorView v;
+  v.dimup = u.dim;
+  v.dimdw = d.dim;
+  v.wup = u.width;
+  v.wdw = d.width;
+  v.up_words = u.words;
+  v.dw_words = d.words;
+  v.up_cnt = u.cnt;
+  v.dw_cnt = d.cnt;
+  v.up_src = u.src;
+  v.dw_src = d.src;
+  v.up_amp = u.amp;
+  v.dw_amp = d.amp;
+  v.up_e1 = u.e1;
+  v.dw_e1 = d.e1;
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// One-body data of a solve point -> hop tables and diagonal energies.
+// ---------------------------------------------------------------------------
+int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath_v) {
+  const vca_config& c = g->cfg;
+  if (!Hloc) VFAIL(VCA_ERR_ARG, "Hloc is NULL");
+  if ((bath_h == nullptr) != (bath_v == nullptr)) VFAIL(VCA_ERR_ARG, "bath_h and bath_v must be given together");
+  if (g->has_bath && !bath_h) VFAIL(VCA_ERR_SHAPE, "the solver was initialised with a bath: bath_h/bath_v required");
+  if (!g->has_bath && bath_h) VFAIL(VCA_ERR_SHAPE, "the solver was initialised without a bath (Nlat_bath=Norb_bath=0)");
+  RCHK(check_finite(Hloc, 2 * hloc_len(c), "Hloc"));
+  g->Hloc.resize(hloc_len(c));
+  for (size_t i = 0; i < g->Hloc.size(); i++) g->Hloc[i] = cd(Hloc[2 * i], Hloc[2 * i + 1]);
+  if (g->has_bath) {
+    RCHK(check_finite(bath_h, 2 * bh_len(c), "bath_h"));
+    RCHK(check_finite(bath_v, 2 * bv_len(c), "bath_v"));
+    g->bath_h.resize(bh_len(c));
+    g->bath_v.resize(bv_len(c));
+    for (size_t i = 0; i < g->bath_h.size(); i++) g->bath_h[i] = cd(bath_h[2 * i], bath_h[2 * i + 1]);
+    for (size_t i = 0; i < g->bath_v.size(); i++) g->bath_v[i] = cd(bath_v[2 * i], bath_v[2 * i + 1]);
+    // vca_set_bath Hartree shift (VCA_BATH_SETUP.f90:127-136)
+    if (c.hfmode && !c.hfshift)
+      for (int il = 0; il < c.Nlat_bath; il++)
+        for (int io = 0; io < c.Norb_bath && io < 5; io++)
+          for (int is = 0; is < c.Nspin; is++)
+            g->bath_h[idx_bh(c, il, il, is, is, io, io)] -=
+                0.5 * c.Uloc[io] + 0.5 * c.Ust * (c.Norb - 1) + 0.5 * (c.Ust - c.Jh) * (c.Norb - 1);
+  }
+  g->ham.release();
+  const int nsets = (c.Nspin == 2) ? 2 : 1;
+  g->dwset = nsets - 1;
+  // real model?  (only spin-diagonal blocks enter H, VCA_HAMILTONIAN/stored/*)
+  bool real = true;
+  for (int s = 0; s < c.Nspin; s++) {
+    for (int il = 0; il < c.Nlat; il++)
+      for (int jl = 0; jl < c.Nlat; jl++)
+        for (int io = 0; io < c.Norb; io++)
+          for (int jo = 0; jo < c.Norb; jo++)
+            if (g->Hloc[idx_nnn(c, il, jl, s, s, io, jo)].imag() != 0.0) real = false;
+    if (g->has_bath) {
+      for (int a = 0; a < c.Nlat_bath; a++)
+        for (int b = 0; b < c.Nlat_bath; b++)
+          for (int oa = 0; oa < c.Norb_bath; oa++)
+            for (int ob = 0; ob < c.Norb_bath; ob++)
+              if (g->bath_h[idx_bh(c, a, b, s, s, oa, ob)].imag() != 0.0) real = false;
+      for (int il = 0; il < c.Nlat; il++)
+        for (int b = 0; b < c.Nlat_bath; b++)
+          for (int io = 0; io < c.Norb; io++)
+            for (int ob = 0; ob < c.Norb_bath; ob++)
+              if (g->bath_v[idx_bv(c, il, b, s, s, io, ob)].imag() != 0.0) real = false;
+    }
+  }
+  g->real_model = real;
+  const int LC = c.Nlat * c.Norb;
+  for (int set = 0; set < nsets; set++) {
+    const int sidx = (set == 0) ? 0 : c.Nspin - 1;
+    std::vector<HopPair> pairs;
+    for (int il = 0; il < c.Nlat; il++)  // H_cluster_up.f90:1-28
+      for (int jl = 0; jl < c.Nlat; jl++)
+        for (int io = 0; io < c.Norb; io++)
+          for (int jo = 0; jo < c.Norb; jo++) {
+            int is = io + il * c.Norb, js = jo + jl * c.Norb;
+            cd h = g->Hloc[idx_nnn(c, il, jl, sidx, sidx, io, jo)];
+            if (is != js && h != 0.0) pairs.push_back({is, js, h.real(), h.imag()});
+          }
+    if (g->has_bath) {
+      for (int la = 0; la < c.Nlat_bath; la++)  // H_cluster_up.f90:30-55
+        for (int lb = 0; lb < c.Nlat_bath; lb++)
+          for (int oa = 0; oa < c.Norb_bath; oa++)
+            for (int ob = 0; ob < c.Norb_bath; ob++) {
+              int ia = LC + la * c.Norb_bath + oa, ib = LC + lb * c.Norb_bath + ob;
+              cd h = g->bath_h[idx_bh(c, la, lb, sidx, sidx, oa, ob)];
+              if (ia != ib && h != 0.0) pairs.push_back({ia, ib, h.real(), h.imag()});
+            }
+      for (int il = 0; il < c.Nlat; il++)  // H_cluster_up.f90:57-86
+        for (int io = 0; io < c.Norb; io++)
+          for (int lb = 0; lb < c.Nlat_bath; lb++)
+            for (int ob = 0; ob < c.Norb_bath; ob++) {
+              int ia = LC + lb * c.Norb_bath + ob, is = io + il * c.Norb;
+              cd v = g->bath_v[idx_bv(c, il, lb, sidx, sidx, io, ob)];
+              if (v == 0.0) continue;
+              pairs.push_back({is, ia, v.real(), v.imag()});
+              pairs.push_back({ia, is, v.real(), -v.imag()});
+            }
+    }
+    if ((int)pairs.size() > VCA_MAX_PAIRS) VFAIL(VCA_ERR_UNSUPPORTED, "too many one-body pairs");
+    RCHK(g->ham.alloc(&g->d_pairs[set], pairs.size()));
+    if (!pairs.empty())
+      CUCHK(cudaMemcpyAsync(g->d_pairs[set], pairs.data(), pairs.size() * sizeof(HopPair),
+                            cudaMemcpyHostToDevice, g->st));
+    // diagonal one-body energies (H_cluster_local.f90)
+    E1Params ep{};
+    ep.norb = c.Norb;
+    ep.upar = (c.Norb > 1) ? (c.Ust - c.Jh) : 0.0;
+    for (int o = 0; o < c.Norb; o++) {
+      unsigned m = 0;
+      for (int il = 0; il < c.Nlat; il++) m |= 1u << (o + il * c.Norb);
+      ep.omask[o] = m;
+    }
+    for (int il = 0; il < c.Nlat; il++)
+      for (int io = 0; io < c.Norb; io++) {
+        cd e = g->Hloc[idx_nnn(c, il, il, sidx, sidx, io, io)] - c.xmu;
+        if (c.hfmode) {
+          e += -0.5 * c.Uloc[io];
+          if (c.Norb > 1) e += -0.5 * (2.0 * c.Ust - c.Jh) * (c.Norb - 1);
+        }
+        ep.eps[io + il * c.Norb] = make_double2(e.real(), e.imag());
+      }
+    if (g->has_bath)
+      for (int lb = 0; lb < c.Nlat_bath; lb++)
+        for (int ob = 0; ob < c.Norb_bath; ob++) {
+          cd e = g->bath_h[idx_bh(c, lb, lb, sidx, sidx, ob, ob)] - c.xmu;
+          ep.eps[LC + lb * c.Norb_bath + ob] = make_double2(e.real(), e.imag());
+        }
+    g->sp[set].assign(g->Ns + 1, SpinSpace());
+    for (int n = 0; n <= g->Ns; n++) {
+      SpinSpace& S = g->sp[set][n];
+      S.n = n;
+      S.dim = g->dimn[n];
+      S.words = g->words[n];
+      RCHK(g->ham.alloc(&S.cnt, S.dim));
+      S.width = launch_hop_count(g->Ns, n, S.dim, S.words, g->d_pairs[set], (int)pairs.size(), S.cnt,
+                                 g->d_iscratch, g->st);
+      CUCHK(cudaGetLastError());
+      RCHK(g->ham.alloc(&S.src, (size_t)S.width * S.dim));
+      RCHK(g->ham.alloc(&S.amp, (size_t)S.width * S.dim));
+      RCHK(g->ham.alloc(&S.e1, S.dim));
+      launch_hop_fill(g->Ns, n, S.dim, S.width, S.words, g->d_pairs[set], (int)pairs.size(), S.src, S.amp,
+                      g->st);
+      launch_e1(S.dim, S.words, ep, false, S.e1, g->st);
+      CUCHK(cudaGetLastError());
+    }
+  }
+  if (nsets == 1) g->sp[1] = g->sp[0];
+  // opposite-spin terms and constants (H_cluster_local.f90:26-76)
+  MixedDiag md{};
+  md.norb = c.Norb;
+  for (int o = 0; o < c.Norb; o++) {
+    unsigned m = 0;
+    for (int il = 0; il < c.Nlat; il++) m |= 1u << (o + il * c.Norb);
+    md.omask[o] = m;
+    md.U[o] = c.Uloc[o];
+  }
+  md.Ust = (c.Norb > 1) ? c.Ust : 0.0;
+  md.c0 = 0.0;
+  if (c.hfmode) {
+    for (int io = 0; io < c.Norb; io++) md.c0 += 0.25 * c.Uloc[io] * c.Nlat;
+    if (c.Norb > 1) md.c0 += c.Nlat * (c.Norb * (c.Norb - 1) / 2) * 0.25 * (2.0 * c.Ust - c.Jh);
+  }
+  g->md = md;
+  g->ham_set = true;
+  CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched Lanczos driver on a column batch (GS: one chain; GF: many).
+// ---------------------------------------------------------------------------
+struct BatchBufs {
+  void* b[3];
+  double* partial;
+  int nblk;
+  double *col_a, *ch_a, *ch_b2, *invb, *bnow;
+  double *A, *Bt;
+  ChainMeta* meta;
+  int* col2ch;
+};
+
+int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k, double tol, int ldab) {
+  cudaStream_t st = g->st;
+  void* X = bb.b[0];
+  void* Xp = bb.b[1];
+  void* Y = bb.b[2];
+  if (cb.cplx)
+    launch_hxv_cplx(sv, g->md, cb.m, (const double2*)X, (double2*)Y, st);
+  else
+    launch_hxv_real(sv, g->md, cb.m, (const double*)X, (double*)Y, st);
+  if (k > 1) launch_col_axpy(cb, bb.bnow, Xp, Y, true, st);
+  launch_col_dot(cb, X, Y, bb.partial, bb.nblk, bb.col_a, st);
+  launch_chain_sum(cb, bb.col_a, bb.ch_a, st);
+  launch_col_axpy(cb, bb.ch_a, X, Y, true, st);
+  launch_col_dot(cb, Y, Y, bb.partial, bb.nblk, bb.col_a, st);
+  launch_chain_sum(cb, bb.col_a, bb.ch_b2, st);
+  launch_lanczos_record(cb.nch, bb.meta, k, bb.ch_a, bb.ch_b2, bb.A, bb.Bt, ldab, tol, bb.invb, bb.bnow, st);
+  launch_col_scale(cb, bb.invb, Y, Y, st);
+  // rotate (X, Xp, Y) <- (Y, X, Xp)
+  bb.b[0] = Y;
+  bb.b[1] = X;
+  bb.b[2] = Xp;
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
+
+int alloc_batch(Arena& ar, int64_t rows, int m, bool cplx, int nch, int ldab, BatchBufs& bb) {
+  const size_t es = cplx ? sizeof(double2) : sizeof(double);
+  for (int q = 0; q < 3; q++) {
+    char* p;
+    RCHK(ar.alloc(&p, (size_t)rows * m * es));
+    bb.b[q] = p;
+  }
+  bb.nblk = (int)std::min<int64_t>(std::max<int64_t>(1, rows / 256), 608);
+  RCHK(ar.alloc(&bb.partial, (size_t)bb.nblk * m));
+  RCHK(ar.alloc(&bb.col_a, m));
+  RCHK(ar.alloc(&bb.ch_a, nch));
+  RCHK(ar.alloc(&bb.ch_b2, nch));
+  RCHK(ar.alloc(&bb.invb, nch));
+  RCHK(ar.alloc(&bb.bnow, nch));
+  RCHK(ar.alloc(&bb.A, (size_t)nch * ldab));
+  RCHK(ar.alloc(&bb.Bt, (size_t)nch * ldab));
+  RCHK(ar.alloc(&bb.meta, nch));
+  RCHK(ar.alloc(&bb.col2ch, m));
+  CUCHK(cudaMemsetAsync(bb.A, 0, sizeof(double) * nch * ldab, g->st));
+  CUCHK(cudaMemsetAsync(bb.Bt, 0, sizeof(double) * nch * ldab, g->st));
+  CUCHK(cudaMemsetAsync(bb.bnow, 0, sizeof(double) * nch, g->st));
+  return VCA_OK;
+}
+
+// Ground state of one sector by Lanczos (replaces SciFortran sp_lanc_eigh,
+// VCA_DIAG.f90:172-184): deterministic start vector, residual test every
+// gs_check_every steps, eigenvector by a second pass over stored coefficients.
+int sector_gs(int isector, double* E, void** vec_out, Arena& keep) {
+  const vca_config& c = g->cfg;
+  const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+  SectorView sv = view_of(nup, ndw);
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const bool cplx = !g->real_model;
+  const int nmax = (int)std::min<int64_t>(D, std::min(c.lanc_niter, 512));
+  Arena ar;
+  BatchBufs bb;
+  int rc = alloc_batch(ar, D, 1, cplx, 1, nmax + 1, bb);
+  if (rc) { ar.release(); return rc; }
+  double *theta, *svec, *resid, *invB, *norm2, *invn;
+  double2* dummy = nullptr;
+  (void)dummy;
+  if ((rc = ar.alloc(&theta, 1)) || (rc = ar.alloc(&svec, 5 * (size_t)(nmax + 1))) ||
+      (rc = ar.alloc(&resid, 1)) || (rc = ar.alloc(&invB, nmax + 1)) || (rc = ar.alloc(&norm2, 1)) ||
+      (rc = ar.alloc(&invn, 1))) {
+    ar.release();
+    return rc;
+  }
+  ChainMeta m0{1, 0, nmax, 1, 0};
+  int zero = 0;
+  cudaMemcpyAsync(bb.meta, &m0, sizeof(m0), cudaMemcpyHostToDevice, g->st);
+  cudaMemcpyAsync(bb.col2ch, &zero, sizeof(int), cudaMemcpyHostToDevice, g->st);
+  ColBatch cb{D, 1, cplx, 1, bb.col2ch, bb.meta};
+  auto start = [&](void* X) {
+    if (cplx) {
+      launch_start_vector(D, c.start_seed, isector, (double*)bb.b[2], g->st);
+      launch_real_to_cplx(D, (const double*)bb.b[2], (double2*)X, g->st);
+    } else {
+      launch_start_vector(D, c.start_seed, isector, (double*)X, g->st);
+    }
+    launch_col_dot(cb, X, X, bb.partial, bb.nblk, norm2, g->st);
+    launch_chain_norm_init(1, bb.meta, norm2, invn, g->st);
+    launch_col_scale(cb, invn, X, X, g->st);
+  };
+  start(bb.b[0]);
+  int mconv = 0;
+  double th = 0.0;
+  for (int k = 1; k <= nmax; k++) {
+    if ((rc = lanczos_step(sv, cb, bb, k, c.gf_beta_tol, nmax + 1))) { ar.release(); return rc; }
+    if (k % std::max(1, c.gs_check_every) == 0 || k == nmax) {
+      ChainMeta mh;
+      double bn;
+      cudaMemcpyAsync(&mh, bb.meta, sizeof(mh), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(&bn, bb.bnow, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+      CUCHK(cudaStreamSynchronize(g->st));
+      const int kk = mh.len;
+      if (kk < 1) { ar.release(); VFAIL(VCA_ERR_NUMERIC, "Lanczos start vector has zero norm"); }
+      launch_tri_lowest(bb.A, bb.Bt, kk, bn, theta, svec, resid, g->st);
+      double rs;
+      cudaMemcpyAsync(&th, theta, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(&rs, resid, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+      CUCHK(cudaStreamSynchronize(g->st));
+      const bool exhausted = !mh.active && kk < nmax;
+      if (exhausted || rs <= c.gs_residual_tol * std::max(1.0, std::fabs(th)) || k == nmax || !mh.active) {
+        mconv = kk;
+        break;
+      }
+    }
+  }
+  // second pass: psi = sum_k s_k v_k with the stored alpha/beta
+  const size_t es = cplx ? sizeof(double2) : sizeof(double);
+  char* psi;
+  if ((rc = keep.alloc(&psi, (size_t)D * es))) { ar.release(); return rc; }
+  CUCHK(cudaMemsetAsync(psi, 0, (size_t)D * es, g->st));
+  m0 = ChainMeta{1, 0, nmax, 1, 0};
+  cudaMemcpyAsync(bb.meta, &m0, sizeof(m0), cudaMemcpyHostToDevice, g->st);
+  launch_recip(nmax + 1, bb.Bt, invB, g->st);
+  bb.b[0] = bb.b[0];
+  void* X = bb.b[0];
+  void* Xp = bb.b[1];
+  void* Y = bb.b[2];
+  start(X);
+  for (int k = 1; k <= mconv; k++) {
+    launch_psi_accum(D, cplx, svec, k - 1, X, psi, g->st);
+    if (k == mconv) break;
+    if (cplx) launch_hxv_cplx(sv, g->md, 1, (const double2*)X, (double2*)Y, g->st);
+    else launch_hxv_real(sv, g->md, 1, (const double*)X, (double*)Y, g->st);
+    if (k > 1) launch_col_axpy(cb, bb.Bt + (k - 1), Xp, Y, true, g->st);
+    launch_col_axpy(cb, bb.A + (k - 1), X, Y, true, g->st);
+    launch_col_scale(cb, invB + k, Y, Y, g->st);
+    void* t = Xp;
+    Xp = X;
+    X = Y;
+    Y = t;
+  }
+  launch_col_dot(cb, psi, psi, bb.partial, bb.nblk, norm2, g->st);
+  launch_chain_norm_init(1, bb.meta, norm2, invn, g->st);
+  launch_col_scale(cb, invn, psi, psi, g->st);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(g->st));
+  ar.release();
+  *E = th;
+  *vec_out = psi;
+  return VCA_OK;
+}
+
+// vca_diag_c at T=0 with LANC_METHOD="lanczos" (VCA_DIAG.f90:49-267)
+int diagonalize() {
+  const vca_config& c = g->cfg;
+  g->states.release();
+  g->gs.clear();
+  g->sector_e.assign(g->Nsectors, INFINITY);
+  double oldzero = 1000.0;
+  const double thr = c.gs_threshold;
+  for (int isector = 1; isector <= g->Nsectors; isector++) {
+    double e;
+    void* vec = nullptr;
+    Arena tmp;
+    RCHK(sector_gs(isector, &e, &vec, tmp));
+    g->sector_e[isector - 1] = e;
+    // T=0 bookkeeping (VCA_DIAG.f90:224-236), list ordered by energy
+    // (es_insert_state_c, VCA_EIGENSPACE.f90:167-216)
+    if (e < oldzero - 10.0 * thr) {
+      oldzero = e;
+      g->states.release();
+      g->gs.clear();
+      g->states.ptrs = tmp.ptrs;
+      g->gs.push_back({isector, e, vec});
+    } else if (std::fabs(e - oldzero) <= thr) {
+      oldzero = std::min(oldzero, e);
+      for (void* p : tmp.ptrs) g->states.ptrs.push_back(p);
+      auto it = g->gs.begin();
+      while (it != g->gs.end() && !(e <= it->e)) ++it;
+      g->gs.insert(it, GState{isector, e, vec});
+    } else {
+      tmp.release();
+    }
+  }
+  g->egs = INFINITY;
+  for (auto& s : g->gs) g->egs = std::min(g->egs, s.e);
+  g->zeta = (double)g->gs.size();  // VCA_DIAG.f90:363
+  return VCA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Green's function chains (build_gf_normal, VCA_GF_NORMAL.f90:37-104): every
+// chain of one (state, spin, particle|hole) target sector runs as one column
+// batch; batches are split to fit device memory.
+// ---------------------------------------------------------------------------
+struct ChainSpec {
+  ChainInit ci;
+  ChainRec rec;
+  int isign;
+  cd wfac;
+  int ncol;
+};
+
+int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs) {
+  const vca_config& c = g->cfg;
+  const GState& S = g->gs[state];
+  const int nup = sec_nup(S.sector), ndw = sec_ndw(S.sector);
+  const int tup = nup + (spin == 0 ? (dag ? 1 : -1) : 0);
+  const int tdw = ndw + (spin == 1 ? (dag ? 1 : -1) : 0);
+  if (tup < 0 || tup > g->Ns || tdw < 0 || tdw > g->Ns) return VCA_OK;  // no target sector
+  SectorView tv = view_of(tup, tdw);
+  const int64_t D = (int64_t)tv.dimup * tv.dimdw;
+  const bool cplx = !g->real_model;
+  const int nlanc = (int)std::min<int64_t>(D, c.lanc_ngfiter);
+  const size_t es = cplx ? sizeof(double2) : sizeof(double);
+  // memory budget: three column buffers per batch
+  size_t freeb = 0, totb = 0;
+  CUCHK(cudaMemGetInfo(&freeb, &totb));
+  const size_t budget = (size_t)(0.5 * (double)freeb);
+  int64_t maxcols = (int64_t)(budget / (3 * (size_t)D * es + 1));
+  if (maxcols < 2) VFAIL(VCA_ERR_ALLOC, "not enough device memory for one Green's function chain");
+  size_t q0 = 0;
+  while (q0 < specs.size()) {
+    // group of chains whose columns fit
+    size_t q1 = q0;
+    int m = 0;
+    while (q1 < specs.size() && m + specs[q1].ncol <= maxcols) { m += specs[q1].ncol; q1++; }
+    const int nch = (int)(q1 - q0);
+    Arena ar;
+    BatchBufs bb;
+    int rc = alloc_batch(ar, D, m, cplx, nch, g->ld, bb);
+    double *norm2c, *norm2, *invn;
+    ChainInit* d_ci;
+    int* d_isign;
+    double2* d_wfac;
+    double* d_work;
+    if (!rc) rc = ar.alloc(&norm2c, m);
+    if (!rc) rc = ar.alloc(&norm2, nch);
+    if (!rc) rc = ar.alloc(&invn, nch);
+    if (!rc) rc = ar.alloc(&d_ci, nch);
+    if (!rc) rc = ar.alloc(&d_isign, nch);
+    if (!rc) rc = ar.alloc(&d_wfac, nch);
+    if (!rc) rc = ar.alloc(&d_work, (size_t)nch * 3 * g->ld);
+    if (rc) { ar.release(); return rc; }
+    std::vector<ChainMeta> meta(nch);
+    std::vector<int> col2ch(m);
+    std::vector<ChainInit> ci(nch);
+    std::vector<int> isg(nch);
+    std::vector<double2> wf(nch);
+    int col = 0;
+    for (int q = 0; q < nch; q++) {
+      ChainSpec& sp = specs[q0 + q];
+      sp.ci.col0 = col;
+      ci[q] = sp.ci;
+      meta[q] = ChainMeta{sp.ncol, col, nlanc, 1, 0};
+      for (int t = 0; t < sp.ncol; t++) col2ch[col + t] = q;
+      col += sp.ncol;
+      isg[q] = sp.isign;
+      wf[q] = make_double2(sp.wfac.real(), sp.wfac.imag());
+    }
+    cudaMemcpyAsync(bb.meta, meta.data(), sizeof(ChainMeta) * nch, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(bb.col2ch, col2ch.data(), sizeof(int) * m, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(d_ci, ci.data(), sizeof(ChainInit) * nch, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(d_isign, isg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(d_wfac, wf.data(), sizeof(double2) * nch, cudaMemcpyHostToDevice, g->st);
+    ColBatch cb{D, m, cplx, nch, bb.col2ch, bb.meta};
+    // start vectors: gather from the ground state, normalise per chain
+    launch_chain_init(tv, g->sp[0][nup].dim, S.vec, cplx, nch, d_ci, m, cplx, bb.b[0], g->st);
+    launch_col_dot(cb, bb.b[0], bb.b[0], bb.partial, bb.nblk, norm2c, g->st);
+    launch_chain_sum(cb, norm2c, norm2, g->st);
+    launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
+    launch_col_scale(cb, invn, bb.b[0], bb.b[0], g->st);
+    for (int k = 1; k <= nlanc; k++)
+      if ((rc = lanczos_step(tv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
+    // poles and weights into the global chain table
+    const int base = (int)g->chains.size();
+    launch_chain_poles(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, g->zeta, d_work,
+                       g->d_poles + (size_t)base * g->ld, g->d_weights + (size_t)base * g->ld,
+                       g->d_nexc + base, g->st);
+    CUCHK(cudaGetLastError());
+    CUCHK(cudaStreamSynchronize(g->st));
+    for (int q = 0; q < nch; q++) g->chains.push_back(specs[q0 + q].rec);
+    ar.release();
+    q0 = q1;
+  }
+  return VCA_OK;
+}
+
+int count_chains() {
+  const vca_config& c = g->cfg;
+  const int L = c.Nlat * c.Norb;
+  const int per = c.vca_gf_symmetric ? 2 : 4;
+  return (int)g->gs.size() * c.Nspin * (2 * L + per * L * (L - 1));
+}
+
+int build_gf() {
+  const vca_config& c = g->cfg;
+  g->gf.release();
+  g->chains.clear();
+  g->ld = std::max(1, c.lanc_ngfiter);
+  const int nmax = count_chains();
+  RCHK(g->gf.alloc(&g->d_poles, (size_t)nmax * g->ld));
+  RCHK(g->gf.alloc(&g->d_weights, (size_t)nmax * g->ld));
+  RCHK(g->gf.alloc(&g->d_nexc, nmax));
+  CUCHK(cudaMemsetAsync(g->d_nexc, 0, sizeof(int) * nmax, g->st));
+  const bool cplx = !g->real_model;
+  const cd XI(0.0, 1.0);
+  for (int k = 0; k < (int)g->gs.size(); k++)
+    for (int is = 0; is < c.Nspin; is++) {
+      std::vector<ChainSpec> part, hole;
+      auto add = [&](std::vector<ChainSpec>& v, int dag, int e, int chan, int p, cd cp, int q, cd cq,
+                     int nterm, cd wfac) {
+        ChainSpec s{};
+        s.ci.spin = is;
+        s.ci.dag = dag;
+        s.ci.nterm = nterm;
+        s.ci.t[0] = OpTerm{p, cp.real(), cp.imag()};
+        s.ci.t[1] = OpTerm{q, cq.real(), cq.imag()};
+        const bool imagcoef = (cp.imag() != 0.0) || (nterm > 1 && cq.imag() != 0.0);
+        s.ci.cplxcol = (!cplx && imagcoef) ? 1 : 0;
+        s.ncol = cplx ? 1 : (imagcoef ? 2 : 1);
+        s.rec = ChainRec{e, k, chan};
+        s.isign = dag ? 1 : -1;
+        s.wfac = wfac;
+        v.push_back(s);
+      };
+      for (int io = 0; io < c.Norb; io++)
+        for (int il = 0; il < c.Nlat; il++) {
+          const int p = io + il * c.Norb;
+          const int ed = elem_index(c, il, il, is, io, io);
+          add(part, 1, ed, 1, p, 1.0, 0, 0.0, 1, 1.0);  // VCA_GF_NORMAL.f90:121-318
+          add(hole, 0, ed, 2, p, 1.0, 0, 0.0, 1, 1.0);
+          for (int jl = 0; jl < c.Nlat; jl++)
+            for (int jo = 0; jo < c.Norb; jo++) {
+              if (il == jl && io == jo) continue;
+              const int q = jo + jl * c.Norb;
+              const int e = elem_index(c, il, jl, is, io, jo);
+              add(part, 1, e, 1, p, 1.0, q, 1.0, 2, 1.0);
+              add(hole, 0, e, 2, p, 1.0, q, 1.0, 2, 1.0);
+              if (!c.vca_gf_symmetric) {  // chan4 (VCA_GF_NORMAL.f90:561-958)
+                add(part, 1, e, 3, p, 1.0, q, XI, 2, -XI);
+                add(hole, 0, e, 4, p, 1.0, q, -XI, 2, -XI);
+              }
+            }
+        }
+      RCHK(run_chain_batch(k, is, true, part));
+      RCHK(run_chain_batch(k, is, false, hole));
+    }
+  // element -> chains CSR
+  g->nelem = c.Nlat * c.Nlat * c.Nspin * c.Norb * c.Norb;
+  std::vector<std::vector<int>> lists(g->nelem);
+  for (int ch = 0; ch < (int)g->chains.size(); ch++) lists[g->chains[ch].elem].push_back(ch);
+  std::vector<int> ptr(g->nelem + 1, 0), flat;
+  for (int e = 0; e < g->nelem; e++) {
+    ptr[e + 1] = ptr[e] + (int)lists[e].size();
+    flat.insert(flat.end(), lists[e].begin(), lists[e].end());
+  }
+  RCHK(g->gf.alloc(&g->d_elem_ptr, ptr.size()));
+  RCHK(g->gf.alloc(&g->d_elem_chain, std::max<size_t>(1, flat.size())));
+  CUCHK(cudaMemcpyAsync(g->d_elem_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, g->st));
+  if (!flat.empty())
+    CUCHK(cudaMemcpyAsync(g->d_elem_chain, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+GfLayout gf_layout() {
+  GfLayout gl;
+  gl.nelem = g->nelem;
+  gl.elem_ptr = g->d_elem_ptr;
+  gl.elem_chain = g->d_elem_chain;
+  gl.nexc = g->d_nexc;
+  gl.poles = g->d_poles;
+  gl.weights = g->d_weights;
+  gl.ld = g->ld;
+  return gl;
+}
+
+// G'(z) in lso layout for nz device points
+int gf_lso(int nz, const double2* d_z, double2* d_Glso, Arena& ar) {
+  const vca_config& c = g->cfg;
+  double2* raw;
+  RCHK(ar.alloc(&raw, (size_t)nz * g->nelem));
+  launch_gf_eval(gf_layout(), nz, d_z, raw, g->st);
+  ClusterDims cdm{c.Nlat, c.Norb, c.Nspin, g->N, c.vca_gf_symmetric ? 0 : 1};
+  launch_gf_assemble(cdm, nz, raw, d_Glso, g->st);
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
+
+// Bath matrices in lso layout (VCA_AUX_FUNX.f90:255-279, :445-468)
+void bath_lso(std::vector<double2>& hb, std::vector<double2>& V) {
+  const vca_config& c = g->cfg;
+  const int N = g->N, Nb = g->Nb;
+  hb.assign((size_t)Nb * Nb, make_double2(0, 0));
+  V.assign((size_t)N * Nb, make_double2(0, 0));
+  for (int a = 0; a < c.Nlat_bath; a++)
+    for (int b = 0; b < c.Nlat_bath; b++)
+      for (int is = 0; is < c.Nspin; is++)
+        for (int js = 0; js < c.Nspin; js++)
+          for (int oa = 0; oa < c.Norb_bath; oa++)
+            for (int ob = 0; ob < c.Norb_bath; ob++) {
+              int r = oa + a * c.Norb_bath + is * c.Norb_bath * c.Nlat_bath;
+              int q = ob + b * c.Norb_bath + js * c.Norb_bath * c.Nlat_bath;
+              cd h = g->bath_h[idx_bh(c, a, b, is, js, oa, ob)];
+              hb[r + (size_t)q * Nb] = make_double2(h.real(), h.imag());
+            }
+  for (int il = 0; il < c.Nlat; il++)
+    for (int b = 0; b < c.Nlat_bath; b++)
+      for (int is = 0; is < c.Nspin; is++)
+        for (int js = 0; js < c.Nspin; js++)
+          for (int io = 0; io < c.Norb; io++)
+            for (int ob = 0; ob < c.Norb_bath; ob++) {
+              int r = io + il * c.Norb + is * c.Norb * c.Nlat;
+              int q = ob + b * c.Norb_bath + js * c.Norb_bath * c.Nlat_bath;
+              cd v = g->bath_v[idx_bv(c, il, b, is, js, io, ob)];
+              V[r + (size_t)q * N] = make_double2(v.real(), v.imag());
+            }
+}
+
+// spin-block structure of the Omega matrices (all spin-off-diagonal blocks 0)
+bool spin_block_diagonal(const double* Hk, int64_t Nk) {
+  const vca_config& c = g->cfg;
+  if (c.Nspin == 1) return true;
+  const size_t nel = hloc_len(c);
+  for (int il = 0; il < c.Nlat; il++)
+    for (int jl = 0; jl < c.Nlat; jl++)
+      for (int io = 0; io < c.Norb; io++)
+        for (int jo = 0; jo < c.Norb; jo++)
+          for (int s = 0; s < 2; s++) {
+            int64_t x = idx_nnn(c, il, jl, s, 1 - s, io, jo);
+            if (g->Hloc[x] != 0.0) return false;
+            for (int64_t k = 0; k < Nk; k++)
+              if (Hk[2 * (k * nel + x)] != 0.0 || Hk[2 * (k * nel + x) + 1] != 0.0) return false;
+          }
+  if (g->has_bath) {
+    for (int a = 0; a < c.Nlat_bath; a++)
+      for (int b = 0; b < c.Nlat_bath; b++)
+        for (int oa = 0; oa < c.Norb_bath; oa++)
+          for (int ob = 0; ob < c.Norb_bath; ob++)
+            for (int s = 0; s < 2; s++)
+              if (g->bath_h[idx_bh(c, a, b, s, 1 - s, oa, ob)] != 0.0) return false;
+    for (int il = 0; il < c.Nlat; il++)
+      for (int b = 0; b < c.Nlat_bath; b++)
+        for (int io = 0; io < c.Norb; io++)
+          for (int ob = 0; ob < c.Norb_bath; ob++)
+            for (int s = 0; s < 2; s++)
+              if (g->bath_v[idx_bv(c, il, b, s, 1 - s, io, ob)] != 0.0) return false;
+  }
+  return true;
+}
+
+// Omega integral (frequency_integration, VCA_OMEGA.f90:123-146) with the
+// fixed Gauss-Legendre rule; also returns f(w) at the nodes when asked.
+int omega_integral(const double* Hk_host, int64_t Nk, double* out, int nz_eval, const double* w_eval,
+                   double* f_eval) {
+  const vca_config& c = g->cfg;
+  Arena ar;
+  const int N = g->N, NN = N * N;
+  int rc = VCA_OK;
+  // nodes
+  int n;
+  double2* d_z;
+  double* d_W = nullptr;
+  if (f_eval) {
+    n = nz_eval;
+    std::vector<double2> zh(n);
+    for (int i = 0; i < n; i++) zh[i] = make_double2(0.0, w_eval[i]);
+    if ((rc = ar.alloc(&d_z, n))) { ar.release(); return rc; }
+    cudaMemcpyAsync(d_z, zh.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, g->st);
+  } else {
+    n = c.omega_nodes;
+    double *s, *w;
+    if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = ar.alloc(&d_z, n)) || (rc = ar.alloc(&d_W, n))) {
+      ar.release();
+      return rc;
+    }
+    launch_gauss_legendre(n, s, w, g->st);
+    launch_omega_nodes(n, c.omega_scale, s, w, d_z, d_W, g->st);
+  }
+  // G'(i w) in lso
+  double2 *Glso, *P, *D = nullptr, *Hl;
+  if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = ar.alloc(&P, (size_t)n * NN)) ||
+      (rc = ar.alloc(&Hl, NN))) { ar.release(); return rc; }
+  if ((rc = gf_lso(n, d_z, Glso, ar))) { ar.release(); return rc; }
+  // Hloc in lso
+  {
+    double2* hraw;
+    if ((rc = ar.alloc(&hraw, NN))) { ar.release(); return rc; }
+    cudaMemcpyAsync(hraw, g->Hloc.data(), sizeof(double2) * NN, cudaMemcpyHostToDevice, g->st);
+    launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, 1, hraw, Hl, g->st);
+  }
+  if (g->has_bath) {  // Delta(i w)
+    std::vector<double2> hb, V;
+    bath_lso(hb, V);
+    double2 *dhb, *dV, *work;
+    const int Nb = g->Nb;
+    if ((rc = ar.alloc(&dhb, (size_t)Nb * Nb)) || (rc = ar.alloc(&dV, (size_t)N * Nb)) ||
+        (rc = ar.alloc(&work, (size_t)n * 2 * Nb * Nb)) || (rc = ar.alloc(&D, (size_t)n * NN))) {
+      ar.release();
+      return rc;
+    }
+    cudaMemcpyAsync(dhb, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(dV, V.data(), sizeof(double2) * V.size(), cudaMemcpyHostToDevice, g->st);
+    launch_delta_bath(n, d_z, N, Nb, dhb, dV, c.xmu, work, D, g->st);
+  }
+  launch_add_hloc(n, NN, D, Hl, P, g->st);
+  const bool blk = spin_block_diagonal(Hk_host, Nk);
+  const int nblk = blk ? c.Nspin : 1;
+  const int nb = N / nblk;
+  if (nb > 32) { ar.release(); VFAIL(VCA_ERR_UNSUPPORTED, "Omega k-sum supports spin blocks up to 32 orbitals"); }
+  int kchunks = (int)std::max<int64_t>(1, std::min<int64_t>(Nk, (152 * 8 + n - 1) / n));
+  double* fpart;
+  double* f;
+  if ((rc = ar.alloc(&fpart, (size_t)n * kchunks)) || (rc = ar.alloc(&f, n))) { ar.release(); return rc; }
+  launch_omega_ksum(n, N, nblk, nb, P, Glso, Nk, g->d_Hk, fpart, kchunks, g->st);
+  launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, f, g->st);
+  CUCHK(cudaGetLastError());
+  if (f_eval) {
+    CUCHK(cudaMemcpyAsync(f_eval, f, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st));
+    CUCHK(cudaStreamSynchronize(g->st));
+    ar.release();
+    return VCA_OK;
+  }
+  double* acc;
+  if ((rc = ar.alloc(&acc, 1))) { ar.release(); return rc; }
+  launch_wsum(n, d_W, f, acc, g->st);
+  double integral = 0.0;
+  CUCHK(cudaMemcpyAsync(&integral, acc, sizeof(double), cudaMemcpyDeviceToHost, g->st));
+  CUCHK(cudaStreamSynchronize(g->st));
+  ar.release();
+  *out = (3.0 - c.Nspin) * integral / M_PI;
+  return VCA_OK;
+}
+
+int upload_hk(const double* Hk, int64_t Nk) {
+  const vca_config& c = g->cfg;
+  if (!Hk || Nk <= 0) VFAIL(VCA_ERR_SHAPE, "Hk must hold at least one k-point");
+  const size_t nel = hloc_len(c);
+  RCHK(check_finite(Hk, 2 * nel * Nk, "Hk"));
+  g->omega.release();
+  double2* raw;
+  RCHK(g->omega.alloc(&raw, nel * Nk));
+  RCHK(g->omega.alloc(&g->d_Hk, nel * Nk));
+  CUCHK(cudaMemcpyAsync(raw, Hk, sizeof(double2) * nel * Nk, cudaMemcpyHostToDevice, g->st));
+  launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, Nk, raw, g->d_Hk, g->st);
+  CUCHK(cudaGetLastError());
+  g->Nk = Nk;
+  return VCA_OK;
+}
+
+int solve_one(const double* Hloc, const double* Hk, int64_t Nk, const double* bath_h,
+              const double* bath_v, double* omega_out) {
+  if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  g->solved = false;
+  RCHK(set_hamiltonian(Hloc, bath_h, bath_v));
+  RCHK(upload_hk(Hk, Nk));
+  RCHK(diagonalize());
+  RCHK(build_gf());
+  RCHK(omega_integral(Hk, Nk, &g->omega_int, 0, nullptr, nullptr));
+  g->sft = g->egs - g->omega_int;  // VCA_MAIN.f90:183-197
+  g->solved = true;
+  if (omega_out) *omega_out = g->sft;
+  return VCA_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+void vca_config_defaults(vca_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->Norb = 1;
+  c->Nspin = 1;
+  c->Nlat = 1;
+  c->Nlat_bath = 0;
+  c->Norb_bath = 0;
+  c->Uloc[0] = 2.0;
+  c->beta = 1000.0;
+  c->xmu = 0.0;
+  c->hfmode = 1;
+  c->hfshift = 1;
+  c->Lmats = 5000;
+  c->Lreal = 5000;
+  c->wini = -5.0;
+  c->wfin = 5.0;
+  c->eps = 0.01;
+  c->vca_twin = 0;
+  c->vca_sectors = 0;
+  c->vca_sectors_shift = 1;
+  c->vca_sparse_H = 1;
+  c->vca_gf_symmetric = 0;
+  c->lanc_method = VCA_LANC_ARPACK;
+  c->lanc_nstates_sector = 6;
+  c->lanc_nstates_total = 1;
+  c->lanc_niter = 512;
+  c->lanc_ngfiter = 200;
+  c->lanc_tolerance = 1e-12;
+  c->lanc_dim_threshold = 256;
+  c->gs_threshold = 1e-9;
+  c->verbose = 3;
+  c->omega_nodes = 4096;
+  c->gs_check_every = 10;
+  c->omega_scale = 1.0;
+  c->gs_residual_tol = 1e-11;
+  c->gf_beta_tol = 1e-12;
+  c->start_seed = 20261203ull;
+}
+
+int vca_gpu_last_error(char* buf, int32_t len) {
+  if (buf && len > 0) {
+    std::strncpy(buf, g_err.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)g_err.size();
+}
+
+int vca_gpu_finalize(void) {
+  if (!g) return VCA_OK;
+  g->work.release();
+  g->omega.release();
+  g->gf.release();
+  g->states.release();
+  g->ham.release();
+  g->basis.release();
+  if (g->st) cudaStreamDestroy(g->st);
+  delete g;
+  g = nullptr;
+  return VCA_OK;
+}
+
+int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath_v) {
+  g_err.clear();
+  if (!cfg) VFAIL(VCA_ERR_ARG, "cfg is NULL");
+  vca_config c = *cfg;
+  if ((bath_h == nullptr) != (bath_v == nullptr)) VFAIL(VCA_ERR_ARG, "bath_h and bath_v must be given together");
+  const bool has_bath = bath_h != nullptr;
+  if (has_bath && (c.Nlat_bath < 1 || c.Norb_bath < 1))
+    VFAIL(VCA_ERR_CONFIG, "VCA_INIT_SOLVER error: wrong bath dimensions");  // VCA_MAIN.f90:61
+  if (!has_bath) { c.Nlat_bath = 0; c.Norb_bath = 0; }  // VCA_MAIN.f90:64-66
+  if (c.Nspin < 1 || c.Nspin > 2) VFAIL(VCA_ERR_CONFIG, "ED ERROR: Nspin > 2 is currently not supported");
+  if (c.Norb < 1 || c.Norb > 5) VFAIL(VCA_ERR_CONFIG, "ED ERROR: Norb > 5 is currently not supported");
+  if (c.Nlat < 1) VFAIL(VCA_ERR_CONFIG, "Nlat must be >= 1");
+  if (c.lanc_nstates_total != 1)
+    VFAIL(VCA_ERR_UNSUPPORTED, "finite temperature (LANC_NSTATES_TOTAL != 1) is outside the GPU path");
+  if (c.vca_twin) VFAIL(VCA_ERR_UNSUPPORTED, "VCA_TWIN is outside the GPU path");
+  if (c.lanc_ngfiter < 1 || c.lanc_niter < 1) VFAIL(VCA_ERR_CONFIG, "LANC_NITER and LANC_NGFITER must be >= 1");
+  if (c.omega_nodes < 2) VFAIL(VCA_ERR_CONFIG, "omega_nodes must be >= 2");
+  if (!(c.omega_scale > 0.0)) VFAIL(VCA_ERR_CONFIG, "omega_scale must be > 0");
+  if (c.gs_check_every < 1) c.gs_check_every = 1;
+  const int Ns = c.Nlat * c.Norb + c.Nlat_bath * c.Norb_bath;  // VCA_SETUP.f90:82
+  if (Ns > VCA_MAX_NS) VFAIL(VCA_ERR_UNSUPPORTED, "more than 24 levels per spin");
+  vca_gpu_finalize();
+  g = new Ctx();
+  g->cfg = c;
+  g->has_bath = has_bath;
+  g->Ns = Ns;
+  g->Nsectors = (Ns + 1) * (Ns + 1);  // VCA_SETUP.f90:93
+  g->N = c.Nlat * c.Nspin * c.Norb;
+  g->L = c.Nlat * c.Norb;
+  g->Nb = c.Nlat_bath * c.Nspin * c.Norb_bath;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev < 1) {
+    g_err = "no CUDA device available: the GPU path has no CPU fallback";
+    delete g;
+    g = nullptr;
+    cudaGetLastError();
+    return VCA_ERR_CUDA;
+  }
+  // a blocking stream: the synchronous getters on the legacy stream order after it
+  CUCHK(cudaStreamCreate(&g->st));
+  set_binomials(Ns, g->st);
+  g->dimn.resize(Ns + 1);
+  g->words.resize(Ns + 1);
+  for (int n = 0; n <= Ns; n++) {
+    g->dimn[n] = (int)binom_h(Ns, n);
+    RCHK(g->basis.alloc(&g->words[n], g->dimn[n]));
+    launch_build_words(Ns, n, g->dimn[n], g->words[n], g->st);
+  }
+  RCHK(g->basis.alloc(&g->d_iscratch, 16));
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+int vca_gpu_set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath_v) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  return set_hamiltonian(Hloc, bath_h, bath_v);
+}
+
+int vca_gpu_solve(const double* Hloc, const double* Hk, int64_t Nk, const double* bath_h,
+                  const double* bath_v, double* omega_out) {
+  g_err.clear();
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  return solve_one(Hloc, Hk, Nk, bath_h, bath_v, omega_out);
+}
+
+int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc, const double* Hk, int64_t Nk,
+                        const double* bath_h, int64_t stride_bath_h, const double* bath_v,
+                        int64_t stride_bath_v, double* omega_out) {
+  g_err.clear();
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (B < 0 || !omega_out) VFAIL(VCA_ERR_ARG, "bad batch arguments");
+  for (int b = 0; b < B; b++) {
+    RCHK(solve_one(Hloc + 2 * (size_t)b * stride_hloc, Hk, Nk,
+                   bath_h ? bath_h + 2 * (size_t)b * stride_bath_h : nullptr,
+                   bath_v ? bath_v + 2 * (size_t)b * stride_bath_v : nullptr, omega_out + b));
+  }
+  return VCA_OK;
+}
+
+int vca_gpu_get_sft_potential(double* omega) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!omega) VFAIL(VCA_ERR_ARG, "NULL output");
+  *omega = g->sft;
+  return VCA_OK;
+}
+
+int vca_gpu_get_energies(double* egs, double* omega_int) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (egs) *egs = g->egs;
+  if (omega_int) *omega_int = g->omega_int;
+  return VCA_OK;
+}
+
+int vca_gpu_get_state_count(int32_t* nstates) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  *nstates = (int32_t)g->gs.size();
+  return VCA_OK;
+}
+
+int vca_gpu_get_state(int32_t istate, int32_t* isector, double* energy) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (istate < 1 || istate > (int)g->gs.size()) VFAIL(VCA_ERR_ARG, "state index out of range");
+  if (isector) *isector = g->gs[istate - 1].sector;
+  if (energy) *energy = g->gs[istate - 1].e;
+  return VCA_OK;
+}
+
+int vca_gpu_get_sector_energies(double* e_out, int32_t n) {
+  if (!g || g->sector_e.empty()) VFAIL(VCA_ERR_STATE, "no diagonalisation yet");
+  if (!e_out || n < g->Nsectors) VFAIL(VCA_ERR_ARG, "output too small");
+  for (int i = 0; i < g->Nsectors; i++) e_out[i] = g->sector_e[i];
+  return VCA_OK;
+}
+
+int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t iorb, int32_t jorb,
+                           int32_t istate, int32_t ichan, int32_t* nexc, double* poles, double* weights,
+                           int32_t cap) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  const vca_config& c = g->cfg;
+  if (ilat < 1 || ilat > c.Nlat || jlat < 1 || jlat > c.Nlat || ispin < 1 || ispin > c.Nspin ||
+      iorb < 1 || iorb > c.Norb || jorb < 1 || jorb > c.Norb)
+    VFAIL(VCA_ERR_ARG, "element index out of range");
+  const int e = elem_index(c, ilat - 1, jlat - 1, ispin - 1, iorb - 1, jorb - 1);
+  for (int ch = 0; ch < (int)g->chains.size(); ch++) {
+    const ChainRec& r = g->chains[ch];
+    if (r.elem != e || r.state != istate - 1 || r.chan != ichan) continue;
+    int n = 0;
+    CUCHK(cudaMemcpy(&n, g->d_nexc + ch, sizeof(int), cudaMemcpyDeviceToHost));
+    if (nexc) *nexc = n;
+    if (cap >= n && n > 0) {
+      std::vector<double> p(n);
+      std::vector<double2> w(n);
+      CUCHK(cudaMemcpy(p.data(), g->d_poles + (size_t)ch * g->ld, sizeof(double) * n, cudaMemcpyDeviceToHost));
+      CUCHK(cudaMemcpy(w.data(), g->d_weights + (size_t)ch * g->ld, sizeof(double2) * n, cudaMemcpyDeviceToHost));
+      for (int j = 0; j < n; j++) {
+        if (poles) { poles[2 * j] = p[j]; poles[2 * j + 1] = 0.0; }
+        if (weights) { weights[2 * j] = w[j].x; weights[2 * j + 1] = w[j].y; }
+      }
+    }
+    return VCA_OK;
+  }
+  if (nexc) *nexc = 0;  // channel absent (no target sector), as Nexc=0 in the reference
+  return VCA_OK;
+}
+
+int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!z || !gf_out || nz < 0) VFAIL(VCA_ERR_ARG, "bad arguments");
+  if (nz == 0) return VCA_OK;
+  const vca_config& c = g->cfg;
+  const int N = g->N, NN = N * N;
+  Arena ar;
+  double2 *dz, *Glso;
+  int rc;
+  if ((rc = ar.alloc(&dz, nz)) || (rc = ar.alloc(&Glso, (size_t)nz * NN))) { ar.release(); return rc; }
+  cudaMemcpyAsync(dz, z, sizeof(double2) * nz, cudaMemcpyHostToDevice, g->st);
+  if ((rc = gf_lso((int)nz, dz, Glso, ar))) { ar.release(); return rc; }
+  std::vector<double2> h((size_t)nz * NN);
+  cudaMemcpyAsync(h.data(), Glso, sizeof(double2) * h.size(), cudaMemcpyDeviceToHost, g->st);
+  cudaError_t e = cudaStreamSynchronize(g->st);
+  ar.release();
+  if (e != cudaSuccess) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e));
+  // lso -> (Nlat,Nlat,Nspin,Nspin,Norb,Norb,nz)
+  const size_t nel = hloc_len(c);
+  for (int64_t q = 0; q < nz; q++)
+    for (int il = 0; il < c.Nlat; il++)
+      for (int jl = 0; jl < c.Nlat; jl++)
+        for (int is = 0; is < c.Nspin; is++)
+          for (int js = 0; js < c.Nspin; js++)
+            for (int io = 0; io < c.Norb; io++)
+              for (int jo = 0; jo < c.Norb; jo++) {
+                int a = io + il * c.Norb + is * c.Norb * c.Nlat, b = jo + jl * c.Norb + js * c.Norb * c.Nlat;
+                double2 v = h[(size_t)q * NN + a + (size_t)b * N];
+                size_t o = (size_t)q * nel + idx_nnn(c, il, jl, is, js, io, jo);
+                gf_out[2 * o] = v.x;
+                gf_out[2 * o + 1] = v.y;
+              }
+  return VCA_OK;
+}
+
+static int gimp_grid(bool mats, double* g_out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!g_out) VFAIL(VCA_ERR_ARG, "NULL output");
+  const vca_config& c = g->cfg;
+  const int L = mats ? c.Lmats : c.Lreal;
+  std::vector<double> z(2 * (size_t)L);
+  for (int i = 0; i < L; i++) {
+    if (mats) {  // wm = pi/beta*(2n-1) (VCA_GF_SHARED.f90:50)
+      z[2 * i] = 0.0;
+      z[2 * i + 1] = M_PI / c.beta * (2.0 * (i + 1) - 1.0);
+    } else {     // wr = linspace(wini,wfin,Lreal), +i*eps (VCA_GF_NORMAL.f90:1029)
+      z[2 * i] = (L > 1) ? c.wini + (c.wfin - c.wini) * i / (double)(L - 1) : c.wini;
+      z[2 * i + 1] = c.eps;
+    }
+  }
+  return vca_gpu_gf_cluster(z.data(), L, g_out);
+}
+int vca_gpu_get_gimp_matsubara(double* g_out) { return gimp_grid(true, g_out); }
+int vca_gpu_get_gimp_realaxis(double* g_out) { return gimp_grid(false, g_out); }
+
+int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!w || !f_out || nw < 1) VFAIL(VCA_ERR_ARG, "bad arguments");
+  // the Hk of the last solve is resident (lso); the spin-block test needs
+  // host Hk, so re-derive it conservatively from the device copy
+  const size_t NN = (size_t)g->N * g->N;
+  std::vector<double2> hk(NN * g->Nk);
+  CUCHK(cudaMemcpy(hk.data(), g->d_Hk, sizeof(double2) * hk.size(), cudaMemcpyDeviceToHost));
+  // rebuild an nnn-ordered host copy for the block test
+  const vca_config& c = g->cfg;
+  const size_t nel = hloc_len(c);
+  std::vector<double> hn(2 * nel * g->Nk);
+  for (int64_t k = 0; k < g->Nk; k++)
+    for (int il = 0; il < c.Nlat; il++)
+      for (int jl = 0; jl < c.Nlat; jl++)
+        for (int is = 0; is < c.Nspin; is++)
+          for (int js = 0; js < c.Nspin; js++)
+            for (int io = 0; io < c.Norb; io++)
+              for (int jo = 0; jo < c.Norb; jo++) {
+                int a = io + il * c.Norb + is * c.Norb * c.Nlat, b = jo + jl * c.Norb + js * c.Norb * c.Nlat;
+                double2 v = hk[k * NN + a + (size_t)b * g->N];
+                size_t o = k * nel + idx_nnn(c, il, jl, is, js, io, jo);
+                hn[2 * o] = v.x;
+                hn[2 * o + 1] = v.y;
+              }
+  double dummy;
+  return omega_integral(hn.data(), g->Nk, &dummy, (int)nw, w, f_out);
+}
+
+int vca_gpu_sector_info(int32_t isector, int32_t* nup, int32_t* ndw, int64_t* dimup, int64_t* dimdw) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  const int u = sec_nup(isector), d = sec_ndw(isector);
+  if (nup) *nup = u;
+  if (ndw) *ndw = d;
+  if (dimup) *dimup = g->dimn[u];
+  if (dimdw) *dimdw = g->dimn[d];
+  return VCA_OK;
+}
+
+int vca_gpu_sector_map(int32_t isector, int32_t spin, int64_t* map, int64_t cap) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (isector < 1 || isector > g->Nsectors || (spin != 1 && spin != 2)) VFAIL(VCA_ERR_ARG, "bad sector/spin");
+  const int n = (spin == 1) ? sec_nup(isector) : sec_ndw(isector);
+  const int dim = g->dimn[n];
+  if (!map || cap < dim) VFAIL(VCA_ERR_ARG, "map buffer too small");
+  std::vector<int> w(dim);
+  CUCHK(cudaMemcpy(w.data(), g->words[n], sizeof(int) * dim, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < dim; i++) map[i] = w[i];
+  return VCA_OK;
+}
+
+int vca_gpu_hxv_device(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  if (!is_complex && !g->real_model) VFAIL(VCA_ERR_ARG, "real vectors need a real Hamiltonian");
+  SectorView sv = view_of(sec_nup(isector), sec_ndw(isector));
+  if (is_complex) {
+    if (g->real_model) {  // complex vector on a real H: (re, im) as two real columns
+      launch_hxv_real(sv, g->md, 2, (const double*)d_v, (double*)d_hv, g->st);
+    } else {
+      launch_hxv_cplx(sv, g->md, 1, (const double2*)d_v, (double2*)d_hv, g->st);
+    }
+  } else {
+    launch_hxv_real(sv, g->md, 1, (const double*)d_v, (double*)d_hv, g->st);
+  }
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
+
+int vca_gpu_hxv(int32_t isector, const double* v, double* hv) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  if (!v || !hv) VFAIL(VCA_ERR_ARG, "NULL vector");
+  const int64_t D = (int64_t)g->dimn[sec_nup(isector)] * g->dimn[sec_ndw(isector)];
+  Arena ar;
+  double2 *dv, *dh;
+  int rc;
+  if ((rc = ar.alloc(&dv, D)) || (rc = ar.alloc(&dh, D))) { ar.release(); return rc; }
+  cudaMemcpyAsync(dv, v, sizeof(double2) * D, cudaMemcpyHostToDevice, g->st);
+  rc = vca_gpu_hxv_device(isector, dv, dh, 1);
+  if (rc) { ar.release(); return rc; }
+  cudaMemcpyAsync(hv, dh, sizeof(double2) * D, cudaMemcpyDeviceToHost, g->st);
+  cudaError_t e = cudaStreamSynchronize(g->st);
+  ar.release();
+  if (e != cudaSuccess) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e));
+  return VCA_OK;
+}
+
+int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t reps,
+                      double* ms_per_call) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
+  if (reps < 1 || !ms_per_call) VFAIL(VCA_ERR_ARG, "bad arguments");
+  cudaEvent_t e0, e1;
+  CUCHK(cudaEventCreate(&e0));
+  CUCHK(cudaEventCreate(&e1));
+  RCHK(vca_gpu_hxv_device(isector, d_v, d_hv, is_complex));  // warm-up
+  CUCHK(cudaEventRecord(e0, g->st));
+  for (int r = 0; r < reps; r++) RCHK(vca_gpu_hxv_device(isector, d_v, d_hv, is_complex));
+  CUCHK(cudaEventRecord(e1, g->st));
+  CUCHK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CUCHK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_call = ms / reps;
+  return VCA_OK;
+}
+
+}  // extern "C"

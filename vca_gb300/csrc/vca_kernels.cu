@@ -1,0 +1,1167 @@
+// vca_kernels.cu -- sm_103a kernels of the cluster-ED -> Lanczos GF -> Omega
+// path (GB300).  Every grid is bounded by its buffers: grid-stride loops over
+// explicit 64-bit extents, no device-side waits.
+#include "vca_kernels.cuh"
+
+#include <cmath>
+#include <cstdio>
+
+namespace vca {
+
+__constant__ int64_t c_binom[VCA_MAX_NS + 1][VCA_MAX_NS + 1];
+
+static inline int nblocks(int64_t n, int threads, int cap = 152 * 16) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+void set_binomials(int Ns, cudaStream_t st) {
+  static Binom h;
+  for (int n = 0; n <= VCA_MAX_NS; n++)
+    for (int k = 0; k <= VCA_MAX_NS; k++) {
+      if (k > n) { h.c[n][k] = 0; continue; }
+      int64_t v = 1;
+      for (int t = 1; t <= k; t++) v = v * (n + 1 - t) / t;
+      h.c[n][k] = v;
+    }
+  (void)Ns;
+  cudaMemcpyToSymbolAsync(c_binom, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
+}
+
+// colex rank of a Fock word: sum_t C(pos_t, t) over set bits (ascending)
+__device__ __forceinline__ int rank_word(unsigned w) {
+  int64_t r = 0;
+  int t = 1;
+  while (w) {
+    int p = __ffs(w) - 1;
+    r += c_binom[p][t];
+    t++;
+    w &= w - 1;
+  }
+  return (int)r;
+}
+
+__device__ __forceinline__ double parity(unsigned x) { return (__popc(x) & 1) ? -1.0 : 1.0; }
+
+// ---------------------------------------------------------------------------
+// Fock maps: ascending words of popcount n (build_sector, VCA_SETUP.f90:660-695)
+// ---------------------------------------------------------------------------
+__global__ void k_build_words(int Ns, int n, int dim, int* words) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += gridDim.x * blockDim.x) {
+    int64_t rr = r;
+    unsigned w = 0;
+    for (int t = n; t >= 1; --t) {
+      int p = Ns - 1;
+      while (p >= t && c_binom[p][t] > rr) --p;  // largest p with C(p,t) <= rr
+      w |= 1u << p;
+      rr -= c_binom[p][t];
+    }
+    words[r] = (int)w;
+  }
+}
+void launch_build_words(int Ns, int n, int dim, int* words, cudaStream_t st) {
+  k_build_words<<<nblocks(dim, 256), 256, 0, st>>>(Ns, n, dim, words);
+}
+
+// ---------------------------------------------------------------------------
+// Pull hop tables.  Row = target word w; a pair (i <- j) with amplitude A of
+// c^dag_i c_j contributes when bit i is set and bit j clear in w; the source
+// is ws = w - i + j and the element is A * sg1 * sg2 with the one-word sign
+// convention of c/cdg (VCA_SETUP.f90:724-750): sg1 from bits of ws below j,
+// sg2 from bits of (ws without j) below i.  Same elements as the stored
+// spH0ups/spH0dws of VCA_HAMILTONIAN/stored/H_cluster_up.f90 (cluster :1-28,
+// bath :30-55, hybridisation :57-86) enumerated by target instead of source.
+// ---------------------------------------------------------------------------
+__global__ void k_hop_count(int dim, const int* words, const HopPair* pairs, int npairs, int* cnt,
+                            int* gmax) {
+  int local_max = 0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += gridDim.x * blockDim.x) {
+    unsigned w = (unsigned)words[r];
+    int c = 0;
+    for (int q = 0; q < npairs; q++) {
+      HopPair p = pairs[q];
+      if (((w >> p.i) & 1u) && !((w >> p.j) & 1u)) c++;
+    }
+    cnt[r] = c;
+    local_max = max(local_max, c);
+  }
+  atomicMax(gmax, local_max);
+}
+int launch_hop_count(int Ns, int n, int dim, const int* words, const HopPair* d_pairs, int npairs,
+                     int* cnt, int* d_scratch_max, cudaStream_t st) {
+  (void)Ns;
+  (void)n;
+  cudaMemsetAsync(d_scratch_max, 0, sizeof(int), st);
+  k_hop_count<<<nblocks(dim, 256), 256, 0, st>>>(dim, words, d_pairs, npairs, cnt, d_scratch_max);
+  int h = 0;
+  cudaMemcpyAsync(&h, d_scratch_max, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  return h;
+}
+
+__global__ void k_hop_fill(int dim, int width, const int* words, const HopPair* pairs, int npairs,
+                           int* src, double2* amp) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += gridDim.x * blockDim.x) {
+    unsigned w = (unsigned)words[r];
+    int c = 0;
+    for (int q = 0; q < npairs && c < width; q++) {
+      HopPair p = pairs[q];
+      if (!(((w >> p.i) & 1u) && !((w >> p.j) & 1u))) continue;
+      unsigned ws = (w ^ (1u << p.i)) | (1u << p.j);
+      double sg1 = parity(ws & ((1u << p.j) - 1u));
+      unsigned k1 = ws & ~(1u << p.j);
+      double sg2 = parity(k1 & ((1u << p.i) - 1u));
+      double sg = sg1 * sg2;
+      src[(int64_t)c * dim + r] = rank_word(ws);
+      amp[(int64_t)c * dim + r] = make_double2(p.re * sg, p.im * sg);
+      c++;
+    }
+    for (; c < width; c++) {  // padding never read (cnt[r] bounds the loop)
+      src[(int64_t)c * dim + r] = 0;
+      amp[(int64_t)c * dim + r] = make_double2(0.0, 0.0);
+    }
+  }
+}
+void launch_hop_fill(int Ns, int n, int dim, int width, const int* words, const HopPair* d_pairs,
+                     int npairs, int* src, double2* amp, cudaStream_t st) {
+  (void)Ns;
+  (void)n;
+  if (width == 0) return;
+  k_hop_fill<<<nblocks(dim, 256), 256, 0, st>>>(dim, width, words, d_pairs, npairs, src, amp);
+}
+
+// one-body + same-spin energy of a word (H_cluster_local.f90:19-25,46-55,59-76,84-92)
+__global__ void k_e1(int dim, const int* words, E1Params p, int with_const, double2* e1) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += gridDim.x * blockDim.x) {
+    unsigned w = (unsigned)words[r];
+    double er = 0.0, ei = 0.0;
+    unsigned x = w;
+    while (x) {
+      int b = __ffs(x) - 1;
+      er += p.eps[b].x;
+      ei += p.eps[b].y;
+      x &= x - 1;
+    }
+    int same = 0;
+    for (int o = 0; o < p.norb; o++)
+      for (int q = o + 1; q < p.norb; q++) same += __popc(w & p.omask[o] & (w >> (q - o)));
+    er += p.upar * same;
+    if (with_const) { er += p.cst.x; ei += p.cst.y; }
+    e1[r] = make_double2(er, ei);
+  }
+}
+void launch_e1(int dim, const int* words, const E1Params& p, bool with_const, double2* e1,
+               cudaStream_t st) {
+  k_e1<<<nblocks(dim, 256), 256, 0, st>>>(dim, words, p, with_const ? 1 : 0, e1);
+}
+
+// opposite-spin density-density terms (H_cluster_local.f90:26-45)
+__device__ __forceinline__ double mixed_diag(const MixedDiag& md, unsigned u, unsigned d) {
+  double s = 0.0;
+  for (int o = 0; o < md.norb; o++) s += md.U[o] * (double)__popc(u & d & md.omask[o]);
+  int c = 0;
+  for (int o = 0; o < md.norb; o++)
+    for (int q = o + 1; q < md.norb; q++)
+      c += __popc(u & md.omask[o] & (d >> (q - o))) + __popc(u & md.omask[q] & (d << (q - o)));
+  if (c) s += md.Ust * (double)c;
+  return s + md.c0;
+}
+
+// ---------------------------------------------------------------------------
+// H x v on a column batch: Y = d o X + H_up X + X H_dw^T per column, the
+// stored product of VCA_HAMILTONIAN_SPARSE_HxV.f90:152-200 with the diagonal
+// of H_cluster_local.f90 computed on the fly from the two words.
+// Thread block = CW columns x RB rows; each thread walks its rows and its
+// columns c = tx, tx+CW, ... (neighbour loads are contiguous across tx).
+// ---------------------------------------------------------------------------
+__global__ void k_hxv_real(SectorView sv, MixedDiag md, int m, const double* __restrict__ X,
+                           double* __restrict__ Y) {
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int CW = blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; i < D;
+       i += (int64_t)gridDim.x * blockDim.y) {
+    const int idw = (int)(i / sv.dimup);
+    const int iup = (int)(i - (int64_t)idw * sv.dimup);
+    const double d = sv.up_e1[iup].x + sv.dw_e1[idw].x +
+                     mixed_diag(md, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
+    const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
+    const int64_t colbase = (int64_t)idw * sv.dimup;
+    for (int c = threadIdx.x; c < m; c += CW) {
+      double acc = d * X[i * m + c];
+      for (int k = 0; k < nu; k++) {
+        const int s = sv.up_src[(int64_t)k * sv.dimup + iup];
+        acc = fma(sv.up_amp[(int64_t)k * sv.dimup + iup].x, X[(colbase + s) * m + c], acc);
+      }
+      for (int k = 0; k < nd; k++) {
+        const int s = sv.dw_src[(int64_t)k * sv.dimdw + idw];
+        acc = fma(sv.dw_amp[(int64_t)k * sv.dimdw + idw].x, X[((int64_t)iup + (int64_t)s * sv.dimup) * m + c], acc);
+      }
+      Y[i * m + c] = acc;
+    }
+  }
+}
+
+__device__ __forceinline__ double2 cfma(double2 a, double2 x, double2 acc) {
+  acc.x = fma(a.x, x.x, acc.x);
+  acc.x = fma(-a.y, x.y, acc.x);
+  acc.y = fma(a.x, x.y, acc.y);
+  acc.y = fma(a.y, x.x, acc.y);
+  return acc;
+}
+
+__global__ void k_hxv_cplx(SectorView sv, MixedDiag md, int m, const double2* __restrict__ X,
+                           double2* __restrict__ Y) {
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int CW = blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; i < D;
+       i += (int64_t)gridDim.x * blockDim.y) {
+    const int idw = (int)(i / sv.dimup);
+    const int iup = (int)(i - (int64_t)idw * sv.dimup);
+    double2 d = make_double2(sv.up_e1[iup].x + sv.dw_e1[idw].x +
+                                 mixed_diag(md, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]),
+                             sv.up_e1[iup].y + sv.dw_e1[idw].y);
+    const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
+    const int64_t colbase = (int64_t)idw * sv.dimup;
+    for (int c = threadIdx.x; c < m; c += CW) {
+      double2 acc = cfma(d, X[i * m + c], make_double2(0.0, 0.0));
+      for (int k = 0; k < nu; k++) {
+        const int s = sv.up_src[(int64_t)k * sv.dimup + iup];
+        acc = cfma(sv.up_amp[(int64_t)k * sv.dimup + iup], X[(colbase + s) * m + c], acc);
+      }
+      for (int k = 0; k < nd; k++) {
+        const int s = sv.dw_src[(int64_t)k * sv.dimdw + idw];
+        acc = cfma(sv.dw_amp[(int64_t)k * sv.dimdw + idw], X[((int64_t)iup + (int64_t)s * sv.dimup) * m + c], acc);
+      }
+      Y[i * m + c] = acc;
+    }
+  }
+}
+
+static void col_shape(int m, dim3& blk) {
+  int cw = 1;
+  while (cw < m && cw < 32) cw <<= 1;
+  blk = dim3(cw, 256 / cw, 1);
+}
+void launch_hxv_real(const SectorView& sv, const MixedDiag& md, int m, const double* X, double* Y,
+                     cudaStream_t st) {
+  dim3 blk;
+  col_shape(m, blk);
+  int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  k_hxv_real<<<nblocks(D, blk.y, 152 * 32), blk, 0, st>>>(sv, md, m, X, Y);
+}
+void launch_hxv_cplx(const SectorView& sv, const MixedDiag& md, int m, const double2* X, double2* Y,
+                     cudaStream_t st) {
+  dim3 blk;
+  col_shape(m, blk);
+  int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  k_hxv_cplx<<<nblocks(D, blk.y, 152 * 32), blk, 0, st>>>(sv, md, m, X, Y);
+}
+
+// ---------------------------------------------------------------------------
+// Column-batch vector operations.  Reductions are two-stage with a fixed
+// grid: per-block partials, then a per-column sum in block order, so a
+// repeated run reproduces the same bits.
+// ---------------------------------------------------------------------------
+template <bool CPLX>
+__global__ void k_col_dot(int64_t rows, int m, const void* Xv, const void* Yv, double* partial) {
+  extern __shared__ double sh[];
+  const int CW = blockDim.x, RB = blockDim.y;
+  const int c = blockIdx.y * CW + threadIdx.x;
+  double s = 0.0;
+  if (c < m) {
+    for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB) {
+      if (CPLX) {
+        double2 x = ((const double2*)Xv)[i * m + c], y = ((const double2*)Yv)[i * m + c];
+        s = fma(x.x, y.x, s);
+        s = fma(x.y, y.y, s);
+      } else {
+        s = fma(((const double*)Xv)[i * m + c], ((const double*)Yv)[i * m + c], s);
+      }
+    }
+  }
+  sh[threadIdx.y * CW + threadIdx.x] = s;
+  __syncthreads();
+  for (int h = RB / 2; h > 0; h >>= 1) {
+    if (threadIdx.y < h) sh[threadIdx.y * CW + threadIdx.x] += sh[(threadIdx.y + h) * CW + threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.y == 0 && c < m) partial[(int64_t)blockIdx.x * m + c] = sh[threadIdx.x];
+}
+__global__ void k_col_reduce(int m, int nblk, const double* partial, double* out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; b++) s += partial[(int64_t)b * m + c];
+    out[c] = s;
+  }
+}
+void launch_col_dot(const ColBatch& b, const void* X, const void* Y, double* partial, int nblk,
+                    double* out_col, cudaStream_t st) {
+  dim3 blk;
+  col_shape(b.m, blk);
+  dim3 grd(nblk, (b.m + blk.x - 1) / blk.x, 1);
+  size_t shm = sizeof(double) * 256;
+  if (b.cplx)
+    k_col_dot<true><<<grd, blk, shm, st>>>(b.rows, b.m, X, Y, partial);
+  else
+    k_col_dot<false><<<grd, blk, shm, st>>>(b.rows, b.m, X, Y, partial);
+  k_col_reduce<<<nblocks(b.m, 128), 128, 0, st>>>(b.m, nblk, partial, out_col);
+}
+
+template <bool CPLX>
+__global__ void k_col_axpy(int64_t rows, int m, const int* col2ch, const ChainMeta* meta,
+                           const double* coef, double sgn, const void* Xv, void* Yv) {
+  const int64_t n = rows * m;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(g % m);
+    const int ch = col2ch[c];
+    if (!meta[ch].active) continue;
+    const double a = sgn * coef[ch];
+    if (CPLX) {
+      double2 x = ((const double2*)Xv)[g];
+      double2& y = ((double2*)Yv)[g];
+      y.x = fma(a, x.x, y.x);
+      y.y = fma(a, x.y, y.y);
+    } else {
+      ((double*)Yv)[g] = fma(a, ((const double*)Xv)[g], ((double*)Yv)[g]);
+    }
+  }
+}
+void launch_col_axpy(const ColBatch& b, const double* coef, const void* X, void* Y, bool negate,
+                     cudaStream_t st) {
+  int64_t n = b.rows * b.m;
+  if (b.cplx)
+    k_col_axpy<true><<<nblocks(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, coef,
+                                                      negate ? -1.0 : 1.0, X, Y);
+  else
+    k_col_axpy<false><<<nblocks(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, coef,
+                                                       negate ? -1.0 : 1.0, X, Y);
+}
+
+template <bool CPLX>
+__global__ void k_col_scale(int64_t rows, int m, const int* col2ch, const ChainMeta* meta,
+                            const double* scale, const void* Yv, void* Xv) {
+  const int64_t n = rows * m;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(g % m);
+    const int ch = col2ch[c];
+    // retired chains get zero columns, so later products on them stay finite
+    const double a = meta[ch].active ? scale[ch] : 0.0;
+    if (CPLX) {
+      double2 y = ((const double2*)Yv)[g];
+      ((double2*)Xv)[g] = make_double2(a * y.x, a * y.y);
+    } else {
+      ((double*)Xv)[g] = a * ((const double*)Yv)[g];
+    }
+  }
+}
+void launch_col_scale(const ColBatch& b, const double* scale, const void* Y, void* X, cudaStream_t st) {
+  int64_t n = b.rows * b.m;
+  if (b.cplx)
+    k_col_scale<true><<<nblocks(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scale, Y, X);
+  else
+    k_col_scale<false><<<nblocks(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scale, Y, X);
+}
+
+__global__ void k_chain_sum(int nch, const ChainMeta* meta, const double* in_col, double* out) {
+  for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = 0; q < meta[ch].ncol; q++) s += in_col[meta[ch].col0 + q];
+    out[ch] = s;
+  }
+}
+void launch_chain_sum(const ColBatch& b, const double* in_col, double* out_ch, cudaStream_t st) {
+  k_chain_sum<<<nblocks(b.nch, 128), 128, 0, st>>>(b.nch, b.meta, in_col, out_ch);
+}
+
+// sp_lanc_tridiag bookkeeping (SciFortran, restated): alpha_k stored, the
+// chain stops when beta_{k+1} < tol, otherwise beta_{k+1} -> Bt[k] for k < nlanc.
+__global__ void k_lanczos_record(int nch, ChainMeta* meta, int k, const double* alpha_ch,
+                                 const double* beta2_ch, double* A, double* Bt, int ldab, double tol,
+                                 double* invbeta, double* beta_now) {
+  for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
+    ChainMeta mt = meta[ch];
+    if (!mt.active) continue;
+    const double a = alpha_ch[ch];
+    const double b = sqrt(fmax(beta2_ch[ch], 0.0));
+    A[(int64_t)ch * ldab + (k - 1)] = a;
+    mt.len = k;
+    if (b < tol) {
+      mt.active = 0;
+      invbeta[ch] = 0.0;
+      beta_now[ch] = b;
+    } else {
+      if (k < mt.nlanc) Bt[(int64_t)ch * ldab + k] = b;
+      if (k >= mt.nlanc) mt.active = 0;
+      invbeta[ch] = 1.0 / b;
+      beta_now[ch] = b;
+    }
+    meta[ch] = mt;
+  }
+}
+void launch_lanczos_record(int nch, ChainMeta* meta, int k, const double* alpha_ch,
+                           const double* beta2_ch, double* A, double* Bt, int ldab, double tol,
+                           double* invbeta, double* beta_now, cudaStream_t st) {
+  k_lanczos_record<<<nblocks(nch, 128), 128, 0, st>>>(nch, meta, k, alpha_ch, beta2_ch, A, Bt, ldab,
+                                                      tol, invbeta, beta_now);
+}
+
+template <bool CPLX>
+__global__ void k_psi_accum(int64_t n, const double* s, int k, const void* Xv, void* Pv) {
+  const double a = s[k];
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    if (CPLX) {
+      double2 x = ((const double2*)Xv)[g];
+      double2& p = ((double2*)Pv)[g];
+      p.x = fma(a, x.x, p.x);
+      p.y = fma(a, x.y, p.y);
+    } else {
+      ((double*)Pv)[g] = fma(a, ((const double*)Xv)[g], ((double*)Pv)[g]);
+    }
+  }
+}
+void launch_psi_accum(int64_t n, bool cplx, const double* s, int k, const void* X, void* psi,
+                      cudaStream_t st) {
+  if (cplx)
+    k_psi_accum<true><<<nblocks(n, 256), 256, 0, st>>>(n, s, k, X, psi);
+  else
+    k_psi_accum<false><<<nblocks(n, 256), 256, 0, st>>>(n, s, k, X, psi);
+}
+
+// splitmix64 (Steele, Lea & Flood 2014) of (seed, sector, index) -> [-1, 1)
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void k_start_vector(int64_t n, uint64_t seed, int isector, double* X) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = splitmix64(seed + 0xD1B54A32D192ED03ull * (uint64_t)isector + (uint64_t)i);
+    X[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  }
+}
+void launch_start_vector(int64_t n, uint64_t seed, int isector, double* X, cudaStream_t st) {
+  k_start_vector<<<nblocks(n, 256), 256, 0, st>>>(n, seed, isector, X);
+}
+__global__ void k_fill(int64_t n, double v, double* X) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    X[i] = v;
+}
+void launch_fill(int64_t n, double v, double* X, cudaStream_t st) {
+  k_fill<<<nblocks(n, 256), 256, 0, st>>>(n, v, X);
+}
+
+// ---------------------------------------------------------------------------
+// Lowest eigenpair of the Lanczos T_k: warp multisection on the Sturm count
+// (33 points a round) then inverse iteration with a partially pivoted
+// tridiagonal LU (Wilkinson ch. 5).  Residual estimate |beta_{k+1} s_k|.
+// ---------------------------------------------------------------------------
+__device__ int sturm_count_dev(const double* a, const double* b1, int k, double x) {
+  // b1[j] = beta_{j+1} for j >= 1 (off-diagonal between rows j-1 and j)
+  int cnt = 0;
+  double q = a[0] - x;
+  if (q < 0) cnt++;
+  for (int j = 1; j < k; j++) {
+    if (q == 0.0) q = 1e-300;
+    q = a[j] - x - b1[j] * b1[j] / q;
+    if (q < 0) cnt++;
+  }
+  return cnt;
+}
+
+__global__ void k_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta_out,
+                             double* s, double* resid) {
+  __shared__ double lo_s, hi_s;
+  __shared__ int first_s;
+  const int lane = threadIdx.x;
+  if (lane == 0) {
+    double lo = A[0], hi = A[0];
+    for (int j = 0; j < k; j++) {
+      double r = (j > 0 ? fabs(Bt[j]) : 0.0) + (j < k - 1 ? fabs(Bt[j + 1]) : 0.0);
+      lo = fmin(lo, A[j] - r);
+      hi = fmax(hi, A[j] + r);
+    }
+    lo_s = lo;
+    hi_s = hi;
+  }
+  __syncthreads();
+  for (int round = 0; round < 100; round++) {
+    double lo = lo_s, hi = hi_s;
+    double x = lo + (hi - lo) * (double)(lane + 1) / 33.0;
+    int c = (x > lo && x < hi) ? sturm_count_dev(A, Bt, k, x) : (x >= hi ? 1 : 0);
+    unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
+    __syncthreads();
+    if (lane == 0) {
+      int f = ball ? (__ffs(ball) - 1) : 32;  // first point with count >= 1
+      double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 33.0;
+      double nhi = (f == 32) ? hi : lo + (hi - lo) * (double)(f + 1) / 33.0;
+      if (nlo < lo) nlo = lo;
+      if (nhi > hi) nhi = hi;
+      first_s = (nhi - nlo <= 2.220446049250313e-16 * fmax(fabs(nlo), fabs(nhi)) || !(nlo < nhi) ||
+                 (nlo == lo && nhi == hi)) ? 1 : 0;
+      lo_s = nlo;
+      hi_s = nhi;
+    }
+    __syncthreads();
+    if (first_s) break;
+  }
+  if (lane != 0) return;
+  // refine to adjacent doubles by plain bisection (a handful of steps)
+  double lo = lo_s, hi = hi_s;
+  for (int it = 0; it < 200; it++) {
+    double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (sturm_count_dev(A, Bt, k, mid) >= 1) hi = mid; else lo = mid;
+  }
+  const double th = 0.5 * (lo + hi);
+  theta_out[0] = th;
+  // inverse iteration: s <- (T - th)^{-1} s, 3 steps (dgttrf/dgttrs restated)
+  double* y = s;
+  for (int j = 0; j < k; j++) y[j] = 1.0;
+  if (k == 1) {
+    y[0] = 1.0;
+    resid[0] = fabs(btail);
+    return;
+  }
+  // local work lives in s[k..5k) of the caller-provided buffer
+  double* dl = s + k;
+  double* dd = s + 2 * k;
+  double* du = s + 3 * k;
+  double* du2 = s + 4 * k;
+  for (int it = 0; it < 3; it++) {
+    for (int j = 0; j < k; j++) dd[j] = A[j] - th;
+    for (int j = 0; j < k - 1; j++) { dl[j] = Bt[j + 1]; du[j] = Bt[j + 1]; du2[j] = 0.0; }
+    unsigned long long pivbits[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // k <= 512
+    for (int j = 0; j < k - 1; j++) {
+      if (fabs(dd[j]) >= fabs(dl[j])) {
+        if (dd[j] == 0.0) dd[j] = 1e-300;
+        double f = dl[j] / dd[j];
+        dl[j] = f;
+        dd[j + 1] -= f * du[j];
+      } else {
+        double f = dd[j] / dl[j];
+        dd[j] = dl[j];
+        dl[j] = f;
+        double t = du[j];
+        du[j] = dd[j + 1];
+        dd[j + 1] = t - f * dd[j + 1];
+        if (j < k - 2) { du2[j] = du[j + 1]; du[j + 1] = -f * du[j + 1]; }
+        pivbits[j >> 6] |= 1ull << (j & 63);
+      }
+    }
+    if (dd[k - 1] == 0.0) dd[k - 1] = 1e-300;
+    for (int j = 0; j < k - 1; j++) {
+      if (!((pivbits[j >> 6] >> (j & 63)) & 1ull)) y[j + 1] -= dl[j] * y[j];
+      else { double t = y[j]; y[j] = y[j + 1]; y[j + 1] = t - dl[j] * y[j]; }
+    }
+    y[k - 1] /= dd[k - 1];
+    y[k - 2] = (y[k - 2] - du[k - 2] * y[k - 1]) / dd[k - 2];
+    for (int j = k - 3; j >= 0; j--) y[j] = (y[j] - du[j] * y[j + 1] - du2[j] * y[j + 2]) / dd[j];
+    double nr = 0.0;
+    for (int j = 0; j < k; j++) nr += y[j] * y[j];
+    nr = sqrt(nr);
+    for (int j = 0; j < k; j++) y[j] /= nr;
+  }
+  if (y[0] < 0) for (int j = 0; j < k; j++) y[j] = -y[j];
+  resid[0] = fabs(btail * y[k - 1]);
+}
+void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta,
+                       double* s, double* resid, cudaStream_t st) {
+  k_tri_lowest<<<1, 32, 0, st>>>(A, Bt, k, btail, theta, s, resid);
+}
+
+// ---------------------------------------------------------------------------
+// Chain tridiagonal -> poles and weights.  Implicit QL with Wilkinson shift
+// (EISPACK tql2; the reference calls SciFortran eigh(d,e,Ev=Z) at
+// VCA_GF_NORMAL.f90:1012) tracking only the first row of Z.  One thread per
+// chain; work = 3*ld doubles per chain.
+// ---------------------------------------------------------------------------
+__global__ void k_chain_poles(int nch, const ChainMeta* meta, const double* A, const double* Bt,
+                              int ldab, const double* norm2, const double2* wfac, const int* isign,
+                              double Ei, double zeta, double* work, double* poles, double2* weights,
+                              int* nexc) {
+  for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
+    const int n = meta[ch].len;
+    nexc[ch] = n;
+    if (n <= 0) continue;
+    double* d = work + (int64_t)ch * 3 * ldab;
+    double* e = d + ldab;
+    double* z = e + ldab;
+    for (int i = 0; i < n; i++) {
+      d[i] = A[(int64_t)ch * ldab + i];
+      e[i] = (i + 1 < n) ? Bt[(int64_t)ch * ldab + i + 1] : 0.0;  // e[i] couples i,i+1
+      z[i] = (i == 0) ? 1.0 : 0.0;
+    }
+    double f = 0.0, tst1 = 0.0;
+    const double eps = 2.220446049250313e-16;
+    for (int l = 0; l < n; l++) {
+      int iter = 0;
+      double h = fabs(d[l]) + fabs(e[l]);
+      if (tst1 < h) tst1 = h;
+      int m = l;
+      while (m < n - 1 && fabs(e[m]) > eps * tst1) m++;
+      if (m > l) {
+        do {
+          if (++iter > 60) break;
+          double g = d[l];
+          double p = (d[l + 1] - g) / (2.0 * e[l]);
+          double r = hypot(p, 1.0);
+          double sr = (p >= 0.0) ? r : -r;
+          d[l] = e[l] / (p + sr);
+          d[l + 1] = e[l] * (p + sr);
+          double dl1 = d[l + 1];
+          h = g - d[l];
+          for (int i = l + 2; i < n; i++) d[i] -= h;
+          f += h;
+          p = d[m];
+          double c = 1.0, c2 = 1.0, c3 = 1.0, el1 = e[l + 1], s = 0.0, s2 = 0.0;
+          for (int i = m - 1; i >= l; i--) {
+            c3 = c2;
+            c2 = c;
+            s2 = s;
+            g = c * e[i];
+            h = c * p;
+            r = hypot(p, e[i]);
+            e[i + 1] = s * r;
+            s = e[i] / r;
+            c = p / r;
+            p = c * d[i] - s * g;
+            d[i + 1] = h + s * (c * g + s * d[i]);
+            double zi1 = z[i + 1], zi = z[i];
+            z[i + 1] = s * zi + c * zi1;
+            z[i] = c * zi - s * zi1;
+          }
+          p = -s * s2 * c3 * el1 * e[l] / dl1;
+          e[l] = s * p;
+          d[l] = c * p;
+        } while (fabs(e[l]) > eps * tst1);
+      }
+      d[l] += f;
+      e[l] = 0.0;
+    }
+    for (int ii = 1; ii < n; ii++) {  // ascending, as tql2
+      int i = ii - 1, kk = i;
+      double p = d[i];
+      for (int j = ii; j < n; j++) if (d[j] < p) { kk = j; p = d[j]; }
+      if (kk != i) {
+        d[kk] = d[i];
+        d[i] = p;
+        double t = z[i];
+        z[i] = z[kk];
+        z[kk] = t;
+      }
+    }
+    const double2 wf = wfac[ch];
+    const double pes = norm2[ch] / zeta;
+    for (int j = 0; j < n; j++) {
+      double w2 = z[j] * z[j] * pes;
+      poles[(int64_t)ch * ldab + j] = (double)isign[ch] * (d[j] - Ei);
+      weights[(int64_t)ch * ldab + j] = make_double2(wf.x * w2, wf.y * w2);
+    }
+  }
+}
+void launch_chain_poles(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
+                        const double* norm2, const double2* wfac, const int* isign, double Ei,
+                        double zeta, double* work, double* poles, double2* weights, int* nexc,
+                        cudaStream_t st) {
+  k_chain_poles<<<nblocks(nch, 64), 64, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta,
+                                                 work, poles, weights, nexc);
+}
+
+// ---------------------------------------------------------------------------
+// Chain start vectors by gather: target row t, term (pos, coef): for c^dag
+// the target spin word must hold pos and the source is w - pos; for c it must
+// not and the source is w + pos.  sign = parity of source bits below pos
+// (cdg/c, VCA_SETUP.f90:724-750) -- the same bits as in the target word.
+// ---------------------------------------------------------------------------
+template <bool GSC, bool COLC>
+__global__ void k_chain_init(SectorView tgt, int src_dimup, const void* gsv, int nchain,
+                             const ChainInit* ci, int m, void* Xv) {
+  const int64_t D = (int64_t)tgt.dimup * tgt.dimdw;
+  const int64_t n = D * nchain;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int ch = (int)(g % nchain);
+    const int64_t i = g / nchain;
+    const int idw = (int)(i / tgt.dimup);
+    const int iup = (int)(i - (int64_t)idw * tgt.dimup);
+    const ChainInit c = ci[ch];
+    const unsigned w = (unsigned)(c.spin == 0 ? tgt.up_words[iup] : tgt.dw_words[idw]);
+    double vr = 0.0, vi = 0.0;
+    for (int q = 0; q < c.nterm; q++) {
+      const int pos = c.t[q].pos;
+      const bool occ = (w >> pos) & 1u;
+      if (c.dag ? !occ : occ) continue;
+      const unsigned ws = w ^ (1u << pos);
+      const double sg = parity(ws & ((1u << pos) - 1u));
+      const int rs = rank_word(ws);
+      const int64_t si = (c.spin == 0) ? ((int64_t)rs + (int64_t)idw * src_dimup)
+                                       : ((int64_t)iup + (int64_t)rs * src_dimup);
+      double gr, gi;
+      if (GSC) { double2 gv = ((const double2*)gsv)[si]; gr = gv.x; gi = gv.y; }
+      else { gr = ((const double*)gsv)[si]; gi = 0.0; }
+      // (coef * sg) * gs
+      const double ar = c.t[q].re * sg, ai = c.t[q].im * sg;
+      vr += ar * gr - ai * gi;
+      vi += ar * gi + ai * gr;
+    }
+    if (COLC) {
+      ((double2*)Xv)[i * m + c.col0] = make_double2(vr, vi);
+    } else {
+      ((double*)Xv)[i * m + c.col0] = vr;
+      if (c.cplxcol) ((double*)Xv)[i * m + c.col0 + 1] = vi;
+    }
+  }
+}
+void launch_chain_init(const SectorView& tgt, int src_dimup, const void* gs, bool gs_cplx,
+                       int nchain, const ChainInit* d_ci, int m, bool cols_cplx, void* X,
+                       cudaStream_t st) {
+  int64_t n = (int64_t)tgt.dimup * tgt.dimdw * nchain;
+  int nb = nblocks(n, 256);
+  if (cols_cplx) {
+    if (gs_cplx) k_chain_init<true, true><<<nb, 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, X);
+    else k_chain_init<false, true><<<nb, 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, X);
+  } else {
+    k_chain_init<false, false><<<nb, 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, X);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cluster Green's function from poles (vca_gf_cluster_scalar,
+// VCA_IO/gf_cluster.f90:23-49) and recombination (:50-62).
+// ---------------------------------------------------------------------------
+__global__ void k_gf_eval(GfLayout g, int nz, const double2* z, double2* G) {
+  const int64_t n = (int64_t)nz * g.nelem;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t % g.nelem);
+    const int q = (int)(t / g.nelem);
+    const double zr = z[q].x, zi = z[q].y;
+    double ar = 0.0, ai = 0.0;
+    for (int x = g.elem_ptr[e]; x < g.elem_ptr[e + 1]; x++) {
+      const int ch = g.elem_chain[x];
+      const int np = g.nexc[ch];
+      const double* P = g.poles + (int64_t)ch * g.ld;
+      const double2* W = g.weights + (int64_t)ch * g.ld;
+      for (int j = 0; j < np; j++) {
+        const double dr = zr - P[j];
+        const double inv = 1.0 / fma(dr, dr, zi * zi);
+        // w / (z - p) = w * (dr - i zi) / |z - p|^2
+        const double2 w = W[j];
+        ar += (w.x * dr + w.y * zi) * inv;
+        ai += (w.y * dr - w.x * zi) * inv;
+      }
+    }
+    G[t] = make_double2(ar, ai);
+  }
+}
+void launch_gf_eval(const GfLayout& g, int nz, const double2* z, double2* G, cudaStream_t st) {
+  int64_t n = (int64_t)nz * g.nelem;
+  k_gf_eval<<<nblocks(n, 128), 128, 0, st>>>(g, nz, z, G);
+}
+
+__global__ void k_gf_assemble(ClusterDims cd, int nz, const double2* Graw, double2* Glso) {
+  const int N = cd.N, NN = N * N;
+  const int nel = cd.Nlat * cd.Nlat * cd.Nspin * cd.Norb * cd.Norb;
+  const int64_t n = (int64_t)nz * NN;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(t / NN);
+    const int ab = (int)(t % NN);
+    const int a = ab % N, b = ab / N;
+    // lso a = io + il*Norb + is*Norb*Nlat (VCA_AUX_FUNX.f90:261-262)
+    const int io = a % cd.Norb, il = (a / cd.Norb) % cd.Nlat, is = a / (cd.Norb * cd.Nlat);
+    const int jo = b % cd.Norb, jl = (b / cd.Norb) % cd.Nlat, js = b / (cd.Norb * cd.Nlat);
+    double2 out = make_double2(0.0, 0.0);
+    if (is == js) {
+      auto E = [&](int i1, int j1, int o1, int p1) {
+        return i1 + cd.Nlat * (j1 + cd.Nlat * (is + cd.Nspin * (o1 + cd.Norb * p1)));
+      };
+      const double2* G = Graw + (int64_t)q * nel;
+      double2 g = G[E(il, jl, io, jo)];
+      if (il == jl && io == jo) {
+        out = g;
+      } else {
+        double2 gi = G[E(il, il, io, io)], gj = G[E(jl, jl, jo, jo)];
+        double sr = gi.x + gj.x, si = gi.y + gj.y;
+        // (1 - i*chan4)*(sr + i si) = (sr + chan4*si) + i(si - chan4*sr)
+        const double c4 = (double)cd.chan4;
+        out.x = 0.5 * (g.x - (sr + c4 * si));
+        out.y = 0.5 * (g.y - (si - c4 * sr));
+      }
+    }
+    Glso[t] = out;
+  }
+}
+void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, double2* Glso,
+                        cudaStream_t st) {
+  int64_t n = (int64_t)nz * cd.N * cd.N;
+  k_gf_assemble<<<nblocks(n, 256), 256, 0, st>>>(cd, nz, Graw, Glso);
+}
+
+// ---------------------------------------------------------------------------
+// Omega integrand (sum_kmesh, VCA_OMEGA.f90:37-75): per (w, k) and spin block
+// A = (P_w - Hk_k) G_w, ln|det(1 + A)|.  One warp per (k, block); lane j owns
+// column j (nb <= 32).  ||A||_inf < 1/2: elimination without pivoting with
+// the identity implicit and log1p on the pivots; otherwise partial pivoting.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  double den = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+__global__ void k_omega_ksum(int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
+                             const double2* Hk, double* fpart, int kchunks) {
+  extern __shared__ double2 shm[];
+  const int w = blockIdx.y;
+  const int chunk = blockIdx.x;
+  const int NN = N * N;
+  double2* Gs = shm;            // N*N
+  double2* Ps = shm + NN;       // N*N
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  double2* Aw = shm + 2 * NN + (int64_t)warp * nb * nb;
+  for (int t = threadIdx.x; t < NN; t += blockDim.x) {
+    Gs[t] = Glso[(int64_t)w * NN + t];
+    Ps[t] = P[(int64_t)w * NN + t];
+  }
+  __syncthreads();
+  const int64_t k0 = (Nk * chunk) / kchunks, k1 = (Nk * (chunk + 1)) / kchunks;
+  double acc = 0.0;
+  const int64_t ntask = (k1 - k0) * nblk;
+  for (int64_t task = warp; task < ntask; task += nwarps) {
+    const int64_t k = k0 + task / nblk;
+    const int sb = (int)(task % nblk);
+    const int off = sb * nb;
+    const double2* H = Hk + k * NN;
+    // A(:,j) = sum_l (P - Hk)(off+i, off+l) G(off+l, off+j)
+    if (lane < nb) {
+      const int j = lane;
+      for (int i = 0; i < nb; i++) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int l = 0; l < nb; l++) {
+          const int il = (off + i) + (off + l) * N;
+          double2 mm = make_double2(Ps[il].x - H[il].x, Ps[il].y - H[il].y);
+          double2 gg = Gs[(off + l) + (off + j) * N];
+          s.x = fma(mm.x, gg.x, s.x);
+          s.x = fma(-mm.y, gg.y, s.x);
+          s.y = fma(mm.x, gg.y, s.y);
+          s.y = fma(mm.y, gg.x, s.y);
+        }
+        Aw[i + j * nb] = s;
+      }
+    }
+    __syncwarp();
+    // infinity norm: row sums
+    double rs = 0.0;
+    if (lane < nb)
+      for (int j = 0; j < nb; j++) {
+        double2 a = Aw[lane + j * nb];
+        rs += hypot(a.x, a.y);
+      }
+    for (int o = 16; o > 0; o >>= 1) rs = fmax(rs, __shfl_xor_sync(0xffffffffu, rs, o));
+    double ld = 0.0;
+    if (rs < 0.5) {
+      for (int kk = 0; kk < nb; kk++) {
+        const double2 akk = Aw[kk + kk * nb];
+        const double2 piv = make_double2(1.0 + akk.x, akk.y);
+        ld += 0.5 * log1p(2.0 * akk.x + akk.x * akk.x + akk.y * akk.y);
+        if (lane > kk && lane < nb) Aw[lane + kk * nb] = cdiv(Aw[lane + kk * nb], piv);  // l_i
+        __syncwarp();
+        if (lane > kk && lane < nb) {
+          const int j = lane;
+          const double2 ukj = Aw[kk + j * nb];
+          for (int i = kk + 1; i < nb; i++) {
+            double2 t = cmul(Aw[i + kk * nb], ukj);
+            Aw[i + j * nb].x -= t.x;
+            Aw[i + j * nb].y -= t.y;
+          }
+        }
+        __syncwarp();
+      }
+    } else {
+      if (lane < nb) Aw[lane + lane * nb].x += 1.0;
+      __syncwarp();
+      for (int kk = 0; kk < nb; kk++) {
+        double mag = -1.0;
+        int arg = kk;
+        if (lane >= kk && lane < nb) { double2 a = Aw[lane + kk * nb]; mag = hypot(a.x, a.y); arg = lane; }
+        for (int o = 16; o > 0; o >>= 1) {
+          double om = __shfl_xor_sync(0xffffffffu, mag, o);
+          int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+          if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
+        }
+        if (mag == 0.0) { ld = -INFINITY; break; }
+        if (arg != kk && lane < nb) {  // swap rows kk and arg in column `lane`
+          double2 t = Aw[kk + lane * nb];
+          Aw[kk + lane * nb] = Aw[arg + lane * nb];
+          Aw[arg + lane * nb] = t;
+        }
+        __syncwarp();
+        const double2 piv = Aw[kk + kk * nb];
+        ld += log(hypot(piv.x, piv.y));
+        if (lane > kk && lane < nb) Aw[lane + kk * nb] = cdiv(Aw[lane + kk * nb], piv);
+        __syncwarp();
+        if (lane > kk && lane < nb) {
+          const int j = lane;
+          const double2 ukj = Aw[kk + j * nb];
+          for (int i = kk + 1; i < nb; i++) {
+            double2 t = cmul(Aw[i + kk * nb], ukj);
+            Aw[i + j * nb].x -= t.x;
+            Aw[i + j * nb].y -= t.y;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (lane == 0) acc += ld;
+    __syncwarp();
+  }
+  // block reduce of the per-warp sums (lane 0 of each warp)
+  __shared__ double red[32];
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < nwarps; q++) s += red[q];
+    fpart[(int64_t)w * kchunks + chunk] = s;
+  }
+}
+void launch_omega_ksum(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso,
+                       int64_t Nk, const double2* Hk, double* fpart, int kchunks, cudaStream_t st) {
+  const int threads = 128;
+  size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
+  if (shm > 48 * 1024)
+    cudaFuncSetAttribute(k_omega_ksum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  dim3 grd(kchunks, nw, 1);
+  k_omega_ksum<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, fpart, kchunks);
+}
+
+__global__ void k_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < ncols; c++) s += in[(int64_t)r * ncols + c];
+    out[r] = s * scale;
+  }
+}
+void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out,
+                        cudaStream_t st) {
+  k_reduce_rows<<<nblocks(nrows, 128), 128, 0, st>>>(nrows, ncols, in, scale, out);
+}
+
+// Gauss-Legendre nodes/weights on (0,1): Newton on P_n from
+// cos(pi (i+3/4)/(n+1/2)), ascending nodes.
+__global__ void k_gauss_legendre(int n, double* x, double* w) {
+  const int half = (n + 1) / 2;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < half; i += gridDim.x * blockDim.x) {
+    double z = cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0.0;
+    for (int it = 0; it < 100; it++) {
+      double p1 = 1.0, p2 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      double z1 = z;
+      z = z1 - p1 / pp;
+      if (fabs(z - z1) < 1e-16) {
+        p1 = 1.0;
+        p2 = 0.0;
+        for (int j = 1; j <= n; j++) {
+          double p3 = p2;
+          p2 = p1;
+          p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+        }
+        pp = n * (z * p1 - p2) / (z * z - 1.0);
+        break;
+      }
+    }
+    double wt = 2.0 / ((1.0 - z * z) * pp * pp);
+    x[i] = 0.5 * (1.0 - z);
+    x[n - 1 - i] = 0.5 * (1.0 + z);
+    w[i] = 0.5 * wt;
+    w[n - 1 - i] = 0.5 * wt;
+  }
+}
+void launch_gauss_legendre(int n, double* x, double* w, cudaStream_t st) {
+  k_gauss_legendre<<<nblocks((n + 1) / 2, 128), 128, 0, st>>>(n, x, w);
+}
+
+// Delta_bath(z) = V [(z+xmu) - h]^{-1} V^dag (VCA_BATH_FUNCTIONS.f90:127-150);
+// one thread per z, Gauss-Jordan with partial pivoting in `work`
+// (2*Nb*Nb complex per z).  hb, V in lso layout (Nb x Nb, N x Nb).
+__global__ void k_delta_bath(int nz, const double2* z, int N, int Nb, const double2* hb, const double2* V,
+                             double xmu, double2* work, double2* out) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nz; q += gridDim.x * blockDim.x) {
+    double2* M = work + (int64_t)q * 2 * Nb * Nb;
+    double2* I = M + Nb * Nb;
+    for (int i = 0; i < Nb; i++)
+      for (int j = 0; j < Nb; j++) {
+        double2 h = hb[i + j * Nb];
+        M[i + j * Nb] = make_double2(-h.x, -h.y);
+        I[i + j * Nb] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+      }
+    for (int i = 0; i < Nb; i++) { M[i + i * Nb].x += z[q].x + xmu; M[i + i * Nb].y += z[q].y; }
+    for (int k = 0; k < Nb; k++) {
+      int p = k;
+      double best = hypot(M[k + k * Nb].x, M[k + k * Nb].y);
+      for (int i = k + 1; i < Nb; i++) {
+        double mg = hypot(M[i + k * Nb].x, M[i + k * Nb].y);
+        if (mg > best) { best = mg; p = i; }
+      }
+      if (p != k)
+        for (int j = 0; j < Nb; j++) {
+          double2 t = M[k + j * Nb]; M[k + j * Nb] = M[p + j * Nb]; M[p + j * Nb] = t;
+          t = I[k + j * Nb]; I[k + j * Nb] = I[p + j * Nb]; I[p + j * Nb] = t;
+        }
+      double2 piv = M[k + k * Nb];
+      for (int j = 0; j < Nb; j++) { M[k + j * Nb] = cdiv(M[k + j * Nb], piv); I[k + j * Nb] = cdiv(I[k + j * Nb], piv); }
+      for (int i = 0; i < Nb; i++) {
+        if (i == k) continue;
+        double2 f = M[i + k * Nb];
+        if (f.x == 0.0 && f.y == 0.0) continue;
+        for (int j = 0; j < Nb; j++) {
+          double2 t = cmul(f, M[k + j * Nb]);
+          M[i + j * Nb].x -= t.x; M[i + j * Nb].y -= t.y;
+          t = cmul(f, I[k + j * Nb]);
+          I[i + j * Nb].x -= t.x; I[i + j * Nb].y -= t.y;
+        }
+      }
+    }
+    // out = V * I * V^dag
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int a = 0; a < Nb; a++) {
+          double2 va = V[i + a * N];
+          for (int b = 0; b < Nb; b++) {
+            double2 vb = V[j + b * N];
+            double2 t = cmul(va, I[a + b * Nb]);
+            s.x += t.x * vb.x + t.y * vb.y;  // t * conj(vb)
+            s.y += t.y * vb.x - t.x * vb.y;
+          }
+        }
+        out[(int64_t)q * N * N + i + j * N] = s;
+      }
+  }
+}
+void launch_delta_bath(int nz, const double2* z, int N, int Nb, const double2* hb, const double2* V,
+                       double xmu, double2* work, double2* out, cudaStream_t st) {
+  k_delta_bath<<<nblocks(nz, 64), 64, 0, st>>>(nz, z, N, Nb, hb, V, xmu, work, out);
+}
+
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+// chain start-vector norms: invnorm = 1/sqrt(norm2); a zero-norm chain is
+// retired with no excitations (the reference would divide by zero).
+__global__ void k_chain_norm_init(int nch, ChainMeta* meta, const double* norm2, double* invnorm) {
+  for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
+    double n2 = norm2[ch];
+    if (n2 > 0.0) {
+      invnorm[ch] = 1.0 / sqrt(n2);
+    } else {
+      invnorm[ch] = 0.0;
+      meta[ch].active = 0;
+      meta[ch].len = 0;
+    }
+  }
+}
+void launch_chain_norm_init(int nch, ChainMeta* meta, const double* norm2, double* invnorm,
+                            cudaStream_t st) {
+  k_chain_norm_init<<<nblocks(nch, 128), 128, 0, st>>>(nch, meta, norm2, invnorm);
+}
+__global__ void k_recip(int n, const double* in, double* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = (in[i] != 0.0) ? 1.0 / in[i] : 0.0;
+}
+void launch_recip(int n, const double* in, double* out, cudaStream_t st) {
+  k_recip<<<nblocks(n, 128), 128, 0, st>>>(n, in, out);
+}
+// (Nlat,Nlat,Nspin,Nspin,Norb,Norb[,L]) -> lso N x N per slice (VCA_AUX_FUNX.f90:255-279)
+__global__ void k_nnn2lso(int Nlat, int Nspin, int Norb, int64_t L, const double2* in, double2* out) {
+  const int N = Nlat * Nspin * Norb;
+  const int64_t NN = (int64_t)N * N;
+  const int64_t n = NN * L;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = t / NN;
+    const int ab = (int)(t % NN);
+    const int a = ab % N, b = ab / N;
+    const int io = a % Norb, il = (a / Norb) % Nlat, is = a / (Norb * Nlat);
+    const int jo = b % Norb, jl = (b / Norb) % Nlat, js = b / (Norb * Nlat);
+    const int64_t src = il + (int64_t)Nlat * (jl + (int64_t)Nlat * (is + (int64_t)Nspin *
+                        (js + (int64_t)Nspin * (io + (int64_t)Norb * jo))));
+    out[t] = in[l * NN + src];
+  }
+}
+void launch_nnn2lso(int Nlat, int Nspin, int Norb, int64_t L, const double2* in, double2* out,
+                    cudaStream_t st) {
+  const int N = Nlat * Nspin * Norb;
+  k_nnn2lso<<<nblocks((int64_t)N * N * L, 256), 256, 0, st>>>(Nlat, Nspin, Norb, L, in, out);
+}
+// P[w] = D[w] + H (lso), or H alone when D == nullptr
+__global__ void k_add_hloc(int nw, int NN, const double2* D, const double2* H, double2* P) {
+  const int64_t n = (int64_t)nw * NN;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    double2 h = H[t % NN];
+    if (D) { h.x += D[t].x; h.y += D[t].y; }
+    P[t] = h;
+  }
+}
+void launch_add_hloc(int nw, int NN, const double2* D, const double2* H, double2* P, cudaStream_t st) {
+  k_add_hloc<<<nblocks((int64_t)nw * NN, 256), 256, 0, st>>>(nw, NN, D, H, P);
+}
+// omega nodes: z = i*scale*s/(1-s), W = w*scale/(1-s)^2
+__global__ void k_omega_nodes(int n, double scale, const double* s, const double* w, double2* z,
+                              double* W) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double om = 1.0 - s[i];
+    z[i] = make_double2(0.0, scale * s[i] / om);
+    W[i] = w[i] * scale / (om * om);
+  }
+}
+void launch_omega_nodes(int n, double scale, const double* s, const double* w, double2* z, double* W,
+                        cudaStream_t st) {
+  k_omega_nodes<<<nblocks(n, 128), 128, 0, st>>>(n, scale, s, w, z, W);
+}
+// deterministic weighted sum: out = sum_i a[i]*b[i] (single block)
+__global__ void k_wsum(int n, const double* a, const double* b, double* out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(a[i], b[i], s);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+void launch_wsum(int n, const double* a, const double* b, double* out, cudaStream_t st) {
+  k_wsum<<<1, 256, 0, st>>>(n, a, b, out);
+}
+// complex start vector (real values, zero imaginary part)
+__global__ void k_real_to_cplx(int64_t n, const double* in, double2* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(in[i], 0.0);
+}
+void launch_real_to_cplx(int64_t n, const double* in, double2* out, cudaStream_t st) {
+  k_real_to_cplx<<<nblocks(n, 256), 256, 0, st>>>(n, in, out);
+}
+
+}  // namespace vca

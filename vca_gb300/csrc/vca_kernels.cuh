@@ -1,0 +1,143 @@
+// vca_kernels.cuh -- host-callable launchers of the sm_103a kernels.
+#pragma once
+
+#include "vca_common.cuh"
+
+namespace vca {
+
+// ---- Fock basis (VCA_SETUP.f90:660-695, 724-750) ---------------------------
+void set_binomials(int Ns, cudaStream_t st);
+void launch_build_words(int Ns, int n, int dim, int* words, cudaStream_t st);
+
+struct HopPair {     // amplitude of c^dag_i c_j for one spin (i != j), 0-based bits
+  int i, j;
+  double re, im;
+};
+struct E1Params {    // one-body + same-spin diagonal energy of a spin word
+  double2 eps[VCA_MAX_NS];   // per-level energy (incl. -xmu and Hartree shifts)
+  double2 cst;               // constant added once (carried by the up word)
+  double upar;               // (Ust - Jh), same site, parallel spins
+  int norb;
+  unsigned int omask[VCA_MAX_NORB];
+};
+// count hops per target word and return the ELL width (max count)
+int launch_hop_count(int Ns, int n, int dim, const int* words, const HopPair* d_pairs, int npairs,
+                     int* cnt, int* d_scratch_max, cudaStream_t st);
+void launch_hop_fill(int Ns, int n, int dim, int width, const int* words, const HopPair* d_pairs,
+                     int npairs, int* src, double2* amp, cudaStream_t st);
+void launch_e1(int dim, const int* words, const E1Params& p, bool with_const, double2* e1,
+               cudaStream_t st);
+
+// ---- H x v on column batches (VCA_HAMILTONIAN_SPARSE_HxV.f90:152-200) -----
+// real Hamiltonian, m real columns
+void launch_hxv_real(const SectorView& sv, const MixedDiag& md, int m, const double* X, double* Y,
+                     cudaStream_t st);
+// complex Hamiltonian, m complex columns
+void launch_hxv_cplx(const SectorView& sv, const MixedDiag& md, int m, const double2* X, double2* Y,
+                     cudaStream_t st);
+
+// ---- Lanczos vector operations on column batches --------------------------
+// Work arrays: partial[nblk*m] (double2), chain arrays of length nch.
+struct ColBatch {
+  int64_t rows;     // sector dimension
+  int m;            // columns (real doubles, or double2 when cplx)
+  bool cplx;        // double2 columns
+  int nch;          // chains
+  const int* col2ch;  // [m]
+  const ChainMeta* meta;  // [nch] device
+};
+// per-column dot: out_col[c] = sum_i conj(X)Y (real part used) ; deterministic
+void launch_col_dot(const ColBatch& b, const void* X, const void* Y, double* partial, int nblk,
+                    double* out_col, cudaStream_t st);
+// Y -= coef[ch(c)] * X  for active chains
+void launch_col_axpy(const ColBatch& b, const double* coef, const void* X, void* Y, bool negate,
+                     cudaStream_t st);
+// X = Y * scale[ch(c)] for active chains
+void launch_col_scale(const ColBatch& b, const double* scale, const void* Y, void* X, cudaStream_t st);
+// sum columns of each chain: out_ch[ch] = sum_{c in ch} in_col[c]
+void launch_chain_sum(const ColBatch& b, const double* in_col, double* out_ch, cudaStream_t st);
+// after alpha/beta^2 of step k are known: record, deactivate exhausted chains,
+// produce 1/beta for the scale.  alpha/beta stored [ch*ldab + k-1].
+void launch_lanczos_record(int nch, ChainMeta* meta, int k, const double* alpha_ch,
+                           const double* beta2_ch, double* A, double* Bt, int ldab, double tol,
+                           double* invbeta, double* beta_now, cudaStream_t st);
+// psi += s[k] * X (single column batch of the GS second pass)
+void launch_psi_accum(int64_t n, bool cplx, const double* s, int k, const void* X, void* psi,
+                      cudaStream_t st);
+// deterministic start vector (splitmix64) for the GS Lanczos
+void launch_start_vector(int64_t n, uint64_t seed, int isector, double* X, cudaStream_t st);
+void launch_fill(int64_t n, double v, double* X, cudaStream_t st);
+
+// ---- tridiagonal problems --------------------------------------------------
+// lowest eigenpair of T_k (a[0..k-1], b = beta_{2..k}), residual test;
+// writes theta, s[0..k-1] and flag (1 = converged)
+void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta,
+                       double* s, double* resid, cudaStream_t st);
+// chains -> poles/weights (add_to_lanczos_gf_normal, VCA_GF_NORMAL.f90:970-1033)
+void launch_chain_poles(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
+                        const double* norm2, const double2* wfac, const int* isign, double Ei,
+                        double zeta, double* work, double* poles, double2* weights, int* nexc,
+                        cudaStream_t st);
+
+// ---- chain initial vectors (VCA_GF_NORMAL.f90:179-197, :251-268, :608-646) -
+struct OpTerm {
+  int pos;          // 0-based bit
+  double re, im;    // coefficient
+};
+struct ChainInit {
+  int spin;         // 0 up, 1 down
+  int dag;          // 1 = c^dag (particle), 0 = c (hole)
+  int nterm;
+  OpTerm t[2];
+  int col0;         // first column of the chain
+  int cplxcol;      // real-H batch: 1 when the chain owns (re,im) columns
+};
+// X (target sector tgt, m columns) from the ground state gs (source sector,
+// its up dimension src_dimup): one thread per (target row, chain)
+void launch_chain_init(const SectorView& tgt, int src_dimup, const void* gs, bool gs_cplx,
+                       int nchain, const ChainInit* d_ci, int m, bool cols_cplx, void* X,
+                       cudaStream_t st);
+
+// ---- Green's function and Omega (VCA_IO/gf_cluster.f90, VCA_OMEGA.f90) ---
+struct GfLayout {
+  int nelem;              // spin-diagonal elements (il,jl,is,io,jo)
+  const int* elem_ptr;    // [nelem+1] chains per element (CSR)
+  const int* elem_chain;  // chain ids
+  const int* nexc;        // [nch] poles per chain
+  const double* poles;    // [nch*ld]
+  const double2* weights; // [nch*ld]
+  int ld;
+};
+// raw element sums at nz points z (complex): G[z*nelem + e]
+void launch_gf_eval(const GfLayout& g, int nz, const double2* z, double2* G, cudaStream_t st);
+// recombination + lso assembly: Glso[z][N*N] from raw G
+struct ClusterDims {
+  int Nlat, Norb, Nspin, N;
+  int chan4;  // 1 when VCA_GF_SYMMETRIC=F
+};
+void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, double2* Glso,
+                        cudaStream_t st);
+// Omega integrand: f[w] = (1/Lk) sum_k ln|det(1 + (P_w - Hk_k) G_w)| per spin block
+void launch_omega_ksum(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso,
+                       int64_t Nk, const double2* Hk, double* fpart, int kchunks, cudaStream_t st);
+void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out,
+                        cudaStream_t st);
+// Gauss-Legendre nodes on (0,1)
+void launch_gauss_legendre(int n, double* x, double* w, cudaStream_t st);
+// Delta_bath(z) (VCA_BATH_FUNCTIONS.f90:127-150) for nz points, lso N x N
+void launch_delta_bath(int nz, const double2* z, int N, int Nb, const double2* hb, const double2* V,
+                       double xmu, double2* work, double2* out, cudaStream_t st);
+
+// ---- helpers ---------------------------------------------------------------
+void launch_chain_norm_init(int nch, ChainMeta* meta, const double* norm2, double* invnorm,
+                            cudaStream_t st);
+void launch_recip(int n, const double* in, double* out, cudaStream_t st);
+void launch_nnn2lso(int Nlat, int Nspin, int Norb, int64_t L, const double2* in, double2* out,
+                    cudaStream_t st);
+void launch_add_hloc(int nw, int NN, const double2* D, const double2* H, double2* P, cudaStream_t st);
+void launch_omega_nodes(int n, double scale, const double* s, const double* w, double2* z, double* W,
+                        cudaStream_t st);
+void launch_wsum(int n, const double* a, const double* b, double* out, cudaStream_t st);
+void launch_real_to_cplx(int64_t n, const double* in, double2* out, cudaStream_t st);
+
+}  // namespace vca

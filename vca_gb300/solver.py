@@ -1,0 +1,284 @@
+"""Python mirror of the reference's VCA module over the C-ABI.
+
+The names follow ``VCA.f90:1-38`` / ``VCA_MAIN.f90:21-39`` of QcmPlab/VCA:
+``vca_init_solver``, ``vca_solve``, ``vca_get_sft_potential``,
+``vca_gf_cluster``, ``vca_get_gimp_matsubara``, ``vca_get_gimp_realaxis``.
+Arrays are Fortran-ordered complex128 with the reference's shapes.  Errors the
+reference turns into ``stop "..."`` raise :class:`VcaError` with the library's
+message.  There is no CPU fallback: if ``libvca_gpu.so`` is missing or no GPU
+is visible the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+from .config import VcaConfig, hloc_shape, bath_h_shape, bath_v_shape
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "libvca_gpu.so")
+_lib = None
+
+# exported symbols of include/vca_gpu.h
+EXPORTS = [
+    "vca_config_defaults", "vca_gpu_init", "vca_gpu_solve", "vca_gpu_solve_batch",
+    "vca_gpu_get_sft_potential", "vca_gpu_get_energies", "vca_gpu_gf_cluster",
+    "vca_gpu_get_gimp_matsubara", "vca_gpu_get_gimp_realaxis", "vca_gpu_get_state_count",
+    "vca_gpu_get_state", "vca_gpu_get_sector_energies", "vca_gpu_get_gf_channel",
+    "vca_gpu_sum_kmesh", "vca_gpu_finalize", "vca_gpu_last_error", "vca_gpu_sector_info",
+    "vca_gpu_sector_map", "vca_gpu_set_hamiltonian", "vca_gpu_hxv", "vca_gpu_hxv_device",
+    "vca_gpu_hxv_timed",
+]
+
+
+class VcaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def load(path: Optional[str] = None):
+    """Load the C-ABI library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIBPATH
+    if not os.path.exists(p):
+        raise VcaError(-4, f"{p} is missing: run vca_gb300.build.build() (no CPU fallback)")
+    L = ctypes.CDLL(p)
+    dp = ctypes.POINTER(ctypes.c_double)
+    i32, i64 = ctypes.c_int32, ctypes.c_int64
+    vp = ctypes.c_void_p
+    cfgp = ctypes.POINTER(VcaConfig)
+    sig = {
+        "vca_config_defaults": (None, [cfgp]),
+        "vca_gpu_init": (ctypes.c_int, [cfgp, dp, dp]),
+        "vca_gpu_solve": (ctypes.c_int, [dp, dp, i64, dp, dp, dp]),
+        "vca_gpu_solve_batch": (ctypes.c_int, [i32, dp, i64, dp, i64, dp, i64, dp, i64, dp]),
+        "vca_gpu_get_sft_potential": (ctypes.c_int, [dp]),
+        "vca_gpu_get_energies": (ctypes.c_int, [dp, dp]),
+        "vca_gpu_gf_cluster": (ctypes.c_int, [dp, i64, dp]),
+        "vca_gpu_get_gimp_matsubara": (ctypes.c_int, [dp]),
+        "vca_gpu_get_gimp_realaxis": (ctypes.c_int, [dp]),
+        "vca_gpu_get_state_count": (ctypes.c_int, [ctypes.POINTER(i32)]),
+        "vca_gpu_get_state": (ctypes.c_int, [i32, ctypes.POINTER(i32), dp]),
+        "vca_gpu_get_sector_energies": (ctypes.c_int, [dp, i32]),
+        "vca_gpu_get_gf_channel": (ctypes.c_int, [i32, i32, i32, i32, i32, i32, i32,
+                                                  ctypes.POINTER(i32), dp, dp, i32]),
+        "vca_gpu_sum_kmesh": (ctypes.c_int, [dp, i64, dp]),
+        "vca_gpu_finalize": (ctypes.c_int, []),
+        "vca_gpu_last_error": (ctypes.c_int, [ctypes.c_char_p, i32]),
+        "vca_gpu_sector_info": (ctypes.c_int, [i32, ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                               ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+        "vca_gpu_sector_map": (ctypes.c_int, [i32, i32, ctypes.POINTER(i64), i64]),
+        "vca_gpu_set_hamiltonian": (ctypes.c_int, [dp, dp, dp]),
+        "vca_gpu_hxv": (ctypes.c_int, [i32, dp, dp]),
+        "vca_gpu_hxv_device": (ctypes.c_int, [i32, vp, vp, i32]),
+        "vca_gpu_hxv_timed": (ctypes.c_int, [i32, vp, vp, i32, i32, dp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _c128(a, shape=None, name="array"):
+    if a is None:
+        return None
+    a = np.asfortranarray(a, dtype=np.complex128)
+    if shape is not None and tuple(a.shape) != tuple(shape):
+        raise VcaError(-2, f"{name} has shape {a.shape}, expected {tuple(shape)}")
+    return a
+
+
+def check(rc: int):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(1024)
+        load().vca_gpu_last_error(buf, 1024)
+        raise VcaError(rc, buf.value.decode(errors="replace"))
+
+
+def library_defaults() -> VcaConfig:
+    c = VcaConfig()
+    load().vca_config_defaults(ctypes.byref(c))
+    return c
+
+
+class VcaSolver:
+    """One solver context (the library keeps one global context, as the
+    reference keeps module globals)."""
+
+    def __init__(self, cfg: VcaConfig, bath_h=None, bath_v=None):
+        self.L = load()
+        self.cfg = cfg.copy()
+        self.has_bath = bath_h is not None
+        if self.has_bath:
+            bath_h = _c128(bath_h, bath_h_shape(cfg), "bath_h")
+            bath_v = _c128(bath_v, bath_v_shape(cfg), "bath_v")
+        else:
+            self.cfg.Nlat_bath = 0
+            self.cfg.Norb_bath = 0
+        check(self.L.vca_gpu_init(ctypes.byref(self.cfg), _dp(bath_h), _dp(bath_v)))
+
+    # ---- vca_solve -----------------------------------------------------
+    def solve(self, Hloc, Hk, bath_h=None, bath_v=None) -> float:
+        c = self.cfg
+        Hloc = _c128(Hloc, hloc_shape(c), "Hloc")
+        Hk = _c128(Hk, None, "Hk")
+        if Hk.shape[:6] != hloc_shape(c) or Hk.ndim != 7:
+            raise VcaError(-2, f"Hk has shape {Hk.shape}, expected {hloc_shape(c)} + (Nk,)")
+        if bath_h is not None:
+            bath_h = _c128(bath_h, bath_h_shape(c), "bath_h")
+            bath_v = _c128(bath_v, bath_v_shape(c), "bath_v")
+        out = ctypes.c_double()
+        check(self.L.vca_gpu_solve(_dp(Hloc), _dp(Hk), Hk.shape[6], _dp(bath_h), _dp(bath_v),
+                                   ctypes.byref(out)))
+        return out.value
+
+    def solve_batch(self, Hloc_b, Hk, bath_h_b=None, bath_v_b=None) -> np.ndarray:
+        c = self.cfg
+        Hloc_b = np.asfortranarray(Hloc_b, dtype=np.complex128)
+        B = Hloc_b.shape[-1]
+        Hk = _c128(Hk)
+        out = np.zeros(B)
+        n_h = int(np.prod(hloc_shape(c)))
+        bh = np.asfortranarray(bath_h_b, dtype=np.complex128) if bath_h_b is not None else None
+        bv = np.asfortranarray(bath_v_b, dtype=np.complex128) if bath_v_b is not None else None
+        check(self.L.vca_gpu_solve_batch(B, _dp(Hloc_b), n_h, _dp(Hk), Hk.shape[6],
+                                         _dp(bh), int(np.prod(bath_h_shape(c))) if bh is not None else 0,
+                                         _dp(bv), int(np.prod(bath_v_shape(c))) if bv is not None else 0,
+                                         _dp(out)))
+        return out
+
+    def get_sft_potential(self) -> float:
+        out = ctypes.c_double()
+        check(self.L.vca_gpu_get_sft_potential(ctypes.byref(out)))
+        return out.value
+
+    def energies(self):
+        egs, oi = ctypes.c_double(), ctypes.c_double()
+        check(self.L.vca_gpu_get_energies(ctypes.byref(egs), ctypes.byref(oi)))
+        return egs.value, oi.value
+
+    def states(self):
+        n = ctypes.c_int32()
+        check(self.L.vca_gpu_get_state_count(ctypes.byref(n)))
+        out = []
+        for k in range(1, n.value + 1):
+            s, e = ctypes.c_int32(), ctypes.c_double()
+            check(self.L.vca_gpu_get_state(k, ctypes.byref(s), ctypes.byref(e)))
+            out.append((s.value, e.value))
+        return out
+
+    def sector_energies(self) -> np.ndarray:
+        ns = (self.Ns + 1) ** 2
+        out = np.zeros(ns)
+        check(self.L.vca_gpu_get_sector_energies(_dp(out), ns))
+        return out
+
+    @property
+    def Ns(self) -> int:
+        c = self.cfg
+        return c.Nlat * c.Norb + c.Nlat_bath * c.Norb_bath
+
+    def gf_channel(self, il, jl, ispin, io, jo, istate, ichan, cap=4096):
+        n = ctypes.c_int32()
+        p = np.zeros(cap, dtype=np.complex128)
+        w = np.zeros(cap, dtype=np.complex128)
+        check(self.L.vca_gpu_get_gf_channel(il, jl, ispin, io, jo, istate, ichan, ctypes.byref(n),
+                                            _dp(p), _dp(w), cap))
+        return p[: n.value], w[: n.value]
+
+    def gf_cluster(self, z) -> np.ndarray:
+        z = np.ascontiguousarray(np.atleast_1d(z), dtype=np.complex128)
+        c = self.cfg
+        out = np.zeros(hloc_shape(c) + (len(z),), dtype=np.complex128, order="F")
+        check(self.L.vca_gpu_gf_cluster(_dp(z), len(z), _dp(out)))
+        return out
+
+    def gimp_matsubara(self) -> np.ndarray:
+        out = np.zeros(hloc_shape(self.cfg) + (self.cfg.Lmats,), dtype=np.complex128, order="F")
+        check(self.L.vca_gpu_get_gimp_matsubara(_dp(out)))
+        return out
+
+    def gimp_realaxis(self) -> np.ndarray:
+        out = np.zeros(hloc_shape(self.cfg) + (self.cfg.Lreal,), dtype=np.complex128, order="F")
+        check(self.L.vca_gpu_get_gimp_realaxis(_dp(out)))
+        return out
+
+    def sum_kmesh(self, w) -> np.ndarray:
+        w = np.ascontiguousarray(np.atleast_1d(w), dtype=np.float64)
+        out = np.zeros(len(w))
+        check(self.L.vca_gpu_sum_kmesh(_dp(w), len(w), _dp(out)))
+        return out
+
+    # ---- parity hooks ------------------------------------------------------
+    def sector_info(self, isector):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        du, dd = ctypes.c_int64(), ctypes.c_int64()
+        check(self.L.vca_gpu_sector_info(isector, ctypes.byref(a), ctypes.byref(b), ctypes.byref(du),
+                                         ctypes.byref(dd)))
+        return a.value, b.value, du.value, dd.value
+
+    def sector_map(self, isector, spin) -> np.ndarray:
+        _, _, du, dd = self.sector_info(isector)
+        n = du if spin == 1 else dd
+        out = np.zeros(n, dtype=np.int64)
+        check(self.L.vca_gpu_sector_map(isector, spin, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n))
+        return out
+
+    def set_hamiltonian(self, Hloc, bath_h=None, bath_v=None):
+        c = self.cfg
+        Hloc = _c128(Hloc, hloc_shape(c), "Hloc")
+        if bath_h is not None:
+            bath_h = _c128(bath_h, bath_h_shape(c), "bath_h")
+            bath_v = _c128(bath_v, bath_v_shape(c), "bath_v")
+        check(self.L.vca_gpu_set_hamiltonian(_dp(Hloc), _dp(bath_h), _dp(bath_v)))
+
+    def hxv(self, isector, v) -> np.ndarray:
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        hv = np.zeros_like(v)
+        check(self.L.vca_gpu_hxv(isector, _dp(v), _dp(hv)))
+        return hv
+
+    def close(self):
+        self.L.vca_gpu_finalize()
+
+
+# ---- functional interface with the reference's names ---------------------
+_solver: Optional[VcaSolver] = None
+
+
+def vca_init_solver(cfg: VcaConfig, bath_h=None, bath_v=None) -> VcaSolver:
+    """vca_init_solver (VCA_MAIN.f90:51-76)."""
+    global _solver
+    _solver = VcaSolver(cfg, bath_h, bath_v)
+    return _solver
+
+
+def vca_solve(Hloc, Hk, bath_h=None, bath_v=None) -> float:
+    """vca_solve (VCA_MAIN.f90:124-215): returns the SFT potential."""
+    if _solver is None:
+        raise VcaError(-3, "vca_init_solver has not been called")
+    return _solver.solve(Hloc, Hk, bath_h, bath_v)
+
+
+def vca_get_sft_potential() -> float:
+    if _solver is None:
+        raise VcaError(-3, "vca_init_solver has not been called")
+    return _solver.get_sft_potential()
+
+
+def vca_gf_cluster(z) -> np.ndarray:
+    if _solver is None:
+        raise VcaError(-3, "vca_init_solver has not been called")
+    return _solver.gf_cluster(z)
