@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Omega evaluations per second of the GB300 cluster-ED path.
+
+Workload: the 4x3 square Hubbard cluster (Ns=12, Nspin=2, U=8, xmu=4) with a
+variational antiferromagnetic Weiss field M swept over 16 points in [0, 0.3],
+a 32x32 k-grid in the reduced zone, 200-step Green's function chains for every
+site and spin, and the Potthoff Omega integrated on the imaginary axis with an
+8192-node rule.  One step = one full vca_solve (all 169 sectors diagonalised,
+all chains, Omega) at the next M of the sweep.  Synthetic inputs restated from
+the reference's square-lattice driver recipe (no dataset exists).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` = Omega evals/s with Hk resident in HBM (CUDA events on the library
+stream); `e2e` = the same through vca_gpu_solve with host buffers (Hk and Hloc
+copied in, Omega copied out every step).  N > 1 (torchrun) runs independent
+replicas over different M (weak scaling, no data-path collective).
+`--impl reference` times the CPU restatement of the reference path on the
+host cores (the Fortran reference does not build on this image).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Omega evals/sec (plain GPU path, |dOmega|<=1e-10 vs FP64 oracle)"
+UNIT = "Omega evals/s"
+WORKLOAD = ("square4x3 Hubbard U=8 Nspin=2, M_AF sweep 16 pts [0,0.3], 32x32 k-grid, "
+            "200-step GF chains (chan4), 8192-node Omega rule")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name: str):
+    """dram bytes per launch recorded in a committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_points():
+    import numpy as np
+    from vca_gb300 import clusters
+    ms = np.linspace(0.0, 0.3, 16)
+    return [clusters.square(nx=4, ny=3, U=8.0, xmu=4.0, maf=float(m), nspin=2, nkx=32, nky=32,
+                            ngfiter=200, omega_nodes=8192) for m in ms]
+
+
+# ---------------------------------------------------------------------------
+# CPU timing of the oracle on a bounded sample of one Omega evaluation
+# ---------------------------------------------------------------------------
+def cpu_sample(pt, threads: int):
+    import numpy as np
+    from oracle import oracle as orc
+    from oracle.oracle import Oracle
+    orc.set_threads(threads)
+    o = Oracle.from_point(pt)
+    Ns = o.Ns
+    big = 1 + 6 + 6 * (Ns + 1)         # sector (6,6), dim 853,776
+    tgt = 1 + 6 + 7 * (Ns + 1)         # GF target sector (7,6), dim 731,808
+    t0 = time.perf_counter()
+    e, psi, iters = o.lanczos_gs(big)
+    t_gs = time.perf_counter() - t0
+    dims = [o.dim(s) for s in range(1, o.Nsectors + 1)]
+    gs_total = t_gs * sum(dims) / dims[big - 1]
+    d = o.dim(tgt)
+    rng = np.random.default_rng(1)
+    v = rng.normal(size=d) + 0j
+    v /= np.linalg.norm(v)
+    nch = 2
+    t0 = time.perf_counter()
+    for _ in range(nch):
+        o.lanczos_tridiag(tgt, v, 200)
+    t_chain = (time.perf_counter() - t0) / nch
+    L = pt.cfg.Nlat * pt.cfg.Norb
+    chains = pt.cfg.Nspin * (2 * L + 4 * L * (L - 1))
+    nn = 8
+    t0 = time.perf_counter()
+    for w in np.linspace(0.1, 5.0, nn):
+        o.sum_kmesh(float(w))
+    t_node = (time.perf_counter() - t0) / nn
+    total = gs_total + chains * t_chain + pt.cfg.omega_nodes * t_node
+    sample = (f"oracle (C++/OpenMP restatement) timed on: GS Lanczos of sector (6,6) "
+              f"[{iters} its, {t_gs:.2f}s] scaled by total/largest sector dim; {nch} of {chains} "
+              f"200-step chains on sector (7,6) [{t_chain:.2f}s each]; {nn} of 8192 Omega nodes "
+              f"[{t_node * 1e3:.1f}ms each]; one eval estimated at {total:.0f}s")
+    return 1.0 / total, sample, total
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    pts = build_points()
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, sample, tot = cpu_sample(pts[s % len(pts)], threads)
+        if s >= args.warmup:
+            vals.append(v)
+    value = sum(vals) / len(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import numpy as np
+    from vca_gb300 import build as vbuild
+    vbuild.build()
+    from vca_gb300.solver import VcaSolver
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def allmax(x: float) -> float:
+        if dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    pts = build_points()
+    mine = pts[rank::world] if world > 1 else pts
+    s = VcaSolver(mine[0].cfg)
+    s.upload_hk(mine[0].Hk)
+    for i in range(args.warmup):
+        s.solve_resident(mine[i % len(mine)].Hloc)
+    stage_ms = s.timings().tolist()
+    # ---- value: Hk resident, device time on the library stream ----------
+    clocks = ClockSampler(0 if world > 1 else local)
+    barrier()
+    s.synchronize()
+    l0 = s.kernel_launches()
+    s.timer_start()
+    omegas = []
+    for i in range(args.steps):
+        omegas.append(s.solve_resident(mine[(args.warmup + i) % len(mine)].Hloc))
+    ms = s.timer_stop()
+    launches = s.kernel_launches() - l0
+    barrier()
+    ck = clocks.stop()
+    ms = allmax(ms)
+    value = args.steps * world / (ms / 1e3)
+    # ---- e2e: host buffers through vca_gpu_solve ------------------------
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        p = mine[(args.warmup + i) % len(mine)]
+        s.solve(p.Hloc, p.Hk)
+    e2e_s = allmax(time.perf_counter() - t0)
+    e2e = args.steps * world / e2e_s
+    p0 = mine[0]
+    h2d = int(p0.Hloc.nbytes + p0.Hk.nbytes)
+    # ---- roofline of the dominant kernel: batched real H x v on the chain
+    # target sector (7,6) with the particle batch of one spin (408 columns)
+    roof = None
+    if rank == 0:
+        import torch
+        isec = 1 + 6 + 7 * 13
+        _, _, du, dd = s.sector_info(isec)
+        D = du * dd
+        L = 12
+        m = L + L * (L - 1) + 2 * L * (L - 1)
+        x = torch.randn(D * m, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        torch.cuda.synchronize()
+        reps = 5
+        t_ms = s.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, m, reps)
+        bytes_alg = 16.0 * D * m
+        peak, kind = measured_peaks()
+        ach = bytes_alg / (t_ms / 1e3) / 1e9
+        traffic = profile_traffic("hxv_real_square4x3.md")
+        roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": traffic,
+                "kernel": "k_hxv_real", "launch_ms": round(t_ms, 4),
+                "algorithmic_bytes_per_launch": bytes_alg,
+                "peak_kind": kind,
+                "shape": f"sector (7,6) D={D}, {m} real columns"}
+        del x, y
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (chain column batches 2.3 GB per buffer)",
+                   "stage_ms_last_warmup": [round(x, 1) for x in stage_ms]},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8},
+        "gpu_launches": int(launches),
+        "clocks": ck,
+        "omega_samples": [round(x, 12) for x in omegas[:3]],
+    }
+    if roof is not None:
+        out["roofline"] = roof
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, sample, _ = cpu_sample(pts[0], os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": sample}
+    if rank == 0:
+        print(json.dumps(out))
+    s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def profile_hxv(ncols: int, reps: int) -> int:
+    """Batched H x v only (for ncu captures of k_hxv_real)."""
+    import torch
+    from vca_gb300 import build as vbuild
+    vbuild.build()
+    from vca_gb300.solver import VcaSolver
+    pt = build_points()[5]
+    s = VcaSolver(pt.cfg)
+    s.set_hamiltonian(pt.Hloc)
+    isec = 1 + 6 + 7 * 13
+    _, _, du, dd = s.sector_info(isec)
+    D = du * dd
+    x = torch.randn(D * ncols, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    ms = s.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, ncols, reps)
+    print(json.dumps({"kernel": "k_hxv_real", "sector": [7, 6], "D": D, "ncols": ncols, "reps": reps,
+                      "ms_per_launch": ms, "alg_GBps": 16.0 * D * ncols / (ms / 1e3) / 1e9}))
+    s.close()
+    return 0
+
+
+def profile_solve() -> int:
+    """One warm-up and one timed plain solve of a reduced 4x3 point."""
+    from vca_gb300 import build as vbuild, clusters
+    vbuild.build()
+    from vca_gb300.solver import VcaSolver
+    pt = clusters.square(nx=4, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=8, nky=8, ngfiter=200,
+                         omega_nodes=1024)
+    s = VcaSolver(pt.cfg)
+    s.solve(pt.Hloc, pt.Hk)
+    t0 = time.perf_counter()
+    om = s.solve(pt.Hloc, pt.Hk)
+    print(json.dumps({"omega": om, "s": time.perf_counter() - t0, "stage_ms": s.timings().tolist(),
+                      "launches": s.kernel_launches()}))
+    s.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile-hxv", type=int, default=0, metavar="NCOLS",
+                    help="profiling mode: load the 4x3 Hamiltonian and launch the batched H x v "
+                         "on sector (7,6) with NCOLS real columns --reps times (no solve)")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="profiling mode: one plain solve of a reduced 4x3 point "
+                         "(8x8 k-grid, 1024 nodes) after one warm-up solve")
+    ap.add_argument("--reps", type=int, default=3)
+    args = ap.parse_args()
+    if args.profile_hxv:
+        return profile_hxv(args.profile_hxv, args.reps)
+    if args.profile_solve:
+        return profile_solve()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

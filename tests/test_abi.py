@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     txt = open(os.path.join(ROOT, "include", "vca_gpu.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void)\s+(vca_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int64_t|int|void)\s+(vca_\w+)\s*\(", txt, re.M)))
 
 
 @pytest.fixture(scope="module")

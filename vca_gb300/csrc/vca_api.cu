@@ -11,6 +11,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <string>
 #include <vector>
 
@@ -111,6 +112,8 @@ struct Ctx {
   // Hk and Omega
   int64_t Nk = 0;
   double2* d_Hk = nullptr;  // lso per k
+  bool hk_spin_diag = true;
+  double t_ms[4] = {0, 0, 0, 0};  // set_hamiltonian, diagonalise, chains, Omega
 };
 Ctx* g = nullptr;
 
@@ -764,7 +767,7 @@ void bath_lso(std::vector<double2>& hb, std::vector<double2>& V) {
 }
 
 // spin-block structure of the Omega matrices (all spin-off-diagonal blocks 0)
-bool spin_block_diagonal(const double* Hk, int64_t Nk) {
+bool hk_spin_diagonal(const double* Hk, int64_t Nk) {
   const vca_config& c = g->cfg;
   if (c.Nspin == 1) return true;
   const size_t nel = hloc_len(c);
@@ -774,10 +777,20 @@ bool spin_block_diagonal(const double* Hk, int64_t Nk) {
         for (int jo = 0; jo < c.Norb; jo++)
           for (int s = 0; s < 2; s++) {
             int64_t x = idx_nnn(c, il, jl, s, 1 - s, io, jo);
-            if (g->Hloc[x] != 0.0) return false;
             for (int64_t k = 0; k < Nk; k++)
               if (Hk[2 * (k * nel + x)] != 0.0 || Hk[2 * (k * nel + x) + 1] != 0.0) return false;
           }
+  return true;
+}
+bool point_spin_diagonal() {
+  const vca_config& c = g->cfg;
+  if (c.Nspin == 1) return true;
+  for (int il = 0; il < c.Nlat; il++)
+    for (int jl = 0; jl < c.Nlat; jl++)
+      for (int io = 0; io < c.Norb; io++)
+        for (int jo = 0; jo < c.Norb; jo++)
+          for (int s = 0; s < 2; s++)
+            if (g->Hloc[idx_nnn(c, il, jl, s, 1 - s, io, jo)] != 0.0) return false;
   if (g->has_bath) {
     for (int a = 0; a < c.Nlat_bath; a++)
       for (int b = 0; b < c.Nlat_bath; b++)
@@ -797,8 +810,7 @@ bool spin_block_diagonal(const double* Hk, int64_t Nk) {
 
 // Omega integral (frequency_integration, VCA_OMEGA.f90:123-146) with the
 // fixed Gauss-Legendre rule; also returns f(w) at the nodes when asked.
-int omega_integral(const double* Hk_host, int64_t Nk, double* out, int nz_eval, const double* w_eval,
-                   double* f_eval) {
+int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, double* f_eval) {
   const vca_config& c = g->cfg;
   Arena ar;
   const int N = g->N, NN = N * N;
@@ -850,7 +862,7 @@ int omega_integral(const double* Hk_host, int64_t Nk, double* out, int nz_eval, 
     launch_delta_bath(n, d_z, N, Nb, dhb, dV, c.xmu, work, D, g->st);
   }
   launch_add_hloc(n, NN, D, Hl, P, g->st);
-  const bool blk = spin_block_diagonal(Hk_host, Nk);
+  const bool blk = g->hk_spin_diag && point_spin_diagonal();
   const int nblk = blk ? c.Nspin : 1;
   const int nb = N / nblk;
   if (nb > 32) { ar.release(); VFAIL(VCA_ERR_UNSUPPORTED, "Omega k-sum supports spin blocks up to 32 orbitals"); }
@@ -891,22 +903,46 @@ int upload_hk(const double* Hk, int64_t Nk) {
   launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, Nk, raw, g->d_Hk, g->st);
   CUCHK(cudaGetLastError());
   g->Nk = Nk;
+  g->hk_spin_diag = hk_spin_diagonal(Hk, Nk);
+  CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+double now_ms() {
+  timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+// Hk must already be resident (upload_hk)
+int solve_resident(const double* Hloc, const double* bath_h, const double* bath_v, double* omega_out) {
+  if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (!g->d_Hk) VFAIL(VCA_ERR_STATE, "no Hk resident: call vca_gpu_solve or vca_gpu_upload_hk first");
+  g->solved = false;
+  double t0 = now_ms();
+  RCHK(set_hamiltonian(Hloc, bath_h, bath_v));
+  double t1 = now_ms();
+  RCHK(diagonalize());
+  double t2 = now_ms();
+  RCHK(build_gf());
+  double t3 = now_ms();
+  RCHK(omega_integral(g->Nk, &g->omega_int, 0, nullptr, nullptr));
+  double t4 = now_ms();
+  g->t_ms[0] = t1 - t0;
+  g->t_ms[1] = t2 - t1;
+  g->t_ms[2] = t3 - t2;
+  g->t_ms[3] = t4 - t3;
+  g->sft = g->egs - g->omega_int;  // VCA_MAIN.f90:183-197
+  g->solved = true;
+  if (omega_out) *omega_out = g->sft;
   return VCA_OK;
 }
 
 int solve_one(const double* Hloc, const double* Hk, int64_t Nk, const double* bath_h,
               const double* bath_v, double* omega_out) {
   if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
-  g->solved = false;
-  RCHK(set_hamiltonian(Hloc, bath_h, bath_v));
   RCHK(upload_hk(Hk, Nk));
-  RCHK(diagonalize());
-  RCHK(build_gf());
-  RCHK(omega_integral(Hk, Nk, &g->omega_int, 0, nullptr, nullptr));
-  g->sft = g->egs - g->omega_int;  // VCA_MAIN.f90:183-197
-  g->solved = true;
-  if (omega_out) *omega_out = g->sft;
-  return VCA_OK;
+  return solve_resident(Hloc, bath_h, bath_v, omega_out);
 }
 
 }  // namespace
@@ -1183,30 +1219,8 @@ int vca_gpu_get_gimp_realaxis(double* g_out) { return gimp_grid(false, g_out); }
 int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out) {
   if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   if (!w || !f_out || nw < 1) VFAIL(VCA_ERR_ARG, "bad arguments");
-  // the Hk of the last solve is resident (lso); the spin-block test needs
-  // host Hk, so re-derive it conservatively from the device copy
-  const size_t NN = (size_t)g->N * g->N;
-  std::vector<double2> hk(NN * g->Nk);
-  CUCHK(cudaMemcpy(hk.data(), g->d_Hk, sizeof(double2) * hk.size(), cudaMemcpyDeviceToHost));
-  // rebuild an nnn-ordered host copy for the block test
-  const vca_config& c = g->cfg;
-  const size_t nel = hloc_len(c);
-  std::vector<double> hn(2 * nel * g->Nk);
-  for (int64_t k = 0; k < g->Nk; k++)
-    for (int il = 0; il < c.Nlat; il++)
-      for (int jl = 0; jl < c.Nlat; jl++)
-        for (int is = 0; is < c.Nspin; is++)
-          for (int js = 0; js < c.Nspin; js++)
-            for (int io = 0; io < c.Norb; io++)
-              for (int jo = 0; jo < c.Norb; jo++) {
-                int a = io + il * c.Norb + is * c.Norb * c.Nlat, b = jo + jl * c.Norb + js * c.Norb * c.Nlat;
-                double2 v = hk[k * NN + a + (size_t)b * g->N];
-                size_t o = k * nel + idx_nnn(c, il, jl, is, js, io, jo);
-                hn[2 * o] = v.x;
-                hn[2 * o + 1] = v.y;
-              }
   double dummy;
-  return omega_integral(hn.data(), g->Nk, &dummy, (int)nw, w, f_out);
+  return omega_integral(g->Nk, &dummy, (int)nw, w, f_out);
 }
 
 int vca_gpu_sector_info(int32_t isector, int32_t* nup, int32_t* ndw, int64_t* dimup, int64_t* dimdw) {
@@ -1232,22 +1246,26 @@ int vca_gpu_sector_map(int32_t isector, int32_t spin, int64_t* map, int64_t cap)
   return VCA_OK;
 }
 
-int vca_gpu_hxv_device(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex) {
+static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t ncols) {
   if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
   if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  if (ncols < 1) VFAIL(VCA_ERR_ARG, "ncols must be >= 1");
   if (!is_complex && !g->real_model) VFAIL(VCA_ERR_ARG, "real vectors need a real Hamiltonian");
   SectorView sv = view_of(sec_nup(isector), sec_ndw(isector));
   if (is_complex) {
-    if (g->real_model) {  // complex vector on a real H: (re, im) as two real columns
-      launch_hxv_real(sv, g->md, 2, (const double*)d_v, (double*)d_hv, g->st);
-    } else {
-      launch_hxv_cplx(sv, g->md, 1, (const double2*)d_v, (double2*)d_hv, g->st);
-    }
+    if (g->real_model)  // complex columns on a real H: (re, im) as two real columns
+      launch_hxv_real(sv, g->md, 2 * ncols, (const double*)d_v, (double*)d_hv, g->st);
+    else
+      launch_hxv_cplx(sv, g->md, ncols, (const double2*)d_v, (double2*)d_hv, g->st);
   } else {
-    launch_hxv_real(sv, g->md, 1, (const double*)d_v, (double*)d_hv, g->st);
+    launch_hxv_real(sv, g->md, ncols, (const double*)d_v, (double*)d_hv, g->st);
   }
   CUCHK(cudaGetLastError());
   return VCA_OK;
+}
+
+int vca_gpu_hxv_device(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex) {
+  return hxv_cols(isector, d_v, d_hv, is_complex, 1);
 }
 
 int vca_gpu_hxv(int32_t isector, const double* v, double* hv) {
@@ -1269,16 +1287,16 @@ int vca_gpu_hxv(int32_t isector, const double* v, double* hv) {
   return VCA_OK;
 }
 
-int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t reps,
-                      double* ms_per_call) {
+int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t ncols,
+                      int32_t reps, double* ms_per_call) {
   if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
   if (reps < 1 || !ms_per_call) VFAIL(VCA_ERR_ARG, "bad arguments");
   cudaEvent_t e0, e1;
   CUCHK(cudaEventCreate(&e0));
   CUCHK(cudaEventCreate(&e1));
-  RCHK(vca_gpu_hxv_device(isector, d_v, d_hv, is_complex));  // warm-up
+  RCHK(hxv_cols(isector, d_v, d_hv, is_complex, ncols));  // warm-up
   CUCHK(cudaEventRecord(e0, g->st));
-  for (int r = 0; r < reps; r++) RCHK(vca_gpu_hxv_device(isector, d_v, d_hv, is_complex));
+  for (int r = 0; r < reps; r++) RCHK(hxv_cols(isector, d_v, d_hv, is_complex, ncols));
   CUCHK(cudaEventRecord(e1, g->st));
   CUCHK(cudaEventSynchronize(e1));
   float ms = 0.f;
@@ -1286,6 +1304,49 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms_per_call = ms / reps;
+  return VCA_OK;
+}
+
+int vca_gpu_upload_hk(const double* Hk, int64_t Nk) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  return upload_hk(Hk, Nk);
+}
+
+int vca_gpu_solve_resident(const double* Hloc, const double* bath_h, const double* bath_v,
+                           double* omega_out) {
+  g_err.clear();
+  return solve_resident(Hloc, bath_h, bath_v, omega_out);
+}
+
+int64_t vca_gpu_kernel_launches(void) { return (int64_t)launch_count(); }
+
+int vca_gpu_get_timings(double* ms, int32_t n) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (!ms) VFAIL(VCA_ERR_ARG, "NULL output");
+  for (int i = 0; i < n && i < 4; i++) ms[i] = g->t_ms[i];
+  return VCA_OK;
+}
+
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+int vca_gpu_timer_start(void) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (!g_t0) { CUCHK(cudaEventCreate(&g_t0)); CUCHK(cudaEventCreate(&g_t1)); }
+  CUCHK(cudaEventRecord(g_t0, g->st));
+  return VCA_OK;
+}
+int vca_gpu_timer_stop(double* ms) {
+  if (!g || !g_t0) VFAIL(VCA_ERR_STATE, "vca_gpu_timer_start has not been called");
+  CUCHK(cudaEventRecord(g_t1, g->st));
+  CUCHK(cudaEventSynchronize(g_t1));
+  float f = 0.f;
+  CUCHK(cudaEventElapsedTime(&f, g_t0, g_t1));
+  if (ms) *ms = f;
+  return VCA_OK;
+}
+
+int vca_gpu_synchronize(void) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  CUCHK(cudaStreamSynchronize(g->st));
   return VCA_OK;
 }
 

@@ -4,9 +4,14 @@
 #include "vca_kernels.cuh"
 
 #include <cmath>
+#include <atomic>
 #include <cstdio>
 
 namespace vca {
+
+static std::atomic<long long> g_launches{0};
+long long launch_count() { return g_launches.load(); }
+#define COUNT_LAUNCH() g_launches.fetch_add(1, std::memory_order_relaxed)
 
 __constant__ int64_t c_binom[VCA_MAX_NS + 1][VCA_MAX_NS + 1];
 
@@ -62,6 +67,7 @@ __global__ void k_build_words(int Ns, int n, int dim, int* words) {
   }
 }
 void launch_build_words(int Ns, int n, int dim, int* words, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_build_words<<<nblocks(dim, 256), 256, 0, st>>>(Ns, n, dim, words);
 }
 
@@ -91,6 +97,7 @@ __global__ void k_hop_count(int dim, const int* words, const HopPair* pairs, int
 }
 int launch_hop_count(int Ns, int n, int dim, const int* words, const HopPair* d_pairs, int npairs,
                      int* cnt, int* d_scratch_max, cudaStream_t st) {
+  COUNT_LAUNCH();
   (void)Ns;
   (void)n;
   cudaMemsetAsync(d_scratch_max, 0, sizeof(int), st);
@@ -126,6 +133,7 @@ __global__ void k_hop_fill(int dim, int width, const int* words, const HopPair* 
 }
 void launch_hop_fill(int Ns, int n, int dim, int width, const int* words, const HopPair* d_pairs,
                      int npairs, int* src, double2* amp, cudaStream_t st) {
+  COUNT_LAUNCH();
   (void)Ns;
   (void)n;
   if (width == 0) return;
@@ -154,6 +162,7 @@ __global__ void k_e1(int dim, const int* words, E1Params p, int with_const, doub
 }
 void launch_e1(int dim, const int* words, const E1Params& p, bool with_const, double2* e1,
                cudaStream_t st) {
+  COUNT_LAUNCH();
   k_e1<<<nblocks(dim, 256), 256, 0, st>>>(dim, words, p, with_const ? 1 : 0, e1);
 }
 
@@ -246,6 +255,7 @@ static void col_shape(int m, dim3& blk) {
 }
 void launch_hxv_real(const SectorView& sv, const MixedDiag& md, int m, const double* X, double* Y,
                      cudaStream_t st) {
+  COUNT_LAUNCH();
   dim3 blk;
   col_shape(m, blk);
   int64_t D = (int64_t)sv.dimup * sv.dimdw;
@@ -253,6 +263,7 @@ void launch_hxv_real(const SectorView& sv, const MixedDiag& md, int m, const dou
 }
 void launch_hxv_cplx(const SectorView& sv, const MixedDiag& md, int m, const double2* X, double2* Y,
                      cudaStream_t st) {
+  COUNT_LAUNCH();
   dim3 blk;
   col_shape(m, blk);
   int64_t D = (int64_t)sv.dimup * sv.dimdw;
@@ -298,6 +309,7 @@ __global__ void k_col_reduce(int m, int nblk, const double* partial, double* out
 }
 void launch_col_dot(const ColBatch& b, const void* X, const void* Y, double* partial, int nblk,
                     double* out_col, cudaStream_t st) {
+  COUNT_LAUNCH();
   dim3 blk;
   col_shape(b.m, blk);
   dim3 grd(nblk, (b.m + blk.x - 1) / blk.x, 1);
@@ -306,6 +318,7 @@ void launch_col_dot(const ColBatch& b, const void* X, const void* Y, double* par
     k_col_dot<true><<<grd, blk, shm, st>>>(b.rows, b.m, X, Y, partial);
   else
     k_col_dot<false><<<grd, blk, shm, st>>>(b.rows, b.m, X, Y, partial);
+  COUNT_LAUNCH();
   k_col_reduce<<<nblocks(b.m, 128), 128, 0, st>>>(b.m, nblk, partial, out_col);
 }
 
@@ -331,6 +344,7 @@ __global__ void k_col_axpy(int64_t rows, int m, const int* col2ch, const ChainMe
 }
 void launch_col_axpy(const ColBatch& b, const double* coef, const void* X, void* Y, bool negate,
                      cudaStream_t st) {
+  COUNT_LAUNCH();
   int64_t n = b.rows * b.m;
   if (b.cplx)
     k_col_axpy<true><<<nblocks(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, coef,
@@ -359,6 +373,7 @@ __global__ void k_col_scale(int64_t rows, int m, const int* col2ch, const ChainM
   }
 }
 void launch_col_scale(const ColBatch& b, const double* scale, const void* Y, void* X, cudaStream_t st) {
+  COUNT_LAUNCH();
   int64_t n = b.rows * b.m;
   if (b.cplx)
     k_col_scale<true><<<nblocks(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scale, Y, X);
@@ -374,6 +389,7 @@ __global__ void k_chain_sum(int nch, const ChainMeta* meta, const double* in_col
   }
 }
 void launch_chain_sum(const ColBatch& b, const double* in_col, double* out_ch, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_chain_sum<<<nblocks(b.nch, 128), 128, 0, st>>>(b.nch, b.meta, in_col, out_ch);
 }
 
@@ -405,6 +421,7 @@ __global__ void k_lanczos_record(int nch, ChainMeta* meta, int k, const double* 
 void launch_lanczos_record(int nch, ChainMeta* meta, int k, const double* alpha_ch,
                            const double* beta2_ch, double* A, double* Bt, int ldab, double tol,
                            double* invbeta, double* beta_now, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_lanczos_record<<<nblocks(nch, 128), 128, 0, st>>>(nch, meta, k, alpha_ch, beta2_ch, A, Bt, ldab,
                                                       tol, invbeta, beta_now);
 }
@@ -426,6 +443,7 @@ __global__ void k_psi_accum(int64_t n, const double* s, int k, const void* Xv, v
 }
 void launch_psi_accum(int64_t n, bool cplx, const double* s, int k, const void* X, void* psi,
                       cudaStream_t st) {
+  COUNT_LAUNCH();
   if (cplx)
     k_psi_accum<true><<<nblocks(n, 256), 256, 0, st>>>(n, s, k, X, psi);
   else
@@ -447,6 +465,7 @@ __global__ void k_start_vector(int64_t n, uint64_t seed, int isector, double* X)
   }
 }
 void launch_start_vector(int64_t n, uint64_t seed, int isector, double* X, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_start_vector<<<nblocks(n, 256), 256, 0, st>>>(n, seed, isector, X);
 }
 __global__ void k_fill(int64_t n, double v, double* X) {
@@ -455,6 +474,7 @@ __global__ void k_fill(int64_t n, double v, double* X) {
     X[i] = v;
 }
 void launch_fill(int64_t n, double v, double* X, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_fill<<<nblocks(n, 256), 256, 0, st>>>(n, v, X);
 }
 
@@ -574,6 +594,7 @@ __global__ void k_tri_lowest(const double* A, const double* Bt, int k, double bt
 }
 void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta,
                        double* s, double* resid, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_tri_lowest<<<1, 32, 0, st>>>(A, Bt, k, btail, theta, s, resid);
 }
 
@@ -671,6 +692,7 @@ void launch_chain_poles(int nch, const ChainMeta* meta, const double* A, const d
                         const double* norm2, const double2* wfac, const int* isign, double Ei,
                         double zeta, double* work, double* poles, double2* weights, int* nexc,
                         cudaStream_t st) {
+  COUNT_LAUNCH();
   k_chain_poles<<<nblocks(nch, 64), 64, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta,
                                                  work, poles, weights, nexc);
 }
@@ -723,6 +745,7 @@ __global__ void k_chain_init(SectorView tgt, int src_dimup, const void* gsv, int
 void launch_chain_init(const SectorView& tgt, int src_dimup, const void* gs, bool gs_cplx,
                        int nchain, const ChainInit* d_ci, int m, bool cols_cplx, void* X,
                        cudaStream_t st) {
+  COUNT_LAUNCH();
   int64_t n = (int64_t)tgt.dimup * tgt.dimdw * nchain;
   int nb = nblocks(n, 256);
   if (cols_cplx) {
@@ -763,6 +786,7 @@ __global__ void k_gf_eval(GfLayout g, int nz, const double2* z, double2* G) {
   }
 }
 void launch_gf_eval(const GfLayout& g, int nz, const double2* z, double2* G, cudaStream_t st) {
+  COUNT_LAUNCH();
   int64_t n = (int64_t)nz * g.nelem;
   k_gf_eval<<<nblocks(n, 128), 128, 0, st>>>(g, nz, z, G);
 }
@@ -802,6 +826,7 @@ __global__ void k_gf_assemble(ClusterDims cd, int nz, const double2* Graw, doubl
 }
 void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, double2* Glso,
                         cudaStream_t st) {
+  COUNT_LAUNCH();
   int64_t n = (int64_t)nz * cd.N * cd.N;
   k_gf_assemble<<<nblocks(n, 256), 256, 0, st>>>(cd, nz, Graw, Glso);
 }
@@ -939,6 +964,7 @@ __global__ void k_omega_ksum(int N, int nblk, int nb, const double2* P, const do
 }
 void launch_omega_ksum(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso,
                        int64_t Nk, const double2* Hk, double* fpart, int kchunks, cudaStream_t st) {
+  COUNT_LAUNCH();
   const int threads = 128;
   size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
   if (shm > 48 * 1024)
@@ -956,6 +982,7 @@ __global__ void k_reduce_rows(int nrows, int ncols, const double* in, double sca
 }
 void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out,
                         cudaStream_t st) {
+  COUNT_LAUNCH();
   k_reduce_rows<<<nblocks(nrows, 128), 128, 0, st>>>(nrows, ncols, in, scale, out);
 }
 
@@ -995,6 +1022,7 @@ __global__ void k_gauss_legendre(int n, double* x, double* w) {
   }
 }
 void launch_gauss_legendre(int n, double* x, double* w, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_gauss_legendre<<<nblocks((n + 1) / 2, 128), 128, 0, st>>>(n, x, w);
 }
 
@@ -1058,6 +1086,7 @@ __global__ void k_delta_bath(int nz, const double2* z, int N, int Nb, const doub
 }
 void launch_delta_bath(int nz, const double2* z, int N, int Nb, const double2* hb, const double2* V,
                        double xmu, double2* work, double2* out, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_delta_bath<<<nblocks(nz, 64), 64, 0, st>>>(nz, z, N, Nb, hb, V, xmu, work, out);
 }
 
@@ -1081,6 +1110,7 @@ __global__ void k_chain_norm_init(int nch, ChainMeta* meta, const double* norm2,
 }
 void launch_chain_norm_init(int nch, ChainMeta* meta, const double* norm2, double* invnorm,
                             cudaStream_t st) {
+  COUNT_LAUNCH();
   k_chain_norm_init<<<nblocks(nch, 128), 128, 0, st>>>(nch, meta, norm2, invnorm);
 }
 __global__ void k_recip(int n, const double* in, double* out) {
@@ -1088,6 +1118,7 @@ __global__ void k_recip(int n, const double* in, double* out) {
     out[i] = (in[i] != 0.0) ? 1.0 / in[i] : 0.0;
 }
 void launch_recip(int n, const double* in, double* out, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_recip<<<nblocks(n, 128), 128, 0, st>>>(n, in, out);
 }
 // (Nlat,Nlat,Nspin,Nspin,Norb,Norb[,L]) -> lso N x N per slice (VCA_AUX_FUNX.f90:255-279)
@@ -1109,6 +1140,7 @@ __global__ void k_nnn2lso(int Nlat, int Nspin, int Norb, int64_t L, const double
 }
 void launch_nnn2lso(int Nlat, int Nspin, int Norb, int64_t L, const double2* in, double2* out,
                     cudaStream_t st) {
+  COUNT_LAUNCH();
   const int N = Nlat * Nspin * Norb;
   k_nnn2lso<<<nblocks((int64_t)N * N * L, 256), 256, 0, st>>>(Nlat, Nspin, Norb, L, in, out);
 }
@@ -1123,6 +1155,7 @@ __global__ void k_add_hloc(int nw, int NN, const double2* D, const double2* H, d
   }
 }
 void launch_add_hloc(int nw, int NN, const double2* D, const double2* H, double2* P, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_add_hloc<<<nblocks((int64_t)nw * NN, 256), 256, 0, st>>>(nw, NN, D, H, P);
 }
 // omega nodes: z = i*scale*s/(1-s), W = w*scale/(1-s)^2
@@ -1136,6 +1169,7 @@ __global__ void k_omega_nodes(int n, double scale, const double* s, const double
 }
 void launch_omega_nodes(int n, double scale, const double* s, const double* w, double2* z, double* W,
                         cudaStream_t st) {
+  COUNT_LAUNCH();
   k_omega_nodes<<<nblocks(n, 128), 128, 0, st>>>(n, scale, s, w, z, W);
 }
 // deterministic weighted sum: out = sum_i a[i]*b[i] (single block)
@@ -1152,6 +1186,7 @@ __global__ void k_wsum(int n, const double* a, const double* b, double* out) {
   if (threadIdx.x == 0) out[0] = sh[0];
 }
 void launch_wsum(int n, const double* a, const double* b, double* out, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_wsum<<<1, 256, 0, st>>>(n, a, b, out);
 }
 // complex start vector (real values, zero imaginary part)
@@ -1161,6 +1196,7 @@ __global__ void k_real_to_cplx(int64_t n, const double* in, double2* out) {
     out[i] = make_double2(in[i], 0.0);
 }
 void launch_real_to_cplx(int64_t n, const double* in, double2* out, cudaStream_t st) {
+  COUNT_LAUNCH();
   k_real_to_cplx<<<nblocks(n, 256), 256, 0, st>>>(n, in, out);
 }
 

@@ -5,6 +5,9 @@
 
 namespace vca {
 
+// number of kernel launches issued by this library since load
+long long launch_count();
+
 // ---- Fock basis (VCA_SETUP.f90:660-695, 724-750) ---------------------------
 void set_binomials(int Ns, cudaStream_t st);
 void launch_build_words(int Ns, int n, int dim, int* words, cudaStream_t st);

@@ -30,7 +30,8 @@ EXPORTS = [
     "vca_gpu_get_state", "vca_gpu_get_sector_energies", "vca_gpu_get_gf_channel",
     "vca_gpu_sum_kmesh", "vca_gpu_finalize", "vca_gpu_last_error", "vca_gpu_sector_info",
     "vca_gpu_sector_map", "vca_gpu_set_hamiltonian", "vca_gpu_hxv", "vca_gpu_hxv_device",
-    "vca_gpu_hxv_timed",
+    "vca_gpu_hxv_timed", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
+    "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
 ]
 
 
@@ -77,7 +78,14 @@ def load(path: Optional[str] = None):
         "vca_gpu_set_hamiltonian": (ctypes.c_int, [dp, dp, dp]),
         "vca_gpu_hxv": (ctypes.c_int, [i32, dp, dp]),
         "vca_gpu_hxv_device": (ctypes.c_int, [i32, vp, vp, i32]),
-        "vca_gpu_hxv_timed": (ctypes.c_int, [i32, vp, vp, i32, i32, dp]),
+        "vca_gpu_hxv_timed": (ctypes.c_int, [i32, vp, vp, i32, i32, i32, dp]),
+        "vca_gpu_upload_hk": (ctypes.c_int, [dp, i64]),
+        "vca_gpu_solve_resident": (ctypes.c_int, [dp, dp, dp, dp]),
+        "vca_gpu_kernel_launches": (i64, []),
+        "vca_gpu_get_timings": (ctypes.c_int, [dp, i32]),
+        "vca_gpu_synchronize": (ctypes.c_int, []),
+        "vca_gpu_timer_start": (ctypes.c_int, []),
+        "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -158,6 +166,45 @@ class VcaSolver:
                                          _dp(bv), int(np.prod(bath_v_shape(c))) if bv is not None else 0,
                                          _dp(out)))
         return out
+
+    def upload_hk(self, Hk):
+        Hk = _c128(Hk)
+        check(self.L.vca_gpu_upload_hk(_dp(Hk), Hk.shape[6]))
+
+    def solve_resident(self, Hloc, bath_h=None, bath_v=None) -> float:
+        c = self.cfg
+        Hloc = _c128(Hloc, hloc_shape(c), "Hloc")
+        if bath_h is not None:
+            bath_h = _c128(bath_h, bath_h_shape(c), "bath_h")
+            bath_v = _c128(bath_v, bath_v_shape(c), "bath_v")
+        out = ctypes.c_double()
+        check(self.L.vca_gpu_solve_resident(_dp(Hloc), _dp(bath_h), _dp(bath_v), ctypes.byref(out)))
+        return out.value
+
+    def timings(self):
+        out = np.zeros(4)
+        check(self.L.vca_gpu_get_timings(_dp(out), 4))
+        return out
+
+    def timer_start(self):
+        check(self.L.vca_gpu_timer_start())
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_double()
+        check(self.L.vca_gpu_timer_stop(ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        check(self.L.vca_gpu_synchronize())
+
+    def kernel_launches(self) -> int:
+        return int(self.L.vca_gpu_kernel_launches())
+
+    def hxv_timed(self, isector, d_v, d_hv, is_complex, ncols, reps) -> float:
+        ms = ctypes.c_double()
+        check(self.L.vca_gpu_hxv_timed(isector, ctypes.c_void_p(d_v), ctypes.c_void_p(d_hv), is_complex,
+                                       ncols, reps, ctypes.byref(ms)))
+        return ms.value
 
     def get_sft_potential(self) -> float:
         out = ctypes.c_double()
