@@ -189,6 +189,18 @@ def run_reference(args):
     return 0
 
 
+def hxv_operand(s, D, m):
+    """Unit-norm random columns in the library's arithmetic (FP64, or int64
+    fixed point with scale 2^-F when the fixed-point path is active)."""
+    import torch
+    fx, F, _ = s.arith_info()
+    x = torch.randn(D, m, dtype=torch.float64, device="cuda")
+    x /= torch.linalg.vector_norm(x, dim=0, keepdim=True)
+    if fx:
+        return torch.round(x * 2.0 ** F).to(torch.int64).reshape(-1), "k_hxv_fx"
+    return x.reshape(-1), "k_hxv_real"
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -260,7 +272,7 @@ def run_gpu(args):
         D = du * dd
         L = 12
         m = L + L * (L - 1) + 2 * L * (L - 1)
-        x = torch.randn(D * m, dtype=torch.float64, device="cuda")
+        x, kname = hxv_operand(s, D, m)
         y = torch.empty_like(x)
         torch.cuda.synchronize()
         reps = 5
@@ -268,10 +280,10 @@ def run_gpu(args):
         bytes_alg = 16.0 * D * m
         peak, kind = measured_peaks()
         ach = bytes_alg / (t_ms / 1e3) / 1e9
-        traffic = profile_traffic("hxv_real_square4x3.md")
+        traffic = profile_traffic(kname.replace("k_", "") + "_square4x3.md")
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic,
-                "kernel": "k_hxv_real", "launch_ms": round(t_ms, 4),
+                "kernel": kname, "launch_ms": round(t_ms, 4),
                 "algorithmic_bytes_per_launch": bytes_alg,
                 "peak_kind": kind,
                 "shape": f"sector (7,6) D={D}, {m} real columns"}
@@ -303,7 +315,7 @@ def run_gpu(args):
 
 
 def profile_hxv(ncols: int, reps: int) -> int:
-    """Batched H x v only (for ncu captures of k_hxv_real)."""
+    """Batched H x v only (for ncu captures of the H x v kernel)."""
     import torch
     from vca_gb300 import build as vbuild
     vbuild.build()
@@ -314,11 +326,11 @@ def profile_hxv(ncols: int, reps: int) -> int:
     isec = 1 + 6 + 7 * 13
     _, _, du, dd = s.sector_info(isec)
     D = du * dd
-    x = torch.randn(D * ncols, dtype=torch.float64, device="cuda")
+    x, kname = hxv_operand(s, D, ncols)
     y = torch.empty_like(x)
     torch.cuda.synchronize()
     ms = s.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, ncols, reps)
-    print(json.dumps({"kernel": "k_hxv_real", "sector": [7, 6], "D": D, "ncols": ncols, "reps": reps,
+    print(json.dumps({"kernel": kname, "sector": [7, 6], "D": D, "ncols": ncols, "reps": reps,
                       "ms_per_launch": ms, "alg_GBps": 16.0 * D * ncols / (ms / 1e3) / 1e9}))
     s.close()
     return 0

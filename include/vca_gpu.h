@@ -42,6 +42,14 @@ extern "C" {
 #define VCA_LANC_ARPACK 0
 #define VCA_LANC_LANCZOS 1
 
+/* Vector arithmetic of the Lanczos kernels.  FX keeps vectors as exact
+ * 64-bit fixed point with integer hop sums (real Hamiltonians whose hopping
+ * amplitudes take at most 4 magnitudes); FP64 is the general path.  AUTO
+ * picks FX when it applies. */
+#define VCA_ARITH_AUTO 0
+#define VCA_ARITH_FP64 1
+#define VCA_ARITH_FX 2
+
 /*
  * Input variables.  Field names, meanings and defaults follow
  * VCA_INPUT_VARS.f90:14-81 / :112-172.  Integers are 32-bit, logicals are
@@ -92,7 +100,8 @@ typedef struct vca_config {
   double gs_residual_tol;  /* GS stop: |beta_{k+1} s_k| <= tol*max(1,|E|)   */
   double gf_beta_tol;      /* GF chain stop: beta_{k+1} < tol (exhausted)   */
   uint64_t start_seed;     /* seed of the deterministic Lanczos start vector */
-  int32_t reserved[8];
+  int32_t arith;           /* VCA_ARITH_AUTO | VCA_ARITH_FP64 | VCA_ARITH_FX   */
+  int32_t reserved[7];
 } vca_config;
 
 /* Fill *cfg with the reference defaults (VCA_INPUT_VARS.f90:112-172) plus
@@ -230,6 +239,11 @@ int64_t vca_gpu_kernel_launches(void);
 /* Wall-clock milliseconds of the last solve's stages: [0] one-body tables,
  * [1] sector diagonalisation, [2] Green's function chains, [3] Omega. */
 int vca_gpu_get_timings(double* ms, int32_t n);
+/* Arithmetic of the loaded Hamiltonian: *fx = 1 when the fixed-point path is
+ * active, with vector scale 2^-F and H v scale 2^-G.  In that case the device
+ * buffers of vca_gpu_hxv_device / vca_gpu_hxv_timed hold int64 fixed-point
+ * columns (unit norm, scale 2^-F in, 2^-G out). */
+int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);
 /* CUDA events on the library stream: device time between start and stop. */

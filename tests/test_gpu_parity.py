@@ -121,3 +121,23 @@ def test_shape_errors_raise():
     with pytest.raises(VcaError) as ei:
         s.solve(bad, pt.Hk)
     assert ei.value.code == -7
+
+
+@pytest.mark.parametrize("arith", [1, 2], ids=["fp64", "fx"])
+@pytest.mark.parametrize("name", ["chain4", "square2x2_afm"])
+def test_fixed_point_and_fp64_paths_agree(name, arith):
+    """Both arithmetic paths of a real Hamiltonian against the oracle."""
+    pt = POINTS[name]()
+    cfg = pt.cfg.copy()
+    cfg.arith = arith
+    s = VcaSolver(cfg)
+    om = s.solve(pt.Hloc, pt.Hk)
+    assert s.arith_info()[0] == (arith == 2)
+    o = Oracle.from_point(pt)
+    ref, egs_ref, _ = o.solve()
+    egs, _ = s.energies()
+    assert abs(egs - egs_ref) <= E_TOL * abs(egs_ref)
+    assert abs(om - ref) <= E_TOL * abs(ref), (om, ref)
+    np.testing.assert_allclose(s.sector_energies(), o.sector_energies(), rtol=E_TOL, atol=E_TOL)
+    z = 1j * np.array([0.05, 0.3, 1.0, 3.0, 10.0])
+    assert np.abs(s.gf_cluster(z) - o.gf_cluster(z)).max() < G_TOL

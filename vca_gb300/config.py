@@ -13,6 +13,7 @@ import ctypes
 
 LANC_ARPACK = 0
 LANC_LANCZOS = 1
+ARITH_AUTO, ARITH_FP64, ARITH_FX = 0, 1, 2
 
 
 class VcaConfig(ctypes.Structure):
@@ -57,7 +58,8 @@ class VcaConfig(ctypes.Structure):
         ("gs_residual_tol", ctypes.c_double),
         ("gf_beta_tol", ctypes.c_double),
         ("start_seed", ctypes.c_uint64),
-        ("reserved", ctypes.c_int32 * 8),
+        ("arith", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
     ]
 
     def copy(self) -> "VcaConfig":
@@ -100,6 +102,7 @@ def default_config(**overrides) -> VcaConfig:
     c.gs_residual_tol = 1e-11
     c.gf_beta_tol = 1e-12
     c.start_seed = 20261203
+    c.arith = ARITH_AUTO
     for k, v in overrides.items():
         if k == "Uloc":
             for i in range(5):

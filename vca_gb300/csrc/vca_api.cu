@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/vca_gpu.h"
+#include "vca_fx.cuh"
 #include "vca_kernels.cuh"
 
 using namespace vca;
@@ -96,6 +97,14 @@ struct Ctx {
   int dwset = 0;  // spin table used by the down word (0 when Nspin == 1)
   MixedDiag md{};
   HopPair* d_pairs[2] = {nullptr, nullptr};
+  // fixed-point path (real Hamiltonians with <= 4 hopping magnitudes)
+  bool fx = false;
+  FxScales fxs{};
+  FxView fxbase{};
+  std::vector<signed char*> fx_code[2];
+  std::vector<i64*> fx_e1[2];
+  std::vector<HopPair> host_pairs;
+  std::vector<double> host_eps_abs;  // per spin set: bound of |one-body energy|
   // results
   bool solved = false;
   std::vector<double> sector_e;
@@ -179,6 +188,22 @@ SectorView view_of(int nup, int ndw) {
   v.up_e1 = u.e1;
   v.dw_e1 = d.e1;
   return v;
+}
+
+FxView fx_view_of(int nup, int ndw) {
+  FxView f = g->fxbase;
+  f.up_code = g->fx_code[0][nup];
+  f.dw_code = g->fx_code[g->dwset][ndw];
+  f.up_e1 = g->fx_e1[0][nup];
+  f.dw_e1 = g->fx_e1[g->dwset][ndw];
+  return f;
+}
+
+inline int ceil_log2(double x) {  // smallest e with 2^e >= x (x > 0)
+  int e = 0;
+  double p = 1.0;
+  while (p < x) { p *= 2.0; e++; }
+  return e;
 }
 
 // ---------------------------------------------------------------------------
@@ -266,6 +291,8 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
             }
     }
     if ((int)pairs.size() > VCA_MAX_PAIRS) VFAIL(VCA_ERR_UNSUPPORTED, "too many one-body pairs");
+    if (set == 0) { g->host_pairs.clear(); g->host_eps_abs.clear(); }
+    g->host_pairs.insert(g->host_pairs.end(), pairs.begin(), pairs.end());
     RCHK(g->ham.alloc(&g->d_pairs[set], pairs.size()));
     if (!pairs.empty())
       CUCHK(cudaMemcpyAsync(g->d_pairs[set], pairs.data(), pairs.size() * sizeof(HopPair),
@@ -294,6 +321,11 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
           cd e = g->bath_h[idx_bh(c, lb, lb, sidx, sidx, ob, ob)] - c.xmu;
           ep.eps[LC + lb * c.Norb_bath + ob] = make_double2(e.real(), e.imag());
         }
+    {
+      double em = 0.0;
+      for (int l = 0; l < g->Ns; l++) em = std::max(em, std::abs(cd(ep.eps[l].x, ep.eps[l].y)));
+      g->host_eps_abs.push_back(em * g->Ns + std::fabs(ep.upar) * c.Nlat * c.Norb * c.Norb);
+    }
     g->sp[set].assign(g->Ns + 1, SpinSpace());
     for (int n = 0; n <= g->Ns; n++) {
       SpinSpace& S = g->sp[set][n];
@@ -330,6 +362,69 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
     if (c.Norb > 1) md.c0 += c.Nlat * (c.Norb * (c.Norb - 1) / 2) * 0.25 * (2.0 * c.Ust - c.Jh);
   }
   g->md = md;
+  // ---- fixed-point tables -------------------------------------------------
+  g->fx = false;
+  if (c.arith != VCA_ARITH_FP64 && real) {
+    std::vector<double> classes;
+    double amax = 0.0, epsmax = 0.0;
+    // distinct hopping magnitudes over both spin tables
+    for (const HopPair& hp : g->host_pairs) {
+      double m = std::fabs(hp.re);
+      amax = std::max(amax, m);
+      bool seen = false;
+      for (double x : classes) if (x == m) seen = true;
+      if (!seen) classes.push_back(m);
+    }
+    if ((int)classes.size() <= VCA_FX_KMAX) {
+      // bound on max_i sum_j |H_ij| and on |d|
+      for (double e : g->host_eps_abs) epsmax = std::max(epsmax, e);
+      double dmax = 2.0 * epsmax;
+      for (int o = 0; o < c.Norb; o++) dmax += std::fabs(c.Uloc[o]) * c.Nlat;
+      if (c.Norb > 1) dmax += std::fabs(c.Ust) * c.Nlat * c.Norb * (c.Norb - 1);
+      dmax += std::fabs(md.c0);
+      int wmax = 0;
+      for (int set = 0; set < nsets; set++)
+        for (int n = 0; n <= g->Ns; n++) wmax = std::max(wmax, g->sp[set][n].width);
+      const double hbound = dmax + 2.0 * wmax * amax + 1.0;
+      FxScales fs;
+      fs.F = 59;
+      fs.G = 61 - ceil_log2(4.0 * hbound);
+      fs.A = 62 - ceil_log2(std::max(dmax, amax) + 1.0);
+      fs.C = 62 - ceil_log2(hbound + 1.0);
+      FxView fb{};
+      fb.K = (int)classes.size();
+      for (int k = 0; k < fb.K; k++) fb.afx[k] = (i64)std::llrint(std::ldexp(classes[k], fs.A));
+      fb.norb = c.Norb;
+      for (int o = 0; o < c.Norb; o++) {
+        fb.omask[o] = md.omask[o];
+        fb.Ufx[o] = (i64)std::llrint(std::ldexp(md.U[o], fs.A));
+      }
+      fb.Ustfx = (i64)std::llrint(std::ldexp(md.Ust, fs.A));
+      fb.c0fx = (i64)std::llrint(std::ldexp(md.c0, fs.A));
+      fb.shift = fs.A + fs.F - fs.G;
+      double* d_cls;
+      RCHK(g->ham.alloc(&d_cls, classes.size()));
+      CUCHK(cudaMemcpyAsync(d_cls, classes.data(), sizeof(double) * classes.size(), cudaMemcpyHostToDevice, g->st));
+      for (int set = 0; set < nsets; set++) {
+        g->fx_code[set].assign(g->Ns + 1, nullptr);
+        g->fx_e1[set].assign(g->Ns + 1, nullptr);
+        for (int n = 0; n <= g->Ns; n++) {
+          SpinSpace& S = g->sp[set][n];
+          RCHK(g->ham.alloc(&g->fx_code[set][n], (size_t)S.width * S.dim));
+          RCHK(g->ham.alloc(&g->fx_e1[set][n], S.dim));
+          launch_fx_codes(S.dim, S.width, S.amp, d_cls, fb.K, g->fx_code[set][n], g->st);
+          launch_fx_e1(S.dim, S.e1, fs.A, g->fx_e1[set][n], g->st);
+        }
+      }
+      if (nsets == 1) { g->fx_code[1] = g->fx_code[0]; g->fx_e1[1] = g->fx_e1[0]; }
+      CUCHK(cudaGetLastError());
+      g->fxs = fs;
+      g->fxbase = fb;
+      g->fx = true;
+    }
+  }
+  if (c.arith == VCA_ARITH_FX && !g->fx)
+    VFAIL(VCA_ERR_UNSUPPORTED, "fixed-point arithmetic needs a real Hamiltonian with at most 4 hopping magnitudes");
   g->ham_set = true;
   CUCHK(cudaStreamSynchronize(g->st));
   return VCA_OK;
@@ -346,6 +441,7 @@ struct BatchBufs {
   double *A, *Bt;
   ChainMeta* meta;
   int* col2ch;
+  i64 *afx, *bfx, *scr;  // fixed-point coefficients and per-chain scratch (2*nch)
 };
 
 int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k, double tol, int ldab) {
@@ -373,6 +469,32 @@ int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k,
   return VCA_OK;
 }
 
+// One Lanczos step in fixed point: X (2^-F) -> W = H X - a X - b Xp (2^-G)
+// -> X_next = W / beta (2^-F).  Buffers rotate as (X, Xp, YW) <- (new, X, YW).
+int lanczos_step_fx(const SectorView& sv, const FxView& fv, const ColBatch& cb, BatchBufs& bb, int k,
+                    double tol, int ldab) {
+  cudaStream_t st = g->st;
+  const FxScales& fs = g->fxs;
+  i64* X = (i64*)bb.b[0];
+  i64* Xp = (i64*)bb.b[1];
+  i64* YW = (i64*)bb.b[2];
+  launch_hxv_fx(sv, fv, cb.m, X, YW, st);
+  launch_fx_dot(cb, X, YW, fs.F, fs.G, (i64*)bb.partial, bb.nblk, bb.col_a, st);
+  launch_chain_sum(cb, bb.col_a, bb.ch_a, st);
+  launch_fx_coef(cb.nch, bb.ch_a, 1.0, fs.C, bb.afx, st);
+  if (k > 1) launch_fx_coef(cb.nch, bb.bnow, 1.0, fs.C, bb.bfx, st);
+  launch_fx_update(cb, fs, bb.afx, bb.bfx, k > 1, X, Xp, YW, YW, st);
+  launch_fx_dot(cb, YW, YW, fs.G, fs.G, (i64*)bb.partial, bb.nblk, bb.col_a, st);
+  launch_chain_sum(cb, bb.col_a, bb.ch_b2, st);
+  launch_lanczos_record(cb.nch, bb.meta, k, bb.ch_a, bb.ch_b2, bb.A, bb.Bt, ldab, tol, bb.invb, bb.bnow, st);
+  launch_fx_normalize(cb, fs, bb.invb, YW, Xp, bb.scr, st);  // X_next into the old Xp buffer
+  bb.b[0] = Xp;
+  bb.b[1] = X;
+  bb.b[2] = YW;
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
+
 int alloc_batch(Arena& ar, int64_t rows, int m, bool cplx, int nch, int ldab, BatchBufs& bb) {
   const size_t es = cplx ? sizeof(double2) : sizeof(double);
   for (int q = 0; q < 3; q++) {
@@ -381,7 +503,10 @@ int alloc_batch(Arena& ar, int64_t rows, int m, bool cplx, int nch, int ldab, Ba
     bb.b[q] = p;
   }
   bb.nblk = (int)std::min<int64_t>(std::max<int64_t>(1, rows / 256), 608);
-  RCHK(ar.alloc(&bb.partial, (size_t)bb.nblk * m));
+  RCHK(ar.alloc(&bb.partial, (size_t)bb.nblk * m * 2));  // int128 partials in the FX path
+  RCHK(ar.alloc(&bb.afx, nch));
+  RCHK(ar.alloc(&bb.bfx, nch));
+  RCHK(ar.alloc(&bb.scr, 2 * (size_t)nch));
   RCHK(ar.alloc(&bb.col_a, m));
   RCHK(ar.alloc(&bb.ch_a, nch));
   RCHK(ar.alloc(&bb.ch_b2, nch));
@@ -498,6 +623,98 @@ int sector_gs(int isector, double* E, void** vec_out, Arena& keep) {
   return VCA_OK;
 }
 
+// Fixed-point variant of sector_gs: same start vector (normalised in FP64,
+// then converted), same stopping rule and second pass; psi stays fixed point
+// (scale 2^-F) for the exact chain gathers.
+int sector_gs_fx(int isector, double* E, void** vec_out, Arena& keep) {
+  const vca_config& c = g->cfg;
+  const FxScales& fs = g->fxs;
+  const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+  SectorView sv = view_of(nup, ndw);
+  FxView fv = fx_view_of(nup, ndw);
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int nmax = (int)std::min<int64_t>(D, std::min(c.lanc_niter, 512));
+  Arena ar;
+  BatchBufs bb;
+  int rc = alloc_batch(ar, D, 1, false, 1, nmax + 1, bb);
+  if (rc) { ar.release(); return rc; }
+  double *theta, *svec, *resid, *invB, *norm2, *invn, *dtmp;
+  if ((rc = ar.alloc(&theta, 1)) || (rc = ar.alloc(&svec, 5 * (size_t)(nmax + 1))) ||
+      (rc = ar.alloc(&resid, 1)) || (rc = ar.alloc(&invB, nmax + 1)) || (rc = ar.alloc(&norm2, 1)) ||
+      (rc = ar.alloc(&invn, 1)) || (rc = ar.alloc(&dtmp, D))) {
+    ar.release();
+    return rc;
+  }
+  ChainMeta m0{1, 0, nmax, 1, 0};
+  int zero = 0;
+  cudaMemcpyAsync(bb.meta, &m0, sizeof(m0), cudaMemcpyHostToDevice, g->st);
+  cudaMemcpyAsync(bb.col2ch, &zero, sizeof(int), cudaMemcpyHostToDevice, g->st);
+  ColBatch cb{D, 1, false, 1, bb.col2ch, bb.meta};
+  auto start = [&](i64* X) {
+    launch_start_vector(D, c.start_seed, isector, dtmp, g->st);
+    launch_col_dot(cb, dtmp, dtmp, bb.partial, bb.nblk, norm2, g->st);
+    launch_chain_norm_init(1, bb.meta, norm2, invn, g->st);
+    launch_col_scale(cb, invn, dtmp, dtmp, g->st);
+    launch_fx_from_double(D, dtmp, fs.F, X, g->st);
+  };
+  start((i64*)bb.b[0]);
+  int mconv = 0;
+  double th = 0.0;
+  for (int k = 1; k <= nmax; k++) {
+    if ((rc = lanczos_step_fx(sv, fv, cb, bb, k, c.gf_beta_tol, nmax + 1))) { ar.release(); return rc; }
+    if (k % std::max(1, c.gs_check_every) == 0 || k == nmax) {
+      ChainMeta mh;
+      double bn;
+      cudaMemcpyAsync(&mh, bb.meta, sizeof(mh), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(&bn, bb.bnow, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+      CUCHK(cudaStreamSynchronize(g->st));
+      const int kk = mh.len;
+      if (kk < 1) { ar.release(); VFAIL(VCA_ERR_NUMERIC, "Lanczos start vector has zero norm"); }
+      launch_tri_lowest(bb.A, bb.Bt, kk, bn, theta, svec, resid, g->st);
+      double rs;
+      cudaMemcpyAsync(&th, theta, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(&rs, resid, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+      CUCHK(cudaStreamSynchronize(g->st));
+      if (!mh.active || rs <= c.gs_residual_tol * std::max(1.0, std::fabs(th)) || k == nmax) {
+        mconv = kk;
+        break;
+      }
+    }
+  }
+  // second pass: psi = sum_k s_k v_k from the stored coefficients
+  i64* psi;
+  if ((rc = keep.alloc(&psi, (size_t)D))) { ar.release(); return rc; }
+  CUCHK(cudaMemsetAsync(psi, 0, (size_t)D * sizeof(i64), g->st));
+  m0 = ChainMeta{1, 0, nmax, 1, 0};
+  cudaMemcpyAsync(bb.meta, &m0, sizeof(m0), cudaMemcpyHostToDevice, g->st);
+  launch_recip(nmax + 1, bb.Bt, invB, g->st);
+  i64* X = (i64*)bb.b[0];
+  i64* Xp = (i64*)bb.b[1];
+  i64* YW = (i64*)bb.b[2];
+  start(X);
+  for (int k = 1; k <= mconv; k++) {
+    launch_fx_psi_accum(D, svec, k - 1, X, psi, g->st);
+    if (k == mconv) break;
+    launch_hxv_fx(sv, fv, 1, X, YW, g->st);
+    launch_fx_coef(1, bb.A + (k - 1), 1.0, fs.C, bb.afx, g->st);
+    if (k > 1) launch_fx_coef(1, bb.Bt + (k - 1), 1.0, fs.C, bb.bfx, g->st);
+    launch_fx_update(cb, fs, bb.afx, bb.bfx, k > 1, X, Xp, YW, YW, g->st);
+    launch_fx_normalize(cb, fs, invB + k, YW, Xp, bb.scr, g->st);
+    i64* t = Xp;
+    Xp = X;
+    X = t;
+  }
+  launch_fx_dot(cb, psi, psi, fs.F, fs.F, (i64*)bb.partial, bb.nblk, norm2, g->st);
+  launch_chain_norm_init(1, bb.meta, norm2, invn, g->st);
+  launch_fx_rescale(cb, invn, fs.F, fs.F, psi, psi, bb.scr, g->st);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(g->st));
+  ar.release();
+  *E = th;
+  *vec_out = psi;
+  return VCA_OK;
+}
+
 // vca_diag_c at T=0 with LANC_METHOD="lanczos" (VCA_DIAG.f90:49-267)
 int diagonalize() {
   const vca_config& c = g->cfg;
@@ -510,7 +727,7 @@ int diagonalize() {
     double e;
     void* vec = nullptr;
     Arena tmp;
-    RCHK(sector_gs(isector, &e, &vec, tmp));
+    RCHK(g->fx ? sector_gs_fx(isector, &e, &vec, tmp) : sector_gs(isector, &e, &vec, tmp));
     g->sector_e[isector - 1] = e;
     // T=0 bookkeeping (VCA_DIAG.f90:224-236), list ordered by energy
     // (es_insert_state_c, VCA_EIGENSPACE.f90:167-216)
@@ -613,13 +830,25 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     cudaMemcpyAsync(d_wfac, wf.data(), sizeof(double2) * nch, cudaMemcpyHostToDevice, g->st);
     ColBatch cb{D, m, cplx, nch, bb.col2ch, bb.meta};
     // start vectors: gather from the ground state, normalise per chain
-    launch_chain_init(tv, g->sp[0][nup].dim, S.vec, cplx, nch, d_ci, m, cplx, bb.b[0], g->st);
-    launch_col_dot(cb, bb.b[0], bb.b[0], bb.partial, bb.nblk, norm2c, g->st);
-    launch_chain_sum(cb, norm2c, norm2, g->st);
-    launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
-    launch_col_scale(cb, invn, bb.b[0], bb.b[0], g->st);
-    for (int k = 1; k <= nlanc; k++)
-      if ((rc = lanczos_step(tv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
+    if (g->fx) {
+      const FxScales& fs = g->fxs;
+      FxView fv = fx_view_of(tup, tdw);
+      launch_chain_init_fx(tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, d_ci, m, (i64*)bb.b[0], g->st);
+      launch_fx_dot(cb, (i64*)bb.b[0], (i64*)bb.b[0], fs.F, fs.F, (i64*)bb.partial, bb.nblk, norm2c, g->st);
+      launch_chain_sum(cb, norm2c, norm2, g->st);
+      launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
+      launch_fx_rescale(cb, invn, fs.F, fs.F, (i64*)bb.b[0], (i64*)bb.b[0], bb.scr, g->st);
+      for (int k = 1; k <= nlanc; k++)
+        if ((rc = lanczos_step_fx(tv, fv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
+    } else {
+      launch_chain_init(tv, g->sp[0][nup].dim, S.vec, cplx, nch, d_ci, m, cplx, bb.b[0], g->st);
+      launch_col_dot(cb, bb.b[0], bb.b[0], bb.partial, bb.nblk, norm2c, g->st);
+      launch_chain_sum(cb, norm2c, norm2, g->st);
+      launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
+      launch_col_scale(cb, invn, bb.b[0], bb.b[0], g->st);
+      for (int k = 1; k <= nlanc; k++)
+        if ((rc = lanczos_step(tv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
+    }
     // poles and weights into the global chain table
     const int base = (int)g->chains.size();
     launch_chain_poles(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, g->zeta, d_work,
@@ -1251,14 +1480,15 @@ static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_com
   if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
   if (ncols < 1) VFAIL(VCA_ERR_ARG, "ncols must be >= 1");
   if (!is_complex && !g->real_model) VFAIL(VCA_ERR_ARG, "real vectors need a real Hamiltonian");
-  SectorView sv = view_of(sec_nup(isector), sec_ndw(isector));
-  if (is_complex) {
-    if (g->real_model)  // complex columns on a real H: (re, im) as two real columns
-      launch_hxv_real(sv, g->md, 2 * ncols, (const double*)d_v, (double*)d_hv, g->st);
-    else
-      launch_hxv_cplx(sv, g->md, ncols, (const double2*)d_v, (double2*)d_hv, g->st);
+  const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+  SectorView sv = view_of(nup, ndw);
+  const int m = (is_complex && g->real_model) ? 2 * ncols : ncols;
+  if (g->fx) {  // buffers hold fixed-point columns (scale 2^-F, unit norm)
+    launch_hxv_fx(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
+  } else if (is_complex && !g->real_model) {
+    launch_hxv_cplx(sv, g->md, ncols, (const double2*)d_v, (double2*)d_hv, g->st);
   } else {
-    launch_hxv_real(sv, g->md, ncols, (const double*)d_v, (double*)d_hv, g->st);
+    launch_hxv_real(sv, g->md, m, (const double*)d_v, (double*)d_hv, g->st);
   }
   CUCHK(cudaGetLastError());
   return VCA_OK;
@@ -1277,6 +1507,26 @@ int vca_gpu_hxv(int32_t isector, const double* v, double* hv) {
   double2 *dv, *dh;
   int rc;
   if ((rc = ar.alloc(&dv, D)) || (rc = ar.alloc(&dh, D))) { ar.release(); return rc; }
+  if (g->fx) {
+    // fixed point holds unit-norm vectors: scale by 1/||v||, convert, apply, undo
+    double nrm = 0.0;
+    for (int64_t i = 0; i < 2 * D; i++) nrm += v[i] * v[i];
+    nrm = std::sqrt(nrm);
+    if (nrm == 0.0) { ar.release(); std::memset(hv, 0, sizeof(double) * 2 * D); return VCA_OK; }
+    std::vector<double> vs(2 * D);
+    for (int64_t i = 0; i < 2 * D; i++) vs[i] = v[i] / nrm;
+    cudaMemcpyAsync(dv, vs.data(), sizeof(double2) * D, cudaMemcpyHostToDevice, g->st);
+    launch_fx_from_double(2 * D, (const double*)dv, g->fxs.F, (i64*)dh, g->st);
+    rc = hxv_cols(isector, dh, dv, 1, 1);
+    if (rc) { ar.release(); return rc; }
+    launch_fx_to_double(2 * D, (const i64*)dv, g->fxs.G, (double*)dh, g->st);
+    cudaMemcpyAsync(hv, dh, sizeof(double2) * D, cudaMemcpyDeviceToHost, g->st);
+    cudaError_t e = cudaStreamSynchronize(g->st);
+    ar.release();
+    if (e != cudaSuccess) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e));
+    for (int64_t i = 0; i < 2 * D; i++) hv[i] *= nrm;
+    return VCA_OK;
+  }
   cudaMemcpyAsync(dv, v, sizeof(double2) * D, cudaMemcpyHostToDevice, g->st);
   rc = vca_gpu_hxv_device(isector, dv, dh, 1);
   if (rc) { ar.release(); return rc; }
@@ -1341,6 +1591,14 @@ int vca_gpu_timer_stop(double* ms) {
   float f = 0.f;
   CUCHK(cudaEventElapsedTime(&f, g_t0, g_t1));
   if (ms) *ms = f;
+  return VCA_OK;
+}
+
+int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded");
+  if (fx) *fx = g->fx ? 1 : 0;
+  if (F) *F = g->fxs.F;
+  if (G) *G = g->fxs.G;
   return VCA_OK;
 }
 

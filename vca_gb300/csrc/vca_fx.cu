@@ -1,0 +1,302 @@
+// vca_fx.cu -- fixed-point (int64 / int128) Lanczos kernels for real
+// Hamiltonians on GB300.  See vca_fx.cuh for the number format.
+#include "vca_fx.cuh"
+
+#include <atomic>
+#include <cmath>
+
+namespace vca {
+
+void count_launch_external();
+
+typedef __int128 i128;
+typedef unsigned long long u64;
+
+static inline int nblk_fx(int64_t n, int threads, int cap = 152 * 16) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+// round-half-up arithmetic shift of an int128 by s >= 0
+__device__ __forceinline__ i64 rshift_round(i128 p, int s) {
+  if (s <= 0) return (i64)p;
+  p += ((i128)1) << (s - 1);
+  return (i64)(p >> s);
+}
+
+__device__ __forceinline__ double i128_to_double(i128 v, int scale_exp) {
+  const bool neg = v < 0;
+  unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const u64 hi = (u64)(u >> 64), lo = (u64)u;
+  double d = (double)hi * 18446744073709551616.0 + (double)lo;
+  d = ldexp(d, -scale_exp);
+  return neg ? -d : d;
+}
+
+// ---------------------------------------------------------------------------
+// tables
+// ---------------------------------------------------------------------------
+__global__ void k_fx_codes(int64_t n, const double2* amp, const double* classes, int K, signed char* code) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double a = amp[t].x;
+    const double mag = fabs(a);
+    int cls = 0;
+    for (int k = 0; k < K; k++)
+      if (classes[k] == mag) cls = k;
+    code[t] = (signed char)(cls | (a < 0.0 ? 0x80 : 0));
+  }
+}
+void launch_fx_codes(int dim, int width, const double2* amp, const double* classes, int K,
+                     signed char* code, cudaStream_t st) {
+  count_launch_external();
+  int64_t n = (int64_t)dim * width;
+  if (n == 0) return;
+  k_fx_codes<<<nblk_fx(n, 256), 256, 0, st>>>(n, amp, classes, K, code);
+}
+
+__global__ void k_fx_e1(int dim, const double2* e1, int A, i64* e1fx) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += gridDim.x * blockDim.x)
+    e1fx[r] = __double2ll_rn(ldexp(e1[r].x, A));
+}
+void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st) {
+  count_launch_external();
+  k_fx_e1<<<nblk_fx(dim, 256), 256, 0, st>>>(dim, e1, A, e1fx);
+}
+
+// ---------------------------------------------------------------------------
+// H x v in fixed point.  Same row/column mapping as the FP64 kernel; every hop
+// is an exact int64 add into the accumulator of its amplitude class.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ i64 mixed_fx(const FxView& f, unsigned u, unsigned d) {
+  i64 s = f.c0fx;
+  for (int o = 0; o < f.norb; o++) s += f.Ufx[o] * (i64)__popc(u & d & f.omask[o]);
+  int c = 0;
+  for (int o = 0; o < f.norb; o++)
+    for (int q = o + 1; q < f.norb; q++)
+      c += __popc(u & f.omask[o] & (d >> (q - o))) + __popc(u & f.omask[q] & (d << (q - o)));
+  return s + f.Ustfx * (i64)c;
+}
+
+template <int K>
+__device__ __forceinline__ void acc_hop(i64 (&S)[K], signed char code, i64 v) {
+  const i64 sv = (code < 0) ? -v : v;
+  if (K == 1) {
+    S[0] += sv;
+  } else {
+    const int cls = code & 3;
+#pragma unroll
+    for (int k = 0; k < K; k++) S[k] += (cls == k) ? sv : 0;
+  }
+}
+
+template <int K>
+__global__ void k_hxv_fx(SectorView sv, FxView fv, int m, const i64* __restrict__ X, i64* __restrict__ Y) {
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int CW = blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; i < D;
+       i += (int64_t)gridDim.x * blockDim.y) {
+    const int idw = (int)(i / sv.dimup);
+    const int iup = (int)(i - (int64_t)idw * sv.dimup);
+    const i64 dfx = fv.up_e1[iup] + fv.dw_e1[idw] +
+                    mixed_fx(fv, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
+    const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
+    const int64_t colbase = (int64_t)idw * sv.dimup;
+    for (int c = threadIdx.x; c < m; c += CW) {
+      i64 S[K];
+#pragma unroll
+      for (int k = 0; k < K; k++) S[k] = 0;
+      for (int h = 0; h < nu; h++) {
+        const int64_t o = (int64_t)h * sv.dimup + iup;
+        acc_hop<K>(S, fv.up_code[o], X[(colbase + sv.up_src[o]) * m + c]);
+      }
+      for (int h = 0; h < nd; h++) {
+        const int64_t o = (int64_t)h * sv.dimdw + idw;
+        acc_hop<K>(S, fv.dw_code[o], X[((int64_t)iup + (int64_t)sv.dw_src[o] * sv.dimup) * m + c]);
+      }
+      i128 p = (i128)dfx * X[i * m + c];
+#pragma unroll
+      for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
+      Y[i * m + c] = rshift_round(p, fv.shift);
+    }
+  }
+}
+
+static void col_shape_fx(int m, dim3& blk) {
+  int cw = 1;
+  while (cw < m && cw < 32) cw <<= 1;
+  blk = dim3(cw, 256 / cw, 1);
+}
+
+void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st) {
+  count_launch_external();
+  dim3 blk;
+  col_shape_fx(m, blk);
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int nb = nblk_fx(D, blk.y, 152 * 32);
+  switch (fv.K) {
+    case 1: k_hxv_fx<1><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    case 2: k_hxv_fx<2><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    case 3: k_hxv_fx<3><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    default: k_hxv_fx<4><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// exact dot products
+// ---------------------------------------------------------------------------
+__global__ void k_fx_dot(int64_t rows, int m, const i64* X, const i64* Y, i64* partial) {
+  extern __shared__ i128 shq[];
+  const int CW = blockDim.x, RB = blockDim.y;
+  const int c = blockIdx.y * CW + threadIdx.x;
+  i128 s = 0;
+  if (c < m)
+    for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB)
+      s += (i128)X[i * m + c] * Y[i * m + c];
+  shq[threadIdx.y * CW + threadIdx.x] = s;
+  __syncthreads();
+  for (int h = RB / 2; h > 0; h >>= 1) {
+    if (threadIdx.y < h) shq[threadIdx.y * CW + threadIdx.x] += shq[(threadIdx.y + h) * CW + threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.y == 0 && c < m) {
+    const i128 v = shq[threadIdx.x];
+    partial[2 * ((int64_t)blockIdx.x * m + c)] = (i64)(u64)v;
+    partial[2 * ((int64_t)blockIdx.x * m + c) + 1] = (i64)(v >> 64);
+  }
+}
+__global__ void k_fx_dot_reduce(int m, int nblk, const i64* partial, int scale_exp, double* out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+    i128 s = 0;
+    for (int b = 0; b < nblk; b++) {
+      const u64 lo = (u64)partial[2 * ((int64_t)b * m + c)];
+      const i64 hi = partial[2 * ((int64_t)b * m + c) + 1];
+      s += (i128)(((unsigned __int128)(u64)hi << 64) | lo);
+    }
+    out[c] = i128_to_double(s, scale_exp);
+  }
+}
+void launch_fx_dot(const ColBatch& b, const i64* X, const i64* Y, int sx, int sy, i64* partial, int nblk,
+                   double* out_col, cudaStream_t st) {
+  count_launch_external();
+  count_launch_external();
+  dim3 blk;
+  col_shape_fx(b.m, blk);
+  dim3 grd(nblk, (b.m + blk.x - 1) / blk.x, 1);
+  k_fx_dot<<<grd, blk, sizeof(i128) * 256, st>>>(b.rows, b.m, X, Y, partial);
+  k_fx_dot_reduce<<<nblk_fx(b.m, 128), 128, 0, st>>>(b.m, nblk, partial, sx + sy, out_col);
+}
+
+// ---------------------------------------------------------------------------
+// element updates
+// ---------------------------------------------------------------------------
+__global__ void k_fx_coef(int nch, const double* x, double scale, int C, i64* cfx) {
+  for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x)
+    cfx[ch] = __double2ll_rn(ldexp(scale * x[ch], C));
+}
+void launch_fx_coef(int nch, const double* x, double scale, int C, i64* cfx, cudaStream_t st) {
+  count_launch_external();
+  k_fx_coef<<<nblk_fx(nch, 128), 128, 0, st>>>(nch, x, scale, C, cfx);
+}
+
+__global__ void k_fx_update(int64_t rows, int m, const int* col2ch, const ChainMeta* meta, int sh,
+                            const i64* afx, const i64* bfx, int use_b, const i64* X, const i64* Xp,
+                            const i64* Y, i64* W) {
+  const int64_t n = rows * m;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(g % m);
+    const int ch = col2ch[c];
+    if (!meta[ch].active) continue;
+    i128 p = (i128)afx[ch] * X[g];
+    if (use_b) p += (i128)bfx[ch] * Xp[g];
+    W[g] = Y[g] - rshift_round(p, sh);
+  }
+}
+void launch_fx_update(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,
+                      const i64* X, const i64* Xp, const i64* Y, i64* W, cudaStream_t st) {
+  count_launch_external();
+  const int64_t n = b.rows * b.m;
+  k_fx_update<<<nblk_fx(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx, bfx,
+                                                use_b ? 1 : 0, X, Xp, Y, W);
+}
+
+// per-chain multiplier m = round(f * 2^E) < 2^61 and shift E + si - so
+__global__ void k_fx_mult(int nch, const double* f, int si, int so, i64* mul, i64* sh) {
+  for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
+    const double x = f[ch];
+    if (x == 0.0 || !isfinite(x)) { mul[ch] = 0; sh[ch] = 0; continue; }
+    int e;
+    frexp(fabs(x), &e);       // |x| in [2^(e-1), 2^e)
+    int E = 60 - e;           // |x| * 2^E < 2^60
+    int shift = E + si - so;
+    if (shift > 120) { E -= shift - 120; shift = 120; }
+    if (shift < 0) { E -= shift; shift = 0; }
+    mul[ch] = __double2ll_rn(ldexp(x, E));
+    sh[ch] = shift;
+  }
+}
+__global__ void k_fx_apply(int64_t rows, int m, const int* col2ch, const ChainMeta* meta, const i64* mul,
+                           const i64* sh, int zero_inactive, const i64* Xi, i64* Xo) {
+  const int64_t n = rows * m;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(g % m);
+    const int ch = col2ch[c];
+    if (!meta[ch].active) {
+      if (zero_inactive) Xo[g] = 0;
+      continue;
+    }
+    Xo[g] = rshift_round((i128)mul[ch] * Xi[g], (int)sh[ch]);
+  }
+}
+void launch_fx_normalize(const ColBatch& b, const FxScales& s, const double* invbeta, const i64* W,
+                         i64* X, i64* scratch, cudaStream_t st) {
+  count_launch_external();
+  count_launch_external();
+  k_fx_mult<<<nblk_fx(b.nch, 128), 128, 0, st>>>(b.nch, invbeta, s.G, s.F, scratch, scratch + b.nch);
+  const int64_t n = b.rows * b.m;
+  k_fx_apply<<<nblk_fx(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scratch, scratch + b.nch, 1, W, X);
+}
+void launch_fx_rescale(const ColBatch& b, const double* f, int si, int so, const i64* Xi, i64* Xo,
+                       i64* scratch, cudaStream_t st) {
+  count_launch_external();
+  count_launch_external();
+  k_fx_mult<<<nblk_fx(b.nch, 128), 128, 0, st>>>(b.nch, f, si, so, scratch, scratch + b.nch);
+  const int64_t n = b.rows * b.m;
+  k_fx_apply<<<nblk_fx(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scratch, scratch + b.nch, 0, Xi, Xo);
+}
+
+__global__ void k_fx_psi_accum(int64_t n, const double* s, int k, const i64* X, i64* psi) {
+  const i64 sfx = __double2ll_rn(ldexp(s[k], 61));  // |s| <= 1
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x)
+    psi[g] += rshift_round((i128)sfx * X[g], 61);
+}
+void launch_fx_psi_accum(int64_t n, const double* s, int k, const i64* X, i64* psi, cudaStream_t st) {
+  count_launch_external();
+  k_fx_psi_accum<<<nblk_fx(n, 256), 256, 0, st>>>(n, s, k, X, psi);
+}
+
+__global__ void k_fx_from_double(int64_t n, const double* x, int F, i64* X) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x)
+    X[g] = __double2ll_rn(ldexp(x[g], F));
+}
+void launch_fx_from_double(int64_t n, const double* x, int F, i64* X, cudaStream_t st) {
+  count_launch_external();
+  k_fx_from_double<<<nblk_fx(n, 256), 256, 0, st>>>(n, x, F, X);
+}
+__global__ void k_fx_to_double(int64_t n, const i64* X, int F, double* x) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x)
+    x[g] = ldexp((double)X[g], -F);
+}
+void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t st) {
+  count_launch_external();
+  k_fx_to_double<<<nblk_fx(n, 256), 256, 0, st>>>(n, X, F, x);
+}
+
+}  // namespace vca

@@ -1,0 +1,80 @@
+// vca_fx.cuh -- exact 64-bit fixed-point ("FX") Lanczos arithmetic for real
+// Hamiltonians.
+//
+// GB300 issues FP64 at ~0.5 T instructions/s but 64-bit integer adds ~50x
+// faster, so the real-Hamiltonian path keeps every Lanczos vector as int64
+// fixed point and does all per-element arithmetic on the integer pipes:
+//   * vectors v (norm 1):           V = round(v * 2^F)
+//   * H v, Lanczos residuals w:      Y = round(y * 2^G), G set from a bound on
+//                                    max_i sum_j |H_ij| so |Y| < 2^61
+//   * hop sums: amplitudes fall in K <= 4 magnitude classes; per element
+//     S_k = sum_{hops in k} (+/-)V[src] is an exact int64 sum, then
+//     Y = round((d_fx*V + sum_k a_fx[k]*S_k) / 2^(A+F-G)) with one rounding
+//     (int64 x int64 -> int128 products)
+//   * dot products are exact int128 sums (order independent, reproducible)
+// Scalars (alpha, beta) stay FP64; they enter the element updates as int64
+// fixed-point coefficients.
+#pragma once
+
+#include "vca_common.cuh"
+#include "vca_kernels.cuh"
+
+namespace vca {
+
+#define VCA_FX_KMAX 4
+
+typedef long long i64;
+
+struct FxScales {
+  int F;   // vector scale 2^-F
+  int G;   // H v / residual scale 2^-G
+  int A;   // diagonal and amplitude coefficients 2^-A
+  int C;   // alpha/beta coefficients 2^-C
+};
+
+struct FxView {
+  const signed char* up_code;  // [width*dim]: class (bits 0-1), sign (bit 7)
+  const signed char* dw_code;
+  const i64* up_e1;            // one-body + same-spin diagonal, scale 2^-A
+  const i64* dw_e1;
+  int K;
+  i64 afx[VCA_FX_KMAX];        // class amplitudes, scale 2^-A
+  int norb;
+  unsigned int omask[VCA_MAX_NORB];
+  i64 Ufx[VCA_MAX_NORB];
+  i64 Ustfx;
+  i64 c0fx;
+  int shift;                   // A + F - G
+};
+
+// per-hop class/sign codes from the FP64 amplitude tables
+void launch_fx_codes(int dim, int width, const double2* amp, const double* classes, int K,
+                     signed char* code, cudaStream_t st);
+// FP64 one-body table -> fixed point
+void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st);
+// Y = H X (FX) on a column batch
+void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st);
+// per-column exact dot: out_col[c] = (sum X*Y) * 2^-(sx+sy) (double)
+void launch_fx_dot(const ColBatch& b, const i64* X, const i64* Y, int sx, int sy, i64* partial, int nblk,
+                   double* out_col, cudaStream_t st);
+// per-chain coefficient to fixed point: cfx[ch] = round(scale * x[ch] * 2^C)
+void launch_fx_coef(int nch, const double* x, double scale, int C, i64* cfx, cudaStream_t st);
+// W = Y - (afx*X + bfx*Xp) >> (C+F-G)  (bfx ignored when use_b == 0)
+void launch_fx_update(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,
+                      const i64* X, const i64* Xp, const i64* Y, i64* W, cudaStream_t st);
+// normalisation: X = W / beta per chain (scale 2^-G -> 2^-F), zero for retired chains
+void launch_fx_normalize(const ColBatch& b, const FxScales& s, const double* invbeta, const i64* W,
+                         i64* X, i64* scratch2nch, cudaStream_t st);
+// generic per-chain scaling between scales: Xo = round(Xi * f[ch] * 2^(so - si))
+void launch_fx_rescale(const ColBatch& b, const double* f, int si, int so, const i64* Xi, i64* Xo,
+                       i64* scratch2nch, cudaStream_t st);
+// psi += s[k] * X (single column, scale 2^-F)
+void launch_fx_psi_accum(int64_t n, const double* s, int k, const i64* X, i64* psi, cudaStream_t st);
+// FP64 <-> fixed point (one-time conversions)
+void launch_fx_from_double(int64_t n, const double* x, int F, i64* X, cudaStream_t st);
+void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t st);
+// chain start vectors by exact gather (+/- psi, re/im columns) from a FX ground state
+void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const i64* gs, int nchain,
+                          const ChainInit* d_ci, int m, i64* X, cudaStream_t st);
+
+}  // namespace vca

@@ -12,6 +12,7 @@ namespace vca {
 static std::atomic<long long> g_launches{0};
 long long launch_count() { return g_launches.load(); }
 #define COUNT_LAUNCH() g_launches.fetch_add(1, std::memory_order_relaxed)
+void count_launch_external() { COUNT_LAUNCH(); }
 
 __constant__ int64_t c_binom[VCA_MAX_NS + 1][VCA_MAX_NS + 1];
 
@@ -1198,6 +1199,47 @@ __global__ void k_real_to_cplx(int64_t n, const double* in, double2* out) {
 void launch_real_to_cplx(int64_t n, const double* in, double2* out, cudaStream_t st) {
   COUNT_LAUNCH();
   k_real_to_cplx<<<nblocks(n, 256), 256, 0, st>>>(n, in, out);
+}
+
+
+// Fixed-point chain start vectors: the chain operators carry coefficients in
+// {+-1, +-i}, so the gather from a fixed-point ground state is exact.
+__global__ void k_chain_init_fx(SectorView tgt, int src_dimup, const long long* gs, int nchain,
+                                const ChainInit* ci, int m, long long* X) {
+  const int64_t D = (int64_t)tgt.dimup * tgt.dimdw;
+  const int64_t n = D * nchain;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int ch = (int)(g % nchain);
+    const int64_t i = g / nchain;
+    const int idw = (int)(i / tgt.dimup);
+    const int iup = (int)(i - (int64_t)idw * tgt.dimup);
+    const ChainInit c = ci[ch];
+    const unsigned w = (unsigned)(c.spin == 0 ? tgt.up_words[iup] : tgt.dw_words[idw]);
+    long long vr = 0, vi = 0;
+    for (int q = 0; q < c.nterm; q++) {
+      const int pos = c.t[q].pos;
+      const bool occ = (w >> pos) & 1u;
+      if (c.dag ? !occ : occ) continue;
+      const unsigned ws = w ^ (1u << pos);
+      const bool neg = __popc(ws & ((1u << pos) - 1u)) & 1;
+      const int rs = rank_word(ws);
+      const int64_t si = (c.spin == 0) ? ((int64_t)rs + (int64_t)idw * src_dimup)
+                                       : ((int64_t)iup + (int64_t)rs * src_dimup);
+      const long long gv = neg ? -gs[si] : gs[si];
+      const int cr = (int)c.t[q].re, cim = (int)c.t[q].im;  // in {-1,0,1}
+      vr += cr * gv;
+      vi += cim * gv;
+    }
+    X[i * m + c.col0] = vr;
+    if (c.cplxcol) X[i * m + c.col0 + 1] = vi;
+  }
+}
+void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long* gs, int nchain,
+                          const ChainInit* d_ci, int m, long long* X, cudaStream_t st) {
+  COUNT_LAUNCH();
+  int64_t n = (int64_t)tgt.dimup * tgt.dimdw * nchain;
+  k_chain_init_fx<<<nblocks(n, 256), 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, X);
 }
 
 }  // namespace vca

@@ -131,6 +131,10 @@ void launch_gauss_legendre(int n, double* x, double* w, cudaStream_t st);
 void launch_delta_bath(int nz, const double2* z, int N, int Nb, const double2* hb, const double2* V,
                        double xmu, double2* work, double2* out, cudaStream_t st);
 
+void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long* gs, int nchain,
+                          const ChainInit* d_ci, int m, long long* X, cudaStream_t st);
+void count_launch_external();
+
 // ---- helpers ---------------------------------------------------------------
 void launch_chain_norm_init(int nch, ChainMeta* meta, const double* norm2, double* invnorm,
                             cudaStream_t st);

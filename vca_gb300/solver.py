@@ -32,6 +32,7 @@ EXPORTS = [
     "vca_gpu_sector_map", "vca_gpu_set_hamiltonian", "vca_gpu_hxv", "vca_gpu_hxv_device",
     "vca_gpu_hxv_timed", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
+    "vca_gpu_arith_info",
 ]
 
 
@@ -86,6 +87,7 @@ def load(path: Optional[str] = None):
         "vca_gpu_synchronize": (ctypes.c_int, []),
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
+        "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -185,6 +187,11 @@ class VcaSolver:
         out = np.zeros(4)
         check(self.L.vca_gpu_get_timings(_dp(out), 4))
         return out
+
+    def arith_info(self):
+        fx, F, G = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(self.L.vca_gpu_arith_info(ctypes.byref(fx), ctypes.byref(F), ctypes.byref(G)))
+        return bool(fx.value), F.value, G.value
 
     def timer_start(self):
         check(self.L.vca_gpu_timer_start())
