@@ -197,7 +197,8 @@ def hxv_operand(s, D, m):
     x = torch.randn(D, m, dtype=torch.float64, device="cuda")
     x /= torch.linalg.vector_norm(x, dim=0, keepdim=True)
     if fx:
-        return torch.round(x * 2.0 ** F).to(torch.int64).reshape(-1), "k_hxv_fx"
+        name = "k_hxv_fx_a+k_hxv_fx_b" if (m >= 8 and s.cfg.hxv_variant == 2) else "k_hxv_fx"
+        return torch.round(x * 2.0 ** F).to(torch.int64).reshape(-1), name
     return x.reshape(-1), "k_hxv_real"
 
 
@@ -280,7 +281,7 @@ def run_gpu(args):
         bytes_alg = 16.0 * D * m
         peak, kind = measured_peaks()
         ach = bytes_alg / (t_ms / 1e3) / 1e9
-        traffic = profile_traffic(kname.replace("k_", "") + "_square4x3.md")
+        traffic = profile_traffic(kname.split("+")[0].replace("k_", "") + "_square4x3.md")
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic,
                 "kernel": kname, "launch_ms": round(t_ms, 4),
@@ -314,14 +315,16 @@ def run_gpu(args):
     return 0
 
 
-def profile_hxv(ncols: int, reps: int) -> int:
+def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
     """Batched H x v only (for ncu captures of the H x v kernel)."""
     import torch
     from vca_gb300 import build as vbuild
     vbuild.build()
     from vca_gb300.solver import VcaSolver
     pt = build_points()[5]
-    s = VcaSolver(pt.cfg)
+    cfg = pt.cfg.copy()
+    cfg.hxv_variant = variant
+    s = VcaSolver(cfg)
     s.set_hamiltonian(pt.Hloc)
     isec = 1 + 6 + 7 * 13
     _, _, du, dd = s.sector_info(isec)
@@ -367,9 +370,10 @@ def main():
                     help="profiling mode: one plain solve of a reduced 4x3 point "
                          "(8x8 k-grid, 1024 nodes) after one warm-up solve")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--hxv-variant", type=int, default=0, help="0/1 one pass, 2 two pass")
     args = ap.parse_args()
     if args.profile_hxv:
-        return profile_hxv(args.profile_hxv, args.reps)
+        return profile_hxv(args.profile_hxv, args.reps, args.hxv_variant)
     if args.profile_solve:
         return profile_solve()
     if args.impl == "reference":

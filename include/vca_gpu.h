@@ -101,7 +101,8 @@ typedef struct vca_config {
   double gf_beta_tol;      /* GF chain stop: beta_{k+1} < tol (exhausted)   */
   uint64_t start_seed;     /* seed of the deterministic Lanczos start vector */
   int32_t arith;           /* VCA_ARITH_AUTO | VCA_ARITH_FP64 | VCA_ARITH_FX   */
-  int32_t reserved[7];
+  int32_t hxv_variant;     /* FX column batches: 0/1 one pass, 2 two pass      */
+  int32_t reserved[6];
 } vca_config;
 
 /* Fill *cfg with the reference defaults (VCA_INPUT_VARS.f90:112-172) plus

@@ -59,7 +59,8 @@ class VcaConfig(ctypes.Structure):
         ("gf_beta_tol", ctypes.c_double),
         ("start_seed", ctypes.c_uint64),
         ("arith", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("hxv_variant", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
     def copy(self) -> "VcaConfig":
@@ -103,6 +104,7 @@ def default_config(**overrides) -> VcaConfig:
     c.gf_beta_tol = 1e-12
     c.start_seed = 20261203
     c.arith = ARITH_AUTO
+    c.hxv_variant = 0
     for k, v in overrides.items():
         if k == "Uloc":
             for i in range(5):

@@ -19,6 +19,14 @@ static inline int nblk_fx(int64_t n, int threads, int cap = 152 * 16) {
   return (int)b;
 }
 
+// 16-byte asynchronous global -> shared copies (sm_80+ cp.async): a CTA
+// issues its whole tile before waiting once, so many loads are in flight.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // round-half-up arithmetic shift of an int128 by s >= 0
 __device__ __forceinline__ i64 rshift_round(i128 p, int s) {
   if (s <= 0) return (i64)p;
@@ -297,6 +305,247 @@ __global__ void k_fx_to_double(int64_t n, const i64* X, int F, double* x) {
 void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t st) {
   count_launch_external();
   k_fx_to_double<<<nblk_fx(n, 256), 256, 0, st>>>(n, X, F, x);
+}
+
+
+// ---------------------------------------------------------------------------
+// Two-pass H x v on column batches (fixed point).
+//
+// Pass A (up hops + diagonal): one CTA per (idw, column chunk); the block
+// X[:, idw, chunk] (DimUp x CW int64, <= 200 KB) is staged in shared memory,
+// so every up hop is a shared-memory load and X is read from DRAM once.
+// Pass B (down hops): one CTA per (iup, column chunk); X[iup, :, chunk]
+// (DimDw x CW) is staged likewise, Y is completed in place and the exact
+// int128 partial of alpha = <X, Y> is written per (iup, column).
+// DRAM per column element: A reads X, writes Y (16 B); B reads X, Y and
+// writes Y (24 B).
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(256) k_hxv_fx_a(SectorView sv, FxView fv, int m, int cw,
+                                                  const i64* __restrict__ X, i64* __restrict__ Y) {
+  extern __shared__ i64 xs[];  // [DimUp][cw]
+  const int nchunk = (m + cw - 1) / cw;
+  const int idw = blockIdx.x / nchunk;
+  const int c0 = (blockIdx.x % nchunk) * cw;
+  const int ncol = min(cw, m - c0);
+  const int DU = sv.dimup;
+  const int64_t base = (int64_t)idw * DU;
+  if ((m & 1) == 0 && (ncol & 1) == 0 && (cw & 1) == 0) {
+    // pairs of int64 = 16 B; row starts (base+r)*m + c0 are even -> aligned
+    const int hp = cw >> 1, hn = ncol >> 1;
+    for (int t = threadIdx.x; t < DU * hp; t += blockDim.x) {
+      const int r = t / hp, q = t - r * hp;
+      if (q < hn) cp_async16(xs + r * cw + 2 * q, X + (base + r) * m + c0 + 2 * q);
+      else { xs[r * cw + 2 * q] = 0; xs[r * cw + 2 * q + 1] = 0; }
+    }
+    cp_async_wait_all();
+  } else {
+    for (int t = threadIdx.x; t < DU * cw; t += blockDim.x) {
+      const int r = t / cw, cc = t - r * cw;
+      xs[t] = (cc < ncol) ? X[(base + r) * m + c0 + cc] : 0;
+    }
+  }
+  __syncthreads();
+  const i64 edw = fv.dw_e1[idw];
+  const unsigned wd = (unsigned)sv.dw_words[idw];
+  for (int t = threadIdx.x; t < DU * cw; t += blockDim.x) {
+    const int r = t / cw, cc = t - r * cw;
+    if (cc >= ncol) continue;
+    const i64 dfx = fv.up_e1[r] + edw + mixed_fx(fv, (unsigned)sv.up_words[r], wd);
+    i64 S[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) S[k] = 0;
+    const int nu = sv.up_cnt[r];
+    for (int h = 0; h < nu; h++) {
+      const int64_t o = (int64_t)h * DU + r;
+      acc_hop<K>(S, fv.up_code[o], xs[sv.up_src[o] * cw + cc]);
+    }
+    i128 p = (i128)dfx * xs[t];
+#pragma unroll
+    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
+    Y[(base + r) * m + c0 + cc] = rshift_round(p, fv.shift);
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) k_hxv_fx_b(SectorView sv, FxView fv, int m, int cw,
+                                                  const i64* __restrict__ X, i64* __restrict__ Y,
+                                                  i64* __restrict__ apart) {
+  extern __shared__ i64 xs[];  // [DimDw][cw]
+  __shared__ i128 red[256];
+  const int nchunk = (m + cw - 1) / cw;
+  const int iup = blockIdx.x / nchunk;
+  const int c0 = (blockIdx.x % nchunk) * cw;
+  const int ncol = min(cw, m - c0);
+  const int DU = sv.dimup, DD = sv.dimdw;
+  if ((m & 1) == 0 && (ncol & 1) == 0 && (cw & 1) == 0) {
+    const int hp = cw >> 1, hn = ncol >> 1;
+    for (int t = threadIdx.x; t < DD * hp; t += blockDim.x) {
+      const int r = t / hp, q = t - r * hp;
+      if (q < hn) cp_async16(xs + r * cw + 2 * q, X + ((int64_t)iup + (int64_t)r * DU) * m + c0 + 2 * q);
+      else { xs[r * cw + 2 * q] = 0; xs[r * cw + 2 * q + 1] = 0; }
+    }
+    cp_async_wait_all();
+  } else {
+    for (int t = threadIdx.x; t < DD * cw; t += blockDim.x) {
+      const int r = t / cw, cc = t - r * cw;
+      xs[t] = (cc < ncol) ? X[((int64_t)iup + (int64_t)r * DU) * m + c0 + cc] : 0;
+    }
+  }
+  __syncthreads();
+  // thread t always handles column t % cw (blockDim is a multiple of cw)
+  i128 adot = 0;
+  for (int t = threadIdx.x; t < DD * cw; t += blockDim.x) {
+    const int r = t / cw, cc = t - r * cw;
+    if (cc >= ncol) continue;
+    i64 S[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) S[k] = 0;
+    const int nd = sv.dw_cnt[r];
+    for (int h = 0; h < nd; h++) {
+      const int64_t o = (int64_t)h * DD + r;
+      acc_hop<K>(S, fv.dw_code[o], xs[sv.dw_src[o] * cw + cc]);
+    }
+    i128 p = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
+    const int64_t g = ((int64_t)iup + (int64_t)r * DU) * m + c0 + cc;
+    const i64 y = Y[g] + rshift_round(p, fv.shift);
+    Y[g] = y;
+    adot += (i128)xs[t] * y;
+  }
+  red[threadIdx.x] = adot;
+  __syncthreads();
+  if ((int)threadIdx.x < cw) {
+    i128 s = 0;
+    for (int q = threadIdx.x; q < (int)blockDim.x; q += cw) s += red[q];
+    if ((int)threadIdx.x < ncol) {
+      const int64_t o = 2 * ((int64_t)iup * m + c0 + threadIdx.x);
+      apart[o] = (i64)(u64)s;
+      apart[o + 1] = (i64)(s >> 64);
+    }
+  }
+}
+
+// sum of int128 partials over `rows` rows per column -> double (scale 2^-sexp)
+__global__ void k_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+    i128 s = 0;
+    for (int b = 0; b < rows; b++) {
+      const u64 lo = (u64)partial[2 * ((int64_t)b * m + c)];
+      const i64 hi = partial[2 * ((int64_t)b * m + c) + 1];
+      s += (i128)(((unsigned __int128)(u64)hi << 64) | lo);
+    }
+    out[c] = i128_to_double(s, sexp);
+  }
+}
+
+int hxv_fx_chunk(int rows, int m) {
+  const int budget = 100 * 1024 / 8;  // int64 slots: <= 100 KB so two CTAs share an SM
+  int cw = 32;
+  while (cw > 1 && (cw >= 2 * m || rows * cw > budget)) cw >>= 1;
+  if (rows * cw > budget) return 0;  // a single column does not fit
+  return cw;
+}
+
+bool launch_hxv_fx2(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                    cudaStream_t st) {
+  const int cwa = hxv_fx_chunk(sv.dimup, m), cwb = hxv_fx_chunk(sv.dimdw, m);
+  if (!cwa || !cwb) return false;
+  const size_t sha = (size_t)sv.dimup * cwa * sizeof(i64), shb = (size_t)sv.dimdw * cwb * sizeof(i64);
+  const int ga = sv.dimdw * ((m + cwa - 1) / cwa), gb = sv.dimup * ((m + cwb - 1) / cwb);
+  count_launch_external();
+  count_launch_external();
+#define VCA_FX2(KK)                                                                                  \
+  {                                                                                                  \
+    static bool attr = false;                                                                        \
+    if (!attr) {                                                                                     \
+      cudaFuncSetAttribute(k_hxv_fx_a<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 104 * 1024); \
+      cudaFuncSetAttribute(k_hxv_fx_b<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 104 * 1024); \
+      attr = true;                                                                                   \
+    }                                                                                                \
+  }                                                                                                  \
+  k_hxv_fx_a<KK><<<ga, 256, sha, st>>>(sv, fv, m, cwa, X, Y);                                        \
+  k_hxv_fx_b<KK><<<gb, 256, shb, st>>>(sv, fv, m, cwb, X, Y, apart);
+  switch (fv.K) {
+    case 1: VCA_FX2(1) break;
+    case 2: VCA_FX2(2) break;
+    case 3: VCA_FX2(3) break;
+    default: VCA_FX2(4) break;
+  }
+#undef VCA_FX2
+  return true;
+}
+
+void launch_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out, cudaStream_t st) {
+  count_launch_external();
+  k_fx_partial_reduce<<<nblk_fx(m, 128), 128, 0, st>>>(m, rows, partial, sexp, out);
+}
+
+// W = Y - (afx*X + bfx*Xp) >> sh in place of Y, with the exact int128 partial
+// of beta^2 = <W, W> per (block, column); retired chains are left untouched.
+__global__ void k_fx_update_dot(int64_t rows, int m, const int* col2ch, const ChainMeta* meta, int sh,
+                                const i64* afx, const i64* bfx, int use_b, const i64* X, const i64* Xp,
+                                i64* YW, i64* partial) {
+  extern __shared__ i128 shq[];
+  const int CW = blockDim.x, RB = blockDim.y;
+  const int c = blockIdx.y * CW + threadIdx.x;
+  i128 s = 0;
+  if (c < m) {
+    const int ch = col2ch[c];
+    if (meta[ch].active) {
+      const i64 a = afx[ch], b = use_b ? bfx[ch] : 0;
+      for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB) {
+        const int64_t g = i * m + c;
+        i128 p = (i128)a * X[g];
+        if (use_b) p += (i128)b * Xp[g];
+        const i64 w = YW[g] - rshift_round(p, sh);
+        YW[g] = w;
+        s += (i128)w * w;
+      }
+    }
+  }
+  shq[threadIdx.y * CW + threadIdx.x] = s;
+  __syncthreads();
+  for (int h = RB / 2; h > 0; h >>= 1) {
+    if (threadIdx.y < h) shq[threadIdx.y * CW + threadIdx.x] += shq[(threadIdx.y + h) * CW + threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.y == 0 && c < m) {
+    const i128 v = shq[threadIdx.x];
+    partial[2 * ((int64_t)blockIdx.x * m + c)] = (i64)(u64)v;
+    partial[2 * ((int64_t)blockIdx.x * m + c) + 1] = (i64)(v >> 64);
+  }
+}
+void launch_fx_update_dot(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,
+                          const i64* X, const i64* Xp, i64* YW, i64* partial, int nblk, double* out_col,
+                          cudaStream_t st) {
+  count_launch_external();
+  dim3 blk;
+  col_shape_fx(b.m, blk);
+  dim3 grd(nblk, (b.m + blk.x - 1) / blk.x, 1);
+  k_fx_update_dot<<<grd, blk, sizeof(i128) * 256, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx,
+                                                        bfx, use_b ? 1 : 0, X, Xp, YW, partial);
+  launch_fx_partial_reduce(b.m, nblk, partial, 2 * s.G, out_col, st);
+}
+
+
+// start vector in fixed point: R_i = round(v_i * 2^40) with v_i the
+// splitmix64 value of (seed, sector, index) in [-1, 1)
+__global__ void k_fx_start_raw(int64_t n, uint64_t seed, int isector, i64* R) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed + 0xD1B54A32D192ED03ull * (uint64_t)isector + (uint64_t)i + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    const double v = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    R[i] = __double2ll_rn(ldexp(v, 40));
+  }
+}
+void launch_fx_start_raw(int64_t n, uint64_t seed, int isector, i64* R, cudaStream_t st) {
+  count_launch_external();
+  k_fx_start_raw<<<nblk_fx(n, 256), 256, 0, st>>>(n, seed, isector, R);
 }
 
 }  // namespace vca

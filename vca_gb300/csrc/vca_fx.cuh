@@ -77,4 +77,19 @@ void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const i64* gs, int nchain,
                           const ChainInit* d_ci, int m, i64* X, cudaStream_t st);
 
+// two-pass H x v (shared-memory staged up and down blocks) with the exact
+// alpha partials <X,Y> per (iup, column) in apart[2*DimUp*m]; returns false
+// when a column block does not fit in shared memory
+bool launch_hxv_fx2(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                    cudaStream_t st);
+int hxv_fx_chunk(int rows, int m);
+void launch_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out, cudaStream_t st);
+// fused W = Y - a X - b Xp and beta^2 partials (out_col = <W,W> per column)
+void launch_fx_update_dot(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,
+                          const i64* X, const i64* Xp, i64* YW, i64* partial, int nblk, double* out_col,
+                          cudaStream_t st);
+
+// start vector R = round(v * 2^40), v the splitmix64 values of the FP64 path
+void launch_fx_start_raw(int64_t n, uint64_t seed, int isector, i64* R, cudaStream_t st);
+
 }  // namespace vca

@@ -2,6 +2,7 @@
 // path (GB300).  Every grid is bounded by its buffers: grid-stride loops over
 // explicit 64-bit extents, no device-side waits.
 #include "vca_kernels.cuh"
+#include "vca_tri.cuh"
 
 #include <cmath>
 #include <atomic>
@@ -480,118 +481,11 @@ void launch_fill(int64_t n, double v, double* X, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// Lowest eigenpair of the Lanczos T_k: warp multisection on the Sturm count
-// (33 points a round) then inverse iteration with a partially pivoted
-// tridiagonal LU (Wilkinson ch. 5).  Residual estimate |beta_{k+1} s_k|.
+// Lowest eigenpair of the Lanczos T_k (one warp, vca_tri.cuh)
 // ---------------------------------------------------------------------------
-__device__ int sturm_count_dev(const double* a, const double* b1, int k, double x) {
-  // b1[j] = beta_{j+1} for j >= 1 (off-diagonal between rows j-1 and j)
-  int cnt = 0;
-  double q = a[0] - x;
-  if (q < 0) cnt++;
-  for (int j = 1; j < k; j++) {
-    if (q == 0.0) q = 1e-300;
-    q = a[j] - x - b1[j] * b1[j] / q;
-    if (q < 0) cnt++;
-  }
-  return cnt;
-}
-
 __global__ void k_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta_out,
                              double* s, double* resid) {
-  __shared__ double lo_s, hi_s;
-  __shared__ int first_s;
-  const int lane = threadIdx.x;
-  if (lane == 0) {
-    double lo = A[0], hi = A[0];
-    for (int j = 0; j < k; j++) {
-      double r = (j > 0 ? fabs(Bt[j]) : 0.0) + (j < k - 1 ? fabs(Bt[j + 1]) : 0.0);
-      lo = fmin(lo, A[j] - r);
-      hi = fmax(hi, A[j] + r);
-    }
-    lo_s = lo;
-    hi_s = hi;
-  }
-  __syncthreads();
-  for (int round = 0; round < 100; round++) {
-    double lo = lo_s, hi = hi_s;
-    double x = lo + (hi - lo) * (double)(lane + 1) / 33.0;
-    int c = (x > lo && x < hi) ? sturm_count_dev(A, Bt, k, x) : (x >= hi ? 1 : 0);
-    unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
-    __syncthreads();
-    if (lane == 0) {
-      int f = ball ? (__ffs(ball) - 1) : 32;  // first point with count >= 1
-      double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 33.0;
-      double nhi = (f == 32) ? hi : lo + (hi - lo) * (double)(f + 1) / 33.0;
-      if (nlo < lo) nlo = lo;
-      if (nhi > hi) nhi = hi;
-      first_s = (nhi - nlo <= 2.220446049250313e-16 * fmax(fabs(nlo), fabs(nhi)) || !(nlo < nhi) ||
-                 (nlo == lo && nhi == hi)) ? 1 : 0;
-      lo_s = nlo;
-      hi_s = nhi;
-    }
-    __syncthreads();
-    if (first_s) break;
-  }
-  if (lane != 0) return;
-  // refine to adjacent doubles by plain bisection (a handful of steps)
-  double lo = lo_s, hi = hi_s;
-  for (int it = 0; it < 200; it++) {
-    double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (sturm_count_dev(A, Bt, k, mid) >= 1) hi = mid; else lo = mid;
-  }
-  const double th = 0.5 * (lo + hi);
-  theta_out[0] = th;
-  // inverse iteration: s <- (T - th)^{-1} s, 3 steps (dgttrf/dgttrs restated)
-  double* y = s;
-  for (int j = 0; j < k; j++) y[j] = 1.0;
-  if (k == 1) {
-    y[0] = 1.0;
-    resid[0] = fabs(btail);
-    return;
-  }
-  // local work lives in s[k..5k) of the caller-provided buffer
-  double* dl = s + k;
-  double* dd = s + 2 * k;
-  double* du = s + 3 * k;
-  double* du2 = s + 4 * k;
-  for (int it = 0; it < 3; it++) {
-    for (int j = 0; j < k; j++) dd[j] = A[j] - th;
-    for (int j = 0; j < k - 1; j++) { dl[j] = Bt[j + 1]; du[j] = Bt[j + 1]; du2[j] = 0.0; }
-    unsigned long long pivbits[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // k <= 512
-    for (int j = 0; j < k - 1; j++) {
-      if (fabs(dd[j]) >= fabs(dl[j])) {
-        if (dd[j] == 0.0) dd[j] = 1e-300;
-        double f = dl[j] / dd[j];
-        dl[j] = f;
-        dd[j + 1] -= f * du[j];
-      } else {
-        double f = dd[j] / dl[j];
-        dd[j] = dl[j];
-        dl[j] = f;
-        double t = du[j];
-        du[j] = dd[j + 1];
-        dd[j + 1] = t - f * dd[j + 1];
-        if (j < k - 2) { du2[j] = du[j + 1]; du[j + 1] = -f * du[j + 1]; }
-        pivbits[j >> 6] |= 1ull << (j & 63);
-      }
-    }
-    if (dd[k - 1] == 0.0) dd[k - 1] = 1e-300;
-    for (int j = 0; j < k - 1; j++) {
-      if (!((pivbits[j >> 6] >> (j & 63)) & 1ull)) y[j + 1] -= dl[j] * y[j];
-      else { double t = y[j]; y[j] = y[j + 1]; y[j + 1] = t - dl[j] * y[j]; }
-    }
-    y[k - 1] /= dd[k - 1];
-    y[k - 2] = (y[k - 2] - du[k - 2] * y[k - 1]) / dd[k - 2];
-    for (int j = k - 3; j >= 0; j--) y[j] = (y[j] - du[j] * y[j + 1] - du2[j] * y[j + 2]) / dd[j];
-    double nr = 0.0;
-    for (int j = 0; j < k; j++) nr += y[j] * y[j];
-    nr = sqrt(nr);
-    for (int j = 0; j < k; j++) y[j] /= nr;
-  }
-  if (y[0] < 0) for (int j = 0; j < k; j++) y[j] = -y[j];
-  resid[0] = fabs(btail * y[k - 1]);
+  warp_tri_lowest(A, Bt, k, btail, theta_out, s, resid);
 }
 void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta,
                        double* s, double* resid, cudaStream_t st) {
@@ -1240,6 +1134,169 @@ void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long*
   COUNT_LAUNCH();
   int64_t n = (int64_t)tgt.dimup * tgt.dimdw * nchain;
   k_chain_init_fx<<<nblocks(n, 256), 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, X);
+}
+
+
+// ---------------------------------------------------------------------------
+// Omega integrand, lane-parallel form.  Per (w, k, spin block) one warp:
+//  A = M G with M = P_w - Hk_k restricted to the union sparsity pattern of
+//  M over all k (rowptr/cols, within-block columns), one lane per element;
+//  ln|det(1+A)| by LU with the trailing update spread over all 32 lanes.
+//  ||A||_inf < 1/2: no pivoting, identity implicit, prod |1+a_kk|^2 = 1+delta
+//  tracked as delta' = delta + x + delta*x, one log1p at the end.  Otherwise
+//  partial pivoting with prod |u_kk|^2 kept as mantissa * 2^e (frexp), one
+//  log at the end.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, const double2* P,
+                                                     const double2* Glso, int64_t Nk, const double2* Hk,
+                                                     const int* rowptr, const int* cols, double* fpart,
+                                                     int kchunks) {
+  extern __shared__ double2 shm[];
+  const int w = blockIdx.y;
+  const int chunk = blockIdx.x;
+  const int NN = N * N;
+  double2* Gs = shm;
+  double2* Ps = shm + NN;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  double2* Aw = shm + 2 * NN + (int64_t)warp * nb * nb;
+  for (int t = threadIdx.x; t < NN; t += blockDim.x) {
+    Gs[t] = Glso[(int64_t)w * NN + t];
+    Ps[t] = P[(int64_t)w * NN + t];
+  }
+  __syncthreads();
+  const int64_t k0 = (Nk * chunk) / kchunks, k1 = (Nk * (chunk + 1)) / kchunks;
+  double acc = 0.0;
+  const int64_t ntask = (k1 - k0) * nblk;
+  const int nbb = nb * nb;
+  for (int64_t task = warp; task < ntask; task += nwarps) {
+    const int64_t k = k0 + task / nblk;
+    const int off = (int)(task % nblk) * nb;
+    const double2* H = Hk + k * NN;
+    double rmax = 0.0;
+    for (int e = lane; e < nbb; e += 32) {  // A(i,j), i fastest across lanes
+      const int i = e % nb, j = e / nb;
+      const int gi = off + i;
+      double sr = 0.0, si = 0.0;
+      for (int q = rowptr[gi]; q < rowptr[gi + 1]; q++) {
+        const int gl = cols[q];
+        const int il = gi + gl * N;
+        const double mr = Ps[il].x - H[il].x, mi = Ps[il].y - H[il].y;
+        const double2 gg = Gs[gl + (off + j) * N];
+        sr = fma(mr, gg.x, sr);
+        sr = fma(-mi, gg.y, sr);
+        si = fma(mr, gg.y, si);
+        si = fma(mi, gg.x, si);
+      }
+      Aw[e] = make_double2(sr, si);
+    }
+    __syncwarp();
+    if (lane < nb)
+      for (int j = 0; j < nb; j++) {
+        const double2 a = Aw[lane + j * nb];
+        rmax += fabs(a.x) + fabs(a.y);  // >= sum |a_ij|: a safe bound for the branch
+      }
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    double ld;
+    if (rmax < 0.5) {
+      double delta = 0.0;
+      for (int kk = 0; kk < nb; kk++) {
+        const double2 akk = Aw[kk + kk * nb];
+        const double pr = 1.0 + akk.x, pim = akk.y;
+        const double x = 2.0 * akk.x + akk.x * akk.x + akk.y * akk.y;
+        delta = delta + x + delta * x;
+        const double den = pr * pr + pim * pim;
+        const double ir = pr / den, ii = -pim / den;  // 1/pivot
+        for (int i = kk + 1 + lane; i < nb; i += 32) {
+          const double2 a = Aw[i + kk * nb];
+          Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
+        }
+        __syncwarp();
+        const int r = nb - kk - 1;
+        for (int e = lane; e < r * r; e += 32) {
+          const int i = kk + 1 + e % r, j = kk + 1 + e / r;
+          const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
+          double2& t = Aw[i + j * nb];
+          t.x -= l.x * u.x - l.y * u.y;
+          t.y -= l.x * u.y + l.y * u.x;
+        }
+        __syncwarp();
+      }
+      ld = 0.5 * log1p(delta);
+    } else {
+      for (int i = lane; i < nb; i += 32) Aw[i + i * nb].x += 1.0;
+      __syncwarp();
+      double mant = 1.0;
+      int ex = 0;
+      bool zero = false;
+      for (int kk = 0; kk < nb; kk++) {
+        double mag = -1.0;
+        int arg = kk;
+        if (lane >= kk && lane < nb) {
+          const double2 a = Aw[lane + kk * nb];
+          mag = a.x * a.x + a.y * a.y;
+          arg = lane;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          const double om = __shfl_xor_sync(0xffffffffu, mag, o);
+          const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+          if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
+        }
+        if (mag == 0.0) { zero = true; break; }
+        if (arg != kk)
+          for (int j = lane; j < nb; j += 32) {
+            const double2 t = Aw[kk + j * nb];
+            Aw[kk + j * nb] = Aw[arg + j * nb];
+            Aw[arg + j * nb] = t;
+          }
+        __syncwarp();
+        const double2 piv = Aw[kk + kk * nb];
+        int e2;
+        mant = frexp(mant * mag, &e2);
+        ex += e2;
+        const double ir = piv.x / mag, ii = -piv.y / mag;
+        for (int i = kk + 1 + lane; i < nb; i += 32) {
+          const double2 a = Aw[i + kk * nb];
+          Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
+        }
+        __syncwarp();
+        const int r = nb - kk - 1;
+        for (int e = lane; e < r * r; e += 32) {
+          const int i = kk + 1 + e % r, j = kk + 1 + e / r;
+          const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
+          double2& t = Aw[i + j * nb];
+          t.x -= l.x * u.x - l.y * u.y;
+          t.y -= l.x * u.y + l.y * u.x;
+        }
+        __syncwarp();
+      }
+      ld = zero ? -INFINITY : 0.5 * (log(mant) + ex * 0.6931471805599453);
+    }
+    if (lane == 0) acc += ld;
+    __syncwarp();
+  }
+  __shared__ double red[32];
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int q = 0; q < nwarps; q++) sacc += red[q];
+    fpart[(int64_t)w * kchunks + chunk] = sacc;
+  }
+}
+void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
+                        const double2* Hk, const int* rowptr, const int* cols, double* fpart, int kchunks,
+                        cudaStream_t st) {
+  COUNT_LAUNCH();
+  const int threads = 128;
+  size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_omega_ksum2, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    attr = true;
+  }
+  dim3 grd(kchunks, nw, 1);
+  k_omega_ksum2<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, rowptr, cols, fpart, kchunks);
 }
 
 }  // namespace vca

@@ -123,6 +123,11 @@ void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, doub
 // Omega integrand: f[w] = (1/Lk) sum_k ln|det(1 + (P_w - Hk_k) G_w)| per spin block
 void launch_omega_ksum(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso,
                        int64_t Nk, const double2* Hk, double* fpart, int kchunks, cudaStream_t st);
+// same integrand with M = P - Hk on a sparse row pattern (rowptr/cols, lso
+// indices) and all lanes of a warp on the products and the LU updates
+void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
+                        const double2* Hk, const int* rowptr, const int* cols, double* fpart, int kchunks,
+                        cudaStream_t st);
 void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out,
                         cudaStream_t st);
 // Gauss-Legendre nodes on (0,1)

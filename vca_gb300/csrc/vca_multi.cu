@@ -1,0 +1,329 @@
+// vca_multi.cu -- all sectors' ground-state Lanczos in one batched loop
+// (fixed-point path).
+//
+// The reference diagonalises the (N_up, N_dw) sectors one after the other
+// (VCA_DIAG.f90:83-249).  Most sectors are small, so a sector-at-a-time GPU
+// loop is launch bound.  Here the vectors of every sector of a group are
+// packed back to back and cut into tiles of MS_TILE elements; each Lanczos
+// phase is one launch over all tiles (a tile -> sector work table), the
+// per-sector scalars are reduced by one thread per sector, and the
+// convergence test of every sector is one warp per sector.  The arithmetic is
+// the same fixed-point arithmetic as the single-sector kernels, and every
+// reduction is an exact int128 sum, so each sector gets bitwise the same
+// alpha/beta sequence as when it runs alone.
+#include "vca_multi.cuh"
+#include "vca_tri.cuh"
+
+namespace vca {
+
+void count_launch_external();
+
+typedef __int128 i128;
+typedef unsigned long long u64;
+
+__device__ __forceinline__ i64 ms_rshift(i128 p, int s) {
+  if (s <= 0) return (i64)p;
+  p += ((i128)1) << (s - 1);
+  return (i64)(p >> s);
+}
+__device__ __forceinline__ double ms_i128_to_double(i128 v, int scale_exp) {
+  const bool neg = v < 0;
+  unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const u64 hi = (u64)(u >> 64), lo = (u64)u;
+  double d = (double)hi * 18446744073709551616.0 + (double)lo;
+  d = ldexp(d, -scale_exp);
+  return neg ? -d : d;
+}
+__device__ __forceinline__ uint64_t ms_splitmix64(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ i64 ms_mixed(const FxView& f, unsigned u, unsigned d) {
+  i64 s = f.c0fx;
+  for (int o = 0; o < f.norb; o++) s += f.Ufx[o] * (i64)__popc(u & d & f.omask[o]);
+  int c = 0;
+  for (int o = 0; o < f.norb; o++)
+    for (int q = o + 1; q < f.norb; q++)
+      c += __popc(u & f.omask[o] & (d >> (q - o))) + __popc(u & f.omask[q] & (d << (q - o)));
+  return s + f.Ustfx * (i64)c;
+}
+
+// block reduction of an int128 per-thread value into tpart[t] (2 x int64)
+__device__ __forceinline__ void ms_block_store(i128 v, i64* tpart, int t) {
+  __shared__ i128 red[256];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    tpart[2 * t] = (i64)(u64)red[0];
+    tpart[2 * t + 1] = (i64)(red[0] >> 64);
+  }
+  __syncthreads();
+}
+__device__ __forceinline__ i128 ms_sum_parts(const i64* tpart, int t0, int n) {
+  i128 s = 0;
+  for (int t = t0; t < t0 + n; t++)
+    s += (i128)(((unsigned __int128)(u64)tpart[2 * t + 1] << 64) | (u64)tpart[2 * t]);
+  return s;
+}
+
+// start vector: R_i = round(v_i * 2^40) with v_i the splitmix64 value of the
+// single-sector path; tpart = sum R^2
+__global__ void k_ms_start_raw(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
+                               uint64_t seed, i64* R, i64* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const MsSector& S = secs[tsec[t]];
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    i128 acc = 0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const uint64_t z = ms_splitmix64(seed + 0xD1B54A32D192ED03ull * (uint64_t)S.isector + (uint64_t)i);
+      const double v = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+      const i64 r = __double2ll_rn(ldexp(v, 40));
+      R[S.off + i] = r;
+      acc += (i128)r * r;
+    }
+    ms_block_store(acc, tpart, t);
+  }
+}
+
+// per-sector multiplier f * 2^(so - si) as (mul, shift) (k_fx_mult restated)
+__device__ __forceinline__ void ms_mult(double x, int si, int so, i64& mul, int& sh) {
+  if (x == 0.0 || !isfinite(x)) { mul = 0; sh = 0; return; }
+  int e;
+  frexp(fabs(x), &e);
+  int E = 60 - e;
+  int shift = E + si - so;
+  if (shift > 120) { E -= shift - 120; shift = 120; }
+  if (shift < 0) { E -= shift; shift = 0; }
+  mul = __double2ll_rn(ldexp(x, E));
+  sh = shift;
+}
+
+__global__ void k_ms_start_norm(int nsec, const MsSector* secs, const i64* tpart, int F, ChainMeta* meta,
+                                i64* mul, int* msh) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsec; s += gridDim.x * blockDim.x) {
+    const double n2 = ms_i128_to_double(ms_sum_parts(tpart, secs[s].tile0, secs[s].ntile), 80);
+    double invn = 0.0;
+    if (n2 > 0.0) invn = 1.0 / sqrt(n2);
+    else { meta[s].active = 0; meta[s].len = 0; }
+    i64 m;
+    int sh;
+    ms_mult(invn, 40, F, m, sh);
+    mul[s] = m;
+    msh[s] = sh;
+  }
+}
+
+__global__ void k_ms_apply(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
+                           const ChainMeta* meta, const i64* mul, const int* msh, int zero_inactive,
+                           const i64* Xi, i64* Xo) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    const MsSector& S = secs[s];
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    const bool act = meta[s].active;
+    if (!act && !zero_inactive) continue;
+    const i64 m = mul[s];
+    const int sh = msh[s];
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+      Xo[S.off + i] = act ? ms_rshift((i128)m * Xi[S.off + i], sh) : 0;
+  }
+}
+
+// H x v (single column, fixed point) + exact alpha partial per tile
+template <int K>
+__global__ void __launch_bounds__(256) k_ms_hxv(const MsSector* secs, const int* tsec, const int64_t* tstart,
+                                                int ntiles, const ChainMeta* meta, const i64* __restrict__ X,
+                                                i64* __restrict__ Y, i64* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    i128 adot = 0;
+    if (meta[s].active) {
+      const MsSector& S = secs[s];
+      const SectorView& sv = S.sv;
+      const FxView& fv = S.fv;
+      const i64* Xs = X + S.off;
+      const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int idw = (int)(i / sv.dimup);
+        const int iup = (int)(i - (int64_t)idw * sv.dimup);
+        const i64 dfx = fv.up_e1[iup] + fv.dw_e1[idw] +
+                        ms_mixed(fv, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
+        i64 Sk[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) Sk[k] = 0;
+        const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
+        const int64_t colbase = (int64_t)idw * sv.dimup;
+        for (int h = 0; h < nu; h++) {
+          const int64_t o = (int64_t)h * sv.dimup + iup;
+          const signed char code = fv.up_code[o];
+          const i64 v = Xs[colbase + sv.up_src[o]];
+          const i64 sv_ = (code < 0) ? -v : v;
+#pragma unroll
+          for (int k = 0; k < K; k++) Sk[k] += (K == 1 || (code & 3) == k) ? sv_ : 0;
+        }
+        for (int h = 0; h < nd; h++) {
+          const int64_t o = (int64_t)h * sv.dimdw + idw;
+          const signed char code = fv.dw_code[o];
+          const i64 v = Xs[(int64_t)iup + (int64_t)sv.dw_src[o] * sv.dimup];
+          const i64 sv_ = (code < 0) ? -v : v;
+#pragma unroll
+          for (int k = 0; k < K; k++) Sk[k] += (K == 1 || (code & 3) == k) ? sv_ : 0;
+        }
+        const i64 x = Xs[i];
+        i128 p = (i128)dfx * x;
+#pragma unroll
+        for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * Sk[k];
+        const i64 y = ms_rshift(p, fv.shift);
+        Y[S.off + i] = y;
+        adot += (i128)x * y;
+      }
+    }
+    ms_block_store(adot, tpart, t);
+  }
+}
+
+__global__ void k_ms_alpha(int nsec, const MsSector* secs, const ChainMeta* meta, const i64* tpart, int sexp,
+                           int C, const double* bnow, double* alpha, i64* afx, i64* bfx) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsec; s += gridDim.x * blockDim.x) {
+    if (!meta[s].active) continue;
+    const double a = 0.0 + ms_i128_to_double(ms_sum_parts(tpart, secs[s].tile0, secs[s].ntile), sexp);
+    alpha[s] = a;
+    afx[s] = __double2ll_rn(ldexp(1.0 * a, C));
+    bfx[s] = __double2ll_rn(ldexp(1.0 * bnow[s], C));
+  }
+}
+
+__global__ void k_ms_update(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
+                            const ChainMeta* meta, int sh, const i64* afx, const i64* bfx, int use_b,
+                            const i64* X, const i64* Xp, i64* YW, i64* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    i128 acc = 0;
+    if (meta[s].active) {
+      const MsSector& S = secs[s];
+      const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+      const i64 a = afx[s], b = use_b ? bfx[s] : 0;
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int64_t g = S.off + i;
+        i128 p = (i128)a * X[g];
+        if (use_b) p += (i128)b * Xp[g];
+        const i64 w = YW[g] - ms_rshift(p, sh);
+        YW[g] = w;
+        acc += (i128)w * w;
+      }
+    }
+    ms_block_store(acc, tpart, t);
+  }
+}
+
+// beta^2 -> sp_lanc_tridiag bookkeeping (as k_lanczos_record) + normalisation multiplier
+__global__ void k_ms_record(int nsec, const MsSector* secs, ChainMeta* meta, const i64* tpart, int sexp, int k,
+                            const double* alpha, double* A, double* Bt, int ld, double tol, double* bnow,
+                            int G, int F, i64* mul, int* msh) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsec; s += gridDim.x * blockDim.x) {
+    ChainMeta mt = meta[s];
+    if (!mt.active) continue;
+    const double b2 = 0.0 + ms_i128_to_double(ms_sum_parts(tpart, secs[s].tile0, secs[s].ntile), sexp);
+    const double a = alpha[s];
+    const double b = sqrt(fmax(b2, 0.0));
+    A[(int64_t)s * ld + (k - 1)] = a;
+    mt.len = k;
+    double invb;
+    if (b < tol) {
+      mt.active = 0;
+      invb = 0.0;
+    } else {
+      if (k < mt.nlanc) Bt[(int64_t)s * ld + k] = b;
+      if (k >= mt.nlanc) mt.active = 0;
+      invb = 1.0 / b;
+    }
+    bnow[s] = b;
+    meta[s] = mt;
+    i64 m;
+    int sh;
+    ms_mult(invb, G, F, m, sh);
+    mul[s] = m;
+    msh[s] = sh;
+  }
+}
+
+// convergence test of every unfinished sector, one warp per sector
+__global__ void k_ms_check(int nsec, ChainMeta* meta, const double* A, const double* Bt, int ld,
+                           const double* bnow, double* svec, double* theta, double* resid, int* state,
+                           int* mconv, double tol, int* undone) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = warp; s < nsec; s += nw) {
+    if (state[s]) continue;
+    const ChainMeta mt = meta[s];
+    const int kk = mt.len;
+    if (kk < 1) {  // zero start vector: report as finished without a value
+      if (lane == 0) { state[s] = 2; theta[s] = INFINITY; mconv[s] = 0; }
+      continue;
+    }
+    warp_tri_lowest(A + (int64_t)s * ld, Bt + (int64_t)s * ld, kk, bnow[s], theta + s,
+                    svec + (int64_t)s * 5 * ld, resid + s);
+    __syncwarp();
+    if (lane == 0) {
+      const double th = theta[s];
+      if (!mt.active || resid[s] <= tol * fmax(1.0, fabs(th))) {
+        state[s] = 1;
+        mconv[s] = kk;
+        meta[s].active = 0;
+      } else {
+        atomicAdd(undone, 1);
+      }
+    }
+  }
+}
+
+void ms_launch_start(const MsGroup& gp, uint64_t seed, int F, i64* R, i64* X, i64* tpart, ChainMeta* meta,
+                     i64* mul, int* msh, cudaStream_t st) {
+  count_launch_external();
+  count_launch_external();
+  count_launch_external();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  k_ms_start_raw<<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, seed, R, tpart);
+  k_ms_start_norm<<<(gp.nsec + 127) / 128, 128, 0, st>>>(gp.nsec, gp.secs, tpart, F, meta, mul, msh);
+  k_ms_apply<<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, meta, mul, msh, 1, R, X);
+}
+
+void ms_launch_step(const MsGroup& gp, const FxScales& fs, int K, int k, double tol, MsBufs& b, cudaStream_t st) {
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  const int sb = (gp.nsec + 127) / 128;
+  for (int q = 0; q < 5; q++) count_launch_external();
+  switch (K) {
+    case 1: k_ms_hxv<1><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.X, b.YW, b.tpart); break;
+    case 2: k_ms_hxv<2><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.X, b.YW, b.tpart); break;
+    case 3: k_ms_hxv<3><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.X, b.YW, b.tpart); break;
+    default: k_ms_hxv<4><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.X, b.YW, b.tpart); break;
+  }
+  k_ms_alpha<<<sb, 128, 0, st>>>(gp.nsec, gp.secs, b.meta, b.tpart, fs.F + fs.G, fs.C, b.bnow, b.alpha, b.afx, b.bfx);
+  k_ms_update<<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, fs.C + fs.F - fs.G, b.afx,
+                                  b.bfx, k > 1 ? 1 : 0, b.X, b.Xp, b.YW, b.tpart);
+  k_ms_record<<<sb, 128, 0, st>>>(gp.nsec, gp.secs, b.meta, b.tpart, 2 * fs.G, k, b.alpha, b.A, b.Bt, b.ld, tol,
+                                  b.bnow, fs.G, fs.F, b.mul, b.msh);
+  // X_next into the old Xp buffer (retired sectors get zeros)
+  k_ms_apply<<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.mul, b.msh, 1, b.YW, b.Xp);
+  i64* t = b.Xp;
+  b.Xp = b.X;
+  b.X = t;
+}
+
+void ms_launch_check(const MsGroup& gp, MsBufs& b, double tol, cudaStream_t st) {
+  count_launch_external();
+  const int warps = gp.nsec;
+  const int threads = 128;
+  const int blocks = std::max(1, (warps * 32 + threads - 1) / threads);
+  k_ms_check<<<blocks, threads, 0, st>>>(gp.nsec, b.meta, b.A, b.Bt, b.ld, b.bnow, b.svec, b.theta, b.resid,
+                                         b.state, b.mconv, tol, b.undone);
+}
+
+}  // namespace vca
