@@ -197,7 +197,10 @@ def hxv_operand(s, D, m):
     x = torch.randn(D, m, dtype=torch.float64, device="cuda")
     x /= torch.linalg.vector_norm(x, dim=0, keepdim=True)
     if fx:
-        name = "k_hxv_fx_a+k_hxv_fx_b" if (m >= 8 and s.cfg.hxv_variant == 2) else "k_hxv_fx"
+        if m >= 8 and s.cfg.hxv_variant == 2:
+            name = "k_hxv_fx_a+k_hxv_fx_b"
+        else:
+            name = "k_hxv_fx_w" if m >= 16 else "k_hxv_fx"
         return torch.round(x * 2.0 ** F).to(torch.int64).reshape(-1), name
     return x.reshape(-1), "k_hxv_real"
 

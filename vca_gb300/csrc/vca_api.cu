@@ -103,6 +103,7 @@ struct Ctx {
   FxScales fxs{};
   FxView fxbase{};
   std::vector<signed char*> fx_code[2];
+  std::vector<unsigned*> fx_hop[2];
   std::vector<i64*> fx_e1[2];
   i64* apart_scratch = nullptr;  // alpha partials for the timed two-pass H x v
   int64_t apart_rows = 0, apart_cols = 0;
@@ -199,6 +200,8 @@ FxView fx_view_of(int nup, int ndw) {
   FxView f = g->fxbase;
   f.up_code = g->fx_code[0][nup];
   f.dw_code = g->fx_code[g->dwset][ndw];
+  f.up_hop = g->fx_hop[0][nup];
+  f.dw_hop = g->fx_hop[g->dwset][ndw];
   f.up_e1 = g->fx_e1[0][nup];
   f.dw_e1 = g->fx_e1[g->dwset][ndw];
   return f;
@@ -412,16 +415,19 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
       CUCHK(cudaMemcpyAsync(d_cls, classes.data(), sizeof(double) * classes.size(), cudaMemcpyHostToDevice, g->st));
       for (int set = 0; set < nsets; set++) {
         g->fx_code[set].assign(g->Ns + 1, nullptr);
+        g->fx_hop[set].assign(g->Ns + 1, nullptr);
         g->fx_e1[set].assign(g->Ns + 1, nullptr);
         for (int n = 0; n <= g->Ns; n++) {
           SpinSpace& S = g->sp[set][n];
+          RCHK(g->ham.alloc(&g->fx_hop[set][n], (size_t)S.width * S.dim));
+          launch_fx_pack(S.dim, S.width, S.src, S.amp, d_cls, fb.K, g->fx_hop[set][n], g->st);
           RCHK(g->ham.alloc(&g->fx_code[set][n], (size_t)S.width * S.dim));
           RCHK(g->ham.alloc(&g->fx_e1[set][n], S.dim));
           launch_fx_codes(S.dim, S.width, S.amp, d_cls, fb.K, g->fx_code[set][n], g->st);
           launch_fx_e1(S.dim, S.e1, fs.A, g->fx_e1[set][n], g->st);
         }
       }
-      if (nsets == 1) { g->fx_code[1] = g->fx_code[0]; g->fx_e1[1] = g->fx_e1[0]; }
+      if (nsets == 1) { g->fx_code[1] = g->fx_code[0]; g->fx_hop[1] = g->fx_hop[0]; g->fx_e1[1] = g->fx_e1[0]; }
       CUCHK(cudaGetLastError());
       g->fxs = fs;
       g->fxbase = fb;
@@ -491,7 +497,10 @@ int lanczos_step_fx(const SectorView& sv, const FxView& fv, const ColBatch& cb, 
       launch_hxv_fx2(sv, fv, cb.m, X, YW, bb.apart, st)) {
     launch_fx_partial_reduce(cb.m, sv.dimup, bb.apart, fs.F + fs.G, bb.col_a, st);
   } else {
-    launch_hxv_fx(sv, fv, cb.m, X, YW, st);
+    if (cb.m >= 16 && (int64_t)sv.dimup * sv.dimdw * cb.m < ((int64_t)1 << 31))
+      launch_hxv_fx_w(sv, fv, cb.m, X, YW, st);
+    else
+      launch_hxv_fx(sv, fv, cb.m, X, YW, st);
     launch_fx_dot(cb, X, YW, fs.F, fs.G, (i64*)bb.partial, bb.nblk, bb.col_a, st);
   }
   launch_chain_sum(cb, bb.col_a, bb.ch_a, st);
@@ -1677,7 +1686,10 @@ static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_com
       CUCHK(cudaGetLastError());
       return VCA_OK;
     }
-    launch_hxv_fx(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
+    if (m >= 16 && (int64_t)sv.dimup * sv.dimdw * m < ((int64_t)1 << 31))
+      launch_hxv_fx_w(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
+    else
+      launch_hxv_fx(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
   } else if (is_complex && !g->real_model) {
     launch_hxv_cplx(sv, g->md, ncols, (const double2*)d_v, (double2*)d_hv, g->st);
   } else {

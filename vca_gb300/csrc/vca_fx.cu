@@ -3,6 +3,7 @@
 #include "vca_fx.cuh"
 
 #include <atomic>
+#include <algorithm>
 #include <cmath>
 
 namespace vca {
@@ -26,6 +27,12 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+static void col_shape_fx(int m, dim3& blk) {
+  int cw = 1;
+  while (cw < m && cw < 32) cw <<= 1;
+  blk = dim3(cw, 256 / cw, 1);
+}
 
 // round-half-up arithmetic shift of an int128 by s >= 0
 __device__ __forceinline__ i64 rshift_round(i128 p, int s) {
@@ -132,11 +139,6 @@ __global__ void k_hxv_fx(SectorView sv, FxView fv, int m, const i64* __restrict_
   }
 }
 
-static void col_shape_fx(int m, dim3& blk) {
-  int cw = 1;
-  while (cw < m && cw < 32) cw <<= 1;
-  blk = dim3(cw, 256 / cw, 1);
-}
 
 void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st) {
   count_launch_external();
@@ -246,35 +248,45 @@ __global__ void k_fx_mult(int nch, const double* f, int si, int so, i64* mul, i6
     sh[ch] = shift;
   }
 }
+// column-tiled: block (CW columns x RB rows), column from blockIdx.y, so no
+// per-element division by m
 __global__ void k_fx_apply(int64_t rows, int m, const int* col2ch, const ChainMeta* meta, const i64* mul,
                            const i64* sh, int zero_inactive, const i64* Xi, i64* Xo) {
-  const int64_t n = rows * m;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int c = (int)(g % m);
-    const int ch = col2ch[c];
-    if (!meta[ch].active) {
-      if (zero_inactive) Xo[g] = 0;
-      continue;
-    }
-    Xo[g] = rshift_round((i128)mul[ch] * Xi[g], (int)sh[ch]);
+  const int CW = blockDim.x, RB = blockDim.y;
+  const int c = blockIdx.y * CW + threadIdx.x;
+  if (c >= m) return;
+  const int ch = col2ch[c];
+  const bool act = meta[ch].active;
+  if (!act && !zero_inactive) return;
+  const i64 mu = mul[ch];
+  const int s = (int)sh[ch];
+  for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB) {
+    const int64_t g = i * m + c;
+    Xo[g] = act ? rshift_round((i128)mu * Xi[g], s) : 0;
   }
+}
+static void launch_apply(const ColBatch& b, const i64* mul, const i64* sh, int zero_inactive, const i64* Xi,
+                         i64* Xo, cudaStream_t st) {
+  dim3 blk;
+  col_shape_fx(b.m, blk);
+  const int64_t nrb = (b.rows + blk.y - 1) / blk.y;
+  const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(nrb, 152 * 16));
+  dim3 grd(gx, (b.m + blk.x - 1) / blk.x, 1);
+  k_fx_apply<<<grd, blk, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, mul, sh, zero_inactive, Xi, Xo);
 }
 void launch_fx_normalize(const ColBatch& b, const FxScales& s, const double* invbeta, const i64* W,
                          i64* X, i64* scratch, cudaStream_t st) {
   count_launch_external();
   count_launch_external();
   k_fx_mult<<<nblk_fx(b.nch, 128), 128, 0, st>>>(b.nch, invbeta, s.G, s.F, scratch, scratch + b.nch);
-  const int64_t n = b.rows * b.m;
-  k_fx_apply<<<nblk_fx(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scratch, scratch + b.nch, 1, W, X);
+  launch_apply(b, scratch, scratch + b.nch, 1, W, X, st);
 }
 void launch_fx_rescale(const ColBatch& b, const double* f, int si, int so, const i64* Xi, i64* Xo,
                        i64* scratch, cudaStream_t st) {
   count_launch_external();
   count_launch_external();
   k_fx_mult<<<nblk_fx(b.nch, 128), 128, 0, st>>>(b.nch, f, si, so, scratch, scratch + b.nch);
-  const int64_t n = b.rows * b.m;
-  k_fx_apply<<<nblk_fx(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, scratch, scratch + b.nch, 0, Xi, Xo);
+  launch_apply(b, scratch, scratch + b.nch, 0, Xi, Xo, st);
 }
 
 __global__ void k_fx_psi_accum(int64_t n, const double* s, int k, const i64* X, i64* psi) {
@@ -548,4 +560,132 @@ void launch_fx_start_raw(int64_t n, uint64_t seed, int isector, i64* R, cudaStre
   k_fx_start_raw<<<nblk_fx(n, 256), 256, 0, st>>>(n, seed, isector, R);
 }
 
+
+// ---------------------------------------------------------------------------
+// Packed hop words and the warp-per-row H x v for column batches.
+// ---------------------------------------------------------------------------
+__global__ void k_fx_pack(int64_t n, const int* src, const double2* amp, const double* classes, int K,
+                          unsigned* hop) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double a = amp[t].x;
+    const double mag = fabs(a);
+    unsigned cls = 0;
+    for (int k = 0; k < K; k++)
+      if (classes[k] == mag) cls = (unsigned)k;
+    hop[t] = ((unsigned)src[t] & 0xFFFFFFu) | (cls << 24) | (a < 0.0 ? 0x80000000u : 0u);
+  }
+}
+void launch_fx_pack(int dim, int width, const int* src, const double2* amp, const double* classes, int K,
+                    unsigned* hop, cudaStream_t st) {
+  count_launch_external();
+  const int64_t n = (int64_t)dim * width;
+  if (n == 0) return;
+  k_fx_pack<<<nblk_fx(n, 256), 256, 0, st>>>(n, src, amp, classes, K, hop);
+}
+
+// accumulate one hop's source row into the class accumulators; the class and
+// sign are warp-uniform, so the branches do not diverge
+template <int K, int NCQ>
+__device__ __forceinline__ void hop_row(i64 (&S)[K][NCQ], unsigned hw, const i64* __restrict__ xr, int lim) {
+  const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+  const bool neg = hw >> 31;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    if (k != cls) continue;
+    if (neg) {
+#pragma unroll
+      for (int q = 0; q < NCQ; q++)
+        if (32 * q < lim) S[k][q] -= xr[32 * q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < NCQ; q++)
+        if (32 * q < lim) S[k][q] += xr[32 * q];
+    }
+  }
+}
+
+// MODE 0: full product (rows in idw-major order).
+// MODE 1: diagonal + up hops only, rows in idw-major order: a column block's
+//         up neighbours are the rows being processed, so they stay in L2.
+// MODE 2: down hops added into Y, rows in iup-major order: a slab's down
+//         neighbours stay in L2.  Modes 1 + 2 read X from DRAM about once each.
+template <int K, int NCQ, int MODE>
+__global__ void __launch_bounds__(256) k_hxv_fx_w(SectorView sv, FxView fv, int m, const i64* __restrict__ X,
+                                                  i64* __restrict__ Y) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int D = DU * DD;
+  for (int rr = wid; rr < D; rr += nw) {
+    int idw, iup;
+    if (MODE == 2) { iup = rr / DD; idw = rr - iup * DD; }
+    else { idw = rr / DU; iup = rr - idw * DU; }
+    const int r = iup + idw * DU;
+    i64 dfx = 0;
+    if (MODE != 2)
+      dfx = fv.up_e1[iup] + fv.dw_e1[idw] + mixed_fx(fv, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
+    const int nu = (MODE == 2) ? 0 : sv.up_cnt[iup];
+    const int nd = (MODE == 1) ? 0 : sv.dw_cnt[idw];
+    const int colbase = idw * DU;
+    for (int c0 = 0; c0 < m; c0 += 32 * NCQ) {
+      const int lim = m - c0 - lane;  // column lane + 32q exists while 32q < lim
+      i64 S[K][NCQ];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+#pragma unroll
+        for (int q = 0; q < NCQ; q++) S[k][q] = 0;
+      for (int h = 0, o = iup; h < nu; h++, o += DU) {
+        const unsigned hw = fv.up_hop[o];
+        hop_row<K, NCQ>(S, hw, X + (int64_t)(colbase + (int)(hw & 0xFFFFFFu)) * m + c0 + lane, lim);
+      }
+      for (int h = 0, o = idw; h < nd; h++, o += DD) {
+        const unsigned hw = fv.dw_hop[o];
+        hop_row<K, NCQ>(S, hw, X + (int64_t)(iup + (int)(hw & 0xFFFFFFu) * DU) * m + c0 + lane, lim);
+      }
+      const i64* xo = X + (int64_t)r * m + c0 + lane;
+      i64* yo = Y + (int64_t)r * m + c0 + lane;
+#pragma unroll
+      for (int q = 0; q < NCQ; q++) {
+        if (32 * q < lim) {
+          i128 p = 0;
+          if (MODE != 2) p = (i128)dfx * xo[32 * q];
+#pragma unroll
+          for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k][q];
+          const i64 y = rshift_round(p, fv.shift);
+          yo[32 * q] = (MODE == 2) ? yo[32 * q] + y : y;
+        }
+      }
+    }
+  }
+}
+
+void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st) {
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int blocks = nblk_fx(D * 32, 256, 152 * 8);
+  // columns per pass: 32*NCQ, NCQ limited so K*NCQ int64 accumulators stay in registers
+#define VCA_W(KK, NQ)                                                   \
+  do {                                                                  \
+    count_launch_external();                                            \
+    count_launch_external();                                            \
+    k_hxv_fx_w<KK, NQ, 1><<<blocks, 256, 0, st>>>(sv, fv, m, X, Y);     \
+    k_hxv_fx_w<KK, NQ, 2><<<blocks, 256, 0, st>>>(sv, fv, m, X, Y);     \
+  } while (0)
+  const int ncq = (m + 31) / 32;
+  switch (fv.K) {
+    case 1:
+      if (ncq <= 4) VCA_W(1, 4);
+      else if (ncq <= 8) VCA_W(1, 8);
+      else VCA_W(1, 16);
+      break;
+    case 2:
+      if (ncq <= 4) VCA_W(2, 4);
+      else VCA_W(2, 8);
+      break;
+    case 3: VCA_W(3, 4); break;
+    default: VCA_W(4, 4); break;
+  }
+#undef VCA_W
+}
 }  // namespace vca

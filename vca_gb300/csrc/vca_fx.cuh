@@ -35,6 +35,8 @@ struct FxScales {
 struct FxView {
   const signed char* up_code;  // [width*dim]: class (bits 0-1), sign (bit 7)
   const signed char* dw_code;
+  const unsigned* up_hop;      // [width*dim]: src (bits 0-23) | class << 24 | sign << 31
+  const unsigned* dw_hop;
   const i64* up_e1;            // one-body + same-spin diagonal, scale 2^-A
   const i64* dw_e1;
   int K;
@@ -47,6 +49,12 @@ struct FxView {
   int shift;                   // A + F - G
 };
 
+// packed hop words src | class<<24 | sign<<31 from the FP64 tables
+void launch_fx_pack(int dim, int width, const int* src, const double2* amp, const double* classes, int K,
+                    unsigned* hop, cudaStream_t st);
+// Y = H X on a column batch, one warp per row streaming all m columns per hop
+// (needs DimUp*DimDw*m < 2^31)
+void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st);
 // per-hop class/sign codes from the FP64 amplitude tables
 void launch_fx_codes(int dim, int width, const double2* amp, const double* classes, int K,
                      signed char* code, cudaStream_t st);
