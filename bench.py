@@ -38,10 +38,8 @@ WORKLOAD = ("square4x3 Hubbard U=8 Nspin=2, M_AF sweep 16 pts [0,0.3], 32x32 k-g
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from vca_gb300.replicas import dist_env as _d
+    return _d()
 
 
 def measured_peaks():
@@ -189,18 +187,19 @@ def run_reference(args):
     return 0
 
 
-def hxv_operand(s, D, m):
+def hxv_operand(s, D, m, dimup):
     """Unit-norm random columns in the library's arithmetic (FP64, or int64
-    fixed point with scale 2^-F when the fixed-point path is active)."""
+    fixed point with scale 2^-F when the fixed-point path is active), and the
+    name of the kernel the library runs on them."""
     import torch
     fx, F, _ = s.arith_info()
     x = torch.randn(D, m, dtype=torch.float64, device="cuda")
     x /= torch.linalg.vector_norm(x, dim=0, keepdim=True)
     if fx:
-        if m >= 8 and s.cfg.hxv_variant == 2:
-            name = "k_hxv_fx_a+k_hxv_fx_b"
-        else:
-            name = "k_hxv_fx_w" if m >= 16 else "k_hxv_fx"
+        # shared-memory staged form while an 8-column up block fits, unless
+        # the warp form is forced (hxv_variant 1)
+        staged = m >= 16 and dimup * 8 * 8 <= 100 * 1024 and s.cfg.hxv_variant != 1
+        name = "k_hxv_fx_s" if staged else ("k_hxv_fx_w" if m >= 16 else "k_hxv_fx")
         return torch.round(x * 2.0 ** F).to(torch.int64).reshape(-1), name
     return x.reshape(-1), "k_hxv_real"
 
@@ -217,25 +216,16 @@ def run_gpu(args):
     vbuild.build()
     from vca_gb300.solver import VcaSolver
 
+    from vca_gb300.replicas import Group, partition
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo", init_method="env://")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def allmax(x: float) -> float:
-        if dist is None:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    grp = Group(dist)
+    barrier, allmax = grp.barrier, grp.max
 
     pts = build_points()
-    mine = pts[rank::world] if world > 1 else pts
+    mine = [pts[i] for i in partition(len(pts), rank, world)]
     s = VcaSolver(mine[0].cfg)
     s.upload_hk(mine[0].Hk)
     for i in range(args.warmup):
@@ -276,7 +266,7 @@ def run_gpu(args):
         D = du * dd
         L = 12
         m = L + L * (L - 1) + 2 * L * (L - 1)
-        x, kname = hxv_operand(s, D, m)
+        x, kname = hxv_operand(s, D, m, du)
         y = torch.empty_like(x)
         torch.cuda.synchronize()
         reps = 5
@@ -332,7 +322,7 @@ def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
     isec = 1 + 6 + 7 * 13
     _, _, du, dd = s.sector_info(isec)
     D = du * dd
-    x, kname = hxv_operand(s, D, ncols)
+    x, kname = hxv_operand(s, D, ncols, du)
     y = torch.empty_like(x)
     torch.cuda.synchronize()
     ms = s.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, ncols, reps)
@@ -373,7 +363,7 @@ def main():
                     help="profiling mode: one plain solve of a reduced 4x3 point "
                          "(8x8 k-grid, 1024 nodes) after one warm-up solve")
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--hxv-variant", type=int, default=0, help="0/1 one pass, 2 two pass")
+    ap.add_argument("--hxv-variant", type=int, default=0, help="0 auto, 1 warp form only")
     args = ap.parse_args()
     if args.profile_hxv:
         return profile_hxv(args.profile_hxv, args.reps, args.hxv_variant)

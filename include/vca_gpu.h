@@ -101,7 +101,7 @@ typedef struct vca_config {
   double gf_beta_tol;      /* GF chain stop: beta_{k+1} < tol (exhausted)   */
   uint64_t start_seed;     /* seed of the deterministic Lanczos start vector */
   int32_t arith;           /* VCA_ARITH_AUTO | VCA_ARITH_FP64 | VCA_ARITH_FX   */
-  int32_t hxv_variant;     /* FX column batches: 0/1 one pass, 2 two pass      */
+  int32_t hxv_variant;     /* FX column H x v: 0 auto, 1 warp form only        */
   int32_t reserved[6];
 } vca_config;
 
@@ -243,7 +243,9 @@ int vca_gpu_get_timings(double* ms, int32_t n);
 /* Arithmetic of the loaded Hamiltonian: *fx = 1 when the fixed-point path is
  * active, with vector scale 2^-F and H v scale 2^-G.  In that case the device
  * buffers of vca_gpu_hxv_device / vca_gpu_hxv_timed hold int64 fixed-point
- * columns (unit norm, scale 2^-F in, 2^-G out). */
+ * columns (unit norm, scale 2^-F in, 2^-G out), slab-major once there are 8
+ * or more: slabs of 8 adjacent columns, each a contiguous [dim][8] block
+ * (element (i, c) at ((c/8)*dim + i)*8 + c%8), ncols a multiple of 8. */
 int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);

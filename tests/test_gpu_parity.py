@@ -31,6 +31,9 @@ POINTS = {
     "square2x2_afm": lambda: clusters.square(nx=2, ny=2, U=8.0, xmu=4.0, maf=0.2, nspin=2, nkx=6,
                                              nky=6, ngfiter=80, omega_nodes=256),
     "bath2x2+4": lambda: _small_bath(),
+    # 8 sites: the column kernels run with many warps per CTA
+    "square2x4_afm": lambda: clusters.square(nx=2, ny=4, U=8.0, xmu=4.0, maf=0.2, nspin=2, nkx=4,
+                                             nky=4, ngfiter=60, omega_nodes=128),
     "bhz_small": lambda: clusters.bhz(mass=2.2, delta=0.1, nk1=4, ngfiter=60, omega_nodes=256),
 }
 
@@ -124,7 +127,7 @@ def test_shape_errors_raise():
 
 
 @pytest.mark.parametrize("arith", [1, 2], ids=["fp64", "fx"])
-@pytest.mark.parametrize("name", ["chain4", "square2x2_afm"])
+@pytest.mark.parametrize("name", ["chain4", "square2x2_afm", "square2x4_afm"])
 def test_fixed_point_and_fp64_paths_agree(name, arith):
     """Both arithmetic paths of a real Hamiltonian against the oracle."""
     pt = POINTS[name]()

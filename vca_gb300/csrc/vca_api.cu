@@ -88,6 +88,13 @@ struct Ctx {
   int Ns = 0, Nsectors = 0, N = 0, L = 0, Nb = 0;
   cudaStream_t st = nullptr;
   Arena basis, ham, states, gf, omega, work;
+  // frequency rule of the Omega integral (depends on omega_nodes and
+  // omega_scale only): computed on the first solve, reused after
+  Arena nodes;
+  double2* node_z = nullptr;
+  double* node_w = nullptr;
+  int node_n = 0;
+  double node_scale = 0.0;
   std::vector<int> dimn;
   std::vector<int*> words;
   int* d_iscratch = nullptr;
@@ -105,8 +112,14 @@ struct Ctx {
   std::vector<signed char*> fx_code[2];
   std::vector<unsigned*> fx_hop[2];
   std::vector<i64*> fx_e1[2];
-  i64* apart_scratch = nullptr;  // alpha partials for the timed two-pass H x v
-  int64_t apart_rows = 0, apart_cols = 0;
+  std::vector<int*> fx_npos[2];   // sign-sorted hop lists: positive count per row
+  std::vector<int*> fx_perm[2];   // rows by decreasing hop count
+  struct PermTabs {
+    unsigned* hop = nullptr;
+    int *cnt = nullptr, *npos = nullptr, *word = nullptr;
+    i64* e1 = nullptr;
+  };
+  std::vector<PermTabs> fx_ptab[2];  // tables in perm order
   std::vector<HopPair> host_pairs;
   std::vector<double> host_eps_abs;  // per spin set: bound of |one-body energy|
   // results
@@ -204,6 +217,15 @@ FxView fx_view_of(int nup, int ndw) {
   f.dw_hop = g->fx_hop[g->dwset][ndw];
   f.up_e1 = g->fx_e1[0][nup];
   f.dw_e1 = g->fx_e1[g->dwset][ndw];
+  f.up_npos = g->fx_npos[0][nup];
+  f.dw_npos = g->fx_npos[g->dwset][ndw];
+  f.up_perm = g->fx_perm[0][nup];
+  const Ctx::PermTabs& pt = g->fx_ptab[0][nup];
+  f.up_phop = pt.hop;
+  f.up_pcnt = pt.cnt;
+  f.up_pnpos = pt.npos;
+  f.up_pword = pt.word;
+  f.up_pe1 = pt.e1;
   return f;
 }
 
@@ -417,17 +439,47 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
         g->fx_code[set].assign(g->Ns + 1, nullptr);
         g->fx_hop[set].assign(g->Ns + 1, nullptr);
         g->fx_e1[set].assign(g->Ns + 1, nullptr);
+        g->fx_npos[set].assign(g->Ns + 1, nullptr);
+        g->fx_perm[set].assign(g->Ns + 1, nullptr);
+        g->fx_ptab[set].assign(g->Ns + 1, Ctx::PermTabs{});
         for (int n = 0; n <= g->Ns; n++) {
           SpinSpace& S = g->sp[set][n];
           RCHK(g->ham.alloc(&g->fx_hop[set][n], (size_t)S.width * S.dim));
           launch_fx_pack(S.dim, S.width, S.src, S.amp, d_cls, fb.K, g->fx_hop[set][n], g->st);
+          RCHK(g->ham.alloc(&g->fx_npos[set][n], S.dim));
+          launch_fx_sign_sort(S.dim, S.width, S.cnt, g->fx_hop[set][n], g->fx_npos[set][n], g->st);
+          {  // rows by decreasing hop count (stable), for warps of equal loop length
+            std::vector<int> cnt(S.dim), perm(S.dim);
+            if (S.dim) CUCHK(cudaMemcpy(cnt.data(), S.cnt, sizeof(int) * S.dim, cudaMemcpyDeviceToHost));
+            for (int r = 0; r < S.dim; r++) perm[r] = r;
+            std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return cnt[x] > cnt[y]; });
+            RCHK(g->ham.alloc(&g->fx_perm[set][n], S.dim));
+            if (S.dim)
+              CUCHK(cudaMemcpy(g->fx_perm[set][n], perm.data(), sizeof(int) * S.dim, cudaMemcpyHostToDevice));
+          }
           RCHK(g->ham.alloc(&g->fx_code[set][n], (size_t)S.width * S.dim));
           RCHK(g->ham.alloc(&g->fx_e1[set][n], S.dim));
           launch_fx_codes(S.dim, S.width, S.amp, d_cls, fb.K, g->fx_code[set][n], g->st);
           launch_fx_e1(S.dim, S.e1, fs.A, g->fx_e1[set][n], g->st);
+          Ctx::PermTabs& pt = g->fx_ptab[set][n];
+          RCHK(g->ham.alloc(&pt.hop, (size_t)S.width * S.dim));
+          RCHK(g->ham.alloc(&pt.cnt, S.dim));
+          RCHK(g->ham.alloc(&pt.npos, S.dim));
+          RCHK(g->ham.alloc(&pt.word, S.dim));
+          RCHK(g->ham.alloc(&pt.e1, S.dim));
+          launch_fx_perm_tables(S.dim, S.width, g->fx_perm[set][n], g->fx_hop[set][n], S.cnt,
+                                g->fx_npos[set][n], S.words, g->fx_e1[set][n], pt.hop, pt.cnt, pt.npos,
+                                pt.word, pt.e1, g->st);
         }
       }
-      if (nsets == 1) { g->fx_code[1] = g->fx_code[0]; g->fx_hop[1] = g->fx_hop[0]; g->fx_e1[1] = g->fx_e1[0]; }
+      if (nsets == 1) {
+        g->fx_code[1] = g->fx_code[0];
+        g->fx_hop[1] = g->fx_hop[0];
+        g->fx_e1[1] = g->fx_e1[0];
+        g->fx_npos[1] = g->fx_npos[0];
+        g->fx_perm[1] = g->fx_perm[0];
+        g->fx_ptab[1] = g->fx_ptab[0];
+      }
       CUCHK(cudaGetLastError());
       g->fxs = fs;
       g->fxbase = fb;
@@ -453,8 +505,8 @@ struct BatchBufs {
   ChainMeta* meta;
   int* col2ch;
   i64 *afx, *bfx, *scr;  // fixed-point coefficients and per-chain scratch (2*nch)
-  i64* apart;            // alpha partials of the two-pass H x v [2*DimUp*m]
-  int64_t apart_rows;
+  i64* wpart;            // alpha partials of the column H x v [2*rows*m]
+  int64_t wpart_rows;
 };
 
 int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k, double tol, int ldab) {
@@ -491,16 +543,14 @@ int lanczos_step_fx(const SectorView& sv, const FxView& fv, const ColBatch& cb, 
   i64* X = (i64*)bb.b[0];
   i64* Xp = (i64*)bb.b[1];
   i64* YW = (i64*)bb.b[2];
-  // the one-pass kernel measured faster on GB300 (8.6 vs 12.6 ms, 4x3 batch):
-  // the two-pass form is opt-in (hxv_variant = 2)
-  if (g->cfg.hxv_variant == 2 && cb.m >= 8 && bb.apart_rows >= sv.dimup &&
-      launch_hxv_fx2(sv, fv, cb.m, X, YW, bb.apart, st)) {
-    launch_fx_partial_reduce(cb.m, sv.dimup, bb.apart, fs.F + fs.G, bb.col_a, st);
+  const bool warp_only = g->cfg.hxv_variant == 1;
+  if (cb.m >= 16 && bb.wpart && bb.wpart_rows >= hxv_fx_cols_rows(sv, fv, cb.m, warp_only)) {
+    // alpha partials come out of the product kernel
+    const int rb = hxv_fx_cols_rows(sv, fv, cb.m, warp_only);
+    launch_hxv_fx_cols(sv, fv, cb.m, X, YW, bb.wpart, warp_only, st);
+    launch_fx_partial_reduce(cb.m, rb, bb.wpart, fs.F + fs.G, bb.col_a, st);
   } else {
-    if (cb.m >= 16 && (int64_t)sv.dimup * sv.dimdw * cb.m < ((int64_t)1 << 31))
-      launch_hxv_fx_w(sv, fv, cb.m, X, YW, st);
-    else
-      launch_hxv_fx(sv, fv, cb.m, X, YW, st);
+    launch_hxv_fx(sv, fv, cb.m, X, YW, st);
     launch_fx_dot(cb, X, YW, fs.F, fs.G, (i64*)bb.partial, bb.nblk, bb.col_a, st);
   }
   launch_chain_sum(cb, bb.col_a, bb.ch_a, st);
@@ -519,9 +569,12 @@ int lanczos_step_fx(const SectorView& sv, const FxView& fv, const ColBatch& cb, 
 
 int alloc_batch(Arena& ar, int64_t rows, int m, bool cplx, int nch, int ldab, BatchBufs& bb) {
   const size_t es = cplx ? sizeof(double2) : sizeof(double);
+  // fixed-point batches are slab-major with zero pad columns
+  const int mc = g->fx ? fx_cols_alloc(m) : m;
   for (int q = 0; q < 3; q++) {
     char* p;
-    RCHK(ar.alloc(&p, (size_t)rows * m * es));
+    RCHK(ar.alloc(&p, (size_t)rows * mc * es));
+    if (mc > m) CUCHK(cudaMemsetAsync(p, 0, (size_t)rows * mc * es, g->st));
     bb.b[q] = p;
   }
   bb.nblk = (int)std::min<int64_t>(std::max<int64_t>(1, rows / 256), 608);
@@ -529,8 +582,8 @@ int alloc_batch(Arena& ar, int64_t rows, int m, bool cplx, int nch, int ldab, Ba
   RCHK(ar.alloc(&bb.afx, nch));
   RCHK(ar.alloc(&bb.bfx, nch));
   RCHK(ar.alloc(&bb.scr, 2 * (size_t)nch));
-  bb.apart = nullptr;
-  bb.apart_rows = 0;
+  bb.wpart = nullptr;
+  bb.wpart_rows = 0;
   RCHK(ar.alloc(&bb.col_a, m));
   RCHK(ar.alloc(&bb.ch_a, nch));
   RCHK(ar.alloc(&bb.ch_b2, nch));
@@ -932,6 +985,7 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
   CUCHK(cudaMemGetInfo(&freeb, &totb));
   const size_t budget = (size_t)(0.5 * (double)freeb);
   int64_t maxcols = (int64_t)(budget / (3 * (size_t)D * es + 1));
+  if (g->fx && maxcols > FX_SLAB) maxcols = maxcols / FX_SLAB * FX_SLAB;  // room for the pad columns
   if (maxcols < 2) VFAIL(VCA_ERR_ALLOC, "not enough device memory for one Green's function chain");
   size_t q0 = 0;
   while (q0 < specs.size()) {
@@ -944,8 +998,9 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     BatchBufs bb;
     int rc = alloc_batch(ar, D, m, cplx, nch, g->ld, bb);
     if (!rc && g->fx) {
-      rc = ar.alloc(&bb.apart, 2 * (size_t)tv.dimup * m);
-      bb.apart_rows = tv.dimup;
+      const int rbw = hxv_fx_cols_rows(tv, fx_view_of(tup, tdw), m, g->cfg.hxv_variant == 1);
+      rc = ar.alloc(&bb.wpart, 2 * (size_t)rbw * m);
+      bb.wpart_rows = rbw;
     }
     double *norm2c, *norm2, *invn;
     ChainInit* d_ci;
@@ -1209,13 +1264,22 @@ int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, d
     cudaMemcpyAsync(d_z, zh.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, g->st);
   } else {
     n = c.omega_nodes;
-    double *s, *w;
-    if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = ar.alloc(&d_z, n)) || (rc = ar.alloc(&d_W, n))) {
-      ar.release();
-      return rc;
+    if (g->node_n != n || g->node_scale != c.omega_scale || !g->node_z) {
+      g->nodes.release();
+      g->node_n = 0;
+      double *s, *w;
+      if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = g->nodes.alloc(&g->node_z, n)) ||
+          (rc = g->nodes.alloc(&g->node_w, n))) {
+        ar.release();
+        return rc;
+      }
+      launch_gauss_legendre(n, s, w, g->st);
+      launch_omega_nodes(n, c.omega_scale, s, w, g->node_z, g->node_w, g->st);
+      g->node_n = n;
+      g->node_scale = c.omega_scale;
     }
-    launch_gauss_legendre(n, s, w, g->st);
-    launch_omega_nodes(n, c.omega_scale, s, w, d_z, d_W, g->st);
+    d_z = g->node_z;
+    d_W = g->node_w;
   }
   // G'(i w) in lso
   double2 *Glso, *P, *D = nullptr, *Hl;
@@ -1427,6 +1491,7 @@ int vca_gpu_last_error(char* buf, int32_t len) {
 int vca_gpu_finalize(void) {
   if (!g) return VCA_OK;
   g->work.release();
+  g->nodes.release();
   g->omega.release();
   g->gf.release();
   g->states.release();
@@ -1670,7 +1735,10 @@ int vca_gpu_sector_map(int32_t isector, int32_t spin, int64_t* map, int64_t cap)
   return VCA_OK;
 }
 
-static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t ncols) {
+// apart: optional alpha-partial scratch of the fixed-point column kernels
+// (hxv_fx_cols_rows rows of m int128), as the Lanczos chain steps pass it
+static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t ncols,
+                    i64* apart = nullptr) {
   if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
   if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
   if (ncols < 1) VFAIL(VCA_ERR_ARG, "ncols must be >= 1");
@@ -1678,16 +1746,12 @@ static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_com
   const int nup = sec_nup(isector), ndw = sec_ndw(isector);
   SectorView sv = view_of(nup, ndw);
   const int m = (is_complex && g->real_model) ? 2 * ncols : ncols;
-  if (g->fx) {  // buffers hold fixed-point columns (scale 2^-F, unit norm)
-    // column batches use the two-pass kernel of the Lanczos chains
-    if (g->cfg.hxv_variant == 2 && m >= 8 && g->apart_scratch && g->apart_rows >= sv.dimup &&
-        g->apart_cols >= m &&
-        launch_hxv_fx2(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->apart_scratch, g->st)) {
-      CUCHK(cudaGetLastError());
-      return VCA_OK;
-    }
-    if (m >= 16 && (int64_t)sv.dimup * sv.dimdw * m < ((int64_t)1 << 31))
-      launch_hxv_fx_w(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
+  if (g->fx) {  // slab-major fixed-point columns (scale 2^-F, unit norm)
+    if (m >= FX_SLAB && m % FX_SLAB)
+      VFAIL(VCA_ERR_ARG, "fixed-point column batches of 8 or more columns need a multiple of 8 columns");
+    if (m >= 16)
+      launch_hxv_fx_cols(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, apart,
+                         g->cfg.hxv_variant == 1, g->st);
     else
       launch_hxv_fx(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
   } else if (is_complex && !g->real_model) {
@@ -1748,18 +1812,19 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
   if (reps < 1 || !ms_per_call) VFAIL(VCA_ERR_ARG, "bad arguments");
   cudaEvent_t e0, e1;
   Arena ar;
-  if (g->fx) {  // scratch for the alpha partials of the two-pass kernel
-    const int64_t du = g->dimn[sec_nup(isector)];
-    const int64_t mm = (is_complex && g->real_model) ? 2 * (int64_t)ncols : ncols;
-    RCHK(ar.alloc(&g->apart_scratch, 2 * (size_t)du * mm));
-    g->apart_rows = du;
-    g->apart_cols = mm;
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  i64* apart = nullptr;
+  const int mm = (is_complex && g->real_model) ? 2 * ncols : ncols;
+  if (g->fx && mm >= 16) {  // the alpha partials the chain steps form with the product
+    const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+    const int rows = hxv_fx_cols_rows(view_of(nup, ndw), fx_view_of(nup, ndw), mm, g->cfg.hxv_variant == 1);
+    RCHK(ar.alloc(&apart, 2 * (size_t)rows * mm));
   }
   CUCHK(cudaEventCreate(&e0));
   CUCHK(cudaEventCreate(&e1));
-  RCHK(hxv_cols(isector, d_v, d_hv, is_complex, ncols));  // warm-up
+  RCHK(hxv_cols(isector, d_v, d_hv, is_complex, ncols, apart));  // warm-up
   CUCHK(cudaEventRecord(e0, g->st));
-  for (int r = 0; r < reps; r++) RCHK(hxv_cols(isector, d_v, d_hv, is_complex, ncols));
+  for (int r = 0; r < reps; r++) RCHK(hxv_cols(isector, d_v, d_hv, is_complex, ncols, apart));
   CUCHK(cudaEventRecord(e1, g->st));
   CUCHK(cudaEventSynchronize(e1));
   float ms = 0.f;
@@ -1768,8 +1833,6 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
   cudaEventDestroy(e1);
   CUCHK(cudaStreamSynchronize(g->st));
   ar.release();
-  g->apart_scratch = nullptr;
-  g->apart_rows = g->apart_cols = 0;
   *ms_per_call = ms / reps;
   return VCA_OK;
 }

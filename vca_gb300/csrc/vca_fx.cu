@@ -20,18 +20,16 @@ static inline int nblk_fx(int64_t n, int threads, int cap = 152 * 16) {
   return (int)b;
 }
 
-// 16-byte asynchronous global -> shared copies (sm_80+ cp.async): a CTA
-// issues its whole tile before waiting once, so many loads are in flight.
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-static void col_shape_fx(int m, dim3& blk) {
-  int cw = 1;
-  while (cw < m && cw < 32) cw <<= 1;
-  blk = dim3(cw, 256 / cw, 1);
+// Block shape of the per-column kernels on a slab-major batch: the W
+// columns of one slab across threadIdx.x, a power of two RB of rows across
+// threadIdx.y (W*RB <= 256), one slab per blockIdx.y.  A warp then covers
+// 32/W consecutive rows of one slab: contiguous 256-byte runs.
+static void slab_shape(int m, dim3& blk, int& nslab) {
+  const int W = fx_slab_w(m);
+  int rb = 1;
+  while (rb * 2 * W <= 256) rb <<= 1;
+  blk = dim3(W, rb, 1);
+  nslab = (m + W - 1) / W;
 }
 
 // round-half-up arithmetic shift of an int128 by s >= 0
@@ -107,10 +105,16 @@ __device__ __forceinline__ void acc_hop(i64 (&S)[K], signed char code, i64 v) {
   }
 }
 
+// Small-batch form: column c of slab blockIdx.y on threadIdx.x, rows on
+// threadIdx.y and the grid.
 template <int K>
 __global__ void k_hxv_fx(SectorView sv, FxView fv, int m, const i64* __restrict__ X, i64* __restrict__ Y) {
   const int64_t D = (int64_t)sv.dimup * sv.dimdw;
-  const int CW = blockDim.x;
+  const int W = blockDim.x;
+  if ((int)(blockIdx.y * W + threadIdx.x) >= m) return;
+  const int64_t sb = (int64_t)blockIdx.y * D * W + threadIdx.x;
+  const i64* Xs = X + sb;
+  i64* Ys = Y + sb;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; i < D;
        i += (int64_t)gridDim.x * blockDim.y) {
     const int idw = (int)(i / sv.dimup);
@@ -119,23 +123,21 @@ __global__ void k_hxv_fx(SectorView sv, FxView fv, int m, const i64* __restrict_
                     mixed_fx(fv, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
     const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
     const int64_t colbase = (int64_t)idw * sv.dimup;
-    for (int c = threadIdx.x; c < m; c += CW) {
-      i64 S[K];
+    i64 S[K];
 #pragma unroll
-      for (int k = 0; k < K; k++) S[k] = 0;
-      for (int h = 0; h < nu; h++) {
-        const int64_t o = (int64_t)h * sv.dimup + iup;
-        acc_hop<K>(S, fv.up_code[o], X[(colbase + sv.up_src[o]) * m + c]);
-      }
-      for (int h = 0; h < nd; h++) {
-        const int64_t o = (int64_t)h * sv.dimdw + idw;
-        acc_hop<K>(S, fv.dw_code[o], X[((int64_t)iup + (int64_t)sv.dw_src[o] * sv.dimup) * m + c]);
-      }
-      i128 p = (i128)dfx * X[i * m + c];
-#pragma unroll
-      for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
-      Y[i * m + c] = rshift_round(p, fv.shift);
+    for (int k = 0; k < K; k++) S[k] = 0;
+    for (int h = 0; h < nu; h++) {
+      const int64_t o = (int64_t)h * sv.dimup + iup;
+      acc_hop<K>(S, fv.up_code[o], Xs[(colbase + sv.up_src[o]) * W]);
     }
+    for (int h = 0; h < nd; h++) {
+      const int64_t o = (int64_t)h * sv.dimdw + idw;
+      acc_hop<K>(S, fv.dw_code[o], Xs[((int64_t)iup + (int64_t)sv.dw_src[o] * sv.dimup) * W]);
+    }
+    i128 p = (i128)dfx * Xs[i * W];
+#pragma unroll
+    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
+    Ys[i * W] = rshift_round(p, fv.shift);
   }
 }
 
@@ -143,14 +145,15 @@ __global__ void k_hxv_fx(SectorView sv, FxView fv, int m, const i64* __restrict_
 void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st) {
   count_launch_external();
   dim3 blk;
-  col_shape_fx(m, blk);
+  int ns;
+  slab_shape(m, blk, ns);
   const int64_t D = (int64_t)sv.dimup * sv.dimdw;
-  const int nb = nblk_fx(D, blk.y, 152 * 32);
+  const dim3 grd(nblk_fx(D, blk.y, 152 * 32), ns, 1);
   switch (fv.K) {
-    case 1: k_hxv_fx<1><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
-    case 2: k_hxv_fx<2><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
-    case 3: k_hxv_fx<3><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
-    default: k_hxv_fx<4><<<nb, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    case 1: k_hxv_fx<1><<<grd, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    case 2: k_hxv_fx<2><<<grd, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    case 3: k_hxv_fx<3><<<grd, blk, 0, st>>>(sv, fv, m, X, Y); break;
+    default: k_hxv_fx<4><<<grd, blk, 0, st>>>(sv, fv, m, X, Y); break;
   }
 }
 
@@ -161,10 +164,11 @@ __global__ void k_fx_dot(int64_t rows, int m, const i64* X, const i64* Y, i64* p
   extern __shared__ i128 shq[];
   const int CW = blockDim.x, RB = blockDim.y;
   const int c = blockIdx.y * CW + threadIdx.x;
+  const int64_t sb = (int64_t)blockIdx.y * rows * CW + threadIdx.x;
   i128 s = 0;
   if (c < m)
     for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB)
-      s += (i128)X[i * m + c] * Y[i * m + c];
+      s += (i128)X[sb + i * CW] * Y[sb + i * CW];
   shq[threadIdx.y * CW + threadIdx.x] = s;
   __syncthreads();
   for (int h = RB / 2; h > 0; h >>= 1) {
@@ -177,26 +181,15 @@ __global__ void k_fx_dot(int64_t rows, int m, const i64* X, const i64* Y, i64* p
     partial[2 * ((int64_t)blockIdx.x * m + c) + 1] = (i64)(v >> 64);
   }
 }
-__global__ void k_fx_dot_reduce(int m, int nblk, const i64* partial, int scale_exp, double* out) {
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
-    i128 s = 0;
-    for (int b = 0; b < nblk; b++) {
-      const u64 lo = (u64)partial[2 * ((int64_t)b * m + c)];
-      const i64 hi = partial[2 * ((int64_t)b * m + c) + 1];
-      s += (i128)(((unsigned __int128)(u64)hi << 64) | lo);
-    }
-    out[c] = i128_to_double(s, scale_exp);
-  }
-}
 void launch_fx_dot(const ColBatch& b, const i64* X, const i64* Y, int sx, int sy, i64* partial, int nblk,
                    double* out_col, cudaStream_t st) {
   count_launch_external();
-  count_launch_external();
   dim3 blk;
-  col_shape_fx(b.m, blk);
-  dim3 grd(nblk, (b.m + blk.x - 1) / blk.x, 1);
+  int ns;
+  slab_shape(b.m, blk, ns);
+  dim3 grd(nblk, ns, 1);
   k_fx_dot<<<grd, blk, sizeof(i128) * 256, st>>>(b.rows, b.m, X, Y, partial);
-  k_fx_dot_reduce<<<nblk_fx(b.m, 128), 128, 0, st>>>(b.m, nblk, partial, sx + sy, out_col);
+  launch_fx_partial_reduce(b.m, nblk, partial, sx + sy, out_col, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -213,24 +206,30 @@ void launch_fx_coef(int nch, const double* x, double scale, int C, i64* cfx, cud
 
 __global__ void k_fx_update(int64_t rows, int m, const int* col2ch, const ChainMeta* meta, int sh,
                             const i64* afx, const i64* bfx, int use_b, const i64* X, const i64* Xp,
-                            const i64* Y, i64* W) {
-  const int64_t n = rows * m;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int c = (int)(g % m);
-    const int ch = col2ch[c];
-    if (!meta[ch].active) continue;
-    i128 p = (i128)afx[ch] * X[g];
-    if (use_b) p += (i128)bfx[ch] * Xp[g];
-    W[g] = Y[g] - rshift_round(p, sh);
+                            const i64* Y, i64* Wo) {
+  const int CW = blockDim.x, RB = blockDim.y;
+  const int c = blockIdx.y * CW + threadIdx.x;
+  if (c >= m) return;
+  const int ch = col2ch[c];
+  if (!meta[ch].active) return;
+  const i64 a = afx[ch], b = use_b ? bfx[ch] : 0;
+  const int64_t sb = (int64_t)blockIdx.y * rows * CW + threadIdx.x;
+  for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB) {
+    const int64_t g = sb + i * CW;
+    i128 p = (i128)a * X[g];
+    if (use_b) p += (i128)b * Xp[g];
+    Wo[g] = Y[g] - rshift_round(p, sh);
   }
 }
 void launch_fx_update(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,
                       const i64* X, const i64* Xp, const i64* Y, i64* W, cudaStream_t st) {
   count_launch_external();
-  const int64_t n = b.rows * b.m;
-  k_fx_update<<<nblk_fx(n, 256), 256, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx, bfx,
-                                                use_b ? 1 : 0, X, Xp, Y, W);
+  dim3 blk;
+  int ns;
+  slab_shape(b.m, blk, ns);
+  const dim3 grd(nblk_fx(b.rows, blk.y), ns, 1);
+  k_fx_update<<<grd, blk, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx, bfx, use_b ? 1 : 0, X,
+                                   Xp, Y, W);
 }
 
 // per-chain multiplier m = round(f * 2^E) < 2^61 and shift E + si - so
@@ -248,8 +247,8 @@ __global__ void k_fx_mult(int nch, const double* f, int si, int so, i64* mul, i6
     sh[ch] = shift;
   }
 }
-// column-tiled: block (CW columns x RB rows), column from blockIdx.y, so no
-// per-element division by m
+// slab-tiled: block (W columns x RB rows), slab from blockIdx.y, so no
+// per-element division
 __global__ void k_fx_apply(int64_t rows, int m, const int* col2ch, const ChainMeta* meta, const i64* mul,
                            const i64* sh, int zero_inactive, const i64* Xi, i64* Xo) {
   const int CW = blockDim.x, RB = blockDim.y;
@@ -260,18 +259,20 @@ __global__ void k_fx_apply(int64_t rows, int m, const int* col2ch, const ChainMe
   if (!act && !zero_inactive) return;
   const i64 mu = mul[ch];
   const int s = (int)sh[ch];
+  const int64_t sb = (int64_t)blockIdx.y * rows * CW + threadIdx.x;
   for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB) {
-    const int64_t g = i * m + c;
+    const int64_t g = sb + i * CW;
     Xo[g] = act ? rshift_round((i128)mu * Xi[g], s) : 0;
   }
 }
 static void launch_apply(const ColBatch& b, const i64* mul, const i64* sh, int zero_inactive, const i64* Xi,
                          i64* Xo, cudaStream_t st) {
   dim3 blk;
-  col_shape_fx(b.m, blk);
+  int ns;
+  slab_shape(b.m, blk, ns);
   const int64_t nrb = (b.rows + blk.y - 1) / blk.y;
   const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(nrb, 152 * 16));
-  dim3 grd(gx, (b.m + blk.x - 1) / blk.x, 1);
+  dim3 grd(gx, ns, 1);
   k_fx_apply<<<grd, blk, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, mul, sh, zero_inactive, Xi, Xo);
 }
 void launch_fx_normalize(const ColBatch& b, const FxScales& s, const double* invbeta, const i64* W,
@@ -320,178 +321,37 @@ void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t
 }
 
 
-// ---------------------------------------------------------------------------
-// Two-pass H x v on column batches (fixed point).
-//
-// Pass A (up hops + diagonal): one CTA per (idw, column chunk); the block
-// X[:, idw, chunk] (DimUp x CW int64, <= 200 KB) is staged in shared memory,
-// so every up hop is a shared-memory load and X is read from DRAM once.
-// Pass B (down hops): one CTA per (iup, column chunk); X[iup, :, chunk]
-// (DimDw x CW) is staged likewise, Y is completed in place and the exact
-// int128 partial of alpha = <X, Y> is written per (iup, column).
-// DRAM per column element: A reads X, writes Y (16 B); B reads X, Y and
-// writes Y (24 B).
-// ---------------------------------------------------------------------------
-template <int K>
-__global__ void __launch_bounds__(256) k_hxv_fx_a(SectorView sv, FxView fv, int m, int cw,
-                                                  const i64* __restrict__ X, i64* __restrict__ Y) {
-  extern __shared__ i64 xs[];  // [DimUp][cw]
-  const int nchunk = (m + cw - 1) / cw;
-  const int idw = blockIdx.x / nchunk;
-  const int c0 = (blockIdx.x % nchunk) * cw;
-  const int ncol = min(cw, m - c0);
-  const int DU = sv.dimup;
-  const int64_t base = (int64_t)idw * DU;
-  if ((m & 1) == 0 && (ncol & 1) == 0 && (cw & 1) == 0) {
-    // pairs of int64 = 16 B; row starts (base+r)*m + c0 are even -> aligned
-    const int hp = cw >> 1, hn = ncol >> 1;
-    for (int t = threadIdx.x; t < DU * hp; t += blockDim.x) {
-      const int r = t / hp, q = t - r * hp;
-      if (q < hn) cp_async16(xs + r * cw + 2 * q, X + (base + r) * m + c0 + 2 * q);
-      else { xs[r * cw + 2 * q] = 0; xs[r * cw + 2 * q + 1] = 0; }
-    }
-    cp_async_wait_all();
-  } else {
-    for (int t = threadIdx.x; t < DU * cw; t += blockDim.x) {
-      const int r = t / cw, cc = t - r * cw;
-      xs[t] = (cc < ncol) ? X[(base + r) * m + c0 + cc] : 0;
-    }
-  }
-  __syncthreads();
-  const i64 edw = fv.dw_e1[idw];
-  const unsigned wd = (unsigned)sv.dw_words[idw];
-  for (int t = threadIdx.x; t < DU * cw; t += blockDim.x) {
-    const int r = t / cw, cc = t - r * cw;
-    if (cc >= ncol) continue;
-    const i64 dfx = fv.up_e1[r] + edw + mixed_fx(fv, (unsigned)sv.up_words[r], wd);
-    i64 S[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) S[k] = 0;
-    const int nu = sv.up_cnt[r];
-    for (int h = 0; h < nu; h++) {
-      const int64_t o = (int64_t)h * DU + r;
-      acc_hop<K>(S, fv.up_code[o], xs[sv.up_src[o] * cw + cc]);
-    }
-    i128 p = (i128)dfx * xs[t];
-#pragma unroll
-    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
-    Y[(base + r) * m + c0 + cc] = rshift_round(p, fv.shift);
-  }
-}
-
-template <int K>
-__global__ void __launch_bounds__(256) k_hxv_fx_b(SectorView sv, FxView fv, int m, int cw,
-                                                  const i64* __restrict__ X, i64* __restrict__ Y,
-                                                  i64* __restrict__ apart) {
-  extern __shared__ i64 xs[];  // [DimDw][cw]
-  __shared__ i128 red[256];
-  const int nchunk = (m + cw - 1) / cw;
-  const int iup = blockIdx.x / nchunk;
-  const int c0 = (blockIdx.x % nchunk) * cw;
-  const int ncol = min(cw, m - c0);
-  const int DU = sv.dimup, DD = sv.dimdw;
-  if ((m & 1) == 0 && (ncol & 1) == 0 && (cw & 1) == 0) {
-    const int hp = cw >> 1, hn = ncol >> 1;
-    for (int t = threadIdx.x; t < DD * hp; t += blockDim.x) {
-      const int r = t / hp, q = t - r * hp;
-      if (q < hn) cp_async16(xs + r * cw + 2 * q, X + ((int64_t)iup + (int64_t)r * DU) * m + c0 + 2 * q);
-      else { xs[r * cw + 2 * q] = 0; xs[r * cw + 2 * q + 1] = 0; }
-    }
-    cp_async_wait_all();
-  } else {
-    for (int t = threadIdx.x; t < DD * cw; t += blockDim.x) {
-      const int r = t / cw, cc = t - r * cw;
-      xs[t] = (cc < ncol) ? X[((int64_t)iup + (int64_t)r * DU) * m + c0 + cc] : 0;
-    }
-  }
-  __syncthreads();
-  // thread t always handles column t % cw (blockDim is a multiple of cw)
-  i128 adot = 0;
-  for (int t = threadIdx.x; t < DD * cw; t += blockDim.x) {
-    const int r = t / cw, cc = t - r * cw;
-    if (cc >= ncol) continue;
-    i64 S[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) S[k] = 0;
-    const int nd = sv.dw_cnt[r];
-    for (int h = 0; h < nd; h++) {
-      const int64_t o = (int64_t)h * DD + r;
-      acc_hop<K>(S, fv.dw_code[o], xs[sv.dw_src[o] * cw + cc]);
-    }
-    i128 p = 0;
-#pragma unroll
-    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k];
-    const int64_t g = ((int64_t)iup + (int64_t)r * DU) * m + c0 + cc;
-    const i64 y = Y[g] + rshift_round(p, fv.shift);
-    Y[g] = y;
-    adot += (i128)xs[t] * y;
-  }
-  red[threadIdx.x] = adot;
-  __syncthreads();
-  if ((int)threadIdx.x < cw) {
-    i128 s = 0;
-    for (int q = threadIdx.x; q < (int)blockDim.x; q += cw) s += red[q];
-    if ((int)threadIdx.x < ncol) {
-      const int64_t o = 2 * ((int64_t)iup * m + c0 + threadIdx.x);
-      apart[o] = (i64)(u64)s;
-      apart[o + 1] = (i64)(s >> 64);
-    }
-  }
-}
-
-// sum of int128 partials over `rows` rows per column -> double (scale 2^-sexp)
+// sum of int128 partials over `rows` rows per column -> double (scale
+// 2^-sexp): one warp per column, lanes stride the rows, then an exact
+// shuffle tree (the sum is exact, so the order does not matter)
 __global__ void k_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out) {
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int c = wid; c < m; c += nw) {
     i128 s = 0;
-    for (int b = 0; b < rows; b++) {
+    for (int b = lane; b < rows; b += 32) {
       const u64 lo = (u64)partial[2 * ((int64_t)b * m + c)];
       const i64 hi = partial[2 * ((int64_t)b * m + c) + 1];
       s += (i128)(((unsigned __int128)(u64)hi << 64) | lo);
     }
-    out[c] = i128_to_double(s, sexp);
+    u64 lo = (u64)s;
+    i64 hi = (i64)(s >> 64);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const u64 lo2 = __shfl_xor_sync(0xffffffffu, lo, off);
+      const i64 hi2 = __shfl_xor_sync(0xffffffffu, hi, off);
+      const u64 sl = lo + lo2;
+      hi = hi + hi2 + (sl < lo ? 1 : 0);
+      lo = sl;
+    }
+    if (lane == 0) out[c] = i128_to_double((i128)(((unsigned __int128)(u64)hi << 64) | lo), sexp);
   }
-}
-
-int hxv_fx_chunk(int rows, int m) {
-  const int budget = 100 * 1024 / 8;  // int64 slots: <= 100 KB so two CTAs share an SM
-  int cw = 32;
-  while (cw > 1 && (cw >= 2 * m || rows * cw > budget)) cw >>= 1;
-  if (rows * cw > budget) return 0;  // a single column does not fit
-  return cw;
-}
-
-bool launch_hxv_fx2(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
-                    cudaStream_t st) {
-  const int cwa = hxv_fx_chunk(sv.dimup, m), cwb = hxv_fx_chunk(sv.dimdw, m);
-  if (!cwa || !cwb) return false;
-  const size_t sha = (size_t)sv.dimup * cwa * sizeof(i64), shb = (size_t)sv.dimdw * cwb * sizeof(i64);
-  const int ga = sv.dimdw * ((m + cwa - 1) / cwa), gb = sv.dimup * ((m + cwb - 1) / cwb);
-  count_launch_external();
-  count_launch_external();
-#define VCA_FX2(KK)                                                                                  \
-  {                                                                                                  \
-    static bool attr = false;                                                                        \
-    if (!attr) {                                                                                     \
-      cudaFuncSetAttribute(k_hxv_fx_a<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 104 * 1024); \
-      cudaFuncSetAttribute(k_hxv_fx_b<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 104 * 1024); \
-      attr = true;                                                                                   \
-    }                                                                                                \
-  }                                                                                                  \
-  k_hxv_fx_a<KK><<<ga, 256, sha, st>>>(sv, fv, m, cwa, X, Y);                                        \
-  k_hxv_fx_b<KK><<<gb, 256, shb, st>>>(sv, fv, m, cwb, X, Y, apart);
-  switch (fv.K) {
-    case 1: VCA_FX2(1) break;
-    case 2: VCA_FX2(2) break;
-    case 3: VCA_FX2(3) break;
-    default: VCA_FX2(4) break;
-  }
-#undef VCA_FX2
-  return true;
 }
 
 void launch_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out, cudaStream_t st) {
   count_launch_external();
-  k_fx_partial_reduce<<<nblk_fx(m, 128), 128, 0, st>>>(m, rows, partial, sexp, out);
+  k_fx_partial_reduce<<<nblk_fx((int64_t)m * 32, 256), 256, 0, st>>>(m, rows, partial, sexp, out);
 }
 
 // W = Y - (afx*X + bfx*Xp) >> sh in place of Y, with the exact int128 partial
@@ -507,8 +367,9 @@ __global__ void k_fx_update_dot(int64_t rows, int m, const int* col2ch, const Ch
     const int ch = col2ch[c];
     if (meta[ch].active) {
       const i64 a = afx[ch], b = use_b ? bfx[ch] : 0;
+      const int64_t sb = (int64_t)blockIdx.y * rows * CW + threadIdx.x;
       for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.y; i < rows; i += (int64_t)gridDim.x * RB) {
-        const int64_t g = i * m + c;
+        const int64_t g = sb + i * CW;
         i128 p = (i128)a * X[g];
         if (use_b) p += (i128)b * Xp[g];
         const i64 w = YW[g] - rshift_round(p, sh);
@@ -534,8 +395,9 @@ void launch_fx_update_dot(const ColBatch& b, const FxScales& s, const i64* afx, 
                           cudaStream_t st) {
   count_launch_external();
   dim3 blk;
-  col_shape_fx(b.m, blk);
-  dim3 grd(nblk, (b.m + blk.x - 1) / blk.x, 1);
+  int ns;
+  slab_shape(b.m, blk, ns);
+  dim3 grd(nblk, ns, 1);
   k_fx_update_dot<<<grd, blk, sizeof(i128) * 256, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx,
                                                         bfx, use_b ? 1 : 0, X, Xp, YW, partial);
   launch_fx_partial_reduce(b.m, nblk, partial, 2 * s.G, out_col, st);
@@ -584,10 +446,61 @@ void launch_fx_pack(int dim, int width, const int* src, const double2* amp, cons
   k_fx_pack<<<nblk_fx(n, 256), 256, 0, st>>>(n, src, amp, classes, K, hop);
 }
 
+// In-place partition of each row's hop words, positive amplitudes first;
+// npos[row] = their count.  The fixed-point sums are exact, so the order of
+// a row's hops does not change any result.
+__global__ void k_fx_sign_sort(int dim, int width, const int* cnt, unsigned* hop, int* npos) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= dim) return;
+  int i = 0, j = cnt[r] - 1;
+  while (i <= j) {
+    const unsigned a = hop[r + (int64_t)i * dim];
+    if (!(a >> 31)) { i++; continue; }
+    const unsigned b = hop[r + (int64_t)j * dim];
+    hop[r + (int64_t)i * dim] = b;
+    hop[r + (int64_t)j * dim] = a;
+    j--;
+  }
+  npos[r] = i;
+}
+void launch_fx_sign_sort(int dim, int width, const int* cnt, unsigned* hop, int* npos, cudaStream_t st) {
+  if (dim == 0) return;
+  count_launch_external();
+  k_fx_sign_sort<<<(dim + 127) / 128, 128, 0, st>>>(dim, width, cnt, hop, npos);
+}
+
+__global__ void k_fx_perm_tables(int dim, int width, const int* perm, const unsigned* hop, const int* cnt,
+                                 const int* npos, const int* words, const i64* e1, unsigned* phop, int* pcnt,
+                                 int* pnpos, int* pword, i64* pe1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= dim) return;
+  const int r = perm[i];
+  pcnt[i] = cnt[r];
+  pnpos[i] = npos[r];
+  pword[i] = words[r];
+  pe1[i] = e1[r];
+  for (int h = 0; h < width; h++) {  // source as its first swizzled 16-byte unit (see fxs_unit)
+    const unsigned hw = hop[(int64_t)h * dim + r];
+    const unsigned src = hw & 0xFFFFFFu;
+    phop[(int64_t)h * dim + i] = (src * 4u + ((src >> 1) & 3u)) | (hw & 0xFF000000u);
+  }
+}
+void launch_fx_perm_tables(int dim, int width, const int* perm, const unsigned* hop, const int* cnt,
+                           const int* npos, const int* words, const i64* e1, unsigned* phop, int* pcnt,
+                           int* pnpos, int* pword, i64* pe1, cudaStream_t st) {
+  if (dim == 0) return;
+  count_launch_external();
+  k_fx_perm_tables<<<(dim + 127) / 128, 128, 0, st>>>(dim, width, perm, hop, cnt, npos, words, e1, phop, pcnt,
+                                                      pnpos, pword, pe1);
+}
+
 // accumulate one hop's source row into the class accumulators; the class and
-// sign are warp-uniform, so the branches do not diverge
+// sign are warp-uniform, so the branches do not diverge.  xr points at the
+// source row's first column within slab 0; coff[q] adds lane column q's slab
+// offset.
 template <int K, int NCQ>
-__device__ __forceinline__ void hop_row(i64 (&S)[K][NCQ], unsigned hw, const i64* __restrict__ xr, int lim) {
+__device__ __forceinline__ void hop_row(i64 (&S)[K][NCQ], unsigned hw, const i64* __restrict__ xr,
+                                        const int64_t (&coff)[NCQ], int lim) {
   const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
   const bool neg = hw >> 31;
 #pragma unroll
@@ -596,28 +509,45 @@ __device__ __forceinline__ void hop_row(i64 (&S)[K][NCQ], unsigned hw, const i64
     if (neg) {
 #pragma unroll
       for (int q = 0; q < NCQ; q++)
-        if (32 * q < lim) S[k][q] -= xr[32 * q];
+        if (32 * q < lim) S[k][q] -= xr[coff[q]];
     } else {
 #pragma unroll
       for (int q = 0; q < NCQ; q++)
-        if (32 * q < lim) S[k][q] += xr[32 * q];
+        if (32 * q < lim) S[k][q] += xr[coff[q]];
     }
   }
 }
 
-// MODE 0: full product (rows in idw-major order).
-// MODE 1: diagonal + up hops only, rows in idw-major order: a column block's
-//         up neighbours are the rows being processed, so they stay in L2.
-// MODE 2: down hops added into Y, rows in iup-major order: a slab's down
-//         neighbours stay in L2.  Modes 1 + 2 read X from DRAM about once each.
-template <int K, int NCQ, int MODE>
+// Column-batch H x v, warp form: one warp per row and 128 columns (4 per
+// lane) per CTA column slice (blockIdx.y), hop word decoded once per row and
+// slice.  Rows of 8-column slabs: lane column c of row r sits at
+// r*8 + (c/8)*8*D + c%8.
+// MODE 1: diagonal + up hops, rows in idw-major order (a column block's up
+//         neighbours are the rows in flight: L2 resident).
+// MODE 2: down hops added into Y, rows in iup-major order (a slab's down
+//         neighbours stay in L2); with apart != nullptr it also forms the
+//         exact int128 partials of alpha = <X, Y> per (row block, column).
+#define FXW_NCQ 4
+template <int K, int MODE>
 __global__ void __launch_bounds__(256) k_hxv_fx_w(SectorView sv, FxView fv, int m, const i64* __restrict__ X,
-                                                  i64* __restrict__ Y) {
-  const int lane = threadIdx.x & 31;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+                                                  i64* __restrict__ Y, i64* __restrict__ apart) {
+  constexpr int NCQ = FXW_NCQ, W = FX_SLAB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wid = blockIdx.x * (blockDim.x >> 5) + warp;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int c0 = blockIdx.y * 32 * NCQ;
+  const int lim = m - c0 - lane;  // column c0 + lane + 32q exists while 32q < lim
   const int DU = sv.dimup, DD = sv.dimdw;
   const int D = DU * DD;
+  int64_t coff[NCQ];
+#pragma unroll
+  for (int q = 0; q < NCQ; q++) {
+    const int c = c0 + lane + 32 * q;
+    coff[q] = (int64_t)(c / W) * W * D + (c % W);
+  }
+  i128 adot[NCQ];
+#pragma unroll
+  for (int q = 0; q < NCQ; q++) adot[q] = 0;
   for (int rr = wid; rr < D; rr += nw) {
     int idw, iup;
     if (MODE == 2) { iup = rr / DD; idw = rr - iup * DD; }
@@ -629,63 +559,339 @@ __global__ void __launch_bounds__(256) k_hxv_fx_w(SectorView sv, FxView fv, int 
     const int nu = (MODE == 2) ? 0 : sv.up_cnt[iup];
     const int nd = (MODE == 1) ? 0 : sv.dw_cnt[idw];
     const int colbase = idw * DU;
-    for (int c0 = 0; c0 < m; c0 += 32 * NCQ) {
-      const int lim = m - c0 - lane;  // column lane + 32q exists while 32q < lim
-      i64 S[K][NCQ];
+    i64 S[K][NCQ];
 #pragma unroll
-      for (int k = 0; k < K; k++)
+    for (int k = 0; k < K; k++)
 #pragma unroll
-        for (int q = 0; q < NCQ; q++) S[k][q] = 0;
-      for (int h = 0, o = iup; h < nu; h++, o += DU) {
-        const unsigned hw = fv.up_hop[o];
-        hop_row<K, NCQ>(S, hw, X + (int64_t)(colbase + (int)(hw & 0xFFFFFFu)) * m + c0 + lane, lim);
-      }
-      for (int h = 0, o = idw; h < nd; h++, o += DD) {
-        const unsigned hw = fv.dw_hop[o];
-        hop_row<K, NCQ>(S, hw, X + (int64_t)(iup + (int)(hw & 0xFFFFFFu) * DU) * m + c0 + lane, lim);
-      }
-      const i64* xo = X + (int64_t)r * m + c0 + lane;
-      i64* yo = Y + (int64_t)r * m + c0 + lane;
+      for (int q = 0; q < NCQ; q++) S[k][q] = 0;
+    for (int h = 0, o = iup; h < nu; h++, o += DU) {
+      const unsigned hw = fv.up_hop[o];
+      hop_row<K, NCQ>(S, hw, X + (int64_t)(colbase + (int)(hw & 0xFFFFFFu)) * W, coff, lim);
+    }
+    for (int h = 0, o = idw; h < nd; h++, o += DD) {
+      const unsigned hw = fv.dw_hop[o];
+      hop_row<K, NCQ>(S, hw, X + (int64_t)(iup + (int)(hw & 0xFFFFFFu) * DU) * W, coff, lim);
+    }
+    const i64* xo = X + (int64_t)r * W;
+    i64* yo = Y + (int64_t)r * W;
 #pragma unroll
-      for (int q = 0; q < NCQ; q++) {
-        if (32 * q < lim) {
-          i128 p = 0;
-          if (MODE != 2) p = (i128)dfx * xo[32 * q];
+    for (int q = 0; q < NCQ; q++) {
+      if (32 * q < lim) {
+        i128 p = 0;
+        if (MODE != 2) p = (i128)dfx * xo[coff[q]];
 #pragma unroll
-          for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k][q];
-          const i64 y = rshift_round(p, fv.shift);
-          yo[32 * q] = (MODE == 2) ? yo[32 * q] + y : y;
+        for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * S[k][q];
+        i64 y = rshift_round(p, fv.shift);
+        if (MODE == 2) {
+          y += yo[coff[q]];
+          if (apart) adot[q] += (i128)xo[coff[q]] * y;
         }
+        yo[coff[q]] = y;
+      }
+    }
+  }
+  if (MODE == 2 && apart) {  // block reduction of the alpha partials per column
+    __shared__ i128 red[8][32 * FXW_NCQ];
+#pragma unroll
+    for (int q = 0; q < NCQ; q++) red[warp][lane + 32 * q] = adot[q];
+    __syncthreads();
+    for (int t = threadIdx.x; t < 32 * NCQ; t += blockDim.x) {
+      i128 sum = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += red[w][t];
+      const int c = c0 + t;
+      if (c < m) {
+        const int64_t o2 = 2 * ((int64_t)blockIdx.x * m + c);
+        apart[o2] = (i64)(u64)sum;
+        apart[o2 + 1] = (i64)(sum >> 64);
       }
     }
   }
 }
 
-void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st) {
+// grid.x row blocks of the warp form (its alpha partial rows)
+int hxv_fx_w_rowblocks(int64_t D) { return nblk_fx(D * 32, 256, 152 * 6); }
+
+void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                     cudaStream_t st) {
   const int64_t D = (int64_t)sv.dimup * sv.dimdw;
-  const int blocks = nblk_fx(D * 32, 256, 152 * 8);
-  // columns per pass: 32*NCQ, NCQ limited so K*NCQ int64 accumulators stay in registers
-#define VCA_W(KK, NQ)                                                   \
-  do {                                                                  \
-    count_launch_external();                                            \
-    count_launch_external();                                            \
-    k_hxv_fx_w<KK, NQ, 1><<<blocks, 256, 0, st>>>(sv, fv, m, X, Y);     \
-    k_hxv_fx_w<KK, NQ, 2><<<blocks, 256, 0, st>>>(sv, fv, m, X, Y);     \
+  dim3 grd(hxv_fx_w_rowblocks(D), (m + 32 * FXW_NCQ - 1) / (32 * FXW_NCQ), 1);
+#define VCA_W(KK)                                                              \
+  do {                                                                         \
+    count_launch_external();                                                   \
+    count_launch_external();                                                   \
+    k_hxv_fx_w<KK, 1><<<grd, 256, 0, st>>>(sv, fv, m, X, Y, nullptr);          \
+    k_hxv_fx_w<KK, 2><<<grd, 256, 0, st>>>(sv, fv, m, X, Y, apart);            \
   } while (0)
-  const int ncq = (m + 31) / 32;
   switch (fv.K) {
-    case 1:
-      if (ncq <= 4) VCA_W(1, 4);
-      else if (ncq <= 8) VCA_W(1, 8);
-      else VCA_W(1, 16);
-      break;
-    case 2:
-      if (ncq <= 4) VCA_W(2, 4);
-      else VCA_W(2, 8);
-      break;
-    case 3: VCA_W(3, 4); break;
-    default: VCA_W(4, 4); break;
+    case 1: VCA_W(1); break;
+    case 2: VCA_W(2); break;
+    case 3: VCA_W(3); break;
+    default: VCA_W(4); break;
   }
 #undef VCA_W
 }
+
+// Column-batch H x v, staged form, for sectors whose up-spin block of one
+// slab fits shared memory.  One CTA per (slab cs, down configuration idw);
+// the slab is the slow grid index, so the CTAs in flight all work in one
+// slab (D*64 bytes, 47 MB for the 4x3 cluster's largest chain sectors: L2
+// resident).  The CTA's rows are the DimUp rows idw*DimUp + iup, one
+// contiguous block of X.  Three phases:
+//  1. down hops: the hop list of idw is the same for every row of the CTA,
+//     so the down part is a signed sum of whole blocks X[idw'] -- streamed
+//     with coalesced 16-byte loads into a shared accumulator (exact int64
+//     sums per class for K = 1, the exact int128 sum_k a_k S_k for K > 1);
+//     the CTA's own block is copied into shared memory alongside.
+//  2. up hops and diagonal: two lanes per row, four columns each (16-byte
+//     units q and q+2 of the row), sixteen rows per warp taken in order of
+//     their up-hop count (fv.up_perm) with their tables read in that order
+//     (fv.up_p*); hop lists are sign sorted, so the inner loops are plain
+//     64-bit adds or subtracts; every source row is a shared-memory read.
+//     y = round((d x + sum_k a_k S_k) 2^-shift) overwrites the accumulator.
+//  3. Y streams out with coalesced 16-byte stores; with apart != nullptr the
+//     exact int128 alpha partials <X,Y> of the CTA's columns go to row idw.
+// The 16-byte units of a staged row are XOR-swizzled by (row >> 1) & 3 so
+// random rows spread over the banks.  Pad columns (>= m) of X are zero, so
+// those of Y come out zero.
+__device__ __forceinline__ int fxs_unit(int row, int j) { return row * 4 + (j ^ ((row >> 1) & 3)); }
+
+
+template <int K>
+__global__ void __launch_bounds__(512, 2) k_hxv_fx_s(SectorView sv, FxView fv, int m, const i64* __restrict__ X,
+                                                     i64* __restrict__ Y, i64* __restrict__ apart) {
+  extern __shared__ __align__(16) unsigned char fxs_smem[];
+  constexpr int W = FX_SLAB, RPW = 16;
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int64_t D = (int64_t)DU * DD;
+  const int npair = DU * 4;                                 // 16-byte units per block
+  longlong2* xs2 = (longlong2*)fxs_smem;                   // [DU][4] X block (swizzled)
+  longlong2* ac2 = xs2 + npair;                            // [DU][4] down sums, then y
+  longlong2* ah2 = ac2 + npair;                            // [DU][4] high words (K > 1 only)
+  int64_t* doff = (int64_t*)(ah2 + (K > 1 ? npair : 0));   // idw's down hops: element offsets
+  unsigned char* dcl = (unsigned char*)(doff + sv.wdw);    // and classes
+  const int cs = blockIdx.x / DD;
+  const int idw = blockIdx.x - cs * DD;
+  const int c0 = cs * W;
+  const long long* Xs = (const long long*)X + (int64_t)cs * D * W;  // this slab
+  long long* Ys = (long long*)Y + (int64_t)cs * D * W;
+  const int64_t rowbase = (int64_t)idw * DU;
+  const int nd = sv.dw_cnt[idw];
+  const int ndp = fv.dw_npos[idw];
+  for (int h = threadIdx.x; h < nd; h += blockDim.x) {
+    const unsigned hw = fv.dw_hop[idw + h * DD];
+    doff[h] = (int64_t)(hw & 0xFFFFFFu) * DU * W;
+    dcl[h] = (unsigned char)((hw >> 24) & 3u);
+  }
+  __syncthreads();
+  // ---- phase 1: own block to shared memory, down blocks summed -----------
+  // each thread sums P1 units t, t + blockDim, ... per hop list pass
+  {
+    constexpr int FXS_P1 = (K == 1) ? 4 : 2;
+    const longlong2* xb = (const longlong2*)Xs;
+    const longlong2* own = xb + rowbase * (W / 2);
+    for (int t0 = threadIdx.x; t0 < npair; t0 += FXS_P1 * blockDim.x) {
+      u64 S[K][FXS_P1][2];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+#pragma unroll
+        for (int e = 0; e < FXS_P1; e++) S[k][e][0] = S[k][e][1] = 0;
+      const bool full = t0 + (FXS_P1 - 1) * (int)blockDim.x < npair;
+      for (int h = 0; h < nd; h++) {
+        const longlong2* src = xb + (doff[h] >> 1) + t0;
+        const int cls = (K == 1) ? 0 : (int)dcl[h];
+        longlong2 v[FXS_P1];
+#pragma unroll
+        for (int e = 0; e < FXS_P1; e++)
+          v[e] = (full || t0 + e * (int)blockDim.x < npair) ? __ldcg(src + e * blockDim.x) : make_longlong2(0, 0);
+        if (h < ndp) {
+#pragma unroll
+          for (int k = 0; k < K; k++)
+            if (k == cls)
+#pragma unroll
+              for (int e = 0; e < FXS_P1; e++) { S[k][e][0] += (u64)v[e].x; S[k][e][1] += (u64)v[e].y; }
+        } else {
+#pragma unroll
+          for (int k = 0; k < K; k++)
+            if (k == cls)
+#pragma unroll
+              for (int e = 0; e < FXS_P1; e++) { S[k][e][0] -= (u64)v[e].x; S[k][e][1] -= (u64)v[e].y; }
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < FXS_P1; e++) {
+        const int t = t0 + e * blockDim.x;
+        if (t >= npair) break;
+        const int su = fxs_unit(t >> 2, t & 3);
+        xs2[su] = __ldcg(own + t);
+        if (K == 1) {
+          ac2[su] = make_longlong2((long long)S[0][e][0], (long long)S[0][e][1]);
+        } else {
+          i128 p0 = 0, p1 = 0;
+#pragma unroll
+          for (int k = 0; k < K; k++) {
+            p0 += (i128)fv.afx[k] * (i64)S[k][e][0];
+            p1 += (i128)fv.afx[k] * (i64)S[k][e][1];
+          }
+          ac2[su] = make_longlong2((long long)(u64)p0, (long long)(u64)p1);
+          ah2[su] = make_longlong2((long long)(p0 >> 64), (long long)(p1 >> 64));
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // ---- phase 2: up hops and diagonal, y into the accumulator -------------
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  {
+    const int sub = lane >> 1, q = lane & 1;  // units q and q+2: columns 2q,2q+1,2q+4,2q+5
+    const i64 e1d = fv.dw_e1[idw];
+    const unsigned wdw = (unsigned)sv.dw_words[idw];
+    for (int i = warp * RPW + sub; i < DU; i += nwarp * RPW) {
+      const int iup = fv.up_perm[i];
+      u64 S[K][4];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) S[k][j] = 0;
+      const int nu = fv.up_pcnt[i];
+      const int nup = fv.up_pnpos[i];
+      // table entries hold fxs_unit(src, 0); units q and q+2 are that ^ q and ^ (q|2)
+      int h = 0, o = i;
+#pragma unroll 2
+      for (; h < nup; h++, o += DU) {
+        const unsigned hw = fv.up_phop[o];
+        const int ua = (int)(hw & 0xFFFFFFu) ^ q;
+        const longlong2 a = xs2[ua], b2 = xs2[ua ^ 2];
+        const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (k == cls) { S[k][0] += a.x; S[k][1] += a.y; S[k][2] += b2.x; S[k][3] += b2.y; }
+      }
+#pragma unroll 2
+      for (; h < nu; h++, o += DU) {
+        const unsigned hw = fv.up_phop[o];
+        const int ua = (int)(hw & 0xFFFFFFu) ^ q;
+        const longlong2 a = xs2[ua], b2 = xs2[ua ^ 2];
+        const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (k == cls) { S[k][0] -= a.x; S[k][1] -= a.y; S[k][2] -= b2.x; S[k][3] -= b2.y; }
+      }
+      const int ua = fxs_unit(iup, q), ub = fxs_unit(iup, q + 2);
+      const longlong2 xa = xs2[ua], xb = xs2[ub];
+      const i64 x0[4] = {xa.x, xa.y, xb.x, xb.y};
+      const longlong2 da = ac2[ua], db = ac2[ub];
+      const i64 dlo[4] = {da.x, da.y, db.x, db.y};
+      i64 dhi[4] = {0, 0, 0, 0};
+      if (K > 1) {
+        const longlong2 ha = ah2[ua], hb = ah2[ub];
+        dhi[0] = ha.x; dhi[1] = ha.y; dhi[2] = hb.x; dhi[3] = hb.y;
+      }
+      const i64 dfx = fv.up_pe1[i] + e1d + mixed_fx(fv, (unsigned)fv.up_pword[i], wdw);
+      i64 y[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        i128 p = (i128)dfx * x0[j];
+        if (K == 1) {
+          p += (i128)fv.afx[0] * (i64)(S[0][j] + (u64)dlo[j]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * (i64)S[k][j];
+          p += (i128)(((unsigned __int128)(u64)dhi[j] << 64) | (u64)dlo[j]);
+        }
+        y[j] = rshift_round(p, fv.shift);
+      }
+      ac2[ua] = make_longlong2(y[0], y[1]);
+      ac2[ub] = make_longlong2(y[2], y[3]);
+    }
+  }
+  __syncthreads();
+  // ---- phase 3: Y out, alpha partials -------------------------------------
+  {
+    longlong2* yb = (longlong2*)Ys + rowbase * (W / 2);
+    i128 ad0 = 0, ad1 = 0;  // columns 2u, 2u+1 with u = threadIdx.x & 3
+    for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+      const int su = fxs_unit(t >> 2, t & 3);
+      const longlong2 yv = ac2[su];
+      __stcs(yb + t, yv);
+      if (apart) {
+        const longlong2 xv = xs2[su];
+        ad0 += (i128)xv.x * yv.x;
+        ad1 += (i128)xv.y * yv.y;
+      }
+    }
+    if (apart) {
+      __shared__ i128 red[16][W];
+      const int u = lane & 3;
+      i128 adv[2] = {ad0, ad1};
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        u64 lo = (u64)adv[j];
+        i64 hi = (i64)(adv[j] >> 64);
+#pragma unroll
+        for (int off = 4; off < 32; off <<= 1) {  // lanes holding the same columns
+          const u64 lo2 = __shfl_xor_sync(0xffffffffu, lo, off);
+          const i64 hi2 = __shfl_xor_sync(0xffffffffu, hi, off);
+          const u64 sl = lo + lo2;
+          hi = hi + hi2 + (sl < lo ? 1 : 0);
+          lo = sl;
+        }
+        if (lane < 4) red[warp][2 * u + j] = ((i128)hi << 64) | (i128)lo;
+      }
+      __syncthreads();
+      if ((int)threadIdx.x < W && c0 + (int)threadIdx.x < m) {
+        i128 sum = 0;
+        for (int w = 0; w < nwarp; w++) sum += red[w][threadIdx.x];
+        const int64_t o2 = 2 * ((int64_t)idw * m + c0 + threadIdx.x);
+        apart[o2] = (i64)(u64)sum;
+        apart[o2 + 1] = (i64)(sum >> 64);
+      }
+    }
+  }
+}
+
+#define FXS_THREADS 512
+#define FXS_SMEM_MAX (220 * 1024)
+static size_t hxv_fx_s_smem(const SectorView& sv, int K) {
+  // X block, down sums (and their high words for K > 1), down hop table
+  return (size_t)sv.dimup * FX_SLAB * sizeof(i64) * (K > 1 ? 3 : 2) + (size_t)sv.wdw * 9 + 16;
+}
+
+static bool hxv_fx_s_ok(const SectorView& sv, const FxView& fv, int m, bool warp_only) {
+  return !warp_only && fv.up_perm && fv.up_phop && fv.dw_npos && m >= FX_SLAB &&
+         hxv_fx_s_smem(sv, fv.K) <= FXS_SMEM_MAX &&
+         (int64_t)sv.dimdw * ((m + FX_SLAB - 1) / FX_SLAB) < ((int64_t)1 << 31);
+}
+
+template <int K>
+static void launch_hxv_fx_s_k(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                              cudaStream_t st) {
+  static bool attr_set = false;  // per instantiation, process-wide (every device is sm_103a)
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_hxv_fx_s<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, FXS_SMEM_MAX);
+    attr_set = true;
+  }
+  const int ns = (m + FX_SLAB - 1) / FX_SLAB;
+  count_launch_external();
+  k_hxv_fx_s<K><<<sv.dimdw * ns, FXS_THREADS, hxv_fx_s_smem(sv, K), st>>>(sv, fv, m, X, Y, apart);
+}
+
+int hxv_fx_cols_rows(const SectorView& sv, const FxView& fv, int m, bool warp_only) {
+  if (hxv_fx_s_ok(sv, fv, m, warp_only)) return sv.dimdw;
+  return hxv_fx_w_rowblocks((int64_t)sv.dimup * sv.dimdw);
+}
+
+void launch_hxv_fx_cols(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                        bool warp_only, cudaStream_t st) {
+  if (hxv_fx_s_ok(sv, fv, m, warp_only)) {
+    switch (fv.K) {
+      case 1: launch_hxv_fx_s_k<1>(sv, fv, m, X, Y, apart, st); break;
+      case 2: launch_hxv_fx_s_k<2>(sv, fv, m, X, Y, apart, st); break;
+      case 3: launch_hxv_fx_s_k<3>(sv, fv, m, X, Y, apart, st); break;
+      default: launch_hxv_fx_s_k<4>(sv, fv, m, X, Y, apart, st); break;
+    }
+    return;
+  }
+  launch_hxv_fx_w(sv, fv, m, X, Y, apart, st);
+}
+
 }  // namespace vca

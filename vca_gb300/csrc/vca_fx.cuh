@@ -39,6 +39,19 @@ struct FxView {
   const unsigned* dw_hop;
   const i64* up_e1;            // one-body + same-spin diagonal, scale 2^-A
   const i64* dw_e1;
+  const int* up_npos;          // [dim]: leading positive hops of each row (hops sign sorted)
+  const int* dw_npos;
+  const int* up_perm;          // [dim]: up rows in order of decreasing hop count
+  // up-spin tables re-indexed by position in up_perm (coalesced for the
+  // staged column kernel): hop words [width*dim] k-major with the source as
+  // its first swizzled shared-memory unit (4 src + ((src >> 1) & 3)) and the
+  // class in bits 24-25, counts, positive counts, configurations, one-body
+  // energies
+  const unsigned* up_phop;
+  const int* up_pcnt;
+  const int* up_pnpos;
+  const int* up_pword;
+  const i64* up_pe1;
   int K;
   i64 afx[VCA_FX_KMAX];        // class amplitudes, scale 2^-A
   int norb;
@@ -49,18 +62,49 @@ struct FxView {
   int shift;                   // A + F - G
 };
 
+// Column batches of the fixed-point path are slab-major: slabs of W =
+// fx_slab_w(m) adjacent columns, each slab one contiguous [D][W] block, so
+// element (row i, column c) sits at ((c / W) * D + i) * W + c % W.  W = 8
+// once m >= 8 (memory holds fx_cols_alloc(m) columns, the pad columns stay
+// zero); below 8 columns W = m, plain row-major.  A slab of a 4x3-cluster
+// sector is 47 MB, so the slab an H x v kernel works on stays in L2.
+#define FX_SLAB 8
+__host__ __device__ __forceinline__ int fx_slab_w(int m) { return m >= FX_SLAB ? FX_SLAB : m; }
+__host__ __device__ __forceinline__ int fx_cols_alloc(int m) {
+  return m >= FX_SLAB ? (m + FX_SLAB - 1) / FX_SLAB * FX_SLAB : m;
+}
+__host__ __device__ __forceinline__ int64_t fx_off(int64_t D, int W, int64_t i, int c) {
+  return ((int64_t)(c / W) * D + i) * W + c % W;
+}
+
+// up-spin tables in the order of perm (see FxView::up_phop)
+void launch_fx_perm_tables(int dim, int width, const int* perm, const unsigned* hop, const int* cnt,
+                           const int* npos, const int* words, const i64* e1, unsigned* phop, int* pcnt,
+                           int* pnpos, int* pword, i64* pe1, cudaStream_t st);
+// partition each row's hop words positive-first in place; npos[row] counts them
+void launch_fx_sign_sort(int dim, int width, const int* cnt, unsigned* hop, int* npos, cudaStream_t st);
 // packed hop words src | class<<24 | sign<<31 from the FP64 tables
 void launch_fx_pack(int dim, int width, const int* src, const double2* amp, const double* classes, int K,
                     unsigned* hop, cudaStream_t st);
-// Y = H X on a column batch, one warp per row streaming all m columns per hop
-// (needs DimUp*DimDw*m < 2^31)
-void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st);
+// Y = H X on a slab-major column batch (m >= 16), one warp per row and
+// 128-column slice; with apart != nullptr also the exact alpha partials
+// <X,Y> per (row block, column), hxv_fx_w_rowblocks(D) rows of m int128
+void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                     cudaStream_t st);
+int hxv_fx_w_rowblocks(int64_t D);
+// Y = H X on a slab-major column batch (m >= 16) through the fastest form
+// the sector allows (shared-memory staged up block while DimUp*64 bytes fit
+// and warp_only is false, else the warp form); apart, when given, needs
+// hxv_fx_cols_rows(...) rows of m int128
+int hxv_fx_cols_rows(const SectorView& sv, const FxView& fv, int m, bool warp_only);
+void launch_hxv_fx_cols(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                        bool warp_only, cudaStream_t st);
 // per-hop class/sign codes from the FP64 amplitude tables
 void launch_fx_codes(int dim, int width, const double2* amp, const double* classes, int K,
                      signed char* code, cudaStream_t st);
 // FP64 one-body table -> fixed point
 void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st);
-// Y = H X (FX) on a column batch
+// Y = H X (FX) on a slab-major column batch, any m (the small-batch form)
 void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st);
 // per-column exact dot: out_col[c] = (sum X*Y) * 2^-(sx+sy) (double)
 void launch_fx_dot(const ColBatch& b, const i64* X, const i64* Y, int sx, int sy, i64* partial, int nblk,
@@ -81,16 +125,12 @@ void launch_fx_psi_accum(int64_t n, const double* s, int k, const i64* X, i64* p
 // FP64 <-> fixed point (one-time conversions)
 void launch_fx_from_double(int64_t n, const double* x, int F, i64* X, cudaStream_t st);
 void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t st);
-// chain start vectors by exact gather (+/- psi, re/im columns) from a FX ground state
+// chain start vectors by exact gather (+/- psi, re/im columns) from a FX
+// ground state, into a slab-major batch of m columns
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const i64* gs, int nchain,
                           const ChainInit* d_ci, int m, i64* X, cudaStream_t st);
 
-// two-pass H x v (shared-memory staged up and down blocks) with the exact
-// alpha partials <X,Y> per (iup, column) in apart[2*DimUp*m]; returns false
-// when a column block does not fit in shared memory
-bool launch_hxv_fx2(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
-                    cudaStream_t st);
-int hxv_fx_chunk(int rows, int m);
+// out[c] = (sum over `rows` int128 partials of column c) * 2^-sexp
 void launch_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out, cudaStream_t st);
 // fused W = Y - a X - b Xp and beta^2 partials (out_col = <W,W> per column)
 void launch_fx_update_dot(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,

@@ -2,6 +2,7 @@
 // path (GB300).  Every grid is bounded by its buffers: grid-stride loops over
 // explicit 64-bit extents, no device-side waits.
 #include "vca_kernels.cuh"
+#include "vca_fx.cuh"
 #include "vca_tri.cuh"
 
 #include <cmath>
@@ -588,7 +589,9 @@ void launch_chain_poles(int nch, const ChainMeta* meta, const double* A, const d
                         double zeta, double* work, double* poles, double2* weights, int* nexc,
                         cudaStream_t st) {
   COUNT_LAUNCH();
-  k_chain_poles<<<nblocks(nch, 64), 64, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta,
+  // one warp per block: the chains' FP64 work spreads over as many SMs as
+  // there are warps of chains
+  k_chain_poles<<<nblocks(nch, 32), 32, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta,
                                                  work, poles, weights, nexc);
 }
 
@@ -603,6 +606,7 @@ __global__ void k_chain_init(SectorView tgt, int src_dimup, const void* gsv, int
                              const ChainInit* ci, int m, void* Xv) {
   const int64_t D = (int64_t)tgt.dimup * tgt.dimdw;
   const int64_t n = D * nchain;
+  const int W = fx_slab_w(m);  // slab-major batch
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int ch = (int)(g % nchain);
@@ -1102,6 +1106,7 @@ __global__ void k_chain_init_fx(SectorView tgt, int src_dimup, const long long* 
                                 const ChainInit* ci, int m, long long* X) {
   const int64_t D = (int64_t)tgt.dimup * tgt.dimdw;
   const int64_t n = D * nchain;
+  const int W = fx_slab_w(m);  // slab-major batch
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int ch = (int)(g % nchain);
@@ -1125,8 +1130,8 @@ __global__ void k_chain_init_fx(SectorView tgt, int src_dimup, const long long* 
       vr += cr * gv;
       vi += cim * gv;
     }
-    X[i * m + c.col0] = vr;
-    if (c.cplxcol) X[i * m + c.col0 + 1] = vi;
+    X[fx_off(D, W, i, c.col0)] = vr;
+    if (c.cplxcol) X[fx_off(D, W, i, c.col0 + 1)] = vi;
   }
 }
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long* gs, int nchain,
