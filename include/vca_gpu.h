@@ -229,6 +229,20 @@ int vca_gpu_hxv_device(int32_t isector, const void* d_v, void* d_hv, int32_t is_
 int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex,
                       int32_t ncols, int32_t reps, double* ms_per_call);
 
+/* Allocation-free column H x v: Y = H X on ncols real columns of sector
+ * isector (device buffers laid out as for vca_gpu_hxv_timed) and
+ * d_alpha[c] = <x_c, H x_c> (device, ncols doubles), on the library stream.
+ * For callers that cannot call cudaMalloc while they run (device memory owned
+ * by their own pool allocator, or a sweep that must not reach the driver's
+ * allocator mid-run): the partial sums behind alpha live in a static 8 MiB
+ * device array, so the call allocates nothing.  Batches whose partial sums
+ * exceed 8 MiB are rejected with VCA_ERR_ARG.  The first call on a device
+ * looks the array up (make it before any stream capture); all calls share
+ * the array, so calls whose work overlaps on the GPU race.  No counterpart in
+ * the reference. */
+int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void* d_hv, int32_t ncols,
+                              double* d_alpha);
+
 /* ---- residency and diagnostics (no counterpart in the reference) -------- */
 /* Upload Hk (as in vca_gpu_solve) and keep it resident on the device. */
 int vca_gpu_upload_hk(const double* Hk, int64_t Nk);

@@ -1889,3 +1889,86 @@ int vca_gpu_synchronize(void) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free column H x v with the per-column Rayleigh numerator.
+//
+// Some callers cannot call cudaMalloc while they run: a host code whose
+// device memory belongs to its own pool allocator sized at start-up, or a
+// sweep loop that must not reach the driver's allocator mid-run (cudaMalloc
+// can stall the device and can fail when memory is tight).  For them,
+// vca_gpu_hxv_alpha_noalloc does the column H x v of vca_gpu_hxv_timed and
+// also forms alpha[c] = <x_c, H x_c>, keeping its partial sums in the
+// file-scope device array below instead of allocated scratch.
+//
+// The array's device address is looked up once per device, by the first call
+// made while that device is current; make that first call before any stream
+// capture.  Every call on a device shares the array and the array keeps the
+// last call's contents: each partial is overwritten before it is read, so
+// nothing needs clearing, but calls whose work overlaps on the GPU race.
+// ---------------------------------------------------------------------------
+#define VCA_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define VCA_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) unsigned char g_noalloc_scratch[VCA_NOALLOC_SCRATCH_BYTES];
+static void* g_noalloc_addr[VCA_NOALLOC_MAX_DEVICES];
+
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  CUCHK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= VCA_NOALLOC_MAX_DEVICES) VFAIL(VCA_ERR_CUDA, "device ordinal beyond the scratch table");
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    CUCHK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return VCA_OK;
+}
+
+extern "C" int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void* d_hv, int32_t ncols,
+                                         double* d_alpha) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  if (ncols < 1 || !d_v || !d_hv || !d_alpha) VFAIL(VCA_ERR_ARG, "bad arguments");
+  if (!g->real_model) VFAIL(VCA_ERR_UNSUPPORTED, "real columns need a real Hamiltonian");
+  const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+  const SectorView sv = view_of(nup, ndw);
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const int m = ncols;
+  const bool warp_only = g->cfg.hxv_variant == 1;
+  // partial rows of the reduction behind alpha, as the Lanczos steps size them
+  const int nblk = (int)std::min<int64_t>(std::max<int64_t>(1, D / 256), 608);
+  int rows = nblk;
+  size_t need;
+  if (g->fx) {
+    if (m >= FX_SLAB && m % FX_SLAB)
+      VFAIL(VCA_ERR_ARG, "fixed-point column batches of 8 or more columns need a multiple of 8 columns");
+    if (m >= 16) rows = hxv_fx_cols_rows(sv, fx_view_of(nup, ndw), m, warp_only);
+    need = (size_t)rows * m * 2 * sizeof(i64);
+  } else {
+    need = (size_t)rows * m * sizeof(double);
+  }
+  if (need > VCA_NOALLOC_SCRATCH_BYTES)
+    VFAIL(VCA_ERR_ARG, "this batch needs " + std::to_string(need) +
+                           " bytes of partial sums; the static scratch holds " +
+                           std::to_string((size_t)VCA_NOALLOC_SCRATCH_BYTES) + " (use fewer columns)");
+  void* scr = nullptr;
+  RCHK(noalloc_scratch(&scr));
+  const ColBatch cb{D, m, false, 0, nullptr, nullptr};
+  if (g->fx) {
+    const FxView fv = fx_view_of(nup, ndw);
+    const int sexp = g->fxs.F + g->fxs.G;
+    if (m >= 16) {
+      launch_hxv_fx_cols(sv, fv, m, (const i64*)d_v, (i64*)d_hv, (i64*)scr, warp_only, g->st);
+      launch_fx_partial_reduce(m, rows, (const i64*)scr, sexp, d_alpha, g->st);
+    } else {
+      launch_hxv_fx(sv, fv, m, (const i64*)d_v, (i64*)d_hv, g->st);
+      launch_fx_dot(cb, (const i64*)d_v, (const i64*)d_hv, g->fxs.F, g->fxs.G, (i64*)scr, rows, d_alpha, g->st);
+    }
+  } else {
+    launch_hxv_real(sv, g->md, m, (const double*)d_v, (double*)d_hv, g->st);
+    launch_col_dot(cb, d_v, d_hv, (double*)scr, rows, d_alpha, g->st);
+  }
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
