@@ -144,3 +144,36 @@ def test_fixed_point_and_fp64_paths_agree(name, arith):
     np.testing.assert_allclose(s.sector_energies(), o.sector_energies(), rtol=E_TOL, atol=E_TOL)
     z = 1j * np.array([0.05, 0.3, 1.0, 3.0, 10.0])
     assert np.abs(s.gf_cluster(z) - o.gf_cluster(z)).max() < G_TOL
+
+
+def test_gf_channel_poles_match_oracle():
+    """Poles and weights of single channels (formed on demand from the stored
+    chain tridiagonals) against the oracle's, compared as the pole sums
+    sum_j w_j / (z - p_j) at points off the real axis (1e-8 absolute), and
+    against the continued-fraction G'(z) of the solve for a diagonal element."""
+    pt = POINTS["square2x2_afm"]()
+    s = VcaSolver(pt.cfg)
+    s.solve(pt.Hloc, pt.Hk)
+    o = Oracle.from_point(pt)
+    o.solve()
+    z = np.array([0.3 + 0.1j, -1.0 + 1.0j, 2.0 + 5.0j])
+
+    def psum(p, w):
+        return (w[None, :] / (z[:, None] - p[None, :].real)).sum(axis=1)
+
+    checked = 0
+    for il, jl in ((1, 1), (1, 2), (2, 4)):
+        for ispin in (1, 2):
+            for ichan in (1, 2, 3, 4):
+                if il == jl and ichan > 2:
+                    continue
+                p, w = s.gf_channel(il, jl, ispin, 1, 1, 1, ichan)
+                ref = o.gf_channel(il, jl, ispin, 1, 1, 0, ichan)  # oracle states are 0-based
+                assert ref is not None and len(p) == len(ref[0])
+                assert np.abs(psum(p, w) - psum(ref[0], ref[1])).max() < G_TOL
+                checked += 1
+    assert checked == 20
+    # diagonal element: particle + hole channels of the ground state = G'_11
+    g = s.gf_cluster(z)[0, 0, 0, 0, 0, 0, :]
+    tot = sum(psum(*s.gf_channel(1, 1, 1, 1, 1, 1, ch)) for ch in (1, 2))
+    assert np.abs(g - tot).max() < 1e-10

@@ -129,9 +129,11 @@ struct Ctx {
   double egs = 0, zeta = 0, omega_int = 0, sft = 0;
   std::vector<ChainRec> chains;
   int ld = 0;
-  double* d_poles = nullptr;
+  double* d_poles = nullptr;     // filled on demand from the chain store
   double2* d_weights = nullptr;
   int* d_nexc = nullptr;
+  bool poles_ready = false;
+  ChainStore cstore{};
   int nelem = 0;
   int* d_elem_ptr = nullptr;
   int* d_elem_chain = nullptr;
@@ -1006,14 +1008,12 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     ChainInit* d_ci;
     int* d_isign;
     double2* d_wfac;
-    double* d_work;
     if (!rc) rc = ar.alloc(&norm2c, m);
     if (!rc) rc = ar.alloc(&norm2, nch);
     if (!rc) rc = ar.alloc(&invn, nch);
     if (!rc) rc = ar.alloc(&d_ci, nch);
     if (!rc) rc = ar.alloc(&d_isign, nch);
     if (!rc) rc = ar.alloc(&d_wfac, nch);
-    if (!rc) rc = ar.alloc(&d_work, (size_t)nch * 3 * g->ld);
     if (rc) { ar.release(); return rc; }
     std::vector<ChainMeta> meta(nch);
     std::vector<int> col2ch(m);
@@ -1059,9 +1059,8 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     }
     // poles and weights into the global chain table
     const int base = (int)g->chains.size();
-    launch_chain_poles(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, g->zeta, d_work,
-                       g->d_poles + (size_t)base * g->ld, g->d_weights + (size_t)base * g->ld,
-                       g->d_nexc + base, g->st);
+    launch_chain_store(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, g->zeta, g->cstore, base,
+                       g->st);
     CUCHK(cudaGetLastError());
     CUCHK(cudaStreamSynchronize(g->st));
     for (int q = 0; q < nch; q++) g->chains.push_back(specs[q0 + q].rec);
@@ -1088,6 +1087,17 @@ int build_gf() {
   RCHK(g->gf.alloc(&g->d_weights, (size_t)nmax * g->ld));
   RCHK(g->gf.alloc(&g->d_nexc, nmax));
   CUCHK(cudaMemsetAsync(g->d_nexc, 0, sizeof(int) * nmax, g->st));
+  g->poles_ready = false;
+  ChainStore& cs = g->cstore;
+  cs.ld = g->ld;
+  RCHK(g->gf.alloc(&cs.A, (size_t)nmax * g->ld));
+  RCHK(g->gf.alloc(&cs.B, (size_t)nmax * g->ld));
+  RCHK(g->gf.alloc(&cs.n, nmax));
+  RCHK(g->gf.alloc(&cs.pes, nmax));
+  RCHK(g->gf.alloc(&cs.isign, nmax));
+  RCHK(g->gf.alloc(&cs.wfac, nmax));
+  RCHK(g->gf.alloc(&cs.Ei, nmax));
+  CUCHK(cudaMemsetAsync(cs.n, 0, sizeof(int) * nmax, g->st));
   const bool cplx = !g->real_model;
   const cd XI(0.0, 1.0);
   for (int k = 0; k < (int)g->gs.size(); k++)
@@ -1154,10 +1164,7 @@ GfLayout gf_layout() {
   gl.nelem = g->nelem;
   gl.elem_ptr = g->d_elem_ptr;
   gl.elem_chain = g->d_elem_chain;
-  gl.nexc = g->d_nexc;
-  gl.poles = g->d_poles;
-  gl.weights = g->d_weights;
-  gl.ld = g->ld;
+  gl.cs = g->cstore;
   return gl;
 }
 
@@ -1628,6 +1635,17 @@ int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t io
       iorb < 1 || iorb > c.Norb || jorb < 1 || jorb > c.Norb)
     VFAIL(VCA_ERR_ARG, "element index out of range");
   const int e = elem_index(c, ilat - 1, jlat - 1, ispin - 1, iorb - 1, jorb - 1);
+  if (!g->poles_ready && !g->chains.empty()) {  // poles and weights of every chain, once per solve
+    Arena ar;
+    double* work;
+    const int nch = (int)g->chains.size();
+    RCHK(ar.alloc(&work, (size_t)nch * 3 * g->ld));
+    launch_chain_poles(nch, g->cstore, work, g->d_poles, g->d_weights, g->d_nexc, g->st);
+    cudaError_t err = cudaStreamSynchronize(g->st);
+    ar.release();
+    CUCHK(err);
+    g->poles_ready = true;
+  }
   for (int ch = 0; ch < (int)g->chains.size(); ch++) {
     const ChainRec& r = g->chains[ch];
     if (r.elem != e || r.state != istate - 1 || r.chan != ichan) continue;

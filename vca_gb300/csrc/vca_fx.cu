@@ -265,11 +265,57 @@ __global__ void k_fx_apply(int64_t rows, int m, const int* col2ch, const ChainMe
     Xo[g] = act ? rshift_round((i128)mu * Xi[g], s) : 0;
   }
 }
+// The same on 8-column slabs with 16-byte accesses (columns 2tx, 2tx+1 of
+// slab blockIdx.y); a column that is not written (retired with
+// zero_inactive == 0, or a pad column) keeps its value.
+__global__ void __launch_bounds__(256) k_fx_apply8(int64_t rows, int m, const int* col2ch, const ChainMeta* meta,
+                                                   const i64* mul, const i64* sh, int zero_inactive, const i64* Xi,
+                                                   i64* Xo) {
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int c0 = blockIdx.y * FX_SLAB + 2 * tx;
+  i64 mu[2] = {0, 0};
+  int sv[2] = {0, 0};
+  bool wr[2] = {false, false};
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    const int c = c0 + j;
+    if (c < m) {
+      const int ch = col2ch[c];
+      const bool act = meta[ch].active != 0;
+      wr[j] = act || zero_inactive;
+      if (act) { mu[j] = mul[ch]; sv[j] = (int)sh[ch]; }
+    }
+  }
+  if (!wr[0] && !wr[1]) return;
+  const int64_t sb = (int64_t)blockIdx.y * rows * (FX_SLAB / 2) + tx;
+  const longlong2* I2 = (const longlong2*)Xi + sb;
+  longlong2* O2 = (longlong2*)Xo + sb;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ty; i < rows; i += (int64_t)gridDim.x * blockDim.y) {
+    const longlong2 v = I2[i * 4];
+    const i64 o0 = rshift_round((i128)mu[0] * v.x, sv[0]);
+    const i64 o1 = rshift_round((i128)mu[1] * v.y, sv[1]);
+    if (wr[0] && wr[1]) {
+      O2[i * 4] = make_longlong2(o0, o1);
+    } else {
+      i64* o = (i64*)(O2 + i * 4);
+      if (wr[0]) o[0] = o0;
+      if (wr[1]) o[1] = o1;
+    }
+  }
+}
+
 static void launch_apply(const ColBatch& b, const i64* mul, const i64* sh, int zero_inactive, const i64* Xi,
                          i64* Xo, cudaStream_t st) {
   dim3 blk;
   int ns;
   slab_shape(b.m, blk, ns);
+  if (fx_slab_w(b.m) == FX_SLAB) {
+    const dim3 b8(FX_SLAB / 2, 64, 1);
+    const int64_t nrb = (b.rows + b8.y - 1) / b8.y;
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(nrb, 152 * 8));
+    k_fx_apply8<<<dim3(gx, ns, 1), b8, 0, st>>>(b.rows, b.m, b.col2ch, b.meta, mul, sh, zero_inactive, Xi, Xo);
+    return;
+  }
   const int64_t nrb = (b.rows + blk.y - 1) / blk.y;
   const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(nrb, 152 * 16));
   dim3 grd(gx, ns, 1);
@@ -390,6 +436,83 @@ __global__ void k_fx_update_dot(int64_t rows, int m, const int* col2ch, const Ch
     partial[2 * ((int64_t)blockIdx.x * m + c) + 1] = (i64)(v >> 64);
   }
 }
+// The same on 8-column slabs with 16-byte accesses: thread (tx, ty) owns
+// columns 2tx, 2tx+1 of slab blockIdx.y and rows ty, ty + 64, ... of its
+// block's stride; a warp moves 8 rows x 64 bytes per access.  Retired chains
+// and pad columns get zero coefficients (W = YW, untouched) and no beta^2
+// contribution.
+#define FXU_RB 64
+__global__ void __launch_bounds__(256) k_fx_update_dot8(int64_t rows, int m, const int* col2ch,
+                                                        const ChainMeta* meta, int sh, const i64* afx,
+                                                        const i64* bfx, int use_b, const i64* X, const i64* Xp,
+                                                        i64* YW, i64* partial) {
+  __shared__ i128 red[FXU_RB][FX_SLAB];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int c0 = blockIdx.y * FX_SLAB + 2 * tx;
+  i64 a[2] = {0, 0}, bb[2] = {0, 0};
+  bool act[2] = {false, false};
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    const int c = c0 + j;
+    if (c < m) {
+      const int ch = col2ch[c];
+      act[j] = meta[ch].active != 0;
+      if (act[j]) { a[j] = afx[ch]; bb[j] = use_b ? bfx[ch] : 0; }
+    }
+  }
+  const int64_t sb = (int64_t)blockIdx.y * rows * (FX_SLAB / 2) + tx;  // longlong2 units
+  const longlong2* X2 = (const longlong2*)X + sb;
+  const longlong2* P2 = (const longlong2*)Xp + sb;
+  longlong2* Y2 = (longlong2*)YW + sb;
+  i128 s0 = 0, s1 = 0;
+  const int64_t stride = (int64_t)gridDim.x * FXU_RB;
+  for (int64_t i = (int64_t)blockIdx.x * FXU_RB + ty; i < rows; i += 2 * stride) {
+    const int64_t i2 = i + stride;
+    const bool two = i2 < rows;
+    const longlong2 xa = X2[i * 4], ya = Y2[i * 4];
+    const longlong2 pa = use_b ? P2[i * 4] : make_longlong2(0, 0);
+    longlong2 xb = make_longlong2(0, 0), yb = make_longlong2(0, 0), pb = make_longlong2(0, 0);
+    if (two) {
+      xb = X2[i2 * 4];
+      yb = Y2[i2 * 4];
+      if (use_b) pb = P2[i2 * 4];
+    }
+    const i64 w0 = ya.x - rshift_round((i128)a[0] * xa.x + (i128)bb[0] * pa.x, sh);
+    const i64 w1 = ya.y - rshift_round((i128)a[1] * xa.y + (i128)bb[1] * pa.y, sh);
+    Y2[i * 4] = make_longlong2(w0, w1);
+    s0 += (i128)w0 * w0;
+    s1 += (i128)w1 * w1;
+    if (two) {
+      const i64 v0 = yb.x - rshift_round((i128)a[0] * xb.x + (i128)bb[0] * pb.x, sh);
+      const i64 v1 = yb.y - rshift_round((i128)a[1] * xb.y + (i128)bb[1] * pb.y, sh);
+      Y2[i2 * 4] = make_longlong2(v0, v1);
+      s0 += (i128)v0 * v0;
+      s1 += (i128)v1 * v1;
+    }
+  }
+  red[ty][2 * tx] = act[0] ? s0 : (i128)0;
+  red[ty][2 * tx + 1] = act[1] ? s1 : (i128)0;
+  __syncthreads();
+  for (int h = FXU_RB / 2; h > 0; h >>= 1) {
+    if (ty < h) {
+      red[ty][2 * tx] += red[ty + h][2 * tx];
+      red[ty][2 * tx + 1] += red[ty + h][2 * tx + 1];
+    }
+    __syncthreads();
+  }
+  if (ty == 0) {
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int c = c0 + j;
+      if (c < m) {
+        const i128 v = red[0][2 * tx + j];
+        partial[2 * ((int64_t)blockIdx.x * m + c)] = (i64)(u64)v;
+        partial[2 * ((int64_t)blockIdx.x * m + c) + 1] = (i64)(v >> 64);
+      }
+    }
+  }
+}
+
 void launch_fx_update_dot(const ColBatch& b, const FxScales& s, const i64* afx, const i64* bfx, bool use_b,
                           const i64* X, const i64* Xp, i64* YW, i64* partial, int nblk, double* out_col,
                           cudaStream_t st) {
@@ -398,8 +521,13 @@ void launch_fx_update_dot(const ColBatch& b, const FxScales& s, const i64* afx, 
   int ns;
   slab_shape(b.m, blk, ns);
   dim3 grd(nblk, ns, 1);
-  k_fx_update_dot<<<grd, blk, sizeof(i128) * 256, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx,
-                                                        bfx, use_b ? 1 : 0, X, Xp, YW, partial);
+  if (fx_slab_w(b.m) == FX_SLAB)
+    k_fx_update_dot8<<<grd, dim3(FX_SLAB / 2, FXU_RB, 1), 0, st>>>(b.rows, b.m, b.col2ch, b.meta,
+                                                                    s.C + s.F - s.G, afx, bfx, use_b ? 1 : 0, X,
+                                                                    Xp, YW, partial);
+  else
+    k_fx_update_dot<<<grd, blk, sizeof(i128) * 256, st>>>(b.rows, b.m, b.col2ch, b.meta, s.C + s.F - s.G, afx,
+                                                          bfx, use_b ? 1 : 0, X, Xp, YW, partial);
   launch_fx_partial_reduce(b.m, nblk, partial, 2 * s.G, out_col, st);
 }
 

@@ -495,25 +495,57 @@ void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, d
 }
 
 // ---------------------------------------------------------------------------
+// Chain store: the tridiagonal (alpha, beta) of every Green's function chain,
+// with its prefactor norm^2/zeta, sign (+1 particle, -1 hole), channel
+// weight factor and ground-state energy.  G'(z) is evaluated from it as a
+// continued fraction; poles and weights (add_to_lanczos_gf_normal,
+// VCA_GF_NORMAL.f90:970-1033) are formed from it only when a caller asks for
+// them.
+// ---------------------------------------------------------------------------
+__global__ void k_chain_store(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
+                              const double* norm2, const double2* wfac, const int* isign, double Ei,
+                              double zeta, ChainStore cs, int base) {
+  const int ch = blockIdx.x;
+  if (ch >= nch) return;
+  const int n = meta[ch].len;
+  const int64_t o = (int64_t)(base + ch) * cs.ld;
+  for (int j = threadIdx.x; j < cs.ld; j += blockDim.x) {
+    cs.A[o + j] = (j < n) ? A[(int64_t)ch * ldab + j] : 0.0;
+    cs.B[o + j] = (j < n) ? Bt[(int64_t)ch * ldab + j] : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    cs.n[base + ch] = n;
+    cs.pes[base + ch] = norm2[ch] / zeta;
+    cs.isign[base + ch] = isign[ch];
+    cs.wfac[base + ch] = wfac[ch];
+    cs.Ei[base + ch] = Ei;
+  }
+}
+void launch_chain_store(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
+                        const double* norm2, const double2* wfac, const int* isign, double Ei, double zeta,
+                        const ChainStore& cs, int base, cudaStream_t st) {
+  if (nch <= 0) return;
+  COUNT_LAUNCH();
+  k_chain_store<<<nch, 128, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta, cs, base);
+}
+
 // Chain tridiagonal -> poles and weights.  Implicit QL with Wilkinson shift
 // (EISPACK tql2; the reference calls SciFortran eigh(d,e,Ev=Z) at
 // VCA_GF_NORMAL.f90:1012) tracking only the first row of Z.  One thread per
-// chain; work = 3*ld doubles per chain.
-// ---------------------------------------------------------------------------
-__global__ void k_chain_poles(int nch, const ChainMeta* meta, const double* A, const double* Bt,
-                              int ldab, const double* norm2, const double2* wfac, const int* isign,
-                              double Ei, double zeta, double* work, double* poles, double2* weights,
+// chain, one warp per block; work = 3*ld doubles per chain.
+__global__ void k_chain_poles(int nch, ChainStore cs, double* work, double* poles, double2* weights,
                               int* nexc) {
+  const int ldab = cs.ld;
   for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
-    const int n = meta[ch].len;
+    const int n = cs.n[ch];
     nexc[ch] = n;
     if (n <= 0) continue;
     double* d = work + (int64_t)ch * 3 * ldab;
     double* e = d + ldab;
     double* z = e + ldab;
     for (int i = 0; i < n; i++) {
-      d[i] = A[(int64_t)ch * ldab + i];
-      e[i] = (i + 1 < n) ? Bt[(int64_t)ch * ldab + i + 1] : 0.0;  // e[i] couples i,i+1
+      d[i] = cs.A[(int64_t)ch * ldab + i];
+      e[i] = (i + 1 < n) ? cs.B[(int64_t)ch * ldab + i + 1] : 0.0;  // e[i] couples i,i+1
       z[i] = (i == 0) ? 1.0 : 0.0;
     }
     double f = 0.0, tst1 = 0.0;
@@ -575,24 +607,22 @@ __global__ void k_chain_poles(int nch, const ChainMeta* meta, const double* A, c
         z[kk] = t;
       }
     }
-    const double2 wf = wfac[ch];
-    const double pes = norm2[ch] / zeta;
+    const double2 wf = cs.wfac[ch];
+    const double pes = cs.pes[ch];
+    const double Ei = cs.Ei[ch];
+    const double sg = (double)cs.isign[ch];
     for (int j = 0; j < n; j++) {
       double w2 = z[j] * z[j] * pes;
-      poles[(int64_t)ch * ldab + j] = (double)isign[ch] * (d[j] - Ei);
+      poles[(int64_t)ch * ldab + j] = sg * (d[j] - Ei);
       weights[(int64_t)ch * ldab + j] = make_double2(wf.x * w2, wf.y * w2);
     }
   }
 }
-void launch_chain_poles(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
-                        const double* norm2, const double2* wfac, const int* isign, double Ei,
-                        double zeta, double* work, double* poles, double2* weights, int* nexc,
+void launch_chain_poles(int nch, const ChainStore& cs, double* work, double* poles, double2* weights, int* nexc,
                         cudaStream_t st) {
+  if (nch <= 0) return;
   COUNT_LAUNCH();
-  // one warp per block: the chains' FP64 work spreads over as many SMs as
-  // there are warps of chains
-  k_chain_poles<<<nblocks(nch, 32), 32, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta,
-                                                 work, poles, weights, nexc);
+  k_chain_poles<<<nblocks(nch, 32), 32, 0, st>>>(nch, cs, work, poles, weights, nexc);
 }
 
 // ---------------------------------------------------------------------------
@@ -659,27 +689,40 @@ void launch_chain_init(const SectorView& tgt, int src_dimup, const void* gs, boo
 // Cluster Green's function from poles (vca_gf_cluster_scalar,
 // VCA_IO/gf_cluster.f90:23-49) and recombination (:50-62).
 // ---------------------------------------------------------------------------
+// Per (z, element) thread: sum over the element's chains of
+// isign * pes * wfac / (zeta' - a0 - b1^2 / (zeta' - a1 - ...)), zeta' =
+// isign*z + Ei: the continued fraction of the chain's tridiagonal, equal to
+// the sum over its poles isign*(E_j - Ei) with weights wfac*pes*Z(1,j)^2.
 __global__ void k_gf_eval(GfLayout g, int nz, const double2* z, double2* G) {
   const int64_t n = (int64_t)nz * g.nelem;
+  const ChainStore& cs = g.cs;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int e = (int)(t % g.nelem);
     const int q = (int)(t / g.nelem);
-    const double zr = z[q].x, zi = z[q].y;
     double ar = 0.0, ai = 0.0;
     for (int x = g.elem_ptr[e]; x < g.elem_ptr[e + 1]; x++) {
       const int ch = g.elem_chain[x];
-      const int np = g.nexc[ch];
-      const double* P = g.poles + (int64_t)ch * g.ld;
-      const double2* W = g.weights + (int64_t)ch * g.ld;
-      for (int j = 0; j < np; j++) {
-        const double dr = zr - P[j];
-        const double inv = 1.0 / fma(dr, dr, zi * zi);
-        // w / (z - p) = w * (dr - i zi) / |z - p|^2
-        const double2 w = W[j];
-        ar += (w.x * dr + w.y * zi) * inv;
-        ai += (w.y * dr - w.x * zi) * inv;
+      const int np = cs.n[ch];
+      if (np <= 0) continue;
+      const double sg = (double)cs.isign[ch];
+      const double zr = sg * z[q].x + cs.Ei[ch], zi = sg * z[q].y;
+      const double* A = cs.A + (int64_t)ch * cs.ld;
+      const double* B = cs.B + (int64_t)ch * cs.ld;
+      double tr = zr - A[np - 1], ti = zi;
+      for (int k = np - 2; k >= 0; k--) {
+        const double b2 = B[k + 1] * B[k + 1];
+        const double inv = b2 / fma(tr, tr, ti * ti);  // b^2 / t = b^2 conj(t) / |t|^2
+        tr = zr - A[k] - tr * inv;
+        ti = zi + ti * inv;
       }
+      const double inv = 1.0 / fma(tr, tr, ti * ti);
+      const double cr = tr * inv, ci = -ti * inv;
+      const double f = sg * cs.pes[ch];
+      const double2 w = cs.wfac[ch];
+      const double wr = w.x * f, wi = w.y * f;
+      ar += wr * cr - wi * ci;
+      ai += wr * ci + wi * cr;
     }
     G[t] = make_double2(ar, ai);
   }

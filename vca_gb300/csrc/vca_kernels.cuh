@@ -76,10 +76,28 @@ void launch_fill(int64_t n, double v, double* X, cudaStream_t st);
 // writes theta, s[0..k-1] and flag (1 = converged)
 void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, double* theta,
                        double* s, double* resid, cudaStream_t st);
-// chains -> poles/weights (add_to_lanczos_gf_normal, VCA_GF_NORMAL.f90:970-1033)
-void launch_chain_poles(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
-                        const double* norm2, const double2* wfac, const int* isign, double Ei,
-                        double zeta, double* work, double* poles, double2* weights, int* nexc,
+// Device store of every Green's function chain: tridiagonal rows A, B
+// ([nch*ld], B[j] = beta_j couples rows j-1 and j), length n, prefactor
+// pes = norm^2/zeta, isign (+1 particle, -1 hole), channel weight factor,
+// ground-state energy Ei.
+struct ChainStore {
+  double* A;
+  double* B;
+  int* n;
+  double* pes;
+  int* isign;
+  double2* wfac;
+  double* Ei;
+  int ld;
+};
+// copy one batch's chains (rows of A/Bt with stride ldab) into the store at
+// chain offset base
+void launch_chain_store(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
+                        const double* norm2, const double2* wfac, const int* isign, double Ei, double zeta,
+                        const ChainStore& cs, int base, cudaStream_t st);
+// stored chains -> poles/weights (add_to_lanczos_gf_normal, VCA_GF_NORMAL.f90:970-1033);
+// work: 3*ld doubles per chain
+void launch_chain_poles(int nch, const ChainStore& cs, double* work, double* poles, double2* weights, int* nexc,
                         cudaStream_t st);
 
 // ---- chain initial vectors (VCA_GF_NORMAL.f90:179-197, :251-268, :608-646) -
@@ -106,10 +124,7 @@ struct GfLayout {
   int nelem;              // spin-diagonal elements (il,jl,is,io,jo)
   const int* elem_ptr;    // [nelem+1] chains per element (CSR)
   const int* elem_chain;  // chain ids
-  const int* nexc;        // [nch] poles per chain
-  const double* poles;    // [nch*ld]
-  const double2* weights; // [nch*ld]
-  int ld;
+  ChainStore cs;          // the chains' tridiagonals
 };
 // raw element sums at nz points z (complex): G[z*nelem + e]
 void launch_gf_eval(const GfLayout& g, int nz, const double2* z, double2* G, cudaStream_t st);
