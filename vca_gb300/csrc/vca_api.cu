@@ -190,9 +190,15 @@ size_t bv_len(const vca_config& c) {
   return (size_t)c.Nlat * c.Nlat_bath * c.Nspin * c.Nspin * c.Norb * c.Norb_bath;
 }
 
-SectorView view_of(int nup, int ndw) {
-  const SpinSpace& u = g->sp[0][nup];
-  const SpinSpace& d = g->sp[g->dwset][ndw];
+// View of a sector whose first (fastest) spin index runs over spin space
+// (sa, na) and second over (sb, nb).  view_of is the natural order; the
+// chain batches of sectors with DimUp > DimDw run with the roles swapped
+// (element idw + iup*DimDw): the stored Hamiltonian has no cross-spin sign
+// and a mixed diagonal symmetric in the two words, so H is the same operator
+// in either order, and the staged H x v then holds the smaller block.
+SectorView view_pair(int sa, int na, int sb, int nb) {
+  const SpinSpace& u = g->sp[sa][na];
+  const SpinSpace& d = g->sp[sb][nb];
   SectorView v;
   v.dimup = u.dim;
   v.dimdw = d.dim;
@@ -210,19 +216,20 @@ SectorView view_of(int nup, int ndw) {
   v.dw_e1 = d.e1;
   return v;
 }
+SectorView view_of(int nup, int ndw) { return view_pair(0, nup, g->dwset, ndw); }
 
-FxView fx_view_of(int nup, int ndw) {
+FxView fx_view_pair(int sa, int na, int sb, int nb) {
   FxView f = g->fxbase;
-  f.up_code = g->fx_code[0][nup];
-  f.dw_code = g->fx_code[g->dwset][ndw];
-  f.up_hop = g->fx_hop[0][nup];
-  f.dw_hop = g->fx_hop[g->dwset][ndw];
-  f.up_e1 = g->fx_e1[0][nup];
-  f.dw_e1 = g->fx_e1[g->dwset][ndw];
-  f.up_npos = g->fx_npos[0][nup];
-  f.dw_npos = g->fx_npos[g->dwset][ndw];
-  f.up_perm = g->fx_perm[0][nup];
-  const Ctx::PermTabs& pt = g->fx_ptab[0][nup];
+  f.up_code = g->fx_code[sa][na];
+  f.dw_code = g->fx_code[sb][nb];
+  f.up_hop = g->fx_hop[sa][na];
+  f.dw_hop = g->fx_hop[sb][nb];
+  f.up_e1 = g->fx_e1[sa][na];
+  f.dw_e1 = g->fx_e1[sb][nb];
+  f.up_npos = g->fx_npos[sa][na];
+  f.dw_npos = g->fx_npos[sb][nb];
+  f.up_perm = g->fx_perm[sa][na];
+  const Ctx::PermTabs& pt = g->fx_ptab[sa][na];
   f.up_phop = pt.hop;
   f.up_pcnt = pt.cnt;
   f.up_pnpos = pt.npos;
@@ -230,6 +237,7 @@ FxView fx_view_of(int nup, int ndw) {
   f.up_pe1 = pt.e1;
   return f;
 }
+FxView fx_view_of(int nup, int ndw) { return fx_view_pair(0, nup, g->dwset, ndw); }
 
 inline int ceil_log2(double x) {  // smallest e with 2^e >= x (x > 0)
   int e = 0;
@@ -999,8 +1007,12 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     Arena ar;
     BatchBufs bb;
     int rc = alloc_batch(ar, D, m, cplx, nch, g->ld, bb);
+    // fixed-point batches hold the smaller spin block first (see view_pair)
+    const bool swap = g->fx && tv.dimup > tv.dimdw;
+    const SectorView hv = swap ? view_pair(g->dwset, tdw, 0, tup) : tv;
     if (!rc && g->fx) {
-      const int rbw = hxv_fx_cols_rows(tv, fx_view_of(tup, tdw), m, g->cfg.hxv_variant == 1);
+      const FxView hf = swap ? fx_view_pair(g->dwset, tdw, 0, tup) : fx_view_of(tup, tdw);
+      const int rbw = hxv_fx_cols_rows(hv, hf, m, g->cfg.hxv_variant == 1);
       rc = ar.alloc(&bb.wpart, 2 * (size_t)rbw * m);
       bb.wpart_rows = rbw;
     }
@@ -1040,14 +1052,14 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     // start vectors: gather from the ground state, normalise per chain
     if (g->fx) {
       const FxScales& fs = g->fxs;
-      FxView fv = fx_view_of(tup, tdw);
-      launch_chain_init_fx(tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, d_ci, m, (i64*)bb.b[0], g->st);
+      const FxView fv = swap ? fx_view_pair(g->dwset, tdw, 0, tup) : fx_view_of(tup, tdw);
+      launch_chain_init_fx(tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, d_ci, m, swap, (i64*)bb.b[0], g->st);
       launch_fx_dot(cb, (i64*)bb.b[0], (i64*)bb.b[0], fs.F, fs.F, (i64*)bb.partial, bb.nblk, norm2c, g->st);
       launch_chain_sum(cb, norm2c, norm2, g->st);
       launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
       launch_fx_rescale(cb, invn, fs.F, fs.F, (i64*)bb.b[0], (i64*)bb.b[0], bb.scr, g->st);
       for (int k = 1; k <= nlanc; k++)
-        if ((rc = lanczos_step_fx(tv, fv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
+        if ((rc = lanczos_step_fx(hv, fv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
     } else {
       launch_chain_init(tv, g->sp[0][nup].dim, S.vec, cplx, nch, d_ci, m, cplx, bb.b[0], g->st);
       launch_col_dot(cb, bb.b[0], bb.b[0], bb.partial, bb.nblk, norm2c, g->st);

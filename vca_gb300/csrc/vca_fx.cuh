@@ -126,9 +126,10 @@ void launch_fx_psi_accum(int64_t n, const double* s, int k, const i64* X, i64* p
 void launch_fx_from_double(int64_t n, const double* x, int F, i64* X, cudaStream_t st);
 void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t st);
 // chain start vectors by exact gather (+/- psi, re/im columns) from a FX
-// ground state, into a slab-major batch of m columns
+// ground state, into a slab-major batch of m columns; swapped: batch row of
+// element (iup, idw) is idw + iup*DimDw instead of iup + idw*DimUp
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const i64* gs, int nchain,
-                          const ChainInit* d_ci, int m, i64* X, cudaStream_t st);
+                          const ChainInit* d_ci, int m, bool swapped, i64* X, cudaStream_t st);
 
 // out[c] = (sum over `rows` int128 partials of column c) * 2^-sexp
 void launch_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out, cudaStream_t st);
