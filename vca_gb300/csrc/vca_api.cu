@@ -140,6 +140,12 @@ struct Ctx {
   // Hk and Omega
   int64_t Nk = 0;
   double2* d_Hk = nullptr;  // lso per k
+  // k-points paired by H_k' = conj(H_k) (= H_k^T): representatives (lso)
+  // and their multiplicities, for models whose Omega integrand is equal at
+  // the two points of a pair
+  int64_t Nk_rep = 0;
+  double2* d_Hk_rep = nullptr;
+  double* d_kw = nullptr;
   bool hk_spin_diag = true;
   std::vector<cd> hk_const;       // lso: value of Hk when equal at every k
   std::vector<char> hk_varying;   // lso: 1 when Hk differs between k-points
@@ -1266,6 +1272,37 @@ bool point_spin_diagonal() {
 
 // Omega integral (frequency_integration, VCA_OMEGA.f90:123-146) with the
 // fixed Gauss-Legendre rule; also returns f(w) at the nodes when asked.
+// The Omega integrand is equal at k and its conjugate partner when the model
+// is real and Hloc, bath_h are symmetric with a real bath_v (P and G'
+// symmetric; see pair_kpoints).
+bool omega_pairs_valid() {
+  const vca_config& c = g->cfg;
+  if (!g->real_model) return false;
+  for (int il = 0; il < c.Nlat; il++)
+    for (int jl = 0; jl < c.Nlat; jl++)
+      for (int is = 0; is < c.Nspin; is++)
+        for (int js = 0; js < c.Nspin; js++)
+          for (int io = 0; io < c.Norb; io++)
+            for (int jo = 0; jo < c.Norb; jo++) {
+              const cd a = g->Hloc[idx_nnn(c, il, jl, is, js, io, jo)];
+              if (a.imag() != 0.0 || a != g->Hloc[idx_nnn(c, jl, il, js, is, jo, io)]) return false;
+            }
+  if (g->has_bath) {
+    for (int a = 0; a < c.Nlat_bath; a++)
+      for (int b = 0; b < c.Nlat_bath; b++)
+        for (int is = 0; is < c.Nspin; is++)
+          for (int js = 0; js < c.Nspin; js++)
+            for (int oa = 0; oa < c.Norb_bath; oa++)
+              for (int ob = 0; ob < c.Norb_bath; ob++) {
+                const cd h = g->bath_h[idx_bh(c, a, b, is, js, oa, ob)];
+                if (h.imag() != 0.0 || h != g->bath_h[idx_bh(c, b, a, js, is, ob, oa)]) return false;
+              }
+    for (size_t i = 0; i < g->bath_v.size(); i++)
+      if (g->bath_v[i].imag() != 0.0) return false;
+  }
+  return true;
+}
+
 int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, double* f_eval) {
   const vca_config& c = g->cfg;
   Arena ar;
@@ -1355,7 +1392,10 @@ int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, d
   }
   cudaMemcpyAsync(d_rowptr, rowptr.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice, g->st);
   if (!cols.empty()) cudaMemcpyAsync(d_cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, g->st);
-  launch_omega_ksum2(n, N, nblk, nb, P, Glso, Nk, g->d_Hk, d_rowptr, d_cols, fpart, kchunks, g->st);
+  const bool pairs = g->d_Hk_rep && g->Nk_rep < Nk && omega_pairs_valid();
+  const int64_t nks = pairs ? g->Nk_rep : Nk;
+  launch_omega_ksum2(n, N, nblk, nb, P, Glso, nks, pairs ? g->d_Hk_rep : g->d_Hk, pairs ? g->d_kw : nullptr,
+                     d_rowptr, d_cols, fpart, kchunks, g->st);
   launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, f, g->st);
   CUCHK(cudaGetLastError());
   if (f_eval) {
@@ -1372,6 +1412,85 @@ int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, d
   CUCHK(cudaStreamSynchronize(g->st));
   ar.release();
   *out = (3.0 - c.Nspin) * integral / M_PI;
+  return VCA_OK;
+}
+
+// Pairs k, k' with H_k' = conj(H_k) to 1e-13 of the largest |H_k| entry
+// (time reversal: k' = -k on a symmetric grid).  For a real model whose
+// Omega matrices P = Delta + Hloc and G' are symmetric, M_k' = P - H_k^T =
+// M_k^T and det(1 + M_k^T G) = det(1 + G M_k) = det(1 + M_k G), so the
+// integrand is equal at the two points: the k-sum then runs over one point
+// per pair with weight 2.  Candidates are found through a random linear
+// signature of the matrix (sorted), then checked entry by entry; a point
+// without a partner keeps weight 1.
+int pair_kpoints(const double* Hk, int64_t Nk, size_t nel) {
+  std::vector<double> cr(nel), ci(nel);
+  uint64_t st = 0x9E3779B97F4A7C15ull;
+  auto rnd = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return 0.5 + (double)(st >> 11) * (1.0 / 9007199254740992.0);
+  };
+  double hmax = 0.0, wsum = 0.0;
+  for (size_t x = 0; x < nel; x++) {
+    cr[x] = rnd();
+    ci[x] = rnd();
+    wsum += cr[x] + ci[x];
+  }
+  for (size_t i = 0; i < 2 * nel * (size_t)Nk; i++) hmax = std::max(hmax, std::fabs(Hk[i]));
+  const double tol = 1e-13 * (1.0 + hmax);
+  std::vector<std::pair<double, int64_t>> sig(Nk);
+  std::vector<double> csig(Nk);
+  for (int64_t k = 0; k < Nk; k++) {
+    double a = 0.0, b = 0.0;
+    const double* h = Hk + 2 * nel * k;
+    for (size_t x = 0; x < nel; x++) {
+      a += cr[x] * h[2 * x] + ci[x] * h[2 * x + 1];
+      b += cr[x] * h[2 * x] - ci[x] * h[2 * x + 1];
+    }
+    sig[k] = {a, k};
+    csig[k] = b;
+  }
+  std::sort(sig.begin(), sig.end());
+  const double stol = tol * wsum * 2.0 + 1e-12 * (std::fabs(sig.front().first) + std::fabs(sig.back().first));
+  std::vector<char> used(Nk, 0);
+  std::vector<int64_t> reps;
+  std::vector<double> wts;
+  auto conj_of = [&](int64_t j, int64_t k) {
+    const double* a = Hk + 2 * nel * j;
+    const double* b = Hk + 2 * nel * k;
+    for (size_t x = 0; x < nel; x++)
+      if (std::fabs(a[2 * x] - b[2 * x]) > tol || std::fabs(a[2 * x + 1] + b[2 * x + 1]) > tol) return false;
+    return true;
+  };
+  for (int64_t k = 0; k < Nk; k++) {
+    if (used[k]) continue;
+    used[k] = 1;
+    int64_t partner = -1;
+    auto lo = std::lower_bound(sig.begin(), sig.end(), std::make_pair(csig[k] - stol, (int64_t)-1));
+    for (auto it = lo; it != sig.end() && it->first <= csig[k] + stol; ++it)
+      if (!used[it->second] && conj_of(it->second, k)) { partner = it->second; break; }
+    reps.push_back(k);
+    if (partner >= 0) {
+      used[partner] = 1;
+      wts.push_back(2.0);
+    } else {
+      wts.push_back(1.0);
+    }
+  }
+  g->Nk_rep = (int64_t)reps.size();
+  int64_t* d_rep;
+  Arena tmp;
+  RCHK(g->omega.alloc(&g->d_Hk_rep, nel * g->Nk_rep));
+  RCHK(g->omega.alloc(&g->d_kw, g->Nk_rep));
+  RCHK(tmp.alloc(&d_rep, g->Nk_rep));
+  CUCHK(cudaMemcpyAsync(d_rep, reps.data(), sizeof(int64_t) * g->Nk_rep, cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(g->d_kw, wts.data(), sizeof(double) * g->Nk_rep, cudaMemcpyHostToDevice, g->st));
+  launch_gather_blocks(g->Nk_rep, (int64_t)nel, d_rep, g->d_Hk, g->d_Hk_rep, g->st);
+  cudaError_t e = cudaStreamSynchronize(g->st);
+  tmp.release();
+  CUCHK(e);
   return VCA_OK;
 }
 
@@ -1411,6 +1530,7 @@ int upload_hk(const double* Hk, int64_t Nk) {
                 g->hk_varying[a + (size_t)b * N] = var ? 1 : 0;
               }
   }
+  RCHK(pair_kpoints(Hk, Nk, nel));
   CUCHK(cudaStreamSynchronize(g->st));
   return VCA_OK;
 }

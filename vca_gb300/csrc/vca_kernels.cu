@@ -773,146 +773,13 @@ void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, doub
   k_gf_assemble<<<nblocks(n, 256), 256, 0, st>>>(cd, nz, Graw, Glso);
 }
 
-// ---------------------------------------------------------------------------
-// Omega integrand (sum_kmesh, VCA_OMEGA.f90:37-75): per (w, k) and spin block
-// A = (P_w - Hk_k) G_w, ln|det(1 + A)|.  One warp per (k, block); lane j owns
-// column j (nb <= 32).  ||A||_inf < 1/2: elimination without pivoting with
-// the identity implicit and log1p on the pivots; otherwise partial pivoting.
-// ---------------------------------------------------------------------------
+// complex helpers
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
   double den = b.x * b.x + b.y * b.y;
   return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
-}
-
-__global__ void k_omega_ksum(int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
-                             const double2* Hk, double* fpart, int kchunks) {
-  extern __shared__ double2 shm[];
-  const int w = blockIdx.y;
-  const int chunk = blockIdx.x;
-  const int NN = N * N;
-  double2* Gs = shm;            // N*N
-  double2* Ps = shm + NN;       // N*N
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nwarps = blockDim.x >> 5;
-  double2* Aw = shm + 2 * NN + (int64_t)warp * nb * nb;
-  for (int t = threadIdx.x; t < NN; t += blockDim.x) {
-    Gs[t] = Glso[(int64_t)w * NN + t];
-    Ps[t] = P[(int64_t)w * NN + t];
-  }
-  __syncthreads();
-  const int64_t k0 = (Nk * chunk) / kchunks, k1 = (Nk * (chunk + 1)) / kchunks;
-  double acc = 0.0;
-  const int64_t ntask = (k1 - k0) * nblk;
-  for (int64_t task = warp; task < ntask; task += nwarps) {
-    const int64_t k = k0 + task / nblk;
-    const int sb = (int)(task % nblk);
-    const int off = sb * nb;
-    const double2* H = Hk + k * NN;
-    // A(:,j) = sum_l (P - Hk)(off+i, off+l) G(off+l, off+j)
-    if (lane < nb) {
-      const int j = lane;
-      for (int i = 0; i < nb; i++) {
-        double2 s = make_double2(0.0, 0.0);
-        for (int l = 0; l < nb; l++) {
-          const int il = (off + i) + (off + l) * N;
-          double2 mm = make_double2(Ps[il].x - H[il].x, Ps[il].y - H[il].y);
-          double2 gg = Gs[(off + l) + (off + j) * N];
-          s.x = fma(mm.x, gg.x, s.x);
-          s.x = fma(-mm.y, gg.y, s.x);
-          s.y = fma(mm.x, gg.y, s.y);
-          s.y = fma(mm.y, gg.x, s.y);
-        }
-        Aw[i + j * nb] = s;
-      }
-    }
-    __syncwarp();
-    // infinity norm: row sums
-    double rs = 0.0;
-    if (lane < nb)
-      for (int j = 0; j < nb; j++) {
-        double2 a = Aw[lane + j * nb];
-        rs += hypot(a.x, a.y);
-      }
-    for (int o = 16; o > 0; o >>= 1) rs = fmax(rs, __shfl_xor_sync(0xffffffffu, rs, o));
-    double ld = 0.0;
-    if (rs < 0.5) {
-      for (int kk = 0; kk < nb; kk++) {
-        const double2 akk = Aw[kk + kk * nb];
-        const double2 piv = make_double2(1.0 + akk.x, akk.y);
-        ld += 0.5 * log1p(2.0 * akk.x + akk.x * akk.x + akk.y * akk.y);
-        if (lane > kk && lane < nb) Aw[lane + kk * nb] = cdiv(Aw[lane + kk * nb], piv);  // l_i
-        __syncwarp();
-        if (lane > kk && lane < nb) {
-          const int j = lane;
-          const double2 ukj = Aw[kk + j * nb];
-          for (int i = kk + 1; i < nb; i++) {
-            double2 t = cmul(Aw[i + kk * nb], ukj);
-            Aw[i + j * nb].x -= t.x;
-            Aw[i + j * nb].y -= t.y;
-          }
-        }
-        __syncwarp();
-      }
-    } else {
-      if (lane < nb) Aw[lane + lane * nb].x += 1.0;
-      __syncwarp();
-      for (int kk = 0; kk < nb; kk++) {
-        double mag = -1.0;
-        int arg = kk;
-        if (lane >= kk && lane < nb) { double2 a = Aw[lane + kk * nb]; mag = hypot(a.x, a.y); arg = lane; }
-        for (int o = 16; o > 0; o >>= 1) {
-          double om = __shfl_xor_sync(0xffffffffu, mag, o);
-          int oa = __shfl_xor_sync(0xffffffffu, arg, o);
-          if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
-        }
-        if (mag == 0.0) { ld = -INFINITY; break; }
-        if (arg != kk && lane < nb) {  // swap rows kk and arg in column `lane`
-          double2 t = Aw[kk + lane * nb];
-          Aw[kk + lane * nb] = Aw[arg + lane * nb];
-          Aw[arg + lane * nb] = t;
-        }
-        __syncwarp();
-        const double2 piv = Aw[kk + kk * nb];
-        ld += log(hypot(piv.x, piv.y));
-        if (lane > kk && lane < nb) Aw[lane + kk * nb] = cdiv(Aw[lane + kk * nb], piv);
-        __syncwarp();
-        if (lane > kk && lane < nb) {
-          const int j = lane;
-          const double2 ukj = Aw[kk + j * nb];
-          for (int i = kk + 1; i < nb; i++) {
-            double2 t = cmul(Aw[i + kk * nb], ukj);
-            Aw[i + j * nb].x -= t.x;
-            Aw[i + j * nb].y -= t.y;
-          }
-        }
-        __syncwarp();
-      }
-    }
-    if (lane == 0) acc += ld;
-    __syncwarp();
-  }
-  // block reduce of the per-warp sums (lane 0 of each warp)
-  __shared__ double red[32];
-  if (lane == 0) red[warp] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int q = 0; q < nwarps; q++) s += red[q];
-    fpart[(int64_t)w * kchunks + chunk] = s;
-  }
-}
-void launch_omega_ksum(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso,
-                       int64_t Nk, const double2* Hk, double* fpart, int kchunks, cudaStream_t st) {
-  COUNT_LAUNCH();
-  const int threads = 128;
-  size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
-  if (shm > 48 * 1024)
-    cudaFuncSetAttribute(k_omega_ksum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  dim3 grd(kchunks, nw, 1);
-  k_omega_ksum<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, fpart, kchunks);
 }
 
 __global__ void k_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out) {
@@ -1198,8 +1065,8 @@ void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long*
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, const double2* P,
                                                      const double2* Glso, int64_t Nk, const double2* Hk,
-                                                     const int* rowptr, const int* cols, double* fpart,
-                                                     int kchunks) {
+                                                     const double* kw, const int* rowptr, const int* cols,
+                                                     double* fpart, int kchunks) {
   extern __shared__ double2 shm[];
   const int w = blockIdx.y;
   const int chunk = blockIdx.x;
@@ -1321,7 +1188,7 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
       }
       ld = zero ? -INFINITY : 0.5 * (log(mant) + ex * 0.6931471805599453);
     }
-    if (lane == 0) acc += ld;
+    if (lane == 0) acc += kw ? kw[k] * ld : ld;
     __syncwarp();
   }
   __shared__ double red[32];
@@ -1334,8 +1201,8 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
   }
 }
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
-                        const double2* Hk, const int* rowptr, const int* cols, double* fpart, int kchunks,
-                        cudaStream_t st) {
+                        const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
+                        int kchunks, cudaStream_t st) {
   COUNT_LAUNCH();
   const int threads = 128;
   size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
@@ -1345,7 +1212,22 @@ void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const
     attr = true;
   }
   dim3 grd(kchunks, nw, 1);
-  k_omega_ksum2<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, rowptr, cols, fpart, kchunks);
+  k_omega_ksum2<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, kchunks);
+}
+
+// dst[r] = src[idx[r]] for blocks of nel double2
+__global__ void k_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst) {
+  const int64_t n = nrep * nel;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / nel, x = t - r * nel;
+    dst[t] = src[idx[r] * nel + x];
+  }
+}
+void launch_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst,
+                          cudaStream_t st) {
+  if (nrep <= 0) return;
+  COUNT_LAUNCH();
+  k_gather_blocks<<<nblocks(nrep * nel, 256), 256, 0, st>>>(nrep, nel, idx, src, dst);
 }
 
 }  // namespace vca

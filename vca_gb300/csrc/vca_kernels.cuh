@@ -135,14 +135,17 @@ struct ClusterDims {
 };
 void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, double2* Glso,
                         cudaStream_t st);
-// Omega integrand: f[w] = (1/Lk) sum_k ln|det(1 + (P_w - Hk_k) G_w)| per spin block
-void launch_omega_ksum(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso,
-                       int64_t Nk, const double2* Hk, double* fpart, int kchunks, cudaStream_t st);
-// same integrand with M = P - Hk on a sparse row pattern (rowptr/cols, lso
-// indices) and all lanes of a warp on the products and the LU updates
+// Omega integrand (sum_kmesh, VCA_OMEGA.f90:37-75): fpart[w][chunk] = sum
+// over the chunk's k of kw[k] ln|det(1 + (P_w - Hk_k) G_w)| per spin block
+// (kw == nullptr: weight 1), M = P - Hk on a sparse row pattern
+// (rowptr/cols, lso indices), all lanes of a warp on the products and the LU
+// updates
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
-                        const double2* Hk, const int* rowptr, const int* cols, double* fpart, int kchunks,
-                        cudaStream_t st);
+                        const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
+                        int kchunks, cudaStream_t st);
+// dst[r] = src[idx[r]] for blocks of nel double2 (k-point representatives)
+void launch_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst,
+                          cudaStream_t st);
 void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out,
                         cudaStream_t st);
 // Gauss-Legendre nodes on (0,1)
