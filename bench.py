@@ -196,10 +196,18 @@ def hxv_operand(s, D, m, dimup):
     x = torch.randn(D, m, dtype=torch.float64, device="cuda")
     x /= torch.linalg.vector_norm(x, dim=0, keepdim=True)
     if fx:
-        # shared-memory staged form while an 8-column up block fits, unless
-        # the warp form is forced (hxv_variant 1)
-        staged = m >= 16 and dimup * 8 * 8 <= 100 * 1024 and s.cfg.hxv_variant != 1
-        name = "k_hxv_fx_s" if staged else ("k_hxv_fx_w" if m >= 16 else "k_hxv_fx")
+        # hxv_variant 2: the chains' layout (rows in hop-count order) and
+        # kernel; 0: staged form while the up block fits; 1: warp form
+        fits = m >= 16 and dimup * 8 * 8 <= 100 * 1024
+        v = s.cfg.hxv_variant
+        if m < 16:
+            name = "k_hxv_fx"
+        elif v == 2:
+            name = "k_hxv_fx_r"
+        elif v == 0 and fits:
+            name = "k_hxv_fx_s"
+        else:
+            name = "k_hxv_fx_w"
         return torch.round(x * 2.0 ** F).to(torch.int64).reshape(-1), name
     return x.reshape(-1), "k_hxv_real"
 
@@ -226,7 +234,9 @@ def run_gpu(args):
 
     pts = build_points()
     mine = [pts[i] for i in partition(len(pts), rank, world)]
-    s = VcaSolver(mine[0].cfg)
+    cfg0 = mine[0].cfg.copy()
+    cfg0.hxv_variant = 2  # the roofline H x v runs in the chains' layout and kernel
+    s = VcaSolver(cfg0)
     s.upload_hk(mine[0].Hk)
     for i in range(args.warmup):
         s.solve_resident(mine[i % len(mine)].Hloc)
@@ -363,7 +373,8 @@ def main():
                     help="profiling mode: one plain solve of a reduced 4x3 point "
                          "(8x8 k-grid, 1024 nodes) after one warm-up solve")
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--hxv-variant", type=int, default=0, help="0 auto, 1 warp form only")
+    ap.add_argument("--hxv-variant", type=int, default=2,
+                    help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
     args = ap.parse_args()
     if args.profile_hxv:
         return profile_hxv(args.profile_hxv, args.reps, args.hxv_variant)

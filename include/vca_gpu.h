@@ -101,7 +101,8 @@ typedef struct vca_config {
   double gf_beta_tol;      /* GF chain stop: beta_{k+1} < tol (exhausted)   */
   uint64_t start_seed;     /* seed of the deterministic Lanczos start vector */
   int32_t arith;           /* VCA_ARITH_AUTO | VCA_ARITH_FP64 | VCA_ARITH_FX   */
-  int32_t hxv_variant;     /* FX column H x v: 0 auto, 1 warp form only        */
+  int32_t hxv_variant;     /* FX column H x v of the hxv entry points: 0 auto, */
+                           /* 1 warp form only, 2 rows in hop-count order     */
   int32_t reserved[6];
 } vca_config;
 
@@ -261,6 +262,11 @@ int vca_gpu_get_timings(double* ms, int32_t n);
  * or more: slabs of 8 adjacent columns, each a contiguous [dim][8] block
  * (element (i, c) at ((c/8)*dim + i)*8 + c%8), ncols a multiple of 8. */
 int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
+/* Row order of a sector's fixed-point column batches under hxv_variant 2
+ * (the order the library's Green's function chains use): order[r] is the
+ * sector element index (iup + idw*DimUp) held in batch row r; up
+ * configurations are sorted by decreasing hop count.  cap >= DimUp*DimDw. */
+int vca_gpu_sector_row_order(int32_t isector, int64_t* order, int64_t cap);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);
 /* CUDA events on the library stream: device time between start and stop. */

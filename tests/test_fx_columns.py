@@ -96,3 +96,24 @@ def test_column_count_not_multiple_of_slab_rejected():
     d = torch.zeros(du * dd * 24, dtype=torch.int64, device="cuda")
     with pytest.raises(VcaError):
         s.hxv_timed(isec, d.data_ptr(), d.data_ptr(), 0, 20, 1)
+
+
+@pytest.mark.parametrize("m", [16, 40])
+def test_position_ordered_form_matches_staged_form(m):
+    """hxv_variant 2 (rows of the up role in hop-count order, the chains'
+    layout) gives the staged form's output bit for bit, row-permuted: both
+    round the same exact int128 sum once."""
+    pt = _point()
+    isec = 1 + 4 + 5 * 10
+    probe = VcaSolver(pt.cfg)
+    probe.set_hamiltonian(pt.Hloc)
+    _, _, du, dd = probe.sector_info(isec)
+    fx, F, G = probe.arith_info()
+    order = probe.sector_row_order(isec)
+    del probe
+    D = du * dd
+    assert sorted(order.tolist()) == list(range(D))
+    X = _fx_columns(D, m, F, seed=300 + m)
+    Ys, _, _ = _apply(pt, 0, isec, X, m)
+    Yr, _, _ = _apply(pt, 2, isec, X[order], m)
+    np.testing.assert_array_equal(Yr, Ys[order])

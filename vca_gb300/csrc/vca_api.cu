@@ -116,6 +116,8 @@ struct Ctx {
   std::vector<int*> fx_perm[2];   // rows by decreasing hop count
   struct PermTabs {
     unsigned* hop = nullptr;
+    unsigned* rhop = nullptr;
+    int* pinv = nullptr;
     int *cnt = nullptr, *npos = nullptr, *word = nullptr;
     i64* e1 = nullptr;
   };
@@ -237,6 +239,9 @@ FxView fx_view_pair(int sa, int na, int sb, int nb) {
   f.up_perm = g->fx_perm[sa][na];
   const Ctx::PermTabs& pt = g->fx_ptab[sa][na];
   f.up_phop = pt.hop;
+  f.up_rhop = pt.rhop;
+  f.up_pinv = pt.pinv;
+  f.rows_permuted = 0;
   f.up_pcnt = pt.cnt;
   f.up_pnpos = pt.npos;
   f.up_pword = pt.word;
@@ -469,9 +474,14 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
             if (S.dim) CUCHK(cudaMemcpy(cnt.data(), S.cnt, sizeof(int) * S.dim, cudaMemcpyDeviceToHost));
             for (int r = 0; r < S.dim; r++) perm[r] = r;
             std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return cnt[x] > cnt[y]; });
+            std::vector<int> pinv(S.dim);
+            for (int r = 0; r < S.dim; r++) pinv[perm[r]] = r;
             RCHK(g->ham.alloc(&g->fx_perm[set][n], S.dim));
-            if (S.dim)
+            RCHK(g->ham.alloc(&g->fx_ptab[set][n].pinv, S.dim));
+            if (S.dim) {
               CUCHK(cudaMemcpy(g->fx_perm[set][n], perm.data(), sizeof(int) * S.dim, cudaMemcpyHostToDevice));
+              CUCHK(cudaMemcpy(g->fx_ptab[set][n].pinv, pinv.data(), sizeof(int) * S.dim, cudaMemcpyHostToDevice));
+            }
           }
           RCHK(g->ham.alloc(&g->fx_code[set][n], (size_t)S.width * S.dim));
           RCHK(g->ham.alloc(&g->fx_e1[set][n], S.dim));
@@ -479,12 +489,13 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
           launch_fx_e1(S.dim, S.e1, fs.A, g->fx_e1[set][n], g->st);
           Ctx::PermTabs& pt = g->fx_ptab[set][n];
           RCHK(g->ham.alloc(&pt.hop, (size_t)S.width * S.dim));
+          RCHK(g->ham.alloc(&pt.rhop, (size_t)S.width * S.dim));
           RCHK(g->ham.alloc(&pt.cnt, S.dim));
           RCHK(g->ham.alloc(&pt.npos, S.dim));
           RCHK(g->ham.alloc(&pt.word, S.dim));
           RCHK(g->ham.alloc(&pt.e1, S.dim));
-          launch_fx_perm_tables(S.dim, S.width, g->fx_perm[set][n], g->fx_hop[set][n], S.cnt,
-                                g->fx_npos[set][n], S.words, g->fx_e1[set][n], pt.hop, pt.cnt, pt.npos,
+          launch_fx_perm_tables(S.dim, S.width, g->fx_perm[set][n], pt.pinv, g->fx_hop[set][n], S.cnt,
+                                g->fx_npos[set][n], S.words, g->fx_e1[set][n], pt.hop, pt.rhop, pt.cnt, pt.npos,
                                 pt.word, pt.e1, g->st);
         }
       }
@@ -1013,11 +1024,16 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     Arena ar;
     BatchBufs bb;
     int rc = alloc_batch(ar, D, m, cplx, nch, g->ld, bb);
-    // fixed-point batches hold the smaller spin block first (see view_pair)
+    // fixed-point batches hold the smaller spin block first (see view_pair),
+    // its rows in hop-count order where the position-ordered H x v applies
     const bool swap = g->fx && tv.dimup > tv.dimdw;
     const SectorView hv = swap ? view_pair(g->dwset, tdw, 0, tup) : tv;
+    FxView hf{};
+    if (g->fx) {
+      hf = swap ? fx_view_pair(g->dwset, tdw, 0, tup) : fx_view_of(tup, tdw);
+      hf.rows_permuted = (g->cfg.hxv_variant != 1 && hxv_fx_r_ok(hv, hf, m)) ? 1 : 0;
+    }
     if (!rc && g->fx) {
-      const FxView hf = swap ? fx_view_pair(g->dwset, tdw, 0, tup) : fx_view_of(tup, tdw);
       const int rbw = hxv_fx_cols_rows(hv, hf, m, g->cfg.hxv_variant == 1);
       rc = ar.alloc(&bb.wpart, 2 * (size_t)rbw * m);
       bb.wpart_rows = rbw;
@@ -1058,8 +1074,9 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     // start vectors: gather from the ground state, normalise per chain
     if (g->fx) {
       const FxScales& fs = g->fxs;
-      const FxView fv = swap ? fx_view_pair(g->dwset, tdw, 0, tup) : fx_view_of(tup, tdw);
-      launch_chain_init_fx(tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, d_ci, m, swap, (i64*)bb.b[0], g->st);
+      const FxView& fv = hf;
+      launch_chain_init_fx(tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, d_ci, m, swap,
+                           fv.rows_permuted ? fv.up_pinv : nullptr, (i64*)bb.b[0], g->st);
       launch_fx_dot(cb, (i64*)bb.b[0], (i64*)bb.b[0], fs.F, fs.F, (i64*)bb.partial, bb.nblk, norm2c, g->st);
       launch_chain_sum(cb, norm2c, norm2, g->st);
       launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
@@ -1885,6 +1902,22 @@ int vca_gpu_sector_map(int32_t isector, int32_t spin, int64_t* map, int64_t cap)
   return VCA_OK;
 }
 
+// Fixed-point view for the public column entry points: with hxv_variant 2
+// the caller's rows of the up role are in hop-count order (the layout of the
+// chain batches, vca_gpu_sector_row_order) and the position-ordered kernel
+// runs.
+static int api_fx_view(int nup, int ndw, int m, FxView* out) {
+  FxView f = fx_view_of(nup, ndw);
+  if (g->cfg.hxv_variant == 2) {
+    if (!hxv_fx_r_ok(view_of(nup, ndw), f, m))
+      VFAIL(VCA_ERR_UNSUPPORTED,
+            "hxv_variant 2 needs >= 16 columns, at most 2 hopping classes and an up block that fits shared memory");
+    f.rows_permuted = 1;
+  }
+  *out = f;
+  return VCA_OK;
+}
+
 // apart: optional alpha-partial scratch of the fixed-point column kernels
 // (hxv_fx_cols_rows rows of m int128), as the Lanczos chain steps pass it
 static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_complex, int32_t ncols,
@@ -1899,10 +1932,13 @@ static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_com
   if (g->fx) {  // slab-major fixed-point columns (scale 2^-F, unit norm)
     if (m >= FX_SLAB && m % FX_SLAB)
       VFAIL(VCA_ERR_ARG, "fixed-point column batches of 8 or more columns need a multiple of 8 columns");
-    if (m >= 16)
-      launch_hxv_fx_cols(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, apart,
-                         g->cfg.hxv_variant == 1, g->st);
-    else
+    if (m >= 16) {
+      FxView fv;
+      RCHK(api_fx_view(nup, ndw, m, &fv));
+      launch_hxv_fx_cols(sv, fv, m, (const i64*)d_v, (i64*)d_hv, apart, g->cfg.hxv_variant == 1, g->st);
+    } else if (g->cfg.hxv_variant == 2) {
+      VFAIL(VCA_ERR_UNSUPPORTED, "hxv_variant 2 needs >= 16 columns");
+    } else
       launch_hxv_fx(sv, fx_view_of(nup, ndw), m, (const i64*)d_v, (i64*)d_hv, g->st);
   } else if (is_complex && !g->real_model) {
     launch_hxv_cplx(sv, g->md, ncols, (const double2*)d_v, (double2*)d_hv, g->st);
@@ -1967,7 +2003,9 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
   const int mm = (is_complex && g->real_model) ? 2 * ncols : ncols;
   if (g->fx && mm >= 16) {  // the alpha partials the chain steps form with the product
     const int nup = sec_nup(isector), ndw = sec_ndw(isector);
-    const int rows = hxv_fx_cols_rows(view_of(nup, ndw), fx_view_of(nup, ndw), mm, g->cfg.hxv_variant == 1);
+    FxView fv;
+    RCHK(api_fx_view(nup, ndw, mm, &fv));
+    const int rows = hxv_fx_cols_rows(view_of(nup, ndw), fv, mm, g->cfg.hxv_variant == 1);
     RCHK(ar.alloc(&apart, 2 * (size_t)rows * mm));
   }
   CUCHK(cudaEventCreate(&e0));
@@ -2021,6 +2059,20 @@ int vca_gpu_timer_stop(double* ms) {
   float f = 0.f;
   CUCHK(cudaEventElapsedTime(&f, g_t0, g_t1));
   if (ms) *ms = f;
+  return VCA_OK;
+}
+
+int vca_gpu_sector_row_order(int32_t isector, int64_t* order, int64_t cap) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded");
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  if (!g->fx) VFAIL(VCA_ERR_UNSUPPORTED, "row orders exist in the fixed-point path only");
+  const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+  const int64_t du = g->dimn[nup], dd = g->dimn[ndw];
+  if (!order || cap < du * dd) VFAIL(VCA_ERR_ARG, "order buffer too small");
+  std::vector<int> perm(du);
+  CUCHK(cudaMemcpy(perm.data(), g->fx_perm[0][nup], sizeof(int) * du, cudaMemcpyDeviceToHost));
+  for (int64_t b = 0; b < dd; b++)
+    for (int64_t p = 0; p < du; p++) order[p + b * du] = perm[p] + b * du;
   return VCA_OK;
 }
 
@@ -2093,7 +2145,13 @@ extern "C" int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void*
   if (g->fx) {
     if (m >= FX_SLAB && m % FX_SLAB)
       VFAIL(VCA_ERR_ARG, "fixed-point column batches of 8 or more columns need a multiple of 8 columns");
-    if (m >= 16) rows = hxv_fx_cols_rows(sv, fx_view_of(nup, ndw), m, warp_only);
+    if (m >= 16) {
+      FxView fv;
+      RCHK(api_fx_view(nup, ndw, m, &fv));
+      rows = hxv_fx_cols_rows(sv, fv, m, warp_only);
+    } else if (g->cfg.hxv_variant == 2) {
+      VFAIL(VCA_ERR_UNSUPPORTED, "hxv_variant 2 needs >= 16 columns");
+    }
     need = (size_t)rows * m * 2 * sizeof(i64);
   } else {
     need = (size_t)rows * m * sizeof(double);
@@ -2106,7 +2164,8 @@ extern "C" int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void*
   RCHK(noalloc_scratch(&scr));
   const ColBatch cb{D, m, false, 0, nullptr, nullptr};
   if (g->fx) {
-    const FxView fv = fx_view_of(nup, ndw);
+    FxView fv = fx_view_of(nup, ndw);
+    if (m >= 16) RCHK(api_fx_view(nup, ndw, m, &fv));
     const int sexp = g->fxs.F + g->fxs.G;
     if (m >= 16) {
       launch_hxv_fx_cols(sv, fv, m, (const i64*)d_v, (i64*)d_hv, (i64*)scr, warp_only, g->st);

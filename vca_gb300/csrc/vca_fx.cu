@@ -39,6 +39,15 @@ __device__ __forceinline__ i64 rshift_round(i128 p, int s) {
   return (i64)(p >> s);
 }
 
+// the same for 1 <= s <= 63 on the two 64-bit words (no int128 shift)
+__device__ __forceinline__ i64 rshift_round63(i128 p, int s) {
+  u64 lo = (u64)p, hi = (u64)(p >> 64);
+  const u64 r = 1ull << (s - 1);
+  lo += r;
+  hi += (lo < r) ? 1ull : 0ull;
+  return (i64)((lo >> s) | (hi << (64 - s)));
+}
+
 __device__ __forceinline__ double i128_to_double(i128 v, int scale_exp) {
   const bool neg = v < 0;
   unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
@@ -84,6 +93,7 @@ void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st)
 // is an exact int64 add into the accumulator of its amplitude class.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ i64 mixed_fx(const FxView& f, unsigned u, unsigned d) {
+  if (f.norb == 1) return f.c0fx + f.Ufx[0] * (i64)__popc(u & d & f.omask[0]);
   i64 s = f.c0fx;
   for (int o = 0; o < f.norb; o++) s += f.Ufx[o] * (i64)__popc(u & d & f.omask[o]);
   int c = 0;
@@ -597,9 +607,9 @@ void launch_fx_sign_sort(int dim, int width, const int* cnt, unsigned* hop, int*
   k_fx_sign_sort<<<(dim + 127) / 128, 128, 0, st>>>(dim, width, cnt, hop, npos);
 }
 
-__global__ void k_fx_perm_tables(int dim, int width, const int* perm, const unsigned* hop, const int* cnt,
-                                 const int* npos, const int* words, const i64* e1, unsigned* phop, int* pcnt,
-                                 int* pnpos, int* pword, i64* pe1) {
+__global__ void k_fx_perm_tables(int dim, int width, const int* perm, const int* pinv, const unsigned* hop,
+                                 const int* cnt, const int* npos, const int* words, const i64* e1, unsigned* phop,
+                                 unsigned* rhop, int* pcnt, int* pnpos, int* pword, i64* pe1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= dim) return;
   const int r = perm[i];
@@ -611,15 +621,16 @@ __global__ void k_fx_perm_tables(int dim, int width, const int* perm, const unsi
     const unsigned hw = hop[(int64_t)h * dim + r];
     const unsigned src = hw & 0xFFFFFFu;
     phop[(int64_t)h * dim + i] = (src * 4u + ((src >> 1) & 3u)) | (hw & 0xFF000000u);
+    rhop[(int64_t)h * dim + i] = (h < cnt[r] ? (unsigned)pinv[src] : 0u) | (hw & 0xFF000000u);
   }
 }
-void launch_fx_perm_tables(int dim, int width, const int* perm, const unsigned* hop, const int* cnt,
-                           const int* npos, const int* words, const i64* e1, unsigned* phop, int* pcnt,
-                           int* pnpos, int* pword, i64* pe1, cudaStream_t st) {
+void launch_fx_perm_tables(int dim, int width, const int* perm, const int* pinv, const unsigned* hop,
+                           const int* cnt, const int* npos, const int* words, const i64* e1, unsigned* phop,
+                           unsigned* rhop, int* pcnt, int* pnpos, int* pword, i64* pe1, cudaStream_t st) {
   if (dim == 0) return;
   count_launch_external();
-  k_fx_perm_tables<<<(dim + 127) / 128, 128, 0, st>>>(dim, width, perm, hop, cnt, npos, words, e1, phop, pcnt,
-                                                      pnpos, pword, pe1);
+  k_fx_perm_tables<<<(dim + 127) / 128, 128, 0, st>>>(dim, width, perm, pinv, hop, cnt, npos, words, e1, phop,
+                                                      rhop, pcnt, pnpos, pword, pe1);
 }
 
 // accumulate one hop's source row into the class accumulators; the class and
@@ -977,6 +988,192 @@ __global__ void __launch_bounds__(512, 2) k_hxv_fx_s(SectorView sv, FxView fv, i
   }
 }
 
+// Column-batch H x v, position-ordered form, for chain batches whose rows
+// of the fast spin role are stored in up_perm order (row p + idw*DimUp holds
+// up configuration up_perm[p]; fv.rows_permuted == 1).  One CTA per (slab
+// cs, down configuration idw), 256 threads.  A lane owns 16-byte unit u
+// (columns 2u, 2u+1) of rows p and p+8 of its warp's group of sixteen
+// consecutive positions, so one mapping serves all three parts:
+//  * down hops: rows p of the neighbour blocks X[idw'] (the hop list of idw
+//    is the same for every row) -- coalesced 512-byte loads, summed in
+//    registers;
+//  * up hops: sources are positions (fv.up_rhop) in the shared-memory copy
+//    of the CTA's own block; the sixteen rows of a warp have nearly equal
+//    hop counts (decreasing order), and hop lists are sign sorted;
+//  * Y rows and the exact int128 alpha partials of unit u -- coalesced
+//    stores, partials in registers.
+// Only the own-block copy needs a barrier; shared memory is one block
+// (DimUp*64 bytes), so four CTAs share an SM on the 4x3 chain sectors.
+#define FXR_THREADS 256
+template <int K, bool SH63, bool APART>
+__global__ void __launch_bounds__(FXR_THREADS, 4) k_hxv_fx_r(SectorView sv, FxView fv, int m,
+                                                              const i64* __restrict__ X, i64* __restrict__ Y,
+                                                              i64* __restrict__ apart) {
+  extern __shared__ __align__(16) unsigned char fxr_smem[];
+  constexpr int W = FX_SLAB;
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int64_t D = (int64_t)DU * DD;
+  longlong2* xs2 = (longlong2*)fxr_smem;                // [DU][4] own block, position order
+  int* doff = (int*)(xs2 + (size_t)DU * 4);            // down hops: offsets in 16-byte units
+  unsigned char* dcl = (unsigned char*)(doff + sv.wdw);
+  const int cs = blockIdx.x / DD;
+  const int idw = blockIdx.x - cs * DD;
+  const int c0 = cs * W;
+  const int64_t rowbase = (int64_t)idw * DU;
+  const longlong2* own = (const longlong2*)X + (int64_t)cs * D * (W / 2) + rowbase * 4;
+  longlong2* yown = (longlong2*)Y + (int64_t)cs * D * (W / 2) + rowbase * 4;
+  const int nd = sv.dw_cnt[idw];
+  const int ndp = fv.dw_npos[idw];
+  for (int h = threadIdx.x; h < nd; h += blockDim.x) {
+    const unsigned hw = fv.dw_hop[idw + h * DD];
+    doff[h] = ((int)(hw & 0xFFFFFFu) - idw) * DU * 4;  // neighbour block relative to own (|.| < D*4 < 2^31)
+    dcl[h] = (unsigned char)((hw >> 24) & 3u);
+  }
+  for (int t = threadIdx.x; t < DU * 4; t += blockDim.x) xs2[t] = __ldcg(own + t);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int u = lane & 3, rsub = lane >> 2;
+  const i64 e1d = fv.dw_e1[idw];
+  const unsigned wdw = (unsigned)sv.dw_words[idw];
+  i128 ad0 = 0, ad1 = 0;
+  for (int pb = warp * 16; pb < DU; pb += nwarp * 16) {
+    const int pr0 = pb + rsub, pr1 = pb + 8 + rsub;
+    const bool ok0 = pr0 < DU, ok1 = pr1 < DU;
+    u64 S[K][2][2];
+#pragma unroll
+    for (int k = 0; k < K; k++) S[k][0][0] = S[k][0][1] = S[k][1][0] = S[k][1][1] = 0;
+    // down hops: rows pr0, pr1 of the neighbour blocks
+    // (a row past the block end reads row 0 of the same neighbour block, in
+    // bounds, and is never stored)
+    const longlong2* a0 = own + (ok0 ? pr0 : 0) * 4 + u;
+    const longlong2* a1 = own + (ok1 ? pr1 : 0) * 4 + u;
+    int h = 0;
+#pragma unroll 2
+    for (; h < ndp; h++) {  // hop lists are sign sorted: positive amplitudes first
+      const int o = doff[h];
+      const longlong2 v0 = __ldcg(a0 + o), v1 = __ldcg(a1 + o);
+      const int cls = (K == 1) ? 0 : (int)dcl[h];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) {
+          S[k][0][0] += (u64)v0.x; S[k][0][1] += (u64)v0.y; S[k][1][0] += (u64)v1.x; S[k][1][1] += (u64)v1.y;
+        }
+    }
+#pragma unroll 2
+    for (; h < nd; h++) {
+      const int o = doff[h];
+      const longlong2 v0 = __ldcg(a0 + o), v1 = __ldcg(a1 + o);
+      const int cls = (K == 1) ? 0 : (int)dcl[h];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) {
+          S[k][0][0] -= (u64)v0.x; S[k][0][1] -= (u64)v0.y; S[k][1][0] -= (u64)v1.x; S[k][1][1] -= (u64)v1.y;
+        }
+    }
+    // up hops from the shared block, then the diagonal, Y and alpha
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int p = j ? pr1 : pr0;
+      if (p >= DU) continue;
+      const int nu = fv.up_pcnt[p];
+      const int nup = fv.up_pnpos[p];
+      int h = 0, o = p;
+#pragma unroll 2
+      for (; h < nup; h++, o += DU) {
+        const unsigned hw = fv.up_rhop[o];
+        const longlong2 v = xs2[(int)(hw & 0xFFFFFFu) * 4 + u];
+        const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (k == cls) { S[k][j][0] += (u64)v.x; S[k][j][1] += (u64)v.y; }
+      }
+#pragma unroll 2
+      for (; h < nu; h++, o += DU) {
+        const unsigned hw = fv.up_rhop[o];
+        const longlong2 v = xs2[(int)(hw & 0xFFFFFFu) * 4 + u];
+        const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          if (k == cls) { S[k][j][0] -= (u64)v.x; S[k][j][1] -= (u64)v.y; }
+      }
+      const longlong2 x = xs2[p * 4 + u];
+      const i64 dfx = fv.up_pe1[p] + e1d + mixed_fx(fv, (unsigned)fv.up_pword[p], wdw);
+      i128 q0 = (i128)dfx * x.x, q1 = (i128)dfx * x.y;
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        q0 += (i128)fv.afx[k] * (i64)S[k][j][0];
+        q1 += (i128)fv.afx[k] * (i64)S[k][j][1];
+      }
+      const i64 y0 = SH63 ? rshift_round63(q0, fv.shift) : rshift_round(q0, fv.shift);
+      const i64 y1 = SH63 ? rshift_round63(q1, fv.shift) : rshift_round(q1, fv.shift);
+      __stcs(yown + p * 4 + u, make_longlong2(y0, y1));
+      if (APART) {
+        if (c0 + 2 * u < m) ad0 += (i128)x.x * y0;
+        if (c0 + 2 * u + 1 < m) ad1 += (i128)x.y * y1;
+      }
+    }
+  }
+  if (APART) {
+    __shared__ i128 red[FXR_THREADS / 32][W];
+    i128 adv[2] = {ad0, ad1};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      u64 lo = (u64)adv[j];
+      i64 hi = (i64)(adv[j] >> 64);
+#pragma unroll
+      for (int off = 4; off < 32; off <<= 1) {  // lanes holding the same columns
+        const u64 lo2 = __shfl_xor_sync(0xffffffffu, lo, off);
+        const i64 hi2 = __shfl_xor_sync(0xffffffffu, hi, off);
+        const u64 sl = lo + lo2;
+        hi = hi + hi2 + (sl < lo ? 1 : 0);
+        lo = sl;
+      }
+      if (lane < 4) red[warp][2 * u + j] = ((i128)hi << 64) | (i128)lo;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < W && c0 + (int)threadIdx.x < m) {
+      i128 sum = 0;
+      for (int w = 0; w < nwarp; w++) sum += red[w][threadIdx.x];
+      const int64_t o2 = 2 * ((int64_t)idw * m + c0 + threadIdx.x);
+      apart[o2] = (i64)(u64)sum;
+      apart[o2 + 1] = (i64)(sum >> 64);
+    }
+  }
+}
+
+#define FXR_SMEM_MAX (200 * 1024)
+static size_t hxv_fx_r_smem(const SectorView& sv) {
+  return (size_t)sv.dimup * FX_SLAB * sizeof(i64) + (size_t)sv.wdw * 5 + 16;
+}
+
+bool hxv_fx_r_ok(const SectorView& sv, const FxView& fv, int m) {
+  return fv.up_rhop && fv.up_pcnt && fv.dw_npos && fv.K <= 2 && m >= 16 && hxv_fx_r_smem(sv) <= FXR_SMEM_MAX &&
+         (int64_t)sv.dimdw * ((m + FX_SLAB - 1) / FX_SLAB) < ((int64_t)1 << 31) &&
+         (int64_t)sv.dimup * sv.dimdw * 4 < ((int64_t)1 << 31);
+}
+
+template <int K, bool SH63, bool APART>
+static void launch_hxv_fx_r_t(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                              cudaStream_t st) {
+  static bool attr_set = false;  // per instantiation, process-wide (every device is sm_103a)
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_hxv_fx_r<K, SH63, APART>, cudaFuncAttributeMaxDynamicSharedMemorySize, FXR_SMEM_MAX);
+    attr_set = true;
+  }
+  const int ns = (m + FX_SLAB - 1) / FX_SLAB;
+  count_launch_external();
+  k_hxv_fx_r<K, SH63, APART><<<sv.dimdw * ns, FXR_THREADS, hxv_fx_r_smem(sv), st>>>(sv, fv, m, X, Y, apart);
+}
+template <int K>
+static void launch_hxv_fx_r_k(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                              cudaStream_t st) {
+  const bool sh63 = fv.shift >= 1 && fv.shift <= 63;
+  if (sh63 && apart) launch_hxv_fx_r_t<K, true, true>(sv, fv, m, X, Y, apart, st);
+  else if (sh63) launch_hxv_fx_r_t<K, true, false>(sv, fv, m, X, Y, apart, st);
+  else if (apart) launch_hxv_fx_r_t<K, false, true>(sv, fv, m, X, Y, apart, st);
+  else launch_hxv_fx_r_t<K, false, false>(sv, fv, m, X, Y, apart, st);
+}
+
 #define FXS_THREADS 512
 #define FXS_SMEM_MAX (220 * 1024)
 static size_t hxv_fx_s_smem(const SectorView& sv, int K) {
@@ -1004,12 +1201,17 @@ static void launch_hxv_fx_s_k(const SectorView& sv, const FxView& fv, int m, con
 }
 
 int hxv_fx_cols_rows(const SectorView& sv, const FxView& fv, int m, bool warp_only) {
-  if (hxv_fx_s_ok(sv, fv, m, warp_only)) return sv.dimdw;
+  if (fv.rows_permuted || hxv_fx_s_ok(sv, fv, m, warp_only)) return sv.dimdw;
   return hxv_fx_w_rowblocks((int64_t)sv.dimup * sv.dimdw);
 }
 
 void launch_hxv_fx_cols(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
                         bool warp_only, cudaStream_t st) {
+  if (fv.rows_permuted) {  // callers set it only where hxv_fx_r_ok holds
+    if (fv.K == 1) launch_hxv_fx_r_k<1>(sv, fv, m, X, Y, apart, st);
+    else launch_hxv_fx_r_k<2>(sv, fv, m, X, Y, apart, st);
+    return;
+  }
   if (hxv_fx_s_ok(sv, fv, m, warp_only)) {
     switch (fv.K) {
       case 1: launch_hxv_fx_s_k<1>(sv, fv, m, X, Y, apart, st); break;

@@ -48,6 +48,9 @@ struct FxView {
   // class in bits 24-25, counts, positive counts, configurations, one-body
   // energies
   const unsigned* up_phop;
+  const unsigned* up_rhop;     // the same hops with the source as its position in up_perm
+  const int* up_pinv;          // position of each up configuration in up_perm
+  int rows_permuted;           // 1: the batch's fast-index rows are in up_perm order
   const int* up_pcnt;
   const int* up_pnpos;
   const int* up_pword;
@@ -78,9 +81,9 @@ __host__ __device__ __forceinline__ int64_t fx_off(int64_t D, int W, int64_t i, 
 }
 
 // up-spin tables in the order of perm (see FxView::up_phop)
-void launch_fx_perm_tables(int dim, int width, const int* perm, const unsigned* hop, const int* cnt,
-                           const int* npos, const int* words, const i64* e1, unsigned* phop, int* pcnt,
-                           int* pnpos, int* pword, i64* pe1, cudaStream_t st);
+void launch_fx_perm_tables(int dim, int width, const int* perm, const int* pinv, const unsigned* hop,
+                           const int* cnt, const int* npos, const int* words, const i64* e1, unsigned* phop,
+                           unsigned* rhop, int* pcnt, int* pnpos, int* pword, i64* pe1, cudaStream_t st);
 // partition each row's hop words positive-first in place; npos[row] counts them
 void launch_fx_sign_sort(int dim, int width, const int* cnt, unsigned* hop, int* npos, cudaStream_t st);
 // packed hop words src | class<<24 | sign<<31 from the FP64 tables
@@ -92,11 +95,15 @@ void launch_fx_pack(int dim, int width, const int* src, const double2* amp, cons
 void launch_hxv_fx_w(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
                      cudaStream_t st);
 int hxv_fx_w_rowblocks(int64_t D);
-// Y = H X on a slab-major column batch (m >= 16) through the fastest form
-// the sector allows (shared-memory staged up block while DimUp*64 bytes fit
-// and warp_only is false, else the warp form); apart, when given, needs
+// Y = H X on a slab-major column batch (m >= 16): the position-ordered
+// form when fv.rows_permuted (rows of the fast spin role in up_perm order),
+// else the shared-memory staged form while DimUp*128 bytes fit and
+// warp_only is false, else the warp form; apart, when given, needs
 // hxv_fx_cols_rows(...) rows of m int128
 int hxv_fx_cols_rows(const SectorView& sv, const FxView& fv, int m, bool warp_only);
+// the position-ordered form (fv.rows_permuted) applies: K <= 2, m >= 16 and
+// the up block fits shared memory
+bool hxv_fx_r_ok(const SectorView& sv, const FxView& fv, int m);
 void launch_hxv_fx_cols(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
                         bool warp_only, cudaStream_t st);
 // per-hop class/sign codes from the FP64 amplitude tables
@@ -127,9 +134,11 @@ void launch_fx_from_double(int64_t n, const double* x, int F, i64* X, cudaStream
 void launch_fx_to_double(int64_t n, const i64* X, int F, double* x, cudaStream_t st);
 // chain start vectors by exact gather (+/- psi, re/im columns) from a FX
 // ground state, into a slab-major batch of m columns; swapped: batch row of
-// element (iup, idw) is idw + iup*DimDw instead of iup + idw*DimUp
+// element (iup, idw) is idw + iup*DimDw instead of iup + idw*DimUp; pinv
+// (optional): the fast index is replaced by its position pinv[.]
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const i64* gs, int nchain,
-                          const ChainInit* d_ci, int m, bool swapped, i64* X, cudaStream_t st);
+                          const ChainInit* d_ci, int m, bool swapped, const int* pinv, i64* X,
+                          cudaStream_t st);
 
 // out[c] = (sum over `rows` int128 partials of column c) * 2^-sexp
 void launch_fx_partial_reduce(int m, int rows, const i64* partial, int sexp, double* out, cudaStream_t st);

@@ -1013,7 +1013,7 @@ void launch_real_to_cplx(int64_t n, const double* in, double2* out, cudaStream_t
 // Fixed-point chain start vectors: the chain operators carry coefficients in
 // {+-1, +-i}, so the gather from a fixed-point ground state is exact.
 __global__ void k_chain_init_fx(SectorView tgt, int src_dimup, const long long* gs, int nchain,
-                                const ChainInit* ci, int m, int swapped, long long* X) {
+                                const ChainInit* ci, int m, int swapped, const int* pinv, long long* X) {
   const int64_t D = (int64_t)tgt.dimup * tgt.dimdw;
   const int64_t n = D * nchain;
   const int W = fx_slab_w(m);  // slab-major batch
@@ -1040,16 +1040,21 @@ __global__ void k_chain_init_fx(SectorView tgt, int src_dimup, const long long* 
       vr += cr * gv;
       vi += cim * gv;
     }
-    const int64_t io = swapped ? (int64_t)idw + (int64_t)iup * tgt.dimdw : i;  // batch row
+    // batch row: fast spin role (up, or down when swapped) first, its index
+    // replaced by its position in the hop-count order when pinv is given
+    const int fa = swapped ? idw : iup, fb = swapped ? iup : idw;
+    const int64_t io = (int64_t)(pinv ? pinv[fa] : fa) + (int64_t)fb * (swapped ? tgt.dimdw : tgt.dimup);
     X[fx_off(D, W, io, c.col0)] = vr;
     if (c.cplxcol) X[fx_off(D, W, io, c.col0 + 1)] = vi;
   }
 }
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long* gs, int nchain,
-                          const ChainInit* d_ci, int m, bool swapped, long long* X, cudaStream_t st) {
+                          const ChainInit* d_ci, int m, bool swapped, const int* pinv, long long* X,
+                          cudaStream_t st) {
   COUNT_LAUNCH();
   int64_t n = (int64_t)tgt.dimup * tgt.dimdw * nchain;
-  k_chain_init_fx<<<nblocks(n, 256), 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, swapped ? 1 : 0, X);
+  k_chain_init_fx<<<nblocks(n, 256), 256, 0, st>>>(tgt, src_dimup, gs, nchain, d_ci, m, swapped ? 1 : 0, pinv,
+                                                   X);
 }
 
 

@@ -155,7 +155,8 @@ void launch_delta_bath(int nz, const double2* z, int N, int Nb, const double2* h
                        double xmu, double2* work, double2* out, cudaStream_t st);
 
 void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long* gs, int nchain,
-                          const ChainInit* d_ci, int m, bool swapped, long long* X, cudaStream_t st);
+                          const ChainInit* d_ci, int m, bool swapped, const int* pinv, long long* X,
+                          cudaStream_t st);
 void count_launch_external();
 
 // ---- helpers ---------------------------------------------------------------

@@ -30,7 +30,7 @@ EXPORTS = [
     "vca_gpu_get_state", "vca_gpu_get_sector_energies", "vca_gpu_get_gf_channel",
     "vca_gpu_sum_kmesh", "vca_gpu_finalize", "vca_gpu_last_error", "vca_gpu_sector_info",
     "vca_gpu_sector_map", "vca_gpu_set_hamiltonian", "vca_gpu_hxv", "vca_gpu_hxv_device",
-    "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
+    "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
     "vca_gpu_arith_info",
 ]
@@ -81,6 +81,7 @@ def load(path: Optional[str] = None):
         "vca_gpu_hxv_device": (ctypes.c_int, [i32, vp, vp, i32]),
         "vca_gpu_hxv_timed": (ctypes.c_int, [i32, vp, vp, i32, i32, i32, dp]),
         "vca_gpu_hxv_alpha_noalloc": (ctypes.c_int, [i32, vp, vp, i32, vp]),
+        "vca_gpu_sector_row_order": (ctypes.c_int, [i32, ctypes.POINTER(i64), i64]),
         "vca_gpu_upload_hk": (ctypes.c_int, [dp, i64]),
         "vca_gpu_solve_resident": (ctypes.c_int, [dp, dp, dp, dp]),
         "vca_gpu_kernel_launches": (i64, []),
@@ -207,6 +208,14 @@ class VcaSolver:
 
     def kernel_launches(self) -> int:
         return int(self.L.vca_gpu_kernel_launches())
+
+    def sector_row_order(self, isector) -> np.ndarray:
+        """Sector element index held in each batch row under hxv_variant 2."""
+        _, _, du, dd = self.sector_info(isector)
+        out = np.zeros(du * dd, dtype=np.int64)
+        check(self.L.vca_gpu_sector_row_order(isector, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                              out.size))
+        return out
 
     def hxv_alpha_noalloc(self, isector, d_v, d_hv, ncols, d_alpha):
         """Y = H X on device columns and alpha[c] = <x_c, H x_c> into the
