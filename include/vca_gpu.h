@@ -165,6 +165,18 @@ int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out);
  */
 int vca_gpu_get_gimp_matsubara(double* g_out);
 int vca_gpu_get_gimp_realaxis(double* g_out);
+/* Cluster self-energy Sigma = G0^-1 - G'^-1 with G0^-1(z) = (z + xmu) - Hloc
+ * - Delta(z), on the Matsubara grid (Lmats points) or the real axis (Lreal
+ * points, + i*eps); same layout as the G getters.  Replaces
+ * vca_get_sigma_matsubara / vca_get_sigma_realaxis (VCA_IO/get_sigma_*.f90,
+ * filled by build_sigma_normal, VCA_GF_NORMAL.f90:1045-1111). */
+int vca_gpu_get_sigma_matsubara(double* s_out);
+int vca_gpu_get_sigma_realaxis(double* s_out);
+/* The non-interacting cluster G0 = (G0^-1)^-1 on the same grids; the
+ * reference forms impG0mats/impG0real in build_sigma_normal and writes them
+ * with vca_print_impG0 (VCA_IO.f90:179-205). */
+int vca_gpu_get_g0_matsubara(double* g0_out);
+int vca_gpu_get_g0_realaxis(double* g0_out);
 
 /*
  * Ground-state bookkeeping of the last solve (VCA_DIAG.f90:224-236,

@@ -64,6 +64,7 @@ def lib():
             "orc_gf_channel": (I, [P, I, I, I, I, I, I, I, dp, dp, dp, dp, I]),
             "orc_gf_cluster": (I, [P, dp, L64, dp]),
             "orc_delta_bath": (I, [P, D, D, dp]),
+            "orc_sigma_g0": (I, [P, D, D, dp, dp]),
             "orc_sum_kmesh": (D, [P, D]),
             "orc_gauss_legendre01": (I, [I, dp, dp]),
             "orc_frequency_integration": (D, [P]),
@@ -261,6 +262,15 @@ class Oracle:
         out = np.zeros((n, n), dtype=np.complex128, order="F")
         self.L.orc_delta_bath(self.h, z.real, z.imag, _dp(out))
         return out
+
+    def sigma_g0(self, z: complex):
+        """(Sigma, G0) at z as lso N x N matrices (build_sigma_normal)."""
+        c = self.cfg
+        N = c.Nlat * c.Nspin * c.Norb
+        sg = np.zeros(N * N, dtype=np.complex128)
+        g0 = np.zeros(N * N, dtype=np.complex128)
+        self.L.orc_sigma_g0(self.h, float(np.real(z)), float(np.imag(z)), _dp(sg), _dp(g0))
+        return sg.reshape(N, N, order="F"), g0.reshape(N, N, order="F")
 
     def sum_kmesh(self, w: float) -> float:
         return self.L.orc_sum_kmesh(self.h, float(w))

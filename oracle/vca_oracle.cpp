@@ -1025,6 +1025,28 @@ void to_lso(const Oracle& o, const cd* a, std::vector<cd>& m) {
                   a[nnn(o, il, jl, is, js, io, jo)];
 }
 
+// build_sigma_normal (VCA_GF_NORMAL.f90:1045-1111) at one z:
+// G0^-1 = (z + xmu) 1 - Hloc - Delta(z) (lso, :1061-1073), Sigma = G0^-1 -
+// G'^-1 (:1076-1095), G0 = (G0^-1)^-1 (:1098-1108).  Outputs in lso.
+void sigma_g0(const Oracle& o, cd z, std::vector<cd>& sig, std::vector<cd>& g0) {
+  const int N = o.Nlso;
+  std::vector<cd> gf, G, H, D;
+  gf_cluster(o, z, gf);
+  to_lso(o, gf.data(), G);
+  to_lso(o, o.Hloc.data(), H);
+  delta_bath(o, z, D);
+  std::vector<cd> inv0((size_t)N * N);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++)
+      inv0[i + (size_t)j * N] = (i == j ? z + o.cfg.xmu : cd(0.0)) - H[i + (size_t)j * N] - D[i + (size_t)j * N];
+  std::vector<cd> Gi = G;
+  lu_inv(N, Gi);
+  sig.resize((size_t)N * N);
+  for (size_t x = 0; x < sig.size(); x++) sig[x] = inv0[x] - Gi[x];
+  g0 = inv0;
+  lu_inv(N, g0);
+}
+
 // ln|det(1 + A)| for an n x n complex A (column-major).  The reference takes
 // log(abs(det(eye+A))) (VCA_OMEGA.f90:66-67).  When ||A||_inf < 1/2 the
 // matrix 1+A is strictly diagonally dominant: eliminate without pivoting,
@@ -1322,6 +1344,15 @@ int orc_delta_bath(void* h, double zr, double zi, double* out) {
   std::vector<cd> d;
   delta_bath(*o, cd(zr, zi), d);
   for (size_t i = 0; i < d.size(); i++) { out[2 * i] = d[i].real(); out[2 * i + 1] = d[i].imag(); }
+  return 0;
+}
+int orc_sigma_g0(void* h, double zr, double zi, double* sig_out, double* g0_out) {
+  std::vector<cd> s, g0;
+  sigma_g0(*(Oracle*)h, cd(zr, zi), s, g0);
+  for (size_t i = 0; i < s.size(); i++) {
+    sig_out[2 * i] = s[i].real(); sig_out[2 * i + 1] = s[i].imag();
+    g0_out[2 * i] = g0[i].real(); g0_out[2 * i + 1] = g0[i].imag();
+  }
   return 0;
 }
 double orc_sum_kmesh(void* h, double w) { return sum_kmesh(*(Oracle*)h, w); }

@@ -272,3 +272,22 @@ def test_fixed_rule_against_qagi():
     val, err = scipy.integrate.quad(o.sum_kmesh, 0.0, np.inf, epsabs=1e-13, epsrel=1e-13, limit=500)
     oi_q = 2.0 * val / np.pi
     assert abs(oi - oi_q) < 1e-10 * abs(egs), (oi, oi_q)
+
+
+def test_oracle_sigma_known_answers():
+    """build_sigma_normal restatement: Sigma = 0 at U = 0, and the half-filled
+    Hubbard atom's Sigma(z) = U/2 + U^2/(4z)."""
+    pt = clusters.chain1d(tprime=1.0, nlat=4, U=0.0, xmu=0.0, nk=8, ngfiter=100, omega_nodes=64)
+    o = Oracle.from_point(pt)
+    o.solve()
+    for z in (0.3j, 1.7j, 0.5 + 0.05j):
+        sg, g0 = o.sigma_g0(z)
+        assert np.abs(sg).max() < 1e-12
+    U = 4.0
+    pt = clusters.chain1d(tprime=1.0, nlat=1, U=U, xmu=U / 2, nk=4, ngfiter=20, omega_nodes=64)
+    o = Oracle.from_point(pt)
+    o.solve()
+    for z in (0.5j, 2.0j, 1.0 + 0.1j):
+        sg, g0 = o.sigma_g0(z)
+        assert abs(sg[0, 0] - (U / 2 + U * U / (4 * z))) < 1e-12
+        assert abs(g0[0, 0] - 1.0 / (z + U / 2)) < 1e-14  # G0 = 1/(z + mu), Hloc = 0

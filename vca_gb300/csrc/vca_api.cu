@@ -1852,25 +1852,107 @@ int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out) {
   return VCA_OK;
 }
 
-static int gimp_grid(bool mats, double* g_out) {
-  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
-  if (!g_out) VFAIL(VCA_ERR_ARG, "NULL output");
+// the Matsubara (wm = pi/beta*(2n-1), VCA_GF_SHARED.f90:50) or real-axis
+// (wr = linspace(wini,wfin,Lreal) + i*eps, VCA_GF_NORMAL.f90:1029) grid
+static std::vector<double> freq_grid(bool mats) {
   const vca_config& c = g->cfg;
   const int L = mats ? c.Lmats : c.Lreal;
   std::vector<double> z(2 * (size_t)L);
   for (int i = 0; i < L; i++) {
-    if (mats) {  // wm = pi/beta*(2n-1) (VCA_GF_SHARED.f90:50)
+    if (mats) {
       z[2 * i] = 0.0;
       z[2 * i + 1] = M_PI / c.beta * (2.0 * (i + 1) - 1.0);
-    } else {     // wr = linspace(wini,wfin,Lreal), +i*eps (VCA_GF_NORMAL.f90:1029)
+    } else {
       z[2 * i] = (L > 1) ? c.wini + (c.wfin - c.wini) * i / (double)(L - 1) : c.wini;
       z[2 * i + 1] = c.eps;
     }
   }
-  return vca_gpu_gf_cluster(z.data(), L, g_out);
+  return z;
+}
+
+static int gimp_grid(bool mats, double* g_out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!g_out) VFAIL(VCA_ERR_ARG, "NULL output");
+  const std::vector<double> z = freq_grid(mats);
+  return vca_gpu_gf_cluster(z.data(), (int64_t)(z.size() / 2), g_out);
+}
+
+// Sigma (want_g0 = false) or G0 on the Matsubara or real-axis grid, as
+// build_sigma_normal (VCA_GF_NORMAL.f90:1045-1111), out in
+// (Nlat,Nlat,Nspin,Nspin,Norb,Norb,L) order
+static int sigma_grid(bool mats, bool want_g0, double* out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!out) VFAIL(VCA_ERR_ARG, "NULL output");
+  const vca_config& c = g->cfg;
+  const int N = g->N, NN = N * N;
+  if (N > 32) VFAIL(VCA_ERR_UNSUPPORTED, "self-energy supports up to 32 spin-orbitals");
+  const std::vector<double> zh = freq_grid(mats);
+  const int n = (int)(zh.size() / 2);
+  if (n == 0) return VCA_OK;
+  Arena ar;
+  int rc;
+  double2 *dz, *Glso = nullptr, *P, *Hl, *res;
+  if ((rc = ar.alloc(&dz, n)) || (rc = ar.alloc(&Hl, NN)) || (rc = ar.alloc(&res, (size_t)n * NN))) {
+    ar.release();
+    return rc;
+  }
+  cudaMemcpyAsync(dz, zh.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, g->st);
+  if (!want_g0) {
+    if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = gf_lso(n, dz, Glso, ar))) { ar.release(); return rc; }
+  }
+  {
+    double2* hraw;
+    if ((rc = ar.alloc(&hraw, NN))) { ar.release(); return rc; }
+    cudaMemcpyAsync(hraw, g->Hloc.data(), sizeof(double2) * NN, cudaMemcpyHostToDevice, g->st);
+    launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, 1, hraw, Hl, g->st);
+  }
+  bool per_z = false;
+  P = Hl;
+  if (g->has_bath) {  // P = Delta(z) + Hloc
+    std::vector<double2> hb, V;
+    bath_lso(hb, V);
+    double2 *dhb, *dV, *work, *D;
+    const int Nb = g->Nb;
+    if ((rc = ar.alloc(&dhb, (size_t)Nb * Nb)) || (rc = ar.alloc(&dV, (size_t)N * Nb)) ||
+        (rc = ar.alloc(&work, (size_t)n * 2 * Nb * Nb)) || (rc = ar.alloc(&D, (size_t)n * NN)) ||
+        (rc = ar.alloc(&P, (size_t)n * NN))) {
+      ar.release();
+      return rc;
+    }
+    cudaMemcpyAsync(dhb, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(dV, V.data(), sizeof(double2) * V.size(), cudaMemcpyHostToDevice, g->st);
+    launch_delta_bath(n, dz, N, Nb, dhb, dV, c.xmu, work, D, g->st);
+    launch_add_hloc(n, NN, D, Hl, P, g->st);
+    per_z = true;
+  }
+  launch_sigma_g0(n, N, dz, Glso, P, per_z, c.xmu, want_g0, res, g->st);
+  std::vector<double2> h((size_t)n * NN);
+  cudaMemcpyAsync(h.data(), res, sizeof(double2) * h.size(), cudaMemcpyDeviceToHost, g->st);
+  cudaError_t e = cudaStreamSynchronize(g->st);
+  ar.release();
+  if (e != cudaSuccess) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e));
+  const size_t nel = hloc_len(c);
+  for (int q = 0; q < n; q++)
+    for (int il = 0; il < c.Nlat; il++)
+      for (int jl = 0; jl < c.Nlat; jl++)
+        for (int is = 0; is < c.Nspin; is++)
+          for (int js = 0; js < c.Nspin; js++)
+            for (int io = 0; io < c.Norb; io++)
+              for (int jo = 0; jo < c.Norb; jo++) {
+                const int a = io + il * c.Norb + is * c.Norb * c.Nlat, b = jo + jl * c.Norb + js * c.Norb * c.Nlat;
+                const double2 v = h[(size_t)q * NN + a + (size_t)b * N];
+                const size_t o = (size_t)q * nel + idx_nnn(c, il, jl, is, js, io, jo);
+                out[2 * o] = v.x;
+                out[2 * o + 1] = v.y;
+              }
+  return VCA_OK;
 }
 int vca_gpu_get_gimp_matsubara(double* g_out) { return gimp_grid(true, g_out); }
 int vca_gpu_get_gimp_realaxis(double* g_out) { return gimp_grid(false, g_out); }
+int vca_gpu_get_sigma_matsubara(double* s_out) { return sigma_grid(true, false, s_out); }
+int vca_gpu_get_sigma_realaxis(double* s_out) { return sigma_grid(false, false, s_out); }
+int vca_gpu_get_g0_matsubara(double* g0_out) { return sigma_grid(true, true, g0_out); }
+int vca_gpu_get_g0_realaxis(double* g0_out) { return sigma_grid(false, true, g0_out); }
 
 int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out) {
   if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");

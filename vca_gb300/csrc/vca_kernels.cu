@@ -1220,6 +1220,113 @@ void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const
   k_omega_ksum2<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, kchunks);
 }
 
+// ---------------------------------------------------------------------------
+// Self-energy and Weiss field on a frequency grid (build_sigma_normal,
+// VCA_GF_NORMAL.f90:1045-1111): G0^-1(z) = (z + xmu) 1 - Hloc - Delta(z),
+// Sigma = G0^-1 - G'^-1, G0 = (G0^-1)^-1, per z on N x N lso matrices
+// (N <= 32).  One warp per z: Gauss-Jordan with partial pivoting on the
+// augmented [A | 1] in shared memory, stored column-major with 32-row
+// columns so that lane r (row r) works conflict-free.
+// ---------------------------------------------------------------------------
+__device__ void warp_gj_inverse(double2* M, int N) {
+  const int lane = threadIdx.x & 31;
+  const int N2 = 2 * N;
+  for (int k = 0; k < N; k++) {
+    double mag = -1.0;
+    int arg = k;
+    if (lane >= k && lane < N) {
+      const double2 a = M[k * 32 + lane];
+      mag = a.x * a.x + a.y * a.y;
+      arg = lane;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double om = __shfl_xor_sync(0xffffffffu, mag, o);
+      const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+      if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
+    }
+    if (!(mag > 0.0)) continue;  // singular column: left as is (the result is undefined, as in the reference)
+    if (arg != k)
+      for (int j = lane; j < N2; j += 32) {
+        const double2 t = M[j * 32 + k];
+        M[j * 32 + k] = M[j * 32 + arg];
+        M[j * 32 + arg] = t;
+      }
+    __syncwarp();
+    const double2 piv = M[k * 32 + k];
+    const double ir = piv.x / mag, ii = -piv.y / mag;  // 1/piv
+    __syncwarp();
+    for (int j = lane; j < N2; j += 32) {
+      const double2 a = M[j * 32 + k];
+      M[j * 32 + k] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
+    }
+    __syncwarp();
+    if (lane < N && lane != k) {
+      const double2 f = M[k * 32 + lane];
+      for (int j = 0; j < N2; j++) {
+        const double2 u = M[j * 32 + k];
+        double2& t = M[j * 32 + lane];
+        t.x -= f.x * u.x - f.y * u.y;
+        t.y -= f.x * u.y + f.y * u.x;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// want_g0 = 0: out = Sigma(z); 1: out = G0(z).  P = Delta + Hloc (lso, per z
+// when per_z_p, else one matrix).
+__global__ void k_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const double2* P, int per_z_p,
+                           double xmu, int want_g0, double2* out) {
+  extern __shared__ double2 gjm[];
+  const int q = blockIdx.x;
+  if (q >= nz) return;
+  const int lane = threadIdx.x & 31;
+  const int NN = N * N;
+  const double2 zz = make_double2(z[q].x + xmu, z[q].y);
+  const double2* Pq = P + (per_z_p ? (int64_t)q * NN : 0);
+  // A = G (Sigma) or G0^-1 (G0), augmented with the identity
+  for (int c = 0; c < N; c++) {
+    if (lane < N) {
+      double2 a;
+      if (want_g0) {
+        const double2 p = Pq[lane + c * N];
+        a = make_double2((lane == c ? zz.x : 0.0) - p.x, (lane == c ? zz.y : 0.0) - p.y);
+      } else {
+        a = Glso[(int64_t)q * NN + lane + c * N];
+      }
+      gjm[c * 32 + lane] = a;
+      gjm[(N + c) * 32 + lane] = make_double2(lane == c ? 1.0 : 0.0, 0.0);
+    }
+  }
+  __syncwarp();
+  warp_gj_inverse(gjm, N);
+  for (int c = 0; c < N; c++) {
+    if (lane < N) {
+      const double2 inv = gjm[(N + c) * 32 + lane];
+      double2 r;
+      if (want_g0) {
+        r = inv;
+      } else {  // Sigma = (z + xmu) 1 - P - G^-1
+        const double2 p = Pq[lane + c * N];
+        r = make_double2((lane == c ? zz.x : 0.0) - p.x - inv.x, (lane == c ? zz.y : 0.0) - p.y - inv.y);
+      }
+      out[(int64_t)q * NN + lane + c * N] = r;
+    }
+  }
+}
+void launch_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const double2* P, bool per_z_p,
+                     double xmu, bool want_g0, double2* out, cudaStream_t st) {
+  if (nz <= 0) return;
+  COUNT_LAUNCH();
+  const size_t shm = sizeof(double2) * 2 * (size_t)N * 32;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_sigma_g0, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    attr = true;
+  }
+  k_sigma_g0<<<nz, 32, shm, st>>>(nz, N, z, Glso, P, per_z_p ? 1 : 0, xmu, want_g0 ? 1 : 0, out);
+}
+
 // dst[r] = src[idx[r]] for blocks of nel double2
 __global__ void k_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst) {
   const int64_t n = nrep * nel;

@@ -143,6 +143,11 @@ void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, doub
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
                         int kchunks, cudaStream_t st);
+// Sigma(z) (want_g0 = false) or G0(z) on nz frequencies from G' (lso) and
+// P = Delta + Hloc (per z, or one matrix): build_sigma_normal,
+// VCA_GF_NORMAL.f90:1045-1111.  N <= 32.
+void launch_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const double2* P, bool per_z_p,
+                     double xmu, bool want_g0, double2* out, cudaStream_t st);
 // dst[r] = src[idx[r]] for blocks of nel double2 (k-point representatives)
 void launch_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst,
                           cudaStream_t st);

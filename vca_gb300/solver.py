@@ -30,6 +30,8 @@ EXPORTS = [
     "vca_gpu_get_state", "vca_gpu_get_sector_energies", "vca_gpu_get_gf_channel",
     "vca_gpu_sum_kmesh", "vca_gpu_finalize", "vca_gpu_last_error", "vca_gpu_sector_info",
     "vca_gpu_sector_map", "vca_gpu_set_hamiltonian", "vca_gpu_hxv", "vca_gpu_hxv_device",
+    "vca_gpu_get_sigma_matsubara", "vca_gpu_get_sigma_realaxis", "vca_gpu_get_g0_matsubara",
+    "vca_gpu_get_g0_realaxis",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
     "vca_gpu_arith_info",
@@ -65,6 +67,10 @@ def load(path: Optional[str] = None):
         "vca_gpu_gf_cluster": (ctypes.c_int, [dp, i64, dp]),
         "vca_gpu_get_gimp_matsubara": (ctypes.c_int, [dp]),
         "vca_gpu_get_gimp_realaxis": (ctypes.c_int, [dp]),
+        "vca_gpu_get_sigma_matsubara": (ctypes.c_int, [dp]),
+        "vca_gpu_get_sigma_realaxis": (ctypes.c_int, [dp]),
+        "vca_gpu_get_g0_matsubara": (ctypes.c_int, [dp]),
+        "vca_gpu_get_g0_realaxis": (ctypes.c_int, [dp]),
         "vca_gpu_get_state_count": (ctypes.c_int, [ctypes.POINTER(i32)]),
         "vca_gpu_get_state": (ctypes.c_int, [i32, ctypes.POINTER(i32), dp]),
         "vca_gpu_get_sector_energies": (ctypes.c_int, [dp, i32]),
@@ -284,6 +290,25 @@ class VcaSolver:
         out = np.zeros(hloc_shape(self.cfg) + (self.cfg.Lreal,), dtype=np.complex128, order="F")
         check(self.L.vca_gpu_get_gimp_realaxis(_dp(out)))
         return out
+
+    def _grid(self, fn, mats: bool) -> np.ndarray:
+        L = self.cfg.Lmats if mats else self.cfg.Lreal
+        out = np.zeros(hloc_shape(self.cfg) + (L,), dtype=np.complex128, order="F")
+        check(fn(_dp(out)))
+        return out
+
+    def sigma_matsubara(self) -> np.ndarray:
+        """vca_get_sigma_matsubara: Sigma(i w_n), (Nlat,Nlat,Nspin,Nspin,Norb,Norb,Lmats)."""
+        return self._grid(self.L.vca_gpu_get_sigma_matsubara, True)
+
+    def sigma_realaxis(self) -> np.ndarray:
+        return self._grid(self.L.vca_gpu_get_sigma_realaxis, False)
+
+    def g0_matsubara(self) -> np.ndarray:
+        return self._grid(self.L.vca_gpu_get_g0_matsubara, True)
+
+    def g0_realaxis(self) -> np.ndarray:
+        return self._grid(self.L.vca_gpu_get_g0_realaxis, False)
 
     def sum_kmesh(self, w) -> np.ndarray:
         w = np.ascontiguousarray(np.atleast_1d(w), dtype=np.float64)
