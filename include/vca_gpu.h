@@ -177,6 +177,17 @@ int vca_gpu_get_sigma_realaxis(double* s_out);
  * with vca_print_impG0 (VCA_IO.f90:179-205). */
 int vca_gpu_get_g0_matsubara(double* g0_out);
 int vca_gpu_get_g0_realaxis(double* g0_out);
+/* Ground-state observables of the last solve, (Nlat,Norb) column-major:
+ * density n_up + n_dw, its spin parts, double occupancy n_up n_dw and
+ * magnetisation n_up - n_dw, averaged over the kept ground states with
+ * weight 1/zeta.  Replace vca_get_dens / vca_get_docc / vca_get_mag
+ * (VCA_IO/get_dens.f90, get_docc.f90, get_mag.f90), filled by
+ * vca_lanc_observables (VCA_OBSERVABLES.f90:185-316). */
+int vca_gpu_get_dens(double* out);
+int vca_gpu_get_dens_up(double* out);
+int vca_gpu_get_dens_dw(double* out);
+int vca_gpu_get_docc(double* out);
+int vca_gpu_get_mag(double* out);
 
 /*
  * Ground-state bookkeeping of the last solve (VCA_DIAG.f90:224-236,

@@ -65,6 +65,7 @@ def lib():
             "orc_gf_cluster": (I, [P, dp, L64, dp]),
             "orc_delta_bath": (I, [P, D, D, dp]),
             "orc_sigma_g0": (I, [P, D, D, dp, dp]),
+            "orc_observables": (I, [P, dp]),
             "orc_sum_kmesh": (D, [P, D]),
             "orc_gauss_legendre01": (I, [I, dp, dp]),
             "orc_frequency_integration": (D, [P]),
@@ -262,6 +263,16 @@ class Oracle:
         out = np.zeros((n, n), dtype=np.complex128, order="F")
         self.L.orc_delta_bath(self.h, z.real, z.imag, _dp(out))
         return out
+
+    def observables(self) -> dict:
+        """dens, dens_up, dens_dw, docc, mag as (Nlat, Norb) arrays (vca_lanc_observables)."""
+        c = self.cfg
+        nimp = c.Nlat * c.Norb
+        v = np.zeros(3 * nimp)
+        self.L.orc_observables(self.h, _dp(v))
+        # flat index = bit = iorb + ilat*Norb (imp_state_index)
+        up, dw, dd = (v[q * nimp:(q + 1) * nimp].reshape(c.Nlat, c.Norb) for q in range(3))
+        return {"dens": up + dw, "dens_up": up, "dens_dw": dw, "docc": dd, "mag": up - dw}
 
     def sigma_g0(self, z: complex):
         """(Sigma, G0) at z as lso N x N matrices (build_sigma_normal)."""

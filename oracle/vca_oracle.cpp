@@ -1025,6 +1025,31 @@ void to_lso(const Oracle& o, const cd* a, std::vector<cd>& m) {
                   a[nnn(o, il, jl, is, js, io, jo)];
 }
 
+// vca_lanc_observables (VCA_OBSERVABLES.f90:185-316) at T = 0: over the
+// kept states with weight 1/zeta (:226-228), |psi_i|^2 times n_up, n_dw and
+// n_up n_dw of each cluster site-orbital (imp_state_index = iorb +
+// (ilat-1)*Norb, :248-258).  out[q*nimp + l], q = up, dw, docc.
+void observables(const Oracle& o, std::vector<double>& out) {
+  const vca_config& c = o.cfg;
+  const int nimp = c.Nlat * c.Norb;
+  out.assign(3 * (size_t)nimp, 0.0);
+  for (const State& st : o.states) {
+    const int nup = (st.sector - 1) / (o.Ns + 1), ndw = (st.sector - 1) % (o.Ns + 1);
+    const std::vector<int64_t> mu = build_map(o.Ns, nup), md = build_map(o.Ns, ndw);
+    const int64_t du = (int64_t)mu.size();
+    for (size_t i = 0; i < st.vec.size(); i++) {
+      const int64_t iup = (int64_t)i % du, idw = (int64_t)i / du;  // state2indices (VCA_SETUP.f90:491-502)
+      const double w = std::norm(st.vec[i]) / o.zeta;
+      for (int l = 0; l < nimp; l++) {
+        const int a = (int)((mu[iup] >> l) & 1), b = (int)((md[idw] >> l) & 1);
+        out[l] += a * w;
+        out[nimp + l] += b * w;
+        out[2 * nimp + l] += a * b * w;
+      }
+    }
+  }
+}
+
 // build_sigma_normal (VCA_GF_NORMAL.f90:1045-1111) at one z:
 // G0^-1 = (z + xmu) 1 - Hloc - Delta(z) (lso, :1061-1073), Sigma = G0^-1 -
 // G'^-1 (:1076-1095), G0 = (G0^-1)^-1 (:1098-1108).  Outputs in lso.
@@ -1354,6 +1379,12 @@ int orc_sigma_g0(void* h, double zr, double zi, double* sig_out, double* g0_out)
     g0_out[2 * i] = g0[i].real(); g0_out[2 * i + 1] = g0[i].imag();
   }
   return 0;
+}
+int orc_observables(void* h, double* out) {
+  std::vector<double> v;
+  observables(*(Oracle*)h, v);
+  for (size_t i = 0; i < v.size(); i++) out[i] = v[i];
+  return (int)v.size();
 }
 double orc_sum_kmesh(void* h, double w) { return sum_kmesh(*(Oracle*)h, w); }
 int orc_gauss_legendre01(int n, double* x, double* w) {

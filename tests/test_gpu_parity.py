@@ -217,3 +217,16 @@ def test_sigma_and_g0_grids_match_oracle(name):
         assert np.abs(gg - go).max() <= 1e-10 * (1.0 + np.abs(go).max()), (name, z)
         sref = np.linalg.inv(gg) - np.linalg.inv(nnn2lso(gimp[..., q]))
         assert np.abs(nnn2lso(sig[..., q]) - sref).max() <= 1e-9 * (1.0 + np.abs(sref).max()), (name, z)
+
+
+@pytest.mark.parametrize("name", list(POINTS))
+def test_observables_match_oracle(name):
+    """vca_get_dens/_docc/_mag (vca_lanc_observables) against the oracle."""
+    pt = POINTS[name]()
+    s = VcaSolver(pt.cfg, pt.bath_h, pt.bath_v)
+    s.solve(pt.Hloc, pt.Hk, pt.bath_h, pt.bath_v)
+    o = Oracle.from_point(pt)
+    o.solve()
+    got, ref = s.observables(), o.observables()
+    for key in ref:
+        np.testing.assert_allclose(got[key], ref[key], rtol=0, atol=1e-10, err_msg=f"{name} {key}")

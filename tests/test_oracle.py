@@ -291,3 +291,24 @@ def test_oracle_sigma_known_answers():
         sg, g0 = o.sigma_g0(z)
         assert abs(sg[0, 0] - (U / 2 + U * U / (4 * z))) < 1e-12
         assert abs(g0[0, 0] - 1.0 / (z + U / 2)) < 1e-14  # G0 = 1/(z + mu), Hloc = 0
+
+
+def test_oracle_observables_known_answers():
+    """vca_lanc_observables restatement: the half-filled Hubbard atom has two
+    degenerate ground states (one electron, either spin, weight 1/2 each):
+    dens 1, dens_up = dens_dw = 1/2, docc 0, mag 0; a half-filled 2x2 cluster
+    holds N = 4 electrons and its AFM Weiss field gives a staggered mag."""
+    pt = clusters.chain1d(tprime=1.0, nlat=1, U=4.0, xmu=2.0, nk=4, ngfiter=20, omega_nodes=64)
+    o = Oracle.from_point(pt)
+    o.solve()
+    ob = o.observables()
+    assert abs(ob["dens"][0, 0] - 1.0) < 1e-14 and abs(ob["dens_up"][0, 0] - 0.5) < 1e-14
+    assert abs(ob["docc"][0, 0]) < 1e-14 and abs(ob["mag"][0, 0]) < 1e-14
+    pt = clusters.square(nx=2, ny=2, U=8.0, xmu=4.0, maf=0.2, nspin=2, nkx=4, nky=4, ngfiter=40,
+                         omega_nodes=64)
+    o = Oracle.from_point(pt)
+    o.solve()
+    ob = o.observables()
+    assert abs(ob["dens"].sum() - 4.0) < 1e-12
+    m = ob["mag"][:, 0]
+    assert m[0] < -0.5 and m[1] > 0.5 and m[2] > 0.5 and m[3] < -0.5  # (-1)^(x+y) pattern

@@ -1949,6 +1949,55 @@ static int sigma_grid(bool mats, bool want_g0, double* out) {
 }
 int vca_gpu_get_gimp_matsubara(double* g_out) { return gimp_grid(true, g_out); }
 int vca_gpu_get_gimp_realaxis(double* g_out) { return gimp_grid(false, g_out); }
+// Ground-state observables (vca_lanc_observables, VCA_OBSERVABLES.f90:
+// 185-316, T = 0: weight 1/zeta per kept state): which = 0 dens, 1 dens_up,
+// 2 dens_dw, 3 docc, 4 mag = dens_up - dens_dw (VCA_IO/get_mag.f90), out in
+// (Nlat,Norb) order
+static int observable(int which, double* out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!out) VFAIL(VCA_ERR_ARG, "NULL output");
+  const vca_config& c = g->cfg;
+  const int nimp = c.Nlat * c.Norb;
+  std::vector<double> up(nimp, 0.0), dw(nimp, 0.0), dd(nimp, 0.0);
+  for (const GState& st : g->gs) {
+    const SectorView sv = view_of(sec_nup(st.sector), sec_ndw(st.sector));
+    const int nb = observables_blocks((int64_t)sv.dimup * sv.dimdw);
+    Arena ar;
+    double* part;
+    RCHK(ar.alloc(&part, (size_t)3 * nimp * nb));
+    const int fmt = g->fx ? 0 : (g->real_model ? 1 : 2);
+    launch_observables(sv, fmt, st.vec, g->fxs.F, nimp, part, g->st);
+    std::vector<double> h((size_t)3 * nimp * nb);
+    cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, g->st);
+    cudaError_t e = cudaStreamSynchronize(g->st);
+    ar.release();
+    if (e != cudaSuccess) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e));
+    for (int l = 0; l < nimp; l++) {
+      double a = 0.0, b = 0.0, d = 0.0;
+      for (int x = 0; x < nb; x++) {
+        a += h[((size_t)0 * nimp + l) * nb + x];
+        b += h[((size_t)1 * nimp + l) * nb + x];
+        d += h[((size_t)2 * nimp + l) * nb + x];
+      }
+      up[l] += a / g->zeta;
+      dw[l] += b / g->zeta;
+      dd[l] += d / g->zeta;
+    }
+  }
+  for (int il = 0; il < c.Nlat; il++)
+    for (int io = 0; io < c.Norb; io++) {
+      const int l = io + il * c.Norb;  // imp_state_index (VCA_SETUP.f90:705-710)
+      const double v[5] = {up[l] + dw[l], up[l], dw[l], dd[l], up[l] - dw[l]};
+      out[il + io * c.Nlat] = v[which];
+    }
+  return VCA_OK;
+}
+int vca_gpu_get_dens(double* out) { return observable(0, out); }
+int vca_gpu_get_dens_up(double* out) { return observable(1, out); }
+int vca_gpu_get_dens_dw(double* out) { return observable(2, out); }
+int vca_gpu_get_docc(double* out) { return observable(3, out); }
+int vca_gpu_get_mag(double* out) { return observable(4, out); }
+
 int vca_gpu_get_sigma_matsubara(double* s_out) { return sigma_grid(true, false, s_out); }
 int vca_gpu_get_sigma_realaxis(double* s_out) { return sigma_grid(false, false, s_out); }
 int vca_gpu_get_g0_matsubara(double* g0_out) { return sigma_grid(true, true, g0_out); }

@@ -1327,6 +1327,56 @@ void launch_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const
   k_sigma_g0<<<nz, 32, shm, st>>>(nz, N, z, Glso, P, per_z_p ? 1 : 0, xmu, want_g0 ? 1 : 0, out);
 }
 
+// ---------------------------------------------------------------------------
+// Ground-state observables (vca_lanc_observables, VCA_OBSERVABLES.f90:
+// 185-316): for one state psi of a sector, sums over its elements of
+// |psi_i|^2 n_up(l), |psi_i|^2 n_dw(l) and |psi_i|^2 n_up(l) n_dw(l) for each
+// cluster spin-orbital bit l (imp_state_index = iorb + (ilat-1)*Norb).
+// grid.y = l, grid.z = quantity; each block writes one partial, reduced by
+// the host in a fixed order.  fmt: 0 int64 fixed point (scale 2^-F),
+// 1 double, 2 double2.
+// ---------------------------------------------------------------------------
+__global__ void k_observables(SectorView sv, int fmt, const void* vec, int F, double* part) {
+  const int l = blockIdx.y, qn = blockIdx.z;
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const double sc = ldexp(1.0, -F);
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+    const int idw = (int)(i / sv.dimup);
+    const int iup = (int)(i - (int64_t)idw * sv.dimup);
+    const int nu = (sv.up_words[iup] >> l) & 1, nd = (sv.dw_words[idw] >> l) & 1;
+    const int on = qn == 0 ? nu : (qn == 1 ? nd : nu & nd);
+    if (!on) continue;
+    double w;
+    if (fmt == 0) {
+      const double x = (double)((const long long*)vec)[i] * sc;
+      w = x * x;
+    } else if (fmt == 1) {
+      const double x = ((const double*)vec)[i];
+      w = x * x;
+    } else {
+      const double2 x = ((const double2*)vec)[i];
+      w = x.x * x.x + x.y * x.y;
+    }
+    acc += w;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[((int64_t)qn * gridDim.y + l) * gridDim.x + blockIdx.x] = red[0];
+}
+int observables_blocks(int64_t D) { return (int)std::max<int64_t>(1, std::min<int64_t>((D + 255) / 256, 304)); }
+void launch_observables(const SectorView& sv, int fmt, const void* vec, int F, int nimp, double* part,
+                        cudaStream_t st) {
+  COUNT_LAUNCH();
+  const dim3 grd(observables_blocks((int64_t)sv.dimup * sv.dimdw), nimp, 3);
+  k_observables<<<grd, 256, 0, st>>>(sv, fmt, vec, F, part);
+}
+
 // dst[r] = src[idx[r]] for blocks of nel double2
 __global__ void k_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst) {
   const int64_t n = nrep * nel;

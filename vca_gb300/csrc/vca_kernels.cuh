@@ -148,6 +148,11 @@ void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const
 // VCA_GF_NORMAL.f90:1045-1111.  N <= 32.
 void launch_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const double2* P, bool per_z_p,
                      double xmu, bool want_g0, double2* out, cudaStream_t st);
+// Ground-state observable partials of one state: part[(q*nimp + l)*nb + b]
+// for q = n_up, n_dw, n_up*n_dw, bit l, block b < observables_blocks(D)
+int observables_blocks(int64_t D);
+void launch_observables(const SectorView& sv, int fmt, const void* vec, int F, int nimp, double* part,
+                        cudaStream_t st);
 // dst[r] = src[idx[r]] for blocks of nel double2 (k-point representatives)
 void launch_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const double2* src, double2* dst,
                           cudaStream_t st);

@@ -31,7 +31,8 @@ EXPORTS = [
     "vca_gpu_sum_kmesh", "vca_gpu_finalize", "vca_gpu_last_error", "vca_gpu_sector_info",
     "vca_gpu_sector_map", "vca_gpu_set_hamiltonian", "vca_gpu_hxv", "vca_gpu_hxv_device",
     "vca_gpu_get_sigma_matsubara", "vca_gpu_get_sigma_realaxis", "vca_gpu_get_g0_matsubara",
-    "vca_gpu_get_g0_realaxis",
+    "vca_gpu_get_g0_realaxis", "vca_gpu_get_dens", "vca_gpu_get_dens_up", "vca_gpu_get_dens_dw",
+    "vca_gpu_get_docc", "vca_gpu_get_mag",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
     "vca_gpu_arith_info",
@@ -71,6 +72,11 @@ def load(path: Optional[str] = None):
         "vca_gpu_get_sigma_realaxis": (ctypes.c_int, [dp]),
         "vca_gpu_get_g0_matsubara": (ctypes.c_int, [dp]),
         "vca_gpu_get_g0_realaxis": (ctypes.c_int, [dp]),
+        "vca_gpu_get_dens": (ctypes.c_int, [dp]),
+        "vca_gpu_get_dens_up": (ctypes.c_int, [dp]),
+        "vca_gpu_get_dens_dw": (ctypes.c_int, [dp]),
+        "vca_gpu_get_docc": (ctypes.c_int, [dp]),
+        "vca_gpu_get_mag": (ctypes.c_int, [dp]),
         "vca_gpu_get_state_count": (ctypes.c_int, [ctypes.POINTER(i32)]),
         "vca_gpu_get_state": (ctypes.c_int, [i32, ctypes.POINTER(i32), dp]),
         "vca_gpu_get_sector_energies": (ctypes.c_int, [dp, i32]),
@@ -295,6 +301,15 @@ class VcaSolver:
         L = self.cfg.Lmats if mats else self.cfg.Lreal
         out = np.zeros(hloc_shape(self.cfg) + (L,), dtype=np.complex128, order="F")
         check(fn(_dp(out)))
+        return out
+
+    def observables(self) -> dict:
+        """vca_get_dens / _dens_up / _dens_dw / _docc / _mag: (Nlat, Norb) arrays."""
+        out = {}
+        for key in ("dens", "dens_up", "dens_dw", "docc", "mag"):
+            a = np.zeros((self.cfg.Nlat, self.cfg.Norb), order="F")
+            check(getattr(self.L, "vca_gpu_get_" + key)(_dp(a)))
+            out[key] = a
         return out
 
     def sigma_matsubara(self) -> np.ndarray:
