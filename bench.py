@@ -306,16 +306,54 @@ def run_gpu(args):
     }
     if roof is not None:
         out["roofline"] = roof
+    if rank == 0:
+        # single-vector H x v on the half-filled 4x4 sector (the largest
+        # sector of the 4x4 cluster), the vector size the roofline target
+        # of this path is stated for; measured after the solves (it replaces
+        # the library context)
+        s.close()
+        out["hxv_single_4x4"] = hxv_single_4x4()
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample, _ = cpu_sample(pts[0], os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                                "sample": sample}
     if rank == 0:
         print(json.dumps(out))
-    s.close()
+    else:
+        s.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def hxv_single_4x4(reps: int = 10) -> dict:
+    """One H x v of a unit vector on sector (8,8) of the 4x4 Hubbard cluster
+    (D = 12870^2 = 165,636,900), CUDA events on the library stream;
+    algorithmic bytes 16*D (read v, write Hv)."""
+    import torch
+    from vca_gb300 import clusters
+    from vca_gb300.solver import VcaSolver
+    pt = clusters.square(nx=4, ny=4, U=8.0, xmu=4.0, maf=0.0, nspin=1, nkx=4, nky=4, ngfiter=10,
+                         omega_nodes=64)
+    s4 = VcaSolver(pt.cfg)
+    s4.set_hamiltonian(pt.Hloc)
+    isec = 1 + 8 + 8 * 17
+    _, _, du, dd = s4.sector_info(isec)
+    D = du * dd
+    fx, F, _ = s4.arith_info()
+    x = torch.randn(D, dtype=torch.float64, device="cuda")
+    x /= torch.linalg.vector_norm(x)
+    if fx:
+        x = torch.round(x * 2.0 ** F).to(torch.int64)
+    y = torch.empty_like(x)
+    ms = s4.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, 1, reps)
+    peak, kind = measured_peaks()
+    gbs = 16.0 * D / (ms / 1e3) / 1e9
+    del x, y
+    s4.close()
+    return {"sector": [8, 8], "D": D, "arith": "fx" if fx else "f64", "launch_ms": round(ms, 4),
+            "kernels": "k_hxv1_up + k_hxv1_dw", "achieved_GBps": round(gbs, 1), "peak": peak,
+            "frac": round(gbs / peak, 4), "peak_kind": kind}
 
 
 def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
@@ -372,6 +410,8 @@ def main():
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling mode: one plain solve of a reduced 4x3 point "
                          "(8x8 k-grid, 1024 nodes) after one warm-up solve")
+    ap.add_argument("--profile-hxv1", action="store_true",
+                    help="profiling mode: single-vector H x v on sector (8,8) of the 4x4 cluster")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--hxv-variant", type=int, default=2,
                     help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
@@ -380,6 +420,11 @@ def main():
         return profile_hxv(args.profile_hxv, args.reps, args.hxv_variant)
     if args.profile_solve:
         return profile_solve()
+    if args.profile_hxv1:
+        from vca_gb300 import build as vbuild
+        vbuild.build()
+        print(json.dumps(hxv_single_4x4(args.reps)))
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

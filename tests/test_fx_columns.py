@@ -117,3 +117,32 @@ def test_position_ordered_form_matches_staged_form(m):
     Ys, _, _ = _apply(pt, 0, isec, X, m)
     Yr, _, _ = _apply(pt, 2, isec, X[order], m)
     np.testing.assert_array_equal(Yr, Ys[order])
+
+
+def test_single_vector_large_sector_matches_oracle():
+    """One vector of a large sector (2x7 cluster, sector (7,7), D = 11.8M:
+    the two-kernel staged single-vector form with two L2 row chunks) against
+    the oracle's FP64 H x v of the same fixed-point input (the form rounds
+    its up and down halves separately: 1e-13 of the vector scale)."""
+    import torch
+    pt = clusters.square(nx=7, ny=2, U=8.0, xmu=4.0, maf=0.0, nspin=1, nkx=2, nky=2, ngfiter=10,
+                         omega_nodes=16)
+    s = VcaSolver(pt.cfg)
+    s.set_hamiltonian(pt.Hloc)
+    isec = 1 + 7 + 7 * 15
+    _, _, du, dd = s.sector_info(isec)
+    assert du == dd == 3432
+    fx, F, G = s.arith_info()
+    assert fx
+    D = du * dd
+    x = np.random.default_rng(5).normal(size=D)
+    x /= np.linalg.norm(x)
+    X = np.rint(x * 2.0 ** F).astype(np.int64)
+    dX = torch.from_numpy(X).cuda()
+    dY = torch.zeros_like(dX)
+    s.hxv_timed(isec, dX.data_ptr(), dY.data_ptr(), 0, 1, 1)
+    torch.cuda.synchronize()
+    got = dY.cpu().numpy().astype(np.float64) * 2.0 ** -G
+    o = Oracle.from_point(pt)
+    ref = o.hxv(isec, X.astype(np.float64) * 2.0 ** -F).real
+    assert np.abs(got - ref).max() / max(1.0, np.abs(ref).max()) < 1e-13

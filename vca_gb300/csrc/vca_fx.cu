@@ -152,7 +152,138 @@ __global__ void k_hxv_fx(SectorView sv, FxView fv, int m, const i64* __restrict_
 }
 
 
+// Single-vector H x v for large sectors, in two kernels.
+// Up part (+ diagonal): one CTA per down configuration idw stages its
+// column X[:, idw] (DimUp contiguous int64) in shared memory; every up hop
+// is a shared-memory read.  Y = round((d x + sum_k a_k S_k^up) 2^-shift).
+template <int K>
+__global__ void __launch_bounds__(1024, 2) k_hxv1_up(SectorView sv, FxView fv, const i64* __restrict__ X,
+                                                 i64* __restrict__ Y) {
+  extern __shared__ __align__(16) i64 x1s[];
+  const int DU = sv.dimup;
+  const int idw = blockIdx.x;
+  const int64_t base = (int64_t)idw * DU;
+  for (int t = threadIdx.x; t < DU; t += blockDim.x) x1s[t] = (i64)__ldcg((const long long*)X + base + t);
+  __syncthreads();
+  const i64 e1d = fv.dw_e1[idw];
+  const unsigned wdw = (unsigned)sv.dw_words[idw];
+  for (int iup = threadIdx.x; iup < DU; iup += blockDim.x) {
+    u64 S[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) S[k] = 0;
+    const int nu = sv.up_cnt[iup], np = fv.up_npos[iup];
+    int h = 0, o = iup;
+    for (; h < np; h++, o += DU) {
+      const unsigned hw = fv.up_hop[o];
+      const i64 v = x1s[hw & 0xFFFFFFu];
+      const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) S[k] += (u64)v;
+    }
+    for (; h < nu; h++, o += DU) {
+      const unsigned hw = fv.up_hop[o];
+      const i64 v = x1s[hw & 0xFFFFFFu];
+      const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) S[k] -= (u64)v;
+    }
+    const i64 dfx = fv.up_e1[iup] + e1d + mixed_fx(fv, (unsigned)sv.up_words[iup], wdw);
+    i128 p = (i128)dfx * x1s[iup];
+#pragma unroll
+    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * (i64)S[k];
+    __stcg((long long*)Y + base + iup, (long long)rshift_round(p, fv.shift));
+  }
+}
+
+// Down part: Y[chunk, idw] += round(sum_k a_k S_k^dw 2^-shift), S^dw the
+// signed sum of rows `chunk` of the neighbour columns X[:, idw'] (the hop
+// list of idw, the same for every row).  CTAs are ordered chunk-major, so
+// the rows of one chunk of every column (chunk * DimDw * 8 bytes, <= 64 MB)
+// stay in L2 while the CTAs of that chunk run; every row read is a
+// coalesced stream.
+#define FX1_CHUNK_BYTES (64u << 20)
+template <int K>
+__global__ void __launch_bounds__(256) k_hxv1_dw(SectorView sv, FxView fv, int chunk_rows,
+                                                 const i64* __restrict__ X, i64* __restrict__ Y) {
+  extern __shared__ __align__(16) unsigned char x1d_smem[];
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int ck = blockIdx.x / DD;
+  const int idw = blockIdx.x - ck * DD;
+  int64_t* doff = (int64_t*)x1d_smem;
+  unsigned char* dcl = (unsigned char*)(doff + sv.wdw);
+  const int nd = sv.dw_cnt[idw], ndp = fv.dw_npos[idw];
+  for (int h = threadIdx.x; h < nd; h += blockDim.x) {
+    const unsigned hw = fv.dw_hop[idw + h * DD];
+    doff[h] = ((int64_t)(hw & 0xFFFFFFu) - idw) * DU;
+    dcl[h] = (unsigned char)((hw >> 24) & 3u);
+  }
+  __syncthreads();
+  const int64_t base = (int64_t)idw * DU;
+  const int r0 = ck * chunk_rows, r1 = min(DU, r0 + chunk_rows);
+  const long long* Xb = (const long long*)X + base;
+  for (int iup = r0 + threadIdx.x; iup < r1; iup += blockDim.x) {
+    u64 S[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) S[k] = 0;
+    int h = 0;
+#pragma unroll 4
+    for (; h < ndp; h++) {
+      const i64 v = (i64)__ldcg(Xb + iup + doff[h]);
+      const int cls = (K == 1) ? 0 : (int)dcl[h];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) S[k] += (u64)v;
+    }
+#pragma unroll 4
+    for (; h < nd; h++) {
+      const i64 v = (i64)__ldcg(Xb + iup + doff[h]);
+      const int cls = (K == 1) ? 0 : (int)dcl[h];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) S[k] -= (u64)v;
+    }
+    i128 p = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) p += (i128)fv.afx[k] * (i64)S[k];
+    long long* yo = (long long*)Y + base + iup;
+    __stcg(yo, (long long)((i64)__ldcg(yo) + rshift_round(p, fv.shift)));
+  }
+}
+
+#define FX1_MIN_DIM (1 << 22)
+static bool hxv1_ok(const SectorView& sv, const FxView& fv, int m) {
+  return m == 1 && fv.up_npos && fv.dw_npos && (int64_t)sv.dimup * sv.dimdw >= FX1_MIN_DIM &&
+         (size_t)sv.dimup * sizeof(i64) <= 200 * 1024;
+}
+
+template <int K>
+static void launch_hxv1_k(const SectorView& sv, const FxView& fv, const i64* X, i64* Y, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_hxv1_up<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  count_launch_external();
+  count_launch_external();
+  k_hxv1_up<K><<<sv.dimdw, 1024, (size_t)sv.dimup * sizeof(i64), st>>>(sv, fv, X, Y);
+  int rows = (int)std::max<int64_t>(256, FX1_CHUNK_BYTES / ((int64_t)sv.dimdw * sizeof(i64)));
+  rows = std::min(rows, sv.dimup);
+  const int nck = (sv.dimup + rows - 1) / rows;
+  k_hxv1_dw<K><<<nck * sv.dimdw, 256, (size_t)sv.wdw * 9 + 16, st>>>(sv, fv, rows, X, Y);
+}
+
 void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st) {
+  if (hxv1_ok(sv, fv, m)) {  // one vector of a large sector: the two-kernel staged form
+    switch (fv.K) {
+      case 1: launch_hxv1_k<1>(sv, fv, X, Y, st); break;
+      case 2: launch_hxv1_k<2>(sv, fv, X, Y, st); break;
+      case 3: launch_hxv1_k<3>(sv, fv, X, Y, st); break;
+      default: launch_hxv1_k<4>(sv, fv, X, Y, st); break;
+    }
+    return;
+  }
   count_launch_external();
   dim3 blk;
   int ns;
