@@ -53,10 +53,10 @@ extern "C" {
 /*
  * Input variables.  Field names, meanings and defaults follow
  * VCA_INPUT_VARS.f90:14-81 / :112-172.  Integers are 32-bit, logicals are
- * 0/1.  Fields after `verbose` have no counterpart in the reference: they fix
- * what the reference leaves to SciFortran defaults (Lanczos stopping rule,
- * start vector) or replaces (the adaptive QUADPACK integral becomes a fixed
- * Gauss-Legendre rule).
+ * 0/1.  Fields from `omega_nodes` to `hxv_variant`, and `contour_nodes`, have
+ * no counterpart in the reference: they fix what the reference leaves to
+ * SciFortran defaults (Lanczos stopping rule, start vector) or replaces (the
+ * adaptive QUADPACK integrals become fixed Gauss-Legendre rules).
  */
 typedef struct vca_config {
   int32_t Norb;      /* NORB       orbitals per cluster site (<= 5)          */
@@ -99,11 +99,21 @@ typedef struct vca_config {
   double omega_scale;      /* map w = omega_scale * s/(1-s), s in (0,1)     */
   double gs_residual_tol;  /* GS stop: |beta_{k+1} s_k| <= tol*max(1,|E|)   */
   double gf_beta_tol;      /* GF chain stop: beta_{k+1} < tol (exhausted)   */
+                           /* (the ground-state search uses gs_beta_tol)     */
   uint64_t start_seed;     /* seed of the deterministic Lanczos start vector */
   int32_t arith;           /* VCA_ARITH_AUTO | VCA_ARITH_FP64 | VCA_ARITH_FX   */
   int32_t hxv_variant;     /* FX column H x v of the hxv entry points: 0 auto, */
                            /* 1 warp form only, 2 rows in hop-count order     */
-  int32_t reserved[6];
+  /* ---- finite temperature (LANC_NSTATES_TOTAL > 1) ---------------------- */
+  int32_t lanc_nstates_step;   /* LANC_NSTATES_STEP   list growth per sweep   */
+  int32_t lanc_niter_spectrum; /* LANC_NITER_SPECTRUM annealing sweeps        */
+  int32_t contour_nodes;   /* Gauss-Legendre nodes per panel of the contour  */
+                           /* rule replacing quad(integral_contour, 0, pi)   */
+  int32_t pad1;
+  double cutoff;           /* CUTOFF     spectrum cut-off exp(-beta dE)      */
+  double bandwidth;        /* bandwidth  lattice bandwidth (a module variable */
+                           /* the reference's drivers assign, default 0)     */
+  double gs_beta_tol;      /* ground-state Lanczos: beta_{k+1} < tol ends it */
 } vca_config;
 
 /* Fill *cfg with the reference defaults (VCA_INPUT_VARS.f90:112-172) plus
@@ -121,13 +131,20 @@ void vca_config_defaults(vca_config* cfg);
 int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath_v);
 
 /*
- * vca_solve replacement (VCA_MAIN.f90:124-215), T=0 path.
+ * vca_solve replacement (VCA_MAIN.f90:124-215).
  *   Hloc  (Nlat,Nlat,Nspin,Nspin,Norb,Norb)        complex, read-only
  *   Hk    (Nlat,Nlat,Nspin,Nspin,Norb,Norb,Nk)     complex, read-only
  *   bath_h/bath_v as in vca_gpu_init (NULL when the model has no bath)
- *   omega_out  receives the SFT grand potential E_gs - Omega_int (may be NULL)
+ *   omega_out  receives the SFT grand potential Omega' - Omega_int (may be NULL)
  * Diagonalises every sector, builds the cluster Green's function chains and
- * integrates the Potthoff functional on the imaginary axis.
+ * integrates the Potthoff functional.  T=0 (LANC_NSTATES_TOTAL = 1):
+ * Omega' = E_gs and the integral runs on the imaginary axis.  Finite T: the
+ * lowest state of every sector enters an annealed, capped state list
+ * (VCA_DIAG.f90:78-256, :395-471), the chains carry Boltzmann weights,
+ * Omega' = E_min - T ln sum_i exp(-beta (E_i - E_min)) and the integral is a
+ * Matsubara sum plus a contour integral (VCA_OMEGA.f90:153-204).  The list
+ * size LANC_NSTATES_TOTAL adapts from solve to solve, as the reference's
+ * module variable does; vca_gpu_init resets it.
  */
 int vca_gpu_solve(const double* Hloc, const double* Hk, int64_t Nk,
                   const double* bath_h, const double* bath_v, double* omega_out);
@@ -179,8 +196,8 @@ int vca_gpu_get_g0_matsubara(double* g0_out);
 int vca_gpu_get_g0_realaxis(double* g0_out);
 /* Ground-state observables of the last solve, (Nlat,Norb) column-major:
  * density n_up + n_dw, its spin parts, double occupancy n_up n_dw and
- * magnetisation n_up - n_dw, averaged over the kept ground states with
- * weight 1/zeta.  Replace vca_get_dens / vca_get_docc / vca_get_mag
+ * magnetisation n_up - n_dw, averaged over the kept states with weight
+ * 1/zeta (T=0) or exp(-beta (E_i - E_min))/zeta (finite T).  Replace vca_get_dens / vca_get_docc / vca_get_mag
  * (VCA_IO/get_dens.f90, get_docc.f90, get_mag.f90), filled by
  * vca_lanc_observables (VCA_OBSERVABLES.f90:185-316). */
 int vca_gpu_get_dens(double* out);
@@ -190,9 +207,10 @@ int vca_gpu_get_docc(double* out);
 int vca_gpu_get_mag(double* out);
 
 /*
- * Ground-state bookkeeping of the last solve (VCA_DIAG.f90:224-236,
- * VCA_EIGENSPACE.f90:136-216): number of retained T=0 states, and per state
- * its sector (1-based, as get_Sector) and energy.
+ * State list of the last solve (VCA_DIAG.f90:220-236, VCA_EIGENSPACE.f90:
+ * 136-312): number of retained states (the T=0 ground states, or the trimmed
+ * finite-T list), and per state, in list order (ascending energy), its
+ * sector (1-based, as get_Sector) and energy.
  */
 int vca_gpu_get_state_count(int32_t* nstates);
 int vca_gpu_get_state(int32_t istate, int32_t* isector, double* energy);
@@ -204,8 +222,11 @@ int vca_gpu_get_sector_energies(double* e_out, int32_t n);
  * Pole/weight table of one Green's function element, the GFmatrix of
  * VCA_VARS_GLOBAL.f90:54-71 filled by VCA_GF_NORMAL.f90:970-1033:
  * element (ilat,jlat,ispin,iorb,jorb) 1-based, state istate, channel ichan.
- * *nexc receives the number of excitations; poles and weights (complex,
- * capacity cap) receive them when cap >= *nexc.
+ * *nexc receives the number of excitations, min(target dimension,
+ * LANC_NGFITER) as the reference allocates it: a chain that stopped early
+ * also lists the eigenvalues 0 of its zero-padded coefficients (poles
+ * isign*(0 - E_i), weight 0).  poles and weights (complex, capacity cap)
+ * receive them when cap >= *nexc.
  */
 int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t iorb,
                            int32_t jorb, int32_t istate, int32_t ichan, int32_t* nexc,
@@ -214,6 +235,28 @@ int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t io
 /* Omega integrand f(w) = (1/Lk) sum_k ln|det(1+(Delta+Hloc-Hk)G'(iw))|
  * (VCA_OMEGA.f90:37-75) at nw real frequencies, from the last solve. */
 int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out);
+/* Complex integrand F(z) = (1/Lk) sum_k log det(1+(Delta+Hloc-Hk)G'(z)),
+ * principal branch per k (sum_kmesh_complex, VCA_OMEGA.f90:78-114), at nz
+ * complex points z (interleaved re, im); f_out complex[nz]. */
+int vca_gpu_sum_kmesh_complex(const double* z, int64_t nz, double* f_out);
+
+/* Thermal bookkeeping of the last solve. */
+typedef struct vca_thermal {
+  double zeta;           /* zeta_function (VCA_DIAG.f90:357-363), before trimming */
+  double omega_prime;    /* Omega' of the cluster (VCA_MAIN.f90:186-193)       */
+  double e_min;          /* state_list%emin                                    */
+  double max_exc;        /* largest pole excitation of all chains (VCA_GF_NORMAL.f90:1018) */
+  double integration_R;  /* radius of the contour (VCA_OMEGA.f90:158-166)      */
+  double sum_part;       /* 2/beta sum_{n=0..nmax} Re F(i w_n)                 */
+  double contour_part;   /* integral over the contour                          */
+  int32_t nmax;          /* last Matsubara index of the sum                    */
+  int32_t nstates_total; /* LANC_NSTATES_TOTAL after this solve's adjustment  */
+  int32_t contour_points;/* nodes of the contour rule                          */
+  int32_t finite_t;      /* 1 when the solve ran the finite-T path             */
+} vca_thermal;
+/* At T=0: zeta = number of kept states, omega_prime = e_min = E_gs and the
+ * Omega fields after e_min are 0. */
+int vca_gpu_get_thermal(vca_thermal* out);
 
 /* Release every device buffer and the stream. */
 int vca_gpu_finalize(void);

@@ -70,6 +70,11 @@ def lib():
             "orc_gauss_legendre01": (I, [I, dp, dp]),
             "orc_frequency_integration": (D, [P]),
             "orc_solve": (D, [P, dp, dp]),
+            "orc_sum_kmesh_complex": (D, [P, D, D, dp]),
+            "orc_contour_rule": (I, [D, D, D, I, dp, dp, I]),
+            "orc_contour_integrand": (D, [P, D, D]),
+            "orc_frequency_integration_finite_t": (D, [P]),
+            "orc_thermal": (I, [P, dp, ip]),
             "orc_set_threads": (I, [I]),
         }
         for name, (res, args) in sig.items():
@@ -97,6 +102,15 @@ def gauss_legendre01(n: int):
     w = np.zeros(n)
     lib().orc_gauss_legendre01(n, _dp(x), _dp(w))
     return x, w
+
+
+def contour_rule(R: float, beta: float, mu: float, ngl: int):
+    """Nodes and weights of the fixed rule on the contour angle [0, pi]."""
+    n = lib().orc_contour_rule(R, beta, mu, ngl, None, None, 0)
+    th = np.zeros(n)
+    w = np.zeros(n)
+    lib().orc_contour_rule(R, beta, mu, ngl, _dp(th), _dp(w), n)
+    return th, w
 
 
 def tql2(d, e):
@@ -288,6 +302,40 @@ class Oracle:
 
     def frequency_integration(self) -> float:
         return self.L.orc_frequency_integration(self.h)
+
+    def sum_kmesh_complex(self, z: complex) -> complex:
+        im = ctypes.c_double()
+        re = self.L.orc_sum_kmesh_complex(self.h, float(np.real(z)), float(np.imag(z)), ctypes.byref(im))
+        return complex(re, im.value)
+
+    def contour_integrand(self, R: float, theta: float) -> float:
+        return self.L.orc_contour_integrand(self.h, float(R), float(theta))
+
+    def frequency_integration_finite_t(self) -> float:
+        return self.L.orc_frequency_integration_finite_t(self.h)
+
+    def thermal(self) -> dict:
+        """The fields of vca_thermal for the last solve."""
+        d = np.zeros(7)
+        i = np.zeros(4, dtype=np.int32)
+        self.L.orc_thermal(self.h, _dp(d), i.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        keys = ("zeta", "omega_prime", "e_min", "max_exc", "integration_R", "sum_part", "contour_part")
+        out = dict(zip(keys, d.tolist()))
+        out.update(nmax=int(i[0]), nstates_total=int(i[1]), contour_points=int(i[2]), finite_t=int(i[3]))
+        return out
+
+    def states(self):
+        """[(sector, energy)] of the retained state list, in list order."""
+        out = []
+        k = 0
+        while True:
+            isec = ctypes.c_int()
+            e = ctypes.c_double()
+            if self.L.orc_state(self.h, k, ctypes.byref(isec), ctypes.byref(e), None) != 0:
+                break
+            out.append((isec.value, e.value))
+            k += 1
+        return out
 
     def solve(self):
         egs = ctypes.c_double()

@@ -1,5 +1,6 @@
 // vca_oracle.cpp -- CPU restatement of the QcmPlab/VCA cluster-ED ->
-// Lanczos Green's function -> Potthoff Omega path, T = 0.
+// Lanczos Green's function -> Potthoff Omega path, at T = 0 and at finite T
+// (LANC_METHOD="lanczos": one state per sector).
 //
 // TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
 // entry and the CPU-baseline leg of the benchmark load it; the product path
@@ -19,6 +20,7 @@
 //
 // Build: make -C oracle   ->  oracle/liboracle.so   (g++ -O2 -fopenmp)
 
+#include <cfloat>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -46,6 +48,7 @@ struct Chain {            // one GF channel of one state: GFspectrum
   std::vector<cd> weight;  // VCA_VARS_GLOBAL.f90:61-63
   std::vector<cd> poles;
   std::vector<double> alpha, beta;  // Lanczos coefficients (diagnostics)
+  double maxde = -INFINITY;         // largest excitation diag(j) - Ei
 };
 
 struct State {            // sparse_estate (VCA_EIGENSPACE.f90:7-21)
@@ -63,10 +66,17 @@ struct Oracle {
   bool has_bath = false;
   std::vector<cd> bath_h;  // (Nlb,Nlb,Nspin,Nspin,Nob,Nob), after vca_set_bath
   std::vector<cd> bath_v;  // (Nlat,Nlb,Nspin,Nspin,Norb,Nob)
+  // finite temperature (VCA_SETUP.f90:157-175): LANC_NSTATES_TOTAL is a
+  // module variable every finite-T diagonalisation adjusts (VCA_DIAG.f90:
+  // 434,448); it carries over to the next solve
+  bool finiteT = false;
+  int nstates_total = 1;
   // results
   std::vector<double> sector_e;
   std::vector<State> states;
   double egs = 0, zeta = 0;
+  double max_exc = 0, omega_prime = 0, R = 0, sum_part = 0, contour_part = 0;
+  int nmax = 0, contour_points = 0;
   // impGmatrix(ilat,jlat,ispin,ispin,iorb,jorb)%state(istate)%channel(ichan)
   std::vector<std::vector<std::vector<Chain>>> gmat;  // [elem][state][chan]
   bool gf_built = false;
@@ -650,7 +660,7 @@ double lanczos_gs(const Oracle& o, const SectorH& s, std::vector<cd>& psi, int* 
     double bk1 = vnorm(w);
     a.push_back(ak);
     b.push_back(bk1);
-    bool exhausted = bk1 <= c.gf_beta_tol;
+    bool exhausted = bk1 <= c.gs_beta_tol;
     if (exhausted || k % c.gs_check_every == 0 || k == nmax) {
       theta = tri_lowest(a.data(), b.data(), k);
       tri_vector(a.data(), b.data(), k, theta, svec);
@@ -710,31 +720,114 @@ void lanczos_tridiag(const SectorH& s, const std::vector<cd>& v1, int nlanc, dou
 // ---------------------------------------------------------------------------
 // VCA_DIAG.f90 vca_diag_c, T=0, LANC_METHOD="lanczos" (Neigen = 1).
 // ---------------------------------------------------------------------------
+// Lowest eigenpair of one sector: Lanczos, or dense eigh below
+// LANC_DIM_THRESHOLD (VCA_DIAG.f90:93-96,126-196 with Neigen = 1).
+double lowest_pair(const Oracle& o, int isector, std::vector<cd>& vec) {
+  const vca_config& c = o.cfg;
+  SectorH s = build_sector_h(o, isector);
+  const int64_t D = s.dim;
+  bool lanc_solve = true;
+  if (D == 1) lanc_solve = false;  // Neigen == dim
+  if (D <= std::max(c.lanc_dim_threshold, 1)) lanc_solve = false;
+  double e;
+  if (lanc_solve) {
+    e = lanczos_gs(o, s, vec, nullptr);
+  } else {  // dense eigh(jobz='V') (VCA_DIAG.f90:191-196)
+    std::vector<cd> H = dense_h(s), Z;
+    std::vector<double> w;
+    jacobi_eigh((int)D, H, w, Z);
+    e = w[0];
+    vec.assign(Z.begin(), Z.begin() + D);
+    if (D == 1) vec[0] = 1.0;
+  }
+  return e;
+}
+
+// Finite T (VCA_DIAG.f90:78-256 and vca_post_diag :357-363,:395-451) with
+// one state per sector: the annealing sweeps re-add every sector's lowest
+// state to a list capped at LANC_NSTATES_TOTAL (es_add_state_c with size,
+// VCA_EIGENSPACE.f90:136-159), test exp(-beta(emax-emin)) < cutoff, then
+// vca_post_diag computes zeta over the whole list, and either grows the cap
+// or trims the states beyond the cut-off and resets the cap.  Every sweep
+// finds the same eigenpairs, so they are computed once.
+void diagonalize_finite_t(Oracle& o, const std::vector<int>* mask) {
+  const vca_config& c = o.cfg;
+  const double beta = c.beta, cutoff = c.cutoff;
+  std::vector<State> all(o.Nsectors);
+  std::vector<int> scan;
+  for (int isector = 1; isector <= o.Nsectors; isector++)
+    if (!mask || (*mask)[isector - 1]) scan.push_back(isector);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t q = 0; q < (int64_t)scan.size(); q++) {
+    const int isector = scan[q];
+    State& st = all[isector - 1];
+    st.sector = isector;
+    st.e = lowest_pair(o, isector, st.vec);
+  }
+  for (int isector : scan) o.sector_e[isector - 1] = all[isector - 1].e;
+  // the list holds sector numbers in list order
+  std::vector<int> list;
+  double emin = DBL_MAX, emax = -DBL_MAX;
+  auto E = [&](size_t i) { return all[list[i] - 1].e; };
+  auto insert = [&](int isector) {  // es_insert_state_c (:167-216): before the first c%e >= e
+    const double e = all[isector - 1].e;
+    size_t pos = 0;
+    while (pos < list.size() && !(e <= E(pos))) pos++;
+    list.insert(list.begin() + pos, isector);
+    if (e > emax) emax = e;
+    if (e < emin) emin = e;
+  };
+  auto pop = [&]() {  // es_pop_state without n (:230-312): the last entry
+    list.pop_back();
+    if (!list.empty()) { emax = E(list.size() - 1); emin = E(0); }
+  };
+  bool converged = false;
+  int iter = 0;
+  double zeta = 0.0;
+  while (!converged && iter < c.lanc_niter_spectrum) {
+    iter++;
+    list.clear();  // es_free_espace (:107-125)
+    emin = DBL_MAX;
+    emax = -DBL_MAX;
+    for (int isector : scan) {
+      if ((int)list.size() < o.nstates_total) insert(isector);
+      else if (all[isector - 1].e < E(list.size() - 1)) { pop(); insert(isector); }
+    }
+    converged = std::exp(-beta * (emax - emin)) < cutoff;  // VCA_DIAG.f90:251-256
+    // vca_post_diag
+    zeta = 0.0;
+    for (size_t i = 0; i < list.size(); i++) zeta += std::exp(-beta * (E(i) - emin));
+    if (std::exp(-beta * (emax - emin)) > cutoff) {
+      o.nstates_total += c.lanc_nstates_step;
+    } else {
+      double Ei = E(list.size() - 1);
+      while (std::exp(-beta * (Ei - emin)) <= cutoff) {
+        pop();
+        Ei = E(list.size() - 1);
+      }
+      o.nstates_total = std::max((int)list.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
+    }
+  }
+  o.states.clear();
+  for (int isector : list) o.states.push_back(all[isector - 1]);
+  o.egs = emin;
+  o.zeta = zeta;
+}
+
 void diagonalize(Oracle& o, const std::vector<int>* mask) {
   const vca_config& c = o.cfg;
   o.sector_e.assign(o.Nsectors, INFINITY);
   o.states.clear();
+  if (o.finiteT) {
+    diagonalize_finite_t(o, mask);
+    return;
+  }
   double oldzero = 1000.0;
   const double thr = c.gs_threshold;
   for (int isector = 1; isector <= o.Nsectors; isector++) {
     if (mask && !(*mask)[isector - 1]) continue;
-    SectorH s = build_sector_h(o, isector);
-    const int64_t D = s.dim;
-    bool lanc_solve = true;
-    if (D == 1) lanc_solve = false;  // Neigen == dim
-    if (D <= std::max(c.lanc_dim_threshold, 1)) lanc_solve = false;
-    double e;
     std::vector<cd> vec;
-    if (lanc_solve) {
-      e = lanczos_gs(o, s, vec, nullptr);
-    } else {  // dense eigh(jobz='V') (VCA_DIAG.f90:191-196)
-      std::vector<cd> H = dense_h(s), Z;
-      std::vector<double> w;
-      jacobi_eigh((int)D, H, w, Z);
-      e = w[0];
-      vec.assign(Z.begin(), Z.begin() + D);
-      if (D == 1) vec[0] = 1.0;
-    }
+    const double e = lowest_pair(o, isector, vec);
     o.sector_e[isector - 1] = e;
     // T=0 ground-state bookkeeping (VCA_DIAG.f90:224-236)
     if (e < oldzero - 10.0 * thr) {
@@ -787,13 +880,17 @@ Chain make_chain(const Oracle& o, cd vnorm2, double Ei, const std::vector<double
   ch.alpha = al;
   ch.beta = bl;
   const int n = (int)al.size();
-  cd pesoBZ = vnorm2 / o.zeta;
+  const double Egs = o.egs, beta = o.cfg.beta;
+  cd pesoBZ = 0.0;  // VCA_GF_NORMAL.f90:987-993
+  if (o.finiteT && beta * (Ei - Egs) < 200) pesoBZ = vnorm2 * std::exp(-beta * (Ei - Egs)) / o.zeta;
+  else if (!o.finiteT) pesoBZ = vnorm2 / o.zeta;
   std::vector<double> d = al, e = bl, z0;
   tql2(n, d, e, z0, nullptr);
   ch.weight.resize(n);
   ch.poles.resize(n);
   for (int j = 0; j < n; j++) {
     double de = d[j] - Ei;
+    if (de > ch.maxde) ch.maxde = de;  // max_exc (:1018); al keeps the zeros past an early stop
     ch.weight[j] = pesoBZ * z0[j] * z0[j];
     ch.poles[j] = (double)isign * de;
   }
@@ -870,6 +967,11 @@ void build_gf(Oracle& o) {
     }
     o.gmat[e] = std::move(per_state);
   }
+  o.max_exc = -DBL_MAX;  // VCA_GF_NORMAL.f90:57
+  for (auto& el : o.gmat)
+    for (auto& stc : el)
+      for (auto& ch : stc)
+        if (ch.maxde > o.max_exc) o.max_exc = ch.maxde;
   o.gf_built = true;
 }
 
@@ -1039,7 +1141,9 @@ void observables(const Oracle& o, std::vector<double>& out) {
     const int64_t du = (int64_t)mu.size();
     for (size_t i = 0; i < st.vec.size(); i++) {
       const int64_t iup = (int64_t)i % du, idw = (int64_t)i / du;  // state2indices (VCA_SETUP.f90:491-502)
-      const double w = std::norm(st.vec[i]) / o.zeta;
+      // peso = exp(-beta(Ei-Egs))/zeta at finite T, 1/zeta at T=0 (:248-249)
+      const double peso = (o.finiteT ? std::exp(-o.cfg.beta * (st.e - o.egs)) : 1.0) / o.zeta;
+      const double w = peso * std::norm(st.vec[i]);
       for (int l = 0; l < nimp; l++) {
         const int a = (int)((mu[iup] >> l) & 1), b = (int)((md[idw] >> l) & 1);
         out[l] += a * w;
@@ -1177,6 +1281,145 @@ double frequency_integration(const Oracle& o) {
   return (3.0 - o.cfg.Nspin) * acc / M_PI;
 }
 
+// ---------------------------------------------------------------------------
+// Finite temperature Omega (VCA_OMEGA.f90:78-114, :153-204).
+// ---------------------------------------------------------------------------
+// log det(1 + A), principal branch (log(det(tmp_mat)), VCA_OMEGA.f90:108):
+// the real part as logabsdet_1pa, the imaginary part arg(det) in (-pi, pi].
+double wrap_pi(double x) {
+  double r = std::remainder(x, 2.0 * M_PI);
+  if (r <= -M_PI) r += 2.0 * M_PI;
+  return r;
+}
+cd logdet_1pa(int n, std::vector<cd> A) {
+  double nrm = 0.0;
+  for (int i = 0; i < n; i++) {
+    double r = 0.0;
+    for (int j = 0; j < n; j++) r += std::abs(A[i + (size_t)j * n]);
+    nrm = std::max(nrm, r);
+  }
+  if (nrm < 0.5) {
+    double acc = 0.0, ph = 0.0;
+    for (int k = 0; k < n; k++) {
+      cd akk = A[k + (size_t)k * n];
+      cd piv = 1.0 + akk;
+      acc += 0.5 * std::log1p(2.0 * akk.real() + std::norm(akk));
+      ph += std::arg(piv);
+      for (int i = k + 1; i < n; i++) {
+        cd l = A[i + (size_t)k * n] / piv;
+        if (l == 0.0) continue;
+        for (int j = k + 1; j < n; j++) A[i + (size_t)j * n] -= l * A[k + (size_t)j * n];
+      }
+    }
+    return cd(acc, wrap_pi(ph));
+  }
+  for (int i = 0; i < n; i++) A[i + (size_t)i * n] += 1.0;
+  return std::log(lu_det(n, A));
+}
+
+// sum_kmesh_complex (VCA_OMEGA.f90:78-114) at a complex z
+cd sum_kmesh_complex(const Oracle& o, cd z) {
+  const int N = o.Nlso;
+  std::vector<cd> gf, G, Dl, Hl;
+  gf_cluster(o, z, gf);
+  to_lso(o, gf.data(), G);
+  delta_bath(o, z, Dl);
+  to_lso(o, o.Hloc.data(), Hl);
+  const size_t nel = (size_t)o.cfg.Nlat * o.cfg.Nlat * o.cfg.Nspin * o.cfg.Nspin * o.cfg.Norb * o.cfg.Norb;
+  double re = 0.0, im = 0.0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+  for (int64_t ik = 0; ik < o.Nk; ik++) {
+    std::vector<cd> Hkl, M((size_t)N * N), T((size_t)N * N);
+    to_lso(o, o.Hk.data() + ik * nel, Hkl);
+    for (size_t q = 0; q < M.size(); q++) M[q] = Dl[q] + Hl[q] - Hkl[q];
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++) {
+        cd s = 0.0;
+        for (int k = 0; k < N; k++) s += M[i + (size_t)k * N] * G[k + (size_t)j * N];
+        T[i + (size_t)j * N] = s;
+      }
+    const cd l = logdet_1pa(N, T);
+    re += l.real();
+    im += l.imag();
+  }
+  return cd(re, im) / (double)o.Nk;
+}
+
+// Fixed rule replacing quad(integral_contour, a=0, b=pi, key=6)
+// (VCA_OMEGA.f90:172).  The integrand's only sharp feature is set by the
+// poles mu + i(2n+1)pi/beta of fermi(w - xmu) next to the arc |w| = R: the
+// rule is composite Gauss-Legendre (ngl nodes per panel) on panels graded
+// geometrically away from the angle of the nearest pole, the first panel as
+// wide (in angle) as that pole's distance from the arc over R, each next one
+// twice the previous up to pi/16.
+void contour_rule(double R, double beta, double mu, int ngl, std::vector<double>& th, std::vector<double>& wt) {
+  const double y0 = std::sqrt(std::max(R * R - mu * mu, 0.0));
+  const double nc = std::floor((y0 * beta / M_PI - 1.0) / 2.0);
+  double best = INFINITY, thp = 0.5 * M_PI;
+  for (int d = -1; d <= 2; d++) {
+    const double n = nc + d;
+    if (n < 0) continue;
+    const double y = (2.0 * n + 1.0) * M_PI / beta;
+    const double dist = std::fabs(std::hypot(mu, y) - R);
+    if (dist < best) { best = dist; thp = std::atan2(y, mu); }
+  }
+  const double h0 = std::max(best / R, 1e-15), hmax = M_PI / 16.0;
+  std::vector<double> edges{thp};
+  for (double b = thp, w = h0; b > 0.0; w = std::min(2.0 * w, hmax)) edges.push_back(b = std::max(b - w, 0.0));
+  for (double b = thp, w = h0; b < M_PI; w = std::min(2.0 * w, hmax)) edges.push_back(b = std::min(b + w, M_PI));
+  std::sort(edges.begin(), edges.end());
+  std::vector<double> s, ws;
+  gauss_legendre01(ngl, s, ws);
+  th.clear();
+  wt.clear();
+  for (size_t p = 0; p + 1 < edges.size(); p++) {
+    const double a = edges[p], h = edges[p + 1] - edges[p];
+    for (int i = 0; i < ngl; i++) {
+      th.push_back(a + h * s[i]);
+      wt.push_back(h * ws[i]);
+    }
+  }
+}
+
+// integral_contour (VCA_OMEGA.f90:186-199) at angle theta
+double contour_integrand(const Oracle& o, double R, double theta) {
+  const double beta = o.cfg.beta, mu = o.cfg.xmu;
+  const cd w = R * std::exp(XI * theta);
+  cd fermi = 0.0;
+  if (((w - mu) * beta).real() < 100.0) fermi = 1.0 / (std::exp(beta * (w - mu)) + 1.0);
+  return ((1.0 / M_PI) * w * fermi * sum_kmesh_complex(o, w)).real();
+}
+
+// frequency_integration_finite_t (VCA_OMEGA.f90:153-182)
+double frequency_integration_finite_t(Oracle& o) {
+  const vca_config& c = o.cfg;
+  const double beta = c.beta;
+  int nmax = (int)(2.0 * (std::fabs(o.max_exc) + c.bandwidth) * beta / M_PI);
+  nmax = (nmax % 2 == 0) ? nmax / 2 : (nmax + 1) / 2;
+  const double R = 2.0 * (nmax + 1) * M_PI / beta;
+  double out = 0.0;
+  for (int n = 0; n <= nmax; n++) out += sum_kmesh(o, (2.0 * n + 1.0) * M_PI / beta);
+  out = 2.0 * (1.0 / beta) * out;
+  std::vector<double> th, wt;
+  contour_rule(R, beta, c.xmu, c.contour_nodes, th, wt);
+  double integral = 0.0;
+  for (size_t i = 0; i < th.size(); i++) integral += wt[i] * contour_integrand(o, R, th[i]);
+  o.nmax = nmax;
+  o.R = R;
+  o.sum_part = out;
+  o.contour_part = integral;
+  o.contour_points = (int)th.size();
+  return (3.0 - c.Nspin) * (out + integral);
+}
+
+// Omega' (VCA_MAIN.f90:186-193)
+double omega_prime(const Oracle& o) {
+  if (!o.finiteT) return o.egs;
+  double z = 0.0;
+  for (const State& st : o.states) z += std::exp(-o.cfg.beta * (st.e - o.egs));
+  return o.egs - (1.0 / o.cfg.beta) * std::log(z);
+}
+
 void copy_c(const double* src, size_t n, std::vector<cd>& dst) {
   dst.resize(n);
   for (size_t i = 0; i < n; i++) dst[i] = cd(src[2 * i], src[2 * i + 1]);
@@ -1198,6 +1441,9 @@ void* orc_create(const vca_config* cfg, const double* Hloc, const double* Hk, in
   if (!o->has_bath) { c.Nlat_bath = 0; c.Norb_bath = 0; }  // VCA_MAIN.f90:64-66
   o->Ns = c.Nlat * c.Norb + c.Nlat_bath * c.Norb_bath;       // VCA_SETUP.f90:82
   o->Nsectors = (o->Ns + 1) * (o->Ns + 1);                   // VCA_SETUP.f90:93
+  o->finiteT = (c.lanc_nstates_total != 1);                  // VCA_SETUP.f90:157-162
+  o->nstates_total = c.lanc_nstates_total;
+  if (o->finiteT && o->nstates_total % 2 != 0) o->nstates_total++;  // :172-175
   o->Nlso = c.Nlat * c.Nspin * c.Norb;
   const size_t nel = (size_t)c.Nlat * c.Nlat * c.Nspin * c.Nspin * c.Norb * c.Norb;
   copy_c(Hloc, nel, o->Hloc);
@@ -1395,13 +1641,40 @@ int orc_gauss_legendre01(int n, double* x, double* w) {
 }
 double orc_frequency_integration(void* h) { return frequency_integration(*(Oracle*)h); }
 
-// Full T=0 vca_solve (VCA_MAIN.f90:124-215): returns the SFT potential.
+double orc_sum_kmesh_complex(void* h, double zr, double zi, double* im_out) {
+  const cd f = sum_kmesh_complex(*(Oracle*)h, cd(zr, zi));
+  if (im_out) *im_out = f.imag();
+  return f.real();
+}
+int orc_contour_rule(double R, double beta, double mu, int ngl, double* th, double* w, int cap) {
+  std::vector<double> t, ww;
+  contour_rule(R, beta, mu, ngl, t, ww);
+  for (int i = 0; i < (int)t.size() && i < cap; i++) { th[i] = t[i]; w[i] = ww[i]; }
+  return (int)t.size();
+}
+double orc_contour_integrand(void* h, double R, double theta) { return contour_integrand(*(Oracle*)h, R, theta); }
+double orc_frequency_integration_finite_t(void* h) { return frequency_integration_finite_t(*(Oracle*)h); }
+// zeta, omega_prime, e_min, max_exc, R, sum part, contour part; nmax,
+// nstates_total, contour points, finite_t (the fields of vca_thermal)
+int orc_thermal(void* h, double* d7, int* i4) {
+  Oracle* o = (Oracle*)h;
+  const double d[7] = {o->zeta, omega_prime(*o), o->egs, o->max_exc, o->R, o->sum_part, o->contour_part};
+  for (int i = 0; i < 7; i++) d7[i] = d[i];
+  i4[0] = o->nmax;
+  i4[1] = o->nstates_total;
+  i4[2] = o->contour_points;
+  i4[3] = o->finiteT ? 1 : 0;
+  return 0;
+}
+
+// Full vca_solve (VCA_MAIN.f90:124-215): returns the SFT potential
+// Omega' - Omega_int; egs_out receives E_min (E_gs at T=0).
 double orc_solve(void* h, double* egs_out, double* omega_int_out) {
   Oracle* o = (Oracle*)h;
   diagonalize(*o, nullptr);
   build_gf(*o);
-  o->omega_int = frequency_integration(*o);
-  o->sft = o->egs - o->omega_int;
+  o->omega_int = o->finiteT ? frequency_integration_finite_t(*o) : frequency_integration(*o);
+  o->sft = omega_prime(*o) - o->omega_int;
   if (egs_out) *egs_out = o->egs;
   if (omega_int_out) *omega_int_out = o->omega_int;
   return o->sft;

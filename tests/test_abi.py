@@ -55,5 +55,9 @@ def test_init_without_gpu_reports_error(lib):
 def test_bad_config_rejected_on_host(lib):
     c = default_config(Nlat=2, Nspin=3)
     assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
-    c = default_config(Nlat=2, lanc_nstates_total=2)
+    c = default_config(Nlat=2, vca_twin=1)
     assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -6
+    c = default_config(Nlat=2, lanc_nstates_total=2, cutoff=0.0)
+    assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
+    c = default_config(Nlat=2, lanc_nstates_total=2, lanc_niter_spectrum=0)
+    assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1

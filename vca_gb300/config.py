@@ -2,10 +2,13 @@
 
 Field names, meanings and defaults follow ``VCA_INPUT_VARS.f90:14-81`` and the
 defaults set at ``VCA_INPUT_VARS.f90:112-172`` of QcmPlab/VCA.  The fields after
-``verbose`` have no counterpart in the reference; they pin down what the
-reference leaves to SciFortran (Lanczos stopping rule and start vector) or
-replaces (the adaptive QUADPACK integral of ``VCA_OMEGA.f90:132`` becomes a
-fixed Gauss-Legendre rule).  The layout must match ``include/vca_gpu.h``.
+``verbose`` up to ``hxv_variant``, and ``contour_nodes``, have no counterpart
+in the reference; they pin down what the reference leaves to SciFortran
+(Lanczos stopping rule and start vector) or replaces (the adaptive QUADPACK
+integrals of ``VCA_OMEGA.f90:132,172`` become fixed Gauss-Legendre rules).
+``bandwidth`` is a module variable the reference's drivers assign
+(``drivers/vca_hm_2dsquare.f90:72``).  The layout must match
+``include/vca_gpu.h``.
 """
 from __future__ import annotations
 
@@ -60,7 +63,13 @@ class VcaConfig(ctypes.Structure):
         ("start_seed", ctypes.c_uint64),
         ("arith", ctypes.c_int32),
         ("hxv_variant", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("lanc_nstates_step", ctypes.c_int32),
+        ("lanc_niter_spectrum", ctypes.c_int32),
+        ("contour_nodes", ctypes.c_int32),
+        ("pad1", ctypes.c_int32),
+        ("cutoff", ctypes.c_double),
+        ("bandwidth", ctypes.c_double),
+        ("gs_beta_tol", ctypes.c_double),
     ]
 
     def copy(self) -> "VcaConfig":
@@ -71,7 +80,7 @@ class VcaConfig(ctypes.Structure):
     def as_dict(self) -> dict:
         out = {}
         for name, _ in self._fields_:
-            if name in ("pad0", "reserved"):
+            if name in ("pad0", "pad1"):
                 continue
             v = getattr(self, name)
             out[name] = list(v) if name == "Uloc" else v
@@ -101,10 +110,14 @@ def default_config(**overrides) -> VcaConfig:
     c.gs_check_every = 10
     c.omega_scale = 1.0
     c.gs_residual_tol = 1e-11
-    c.gf_beta_tol = 1e-12
+    c.gf_beta_tol = 1e-6
+    c.gs_beta_tol = 1e-12
     c.start_seed = 20261203
     c.arith = ARITH_AUTO
     c.hxv_variant = 0
+    c.lanc_nstates_step, c.lanc_niter_spectrum = 2, 10
+    c.cutoff, c.bandwidth = 1e-9, 0.0
+    c.contour_nodes = 24
     for k, v in overrides.items():
         if k == "Uloc":
             for i in range(5):

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -80,6 +81,7 @@ struct ChainRec {
   int elem;   // spin-diagonal element index (il,jl,is,io,jo)
   int state;  // 0-based GS index
   int chan;   // 1..4 as the reference's channel numbers
+  int nlanc;  // steps asked for: min(target dimension, LANC_NGFITER)
 };
 
 struct Ctx {
@@ -124,11 +126,17 @@ struct Ctx {
   std::vector<PermTabs> fx_ptab[2];  // tables in perm order
   std::vector<HopPair> host_pairs;
   std::vector<double> host_eps_abs;  // per spin set: bound of |one-body energy|
+  // finite temperature (LANC_NSTATES_TOTAL != 1, VCA_SETUP.f90:157-175); the
+  // list cap is adjusted by every finite-T diagonalisation and carries over
+  bool finiteT = false;
+  int nstates_total = 1;
   // results
   bool solved = false;
   std::vector<double> sector_e;
   std::vector<GState> gs;
   double egs = 0, zeta = 0, omega_int = 0, sft = 0;
+  double omega_prime = 0, max_exc = 0, int_R = 0, sum_part = 0, contour_part = 0;
+  int nmax = 0, contour_points = 0;
   std::vector<ChainRec> chains;
   int ld = 0;
   double* d_poles = nullptr;     // filled on demand from the chain store
@@ -669,7 +677,7 @@ int sector_gs(int isector, double* E, void** vec_out, Arena& keep) {
   int mconv = 0;
   double th = 0.0;
   for (int k = 1; k <= nmax; k++) {
-    if ((rc = lanczos_step(sv, cb, bb, k, c.gf_beta_tol, nmax + 1))) { ar.release(); return rc; }
+    if ((rc = lanczos_step(sv, cb, bb, k, c.gs_beta_tol, nmax + 1))) { ar.release(); return rc; }
     if (k % std::max(1, c.gs_check_every) == 0 || k == nmax) {
       ChainMeta mh;
       double bn;
@@ -767,7 +775,7 @@ int sector_gs_fx(int isector, double* E, void** vec_out, Arena& keep) {
   int mconv = 0;
   double th = 0.0;
   for (int k = 1; k <= nmax; k++) {
-    if ((rc = lanczos_step_fx(sv, fv, cb, bb, k, c.gf_beta_tol, nmax + 1))) { ar.release(); return rc; }
+    if ((rc = lanczos_step_fx(sv, fv, cb, bb, k, c.gs_beta_tol, nmax + 1))) { ar.release(); return rc; }
     if (k % std::max(1, c.gs_check_every) == 0 || k == nmax) {
       ChainMeta mh;
       double bn;
@@ -891,7 +899,7 @@ int batched_sector_energies(std::vector<double>& energy) {
     MsGroup gp{d_secs, d_tsec, d_tstart, nsec, ntiles};
     ms_launch_start(gp, c.start_seed, g->fxs.F, b.YW, b.X, b.tpart, b.meta, b.mul, b.msh, g->st);
     for (int k = 1; k <= nmaxg; k++) {
-      ms_launch_step(gp, g->fxs, g->fxbase.K, k, c.gf_beta_tol, b, g->st);
+      ms_launch_step(gp, g->fxs, g->fxbase.K, k, c.gs_beta_tol, b, g->st);
       if (k % std::max(1, c.gs_check_every) == 0 || k == nmaxg) {
         cudaMemsetAsync(b.undone, 0, sizeof(int), g->st);
         ms_launch_check(gp, b, c.gs_residual_tol, g->st);
@@ -913,11 +921,89 @@ int batched_sector_energies(std::vector<double>& energy) {
 }
 
 // vca_diag_c at T=0 with LANC_METHOD="lanczos" (VCA_DIAG.f90:49-267)
+// Finite T, one state per sector (LANC_METHOD="lanczos", Neigen = 1): the
+// annealing sweeps of VCA_DIAG.f90:78-256 insert every sector's lowest state
+// into a list capped at LANC_NSTATES_TOTAL (es_add_state_c with size,
+// VCA_EIGENSPACE.f90:136-159: below the cap insert in energy order, else
+// replace the last entry when lower) and stop once exp(-beta(emax-emin)) <
+// cutoff; after each sweep vca_post_diag (VCA_DIAG.f90:357-363,:395-451)
+// sums zeta over the list, then grows the cap by LANC_NSTATES_STEP or trims
+// the entries past the cut-off and resets the cap to max(size,step)+step.
+// Every sweep finds the same sector energies, so one pass computes them and
+// the host replays the sweeps; eigenvectors are computed for the states left.
+int diagonalize_finite_t() {
+  const vca_config& c = g->cfg;
+  std::vector<double> E(g->Nsectors, INFINITY);
+  if (g->fx) {
+    RCHK(batched_sector_energies(E));
+  } else {
+    for (int isector = 1; isector <= g->Nsectors; isector++) {
+      Arena tmp;
+      void* vec = nullptr;
+      const int rc = sector_gs(isector, &E[isector - 1], &vec, tmp);
+      tmp.release();
+      if (rc) return rc;
+    }
+  }
+  g->sector_e = E;
+  struct Entry {
+    double e;
+    int sector;
+  };
+  std::vector<Entry> lst;
+  double lo = DBL_MAX, hi = -DBL_MAX;
+  auto put = [&](int isector) {
+    const double e = E[isector - 1];
+    auto at = std::find_if(lst.begin(), lst.end(), [&](const Entry& x) { return e <= x.e; });
+    lst.insert(at, Entry{e, isector});
+    if (e > hi) hi = e;
+    if (e < lo) lo = e;
+  };
+  auto drop = [&]() {
+    lst.pop_back();
+    if (!lst.empty()) { hi = lst.back().e; lo = lst.front().e; }
+  };
+  const double beta = c.beta;
+  double zeta = 0.0;
+  bool done = false;
+  for (int sweep = 0; !done && sweep < c.lanc_niter_spectrum; sweep++) {
+    lst.clear();
+    lo = DBL_MAX;
+    hi = -DBL_MAX;
+    for (int isector = 1; isector <= g->Nsectors; isector++) {
+      if ((int)lst.size() < g->nstates_total) put(isector);
+      else if (E[isector - 1] < lst.back().e) { drop(); put(isector); }
+    }
+    const double spread = std::exp(-beta * (hi - lo));
+    done = spread < c.cutoff;
+    zeta = 0.0;
+    for (const Entry& x : lst) zeta += std::exp(-beta * (x.e - lo));
+    if (spread > c.cutoff) {
+      g->nstates_total += c.lanc_nstates_step;
+    } else {
+      while (std::exp(-beta * (lst.back().e - lo)) <= c.cutoff) drop();
+      g->nstates_total = std::max((int)lst.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
+    }
+  }
+  for (const Entry& x : lst) {
+    double e;
+    void* vec = nullptr;
+    RCHK(g->fx ? sector_gs_fx(x.sector, &e, &vec, g->states) : sector_gs(x.sector, &e, &vec, g->states));
+    if (std::fabs(e - x.e) > 1e-12 * std::max(1.0, std::fabs(e)))
+      VFAIL(VCA_ERR_NUMERIC, "two Lanczos runs on the same sector disagree");
+    g->gs.push_back({x.sector, x.e, vec});
+  }
+  g->egs = lo;
+  g->zeta = zeta;
+  return VCA_OK;
+}
+
 int diagonalize() {
   const vca_config& c = g->cfg;
   g->states.release();
   g->gs.clear();
   g->sector_e.assign(g->Nsectors, INFINITY);
+  if (g->finiteT) return diagonalize_finite_t();
   double oldzero = 1000.0;
   const double thr = c.gs_threshold;
   // fixed-point path: every sector's energy from the batched search, then the
@@ -994,6 +1080,14 @@ struct ChainSpec {
   cd wfac;
   int ncol;
 };
+
+// Boltzmann factor of a state's chains (VCA_GF_NORMAL.f90:987-993): 1 at
+// T=0; exp(-beta(Ei-Egs)) at finite T, 0 once beta(Ei-Egs) >= 200
+double state_weight(const GState& S) {
+  if (!g->finiteT) return 1.0;
+  const double x = g->cfg.beta * (S.e - g->egs);
+  return x < 200.0 ? std::exp(-x) : 0.0;
+}
 
 int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs) {
   const vca_config& c = g->cfg;
@@ -1094,11 +1188,14 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     }
     // poles and weights into the global chain table
     const int base = (int)g->chains.size();
-    launch_chain_store(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, g->zeta, g->cstore, base,
-                       g->st);
+    launch_chain_store(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, state_weight(S), g->zeta,
+                       g->cstore, base, g->st);
     CUCHK(cudaGetLastError());
     CUCHK(cudaStreamSynchronize(g->st));
-    for (int q = 0; q < nch; q++) g->chains.push_back(specs[q0 + q].rec);
+    for (int q = 0; q < nch; q++) {
+      g->chains.push_back(specs[q0 + q].rec);
+      g->chains.back().nlanc = nlanc;
+    }
     ar.release();
     q0 = q1;
   }
@@ -1191,6 +1288,21 @@ int build_gf() {
   if (!flat.empty())
     CUCHK(cudaMemcpyAsync(g->d_elem_chain, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, g->st));
   CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+// Poles and weights of every chain from the chain store, once per solve
+int ensure_poles() {
+  if (g->poles_ready || g->chains.empty()) return VCA_OK;
+  Arena ar;
+  double* work;
+  const int nch = (int)g->chains.size();
+  RCHK(ar.alloc(&work, (size_t)nch * 3 * g->ld));
+  launch_chain_poles(nch, g->cstore, work, g->d_poles, g->d_weights, g->d_nexc, g->st);
+  cudaError_t err = cudaStreamSynchronize(g->st);
+  ar.release();
+  CUCHK(err);
+  g->poles_ready = true;
   return VCA_OK;
 }
 
@@ -1320,62 +1432,33 @@ bool omega_pairs_valid() {
   return true;
 }
 
-int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, double* f_eval) {
+// Omega integrand at n device points d_z (sum_kmesh / sum_kmesh_complex,
+// VCA_OMEGA.f90:37-114): on return *f_re[i] = (1/Nk) sum_k ln|det(1 + (Delta
+// + Hloc - Hk) G'(z_i))| and, when want_im, *f_im[i] = (1/Nk) sum_k arg det
+// (principal), both device arrays owned by ar.
+int ksum_device(int n, const double2* d_z, bool want_im, Arena& ar, double** f_re, double** f_im) {
   const vca_config& c = g->cfg;
-  Arena ar;
+  const int64_t Nk = g->Nk;
   const int N = g->N, NN = N * N;
   int rc = VCA_OK;
-  // nodes
-  int n;
-  double2* d_z;
-  double* d_W = nullptr;
-  if (f_eval) {
-    n = nz_eval;
-    std::vector<double2> zh(n);
-    for (int i = 0; i < n; i++) zh[i] = make_double2(0.0, w_eval[i]);
-    if ((rc = ar.alloc(&d_z, n))) { ar.release(); return rc; }
-    cudaMemcpyAsync(d_z, zh.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, g->st);
-  } else {
-    n = c.omega_nodes;
-    if (g->node_n != n || g->node_scale != c.omega_scale || !g->node_z) {
-      g->nodes.release();
-      g->node_n = 0;
-      double *s, *w;
-      if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = g->nodes.alloc(&g->node_z, n)) ||
-          (rc = g->nodes.alloc(&g->node_w, n))) {
-        ar.release();
-        return rc;
-      }
-      launch_gauss_legendre(n, s, w, g->st);
-      launch_omega_nodes(n, c.omega_scale, s, w, g->node_z, g->node_w, g->st);
-      g->node_n = n;
-      g->node_scale = c.omega_scale;
-    }
-    d_z = g->node_z;
-    d_W = g->node_w;
-  }
-  // G'(i w) in lso
   double2 *Glso, *P, *D = nullptr, *Hl;
-  if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = ar.alloc(&P, (size_t)n * NN)) ||
-      (rc = ar.alloc(&Hl, NN))) { ar.release(); return rc; }
-  if ((rc = gf_lso(n, d_z, Glso, ar))) { ar.release(); return rc; }
-  // Hloc in lso
-  {
+  if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = ar.alloc(&P, (size_t)n * NN)) || (rc = ar.alloc(&Hl, NN)))
+    return rc;
+  RCHK(gf_lso(n, d_z, Glso, ar));
+  {  // Hloc in lso
     double2* hraw;
-    if ((rc = ar.alloc(&hraw, NN))) { ar.release(); return rc; }
+    RCHK(ar.alloc(&hraw, NN));
     cudaMemcpyAsync(hraw, g->Hloc.data(), sizeof(double2) * NN, cudaMemcpyHostToDevice, g->st);
     launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, 1, hraw, Hl, g->st);
   }
-  if (g->has_bath) {  // Delta(i w)
+  if (g->has_bath) {  // Delta(z)
     std::vector<double2> hb, V;
     bath_lso(hb, V);
     double2 *dhb, *dV, *work;
     const int Nb = g->Nb;
     if ((rc = ar.alloc(&dhb, (size_t)Nb * Nb)) || (rc = ar.alloc(&dV, (size_t)N * Nb)) ||
-        (rc = ar.alloc(&work, (size_t)n * 2 * Nb * Nb)) || (rc = ar.alloc(&D, (size_t)n * NN))) {
-      ar.release();
+        (rc = ar.alloc(&work, (size_t)n * 2 * Nb * Nb)) || (rc = ar.alloc(&D, (size_t)n * NN)))
       return rc;
-    }
     cudaMemcpyAsync(dhb, hb.data(), sizeof(double2) * hb.size(), cudaMemcpyHostToDevice, g->st);
     cudaMemcpyAsync(dV, V.data(), sizeof(double2) * V.size(), cudaMemcpyHostToDevice, g->st);
     launch_delta_bath(n, d_z, N, Nb, dhb, dV, c.xmu, work, D, g->st);
@@ -1384,11 +1467,11 @@ int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, d
   const bool blk = g->hk_spin_diag && point_spin_diagonal();
   const int nblk = blk ? c.Nspin : 1;
   const int nb = N / nblk;
-  if (nb > 32) { ar.release(); VFAIL(VCA_ERR_UNSUPPORTED, "Omega k-sum supports spin blocks up to 32 orbitals"); }
-  int kchunks = (int)std::max<int64_t>(1, std::min<int64_t>(Nk, (152 * 8 + n - 1) / n));
-  double* fpart;
-  double* f;
-  if ((rc = ar.alloc(&fpart, (size_t)n * kchunks)) || (rc = ar.alloc(&f, n))) { ar.release(); return rc; }
+  if (nb > 32) VFAIL(VCA_ERR_UNSUPPORTED, "Omega k-sum supports spin blocks up to 32 orbitals");
+  const int kchunks = (int)std::max<int64_t>(1, std::min<int64_t>(Nk, (152 * 8 + n - 1) / n));
+  double *fpart, *fpart_im = nullptr;
+  if ((rc = ar.alloc(&fpart, (size_t)n * kchunks)) || (rc = ar.alloc(f_re, n))) return rc;
+  if (want_im && ((rc = ar.alloc(&fpart_im, (size_t)n * kchunks)) || (rc = ar.alloc(f_im, n)))) return rc;
   // union sparsity pattern of M = Delta + Hloc - Hk within each spin block
   std::vector<int> rowptr(N + 1, 0), cols;
   for (int a = 0; a < N; a++) {
@@ -1403,33 +1486,223 @@ int omega_integral(int64_t Nk, double* out, int nz_eval, const double* w_eval, d
     rowptr[a + 1] = (int)cols.size();
   }
   int *d_rowptr, *d_cols;
-  if ((rc = ar.alloc(&d_rowptr, N + 1)) || (rc = ar.alloc(&d_cols, std::max<size_t>(1, cols.size())))) {
-    ar.release();
-    return rc;
-  }
+  if ((rc = ar.alloc(&d_rowptr, N + 1)) || (rc = ar.alloc(&d_cols, std::max<size_t>(1, cols.size())))) return rc;
   cudaMemcpyAsync(d_rowptr, rowptr.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice, g->st);
   if (!cols.empty()) cudaMemcpyAsync(d_cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, g->st);
   const bool pairs = g->d_Hk_rep && g->Nk_rep < Nk && omega_pairs_valid();
   const int64_t nks = pairs ? g->Nk_rep : Nk;
   launch_omega_ksum2(n, N, nblk, nb, P, Glso, nks, pairs ? g->d_Hk_rep : g->d_Hk, pairs ? g->d_kw : nullptr,
-                     d_rowptr, d_cols, fpart, kchunks, g->st);
-  launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, f, g->st);
+                     d_rowptr, d_cols, fpart, fpart_im, kchunks, g->st);
+  launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, *f_re, g->st);
+  if (want_im) launch_reduce_rows(n, kchunks, fpart_im, 1.0 / (double)Nk, *f_im, g->st);
   CUCHK(cudaGetLastError());
-  if (f_eval) {
-    CUCHK(cudaMemcpyAsync(f_eval, f, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st));
-    CUCHK(cudaStreamSynchronize(g->st));
-    ar.release();
-    return VCA_OK;
+  return VCA_OK;
+}
+
+// The integrand at n host points (f_im may be NULL: real part only)
+int ksum_host(int n, const double2* zh, double* f_re, double* f_im) {
+  Arena ar;
+  double2* d_z;
+  double *dre = nullptr, *dim = nullptr;
+  int rc = ar.alloc(&d_z, n);
+  if (!rc) rc = (cudaMemcpyAsync(d_z, zh, sizeof(double2) * n, cudaMemcpyHostToDevice, g->st) == cudaSuccess)
+                    ? VCA_OK : VCA_ERR_CUDA;
+  if (!rc) rc = ksum_device(n, d_z, f_im != nullptr, ar, &dre, &dim);
+  if (!rc) {
+    cudaMemcpyAsync(f_re, dre, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st);
+    if (f_im) cudaMemcpyAsync(f_im, dim, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st);
+    if (cudaStreamSynchronize(g->st) != cudaSuccess) rc = VCA_ERR_CUDA;
   }
-  double* acc;
-  if ((rc = ar.alloc(&acc, 1))) { ar.release(); return rc; }
-  launch_wsum(n, d_W, f, acc, g->st);
+  ar.release();
+  if (rc == VCA_ERR_CUDA) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  return rc;
+}
+
+// frequency_integration (VCA_OMEGA.f90:123-136) with the fixed rule w =
+// scale*s/(1-s) (Gauss-Legendre in s, nodes cached per context) replacing
+// the adaptive quad(imaginary_axis, 0, inf)
+int omega_integral(double* out) {
+  const vca_config& c = g->cfg;
+  Arena ar;
+  int rc = VCA_OK;
+  const int n = c.omega_nodes;
+  if (g->node_n != n || g->node_scale != c.omega_scale || !g->node_z) {
+    g->nodes.release();
+    g->node_n = 0;
+    double *s, *w;
+    if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = g->nodes.alloc(&g->node_z, n)) ||
+        (rc = g->nodes.alloc(&g->node_w, n))) {
+      ar.release();
+      return rc;
+    }
+    launch_gauss_legendre(n, s, w, g->st);
+    launch_omega_nodes(n, c.omega_scale, s, w, g->node_z, g->node_w, g->st);
+    g->node_n = n;
+    g->node_scale = c.omega_scale;
+  }
+  double *f = nullptr, *acc = nullptr;
+  if ((rc = ksum_device(n, g->node_z, false, ar, &f, nullptr)) || (rc = ar.alloc(&acc, 1))) {
+    ar.release();
+    return rc;
+  }
+  launch_wsum(n, g->node_w, f, acc, g->st);
   double integral = 0.0;
   CUCHK(cudaMemcpyAsync(&integral, acc, sizeof(double), cudaMemcpyDeviceToHost, g->st));
   CUCHK(cudaStreamSynchronize(g->st));
   ar.release();
   *out = (3.0 - c.Nspin) * integral / M_PI;
   return VCA_OK;
+}
+
+// Gauss-Legendre nodes/weights on (0,1), host (Newton on the three-term
+// recurrence of P_n)
+void gauss_legendre01_host(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  for (int i = 0; i < (n + 1) / 2; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = z;  // P_0, P_1
+      for (int j = 2; j <= n; j++) {
+        const double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (n == 1) { p1 = z; p0 = 1.0; }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int j = 2; j <= n; j++) {
+      const double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = n * (z * p1 - p0) / (z * z - 1.0);
+    const double wt = 1.0 / ((1.0 - z * z) * dp * dp);  // 2/((1-z^2)P'^2), halved for (0,1)
+    x[i] = 0.5 * (1.0 - z);
+    x[n - 1 - i] = 0.5 * (1.0 + z);
+    w[i] = wt;
+    w[n - 1 - i] = wt;
+  }
+}
+
+// Angles and weights of the fixed rule replacing quad(integral_contour, 0,
+// pi, key=6) (VCA_OMEGA.f90:172).  The sharp structure of the integrand
+// comes from the poles xmu + i(2n+1)pi/beta of fermi(w - xmu) next to the
+// arc |w| = R; the rule is composite Gauss-Legendre (contour_nodes per
+// panel) on panels growing geometrically (factor 2, at most pi/16) away from
+// the angle of the pole nearest to the arc, the first panel's width that
+// pole's distance from the arc over R.
+void contour_nodes_host(double R, double beta, double mu, int ngl, std::vector<double>& th,
+                        std::vector<double>& wt) {
+  const double ymid = std::sqrt(std::max(R * R - mu * mu, 0.0));
+  const double n0 = std::floor((ymid * beta / M_PI - 1.0) / 2.0);
+  double dist = INFINITY, center = 0.5 * M_PI;
+  for (int d = -1; d <= 2; d++) {
+    const double nn = n0 + d;
+    if (nn < 0.0) continue;
+    const double y = (2.0 * nn + 1.0) * M_PI / beta;
+    const double dd = std::fabs(std::hypot(mu, y) - R);
+    if (dd < dist) { dist = dd; center = std::atan2(y, mu); }
+  }
+  const double h0 = std::max(dist / R, 1e-15), hmax = M_PI / 16.0;
+  std::vector<double> edge{center};
+  for (double b = center, h = h0; b > 0.0; h = std::min(2.0 * h, hmax)) edge.push_back(b = std::max(b - h, 0.0));
+  for (double b = center, h = h0; b < M_PI; h = std::min(2.0 * h, hmax)) edge.push_back(b = std::min(b + h, M_PI));
+  std::sort(edge.begin(), edge.end());
+  std::vector<double> x, w;
+  gauss_legendre01_host(ngl, x, w);
+  th.clear();
+  wt.clear();
+  for (size_t p = 0; p + 1 < edge.size(); p++) {
+    const double a = edge[p], h = edge[p + 1] - edge[p];
+    for (int i = 0; i < ngl; i++) {
+      th.push_back(a + h * x[i]);
+      wt.push_back(h * w[i]);
+    }
+  }
+}
+
+// Largest excitation de = diag(j) - Ei over the poles of every chain
+// (max_exc, VCA_GF_NORMAL.f90:57,1018).  The reference diagonalises the
+// whole nlanc x nlanc tridiagonal: a chain that stopped after n < nlanc steps
+// keeps the zeros its coefficient arrays were cleared to (VCA_GF_NORMAL.f90:
+// 211-213), which add eigenvalues 0, i.e. de = -Ei.  Chains whose start
+// vector vanished (n = 0; NaN in the reference, which the comparison skips)
+// add nothing.
+int chains_max_exc(double* out) {
+  RCHK(ensure_poles());
+  const size_t nch = g->chains.size();
+  double m = -DBL_MAX;
+  if (nch) {
+    std::vector<double> p(nch * (size_t)g->ld);
+    std::vector<int> n(nch), sg(nch);
+    CUCHK(cudaMemcpy(p.data(), g->d_poles, sizeof(double) * p.size(), cudaMemcpyDeviceToHost));
+    CUCHK(cudaMemcpy(n.data(), g->d_nexc, sizeof(int) * nch, cudaMemcpyDeviceToHost));
+    CUCHK(cudaMemcpy(sg.data(), g->cstore.isign, sizeof(int) * nch, cudaMemcpyDeviceToHost));
+    for (size_t ch = 0; ch < nch; ch++) {
+      for (int j = 0; j < n[ch]; j++) m = std::max(m, sg[ch] * p[ch * g->ld + j]);  // poles = isign*de
+      if (n[ch] > 0 && n[ch] < g->chains[ch].nlanc) m = std::max(m, -g->gs[g->chains[ch].state].e);
+    }
+  }
+  *out = m;
+  return VCA_OK;
+}
+
+// frequency_integration_finite_t (VCA_OMEGA.f90:153-182): Matsubara sum up
+// to nmax plus the contour integral over |w| = R, times (3 - Nspin)
+int omega_integral_finite_t(double* out) {
+  const vca_config& c = g->cfg;
+  const double beta = c.beta, mu = c.xmu;
+  RCHK(chains_max_exc(&g->max_exc));
+  if (!std::isfinite(g->max_exc)) VFAIL(VCA_ERR_NUMERIC, "no Green's function pole: max_exc undefined");
+  const double xn = 2.0 * (std::fabs(g->max_exc) + c.bandwidth) * beta / M_PI;
+  if (!(xn < 1e8)) VFAIL(VCA_ERR_UNSUPPORTED, "finite-T Matsubara sum beyond 5e7 frequencies");
+  int nmax = (int)xn;
+  nmax = (nmax % 2 == 0) ? nmax / 2 : (nmax + 1) / 2;
+  const double R = 2.0 * (nmax + 1) * M_PI / beta;
+  // 2) Matsubara sum 2/beta sum_{n=0..nmax} Re F(i w_n)
+  std::vector<double2> zm(nmax + 1);
+  for (int n = 0; n <= nmax; n++) zm[n] = make_double2(0.0, (2.0 * n + 1.0) * M_PI / beta);
+  std::vector<double> fm(nmax + 1);
+  RCHK(ksum_host(nmax + 1, zm.data(), fm.data(), nullptr));
+  double sum = 0.0;
+  for (int n = 0; n <= nmax; n++) sum += fm[n];
+  sum = 2.0 * (1.0 / beta) * sum;
+  // 3) contour part: integral_contour (:186-199) on the fixed rule
+  std::vector<double> th, wt;
+  contour_nodes_host(R, beta, mu, c.contour_nodes, th, wt);
+  const int nc = (int)th.size();
+  std::vector<double2> zc(nc);
+  for (int i = 0; i < nc; i++) zc[i] = make_double2(R * std::cos(th[i]), R * std::sin(th[i]));
+  std::vector<double> fre(nc), fim(nc);
+  RCHK(ksum_host(nc, zc.data(), fre.data(), fim.data()));
+  double integral = 0.0;
+  for (int i = 0; i < nc; i++) {
+    const cd w(zc[i].x, zc[i].y);
+    cd fermi = 0.0;
+    if (((w - mu) * beta).real() < 100.0) fermi = 1.0 / (std::exp(beta * (w - mu)) + 1.0);
+    integral += wt[i] * ((1.0 / M_PI) * w * fermi * cd(fre[i], fim[i])).real();
+  }
+  g->nmax = nmax;
+  g->int_R = R;
+  g->sum_part = sum;
+  g->contour_part = integral;
+  g->contour_points = nc;
+  *out = (3.0 - c.Nspin) * (sum + integral);
+  return VCA_OK;
+}
+
+// Omega' (VCA_MAIN.f90:186-193): E_gs at T=0, E_min - T ln sum_i
+// exp(-beta(E_i - E_min)) over the final state list at finite T
+double omega_prime() {
+  if (!g->finiteT) return g->egs;
+  double z = 0.0;
+  for (const GState& s : g->gs) z += std::exp(-g->cfg.beta * (s.e - g->egs));
+  return g->egs - (1.0 / g->cfg.beta) * std::log(z);
 }
 
 // Pairs k, k' with H_k' = conj(H_k) to 1e-13 of the largest |H_k| entry
@@ -1570,13 +1843,14 @@ int solve_resident(const double* Hloc, const double* bath_h, const double* bath_
   double t2 = now_ms();
   RCHK(build_gf());
   double t3 = now_ms();
-  RCHK(omega_integral(g->Nk, &g->omega_int, 0, nullptr, nullptr));
+  RCHK(g->finiteT ? omega_integral_finite_t(&g->omega_int) : omega_integral(&g->omega_int));
   double t4 = now_ms();
   g->t_ms[0] = t1 - t0;
   g->t_ms[1] = t2 - t1;
   g->t_ms[2] = t3 - t2;
   g->t_ms[3] = t4 - t3;
-  g->sft = g->egs - g->omega_int;  // VCA_MAIN.f90:183-197
+  g->omega_prime = omega_prime();
+  g->sft = g->omega_prime - g->omega_int;  // VCA_MAIN.f90:183-197
   g->solved = true;
   if (omega_out) *omega_out = g->sft;
   return VCA_OK;
@@ -1632,8 +1906,14 @@ void vca_config_defaults(vca_config* c) {
   c->gs_check_every = 10;
   c->omega_scale = 1.0;
   c->gs_residual_tol = 1e-11;
-  c->gf_beta_tol = 1e-12;
+  c->gf_beta_tol = 1e-6;
+  c->gs_beta_tol = 1e-12;
   c->start_seed = 20261203ull;
+  c->lanc_nstates_step = 2;     // VCA_INPUT_VARS.f90:155
+  c->lanc_niter_spectrum = 10;  // VCA_INPUT_VARS.f90:159
+  c->cutoff = 1e-9;             // VCA_INPUT_VARS.f90:169
+  c->bandwidth = 0.0;
+  c->contour_nodes = 24;
 }
 
 int vca_gpu_last_error(char* buf, int32_t len) {
@@ -1671,8 +1951,16 @@ int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath
   if (c.Nspin < 1 || c.Nspin > 2) VFAIL(VCA_ERR_CONFIG, "ED ERROR: Nspin > 2 is currently not supported");
   if (c.Norb < 1 || c.Norb > 5) VFAIL(VCA_ERR_CONFIG, "ED ERROR: Norb > 5 is currently not supported");
   if (c.Nlat < 1) VFAIL(VCA_ERR_CONFIG, "Nlat must be >= 1");
-  if (c.lanc_nstates_total != 1)
-    VFAIL(VCA_ERR_UNSUPPORTED, "finite temperature (LANC_NSTATES_TOTAL != 1) is outside the GPU path");
+  const bool finiteT = c.lanc_nstates_total != 1;  // VCA_SETUP.f90:157-162
+  if (finiteT) {
+    if (c.lanc_nstates_total < 1) VFAIL(VCA_ERR_CONFIG, "LANC_NSTATES_TOTAL must be >= 1");
+    if (c.lanc_niter_spectrum < 1) VFAIL(VCA_ERR_CONFIG, "LANC_NITER_SPECTRUM must be >= 1");
+    if (c.lanc_nstates_step < 0) VFAIL(VCA_ERR_CONFIG, "LANC_NSTATES_STEP must be >= 0");
+    if (!(c.beta > 0.0) || !std::isfinite(c.beta)) VFAIL(VCA_ERR_CONFIG, "BETA must be > 0");
+    if (!(c.cutoff > 0.0 && c.cutoff < 1.0)) VFAIL(VCA_ERR_CONFIG, "CUTOFF must lie in (0,1)");
+    if (c.contour_nodes < 2) VFAIL(VCA_ERR_CONFIG, "contour_nodes must be >= 2");
+    if (!std::isfinite(c.bandwidth)) VFAIL(VCA_ERR_CONFIG, "bandwidth must be finite");
+  }
   if (c.vca_twin) VFAIL(VCA_ERR_UNSUPPORTED, "VCA_TWIN is outside the GPU path");
   if (c.lanc_ngfiter < 1 || c.lanc_niter < 1) VFAIL(VCA_ERR_CONFIG, "LANC_NITER and LANC_NGFITER must be >= 1");
   if (c.omega_nodes < 2) VFAIL(VCA_ERR_CONFIG, "omega_nodes must be >= 2");
@@ -1689,6 +1977,9 @@ int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath
   g->N = c.Nlat * c.Nspin * c.Norb;
   g->L = c.Nlat * c.Norb;
   g->Nb = c.Nlat_bath * c.Nspin * c.Norb_bath;
+  g->finiteT = finiteT;
+  g->nstates_total = c.lanc_nstates_total;
+  if (finiteT && g->nstates_total % 2 != 0) g->nstates_total++;  // VCA_SETUP.f90:172-175
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev < 1) {
@@ -1784,32 +2075,40 @@ int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t io
       iorb < 1 || iorb > c.Norb || jorb < 1 || jorb > c.Norb)
     VFAIL(VCA_ERR_ARG, "element index out of range");
   const int e = elem_index(c, ilat - 1, jlat - 1, ispin - 1, iorb - 1, jorb - 1);
-  if (!g->poles_ready && !g->chains.empty()) {  // poles and weights of every chain, once per solve
-    Arena ar;
-    double* work;
-    const int nch = (int)g->chains.size();
-    RCHK(ar.alloc(&work, (size_t)nch * 3 * g->ld));
-    launch_chain_poles(nch, g->cstore, work, g->d_poles, g->d_weights, g->d_nexc, g->st);
-    cudaError_t err = cudaStreamSynchronize(g->st);
-    ar.release();
-    CUCHK(err);
-    g->poles_ready = true;
-  }
+  RCHK(ensure_poles());
   for (int ch = 0; ch < (int)g->chains.size(); ch++) {
     const ChainRec& r = g->chains[ch];
     if (r.elem != e || r.state != istate - 1 || r.chan != ichan) continue;
-    int n = 0;
+    int n = 0, sg = 1;
     CUCHK(cudaMemcpy(&n, g->d_nexc + ch, sizeof(int), cudaMemcpyDeviceToHost));
-    if (nexc) *nexc = n;
-    if (cap >= n && n > 0) {
+    CUCHK(cudaMemcpy(&sg, g->cstore.isign + ch, sizeof(int), cudaMemcpyDeviceToHost));
+    // a chain that stopped after n < nlanc steps: the reference's table has
+    // Nexc = nlanc entries, the zeros left in its coefficient arrays giving
+    // eigenvalues 0 (pole isign*(0 - Ei), weight 0) in ascending order
+    // (VCA_GF_NORMAL.f90:1006-1022)
+    const int npad = (n > 0 && n < r.nlanc) ? r.nlanc - n : 0;
+    const int ntot = n + npad;
+    if (nexc) *nexc = ntot;
+    if (cap >= ntot && n > 0) {
       std::vector<double> p(n);
       std::vector<double2> w(n);
       CUCHK(cudaMemcpy(p.data(), g->d_poles + (size_t)ch * g->ld, sizeof(double) * n, cudaMemcpyDeviceToHost));
       CUCHK(cudaMemcpy(w.data(), g->d_weights + (size_t)ch * g->ld, sizeof(double2) * n, cudaMemcpyDeviceToHost));
-      for (int j = 0; j < n; j++) {
-        if (poles) { poles[2 * j] = p[j]; poles[2 * j + 1] = 0.0; }
-        if (weights) { weights[2 * j] = w[j].x; weights[2 * j + 1] = w[j].y; }
+      const double Ei = g->gs[r.state].e;
+      int q = 0, out = 0;
+      auto put = [&](double pole, double2 wt) {
+        if (poles) { poles[2 * out] = pole; poles[2 * out + 1] = 0.0; }
+        if (weights) { weights[2 * out] = wt.x; weights[2 * out + 1] = wt.y; }
+        out++;
+      };
+      for (int j = 0; j < n; j++) {  // p[j] = isign*(d_j - Ei), d ascending
+        const double dj = sg * p[j] + Ei;
+        if (q == 0 && npad && dj > 0.0) {
+          for (; q < npad; q++) put(sg * (0.0 - Ei), make_double2(0.0, 0.0));
+        }
+        put(p[j], w[j]);
       }
+      for (; q < npad; q++) put(sg * (0.0 - Ei), make_double2(0.0, 0.0));
     }
     return VCA_OK;
   }
@@ -1979,9 +2278,11 @@ static int observable(int which, double* out) {
         b += h[((size_t)1 * nimp + l) * nb + x];
         d += h[((size_t)2 * nimp + l) * nb + x];
       }
-      up[l] += a / g->zeta;
-      dw[l] += b / g->zeta;
-      dd[l] += d / g->zeta;
+      // peso = exp(-beta(Ei-Egs))/zeta at finite T (VCA_OBSERVABLES.f90:248-249)
+      const double peso = (g->finiteT ? std::exp(-c.beta * (st.e - g->egs)) : 1.0) / g->zeta;
+      up[l] += peso * a;
+      dw[l] += peso * b;
+      dd[l] += peso * d;
     }
   }
   for (int il = 0; il < c.Nlat; il++)
@@ -2006,8 +2307,40 @@ int vca_gpu_get_g0_realaxis(double* g0_out) { return sigma_grid(false, true, g0_
 int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out) {
   if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   if (!w || !f_out || nw < 1) VFAIL(VCA_ERR_ARG, "bad arguments");
-  double dummy;
-  return omega_integral(g->Nk, &dummy, (int)nw, w, f_out);
+  std::vector<double2> z(nw);
+  for (int64_t i = 0; i < nw; i++) z[i] = make_double2(0.0, w[i]);
+  return ksum_host((int)nw, z.data(), f_out, nullptr);
+}
+
+int vca_gpu_sum_kmesh_complex(const double* z, int64_t nz, double* f_out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!z || !f_out || nz < 1 || nz > (1 << 24)) VFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<double2> zh(nz);
+  for (int64_t i = 0; i < nz; i++) zh[i] = make_double2(z[2 * i], z[2 * i + 1]);
+  std::vector<double> re(nz), im(nz);
+  RCHK(ksum_host((int)nz, zh.data(), re.data(), im.data()));
+  for (int64_t i = 0; i < nz; i++) { f_out[2 * i] = re[i]; f_out[2 * i + 1] = im[i]; }
+  return VCA_OK;
+}
+
+int vca_gpu_get_thermal(vca_thermal* out) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!out) VFAIL(VCA_ERR_ARG, "NULL output");
+  std::memset(out, 0, sizeof(*out));
+  out->zeta = g->zeta;
+  out->omega_prime = g->omega_prime;
+  out->e_min = g->egs;
+  out->nstates_total = g->nstates_total;
+  out->finite_t = g->finiteT ? 1 : 0;
+  if (g->finiteT) {
+    out->max_exc = g->max_exc;
+    out->integration_R = g->int_R;
+    out->sum_part = g->sum_part;
+    out->contour_part = g->contour_part;
+    out->nmax = g->nmax;
+    out->contour_points = g->contour_points;
+  }
+  return VCA_OK;
 }
 
 int vca_gpu_sector_info(int32_t isector, int32_t* nup, int32_t* ndw, int64_t* dimup, int64_t* dimdw) {

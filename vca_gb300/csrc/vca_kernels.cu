@@ -504,7 +504,7 @@ void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, d
 // ---------------------------------------------------------------------------
 __global__ void k_chain_store(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
                               const double* norm2, const double2* wfac, const int* isign, double Ei,
-                              double zeta, ChainStore cs, int base) {
+                              double boltz, double zeta, ChainStore cs, int base) {
   const int ch = blockIdx.x;
   if (ch >= nch) return;
   const int n = meta[ch].len;
@@ -515,18 +515,18 @@ __global__ void k_chain_store(int nch, const ChainMeta* meta, const double* A, c
   }
   if (threadIdx.x == 0) {
     cs.n[base + ch] = n;
-    cs.pes[base + ch] = norm2[ch] / zeta;
+    cs.pes[base + ch] = norm2[ch] * boltz / zeta;  // vnorm2*exp(-beta(Ei-Egs))/zeta
     cs.isign[base + ch] = isign[ch];
     cs.wfac[base + ch] = wfac[ch];
     cs.Ei[base + ch] = Ei;
   }
 }
 void launch_chain_store(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
-                        const double* norm2, const double2* wfac, const int* isign, double Ei, double zeta,
-                        const ChainStore& cs, int base, cudaStream_t st) {
+                        const double* norm2, const double2* wfac, const int* isign, double Ei, double boltz,
+                        double zeta, const ChainStore& cs, int base, cudaStream_t st) {
   if (nch <= 0) return;
   COUNT_LAUNCH();
-  k_chain_store<<<nch, 128, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, zeta, cs, base);
+  k_chain_store<<<nch, 128, 0, st>>>(nch, meta, A, Bt, ldab, norm2, wfac, isign, Ei, boltz, zeta, cs, base);
 }
 
 // Chain tridiagonal -> poles and weights.  Implicit QL with Wilkinson shift
@@ -1066,12 +1066,130 @@ void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long*
 //  ||A||_inf < 1/2: no pivoting, identity implicit, prod |1+a_kk|^2 = 1+delta
 //  tracked as delta' = delta + x + delta*x, one log1p at the end.  Otherwise
 //  partial pivoting with prod |u_kk|^2 kept as mantissa * 2^e (frexp), one
-//  log at the end.
+//  log at the end.  The complex form (finite T, sum_kmesh_complex,
+//  VCA_OMEGA.f90:78-114) runs every spin block of one k in the same warp and
+//  also sums the pivots' arguments (plus pi per row swap): arg det of the
+//  whole matrix, reduced to (-pi, pi] as the principal log takes it.
 // ---------------------------------------------------------------------------
+// A = (P - H) G for the nb x nb block at offset off, into the warp's Aw
+__device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off, int N, const double2* Ps,
+                                                   const double2* Gs, const double2* H, const int* rowptr,
+                                                   const int* cols, int lane) {
+  const int nbb = nb * nb;
+  for (int e = lane; e < nbb; e += 32) {  // A(i,j), i fastest across lanes
+    const int i = e % nb, j = e / nb;
+    const int gi = off + i;
+    double sr = 0.0, si = 0.0;
+    for (int q = rowptr[gi]; q < rowptr[gi + 1]; q++) {
+      const int gl = cols[q];
+      const int il = gi + gl * N;
+      const double mr = Ps[il].x - H[il].x, mi = Ps[il].y - H[il].y;
+      const double2 gg = Gs[gl + (off + j) * N];
+      sr = fma(mr, gg.x, sr);
+      sr = fma(-mi, gg.y, sr);
+      si = fma(mr, gg.y, si);
+      si = fma(mi, gg.x, si);
+    }
+    Aw[e] = make_double2(sr, si);
+  }
+  __syncwarp();
+}
+
+// ln|det(1 + A)| of the block in Aw (destroyed); with PH, *ph gains the sum
+// of the pivots' arguments (plus pi per row swap).  Warp-uniform result.
+template <bool PH>
+__device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
+  double rmax = 0.0;
+  if (lane < nb)
+    for (int j = 0; j < nb; j++) {
+      const double2 a = Aw[lane + j * nb];
+      rmax += fabs(a.x) + fabs(a.y);  // >= sum |a_ij|: a safe bound for the branch
+    }
+  for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  if (rmax < 0.5) {
+    double delta = 0.0;
+    for (int kk = 0; kk < nb; kk++) {
+      const double2 akk = Aw[kk + kk * nb];
+      const double pr = 1.0 + akk.x, pim = akk.y;
+      const double x = 2.0 * akk.x + akk.x * akk.x + akk.y * akk.y;
+      delta = delta + x + delta * x;
+      if (PH) *ph += atan2(pim, pr);
+      const double den = pr * pr + pim * pim;
+      const double ir = pr / den, ii = -pim / den;  // 1/pivot
+      for (int i = kk + 1 + lane; i < nb; i += 32) {
+        const double2 a = Aw[i + kk * nb];
+        Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
+      }
+      __syncwarp();
+      const int r = nb - kk - 1;
+      for (int e = lane; e < r * r; e += 32) {
+        const int i = kk + 1 + e % r, j = kk + 1 + e / r;
+        const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
+        double2& t = Aw[i + j * nb];
+        t.x -= l.x * u.x - l.y * u.y;
+        t.y -= l.x * u.y + l.y * u.x;
+      }
+      __syncwarp();
+    }
+    return 0.5 * log1p(delta);
+  }
+  for (int i = lane; i < nb; i += 32) Aw[i + i * nb].x += 1.0;
+  __syncwarp();
+  double mant = 1.0;
+  int ex = 0;
+  bool zero = false;
+  for (int kk = 0; kk < nb; kk++) {
+    double mag = -1.0;
+    int arg = kk;
+    if (lane >= kk && lane < nb) {
+      const double2 a = Aw[lane + kk * nb];
+      mag = a.x * a.x + a.y * a.y;
+      arg = lane;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double om = __shfl_xor_sync(0xffffffffu, mag, o);
+      const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+      if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
+    }
+    if (mag == 0.0) { zero = true; break; }
+    if (arg != kk) {
+      for (int j = lane; j < nb; j += 32) {
+        const double2 t = Aw[kk + j * nb];
+        Aw[kk + j * nb] = Aw[arg + j * nb];
+        Aw[arg + j * nb] = t;
+      }
+      if (PH) *ph += 3.141592653589793;
+    }
+    __syncwarp();
+    const double2 piv = Aw[kk + kk * nb];
+    if (PH) *ph += atan2(piv.y, piv.x);
+    int e2;
+    mant = frexp(mant * mag, &e2);
+    ex += e2;
+    const double ir = piv.x / mag, ii = -piv.y / mag;
+    for (int i = kk + 1 + lane; i < nb; i += 32) {
+      const double2 a = Aw[i + kk * nb];
+      Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
+    }
+    __syncwarp();
+    const int r = nb - kk - 1;
+    for (int e = lane; e < r * r; e += 32) {
+      const int i = kk + 1 + e % r, j = kk + 1 + e / r;
+      const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
+      double2& t = Aw[i + j * nb];
+      t.x -= l.x * u.x - l.y * u.y;
+      t.y -= l.x * u.y + l.y * u.x;
+    }
+    __syncwarp();
+  }
+  return zero ? -INFINITY : 0.5 * (log(mant) + ex * 0.6931471805599453);
+}
+
+template <bool CPLX>
 __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, const double2* P,
                                                      const double2* Glso, int64_t Nk, const double2* Hk,
                                                      const double* kw, const int* rowptr, const int* cols,
-                                                     double* fpart, int kchunks) {
+                                                     double* fpart, double* fpart_im, int kchunks) {
   extern __shared__ double2 shm[];
   const int w = blockIdx.y;
   const int chunk = blockIdx.x;
@@ -1087,137 +1205,56 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
   }
   __syncthreads();
   const int64_t k0 = (Nk * chunk) / kchunks, k1 = (Nk * (chunk + 1)) / kchunks;
-  double acc = 0.0;
-  const int64_t ntask = (k1 - k0) * nblk;
-  const int nbb = nb * nb;
+  double acc = 0.0, acc_im = 0.0;
+  const int64_t ntask = CPLX ? (k1 - k0) : (k1 - k0) * nblk;
   for (int64_t task = warp; task < ntask; task += nwarps) {
-    const int64_t k = k0 + task / nblk;
-    const int off = (int)(task % nblk) * nb;
+    const int64_t k = CPLX ? k0 + task : k0 + task / nblk;
     const double2* H = Hk + k * NN;
-    double rmax = 0.0;
-    for (int e = lane; e < nbb; e += 32) {  // A(i,j), i fastest across lanes
-      const int i = e % nb, j = e / nb;
-      const int gi = off + i;
-      double sr = 0.0, si = 0.0;
-      for (int q = rowptr[gi]; q < rowptr[gi + 1]; q++) {
-        const int gl = cols[q];
-        const int il = gi + gl * N;
-        const double mr = Ps[il].x - H[il].x, mi = Ps[il].y - H[il].y;
-        const double2 gg = Gs[gl + (off + j) * N];
-        sr = fma(mr, gg.x, sr);
-        sr = fma(-mi, gg.y, sr);
-        si = fma(mr, gg.y, si);
-        si = fma(mi, gg.x, si);
-      }
-      Aw[e] = make_double2(sr, si);
+    const int b0 = CPLX ? 0 : (int)(task % nblk), b1 = CPLX ? nblk : b0 + 1;
+    double ld = 0.0, ph = 0.0;
+    for (int b = b0; b < b1; b++) {
+      ksum_block_product(Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, lane);
+      ld += ksum_block_logdet<CPLX>(Aw, nb, lane, &ph);
     }
-    __syncwarp();
-    if (lane < nb)
-      for (int j = 0; j < nb; j++) {
-        const double2 a = Aw[lane + j * nb];
-        rmax += fabs(a.x) + fabs(a.y);  // >= sum |a_ij|: a safe bound for the branch
+    if (lane == 0) {
+      acc += kw ? kw[k] * ld : ld;
+      if (CPLX) {
+        double a = remainder(ph, 6.283185307179586);
+        if (a <= -3.141592653589793) a += 6.283185307179586;
+        acc_im += kw ? kw[k] * a : a;
       }
-    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    double ld;
-    if (rmax < 0.5) {
-      double delta = 0.0;
-      for (int kk = 0; kk < nb; kk++) {
-        const double2 akk = Aw[kk + kk * nb];
-        const double pr = 1.0 + akk.x, pim = akk.y;
-        const double x = 2.0 * akk.x + akk.x * akk.x + akk.y * akk.y;
-        delta = delta + x + delta * x;
-        const double den = pr * pr + pim * pim;
-        const double ir = pr / den, ii = -pim / den;  // 1/pivot
-        for (int i = kk + 1 + lane; i < nb; i += 32) {
-          const double2 a = Aw[i + kk * nb];
-          Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
-        }
-        __syncwarp();
-        const int r = nb - kk - 1;
-        for (int e = lane; e < r * r; e += 32) {
-          const int i = kk + 1 + e % r, j = kk + 1 + e / r;
-          const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
-          double2& t = Aw[i + j * nb];
-          t.x -= l.x * u.x - l.y * u.y;
-          t.y -= l.x * u.y + l.y * u.x;
-        }
-        __syncwarp();
-      }
-      ld = 0.5 * log1p(delta);
-    } else {
-      for (int i = lane; i < nb; i += 32) Aw[i + i * nb].x += 1.0;
-      __syncwarp();
-      double mant = 1.0;
-      int ex = 0;
-      bool zero = false;
-      for (int kk = 0; kk < nb; kk++) {
-        double mag = -1.0;
-        int arg = kk;
-        if (lane >= kk && lane < nb) {
-          const double2 a = Aw[lane + kk * nb];
-          mag = a.x * a.x + a.y * a.y;
-          arg = lane;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-          const double om = __shfl_xor_sync(0xffffffffu, mag, o);
-          const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
-          if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
-        }
-        if (mag == 0.0) { zero = true; break; }
-        if (arg != kk)
-          for (int j = lane; j < nb; j += 32) {
-            const double2 t = Aw[kk + j * nb];
-            Aw[kk + j * nb] = Aw[arg + j * nb];
-            Aw[arg + j * nb] = t;
-          }
-        __syncwarp();
-        const double2 piv = Aw[kk + kk * nb];
-        int e2;
-        mant = frexp(mant * mag, &e2);
-        ex += e2;
-        const double ir = piv.x / mag, ii = -piv.y / mag;
-        for (int i = kk + 1 + lane; i < nb; i += 32) {
-          const double2 a = Aw[i + kk * nb];
-          Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
-        }
-        __syncwarp();
-        const int r = nb - kk - 1;
-        for (int e = lane; e < r * r; e += 32) {
-          const int i = kk + 1 + e % r, j = kk + 1 + e / r;
-          const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
-          double2& t = Aw[i + j * nb];
-          t.x -= l.x * u.x - l.y * u.y;
-          t.y -= l.x * u.y + l.y * u.x;
-        }
-        __syncwarp();
-      }
-      ld = zero ? -INFINITY : 0.5 * (log(mant) + ex * 0.6931471805599453);
     }
-    if (lane == 0) acc += kw ? kw[k] * ld : ld;
     __syncwarp();
   }
-  __shared__ double red[32];
-  if (lane == 0) red[warp] = acc;
+  __shared__ double red[32], red_im[32];
+  if (lane == 0) { red[warp] = acc; red_im[warp] = acc_im; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double sacc = 0.0;
-    for (int q = 0; q < nwarps; q++) sacc += red[q];
+    double sacc = 0.0, sim = 0.0;
+    for (int q = 0; q < nwarps; q++) { sacc += red[q]; sim += red_im[q]; }
     fpart[(int64_t)w * kchunks + chunk] = sacc;
+    if (CPLX) fpart_im[(int64_t)w * kchunks + chunk] = sim;
   }
 }
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                        int kchunks, cudaStream_t st) {
+                        double* fpart_im, int kchunks, cudaStream_t st) {
   COUNT_LAUNCH();
   const int threads = 128;
   size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_omega_ksum2, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_omega_ksum2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_omega_ksum2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     attr = true;
   }
   dim3 grd(kchunks, nw, 1);
-  k_omega_ksum2<<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, kchunks);
+  if (fpart_im)
+    k_omega_ksum2<true><<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im,
+                                                   kchunks);
+  else
+    k_omega_ksum2<false><<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart,
+                                                    nullptr, kchunks);
 }
 
 // ---------------------------------------------------------------------------

@@ -78,8 +78,8 @@ void launch_tri_lowest(const double* A, const double* Bt, int k, double btail, d
                        double* s, double* resid, cudaStream_t st);
 // Device store of every Green's function chain: tridiagonal rows A, B
 // ([nch*ld], B[j] = beta_j couples rows j-1 and j), length n, prefactor
-// pes = norm^2/zeta, isign (+1 particle, -1 hole), channel weight factor,
-// ground-state energy Ei.
+// pes = norm^2*boltz/zeta (boltz = 1 at T=0), isign (+1 particle, -1 hole),
+// channel weight factor, state energy Ei.
 struct ChainStore {
   double* A;
   double* B;
@@ -93,8 +93,8 @@ struct ChainStore {
 // copy one batch's chains (rows of A/Bt with stride ldab) into the store at
 // chain offset base
 void launch_chain_store(int nch, const ChainMeta* meta, const double* A, const double* Bt, int ldab,
-                        const double* norm2, const double2* wfac, const int* isign, double Ei, double zeta,
-                        const ChainStore& cs, int base, cudaStream_t st);
+                        const double* norm2, const double2* wfac, const int* isign, double Ei, double boltz,
+                        double zeta, const ChainStore& cs, int base, cudaStream_t st);
 // stored chains -> poles/weights (add_to_lanczos_gf_normal, VCA_GF_NORMAL.f90:970-1033);
 // work: 3*ld doubles per chain
 void launch_chain_poles(int nch, const ChainStore& cs, double* work, double* poles, double2* weights, int* nexc,
@@ -139,10 +139,11 @@ void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, doub
 // over the chunk's k of kw[k] ln|det(1 + (P_w - Hk_k) G_w)| per spin block
 // (kw == nullptr: weight 1), M = P - Hk on a sparse row pattern
 // (rowptr/cols, lso indices), all lanes of a warp on the products and the LU
-// updates
+// updates.  With fpart_im (sum_kmesh_complex, :78-114) also the k-sum of the
+// principal argument of det over all blocks of each k.
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                        int kchunks, cudaStream_t st);
+                        double* fpart_im, int kchunks, cudaStream_t st);
 // Sigma(z) (want_g0 = false) or G0(z) on nz frequencies from G' (lso) and
 // P = Delta + Hloc (per z, or one matrix): build_sigma_normal,
 // VCA_GF_NORMAL.f90:1045-1111.  N <= 32.

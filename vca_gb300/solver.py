@@ -35,8 +35,25 @@ EXPORTS = [
     "vca_gpu_get_docc", "vca_gpu_get_mag",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
-    "vca_gpu_arith_info",
+    "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal",
 ]
+
+
+class VcaThermal(ctypes.Structure):
+    """Mirror of ``vca_thermal`` (include/vca_gpu.h)."""
+    _fields_ = [
+        ("zeta", ctypes.c_double),
+        ("omega_prime", ctypes.c_double),
+        ("e_min", ctypes.c_double),
+        ("max_exc", ctypes.c_double),
+        ("integration_R", ctypes.c_double),
+        ("sum_part", ctypes.c_double),
+        ("contour_part", ctypes.c_double),
+        ("nmax", ctypes.c_int32),
+        ("nstates_total", ctypes.c_int32),
+        ("contour_points", ctypes.c_int32),
+        ("finite_t", ctypes.c_int32),
+    ]
 
 
 class VcaError(RuntimeError):
@@ -83,6 +100,8 @@ def load(path: Optional[str] = None):
         "vca_gpu_get_gf_channel": (ctypes.c_int, [i32, i32, i32, i32, i32, i32, i32,
                                                   ctypes.POINTER(i32), dp, dp, i32]),
         "vca_gpu_sum_kmesh": (ctypes.c_int, [dp, i64, dp]),
+        "vca_gpu_sum_kmesh_complex": (ctypes.c_int, [dp, i64, dp]),
+        "vca_gpu_get_thermal": (ctypes.c_int, [ctypes.POINTER(VcaThermal)]),
         "vca_gpu_finalize": (ctypes.c_int, []),
         "vca_gpu_last_error": (ctypes.c_int, [ctypes.c_char_p, i32]),
         "vca_gpu_sector_info": (ctypes.c_int, [i32, ctypes.POINTER(i32), ctypes.POINTER(i32),
@@ -330,6 +349,20 @@ class VcaSolver:
         out = np.zeros(len(w))
         check(self.L.vca_gpu_sum_kmesh(_dp(w), len(w), _dp(out)))
         return out
+
+    def sum_kmesh_complex(self, z) -> np.ndarray:
+        """sum_kmesh_complex: (1/Lk) sum_k log det(...) at complex z (principal branch per k)."""
+        z = np.ascontiguousarray(np.atleast_1d(z), dtype=np.complex128)
+        out = np.zeros(len(z), dtype=np.complex128)
+        check(self.L.vca_gpu_sum_kmesh_complex(_dp(z), len(z), _dp(out)))
+        return out
+
+    def thermal(self) -> dict:
+        """zeta, Omega', E_min, max_exc, contour radius, Matsubara and contour
+        parts, nmax, the adapted LANC_NSTATES_TOTAL, contour nodes, finite_t."""
+        t = VcaThermal()
+        check(self.L.vca_gpu_get_thermal(ctypes.byref(t)))
+        return {name: getattr(t, name) for name, _ in VcaThermal._fields_}
 
     # ---- parity hooks ------------------------------------------------------
     def sector_info(self, isector):
