@@ -313,6 +313,7 @@ def run_gpu(args):
         # the library context)
         s.close()
         out["hxv_single_4x4"] = hxv_single_4x4()
+        out["finite_t"] = finite_t_sample(cpu=(world == 1 and not args.no_cpu))
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample, _ = cpu_sample(pts[0], os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -324,6 +325,44 @@ def run_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def finite_t_point():
+    from vca_gb300 import clusters
+    return clusters.square(nx=3, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=8, nky=8, ngfiter=100,
+                           omega_nodes=256, lanc_nstates_total=2, beta=20.0, bandwidth=8.0)
+
+
+def finite_t_sample(reps: int = 3, cpu: bool = True) -> dict:
+    """Finite-temperature solves (LANC_NSTATES_TOTAL = 2, beta = 20) of the
+    3x3 Hubbard cluster with a Weiss field, 8x8 k-grid: GPU wall time per
+    vca_gpu_solve (host buffers) after one warm-up, and, on one process, the
+    oracle's time for the same solve on all host cores."""
+    from vca_gb300.solver import VcaSolver
+    pt = finite_t_point()
+    s = VcaSolver(pt.cfg)
+    om = s.solve(pt.Hloc, pt.Hk)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        om = s.solve(pt.Hloc, pt.Hk)
+    gpu_ms = (time.perf_counter() - t0) * 1e3 / reps
+    th = s.thermal()
+    nst = len(s.states())
+    s.close()
+    out = {"workload": "3x3 Hubbard U=8 xmu=4 M=0.1, Nspin=2, 8x8 k, 100-step chains, beta=20",
+           "gpu_ms_per_solve": round(gpu_ms, 2), "omega": om, "states": nst,
+           "nmax": th["nmax"], "contour_points": th["contour_points"]}
+    if cpu:
+        from oracle import oracle as orc
+        from oracle.oracle import Oracle
+        threads = orc.set_threads(os.cpu_count() or 1)
+        o = Oracle.from_point(pt)
+        t0 = time.perf_counter()
+        ref = o.solve()[0]
+        out["cpu_oracle_ms_per_solve"] = round((time.perf_counter() - t0) * 1e3, 1)
+        out["cpu_cores"] = threads
+        out["omega_rel_diff"] = abs(om - ref) / abs(ref)
+    return out
 
 
 def hxv_single_4x4(reps: int = 10) -> dict:
