@@ -1234,31 +1234,31 @@ double sum_kmesh(const Oracle& o, double w) {
 }
 
 // Gauss-Legendre rule on (0,1) by Newton iteration on P_n (Golub & Welsch
-// give the same nodes; this is the classical Newton form).
+// give the same nodes; this is the classical Newton form), stopped once the
+// step is at rounding level, at most 12 steps.
+void legendre_pn(int n, double z, double& p1, double& p2) {
+  p1 = 1.0;
+  p2 = 0.0;
+  for (int j = 1; j <= n; j++) {
+    const double p3 = p2;
+    p2 = p1;
+    p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+  }
+}
 void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
   x.resize(n);
   w.resize(n);
   for (int i = 0; i < (n + 1) / 2; i++) {
-    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0.0;
-    for (int it = 0; it < 100; it++) {
-      double p1 = 1.0, p2 = 0.0;
-      for (int j = 1; j <= n; j++) {
-        double p3 = p2;
-        p2 = p1;
-        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-      }
-      pp = n * (z * p1 - p2) / (z * z - 1.0);
-      double z1 = z;
-      z = z1 - p1 / pp;
-      if (std::fabs(z - z1) < 1e-16) {
-        // one more evaluation for the weight at the converged node
-        p1 = 1.0; p2 = 0.0;
-        for (int j = 1; j <= n; j++) { double p3 = p2; p2 = p1; p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j; }
-        pp = n * (z * p1 - p2) / (z * z - 1.0);
-        break;
-      }
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), p1, p2;
+    for (int it = 0; it < 12; it++) {
+      legendre_pn(n, z, p1, p2);
+      const double dz = p1 / (n * (z * p1 - p2) / (z * z - 1.0));
+      z -= dz;
+      if (std::fabs(dz) <= 2.5e-16) break;
     }
-    double wt = 2.0 / ((1.0 - z * z) * pp * pp);
+    legendre_pn(n, z, p1, p2);
+    const double pp = n * (z * p1 - p2) / (z * z - 1.0);
+    const double wt = 2.0 / ((1.0 - z * z) * pp * pp);
     x[i] = 0.5 * (1.0 - z);      // ascending on (0,1)
     x[n - 1 - i] = 0.5 * (1.0 + z);
     w[i] = 0.5 * wt;

@@ -1529,13 +1529,13 @@ int omega_integral(double* out) {
   if (g->node_n != n || g->node_scale != c.omega_scale || !g->node_z) {
     g->nodes.release();
     g->node_n = 0;
-    double *s, *w;
-    if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = g->nodes.alloc(&g->node_z, n)) ||
-        (rc = g->nodes.alloc(&g->node_w, n))) {
+    double *s, *w, *inv;
+    if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = ar.alloc(&inv, n + 1)) ||
+        (rc = g->nodes.alloc(&g->node_z, n)) || (rc = g->nodes.alloc(&g->node_w, n))) {
       ar.release();
       return rc;
     }
-    launch_gauss_legendre(n, s, w, g->st);
+    launch_gauss_legendre(n, inv, s, w, g->st);
     launch_omega_nodes(n, c.omega_scale, s, w, g->node_z, g->node_w, g->st);
     g->node_n = n;
     g->node_scale = c.omega_scale;

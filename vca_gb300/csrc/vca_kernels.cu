@@ -797,42 +797,52 @@ void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, do
 
 // Gauss-Legendre nodes/weights on (0,1): Newton on P_n from
 // cos(pi (i+3/4)/(n+1/2)), ascending nodes.
-__global__ void k_gauss_legendre(int n, double* x, double* w) {
+// Gauss-Legendre nodes/weights on (0,1): Newton on P_n from the classical
+// initial guess cos(pi(i+3/4)/(n+1/2)), P_n by the three-term recurrence
+// with the reciprocals 1/j from a table (no division in the loop).  Newton
+// converges quadratically from that guess; the loop ends once the step is at
+// rounding level (at most 12 steps: near +-1 the step need not fall below
+// 1e-16) and P_n is evaluated once more for the weight.
+__global__ void k_recip_table(int n, double* inv) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j <= n; j += gridDim.x * blockDim.x)
+    inv[j] = j ? 1.0 / (double)j : 0.0;
+}
+__device__ __forceinline__ void legendre_pair(int n, double z, const double* __restrict__ inv, double* pn,
+                                              double* pn1) {
+  double p1 = 1.0, p2 = 0.0;
+  for (int j = 1; j <= n; j++) {
+    const double p3 = p2;
+    p2 = p1;
+    p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) * inv[j];
+  }
+  *pn = p1;
+  *pn1 = p2;
+}
+__global__ void k_gauss_legendre(int n, const double* inv, double* x, double* w) {
   const int half = (n + 1) / 2;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < half; i += gridDim.x * blockDim.x) {
-    double z = cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0.0;
-    for (int it = 0; it < 100; it++) {
-      double p1 = 1.0, p2 = 0.0;
-      for (int j = 1; j <= n; j++) {
-        double p3 = p2;
-        p2 = p1;
-        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-      }
-      pp = n * (z * p1 - p2) / (z * z - 1.0);
-      double z1 = z;
-      z = z1 - p1 / pp;
-      if (fabs(z - z1) < 1e-16) {
-        p1 = 1.0;
-        p2 = 0.0;
-        for (int j = 1; j <= n; j++) {
-          double p3 = p2;
-          p2 = p1;
-          p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-        }
-        pp = n * (z * p1 - p2) / (z * z - 1.0);
-        break;
-      }
+    double z = cos(M_PI * (i + 0.75) / (n + 0.5)), p1, p2;
+    for (int it = 0; it < 12; it++) {
+      legendre_pair(n, z, inv, &p1, &p2);
+      const double pp = n * (z * p1 - p2) / (z * z - 1.0);
+      const double dz = p1 / pp;
+      z -= dz;
+      if (fabs(dz) <= 2.5e-16) break;
     }
-    double wt = 2.0 / ((1.0 - z * z) * pp * pp);
+    legendre_pair(n, z, inv, &p1, &p2);
+    const double pp = n * (z * p1 - p2) / (z * z - 1.0);
+    const double wt = 2.0 / ((1.0 - z * z) * pp * pp);
     x[i] = 0.5 * (1.0 - z);
     x[n - 1 - i] = 0.5 * (1.0 + z);
     w[i] = 0.5 * wt;
     w[n - 1 - i] = 0.5 * wt;
   }
 }
-void launch_gauss_legendre(int n, double* x, double* w, cudaStream_t st) {
+void launch_gauss_legendre(int n, double* inv, double* x, double* w, cudaStream_t st) {
   COUNT_LAUNCH();
-  k_gauss_legendre<<<nblocks((n + 1) / 2, 128), 128, 0, st>>>(n, x, w);
+  k_recip_table<<<nblocks(n + 1, 256), 256, 0, st>>>(n, inv);
+  COUNT_LAUNCH();
+  k_gauss_legendre<<<nblocks((n + 1) / 2, 64), 64, 0, st>>>(n, inv, x, w);
 }
 
 // Delta_bath(z) = V [(z+xmu) - h]^{-1} V^dag (VCA_BATH_FUNCTIONS.f90:127-150);

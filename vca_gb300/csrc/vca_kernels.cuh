@@ -159,8 +159,8 @@ void launch_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const d
                           cudaStream_t st);
 void launch_reduce_rows(int nrows, int ncols, const double* in, double scale, double* out,
                         cudaStream_t st);
-// Gauss-Legendre nodes on (0,1)
-void launch_gauss_legendre(int n, double* x, double* w, cudaStream_t st);
+// Gauss-Legendre nodes on (0,1); inv: work array of n+1 doubles
+void launch_gauss_legendre(int n, double* inv, double* x, double* w, cudaStream_t st);
 // Delta_bath(z) (VCA_BATH_FUNCTIONS.f90:127-150) for nz points, lso N x N
 void launch_delta_bath(int nz, const double2* z, int N, int Nb, const double2* hb, const double2* V,
                        double xmu, double2* work, double2* out, cudaStream_t st);
