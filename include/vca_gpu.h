@@ -240,6 +240,22 @@ int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out);
  * complex points z (interleaved re, im); f_out complex[nz]. */
 int vca_gpu_sum_kmesh_complex(const double* z, int64_t nz, double* f_out);
 
+/*
+ * One custom observable of the last solve: init_custom_observables /
+ * add_custom_observable / get_custom_observables (VCA_OBSERVABLES.f90:
+ * 89-170) for a single item, whose value the reference prints and writes
+ * (write_custom_observables).  s is (Nlat,Nlat,Nspin,Nspin,Norb,Norb)
+ * complex, the same at every k (kdep = 0, add_custom_observable_local), or
+ * (...,Nk) (kdep = 1, add_custom_observable_kdep).  With the lattice
+ * G_k(z) = (G'(z)^-1 - (H_k - Hloc - Delta(z)))^-1 the value is, at T=0,
+ * (3-Nspin)/pi * int_0^inf (1/Lk) sum_k Re{Tr[s_k G_k(iw)] - Tr[s_k]/(iw -
+ * 1.1)} dw (:337-347, :408-452) on the fixed rule of the Omega integral; at
+ * finite T the Matsubara sum up to nmax plus the contour over the whole
+ * circle |w| = R (:351-388, :454-500) with the reference's real part of the
+ * trace, times (3-Nspin).
+ */
+int vca_gpu_custom_observable(const double* s, int32_t kdep, double* value);
+
 /* Thermal bookkeeping of the last solve. */
 typedef struct vca_thermal {
   double zeta;           /* zeta_function (VCA_DIAG.f90:357-363), before trimming */

@@ -75,6 +75,8 @@ def lib():
             "orc_contour_integrand": (D, [P, D, D]),
             "orc_frequency_integration_finite_t": (D, [P]),
             "orc_thermal": (I, [P, dp, ip]),
+            "orc_custom_observable": (D, [P, dp, I]),
+            "orc_sum_observable_kmesh": (D, [P, D, D, dp, I, I]),
             "orc_set_threads": (I, [I]),
         }
         for name, (res, args) in sig.items():
@@ -313,6 +315,16 @@ class Oracle:
 
     def frequency_integration_finite_t(self) -> float:
         return self.L.orc_frequency_integration_finite_t(self.h)
+
+    def custom_observable(self, s) -> float:
+        """One custom observable of the last solve; s (Nlat,Nlat,Nspin,Nspin,Norb,Norb[,Nk])."""
+        s = np.asfortranarray(s, dtype=np.complex128)
+        return self.L.orc_custom_observable(self.h, _dp(s), 1 if s.ndim == 7 else 0)
+
+    def sum_observable_kmesh(self, z: complex, s, tail: bool) -> float:
+        s = np.asfortranarray(s, dtype=np.complex128)
+        return self.L.orc_sum_observable_kmesh(self.h, float(np.real(z)), float(np.imag(z)), _dp(s),
+                                               1 if s.ndim == 7 else 0, 1 if tail else 0)
 
     def thermal(self) -> dict:
         """The fields of vca_thermal for the last solve."""

@@ -1412,6 +1412,76 @@ double frequency_integration_finite_t(Oracle& o) {
   return (3.0 - c.Nspin) * (out + integral);
 }
 
+// ---------------------------------------------------------------------------
+// Custom observables (VCA_OBSERVABLES.f90:335-500).
+// ---------------------------------------------------------------------------
+// sum_observable_kmesh (:408-452, tail = true, z = i w) and
+// sum_observable_kmesh_complex (:454-500, tail = false): (1/Lk) sum_k
+// Re{Tr[s_k G_k(z)] - tail Tr[s_k]/(z - 1.1)}, G_k = (G'^-1 - (H_k - Hloc -
+// Delta))^-1.  s: nnn layout, one matrix (stride 0) or one per k.
+double sum_observable_kmesh(const Oracle& o, cd z, const std::vector<cd>& s, bool kdep, bool tail) {
+  const int N = o.Nlso;
+  std::vector<cd> gf, Gi, Dl, Hl;
+  gf_cluster(o, z, gf);
+  to_lso(o, gf.data(), Gi);
+  lu_inv(N, Gi);
+  delta_bath(o, z, Dl);
+  to_lso(o, o.Hloc.data(), Hl);
+  const size_t nel = (size_t)o.cfg.Nlat * o.cfg.Nlat * o.cfg.Nspin * o.cfg.Nspin * o.cfg.Norb * o.cfg.Norb;
+  double out = 0.0;
+#pragma omp parallel for reduction(+ : out) schedule(static)
+  for (int64_t ik = 0; ik < o.Nk; ik++) {
+    std::vector<cd> Hkl, Sl, A((size_t)N * N);
+    to_lso(o, o.Hk.data() + ik * nel, Hkl);
+    to_lso(o, s.data() + (kdep ? ik * nel : 0), Sl);
+    for (size_t q = 0; q < A.size(); q++) A[q] = Gi[q] - (Hkl[q] - Hl[q] - Dl[q]);
+    lu_inv(N, A);
+    cd tr = 0.0, ts = 0.0;
+    for (int i = 0; i < N; i++) {
+      for (int j = 0; j < N; j++) tr += Sl[i + (size_t)j * N] * A[j + (size_t)i * N];
+      ts += Sl[i + (size_t)i * N];
+    }
+    if (tail) tr -= ts / (z - 1.1);
+    out += tr.real();
+  }
+  return out / (double)o.Nk;
+}
+
+// calculate_observable_integral_zero_t (:337-347) on the fixed rule, and
+// calculate_observable_integral_finite_t (:351-388) with the contour over
+// the whole circle (quad from -pi to pi): the rule of contour_rule on the
+// upper half and its mirror image
+double custom_observable(const Oracle& o, const std::vector<cd>& s, bool kdep) {
+  const vca_config& c = o.cfg;
+  if (!o.finiteT) {
+    std::vector<double> x, ws;
+    gauss_legendre01(c.omega_nodes, x, ws);
+    const double sc = c.omega_scale;
+    double acc = 0.0;
+    for (int i = 0; i < c.omega_nodes; i++) {
+      const double om = sc * x[i] / (1.0 - x[i]);
+      const double jac = sc / ((1.0 - x[i]) * (1.0 - x[i]));
+      acc += ws[i] * jac * sum_observable_kmesh(o, cd(0.0, om), s, kdep, true);
+    }
+    return (3.0 - c.Nspin) * acc / M_PI;
+  }
+  const double beta = c.beta, mu = c.xmu;
+  double out = 0.0;
+  for (int n = 0; n <= o.nmax; n++) out += sum_observable_kmesh(o, cd(0.0, (2.0 * n + 1.0) * M_PI / beta), s, kdep, false);
+  out = 2.0 * (1.0 / beta) * out;
+  std::vector<double> th, wt;
+  contour_rule(o.R, beta, mu, c.contour_nodes, th, wt);
+  double integral = 0.0;
+  for (int half = 0; half < 2; half++)
+    for (size_t i = 0; i < th.size(); i++) {
+      const cd w = o.R * std::exp(XI * (half ? -th[i] : th[i]));
+      cd fermi = 0.0;
+      if (((w - mu) * beta).real() < 100.0) fermi = 1.0 / (std::exp(beta * (w - mu)) + 1.0);
+      integral += wt[i] * ((1.0 / M_PI) * w * fermi * sum_observable_kmesh(o, w, s, kdep, false)).real();
+    }
+  return (3.0 - c.Nspin) * (out + integral);
+}
+
 // Omega' (VCA_MAIN.f90:186-193)
 double omega_prime(const Oracle& o) {
   if (!o.finiteT) return o.egs;
@@ -1654,6 +1724,20 @@ int orc_contour_rule(double R, double beta, double mu, int ngl, double* th, doub
 }
 double orc_contour_integrand(void* h, double R, double theta) { return contour_integrand(*(Oracle*)h, R, theta); }
 double orc_frequency_integration_finite_t(void* h) { return frequency_integration_finite_t(*(Oracle*)h); }
+double orc_custom_observable(void* h, const double* s, int kdep) {
+  Oracle* o = (Oracle*)h;
+  const size_t nel = (size_t)o->cfg.Nlat * o->cfg.Nlat * o->cfg.Nspin * o->cfg.Nspin * o->cfg.Norb * o->cfg.Norb;
+  std::vector<cd> sv;
+  copy_c(s, nel * (kdep ? (size_t)o->Nk : 1), sv);
+  return custom_observable(*o, sv, kdep != 0);
+}
+double orc_sum_observable_kmesh(void* h, double zr, double zi, const double* s, int kdep, int tail) {
+  Oracle* o = (Oracle*)h;
+  const size_t nel = (size_t)o->cfg.Nlat * o->cfg.Nlat * o->cfg.Nspin * o->cfg.Nspin * o->cfg.Norb * o->cfg.Norb;
+  std::vector<cd> sv;
+  copy_c(s, nel * (kdep ? (size_t)o->Nk : 1), sv);
+  return sum_observable_kmesh(*o, cd(zr, zi), sv, kdep != 0, tail != 0);
+}
 // zeta, omega_prime, e_min, max_exc, R, sum part, contour part; nmax,
 // nstates_total, contour points, finite_t (the fields of vca_thermal)
 int orc_thermal(void* h, double* d7, int* i4) {

@@ -1432,25 +1432,15 @@ bool omega_pairs_valid() {
   return true;
 }
 
-// Omega integrand at n device points d_z (sum_kmesh / sum_kmesh_complex,
-// VCA_OMEGA.f90:37-114): on return *f_re[i] = (1/Nk) sum_k ln|det(1 + (Delta
-// + Hloc - Hk) G'(z_i))| and, when want_im, *f_im[i] = (1/Nk) sum_k arg det
-// (principal), both device arrays owned by ar.
-int ksum_device(int n, const double2* d_z, bool want_im, Arena& ar, double** f_re, double** f_im) {
+// P(z) = Hloc + Delta(z) in lso at n device points (VCA_OMEGA.f90:62-66)
+int hloc_delta(int n, const double2* d_z, Arena& ar, double2** P_out) {
   const vca_config& c = g->cfg;
-  const int64_t Nk = g->Nk;
   const int N = g->N, NN = N * N;
   int rc = VCA_OK;
-  double2 *Glso, *P, *D = nullptr, *Hl;
-  if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = ar.alloc(&P, (size_t)n * NN)) || (rc = ar.alloc(&Hl, NN)))
-    return rc;
-  RCHK(gf_lso(n, d_z, Glso, ar));
-  {  // Hloc in lso
-    double2* hraw;
-    RCHK(ar.alloc(&hraw, NN));
-    cudaMemcpyAsync(hraw, g->Hloc.data(), sizeof(double2) * NN, cudaMemcpyHostToDevice, g->st);
-    launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, 1, hraw, Hl, g->st);
-  }
+  double2 *P, *D = nullptr, *Hl, *hraw;
+  if ((rc = ar.alloc(&P, (size_t)n * NN)) || (rc = ar.alloc(&Hl, NN)) || (rc = ar.alloc(&hraw, NN))) return rc;
+  cudaMemcpyAsync(hraw, g->Hloc.data(), sizeof(double2) * NN, cudaMemcpyHostToDevice, g->st);
+  launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, 1, hraw, Hl, g->st);
   if (g->has_bath) {  // Delta(z)
     std::vector<double2> hb, V;
     bath_lso(hb, V);
@@ -1464,6 +1454,23 @@ int ksum_device(int n, const double2* d_z, bool want_im, Arena& ar, double** f_r
     launch_delta_bath(n, d_z, N, Nb, dhb, dV, c.xmu, work, D, g->st);
   }
   launch_add_hloc(n, NN, D, Hl, P, g->st);
+  *P_out = P;
+  return VCA_OK;
+}
+
+// Omega integrand at n device points d_z (sum_kmesh / sum_kmesh_complex,
+// VCA_OMEGA.f90:37-114): on return *f_re[i] = (1/Nk) sum_k ln|det(1 + (Delta
+// + Hloc - Hk) G'(z_i))| and, when want_im, *f_im[i] = (1/Nk) sum_k arg det
+// (principal), both device arrays owned by ar.
+int ksum_device(int n, const double2* d_z, bool want_im, Arena& ar, double** f_re, double** f_im) {
+  const vca_config& c = g->cfg;
+  const int64_t Nk = g->Nk;
+  const int N = g->N, NN = N * N;
+  int rc = VCA_OK;
+  double2 *Glso, *P;
+  if ((rc = ar.alloc(&Glso, (size_t)n * NN))) return rc;
+  RCHK(gf_lso(n, d_z, Glso, ar));
+  RCHK(hloc_delta(n, d_z, ar, &P));
   const bool blk = g->hk_spin_diag && point_spin_diagonal();
   const int nblk = blk ? c.Nspin : 1;
   const int nb = N / nblk;
@@ -1521,25 +1528,38 @@ int ksum_host(int n, const double2* zh, double* f_re, double* f_im) {
 // frequency_integration (VCA_OMEGA.f90:123-136) with the fixed rule w =
 // scale*s/(1-s) (Gauss-Legendre in s, nodes cached per context) replacing
 // the adaptive quad(imaginary_axis, 0, inf)
+// Nodes i*w_j and weights of the fixed rule on [0, inf), computed once per
+// context (they depend on omega_nodes and omega_scale only)
+int ensure_omega_nodes() {
+  const vca_config& c = g->cfg;
+  const int n = c.omega_nodes;
+  if (g->node_n == n && g->node_scale == c.omega_scale && g->node_z) return VCA_OK;
+  Arena ar;
+  int rc = VCA_OK;
+  g->nodes.release();
+  g->node_n = 0;
+  double *s, *w, *inv;
+  if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = ar.alloc(&inv, n + 1)) ||
+      (rc = g->nodes.alloc(&g->node_z, n)) || (rc = g->nodes.alloc(&g->node_w, n))) {
+    ar.release();
+    return rc;
+  }
+  launch_gauss_legendre(n, inv, s, w, g->st);
+  launch_omega_nodes(n, c.omega_scale, s, w, g->node_z, g->node_w, g->st);
+  const cudaError_t e = cudaStreamSynchronize(g->st);
+  ar.release();
+  CUCHK(e);
+  g->node_n = n;
+  g->node_scale = c.omega_scale;
+  return VCA_OK;
+}
+
 int omega_integral(double* out) {
   const vca_config& c = g->cfg;
+  RCHK(ensure_omega_nodes());
   Arena ar;
   int rc = VCA_OK;
   const int n = c.omega_nodes;
-  if (g->node_n != n || g->node_scale != c.omega_scale || !g->node_z) {
-    g->nodes.release();
-    g->node_n = 0;
-    double *s, *w, *inv;
-    if ((rc = ar.alloc(&s, n)) || (rc = ar.alloc(&w, n)) || (rc = ar.alloc(&inv, n + 1)) ||
-        (rc = g->nodes.alloc(&g->node_z, n)) || (rc = g->nodes.alloc(&g->node_w, n))) {
-      ar.release();
-      return rc;
-    }
-    launch_gauss_legendre(n, inv, s, w, g->st);
-    launch_omega_nodes(n, c.omega_scale, s, w, g->node_z, g->node_w, g->st);
-    g->node_n = n;
-    g->node_scale = c.omega_scale;
-  }
   double *f = nullptr, *acc = nullptr;
   if ((rc = ksum_device(n, g->node_z, false, ar, &f, nullptr)) || (rc = ar.alloc(&acc, 1))) {
     ar.release();
@@ -1693,6 +1713,119 @@ int omega_integral_finite_t(double* out) {
   g->contour_part = integral;
   g->contour_points = nc;
   *out = (3.0 - c.Nspin) * (sum + integral);
+  return VCA_OK;
+}
+
+// Custom-observable integrand at n device points (sum_observable_kmesh and
+// _complex, VCA_OBSERVABLES.f90:408-500): *f[i] = (1/Lk) sum_k Re{Tr[s_k
+// G_k(z_i)] - tail*Tr[s_k]/(z_i - 1.1)}, G_k = (G'^-1 - (H_k - Hloc -
+// Delta))^-1; d_s holds s_k in lso, sk_stride = N*N per k or 0.
+int obs_device(int n, const double2* d_z, bool tail, const double2* d_s, int64_t sk_stride, Arena& ar,
+               double** f) {
+  const vca_config& c = g->cfg;
+  const int N = g->N, NN = N * N;
+  const int64_t Nk = g->Nk;
+  int rc = VCA_OK;
+  double2 *Glso, *Ginv, *P;
+  if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = ar.alloc(&Ginv, (size_t)n * NN))) return rc;
+  RCHK(gf_lso(n, d_z, Glso, ar));
+  launch_inverse_batch(n, N, Glso, Ginv, g->st);
+  RCHK(hloc_delta(n, d_z, ar, &P));
+  const bool blk = g->hk_spin_diag && point_spin_diagonal();
+  const int nblk = blk ? c.Nspin : 1;
+  const int nb = N / nblk;
+  if (nb > 32) VFAIL(VCA_ERR_UNSUPPORTED, "custom observables support spin blocks up to 32 orbitals");
+  const int kchunks = (int)std::max<int64_t>(1, std::min<int64_t>(Nk, (152 * 8 + n - 1) / n));
+  double* fpart;
+  if ((rc = ar.alloc(&fpart, (size_t)n * kchunks)) || (rc = ar.alloc(f, n))) return rc;
+  launch_obs_ksum(n, N, nblk, nb, d_z, Ginv, P, Nk, g->d_Hk, d_s, sk_stride, tail, fpart, kchunks, g->st);
+  launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, *f, g->st);
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
+
+// The same at n host points, result on the host
+int obs_host(int n, const double2* zh, bool tail, const double2* d_s, int64_t sk_stride, double* f_host) {
+  Arena ar;
+  double2* d_z;
+  double* f = nullptr;
+  int rc = ar.alloc(&d_z, n);
+  if (!rc) rc = cudaMemcpyAsync(d_z, zh, sizeof(double2) * n, cudaMemcpyHostToDevice, g->st) == cudaSuccess
+                    ? VCA_OK : VCA_ERR_CUDA;
+  if (!rc) rc = obs_device(n, d_z, tail, d_s, sk_stride, ar, &f);
+  if (!rc) {
+    cudaMemcpyAsync(f_host, f, sizeof(double) * n, cudaMemcpyDeviceToHost, g->st);
+    if (cudaStreamSynchronize(g->st) != cudaSuccess) rc = VCA_ERR_CUDA;
+  }
+  ar.release();
+  if (rc == VCA_ERR_CUDA) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  return rc;
+}
+
+// One custom observable of the last solve (get_custom_observables with one
+// item, VCA_OBSERVABLES.f90:140-170).  T=0 (:337-347): (3-Nspin)/pi times
+// the integral over [0, inf) of the tail-subtracted integrand, on the fixed
+// rule of the Omega integral.  Finite T (:351-388): 2/beta sum_{n<=nmax} of
+// the integrand at i w_n plus the integral of Re[(1/pi) w fermi(w - xmu)
+// F(w)] over the whole circle |w| = R (quad from -pi to pi), F taken real as
+// the reference's DREAL does, times (3-Nspin); nmax and R as for Omega.
+int custom_observable(const double* s_host, bool kdep, double* value) {
+  const vca_config& c = g->cfg;
+  const int N = g->N, NN = N * N;
+  const int64_t L = kdep ? g->Nk : 1;
+  Arena ar;
+  double2 *sraw, *slso;
+  int rc = VCA_OK;
+  if ((rc = ar.alloc(&sraw, (size_t)L * NN)) || (rc = ar.alloc(&slso, (size_t)L * NN))) { ar.release(); return rc; }
+  CUCHK(cudaMemcpyAsync(sraw, s_host, sizeof(double2) * (size_t)L * NN, cudaMemcpyHostToDevice, g->st));
+  launch_nnn2lso(c.Nlat, c.Nspin, c.Norb, L, sraw, slso, g->st);
+  const int64_t stride = kdep ? NN : 0;
+  if (!g->finiteT) {
+    if ((rc = ensure_omega_nodes())) { ar.release(); return rc; }
+    const int n = c.omega_nodes;
+    double *f = nullptr, *acc = nullptr;
+    if ((rc = obs_device(n, g->node_z, true, slso, stride, ar, &f)) || (rc = ar.alloc(&acc, 1))) {
+      ar.release();
+      return rc;
+    }
+    launch_wsum(n, g->node_w, f, acc, g->st);
+    double integral = 0.0;
+    cudaMemcpyAsync(&integral, acc, sizeof(double), cudaMemcpyDeviceToHost, g->st);
+    const cudaError_t e = cudaStreamSynchronize(g->st);
+    ar.release();
+    CUCHK(e);
+    *value = (3.0 - c.Nspin) * integral / M_PI;
+    return VCA_OK;
+  }
+  const double beta = c.beta, mu = c.xmu, R = g->int_R;
+  const int nmax = g->nmax;
+  std::vector<double2> zm(nmax + 1);
+  for (int n = 0; n <= nmax; n++) zm[n] = make_double2(0.0, (2.0 * n + 1.0) * M_PI / beta);
+  std::vector<double> fm(nmax + 1);
+  if ((rc = obs_host(nmax + 1, zm.data(), false, slso, stride, fm.data()))) { ar.release(); return rc; }
+  double out = 0.0;
+  for (int n = 0; n <= nmax; n++) out += fm[n];
+  out = 2.0 * (1.0 / beta) * out;
+  std::vector<double> th, wt;
+  contour_nodes_host(R, beta, mu, c.contour_nodes, th, wt);
+  const int nh = (int)th.size();
+  std::vector<double2> zc(2 * nh);  // the upper half, then its mirror image
+  for (int i = 0; i < nh; i++) {
+    zc[i] = make_double2(R * std::cos(th[i]), R * std::sin(th[i]));
+    zc[nh + i] = make_double2(zc[i].x, -zc[i].y);
+  }
+  std::vector<double> fc(2 * nh);
+  rc = obs_host(2 * nh, zc.data(), false, slso, stride, fc.data());
+  ar.release();
+  if (rc) return rc;
+  double integral = 0.0;
+  for (int i = 0; i < 2 * nh; i++) {
+    const cd w(zc[i].x, zc[i].y);
+    cd fermi = 0.0;
+    if (((w - mu) * beta).real() < 100.0) fermi = 1.0 / (std::exp(beta * (w - mu)) + 1.0);
+    integral += wt[i % nh] * ((1.0 / M_PI) * w * fermi * fc[i]).real();
+  }
+  *value = (3.0 - c.Nspin) * (out + integral);
   return VCA_OK;
 }
 
@@ -2321,6 +2454,13 @@ int vca_gpu_sum_kmesh_complex(const double* z, int64_t nz, double* f_out) {
   RCHK(ksum_host((int)nz, zh.data(), re.data(), im.data()));
   for (int64_t i = 0; i < nz; i++) { f_out[2 * i] = re[i]; f_out[2 * i + 1] = im[i]; }
   return VCA_OK;
+}
+
+int vca_gpu_custom_observable(const double* s, int32_t kdep, double* value) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!s || !value) VFAIL(VCA_ERR_ARG, "NULL argument");
+  RCHK(check_finite(s, 2 * (size_t)g->N * g->N * (kdep ? (size_t)g->Nk : 1), "s"));
+  return custom_observable(s, kdep != 0, value);
 }
 
 int vca_gpu_get_thermal(vca_thermal* out) {

@@ -1320,6 +1320,120 @@ __device__ void warp_gj_inverse(double2* M, int N) {
   }
 }
 
+// out[q] = A[q]^-1 for nz N x N matrices (lso, column-major), one warp each
+__global__ void k_inverse_batch(int nz, int N, const double2* A, double2* out) {
+  extern __shared__ double2 gjm[];
+  const int q = blockIdx.x;
+  if (q >= nz) return;
+  const int lane = threadIdx.x & 31;
+  const int NN = N * N;
+  for (int c = 0; c < N; c++)
+    if (lane < N) {
+      gjm[c * 32 + lane] = A[(int64_t)q * NN + lane + c * N];
+      gjm[(N + c) * 32 + lane] = make_double2(lane == c ? 1.0 : 0.0, 0.0);
+    }
+  __syncwarp();
+  warp_gj_inverse(gjm, N);
+  for (int c = 0; c < N; c++)
+    if (lane < N) out[(int64_t)q * NN + lane + c * N] = gjm[(N + c) * 32 + lane];
+}
+void launch_inverse_batch(int nz, int N, const double2* A, double2* out, cudaStream_t st) {
+  if (nz <= 0) return;
+  COUNT_LAUNCH();
+  const size_t shm = sizeof(double2) * 2 * (size_t)N * 32;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_inverse_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    attr = true;
+  }
+  k_inverse_batch<<<nz, 32, shm, st>>>(nz, N, A, out);
+}
+
+// Custom-observable integrand (sum_observable_kmesh / _complex,
+// VCA_OBSERVABLES.f90:408-500): fpart[w][chunk] = sum over the chunk's k of
+// Re{ Tr[s_k G_k(z_w)] - tail * Tr[s_k] / (z_w - 1.1) } with the lattice
+// G_k = (G'^-1 - (H_k - P))^-1, P = Hloc + Delta.  G_k is inverted per spin
+// block (nblk blocks of nb) by one warp (Gauss-Jordan); s_k is read only on
+// the blocks (the trace with a block-diagonal G_k needs no more).  s holds
+// one matrix per k (sk_stride = N*N) or one for all (sk_stride = 0).
+__global__ void __launch_bounds__(128) k_obs_ksum(int N, int nblk, int nb, const double2* z, const double2* Ginv,
+                                                  const double2* P, int64_t Nk, const double2* Hk, const double2* s,
+                                                  int64_t sk_stride, int tail, double* fpart, int kchunks) {
+  extern __shared__ double2 shm[];
+  const int w = blockIdx.y;
+  const int chunk = blockIdx.x;
+  const int NN = N * N;
+  double2* Gs = shm;
+  double2* Ps = shm + NN;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  double2* M = shm + 2 * NN + (int64_t)warp * 2 * nb * 32;
+  for (int t = threadIdx.x; t < NN; t += blockDim.x) {
+    Gs[t] = Ginv[(int64_t)w * NN + t];
+    Ps[t] = P[(int64_t)w * NN + t];
+  }
+  __syncthreads();
+  const double2 zw = z[w];
+  // 1/(z - 1.1)
+  const double dr = zw.x - 1.1, di = zw.y, dd = dr * dr + di * di;
+  const double2 rz = make_double2(dr / dd, -di / dd);
+  const int64_t k0 = (Nk * chunk) / kchunks, k1 = (Nk * (chunk + 1)) / kchunks;
+  double acc = 0.0;
+  for (int64_t k = k0 + warp; k < k1; k += nwarps) {
+    const double2* H = Hk + k * NN;
+    const double2* S = s + k * sk_stride;
+    double tr = 0.0;
+    for (int b = 0; b < nblk; b++) {
+      const int off = b * nb;
+      for (int c = 0; c < nb; c++)
+        if (lane < nb) {
+          const int il = (off + lane) + (off + c) * N;
+          const double2 g = Gs[il], h = H[il], p = Ps[il];
+          M[c * 32 + lane] = make_double2(g.x - (h.x - p.x), g.y - (h.y - p.y));
+          M[(nb + c) * 32 + lane] = make_double2(lane == c ? 1.0 : 0.0, 0.0);
+        }
+      __syncwarp();
+      warp_gj_inverse(M, nb);
+      // Tr[s G] over the block: sum_{i,j} s(i,j) G(j,i), lane = i
+      if (lane < nb)
+        for (int j = 0; j < nb; j++) {
+          const double2 sv = S[(off + lane) + (off + j) * N];
+          const double2 gv = M[(nb + lane) * 32 + j];  // G(j, lane)
+          tr += sv.x * gv.x - sv.y * gv.y;
+        }
+      __syncwarp();
+    }
+    if (tail && lane < N) {  // - Re[ s(lane,lane) / (z - 1.1) ]
+      const double2 sv = S[lane + lane * N];
+      tr -= sv.x * rz.x - sv.y * rz.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    if (lane == 0) acc += tr;
+  }
+  __shared__ double red[32];
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int q = 0; q < nwarps; q++) sacc += red[q];
+    fpart[(int64_t)w * kchunks + chunk] = sacc;
+  }
+}
+void launch_obs_ksum(int nw, int N, int nblk, int nb, const double2* z, const double2* Ginv, const double2* P,
+                     int64_t Nk, const double2* Hk, const double2* s, int64_t sk_stride, bool tail, double* fpart,
+                     int kchunks, cudaStream_t st) {
+  COUNT_LAUNCH();
+  const int threads = 128;
+  const size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * 2 * nb * 32);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_obs_ksum, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  k_obs_ksum<<<dim3(kchunks, nw, 1), threads, shm, st>>>(N, nblk, nb, z, Ginv, P, Nk, Hk, s, sk_stride, tail ? 1 : 0,
+                                                         fpart, kchunks);
+}
+
 // want_g0 = 0: out = Sigma(z); 1: out = G0(z).  P = Delta + Hloc (lso, per z
 // when per_z_p, else one matrix).
 __global__ void k_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const double2* P, int per_z_p,

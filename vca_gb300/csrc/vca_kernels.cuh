@@ -149,6 +149,14 @@ void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const
 // VCA_GF_NORMAL.f90:1045-1111.  N <= 32.
 void launch_sigma_g0(int nz, int N, const double2* z, const double2* Glso, const double2* P, bool per_z_p,
                      double xmu, bool want_g0, double2* out, cudaStream_t st);
+// out[q] = A[q]^-1 (nz N x N complex, N <= 32)
+void launch_inverse_batch(int nz, int N, const double2* A, double2* out, cudaStream_t st);
+// custom-observable integrand partials (sum_observable_kmesh,
+// VCA_OBSERVABLES.f90:408-500): fpart[w][chunk] = sum_k Re{Tr[s_k G_k(z_w)]
+// - tail*Tr[s_k]/(z_w - 1.1)}, G_k = (Ginv_w - (H_k - P_w))^-1 per spin block
+void launch_obs_ksum(int nw, int N, int nblk, int nb, const double2* z, const double2* Ginv, const double2* P,
+                     int64_t Nk, const double2* Hk, const double2* s, int64_t sk_stride, bool tail, double* fpart,
+                     int kchunks, cudaStream_t st);
 // Ground-state observable partials of one state: part[(q*nimp + l)*nb + b]
 // for q = n_up, n_dw, n_up*n_dw, bit l, block b < observables_blocks(D)
 int observables_blocks(int64_t D);

@@ -35,7 +35,7 @@ EXPORTS = [
     "vca_gpu_get_docc", "vca_gpu_get_mag",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
-    "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal",
+    "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
 ]
 
 
@@ -102,6 +102,7 @@ def load(path: Optional[str] = None):
         "vca_gpu_sum_kmesh": (ctypes.c_int, [dp, i64, dp]),
         "vca_gpu_sum_kmesh_complex": (ctypes.c_int, [dp, i64, dp]),
         "vca_gpu_get_thermal": (ctypes.c_int, [ctypes.POINTER(VcaThermal)]),
+        "vca_gpu_custom_observable": (ctypes.c_int, [dp, i32, dp]),
         "vca_gpu_finalize": (ctypes.c_int, []),
         "vca_gpu_last_error": (ctypes.c_int, [ctypes.c_char_p, i32]),
         "vca_gpu_sector_info": (ctypes.c_int, [i32, ctypes.POINTER(i32), ctypes.POINTER(i32),
@@ -356,6 +357,42 @@ class VcaSolver:
         out = np.zeros(len(z), dtype=np.complex128)
         check(self.L.vca_gpu_sum_kmesh_complex(_dp(z), len(z), _dp(out)))
         return out
+
+    def custom_observable(self, s) -> float:
+        """Value of one custom observable for the last solve: s has shape
+        (Nlat,Nlat,Nspin,Nspin,Norb,Norb) (the same at every k) or
+        (...,Nk) (k-dependent), as add_custom_observable takes it."""
+        s = np.asfortranarray(s, dtype=np.complex128)
+        kdep = 1 if s.ndim == 7 else 0
+        if s.shape[:6] != hloc_shape(self.cfg):
+            raise ValueError(f"s has shape {s.shape}, expected {hloc_shape(self.cfg)}[+ (Nk,)]")
+        out = ctypes.c_double()
+        check(self.L.vca_gpu_custom_observable(_dp(s), kdep, ctypes.byref(out)))
+        return out.value
+
+    # custom-observable registry with the reference's call sequence
+    # (init_custom_observables, add_custom_observable, get_custom_observables,
+    # clear_custom_observables, VCA_OBSERVABLES.f90:81-189)
+    def init_custom_observables(self, n: int, nk: int):
+        self._custom = {"asked": int(n), "nk": int(nk), "items": []}
+
+    def add_custom_observable(self, name: str, s):
+        if not getattr(self, "_custom", None):
+            raise VcaError(-3, "add_custom_observable: custom observables not initialized")
+        if len(self._custom["items"]) >= self._custom["asked"]:
+            raise VcaError(-9, "add_custom_observable: too many observables given")
+        s = np.asfortranarray(s, dtype=np.complex128)
+        if s.ndim == 7 and s.shape[6] != self._custom["nk"]:
+            raise ValueError("add_custom_observable: k-dependent s must have Nk matrices")
+        self._custom["items"].append((name, s))
+
+    def get_custom_observables(self) -> dict:
+        if not getattr(self, "_custom", None):
+            return {}
+        return {name: self.custom_observable(s) for name, s in self._custom["items"]}
+
+    def clear_custom_observables(self):
+        self._custom = None
 
     def thermal(self) -> dict:
         """zeta, Omega', E_min, max_exc, contour radius, Matsubara and contour
