@@ -230,3 +230,22 @@ def test_observables_match_oracle(name):
     got, ref = s.observables(), o.observables()
     for key in ref:
         np.testing.assert_allclose(got[key], ref[key], rtol=0, atol=1e-10, err_msg=f"{name} {key}")
+
+
+@pytest.mark.parametrize("name", ["chain4", "square2x2_afm", "bhz_small"])
+def test_chan2_solve_matches_oracle(name):
+    """VCA_GF_SYMMETRIC=T: two channels per off-diagonal element
+    (lanc_build_gf_normal_mix_chan2, VCA_GF_NORMAL.f90:327-556) and the
+    recombination with chan4 = 0."""
+    pt = POINTS[name]()
+    pt.cfg.vca_gf_symmetric = 1
+    s = VcaSolver(pt.cfg, pt.bath_h, pt.bath_v)
+    om = s.solve(pt.Hloc, pt.Hk, pt.bath_h, pt.bath_v)
+    o = Oracle.from_point(pt)
+    ref, _, _ = o.solve()
+    assert abs(om - ref) <= E_TOL * abs(ref), (om, ref)
+    z = np.array([0.2j, 1.0j, 0.7 + 0.3j])
+    np.testing.assert_allclose(s.gf_cluster(z), o.gf_cluster(z), rtol=0, atol=G_TOL)
+    p, w = s.gf_channel(1, 2, 1, 1, 1, 1, 1)
+    assert len(p) > 0
+    assert len(s.gf_channel(1, 2, 1, 1, 1, 1, 3)[0]) == 0  # no third channel

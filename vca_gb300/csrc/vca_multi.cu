@@ -72,6 +72,26 @@ __device__ __forceinline__ i128 ms_sum_parts(const i64* tpart, int t0, int n) {
   return s;
 }
 
+// the same sum spread over the lanes of a warp (exact, any order), the
+// total returned to every lane
+__device__ __forceinline__ i128 ms_sum_parts_warp(const i64* tpart, int t0, int n) {
+  const int lane = threadIdx.x & 31;
+  i128 s = 0;
+  for (int t = t0 + lane; t < t0 + n; t += 32)
+    s += (i128)(((unsigned __int128)(u64)tpart[2 * t + 1] << 64) | (u64)tpart[2 * t]);
+  u64 lo = (u64)s;
+  i64 hi = (i64)(s >> 64);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const u64 lo2 = __shfl_xor_sync(0xffffffffu, lo, off);
+    const i64 hi2 = __shfl_xor_sync(0xffffffffu, hi, off);
+    const u64 sl = lo + lo2;
+    hi = hi + hi2 + (sl < lo ? 1 : 0);
+    lo = sl;
+  }
+  return ((i128)hi << 64) | (i128)lo;
+}
+
 // start vector: R_i = round(v_i * 2^40) with v_i the splitmix64 value of the
 // single-sector path; tpart = sum R^2
 __global__ void k_ms_start_raw(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
@@ -188,14 +208,20 @@ __global__ void __launch_bounds__(256) k_ms_hxv(const MsSector* secs, const int*
   }
 }
 
+// one warp per sector
 __global__ void k_ms_alpha(int nsec, const MsSector* secs, const ChainMeta* meta, const i64* tpart, int sexp,
                            int C, const double* bnow, double* alpha, i64* afx, i64* bfx) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsec; s += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nsec; s += nw) {
     if (!meta[s].active) continue;
-    const double a = 0.0 + ms_i128_to_double(ms_sum_parts(tpart, secs[s].tile0, secs[s].ntile), sexp);
-    alpha[s] = a;
-    afx[s] = __double2ll_rn(ldexp(1.0 * a, C));
-    bfx[s] = __double2ll_rn(ldexp(1.0 * bnow[s], C));
+    const i128 v = ms_sum_parts_warp(tpart, secs[s].tile0, secs[s].ntile);
+    if (lane == 0) {
+      const double a = 0.0 + ms_i128_to_double(v, sexp);
+      alpha[s] = a;
+      afx[s] = __double2ll_rn(ldexp(1.0 * a, C));
+      bfx[s] = __double2ll_rn(ldexp(1.0 * bnow[s], C));
+    }
   }
 }
 
@@ -226,10 +252,14 @@ __global__ void k_ms_update(const MsSector* secs, const int* tsec, const int64_t
 __global__ void k_ms_record(int nsec, const MsSector* secs, ChainMeta* meta, const i64* tpart, int sexp, int k,
                             const double* alpha, double* A, double* Bt, int ld, double tol, double* bnow,
                             int G, int F, i64* mul, int* msh) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsec; s += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nsec; s += nw) {
     ChainMeta mt = meta[s];
     if (!mt.active) continue;
-    const double b2 = 0.0 + ms_i128_to_double(ms_sum_parts(tpart, secs[s].tile0, secs[s].ntile), sexp);
+    const i128 v = ms_sum_parts_warp(tpart, secs[s].tile0, secs[s].ntile);
+    if (lane != 0) continue;
+    const double b2 = 0.0 + ms_i128_to_double(v, sexp);
     const double a = alpha[s];
     const double b = sqrt(fmax(b2, 0.0));
     A[(int64_t)s * ld + (k - 1)] = a;
@@ -297,7 +327,7 @@ void ms_launch_start(const MsGroup& gp, uint64_t seed, int F, i64* R, i64* X, i6
 
 void ms_launch_step(const MsGroup& gp, const FxScales& fs, int K, int k, double tol, MsBufs& b, cudaStream_t st) {
   const int nb = std::min(gp.ntiles, 152 * 8);
-  const int sb = (gp.nsec + 127) / 128;
+  const int sb = (gp.nsec * 32 + 127) / 128;  // one warp per sector
   for (int q = 0; q < 5; q++) count_launch_external();
   switch (K) {
     case 1: k_ms_hxv<1><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.X, b.YW, b.tpart); break;
