@@ -314,6 +314,8 @@ def run_gpu(args):
         s.close()
         out["hxv_single_4x4"] = hxv_single_4x4()
         out["finite_t"] = finite_t_sample(cpu=(world == 1 and not args.no_cpu))
+        out["c3_bath_plain"] = batch_sample("c3")
+        out["c4_bhz_plain"] = batch_sample("c4")
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample, _ = cpu_sample(pts[0], os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -363,6 +365,41 @@ def finite_t_sample(reps: int = 3, cpu: bool = True) -> dict:
         out["cpu_cores"] = threads
         out["omega_rel_diff"] = abs(om - ref) / abs(ref)
     return out
+
+
+def batch_sample(which: str) -> dict:
+    """Omega evals/s of the plain path (one point after another through
+    vca_gpu_solve_batch, H_k uploaded once) on the first points of the C3
+    batch (2x2 cluster + 8 bath levels, 24x24 k, 200-step chains, 4096-node
+    rule) or the C4 batch (BHZ 2x2, Norb=2, Nspin=2, 48x48 k, 200-step
+    chains, 4096-node rule), after one warm-up point."""
+    import numpy as np
+    from vca_gb300 import clusters
+    from vca_gb300.solver import VcaSolver
+    if which == "c3":
+        pts = clusters.batch_square_bath(B=5)
+        desc = "C3: 2x2 Hubbard + 8 bath levels, U=4, 24x24 k, 200-step chains, 4096 nodes"
+    else:
+        rng = np.random.Generator(np.random.PCG64(20261203 + 4))
+        prm = rng.uniform([1.5, -0.2], [2.5, 0.2], size=(17, 2))
+        base = clusters.bhz(mass=2.0, delta=0.0)  # H_k (48x48) is the same for every point
+        pts = [clusters.bhz(mass=p[0], delta=p[1], nk1=1) for p in prm]
+        for p in pts:
+            p.Hk = base.Hk
+        desc = "C4: BHZ 2x2, Norb=2, Nspin=2, 48x48 k, 200-step chains, 4096 nodes"
+    cfg = pts[0].cfg
+    s = VcaSolver(cfg, pts[0].bath_h, pts[0].bath_v)
+    s.solve(pts[0].Hloc, pts[0].Hk, pts[0].bath_h, pts[0].bath_v)
+    rest = pts[1:]
+    Hl = np.stack([p.Hloc for p in rest], axis=-1)
+    bh = np.stack([p.bath_h for p in rest], axis=-1) if rest[0].bath_h is not None else None
+    bv = np.stack([p.bath_v for p in rest], axis=-1) if rest[0].bath_v is not None else None
+    t0 = time.perf_counter()
+    om = s.solve_batch(Hl, rest[0].Hk, bh, bv)
+    dt = time.perf_counter() - t0
+    s.close()
+    return {"workload": desc, "points": len(rest), "value": len(rest) / dt, "unit": "Omega evals/s",
+            "ms_per_eval": round(1e3 * dt / len(rest), 1), "omega_first": float(om[0])}
 
 
 def hxv_single_4x4(reps: int = 10) -> dict:

@@ -920,6 +920,103 @@ int batched_sector_energies(std::vector<double>& energy) {
   return VCA_OK;
 }
 
+// All sector energies of the FP64 path (real or complex H) in batched
+// multi-sector Lanczos runs: one launch per phase over every sector of a
+// group (groups bounded to ~2^28 elements per vector); the single-sector
+// recurrence, start vectors and stopping rule.
+int batched_sector_energies_f64(std::vector<double>& energy) {
+  const vca_config& c = g->cfg;
+  const bool cplx = !g->real_model;
+  const size_t es = cplx ? sizeof(double2) : sizeof(double);
+  const int64_t cap = (int64_t)1 << 28;
+  energy.assign(g->Nsectors, INFINITY);
+  int s0 = 1;
+  while (s0 <= g->Nsectors) {
+    std::vector<MsSector> secs;
+    std::vector<int> tsec;
+    std::vector<int64_t> tstart;
+    int64_t tot = 0;
+    int nmaxg = 1;
+    int s1 = s0;
+    while (s1 <= g->Nsectors) {
+      const int nu = sec_nup(s1), nd = sec_ndw(s1);
+      const int64_t D = (int64_t)g->dimn[nu] * g->dimn[nd];
+      if (!secs.empty() && tot + D > cap) break;
+      MsSector m{};
+      m.sv = view_of(nu, nd);
+      m.off = tot;
+      m.D = D;
+      m.tile0 = (int)tsec.size();
+      m.isector = s1;
+      for (int64_t st = 0; st < D; st += MS_TILE) {
+        tsec.push_back((int)secs.size());
+        tstart.push_back(st);
+      }
+      m.ntile = (int)tsec.size() - m.tile0;
+      nmaxg = std::max(nmaxg, (int)std::min<int64_t>(D, std::min(c.lanc_niter, 512)));
+      secs.push_back(m);
+      tot += D;
+      s1++;
+    }
+    const int nsec = (int)secs.size(), ntiles = (int)tsec.size();
+    const int ld = nmaxg + 1;
+    Arena ar;
+    MsSector* d_secs;
+    int* d_tsec;
+    int64_t* d_tstart;
+    char *x0, *x1, *x2;
+    Ms64Bufs b{};
+    b.ld = ld;
+    int rc = VCA_OK;
+    if ((rc = ar.alloc(&d_secs, nsec)) || (rc = ar.alloc(&d_tsec, ntiles)) || (rc = ar.alloc(&d_tstart, ntiles)) ||
+        (rc = ar.alloc(&x0, (size_t)tot * es)) || (rc = ar.alloc(&x1, (size_t)tot * es)) ||
+        (rc = ar.alloc(&x2, (size_t)tot * es)) || (rc = ar.alloc(&b.tpart, ntiles)) ||
+        (rc = ar.alloc(&b.meta, nsec)) || (rc = ar.alloc(&b.alpha, nsec)) || (rc = ar.alloc(&b.bnow, nsec)) ||
+        (rc = ar.alloc(&b.invb, nsec)) || (rc = ar.alloc(&b.A, (size_t)nsec * ld)) ||
+        (rc = ar.alloc(&b.Bt, (size_t)nsec * ld)) || (rc = ar.alloc(&b.svec, (size_t)nsec * 5 * ld)) ||
+        (rc = ar.alloc(&b.theta, nsec)) || (rc = ar.alloc(&b.resid, nsec)) || (rc = ar.alloc(&b.state, nsec)) ||
+        (rc = ar.alloc(&b.mconv, nsec)) || (rc = ar.alloc(&b.undone, 1))) {
+      ar.release();
+      return rc;
+    }
+    b.X = x0;
+    b.Xp = x1;
+    b.Y = x2;
+    std::vector<ChainMeta> meta(nsec);
+    for (int q = 0; q < nsec; q++)
+      meta[q] = ChainMeta{1, q, (int)std::min<int64_t>(secs[q].D, std::min(c.lanc_niter, 512)), 1, 0};
+    cudaMemcpyAsync(d_secs, secs.data(), sizeof(MsSector) * nsec, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(d_tsec, tsec.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(d_tstart, tstart.data(), sizeof(int64_t) * ntiles, cudaMemcpyHostToDevice, g->st);
+    cudaMemcpyAsync(b.meta, meta.data(), sizeof(ChainMeta) * nsec, cudaMemcpyHostToDevice, g->st);
+    cudaMemsetAsync(b.A, 0, sizeof(double) * nsec * ld, g->st);
+    cudaMemsetAsync(b.Bt, 0, sizeof(double) * nsec * ld, g->st);
+    cudaMemsetAsync(b.bnow, 0, sizeof(double) * nsec, g->st);
+    cudaMemsetAsync(b.state, 0, sizeof(int) * nsec, g->st);
+    MsGroup gp{d_secs, d_tsec, d_tstart, nsec, ntiles};
+    m64_launch_start(gp, cplx, c.start_seed, b, g->st);
+    for (int k = 1; k <= nmaxg; k++) {
+      m64_launch_step(gp, cplx, g->md, k, c.gs_beta_tol, b, g->st);
+      if (k % std::max(1, c.gs_check_every) == 0 || k == nmaxg) {
+        cudaMemsetAsync(b.undone, 0, sizeof(int), g->st);
+        m64_launch_check(gp, b, c.gs_residual_tol, g->st);
+        int undone = 0;
+        cudaMemcpyAsync(&undone, b.undone, sizeof(int), cudaMemcpyDeviceToHost, g->st);
+        CUCHK(cudaStreamSynchronize(g->st));
+        if (undone == 0) break;
+      }
+    }
+    CUCHK(cudaGetLastError());
+    std::vector<double> th(nsec);
+    cudaMemcpyAsync(th.data(), b.theta, sizeof(double) * nsec, cudaMemcpyDeviceToHost, g->st);
+    CUCHK(cudaStreamSynchronize(g->st));
+    for (int q = 0; q < nsec; q++) energy[secs[q].isector - 1] = th[q];
+    ar.release();
+    s0 = s1;
+  }
+  return VCA_OK;
+}
+
 // vca_diag_c at T=0 with LANC_METHOD="lanczos" (VCA_DIAG.f90:49-267)
 // Finite T, one state per sector (LANC_METHOD="lanczos", Neigen = 1): the
 // annealing sweeps of VCA_DIAG.f90:78-256 insert every sector's lowest state
@@ -934,17 +1031,7 @@ int batched_sector_energies(std::vector<double>& energy) {
 int diagonalize_finite_t() {
   const vca_config& c = g->cfg;
   std::vector<double> E(g->Nsectors, INFINITY);
-  if (g->fx) {
-    RCHK(batched_sector_energies(E));
-  } else {
-    for (int isector = 1; isector <= g->Nsectors; isector++) {
-      Arena tmp;
-      void* vec = nullptr;
-      const int rc = sector_gs(isector, &E[isector - 1], &vec, tmp);
-      tmp.release();
-      if (rc) return rc;
-    }
-  }
+  RCHK(g->fx ? batched_sector_energies(E) : batched_sector_energies_f64(E));
   g->sector_e = E;
   struct Entry {
     double e;
@@ -1006,12 +1093,12 @@ int diagonalize() {
   if (g->finiteT) return diagonalize_finite_t();
   double oldzero = 1000.0;
   const double thr = c.gs_threshold;
-  // fixed-point path: every sector's energy from the batched search, then the
-  // T=0 list below needs vectors only for the sectors it keeps
+  // every sector's energy from the batched search (fixed point or FP64), then
+  // the T=0 list below needs vectors only for the sectors it keeps
   std::vector<double> eb;
   std::vector<char> keep_sec(g->Nsectors + 1, 1);
-  if (g->fx) {
-    RCHK(batched_sector_energies(eb));
+  {
+    RCHK(g->fx ? batched_sector_energies(eb) : batched_sector_energies_f64(eb));
     double oz = 1000.0;
     std::vector<int> lst;
     for (int isector = 1; isector <= g->Nsectors; isector++) {  // replay VCA_DIAG.f90:224-236
@@ -1026,22 +1113,18 @@ int diagonalize() {
     double e;
     void* vec = nullptr;
     Arena tmp;
-    if (g->fx && !keep_sec[isector]) {
+    if (!keep_sec[isector]) {
       g->sector_e[isector - 1] = eb[isector - 1];
       const double ee = eb[isector - 1];  // advance the running minimum exactly as below
       if (ee < oldzero - 10.0 * thr) { oldzero = ee; g->states.release(); g->gs.clear(); }
       else if (std::fabs(ee - oldzero) <= thr) oldzero = std::min(oldzero, ee);
       continue;
     }
-    if (g->fx) {
-      RCHK(sector_gs_fx(isector, &e, &vec, tmp));
-      // same fixed-point arithmetic and exact reductions: the two runs agree
-      if (std::fabs(e - eb[isector - 1]) > 1e-12 * std::max(1.0, std::fabs(e))) {
-        tmp.release();
-        VFAIL(VCA_ERR_NUMERIC, "batched and single-sector fixed-point Lanczos disagree");
-      }
-    } else {
-      RCHK(sector_gs(isector, &e, &vec, tmp));
+    RCHK(g->fx ? sector_gs_fx(isector, &e, &vec, tmp) : sector_gs(isector, &e, &vec, tmp));
+    // the same recurrence and stopping rule: the two runs agree
+    if (std::fabs(e - eb[isector - 1]) > 1e-12 * std::max(1.0, std::fabs(e))) {
+      tmp.release();
+      VFAIL(VCA_ERR_NUMERIC, "batched and single-sector Lanczos disagree");
     }
     g->sector_e[isector - 1] = e;
     // T=0 bookkeeping (VCA_DIAG.f90:224-236), list ordered by energy
@@ -2156,10 +2239,12 @@ int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc, cons
   g_err.clear();
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   if (B < 0 || !omega_out) VFAIL(VCA_ERR_ARG, "bad batch arguments");
+  if (B == 0) return VCA_OK;
+  RCHK(upload_hk(Hk, Nk));  // shared by every point: uploaded (and its k-pairs found) once
   for (int b = 0; b < B; b++) {
-    RCHK(solve_one(Hloc + 2 * (size_t)b * stride_hloc, Hk, Nk,
-                   bath_h ? bath_h + 2 * (size_t)b * stride_bath_h : nullptr,
-                   bath_v ? bath_v + 2 * (size_t)b * stride_bath_v : nullptr, omega_out + b));
+    RCHK(solve_resident(Hloc + 2 * (size_t)b * stride_hloc,
+                        bath_h ? bath_h + 2 * (size_t)b * stride_bath_h : nullptr,
+                        bath_v ? bath_v + 2 * (size_t)b * stride_bath_v : nullptr, omega_out + b));
   }
   return VCA_OK;
 }

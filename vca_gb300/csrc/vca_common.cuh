@@ -68,6 +68,20 @@ struct MixedDiag {
   double c0;  // constant Hartree shifts (H_cluster_local.f90:59-76), hfmode only
 };
 
+#ifdef __CUDACC__
+// opposite-spin density-density terms (H_cluster_local.f90:26-45)
+__device__ __forceinline__ double mixed_diag(const MixedDiag& md, unsigned u, unsigned d) {
+  double s = 0.0;
+  for (int o = 0; o < md.norb; o++) s += md.U[o] * (double)__popc(u & d & md.omask[o]);
+  int c = 0;
+  for (int o = 0; o < md.norb; o++)
+    for (int q = o + 1; q < md.norb; q++)
+      c += __popc(u & md.omask[o] & (d >> (q - o))) + __popc(u & md.omask[q] & (d << (q - o)));
+  if (c) s += md.Ust * (double)c;
+  return s + md.c0;
+}
+#endif
+
 // Per-chain Lanczos bookkeeping for a column batch.
 struct ChainMeta {
   int ncol;       // columns of this chain (1 real, 2 complex on real H)

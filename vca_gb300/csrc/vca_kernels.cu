@@ -169,18 +169,6 @@ void launch_e1(int dim, const int* words, const E1Params& p, bool with_const, do
   k_e1<<<nblocks(dim, 256), 256, 0, st>>>(dim, words, p, with_const ? 1 : 0, e1);
 }
 
-// opposite-spin density-density terms (H_cluster_local.f90:26-45)
-__device__ __forceinline__ double mixed_diag(const MixedDiag& md, unsigned u, unsigned d) {
-  double s = 0.0;
-  for (int o = 0; o < md.norb; o++) s += md.U[o] * (double)__popc(u & d & md.omask[o]);
-  int c = 0;
-  for (int o = 0; o < md.norb; o++)
-    for (int q = o + 1; q < md.norb; q++)
-      c += __popc(u & md.omask[o] & (d >> (q - o))) + __popc(u & md.omask[q] & (d << (q - o)));
-  if (c) s += md.Ust * (double)c;
-  return s + md.c0;
-}
-
 // ---------------------------------------------------------------------------
 // H x v on a column batch: Y = d o X + H_up X + X H_dw^T per column, the
 // stored product of VCA_HAMILTONIAN_SPARSE_HxV.f90:152-200 with the diagonal

@@ -356,4 +356,256 @@ void ms_launch_check(const MsGroup& gp, MsBufs& b, double tol, cudaStream_t st) 
                                          b.state, b.mconv, tol, b.undone);
 }
 
+
+// ===========================================================================
+// The same batched ground-state search in FP64, real (T = double) or complex
+// (T = double2) vectors, for the Hamiltonians the fixed-point path does not
+// take (more than 4 hopping magnitudes, complex amplitudes).  The recurrence,
+// start vectors and stopping rule are those of the single-sector FP64
+// Lanczos (y = H x - beta x_prev, alpha = <x, y>, y -= alpha x, beta = |y|,
+// x_next = y / beta); tile partial sums are reduced in a fixed order, so the
+// run is deterministic.
+// ===========================================================================
+namespace {
+__device__ __forceinline__ double m64_re(double a, double b) { return a * b; }
+__device__ __forceinline__ double m64_re(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ double m64_axpy(double y, double s, double x) { return fma(-s, x, y); }
+__device__ __forceinline__ double2 m64_axpy(double2 y, double s, double2 x) {
+  return make_double2(fma(-s, x.x, y.x), fma(-s, x.y, y.y));
+}
+__device__ __forceinline__ double m64_scale(double x, double f) { return x * f; }
+__device__ __forceinline__ double2 m64_scale(double2 x, double f) { return make_double2(x.x * f, x.y * f); }
+__device__ __forceinline__ void m64_set(double& x, double v) { x = v; }
+__device__ __forceinline__ void m64_set(double2& x, double v) { x = make_double2(v, 0.0); }
+__device__ __forceinline__ double m64_cfma(double2 a, double x, double acc) { return fma(a.x, x, acc); }
+__device__ __forceinline__ double2 m64_cfma(double2 a, double2 x, double2 acc) {
+  acc.x = fma(a.x, x.x, acc.x);
+  acc.x = fma(-a.y, x.y, acc.x);
+  acc.y = fma(a.x, x.y, acc.y);
+  acc.y = fma(a.y, x.x, acc.y);
+  return acc;
+}
+__device__ __forceinline__ double m64_diag(double d_re, double, double x) { return d_re * x; }
+__device__ __forceinline__ double2 m64_diag(double d_re, double d_im, double2 x) {
+  return make_double2(d_re * x.x - d_im * x.y, d_re * x.y + d_im * x.x);
+}
+
+// fixed-order block reduction of one double per thread into tpart[t]
+__device__ __forceinline__ void m64_block_store(double v, double* tpart, int t) {
+  __shared__ double red[256];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) tpart[t] = red[0];
+  __syncthreads();
+}
+// fixed-order warp sum of the tile partials of one sector
+__device__ __forceinline__ double m64_sum_tiles(const double* tpart, int t0, int n) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int t = t0 + lane; t < t0 + n; t += 32) s += tpart[t];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  return s;
+}
+}  // namespace
+
+// start vector (the values of the single-sector path) and its |x|^2 partials
+template <typename T>
+__global__ void k_m64_start(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles, uint64_t seed,
+                            T* X, double* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const MsSector& S = secs[tsec[t]];
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    double acc = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const uint64_t z = ms_splitmix64(seed + 0xD1B54A32D192ED03ull * (uint64_t)S.isector + (uint64_t)i);
+      const double v = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+      m64_set(X[S.off + i], v);
+      acc += v * v;
+    }
+    m64_block_store(acc, tpart, t);
+  }
+}
+// per sector: 1/|x| (0 and retired when the start vector vanishes)
+__global__ void k_m64_norm(int nsec, const MsSector* secs, const double* tpart, ChainMeta* meta, double* invn) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nsec; s += nw) {
+    const double n2 = m64_sum_tiles(tpart, secs[s].tile0, secs[s].ntile);
+    if (lane == 0) {
+      if (n2 > 0.0) {
+        invn[s] = 1.0 / sqrt(n2);
+      } else {
+        invn[s] = 0.0;
+        meta[s].active = 0;
+        meta[s].len = 0;
+      }
+    }
+  }
+}
+// Xo = f[sector] Xi (f = 0 for retired sectors)
+template <typename T>
+__global__ void k_m64_scale(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles, const double* f,
+                            const T* Xi, T* Xo) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    const MsSector& S = secs[s];
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    const double fs = f[s];
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) Xo[S.off + i] = m64_scale(Xi[S.off + i], fs);
+  }
+}
+// y = H x - beta x_prev and the <x, y> partials (the stored H x v of
+// VCA_HAMILTONIAN_SPARSE_HxV.f90:152-200, one element per thread)
+template <typename T>
+__global__ void __launch_bounds__(256) k_m64_hxv(const MsSector* secs, const int* tsec, const int64_t* tstart,
+                                                 int ntiles, MixedDiag md, const ChainMeta* meta,
+                                                 const double* bnow, int use_b, const T* __restrict__ X,
+                                                 const T* __restrict__ Xp, T* __restrict__ Y, double* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    double acc = 0.0;
+    if (meta[s].active) {
+      const MsSector& S = secs[s];
+      const SectorView& sv = S.sv;
+      const T* x = X + S.off;
+      const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+      const double b = use_b ? bnow[s] : 0.0;
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int idw = (int)(i / sv.dimup);
+        const int iup = (int)(i - (int64_t)idw * sv.dimup);
+        const double dre = sv.up_e1[iup].x + sv.dw_e1[idw].x +
+                           mixed_diag(md, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
+        const double dim_ = sv.up_e1[iup].y + sv.dw_e1[idw].y;
+        const T xi = x[i];
+        T y = m64_diag(dre, dim_, xi);
+        const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
+        const int64_t colbase = (int64_t)idw * sv.dimup;
+        for (int k = 0; k < nu; k++) {
+          const int src = sv.up_src[(int64_t)k * sv.dimup + iup];
+          y = m64_cfma(sv.up_amp[(int64_t)k * sv.dimup + iup], x[colbase + src], y);
+        }
+        for (int k = 0; k < nd; k++) {
+          const int src = sv.dw_src[(int64_t)k * sv.dimdw + idw];
+          y = m64_cfma(sv.dw_amp[(int64_t)k * sv.dimdw + idw], x[(int64_t)iup + (int64_t)src * sv.dimup], y);
+        }
+        if (use_b) y = m64_axpy(y, b, Xp[S.off + i]);
+        Y[S.off + i] = y;
+        acc += m64_re(xi, y);
+      }
+    }
+    m64_block_store(acc, tpart, t);
+  }
+}
+__global__ void k_m64_alpha(int nsec, const MsSector* secs, const ChainMeta* meta, const double* tpart,
+                            double* alpha) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nsec; s += nw) {
+    if (!meta[s].active) continue;
+    const double a = m64_sum_tiles(tpart, secs[s].tile0, secs[s].ntile);
+    if (lane == 0) alpha[s] = a;
+  }
+}
+// y -= alpha x and the |y|^2 partials
+template <typename T>
+__global__ void k_m64_update(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
+                             const ChainMeta* meta, const double* alpha, const T* X, T* Y, double* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    double acc = 0.0;
+    if (meta[s].active) {
+      const MsSector& S = secs[s];
+      const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+      const double a = alpha[s];
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const T y = m64_axpy(Y[S.off + i], a, X[S.off + i]);
+        Y[S.off + i] = y;
+        acc += m64_re(y, y);
+      }
+    }
+    m64_block_store(acc, tpart, t);
+  }
+}
+// beta -> the sp_lanc_tridiag bookkeeping (as k_lanczos_record) and 1/beta
+__global__ void k_m64_record(int nsec, const MsSector* secs, ChainMeta* meta, const double* tpart, int k,
+                             const double* alpha, double* A, double* Bt, int ld, double tol, double* bnow,
+                             double* invb) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nsec; s += nw) {
+    ChainMeta mt = meta[s];
+    if (!mt.active) {
+      if (lane == 0) invb[s] = 0.0;
+      continue;
+    }
+    const double b2 = m64_sum_tiles(tpart, secs[s].tile0, secs[s].ntile);
+    if (lane != 0) continue;
+    const double b = sqrt(fmax(b2, 0.0));
+    A[(int64_t)s * ld + (k - 1)] = alpha[s];
+    mt.len = k;
+    double ib;
+    if (b < tol) {
+      mt.active = 0;
+      ib = 0.0;
+    } else {
+      if (k < mt.nlanc) Bt[(int64_t)s * ld + k] = b;
+      if (k >= mt.nlanc) mt.active = 0;
+      ib = 1.0 / b;
+    }
+    bnow[s] = b;
+    invb[s] = ib;
+    meta[s] = mt;
+  }
+}
+
+template <typename T>
+static void m64_start_t(const MsGroup& gp, uint64_t seed, Ms64Bufs& b, cudaStream_t st) {
+  for (int q = 0; q < 3; q++) count_launch_external();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  const int sb = (gp.nsec * 32 + 127) / 128;
+  k_m64_start<T><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, seed, (T*)b.X, b.tpart);
+  k_m64_norm<<<sb, 128, 0, st>>>(gp.nsec, gp.secs, b.tpart, b.meta, b.invb);
+  k_m64_scale<T><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.invb, (const T*)b.X, (T*)b.X);
+}
+template <typename T>
+static void m64_step_t(const MsGroup& gp, const MixedDiag& md, int k, double tol, Ms64Bufs& b, cudaStream_t st) {
+  for (int q = 0; q < 5; q++) count_launch_external();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  const int sb = (gp.nsec * 32 + 127) / 128;
+  k_m64_hxv<T><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, md, b.meta, b.bnow, k > 1 ? 1 : 0,
+                                   (const T*)b.X, (const T*)b.Xp, (T*)b.Y, b.tpart);
+  k_m64_alpha<<<sb, 128, 0, st>>>(gp.nsec, gp.secs, b.meta, b.tpart, b.alpha);
+  k_m64_update<T><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.meta, b.alpha, (const T*)b.X,
+                                      (T*)b.Y, b.tpart);
+  k_m64_record<<<sb, 128, 0, st>>>(gp.nsec, gp.secs, b.meta, b.tpart, k, b.alpha, b.A, b.Bt, b.ld, tol, b.bnow,
+                                   b.invb);
+  // x_next = y / beta into the old x_prev buffer (retired sectors get zeros)
+  k_m64_scale<T><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, b.invb, (const T*)b.Y, (T*)b.Xp);
+  void* t = b.Xp;
+  b.Xp = b.X;
+  b.X = t;
+}
+
+void m64_launch_start(const MsGroup& gp, bool cplx, uint64_t seed, Ms64Bufs& b, cudaStream_t st) {
+  if (cplx) m64_start_t<double2>(gp, seed, b, st);
+  else m64_start_t<double>(gp, seed, b, st);
+}
+void m64_launch_step(const MsGroup& gp, bool cplx, const MixedDiag& md, int k, double tol, Ms64Bufs& b,
+                     cudaStream_t st) {
+  if (cplx) m64_step_t<double2>(gp, md, k, tol, b, st);
+  else m64_step_t<double>(gp, md, k, tol, b, st);
+}
+void m64_launch_check(const MsGroup& gp, Ms64Bufs& b, double tol, cudaStream_t st) {
+  count_launch_external();
+  const int threads = 128;
+  const int blocks = std::max(1, (gp.nsec * 32 + threads - 1) / threads);
+  k_ms_check<<<blocks, threads, 0, st>>>(gp.nsec, b.meta, b.A, b.Bt, b.ld, b.bnow, b.svec, b.theta, b.resid,
+                                         b.state, b.mconv, tol, b.undone);
+}
+
 }  // namespace vca

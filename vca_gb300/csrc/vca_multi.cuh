@@ -41,4 +41,18 @@ void ms_launch_start(const MsGroup& gp, uint64_t seed, int F, i64* R, i64* X, i6
 void ms_launch_step(const MsGroup& gp, const FxScales& fs, int K, int k, double tol, MsBufs& b, cudaStream_t st);
 void ms_launch_check(const MsGroup& gp, MsBufs& b, double tol, cudaStream_t st);
 
+// the same search in FP64: vectors of double (real H) or double2 (complex H)
+struct Ms64Bufs {
+  void *X, *Xp, *Y;       // packed vectors
+  double* tpart;          // per-tile partial sums
+  ChainMeta* meta;        // per sector
+  double *alpha, *bnow, *invb, *A, *Bt, *svec, *theta, *resid;
+  int *state, *mconv, *undone;
+  int ld;
+};
+void m64_launch_start(const MsGroup& gp, bool cplx, uint64_t seed, Ms64Bufs& b, cudaStream_t st);
+void m64_launch_step(const MsGroup& gp, bool cplx, const MixedDiag& md, int k, double tol, Ms64Bufs& b,
+                     cudaStream_t st);
+void m64_launch_check(const MsGroup& gp, Ms64Bufs& b, double tol, cudaStream_t st);
+
 }  // namespace vca
