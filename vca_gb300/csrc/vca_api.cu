@@ -1581,8 +1581,17 @@ int ksum_device(int n, const double2* d_z, bool want_im, Arena& ar, double** f_r
   if (!cols.empty()) cudaMemcpyAsync(d_cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, g->st);
   const bool pairs = g->d_Hk_rep && g->Nk_rep < Nk && omega_pairs_valid();
   const int64_t nks = pairs ? g->Nk_rep : Nk;
-  launch_omega_ksum2(n, N, nblk, nb, P, Glso, nks, pairs ? g->d_Hk_rep : g->d_Hk, pairs ? g->d_kw : nullptr,
-                     d_rowptr, d_cols, fpart, fpart_im, kchunks, g->st);
+  const double2* hks = pairs ? g->d_Hk_rep : g->d_Hk;
+  // without a bath P = Hloc at every node: M_k = Hloc - H_k once per k
+  const bool pre_m = !g->has_bath;
+  if (pre_m) {
+    double2* M;
+    if ((rc = ar.alloc(&M, (size_t)nks * NN))) return rc;
+    launch_m_from_hk(nks, NN, P, hks, M, g->st);
+    hks = M;
+  }
+  launch_omega_ksum2(n, N, nblk, nb, P, Glso, nks, hks, pairs ? g->d_kw : nullptr, d_rowptr, d_cols, fpart,
+                     fpart_im, kchunks, pre_m, g->st);
   launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, *f_re, g->st);
   if (want_im) launch_reduce_rows(n, kchunks, fpart_im, 1.0 / (double)Nk, *f_im, g->st);
   CUCHK(cudaGetLastError());

@@ -1070,9 +1070,10 @@ void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long*
 //  whole matrix, reduced to (-pi, pi] as the principal log takes it.
 // ---------------------------------------------------------------------------
 // A = (P - H) G for the nb x nb block at offset off, into the warp's Aw
+// pre_m: H already holds M = P - H_k (node-independent P)
 __device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off, int N, const double2* Ps,
                                                    const double2* Gs, const double2* H, const int* rowptr,
-                                                   const int* cols, int lane) {
+                                                   const int* cols, int lane, bool pre_m) {
   const int nbb = nb * nb;
   for (int e = lane; e < nbb; e += 32) {  // A(i,j), i fastest across lanes
     const int i = e % nb, j = e / nb;
@@ -1081,7 +1082,14 @@ __device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off,
     for (int q = rowptr[gi]; q < rowptr[gi + 1]; q++) {
       const int gl = cols[q];
       const int il = gi + gl * N;
-      const double mr = Ps[il].x - H[il].x, mi = Ps[il].y - H[il].y;
+      double mr, mi;
+      if (pre_m) {
+        mr = H[il].x;
+        mi = H[il].y;
+      } else {
+        mr = Ps[il].x - H[il].x;
+        mi = Ps[il].y - H[il].y;
+      }
       const double2 gg = Gs[gl + (off + j) * N];
       sr = fma(mr, gg.x, sr);
       sr = fma(-mi, gg.y, sr);
@@ -1097,14 +1105,17 @@ __device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off,
 // of the pivots' arguments (plus pi per row swap).  Warp-uniform result.
 template <bool PH>
 __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
-  double rmax = 0.0;
+  // row sums of |re| + |im| in FP32 (>= the row sums of |a_ij|); the
+  // elimination without pivoting needs them below 1/2, taken as < 0.49 to
+  // cover the FP32 rounding
+  float rmax = 0.0f;
   if (lane < nb)
     for (int j = 0; j < nb; j++) {
       const double2 a = Aw[lane + j * nb];
-      rmax += fabs(a.x) + fabs(a.y);  // >= sum |a_ij|: a safe bound for the branch
+      rmax += fabsf((float)a.x) + fabsf((float)a.y);
     }
-  for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-  if (rmax < 0.5) {
+  for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  if (rmax < 0.49f) {
     double delta = 0.0;
     for (int kk = 0; kk < nb; kk++) {
       const double2 akk = Aw[kk + kk * nb];
@@ -1124,8 +1135,10 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
         const int i = kk + 1 + e % r, j = kk + 1 + e / r;
         const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
         double2& t = Aw[i + j * nb];
-        t.x -= l.x * u.x - l.y * u.y;
-        t.y -= l.x * u.y + l.y * u.x;
+        t.x = fma(-l.x, u.x, t.x);
+        t.x = fma(l.y, u.y, t.x);
+        t.y = fma(-l.x, u.y, t.y);
+        t.y = fma(-l.y, u.x, t.y);
       }
       __syncwarp();
     }
@@ -1137,19 +1150,27 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
   int ex = 0;
   bool zero = false;
   for (int kk = 0; kk < nb; kk++) {
-    double mag = -1.0;
+    // pivot: the largest |re| + |im| of the column (FP32 comparison; any
+    // row with a nonzero entry is a valid pivot, the largest keeps it stable)
+    float fm = -1.0f;
     int arg = kk;
     if (lane >= kk && lane < nb) {
       const double2 a = Aw[lane + kk * nb];
-      mag = a.x * a.x + a.y * a.y;
+      fm = (a.x != 0.0 || a.y != 0.0) ? fmaxf(fabsf((float)a.x) + fabsf((float)a.y), 1e-37f) : 0.0f;
       arg = lane;
     }
     for (int o = 16; o > 0; o >>= 1) {
-      const double om = __shfl_xor_sync(0xffffffffu, mag, o);
+      const float om = __shfl_xor_sync(0xffffffffu, fm, o);
       const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
-      if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
+      if (om > fm || (om == fm && oa < arg)) { fm = om; arg = oa; }
     }
-    if (mag == 0.0) { zero = true; break; }
+    if (!(fm > 0.0f)) { zero = true; break; }
+    double mag;
+    {
+      const double2 a = Aw[arg + kk * nb];
+      mag = a.x * a.x + a.y * a.y;
+    }
+    if (mag == 0.0) { zero = true; break; }  // |pivot| below 1e-154: treated as singular
     if (arg != kk) {
       for (int j = lane; j < nb; j += 32) {
         const double2 t = Aw[kk + j * nb];
@@ -1175,8 +1196,10 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
       const int i = kk + 1 + e % r, j = kk + 1 + e / r;
       const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
       double2& t = Aw[i + j * nb];
-      t.x -= l.x * u.x - l.y * u.y;
-      t.y -= l.x * u.y + l.y * u.x;
+      t.x = fma(-l.x, u.x, t.x);
+      t.x = fma(l.y, u.y, t.x);
+      t.y = fma(-l.x, u.y, t.y);
+      t.y = fma(-l.y, u.x, t.y);
     }
     __syncwarp();
   }
@@ -1187,7 +1210,7 @@ template <bool CPLX>
 __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, const double2* P,
                                                      const double2* Glso, int64_t Nk, const double2* Hk,
                                                      const double* kw, const int* rowptr, const int* cols,
-                                                     double* fpart, double* fpart_im, int kchunks) {
+                                                     double* fpart, double* fpart_im, int kchunks, int pre_m) {
   extern __shared__ double2 shm[];
   const int w = blockIdx.y;
   const int chunk = blockIdx.x;
@@ -1211,7 +1234,7 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
     const int b0 = CPLX ? 0 : (int)(task % nblk), b1 = CPLX ? nblk : b0 + 1;
     double ld = 0.0, ph = 0.0;
     for (int b = b0; b < b1; b++) {
-      ksum_block_product(Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, lane);
+      ksum_block_product(Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, lane, pre_m != 0);
       ld += ksum_block_logdet<CPLX>(Aw, nb, lane, &ph);
     }
     if (lane == 0) {
@@ -1234,9 +1257,21 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
     if (CPLX) fpart_im[(int64_t)w * kchunks + chunk] = sim;
   }
 }
+__global__ void k_m_from_hk(int64_t n, int NN, const double2* Hl, const double2* Hk, double2* M) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const double2 h = Hl[q % NN], k = Hk[q];
+    M[q] = make_double2(h.x - k.x, h.y - k.y);
+  }
+}
+void launch_m_from_hk(int64_t Nk, int NN, const double2* Hl, const double2* Hk, double2* M, cudaStream_t st) {
+  COUNT_LAUNCH();
+  const int64_t n = Nk * NN;
+  k_m_from_hk<<<nblocks(n, 256), 256, 0, st>>>(n, NN, Hl, Hk, M);
+}
+
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                        double* fpart_im, int kchunks, cudaStream_t st) {
+                        double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
   COUNT_LAUNCH();
   const int threads = 128;
   size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
@@ -1249,10 +1284,10 @@ void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const
   dim3 grd(kchunks, nw, 1);
   if (fpart_im)
     k_omega_ksum2<true><<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im,
-                                                   kchunks);
+                                                   kchunks, pre_m ? 1 : 0);
   else
     k_omega_ksum2<false><<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart,
-                                                    nullptr, kchunks);
+                                                    nullptr, kchunks, pre_m ? 1 : 0);
 }
 
 // ---------------------------------------------------------------------------

@@ -141,9 +141,12 @@ void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, doub
 // (rowptr/cols, lso indices), all lanes of a warp on the products and the LU
 // updates.  With fpart_im (sum_kmesh_complex, :78-114) also the k-sum of the
 // principal argument of det over all blocks of each k.
+// pre_m: Hk holds M_k = P - H_k already (P the same at every node)
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                        double* fpart_im, int kchunks, cudaStream_t st);
+                        double* fpart_im, int kchunks, bool pre_m, cudaStream_t st);
+// M[k] = Hl - Hk[k] for Nk lso matrices of NN elements
+void launch_m_from_hk(int64_t Nk, int NN, const double2* Hl, const double2* Hk, double2* M, cudaStream_t st);
 // Sigma(z) (want_g0 = false) or G0(z) on nz frequencies from G' (lso) and
 // P = Delta + Hloc (per z, or one matrix): build_sigma_normal,
 // VCA_GF_NORMAL.f90:1045-1111.  N <= 32.
