@@ -1102,7 +1102,8 @@ __device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off,
 }
 
 // ln|det(1 + A)| of the block in Aw (destroyed); with PH, *ph gains the sum
-// of the pivots' arguments (plus pi per row swap).  Warp-uniform result.
+// of the pivots' arguments (plus pi per row swap).  Both are valid on lane 0
+// only.
 template <bool PH>
 __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
   // row sums of |re| + |im| in FP32 (>= the row sums of |a_ij|); the
@@ -1116,15 +1117,23 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
     }
   for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
   if (rmax < 0.49f) {
+    // the per-column scalars (log1p accumulator, argument, 1/pivot) on lane
+    // 0 only, 1/pivot broadcast: the FP64 pipe is what bounds this kernel
     double delta = 0.0;
     for (int kk = 0; kk < nb; kk++) {
-      const double2 akk = Aw[kk + kk * nb];
-      const double pr = 1.0 + akk.x, pim = akk.y;
-      const double x = 2.0 * akk.x + akk.x * akk.x + akk.y * akk.y;
-      delta = delta + x + delta * x;
-      if (PH) *ph += atan2(pim, pr);
-      const double den = pr * pr + pim * pim;
-      const double ir = pr / den, ii = -pim / den;  // 1/pivot
+      double ir = 0.0, ii = 0.0;
+      if (lane == 0) {
+        const double2 akk = Aw[kk + kk * nb];
+        const double pr = 1.0 + akk.x, pim = akk.y;
+        const double x = 2.0 * akk.x + akk.x * akk.x + akk.y * akk.y;
+        delta = delta + x + delta * x;
+        if (PH) *ph += atan2(pim, pr);
+        const double den = pr * pr + pim * pim;
+        ir = pr / den;
+        ii = -pim / den;  // 1/pivot
+      }
+      ir = __shfl_sync(0xffffffffu, ir, 0);
+      ii = __shfl_sync(0xffffffffu, ii, 0);
       for (int i = kk + 1 + lane; i < nb; i += 32) {
         const double2 a = Aw[i + kk * nb];
         Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
@@ -1142,7 +1151,7 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
       }
       __syncwarp();
     }
-    return 0.5 * log1p(delta);
+    return lane == 0 ? 0.5 * log1p(delta) : 0.0;
   }
   for (int i = lane; i < nb; i += 32) Aw[i + i * nb].x += 1.0;
   __syncwarp();
@@ -1180,12 +1189,18 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
       if (PH) *ph += 3.141592653589793;
     }
     __syncwarp();
-    const double2 piv = Aw[kk + kk * nb];
-    if (PH) *ph += atan2(piv.y, piv.x);
-    int e2;
-    mant = frexp(mant * mag, &e2);
-    ex += e2;
-    const double ir = piv.x / mag, ii = -piv.y / mag;
+    double ir = 0.0, ii = 0.0;
+    if (lane == 0) {  // per-column scalars on lane 0, 1/pivot broadcast
+      const double2 piv = Aw[kk + kk * nb];
+      if (PH) *ph += atan2(piv.y, piv.x);
+      int e2;
+      mant = frexp(mant * mag, &e2);
+      ex += e2;
+      ir = piv.x / mag;
+      ii = -piv.y / mag;
+    }
+    ir = __shfl_sync(0xffffffffu, ir, 0);
+    ii = __shfl_sync(0xffffffffu, ii, 0);
     for (int i = kk + 1 + lane; i < nb; i += 32) {
       const double2 a = Aw[i + kk * nb];
       Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
@@ -1203,6 +1218,7 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
     }
     __syncwarp();
   }
+  if (lane != 0) return 0.0;
   return zero ? -INFINITY : 0.5 * (log(mant) + ex * 0.6931471805599453);
 }
 
