@@ -1069,13 +1069,27 @@ void launch_chain_init_fx(const SectorView& tgt, int src_dimup, const long long*
 //  also sums the pivots' arguments (plus pi per row swap): arg det of the
 //  whole matrix, reduced to (-pi, pi] as the principal log takes it.
 // ---------------------------------------------------------------------------
-// A = (P - H) G for the nb x nb block at offset off, into the warp's Aw
+// Lane groups: G lanes (8, 16 or 32) work on one (k, spin block) task and a
+// warp runs 32/G tasks side by side.  GB300's FP64 pipe spends an issue slot
+// per warp instruction however few of its lanes are active, so packing
+// several small LUs into one warp divides the FP64 instructions per task
+// (the per-column scalars of four tasks share one instruction, and so do the
+// short trailing updates).  All syncs and shuffles inside a task use the
+// group's lane mask: groups of one warp may take different branches.
+struct KGroup {
+  int gl;         // lane within the group
+  int base;       // first lane of the group
+  unsigned mask;  // the group's lanes
+};
+
+// A = (P - H) G for the nb x nb block at offset off, into the group's Aw;
 // pre_m: H already holds M = P - H_k (node-independent P)
-__device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off, int N, const double2* Ps,
-                                                   const double2* Gs, const double2* H, const int* rowptr,
-                                                   const int* cols, int lane, bool pre_m) {
+template <int G>
+__device__ __forceinline__ void ksum_block_product(const KGroup& kg, double2* Aw, int nb, int off, int N,
+                                                   const double2* Ps, const double2* Gs, const double2* H,
+                                                   const int* rowptr, const int* cols, bool pre_m) {
   const int nbb = nb * nb;
-  for (int e = lane; e < nbb; e += 32) {  // A(i,j), i fastest across lanes
+  for (int e = kg.gl; e < nbb; e += G) {  // A(i,j), i fastest across lanes
     const int i = e % nb, j = e / nb;
     const int gi = off + i;
     double sr = 0.0, si = 0.0;
@@ -1098,31 +1112,36 @@ __device__ __forceinline__ void ksum_block_product(double2* Aw, int nb, int off,
     }
     Aw[e] = make_double2(sr, si);
   }
-  __syncwarp();
+  __syncwarp(kg.mask);
 }
 
 // ln|det(1 + A)| of the block in Aw (destroyed); with PH, *ph gains the sum
-// of the pivots' arguments (plus pi per row swap).  Both are valid on lane 0
-// only.
-template <bool PH>
-__device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
+// of the pivots' arguments (plus pi per row swap).  Both are valid on the
+// group's first lane only.
+template <int G, bool PH>
+__device__ double ksum_block_logdet(const KGroup& kg, double2* Aw, int nb, double* ph) {
+  const int gl = kg.gl;
+  const unsigned gm = kg.mask;
   // row sums of |re| + |im| in FP32 (>= the row sums of |a_ij|); the
   // elimination without pivoting needs them below 1/2, taken as < 0.49 to
   // cover the FP32 rounding
   float rmax = 0.0f;
-  if (lane < nb)
+  for (int i = gl; i < nb; i += G) {
+    float r = 0.0f;
     for (int j = 0; j < nb; j++) {
-      const double2 a = Aw[lane + j * nb];
-      rmax += fabsf((float)a.x) + fabsf((float)a.y);
+      const double2 a = Aw[i + j * nb];
+      r += fabsf((float)a.x) + fabsf((float)a.y);
     }
-  for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    rmax = fmaxf(rmax, r);
+  }
+  for (int o = G / 2; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(gm, rmax, o));
   if (rmax < 0.49f) {
-    // the per-column scalars (log1p accumulator, argument, 1/pivot) on lane
-    // 0 only, 1/pivot broadcast: the FP64 pipe is what bounds this kernel
+    // the per-column scalars (log1p accumulator, argument, 1/pivot) on the
+    // first lane, 1/pivot broadcast to the group
     double delta = 0.0;
     for (int kk = 0; kk < nb; kk++) {
       double ir = 0.0, ii = 0.0;
-      if (lane == 0) {
+      if (gl == 0) {
         const double2 akk = Aw[kk + kk * nb];
         const double pr = 1.0 + akk.x, pim = akk.y;
         const double x = 2.0 * akk.x + akk.x * akk.x + akk.y * akk.y;
@@ -1132,15 +1151,15 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
         ir = pr / den;
         ii = -pim / den;  // 1/pivot
       }
-      ir = __shfl_sync(0xffffffffu, ir, 0);
-      ii = __shfl_sync(0xffffffffu, ii, 0);
-      for (int i = kk + 1 + lane; i < nb; i += 32) {
+      ir = __shfl_sync(gm, ir, kg.base);
+      ii = __shfl_sync(gm, ii, kg.base);
+      for (int i = kk + 1 + gl; i < nb; i += G) {
         const double2 a = Aw[i + kk * nb];
         Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
       }
-      __syncwarp();
+      __syncwarp(gm);
       const int r = nb - kk - 1;
-      for (int e = lane; e < r * r; e += 32) {
+      for (int e = gl; e < r * r; e += G) {
         const int i = kk + 1 + e % r, j = kk + 1 + e / r;
         const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
         double2& t = Aw[i + j * nb];
@@ -1149,12 +1168,12 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
         t.y = fma(-l.x, u.y, t.y);
         t.y = fma(-l.y, u.x, t.y);
       }
-      __syncwarp();
+      __syncwarp(gm);
     }
-    return lane == 0 ? 0.5 * log1p(delta) : 0.0;
+    return gl == 0 ? 0.5 * log1p(delta) : 0.0;
   }
-  for (int i = lane; i < nb; i += 32) Aw[i + i * nb].x += 1.0;
-  __syncwarp();
+  for (int i = gl; i < nb; i += G) Aw[i + i * nb].x += 1.0;
+  __syncwarp(gm);
   double mant = 1.0;
   int ex = 0;
   bool zero = false;
@@ -1163,14 +1182,14 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
     // row with a nonzero entry is a valid pivot, the largest keeps it stable)
     float fm = -1.0f;
     int arg = kk;
-    if (lane >= kk && lane < nb) {
-      const double2 a = Aw[lane + kk * nb];
-      fm = (a.x != 0.0 || a.y != 0.0) ? fmaxf(fabsf((float)a.x) + fabsf((float)a.y), 1e-37f) : 0.0f;
-      arg = lane;
+    for (int i = kk + gl; i < nb; i += G) {
+      const double2 a = Aw[i + kk * nb];
+      const float f = (a.x != 0.0 || a.y != 0.0) ? fmaxf(fabsf((float)a.x) + fabsf((float)a.y), 1e-37f) : 0.0f;
+      if (f > fm) { fm = f; arg = i; }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const float om = __shfl_xor_sync(0xffffffffu, fm, o);
-      const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+    for (int o = G / 2; o > 0; o >>= 1) {
+      const float om = __shfl_xor_sync(gm, fm, o);
+      const int oa = __shfl_xor_sync(gm, arg, o);
       if (om > fm || (om == fm && oa < arg)) { fm = om; arg = oa; }
     }
     if (!(fm > 0.0f)) { zero = true; break; }
@@ -1181,16 +1200,16 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
     }
     if (mag == 0.0) { zero = true; break; }  // |pivot| below 1e-154: treated as singular
     if (arg != kk) {
-      for (int j = lane; j < nb; j += 32) {
+      for (int j = gl; j < nb; j += G) {
         const double2 t = Aw[kk + j * nb];
         Aw[kk + j * nb] = Aw[arg + j * nb];
         Aw[arg + j * nb] = t;
       }
       if (PH) *ph += 3.141592653589793;
     }
-    __syncwarp();
+    __syncwarp(gm);
     double ir = 0.0, ii = 0.0;
-    if (lane == 0) {  // per-column scalars on lane 0, 1/pivot broadcast
+    if (gl == 0) {  // per-column scalars on the first lane, 1/pivot broadcast
       const double2 piv = Aw[kk + kk * nb];
       if (PH) *ph += atan2(piv.y, piv.x);
       int e2;
@@ -1199,15 +1218,15 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
       ir = piv.x / mag;
       ii = -piv.y / mag;
     }
-    ir = __shfl_sync(0xffffffffu, ir, 0);
-    ii = __shfl_sync(0xffffffffu, ii, 0);
-    for (int i = kk + 1 + lane; i < nb; i += 32) {
+    ir = __shfl_sync(gm, ir, kg.base);
+    ii = __shfl_sync(gm, ii, kg.base);
+    for (int i = kk + 1 + gl; i < nb; i += G) {
       const double2 a = Aw[i + kk * nb];
       Aw[i + kk * nb] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
     }
-    __syncwarp();
+    __syncwarp(gm);
     const int r = nb - kk - 1;
-    for (int e = lane; e < r * r; e += 32) {
+    for (int e = gl; e < r * r; e += G) {
       const int i = kk + 1 + e % r, j = kk + 1 + e / r;
       const double2 l = Aw[i + kk * nb], u = Aw[kk + j * nb];
       double2& t = Aw[i + j * nb];
@@ -1216,18 +1235,19 @@ __device__ double ksum_block_logdet(double2* Aw, int nb, int lane, double* ph) {
       t.y = fma(-l.x, u.y, t.y);
       t.y = fma(-l.y, u.x, t.y);
     }
-    __syncwarp();
+    __syncwarp(gm);
   }
-  if (lane != 0) return 0.0;
+  if (gl != 0) return 0.0;
   return zero ? -INFINITY : 0.5 * (log(mant) + ex * 0.6931471805599453);
 }
 
-template <bool CPLX>
+template <bool CPLX, int G>
 __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, const double2* P,
                                                      const double2* Glso, int64_t Nk, const double2* Hk,
                                                      const double* kw, const int* rowptr, const int* cols,
                                                      double* fpart, double* fpart_im, int kchunks, int pre_m) {
   extern __shared__ double2 shm[];
+  constexpr int TPW = 32 / G;
   const int w = blockIdx.y;
   const int chunk = blockIdx.x;
   const int NN = N * N;
@@ -1235,7 +1255,12 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
   double2* Ps = shm + NN;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
-  double2* Aw = shm + 2 * NN + (int64_t)warp * nb * nb;
+  const int grp = lane / G;
+  KGroup kg;
+  kg.gl = lane % G;
+  kg.base = grp * G;
+  kg.mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (grp * G));
+  double2* Aw = shm + 2 * NN + ((int64_t)warp * TPW + grp) * nb * nb;
   for (int t = threadIdx.x; t < NN; t += blockDim.x) {
     Gs[t] = Glso[(int64_t)w * NN + t];
     Ps[t] = P[(int64_t)w * NN + t];
@@ -1244,16 +1269,16 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
   const int64_t k0 = (Nk * chunk) / kchunks, k1 = (Nk * (chunk + 1)) / kchunks;
   double acc = 0.0, acc_im = 0.0;
   const int64_t ntask = CPLX ? (k1 - k0) : (k1 - k0) * nblk;
-  for (int64_t task = warp; task < ntask; task += nwarps) {
+  for (int64_t task = (int64_t)warp * TPW + grp; task < ntask; task += (int64_t)nwarps * TPW) {
     const int64_t k = CPLX ? k0 + task : k0 + task / nblk;
     const double2* H = Hk + k * NN;
     const int b0 = CPLX ? 0 : (int)(task % nblk), b1 = CPLX ? nblk : b0 + 1;
     double ld = 0.0, ph = 0.0;
     for (int b = b0; b < b1; b++) {
-      ksum_block_product(Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, lane, pre_m != 0);
-      ld += ksum_block_logdet<CPLX>(Aw, nb, lane, &ph);
+      ksum_block_product<G>(kg, Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, pre_m != 0);
+      ld += ksum_block_logdet<G, CPLX>(kg, Aw, nb, &ph);
     }
-    if (lane == 0) {
+    if (kg.gl == 0) {
       acc += kw ? kw[k] * ld : ld;
       if (CPLX) {
         double a = remainder(ph, 6.283185307179586);
@@ -1261,7 +1286,12 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
         acc_im += kw ? kw[k] * a : a;
       }
     }
-    __syncwarp();
+    __syncwarp(kg.mask);
+  }
+  // every lane of the warp is here again: fixed-order warp sums
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (CPLX) acc_im += __shfl_xor_sync(0xffffffffu, acc_im, o);
   }
   __shared__ double red[32], red_im[32];
   if (lane == 0) { red[warp] = acc; red_im[warp] = acc_im; }
@@ -1285,25 +1315,40 @@ void launch_m_from_hk(int64_t Nk, int NN, const double2* Hl, const double2* Hk, 
   k_m_from_hk<<<nblocks(n, 256), 256, 0, st>>>(n, NN, Hl, Hk, M);
 }
 
+template <bool CPLX, int G>
+static void ksum2_launch(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
+                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
+                         double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
+  const int threads = 128;
+  const size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / G) * nb * nb);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_omega_ksum2<CPLX, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    attr = true;
+  }
+  k_omega_ksum2<CPLX, G><<<dim3(kchunks, nw, 1), threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols,
+                                                                     fpart, fpart_im, kchunks, pre_m ? 1 : 0);
+}
+template <bool CPLX>
+static void ksum2_dispatch(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
+                           const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
+                           double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
+  // 8 lanes per task up to 12 x 12 blocks, 16 up to 16 x 16, else a warp
+  if (nb <= 12)
+    ksum2_launch<CPLX, 8>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+  else if (nb <= 16)
+    ksum2_launch<CPLX, 16>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+  else
+    ksum2_launch<CPLX, 32>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+}
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
                         double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
   COUNT_LAUNCH();
-  const int threads = 128;
-  size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / 32) * nb * nb);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_omega_ksum2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_omega_ksum2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    attr = true;
-  }
-  dim3 grd(kchunks, nw, 1);
   if (fpart_im)
-    k_omega_ksum2<true><<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im,
-                                                   kchunks, pre_m ? 1 : 0);
+    ksum2_dispatch<true>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
   else
-    k_omega_ksum2<false><<<grd, threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart,
-                                                    nullptr, kchunks, pre_m ? 1 : 0);
+    ksum2_dispatch<false>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, nullptr, kchunks, pre_m, st);
 }
 
 // ---------------------------------------------------------------------------
