@@ -2,9 +2,10 @@
 // Lanczos Green's function -> Potthoff Omega path, at T = 0 and at finite T
 // (LANC_METHOD="lanczos": one state per sector).
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
-// entry and the CPU-baseline leg of the benchmark load it; the product path
-// (vca_gb300/csrc) never links or calls it.
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle the results are checked
+// against: the tests, the smoke entry and the CPU-baseline leg of the
+// benchmark load it; the product path (vca_gb300/csrc) never links or calls
+// it.
 //
 // Parity status: the reference (Fortran 90 + SciFortran + MPI) has no tests,
 // no golden vectors and cannot be compiled in this container (no Fortran
@@ -595,7 +596,7 @@ void tri_vector(const double* a, const double* b, int k, double theta, std::vect
 
 // ---------------------------------------------------------------------------
 // Deterministic Lanczos start vector (the reference's SciFortran sp_lanc_eigh
-// draws a random one; this build fixes it): splitmix64 (Steele, Lea, Flood
+// draws a random one; here it is fixed): splitmix64 (Steele, Lea, Flood
 // 2014) of (seed, sector, index) mapped to [-1, 1).
 // ---------------------------------------------------------------------------
 inline uint64_t splitmix64(uint64_t x) {
