@@ -232,6 +232,23 @@ def test_gf_poles_match_dense_resolvent():
             np.testing.assert_allclose(g[i, j, 0, 0, 0, 0], ge[i, j], atol=1e-10)
 
 
+def test_gf_chan2_matches_dense_resolvent():
+    """VCA_GF_SYMMETRIC=T (two channels, lanc_build_gf_normal_mix_chan2,
+    VCA_GF_NORMAL.f90:327-556): exact for a real symmetric model."""
+    pt = clusters.chain1d(tprime=0.8, nlat=4, U=4.0, xmu=2.0, nk=4, ngfiter=100, omega_nodes=64)
+    pt.cfg.vca_gf_symmetric = 1
+    o = Oracle.from_point(pt)
+    o.diagonalize()
+    o.build_gf()
+    z = np.array([0.2j, 1.0j, 0.5 + 0.3j])
+    g = o.gf_cluster(z)
+    ge = _exact_gf(o, pt, z)
+    for i in range(4):
+        for j in range(4):
+            np.testing.assert_allclose(g[i, j, 0, 0, 0, 0], ge[i, j], atol=1e-10)
+    assert o.gf_channel(1, 2, 1, 1, 1, 0, 3) is None or len(o.gf_channel(1, 2, 1, 1, 1, 0, 3)[0]) == 0
+
+
 def test_omega_u0_closed_form():
     for pt, mu, sfac in (
         (clusters.chain1d(tprime=1.0, nlat=4, U=0.0, xmu=0.3, nk=32, omega_nodes=512), 0.3, 2.0),

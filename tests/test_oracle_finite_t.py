@@ -151,3 +151,25 @@ def test_sum_kmesh_complex_direct_formula():
                      for k in range(pt.Nk)])
         got = o.sum_kmesh_complex(z)
         assert abs(got - f) < 1e-12 * max(1, abs(f)), (z, got, f)
+
+
+@pytest.mark.parametrize("mu_frac", [0.05, 0.97, -0.97])
+def test_contour_rule_with_the_fermi_step_near_the_ends(mu_frac):
+    """The graded rule when the Fermi step sits near theta = 0 or pi (xmu
+    close to +-R): against adaptive QUADPACK on a model integrand with the
+    same Fermi factor and a smooth F(w)."""
+    R, beta = 20.0, 15.0
+    mu = mu_frac * R
+    th, w = orc.contour_rule(R, beta, mu, 24)
+
+    def f(t):
+        z = R * np.exp(1j * t)
+        x = beta * (z - mu)
+        fermi = 0.0 if x.real >= 100 else 1.0 / (np.exp(x) + 1.0)
+        F = np.log(1.0 + 3.0 / (z * z + 2.0 * z + 5.0))
+        return ((1 / np.pi) * z * fermi * F).real
+
+    rule = float(np.dot(w, [f(t) for t in th]))
+    pts = [float(np.arccos(np.clip(mu / R, -1.0, 1.0)))]
+    ref, _ = scipy.integrate.quad(f, 0.0, np.pi, points=pts, limit=2000, epsabs=1e-14, epsrel=1e-14)
+    assert abs(rule - ref) < 1e-12, (mu_frac, rule, ref)
