@@ -38,6 +38,7 @@ extern "C" {
 #define VCA_ERR_NUMERIC (-7)     /* NaN/Inf input, zero-norm vector, breakdown */
 #define VCA_ERR_ALLOC (-8)       /* device memory exhausted                   */
 #define VCA_ERR_ARG (-9)         /* null pointer or out-of-range index        */
+#define VCA_ERR_IO (-10)         /* file open, read, write or layout error    */
 
 #define VCA_LANC_ARPACK 0
 #define VCA_LANC_LANCZOS 1
@@ -231,6 +232,39 @@ int vca_gpu_get_sector_energies(double* e_out, int32_t n);
 int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t iorb,
                            int32_t jorb, int32_t istate, int32_t ichan, int32_t* nexc,
                            double* poles, double* weights, int32_t cap);
+
+/*
+ * GFmatrix restart files (save_gfprime / read_gfprime, VCA_AUX_FUNX.f90:
+ * 601-697): the pole tables of every spin-diagonal element in file
+ * file//suffix//".restart" (".used" when used != 0), formatted = list-directed
+ * text or 0 = sequential unformatted records (write_formatted /
+ * write_unformatted, :486-593).  suffix may be NULL (the reference's
+ * file_suffix, empty by default).
+ * save: the tables of the last solve, as vca_gpu_get_gf_channel lists them.
+ * read: needs vca_gpu_init only; the tables replace the solve's until the
+ * next solve, for vca_gpu_gf_cluster (evaluated on the GPU as
+ * sum weight/(z - pole) per element, then the recombination) and
+ * vca_gpu_get_gf_channel.  The Sigma/G0 getters keep the solve's grids, as
+ * the reference's read_gfprime replaces impGmatrix only.
+ */
+int vca_gpu_save_gfprime(const char* file, const char* suffix, int32_t used, int32_t formatted);
+int vca_gpu_read_gfprime(const char* file, const char* suffix, int32_t used, int32_t formatted);
+/*
+ * The file layout alone, host code that needs no GPU and no context.  A
+ * table of nelem elements (file order: ilat, jlat, ispin, iorb, jorb from the
+ * outer to the inner loop) is flattened as
+ *   nstates[nelem], nchan[sum nstates], nexc[sum nchan],
+ *   poles and weights: 2*sum nexc doubles each (re, im pairs).
+ * vca_gfm_read: sizes[3] receives (sum nstates, sum nchan, sum nexc).  With
+ * nstates == NULL only the sizes are returned; otherwise sizes holds on entry
+ * the capacities of nchan, nexc and of the poles/weights in complex entries
+ * (nstates holds nelem), and VCA_ERR_ARG is returned when the file needs
+ * more.
+ */
+int vca_gfm_write(const char* path, int32_t formatted, int64_t nelem, const int32_t* nstates,
+                  const int32_t* nchan, const int32_t* nexc, const double* poles, const double* weights);
+int vca_gfm_read(const char* path, int32_t formatted, int64_t nelem, int64_t* sizes, int32_t* nstates,
+                 int32_t* nchan, int32_t* nexc, double* poles, double* weights);
 
 /* Omega integrand f(w) = (1/Lk) sum_k ln|det(1+(Delta+Hloc-Hk)G'(iw))|
  * (VCA_OMEGA.f90:37-75) at nw real frequencies, from the last solve. */

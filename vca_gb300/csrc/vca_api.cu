@@ -20,6 +20,7 @@
 #include "vca_fx.cuh"
 #include "vca_multi.cuh"
 #include "vca_kernels.cuh"
+#include "vca_gfmatrix.h"
 
 using namespace vca;
 typedef std::complex<double> cd;
@@ -160,8 +161,20 @@ struct Ctx {
   std::vector<cd> hk_const;       // lso: value of Hk when equal at every k
   std::vector<char> hk_varying;   // lso: 1 when Hk differs between k-points
   double t_ms[4] = {0, 0, 0, 0};  // set_hamiltonian, diagonalise, chains, Omega
+  // GFmatrix read from a restart file (read_gfprime): replaces the solve's
+  // tables for G'(z) and the channel getter until the next solve
+  bool gfm_loaded = false;
+  GfmTable gfm;                     // host copy, file order
+  std::vector<int64_t> gfm_state0;  // per file element: its first entry in gfm.nchan
+  std::vector<int64_t> gfm_chan0;   // per (element, state): its first entry in gfm.nexc
+  std::vector<int64_t> gfm_exc0;    // per channel: its first excitation
+  Arena gfm_dev;
+  int64_t* d_gfm_ptr = nullptr;  // [nelem+1] excitation ranges, elem_index order
+  double2* d_gfm_p = nullptr;
+  double2* d_gfm_w = nullptr;
 };
 Ctx* g = nullptr;
+static void gfm_drop();
 
 inline int64_t binom_h(int n, int k) {
   if (k < 0 || k > n) return 0;
@@ -1398,12 +1411,19 @@ GfLayout gf_layout() {
   return gl;
 }
 
-// G'(z) in lso layout for nz device points
-int gf_lso(int nz, const double2* d_z, double2* d_Glso, Arena& ar) {
+// G'(z) in lso layout for nz device points, from the tables vca_gf_cluster
+// would use: a GFmatrix read by read_gfprime while one is loaded, else the
+// solve's chains (solve_tables = true: always the solve's, as the grids that
+// build_gf_normal accumulates)
+int gf_lso(int nz, const double2* d_z, double2* d_Glso, Arena& ar, bool solve_tables = false) {
   const vca_config& c = g->cfg;
+  const int nelem = c.Nlat * c.Nlat * c.Nspin * c.Norb * c.Norb;
   double2* raw;
-  RCHK(ar.alloc(&raw, (size_t)nz * g->nelem));
-  launch_gf_eval(gf_layout(), nz, d_z, raw, g->st);
+  RCHK(ar.alloc(&raw, (size_t)nz * nelem));
+  if (g->gfm_loaded && !solve_tables)
+    launch_gf_eval_poles(nelem, g->d_gfm_ptr, g->d_gfm_p, g->d_gfm_w, nz, d_z, raw, g->st);
+  else
+    launch_gf_eval(gf_layout(), nz, d_z, raw, g->st);
   ClusterDims cdm{c.Nlat, c.Norb, c.Nspin, g->N, c.vca_gf_symmetric ? 0 : 1};
   launch_gf_assemble(cdm, nz, raw, d_Glso, g->st);
   CUCHK(cudaGetLastError());
@@ -2061,6 +2081,7 @@ int solve_resident(const double* Hloc, const double* bath_h, const double* bath_
   if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   if (!g->d_Hk) VFAIL(VCA_ERR_STATE, "no Hk resident: call vca_gpu_solve or vca_gpu_upload_hk first");
   g->solved = false;
+  gfm_drop();  // vca_solve rebuilds impGmatrix
   double t0 = now_ms();
   RCHK(set_hamiltonian(Hloc, bath_h, bath_v));
   double t1 = now_ms();
@@ -2086,6 +2107,112 @@ int solve_one(const double* Hloc, const double* Hk, int64_t Nk, const double* ba
   if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   RCHK(upload_hk(Hk, Nk));
   return solve_resident(Hloc, bath_h, bath_v, omega_out);
+}
+
+// One chain's table as the reference stores it, from the chain's n poles p
+// and weights w (p = isign*(d_j - Ei), d ascending): a chain that stopped
+// after n < nlanc steps also lists the eigenvalues 0 of its zero-padded
+// coefficients (pole isign*(0 - Ei), weight 0) in ascending position
+// (VCA_GF_NORMAL.f90:1006-1022).  Poles out as complex numbers.
+void chain_table(const ChainRec& r, int n, int sg, const double* p, const double2* w, std::vector<double2>& P,
+                 std::vector<double2>& W) {
+  P.clear();
+  W.clear();
+  if (n <= 0) return;
+  const int npad = n < r.nlanc ? r.nlanc - n : 0;
+  const double Ei = g->gs[r.state].e;
+  int q = 0;
+  auto put = [&](double pole, double2 wt) {
+    P.push_back(make_double2(pole, 0.0));
+    W.push_back(wt);
+  };
+  for (int j = 0; j < n; j++) {
+    const double dj = sg * p[j] + Ei;
+    if (q == 0 && npad && dj > 0.0)
+      for (; q < npad; q++) put(sg * (0.0 - Ei), make_double2(0.0, 0.0));
+    put(p[j], w[j]);
+  }
+  for (; q < npad; q++) put(sg * (0.0 - Ei), make_double2(0.0, 0.0));
+}
+
+// file element of (il, jl, is, io, jo), 0-based: the loops of save_gfprime
+// and read_gfprime, ilat outermost, jorb innermost (VCA_AUX_FUNX.f90:627-641)
+inline int64_t gfm_elem(const vca_config& c, int il, int jl, int is, int io, int jo) {
+  return jo + (int64_t)c.Norb * (io + (int64_t)c.Norb * (is + (int64_t)c.Nspin * (jl + (int64_t)c.Nlat * il)));
+}
+
+// The tables of the last solve in file order (impGmatrix as build_gf_normal
+// fills it, VCA_GF_NORMAL.f90:57-80): every spin-diagonal element holds
+// every kept state; 2 channels on the diagonal, 4 (chan4) or 2 (chan2) off
+// it; a channel without target sector has no excitations.
+static int solve_tables(GfmTable& t) {
+  const vca_config& c = g->cfg;
+  RCHK(ensure_poles());
+  const int nch = (int)g->chains.size();
+  const int nst = (int)g->gs.size();
+  std::vector<int> nx(nch), sg(nch);
+  std::vector<double> P((size_t)nch * g->ld);
+  std::vector<double2> W((size_t)nch * g->ld);
+  if (nch) {
+    CUCHK(cudaMemcpy(nx.data(), g->d_nexc, sizeof(int) * nch, cudaMemcpyDeviceToHost));
+    CUCHK(cudaMemcpy(sg.data(), g->cstore.isign, sizeof(int) * nch, cudaMemcpyDeviceToHost));
+    CUCHK(cudaMemcpy(P.data(), g->d_poles, sizeof(double) * P.size(), cudaMemcpyDeviceToHost));
+    CUCHK(cudaMemcpy(W.data(), g->d_weights, sizeof(double2) * W.size(), cudaMemcpyDeviceToHost));
+  }
+  const int nelem = c.Nlat * c.Nlat * c.Nspin * c.Norb * c.Norb;
+  std::vector<int> which((size_t)nelem * nst * 4, -1);  // (elem, state, chan) -> chain
+  for (int ch = 0; ch < nch; ch++) {
+    const ChainRec& r = g->chains[ch];
+    if (r.chan >= 1 && r.chan <= 4 && r.state >= 0 && r.state < nst && r.elem >= 0 && r.elem < nelem)
+      which[((size_t)r.elem * nst + r.state) * 4 + r.chan - 1] = ch;
+  }
+  t = GfmTable{};
+  std::vector<double2> tp, tw;
+  for (int il = 0; il < c.Nlat; il++)
+    for (int jl = 0; jl < c.Nlat; jl++)
+      for (int is = 0; is < c.Nspin; is++)
+        for (int io = 0; io < c.Norb; io++)
+          for (int jo = 0; jo < c.Norb; jo++) {
+            const int e = elem_index(c, il, jl, is, io, jo);
+            const int nchan = (il == jl && io == jo) ? 2 : (c.vca_gf_symmetric ? 2 : 4);
+            t.nstates.push_back(nst);
+            for (int k = 0; k < nst; k++) {
+              t.nchan.push_back(nchan);
+              for (int ich = 1; ich <= nchan; ich++) {
+                const int ch = which[((size_t)e * nst + k) * 4 + ich - 1];
+                if (ch < 0) {
+                  t.nexc.push_back(0);
+                  continue;
+                }
+                chain_table(g->chains[ch], nx[ch], sg[ch], P.data() + (size_t)ch * g->ld,
+                            W.data() + (size_t)ch * g->ld, tp, tw);
+                t.nexc.push_back((int32_t)tp.size());
+                for (size_t j = 0; j < tp.size(); j++) {
+                  t.poles.push_back(tp[j].x);
+                  t.poles.push_back(tp[j].y);
+                  t.weights.push_back(tw[j].x);
+                  t.weights.push_back(tw[j].y);
+                }
+              }
+            }
+          }
+  return VCA_OK;
+}
+
+static std::string gfm_path(const char* file, const char* suffix, int32_t used) {
+  return std::string(file) + (suffix ? suffix : "") + (used ? ".used" : ".restart");  // VCA_AUX_FUNX.f90:615-617
+}
+
+static void gfm_drop() {
+  if (!g) return;
+  g->gfm_dev.release();
+  g->d_gfm_ptr = nullptr;
+  g->d_gfm_p = g->d_gfm_w = nullptr;
+  g->gfm = GfmTable{};
+  g->gfm_state0.clear();
+  g->gfm_chan0.clear();
+  g->gfm_exc0.clear();
+  g->gfm_loaded = false;
 }
 
 }  // namespace
@@ -2151,6 +2278,7 @@ int vca_gpu_last_error(char* buf, int32_t len) {
 
 int vca_gpu_finalize(void) {
   if (!g) return VCA_OK;
+  gfm_drop();
   g->work.release();
   g->nodes.release();
   g->omega.release();
@@ -2296,11 +2424,28 @@ int vca_gpu_get_sector_energies(double* e_out, int32_t n) {
 int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t iorb, int32_t jorb,
                            int32_t istate, int32_t ichan, int32_t* nexc, double* poles, double* weights,
                            int32_t cap) {
-  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!g || !(g->solved || g->gfm_loaded)) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   const vca_config& c = g->cfg;
   if (ilat < 1 || ilat > c.Nlat || jlat < 1 || jlat > c.Nlat || ispin < 1 || ispin > c.Nspin ||
       iorb < 1 || iorb > c.Norb || jorb < 1 || jorb > c.Norb)
     VFAIL(VCA_ERR_ARG, "element index out of range");
+  if (nexc) *nexc = 0;  // channel absent (no target sector): Nexc=0 in the reference
+  if (g->gfm_loaded) {
+    const GfmTable& t = g->gfm;
+    const int64_t f = gfm_elem(c, ilat - 1, jlat - 1, ispin - 1, iorb - 1, jorb - 1);
+    if (istate < 1 || istate > t.nstates[f]) return VCA_OK;
+    const int64_t st = g->gfm_state0[f] + istate - 1;
+    if (ichan < 1 || ichan > t.nchan[st]) return VCA_OK;
+    const int64_t ci = g->gfm_chan0[st] + ichan - 1;
+    const int n = t.nexc[ci];
+    const int64_t x0 = g->gfm_exc0[ci];
+    if (nexc) *nexc = n;
+    if (cap >= n) {
+      if (poles) std::memcpy(poles, t.poles.data() + 2 * x0, sizeof(double) * 2 * n);
+      if (weights) std::memcpy(weights, t.weights.data() + 2 * x0, sizeof(double) * 2 * n);
+    }
+    return VCA_OK;
+  }
   const int e = elem_index(c, ilat - 1, jlat - 1, ispin - 1, iorb - 1, jorb - 1);
   RCHK(ensure_poles());
   for (int ch = 0; ch < (int)g->chains.size(); ch++) {
@@ -2309,42 +2454,157 @@ int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t io
     int n = 0, sg = 1;
     CUCHK(cudaMemcpy(&n, g->d_nexc + ch, sizeof(int), cudaMemcpyDeviceToHost));
     CUCHK(cudaMemcpy(&sg, g->cstore.isign + ch, sizeof(int), cudaMemcpyDeviceToHost));
-    // a chain that stopped after n < nlanc steps: the reference's table has
-    // Nexc = nlanc entries, the zeros left in its coefficient arrays giving
-    // eigenvalues 0 (pole isign*(0 - Ei), weight 0) in ascending order
-    // (VCA_GF_NORMAL.f90:1006-1022)
-    const int npad = (n > 0 && n < r.nlanc) ? r.nlanc - n : 0;
-    const int ntot = n + npad;
-    if (nexc) *nexc = ntot;
-    if (cap >= ntot && n > 0) {
-      std::vector<double> p(n);
-      std::vector<double2> w(n);
+    std::vector<double> p(std::max(n, 1));
+    std::vector<double2> w(std::max(n, 1));
+    if (n > 0) {
       CUCHK(cudaMemcpy(p.data(), g->d_poles + (size_t)ch * g->ld, sizeof(double) * n, cudaMemcpyDeviceToHost));
       CUCHK(cudaMemcpy(w.data(), g->d_weights + (size_t)ch * g->ld, sizeof(double2) * n, cudaMemcpyDeviceToHost));
-      const double Ei = g->gs[r.state].e;
-      int q = 0, out = 0;
-      auto put = [&](double pole, double2 wt) {
-        if (poles) { poles[2 * out] = pole; poles[2 * out + 1] = 0.0; }
-        if (weights) { weights[2 * out] = wt.x; weights[2 * out + 1] = wt.y; }
-        out++;
-      };
-      for (int j = 0; j < n; j++) {  // p[j] = isign*(d_j - Ei), d ascending
-        const double dj = sg * p[j] + Ei;
-        if (q == 0 && npad && dj > 0.0) {
-          for (; q < npad; q++) put(sg * (0.0 - Ei), make_double2(0.0, 0.0));
-        }
-        put(p[j], w[j]);
-      }
-      for (; q < npad; q++) put(sg * (0.0 - Ei), make_double2(0.0, 0.0));
+    }
+    std::vector<double2> P, W;
+    chain_table(r, n, sg, p.data(), w.data(), P, W);
+    if (nexc) *nexc = (int32_t)P.size();
+    if (cap >= (int)P.size()) {
+      if (poles) std::memcpy(poles, P.data(), sizeof(double2) * P.size());
+      if (weights) std::memcpy(weights, W.data(), sizeof(double2) * W.size());
     }
     return VCA_OK;
   }
-  if (nexc) *nexc = 0;  // channel absent (no target sector), as Nexc=0 in the reference
   return VCA_OK;
 }
 
-int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out) {
-  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+int vca_gpu_save_gfprime(const char* file, const char* suffix, int32_t used, int32_t formatted) {
+  if (!g || !(g->solved || g->gfm_loaded))
+    VFAIL(VCA_ERR_STATE, "vca_gf_cluster ERROR: impGmatrix not allocated!");  // VCA_AUX_FUNX.f90:614
+  if (!file) VFAIL(VCA_ERR_ARG, "file is NULL");
+  std::string err;
+  if (g->gfm_loaded) {
+    if (gfm_write(gfm_path(file, suffix, used), formatted != 0, g->gfm, err)) VFAIL(VCA_ERR_IO, err);
+    return VCA_OK;
+  }
+  GfmTable t;
+  RCHK(solve_tables(t));
+  if (gfm_write(gfm_path(file, suffix, used), formatted != 0, t, err)) VFAIL(VCA_ERR_IO, err);
+  return VCA_OK;
+}
+
+int vca_gpu_read_gfprime(const char* file, const char* suffix, int32_t used, int32_t formatted) {
+  if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (!file) VFAIL(VCA_ERR_ARG, "file is NULL");
+  const vca_config& c = g->cfg;
+  const int64_t nelem = (int64_t)c.Nlat * c.Nlat * c.Nspin * c.Norb * c.Norb;
+  GfmTable t;
+  std::string err;
+  if (gfm_read(gfm_path(file, suffix, used), formatted != 0, nelem, t, err)) VFAIL(VCA_ERR_IO, err);
+  // offsets into the flattened counts, and each file element's excitations
+  // (contiguous in file order)
+  std::vector<int64_t> s0(nelem), c0(t.nchan.size()), x0(t.nexc.size()), ex0(nelem + 1);
+  int64_t a = 0, b = 0, x = 0;
+  for (int64_t f = 0; f < nelem; f++) {
+    s0[f] = a;
+    ex0[f] = x;
+    for (int k = 0; k < t.nstates[f]; k++, a++) {
+      c0[a] = b;
+      for (int q = 0; q < t.nchan[a]; q++, b++) {
+        x0[b] = x;
+        x += t.nexc[b];
+      }
+    }
+  }
+  ex0[nelem] = x;
+  // device layout: elements in elem_index order
+  std::vector<int64_t> ptr(nelem + 1, 0);
+  std::vector<int64_t> src(nelem);  // file element of each elem_index
+  for (int il = 0; il < c.Nlat; il++)
+    for (int jl = 0; jl < c.Nlat; jl++)
+      for (int is = 0; is < c.Nspin; is++)
+        for (int io = 0; io < c.Norb; io++)
+          for (int jo = 0; jo < c.Norb; jo++) src[elem_index(c, il, jl, is, io, jo)] = gfm_elem(c, il, jl, is, io, jo);
+  for (int64_t e = 0; e < nelem; e++) ptr[e + 1] = ptr[e] + (ex0[src[e] + 1] - ex0[src[e]]);
+  std::vector<double2> hp((size_t)std::max<int64_t>(x, 1)), hw((size_t)std::max<int64_t>(x, 1));
+  for (int64_t e = 0; e < nelem; e++) {
+    const int64_t f = src[e], n = ex0[f + 1] - ex0[f];
+    if (n) {
+      std::memcpy(hp.data() + ptr[e], t.poles.data() + 2 * ex0[f], sizeof(double2) * n);
+      std::memcpy(hw.data() + ptr[e], t.weights.data() + 2 * ex0[f], sizeof(double2) * n);
+    }
+  }
+  gfm_drop();
+  int rc;
+  if ((rc = g->gfm_dev.alloc(&g->d_gfm_ptr, nelem + 1)) || (rc = g->gfm_dev.alloc(&g->d_gfm_p, hp.size())) ||
+      (rc = g->gfm_dev.alloc(&g->d_gfm_w, hw.size()))) {
+    gfm_drop();
+    return rc;
+  }
+  cudaError_t ce = cudaMemcpy(g->d_gfm_ptr, ptr.data(), sizeof(int64_t) * ptr.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(g->d_gfm_p, hp.data(), sizeof(double2) * hp.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(g->d_gfm_w, hw.data(), sizeof(double2) * hw.size(), cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) {
+    gfm_drop();
+    VFAIL(VCA_ERR_CUDA, cudaGetErrorString(ce));
+  }
+  g->gfm = std::move(t);
+  g->gfm_state0 = std::move(s0);
+  g->gfm_chan0 = std::move(c0);
+  g->gfm_exc0 = std::move(x0);
+  g->gfm_loaded = true;
+  return VCA_OK;
+}
+
+int vca_gfm_write(const char* path, int32_t formatted, int64_t nelem, const int32_t* nstates, const int32_t* nchan,
+                  const int32_t* nexc, const double* poles, const double* weights) {
+  if (!path || nelem < 0 || (nelem > 0 && !nstates)) VFAIL(VCA_ERR_ARG, "bad arguments");
+  GfmTable t;
+  t.nstates.assign(nstates, nstates + nelem);
+  int64_t ns = 0, nc = 0, ne = 0;
+  for (int32_t v : t.nstates) {
+    if (v < 0) VFAIL(VCA_ERR_ARG, "negative state count");
+    ns += v;
+  }
+  if (ns > 0 && !nchan) VFAIL(VCA_ERR_ARG, "nchan is NULL");
+  t.nchan.assign(nchan, nchan + ns);
+  for (int32_t v : t.nchan) {
+    if (v < 0) VFAIL(VCA_ERR_ARG, "negative channel count");
+    nc += v;
+  }
+  if (nc > 0 && !nexc) VFAIL(VCA_ERR_ARG, "nexc is NULL");
+  t.nexc.assign(nexc, nexc + nc);
+  for (int32_t v : t.nexc) {
+    if (v < 0) VFAIL(VCA_ERR_ARG, "negative excitation count");
+    ne += v;
+  }
+  if (ne > 0 && (!poles || !weights)) VFAIL(VCA_ERR_ARG, "poles or weights is NULL");
+  t.poles.assign(poles, poles + 2 * ne);
+  t.weights.assign(weights, weights + 2 * ne);
+  std::string err;
+  if (gfm_write(path, formatted != 0, t, err)) VFAIL(VCA_ERR_IO, err);
+  return VCA_OK;
+}
+
+int vca_gfm_read(const char* path, int32_t formatted, int64_t nelem, int64_t* sizes, int32_t* nstates,
+                 int32_t* nchan, int32_t* nexc, double* poles, double* weights) {
+  if (!path || !sizes || nelem < 0) VFAIL(VCA_ERR_ARG, "bad arguments");
+  GfmTable t;
+  std::string err;
+  if (gfm_read(path, formatted != 0, nelem, t, err)) VFAIL(VCA_ERR_IO, err);
+  const int64_t ns = (int64_t)t.nchan.size(), nc = (int64_t)t.nexc.size(), ne = (int64_t)t.poles.size() / 2;
+  if (nstates) {
+    if (sizes[0] < ns || sizes[1] < nc || sizes[2] < ne) VFAIL(VCA_ERR_ARG, "arrays smaller than the file's table");
+    if ((ns && !nchan) || (nc && !nexc) || (ne && (!poles || !weights))) VFAIL(VCA_ERR_ARG, "NULL array");
+    std::copy(t.nstates.begin(), t.nstates.end(), nstates);
+    std::copy(t.nchan.begin(), t.nchan.end(), nchan);
+    std::copy(t.nexc.begin(), t.nexc.end(), nexc);
+    std::copy(t.poles.begin(), t.poles.end(), poles);
+    std::copy(t.weights.begin(), t.weights.end(), weights);
+  }
+  sizes[0] = ns;
+  sizes[1] = nc;
+  sizes[2] = ne;
+  return VCA_OK;
+}
+
+// G'(z) at nz host points into the caller's (Nlat,Nlat,Nspin,Nspin,Norb,
+// Norb,nz) array; solve_tables as in gf_lso
+static int gf_cluster_host(const double* z, int64_t nz, double* gf_out, bool solve_tables) {
   if (!z || !gf_out || nz < 0) VFAIL(VCA_ERR_ARG, "bad arguments");
   if (nz == 0) return VCA_OK;
   const vca_config& c = g->cfg;
@@ -2354,7 +2614,7 @@ int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out) {
   int rc;
   if ((rc = ar.alloc(&dz, nz)) || (rc = ar.alloc(&Glso, (size_t)nz * NN))) { ar.release(); return rc; }
   cudaMemcpyAsync(dz, z, sizeof(double2) * nz, cudaMemcpyHostToDevice, g->st);
-  if ((rc = gf_lso((int)nz, dz, Glso, ar))) { ar.release(); return rc; }
+  if ((rc = gf_lso((int)nz, dz, Glso, ar, solve_tables))) { ar.release(); return rc; }
   std::vector<double2> h((size_t)nz * NN);
   cudaMemcpyAsync(h.data(), Glso, sizeof(double2) * h.size(), cudaMemcpyDeviceToHost, g->st);
   cudaError_t e = cudaStreamSynchronize(g->st);
@@ -2376,6 +2636,11 @@ int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out) {
                 gf_out[2 * o + 1] = v.y;
               }
   return VCA_OK;
+}
+
+int vca_gpu_gf_cluster(const double* z, int64_t nz, double* gf_out) {
+  if (!g || !(g->solved || g->gfm_loaded)) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  return gf_cluster_host(z, nz, gf_out, false);
 }
 
 // the Matsubara (wm = pi/beta*(2n-1), VCA_GF_SHARED.f90:50) or real-axis
@@ -2400,7 +2665,7 @@ static int gimp_grid(bool mats, double* g_out) {
   if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   if (!g_out) VFAIL(VCA_ERR_ARG, "NULL output");
   const std::vector<double> z = freq_grid(mats);
-  return vca_gpu_gf_cluster(z.data(), (int64_t)(z.size() / 2), g_out);
+  return gf_cluster_host(z.data(), (int64_t)(z.size() / 2), g_out, true);
 }
 
 // Sigma (want_g0 = false) or G0 on the Matsubara or real-axis grid, as
@@ -2424,7 +2689,7 @@ static int sigma_grid(bool mats, bool want_g0, double* out) {
   }
   cudaMemcpyAsync(dz, zh.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, g->st);
   if (!want_g0) {
-    if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = gf_lso(n, dz, Glso, ar))) { ar.release(); return rc; }
+    if ((rc = ar.alloc(&Glso, (size_t)n * NN)) || (rc = gf_lso(n, dz, Glso, ar, true))) { ar.release(); return rc; }
   }
   {
     double2* hraw;

@@ -721,6 +721,35 @@ void launch_gf_eval(const GfLayout& g, int nz, const double2* z, double2* G, cud
   k_gf_eval<<<nblocks(n, 128), 128, 0, st>>>(g, nz, z, G);
 }
 
+// Pole tables as vca_gf_cluster_scalar sums them (VCA_IO/gf_cluster.f90:
+// 30-45): per (z, element) thread, weight/(z - pole) over the element's
+// states, channels and excitations in table order; poles and weights complex.
+__global__ void k_gf_eval_poles(int nelem, const int64_t* ptr, const double2* poles, const double2* weights,
+                                int nz, const double2* z, double2* G) {
+  const int64_t n = (int64_t)nz * nelem;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t % nelem);
+    const int q = (int)(t / nelem);
+    const double2 zq = z[q];
+    double ar = 0.0, ai = 0.0;
+    for (int64_t x = ptr[e]; x < ptr[e + 1]; x++) {
+      const double dr = zq.x - poles[x].x, di = zq.y - poles[x].y;
+      const double inv = 1.0 / fma(dr, dr, di * di);
+      const double2 w = weights[x];
+      ar += (w.x * dr + w.y * di) * inv;  // w conj(d) / |d|^2
+      ai += (w.y * dr - w.x * di) * inv;
+    }
+    G[t] = make_double2(ar, ai);
+  }
+}
+void launch_gf_eval_poles(int nelem, const int64_t* ptr, const double2* poles, const double2* weights, int nz,
+                          const double2* z, double2* G, cudaStream_t st) {
+  COUNT_LAUNCH();
+  int64_t n = (int64_t)nz * nelem;
+  k_gf_eval_poles<<<nblocks(n, 128), 128, 0, st>>>(nelem, ptr, poles, weights, nz, z, G);
+}
+
 __global__ void k_gf_assemble(ClusterDims cd, int nz, const double2* Graw, double2* Glso) {
   const int N = cd.N, NN = N * N;
   const int nel = cd.Nlat * cd.Nlat * cd.Nspin * cd.Norb * cd.Norb;

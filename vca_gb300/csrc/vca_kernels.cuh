@@ -128,6 +128,10 @@ struct GfLayout {
 };
 // raw element sums at nz points z (complex): G[z*nelem + e]
 void launch_gf_eval(const GfLayout& g, int nz, const double2* z, double2* G, cudaStream_t st);
+// the same raw sums from pole tables (a GFmatrix read from a restart file):
+// G[z*nelem + e] = sum over ptr[e] <= x < ptr[e+1] of weights[x] / (z - poles[x])
+void launch_gf_eval_poles(int nelem, const int64_t* ptr, const double2* poles, const double2* weights, int nz,
+                          const double2* z, double2* G, cudaStream_t st);
 // recombination + lso assembly: Glso[z][N*N] from raw G
 struct ClusterDims {
   int Nlat, Norb, Nspin, N;

@@ -36,6 +36,7 @@ EXPORTS = [
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
+    "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
 ]
 
 
@@ -122,6 +123,12 @@ def load(path: Optional[str] = None):
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
         "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
+        "vca_gpu_save_gfprime": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, i32, i32]),
+        "vca_gpu_read_gfprime": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, i32, i32]),
+        "vca_gfm_write": (ctypes.c_int, [ctypes.c_char_p, i32, i64, ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                         ctypes.POINTER(i32), dp, dp]),
+        "vca_gfm_read": (ctypes.c_int, [ctypes.c_char_p, i32, i64, ctypes.POINTER(i64), ctypes.POINTER(i32),
+                                        ctypes.POINTER(i32), ctypes.POINTER(i32), dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -430,8 +437,93 @@ class VcaSolver:
         check(self.L.vca_gpu_hxv(isector, _dp(v), _dp(hv)))
         return hv
 
+    def save_gfprime(self, file: str = "gfprime", used: bool = False, use_formatted: bool = False,
+                     suffix: str = ""):
+        """save_gfprime (VCA_AUX_FUNX.f90:601-645): the pole tables of the
+        last solve (or of the last read_gfprime) to file//suffix//".restart"
+        (".used" when used)."""
+        check(self.L.vca_gpu_save_gfprime(file.encode(), suffix.encode(), int(used), int(use_formatted)))
+        return gfprime_path(file, used, suffix)
+
+    def read_gfprime(self, file: str = "gfprime", used: bool = False, use_formatted: bool = False,
+                     suffix: str = ""):
+        """read_gfprime (VCA_AUX_FUNX.f90:651-697): the tables replace the
+        solve's for gf_cluster and gf_channel until the next solve."""
+        check(self.L.vca_gpu_read_gfprime(file.encode(), suffix.encode(), int(used), int(use_formatted)))
+
     def close(self):
         self.L.vca_gpu_finalize()
+
+
+# ---- GFmatrix restart files (host only, no GPU needed) --------------------
+def gfprime_path(file: str = "gfprime", used: bool = False, suffix: str = "") -> str:
+    """file//file_suffix//(".used" | ".restart") (VCA_AUX_FUNX.f90:615-617)."""
+    return file + suffix + (".used" if used else ".restart")
+
+
+def gfm_elements(cfg: VcaConfig):
+    """(ilat, jlat, ispin, iorb, jorb), 1-based, in the order of the file's
+    elements: the loops of save_gfprime, ilat outermost (VCA_AUX_FUNX.f90:
+    627-641)."""
+    return [(il, jl, s, io, jo)
+            for il in range(1, cfg.Nlat + 1) for jl in range(1, cfg.Nlat + 1)
+            for s in range(1, cfg.Nspin + 1)
+            for io in range(1, cfg.Norb + 1) for jo in range(1, cfg.Norb + 1)]
+
+
+def write_gfmatrix(path: str, table, formatted: bool = False):
+    """Write a GFmatrix table: table[element][state][channel] = (poles,
+    weights), complex arrays of equal length, elements in file order."""
+    ns, nc, nx, P, W = [], [], [], [], []
+    for el in table:
+        ns.append(len(el))
+        for st in el:
+            nc.append(len(st))
+            for p, w in st:
+                p = np.asarray(p, dtype=np.complex128).ravel()
+                w = np.asarray(w, dtype=np.complex128).ravel()
+                if p.shape != w.shape:
+                    raise VcaError(-9, "poles and weights differ in length")
+                nx.append(len(p))
+                P.append(p)
+                W.append(w)
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    a_ns, a_nc, a_nx = (np.array(v, dtype=np.int32) for v in (ns, nc, nx))
+    a_p = np.ascontiguousarray(np.concatenate(P) if P else np.zeros(0, np.complex128))
+    a_w = np.ascontiguousarray(np.concatenate(W) if W else np.zeros(0, np.complex128))
+    check(load().vca_gfm_write(path.encode(), int(formatted), len(ns), a_ns.ctypes.data_as(i32p),
+                               a_nc.ctypes.data_as(i32p), a_nx.ctypes.data_as(i32p), _dp(a_p), _dp(a_w)))
+
+
+def read_gfmatrix(path: str, nelem: int, formatted: bool = False):
+    """Read nelem elements of a GFmatrix file into
+    table[element][state][channel] = (poles, weights)."""
+    L = load()
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    sizes = np.zeros(3, dtype=np.int64)
+    check(L.vca_gfm_read(path.encode(), int(formatted), nelem, sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                         None, None, None, None, None))
+    ns = np.zeros(max(nelem, 1), np.int32)
+    nc = np.zeros(max(int(sizes[0]), 1), np.int32)
+    nx = np.zeros(max(int(sizes[1]), 1), np.int32)
+    P = np.zeros(max(int(sizes[2]), 1), np.complex128)
+    W = np.zeros(max(int(sizes[2]), 1), np.complex128)
+    check(L.vca_gfm_read(path.encode(), int(formatted), nelem, sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                         ns.ctypes.data_as(i32p), nc.ctypes.data_as(i32p), nx.ctypes.data_as(i32p), _dp(P), _dp(W)))
+    table, a, b, x = [], 0, 0, 0
+    for e in range(nelem):
+        el = []
+        for _ in range(ns[e]):
+            st = []
+            for _ in range(nc[a]):
+                n = int(nx[b])
+                st.append((P[x:x + n].copy(), W[x:x + n].copy()))
+                x += n
+                b += 1
+            el.append(st)
+            a += 1
+        table.append(el)
+    return table
 
 
 # ---- functional interface with the reference's names ---------------------
