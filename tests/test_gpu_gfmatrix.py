@@ -1,8 +1,10 @@
 """GPU: GFmatrix restart files through the C-ABI (vca_gpu_save_gfprime /
 vca_gpu_read_gfprime, VCA_AUX_FUNX.f90:601-697).
 
-* save: the file holds the oracle's impGmatrix -- every element, every state,
-  2 or 4 channels, the same excitation counts (exact) -- with pole sums
+* save: the file holds the oracle's impGmatrix -- every element, every state
+  (in the GPU's list order, which inside a degenerate group follows each
+  run's rounding), 2 or 4 channels, the same excitation counts (exact) --
+  with pole sums
   equal to the oracle's at points off the real axis (1e-8, the G' parity
   tolerance), and exactly the tables vca_gpu_get_gf_channel lists;
 * read into a fresh context (init, no solve): G'(z) from the loaded tables
@@ -57,6 +59,16 @@ def psum(p, w):
     return (w[None, :] / (Z[:, None] - p[None, :])).sum(axis=1)
 
 
+def _align(ref, states, ref_states):
+    """The oracle's table with its states in the order of the GPU's list.
+    Inside a group of degenerate states the list order follows each run's
+    rounding; the Lanczos method keeps one state per sector, so the sector
+    names the state."""
+    assert sorted(x[0] for x in states) == sorted(x[0] for x in ref_states)
+    pos = {sec: k for k, (sec, _) in enumerate(ref_states)}
+    return [[el[pos[sec]] for sec, _ in states] for el in ref]
+
+
 def _read(path, nelem, formatted):
     data = open(path, "rb").read()
     return ogm.decode_formatted(data.decode(), nelem) if formatted else ogm.decode_unformatted(data, nelem)
@@ -70,7 +82,7 @@ def test_save_matches_oracle_and_read_gives_back_gf(tmp_path, name):
     g_solve = s.gf_cluster(Z)
     o = Oracle.from_point(pt)
     o.solve()
-    ref = ogm.table_from_oracle(o, pt.cfg)
+    ref = _align(ogm.table_from_oracle(o, pt.cfg), s.states(), o.states())
     els = gfm_elements(pt.cfg)
     stem = str(tmp_path / "gfprime")
     for formatted in (False, True):
