@@ -115,6 +115,14 @@ typedef struct vca_config {
   double bandwidth;        /* bandwidth  lattice bandwidth (a module variable */
                            /* the reference's drivers assign, default 0)     */
   double gs_beta_tol;      /* ground-state Lanczos: beta_{k+1} < tol ends it */
+  /* ---- output files ----------------------------------------------------- */
+  int32_t print_sigma;     /* PRINT_SIGMA  splot files of Sigma after a solve */
+  int32_t print_impg;      /* PRINT_IMPG   ... of G'  (VCA_INPUT_VARS.f90:137-139; */
+  int32_t print_impg0;     /* PRINT_IMPG0  ... of G0   the reference's default is */
+                           /* on, here off: see vca_gpu_print_impSigma)           */
+  int32_t pad2;
+  char file_suffix[64];    /* the reference's file_suffix, NUL-terminated: ends  */
+                           /* the stem of every file name (VCA_IO.f90:126-128)   */
 } vca_config;
 
 /* Fill *cfg with the reference defaults (VCA_INPUT_VARS.f90:112-172) plus
@@ -195,6 +203,22 @@ int vca_gpu_get_sigma_realaxis(double* s_out);
  * with vca_print_impG0 (VCA_IO.f90:179-205). */
 int vca_gpu_get_g0_matsubara(double* g0_out);
 int vca_gpu_get_g0_realaxis(double* g0_out);
+/* splot files of the last solve (vca_print_impSigma / vca_print_impG /
+ * vca_print_impG0, VCA_IO.f90:112-205): Sigma, G' or G0 on the Matsubara and
+ * the real-axis grid, one file per spin-diagonal element and grid in the
+ * working directory, named
+ *   <impSigma|impG|impG0>_Isite<ilat:4 digits>_Jsite<jlat:4 digits>_l<iorb><jorb>_s<ispin>_<iw|realw><file_suffix>.vca
+ * one line per frequency: x, Im, Re (SciFortran splot's column order) with
+ * 17 significant digits.  vca_gpu_solve, _solve_batch (its last point) and
+ * _solve_resident call them when cfg.print_sigma / print_impg / print_impg0
+ * are set, as vca_solve does with PRINT_SIGMA / PRINT_IMPG / PRINT_IMPG0
+ * (VCA_GREENS_FUNCTIONS.f90:37-41).  The flags default to off here: at the
+ * reference's grid sizes the files hold ~10^6 lines per solve, more time
+ * than the GPU solve itself. */
+int vca_gpu_print_impSigma(void);
+int vca_gpu_print_impG(void);
+int vca_gpu_print_impG0(void);
+
 /* Ground-state observables of the last solve, (Nlat,Norb) column-major:
  * density n_up + n_dw, its spin parts, double occupancy n_up n_dw and
  * magnetisation n_up - n_dw, averaged over the kept states with weight
@@ -238,8 +262,8 @@ int vca_gpu_get_gf_channel(int32_t ilat, int32_t jlat, int32_t ispin, int32_t io
  * 601-697): the pole tables of every spin-diagonal element in file
  * file//suffix//".restart" (".used" when used != 0), formatted = list-directed
  * text or 0 = sequential unformatted records (write_formatted /
- * write_unformatted, :486-593).  suffix may be NULL (the reference's
- * file_suffix, empty by default).
+ * write_unformatted, :486-593).  suffix NULL means cfg.file_suffix, the
+ * module variable the reference appends.
  * save: the tables of the last solve, as vca_gpu_get_gf_channel lists them.
  * read: needs vca_gpu_init only; the tables replace the solve's until the
  * next solve, for vca_gpu_gf_cluster (evaluated on the GPU as

@@ -61,3 +61,24 @@ def test_bad_config_rejected_on_host(lib):
     assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
     c = default_config(Nlat=2, lanc_nstates_total=2, lanc_niter_spectrum=0)
     assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
+
+
+def test_file_calls_without_context(lib):
+    """The output-file entry points fail with VCA_ERR_STATE before a context
+    exists, and the host codec checks its arguments; no GPU call is made."""
+    lib.vca_gpu_finalize()
+    for f in (lib.vca_gpu_print_impSigma, lib.vca_gpu_print_impG, lib.vca_gpu_print_impG0):
+        assert f() == -3
+    assert lib.vca_gpu_save_gfprime(b"gfprime", None, 0, 0) == -3
+    assert lib.vca_gpu_read_gfprime(b"gfprime", None, 0, 0) == -3
+    assert lib.vca_gfm_read(b"x", 0, 1, None, None, None, None, None, None) == -9
+    assert lib.vca_gfm_write(None, 0, 0, None, None, None, None, None) == -9
+    neg = (ctypes.c_int32 * 1)(-1)
+    assert lib.vca_gfm_write(b"x", 0, 1, neg, None, None, None, None) == -9
+
+
+def test_unterminated_file_suffix_rejected(lib):
+    c = default_config(Nlat=2)
+    c.file_suffix = b"x" * 64
+    assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
+    assert default_config(file_suffix="_a").file_suffix == b"_a"

@@ -70,6 +70,11 @@ class VcaConfig(ctypes.Structure):
         ("cutoff", ctypes.c_double),
         ("bandwidth", ctypes.c_double),
         ("gs_beta_tol", ctypes.c_double),
+        ("print_sigma", ctypes.c_int32),
+        ("print_impg", ctypes.c_int32),
+        ("print_impg0", ctypes.c_int32),
+        ("pad2", ctypes.c_int32),
+        ("file_suffix", ctypes.c_char * 64),
     ]
 
     def copy(self) -> "VcaConfig":
@@ -80,7 +85,7 @@ class VcaConfig(ctypes.Structure):
     def as_dict(self) -> dict:
         out = {}
         for name, _ in self._fields_:
-            if name in ("pad0", "pad1"):
+            if name in ("pad0", "pad1", "pad2"):
                 continue
             v = getattr(self, name)
             out[name] = list(v) if name == "Uloc" else v
@@ -118,12 +123,16 @@ def default_config(**overrides) -> VcaConfig:
     c.lanc_nstates_step, c.lanc_niter_spectrum = 2, 10
     c.cutoff, c.bandwidth = 1e-9, 0.0
     c.contour_nodes = 24
+    c.print_sigma = c.print_impg = c.print_impg0 = 0  # on in the reference (VCA_INPUT_VARS.f90:137-139)
+    c.file_suffix = b""
     for k, v in overrides.items():
         if k == "Uloc":
             for i in range(5):
                 c.Uloc[i] = v[i] if i < len(v) else 0.0
         elif not hasattr(c, k):
             raise KeyError(f"unknown input variable {k}")
+        elif k == "file_suffix":
+            c.file_suffix = v.encode() if isinstance(v, str) else v
         else:
             setattr(c, k, v)
     return c

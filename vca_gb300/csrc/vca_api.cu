@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cerrno>
 #include <cfloat>
 #include <cmath>
 #include <complex>
@@ -2200,7 +2201,9 @@ static int solve_tables(GfmTable& t) {
 }
 
 static std::string gfm_path(const char* file, const char* suffix, int32_t used) {
-  return std::string(file) + (suffix ? suffix : "") + (used ? ".used" : ".restart");  // VCA_AUX_FUNX.f90:615-617
+  const vca_config& c = g->cfg;
+  const std::string sfx = suffix ? std::string(suffix) : std::string(c.file_suffix, strnlen(c.file_suffix, sizeof c.file_suffix));
+  return std::string(file) + sfx + (used ? ".used" : ".restart");  // VCA_AUX_FUNX.f90:615-617
 }
 
 static void gfm_drop() {
@@ -2266,6 +2269,8 @@ void vca_config_defaults(vca_config* c) {
   c->cutoff = 1e-9;             // VCA_INPUT_VARS.f90:169
   c->bandwidth = 0.0;
   c->contour_nodes = 24;
+  c->print_sigma = c->print_impg = c->print_impg0 = 0;  // on in the reference (VCA_INPUT_VARS.f90:137-139)
+  c->file_suffix[0] = 0;
 }
 
 int vca_gpu_last_error(char* buf, int32_t len) {
@@ -2315,6 +2320,8 @@ int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath
     if (!std::isfinite(c.bandwidth)) VFAIL(VCA_ERR_CONFIG, "bandwidth must be finite");
   }
   if (c.vca_twin) VFAIL(VCA_ERR_UNSUPPORTED, "VCA_TWIN is outside the GPU path");
+  if (strnlen(c.file_suffix, sizeof c.file_suffix) == sizeof c.file_suffix)
+    VFAIL(VCA_ERR_CONFIG, "file_suffix is not NUL-terminated within 64 characters");
   if (c.lanc_ngfiter < 1 || c.lanc_niter < 1) VFAIL(VCA_ERR_CONFIG, "LANC_NITER and LANC_NGFITER must be >= 1");
   if (c.omega_nodes < 2) VFAIL(VCA_ERR_CONFIG, "omega_nodes must be >= 2");
   if (!(c.omega_scale > 0.0)) VFAIL(VCA_ERR_CONFIG, "omega_scale must be > 0");
@@ -2363,11 +2370,14 @@ int vca_gpu_set_hamiltonian(const double* Hloc, const double* bath_h, const doub
   return set_hamiltonian(Hloc, bath_h, bath_v);
 }
 
+static int print_after_solve();
+
 int vca_gpu_solve(const double* Hloc, const double* Hk, int64_t Nk, const double* bath_h,
                   const double* bath_v, double* omega_out) {
   g_err.clear();
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
-  return solve_one(Hloc, Hk, Nk, bath_h, bath_v, omega_out);
+  RCHK(solve_one(Hloc, Hk, Nk, bath_h, bath_v, omega_out));
+  return print_after_solve();
 }
 
 int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc, const double* Hk, int64_t Nk,
@@ -2383,7 +2393,7 @@ int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc, cons
                         bath_h ? bath_h + 2 * (size_t)b * stride_bath_h : nullptr,
                         bath_v ? bath_v + 2 * (size_t)b * stride_bath_v : nullptr, omega_out + b));
   }
-  return VCA_OK;
+  return print_after_solve();  // the files of the last point, as a loop of vca_solve leaves them
 }
 
 int vca_gpu_get_sft_potential(double* omega) {
@@ -2791,6 +2801,77 @@ int vca_gpu_get_dens_dw(double* out) { return observable(2, out); }
 int vca_gpu_get_docc(double* out) { return observable(3, out); }
 int vca_gpu_get_mag(double* out) { return observable(4, out); }
 
+// ---- splot files (vca_print_impSigma / vca_print_impG / vca_print_impG0,
+// VCA_IO.f90:112-205) -------------------------------------------------------
+static std::string cfg_suffix() {
+  const vca_config& c = g->cfg;
+  return std::string(c.file_suffix, strnlen(c.file_suffix, sizeof c.file_suffix));
+}
+
+// one file per spin-diagonal element and grid:
+// <name>_Isite<ilat:4>_Jsite<jlat:4>_l<iorb><jorb>_s<ispin>_<iw|realw><file_suffix>.vca
+// (the suffix built at VCA_IO.f90:125-128), written as SciFortran's splot
+// writes a complex function: one line per point, x, Im y, Re y; 17
+// significant digits, so the text reads back bit-exact
+static int print_function(int kind /* 0 G', 1 Sigma, 2 G0 */) {
+  static const char* names[3] = {"impG", "impSigma", "impG0"};
+  const vca_config& c = g->cfg;
+  const std::string sfx = cfg_suffix();
+  const size_t nel = hloc_len(c);
+  for (int m = 0; m < 2; m++) {
+    const bool mats = (m == 0);
+    const int L = mats ? c.Lmats : c.Lreal;
+    if (L <= 0) continue;
+    std::vector<double> y(2 * nel * (size_t)L);
+    RCHK(kind == 0 ? gimp_grid(mats, y.data()) : sigma_grid(mats, kind == 2, y.data()));
+    const std::vector<double> z = freq_grid(mats);
+    for (int il = 0; il < c.Nlat; il++)
+      for (int jl = 0; jl < c.Nlat; jl++)
+        for (int io = 0; io < c.Norb; io++)
+          for (int jo = 0; jo < c.Norb; jo++)
+            for (int is = 0; is < c.Nspin; is++) {
+              char tag[96];
+              std::snprintf(tag, sizeof tag, "_Isite%04d_Jsite%04d_l%d%d_s%d_%s", il + 1, jl + 1, io + 1, jo + 1,
+                            is + 1, mats ? "iw" : "realw");
+              const std::string path = std::string(names[kind]) + tag + sfx + ".vca";
+              std::FILE* f = std::fopen(path.c_str(), "w");
+              if (!f) VFAIL(VCA_ERR_IO, "cannot open " + path + ": " + std::strerror(errno));
+              const int64_t off = idx_nnn(c, il, jl, is, is, io, jo);
+              bool bad = false;
+              for (int q = 0; q < L && !bad; q++) {
+                const double x = mats ? z[2 * q + 1] : z[2 * q];
+                const double* v = y.data() + 2 * ((size_t)q * nel + off);
+                bad = std::fprintf(f, "%24.16E %24.16E %24.16E\n", x, v[1], v[0]) < 0;
+              }
+              if (std::fclose(f) != 0 || bad) VFAIL(VCA_ERR_IO, "write error on " + path);
+            }
+  }
+  return VCA_OK;
+}
+
+// PRINT_SIGMA / PRINT_IMPG / PRINT_IMPG0 at the end of a solve, in the
+// reference's order (VCA_GREENS_FUNCTIONS.f90:37-41)
+static int print_after_solve() {
+  const vca_config& c = g->cfg;
+  if (c.print_sigma) RCHK(print_function(1));
+  if (c.print_impg) RCHK(print_function(0));
+  if (c.print_impg0) RCHK(print_function(2));
+  return VCA_OK;
+}
+
+int vca_gpu_print_impSigma(void) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  return print_function(1);
+}
+int vca_gpu_print_impG(void) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  return print_function(0);
+}
+int vca_gpu_print_impG0(void) {
+  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  return print_function(2);
+}
+
 int vca_gpu_get_sigma_matsubara(double* s_out) { return sigma_grid(true, false, s_out); }
 int vca_gpu_get_sigma_realaxis(double* s_out) { return sigma_grid(false, false, s_out); }
 int vca_gpu_get_g0_matsubara(double* g0_out) { return sigma_grid(true, true, g0_out); }
@@ -2996,7 +3077,8 @@ int vca_gpu_upload_hk(const double* Hk, int64_t Nk) {
 int vca_gpu_solve_resident(const double* Hloc, const double* bath_h, const double* bath_v,
                            double* omega_out) {
   g_err.clear();
-  return solve_resident(Hloc, bath_h, bath_v, omega_out);
+  RCHK(solve_resident(Hloc, bath_h, bath_v, omega_out));
+  return print_after_solve();
 }
 
 int64_t vca_gpu_kernel_launches(void) { return (int64_t)launch_count(); }

@@ -37,6 +37,7 @@ EXPORTS = [
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_timer_start", "vca_gpu_timer_stop",
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
+    "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
 ]
 
 
@@ -123,6 +124,9 @@ def load(path: Optional[str] = None):
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
         "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
+        "vca_gpu_print_impSigma": (ctypes.c_int, []),
+        "vca_gpu_print_impG": (ctypes.c_int, []),
+        "vca_gpu_print_impG0": (ctypes.c_int, []),
         "vca_gpu_save_gfprime": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, i32, i32]),
         "vca_gpu_read_gfprime": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, i32, i32]),
         "vca_gfm_write": (ctypes.c_int, [ctypes.c_char_p, i32, i64, ctypes.POINTER(i32), ctypes.POINTER(i32),
@@ -438,18 +442,35 @@ class VcaSolver:
         return hv
 
     def save_gfprime(self, file: str = "gfprime", used: bool = False, use_formatted: bool = False,
-                     suffix: str = ""):
+                     suffix: Optional[str] = None):
         """save_gfprime (VCA_AUX_FUNX.f90:601-645): the pole tables of the
         last solve (or of the last read_gfprime) to file//suffix//".restart"
-        (".used" when used)."""
-        check(self.L.vca_gpu_save_gfprime(file.encode(), suffix.encode(), int(used), int(use_formatted)))
-        return gfprime_path(file, used, suffix)
+        (".used" when used); suffix None = the config's file_suffix."""
+        sfx = None if suffix is None else suffix.encode()
+        check(self.L.vca_gpu_save_gfprime(file.encode(), sfx, int(used), int(use_formatted)))
+        return gfprime_path(file, used, self._suffix(suffix))
 
     def read_gfprime(self, file: str = "gfprime", used: bool = False, use_formatted: bool = False,
-                     suffix: str = ""):
+                     suffix: Optional[str] = None):
         """read_gfprime (VCA_AUX_FUNX.f90:651-697): the tables replace the
         solve's for gf_cluster and gf_channel until the next solve."""
-        check(self.L.vca_gpu_read_gfprime(file.encode(), suffix.encode(), int(used), int(use_formatted)))
+        sfx = None if suffix is None else suffix.encode()
+        check(self.L.vca_gpu_read_gfprime(file.encode(), sfx, int(used), int(use_formatted)))
+
+    def _suffix(self, suffix: Optional[str]) -> str:
+        return self.cfg.file_suffix.decode() if suffix is None else suffix
+
+    def print_impSigma(self):
+        """vca_print_impSigma (VCA_IO.f90:112-136): splot files of Sigma."""
+        check(self.L.vca_gpu_print_impSigma())
+
+    def print_impG(self):
+        """vca_print_impG (VCA_IO.f90:143-170): splot files of G'."""
+        check(self.L.vca_gpu_print_impG())
+
+    def print_impG0(self):
+        """vca_print_impG0 (VCA_IO.f90:176-205): splot files of G0."""
+        check(self.L.vca_gpu_print_impG0())
 
     def close(self):
         self.L.vca_gpu_finalize()
@@ -459,6 +480,20 @@ class VcaSolver:
 def gfprime_path(file: str = "gfprime", used: bool = False, suffix: str = "") -> str:
     """file//file_suffix//(".used" | ".restart") (VCA_AUX_FUNX.f90:615-617)."""
     return file + suffix + (".used" if used else ".restart")
+
+
+def splot_name(name: str, ilat: int, jlat: int, iorb: int, jorb: int, ispin: int, matsubara: bool,
+               suffix: str = "") -> str:
+    """File of one element written by vca_print_impSigma / _impG / _impG0
+    (VCA_IO.f90:125-128): name in impSigma, impG, impG0; indices 1-based."""
+    return (f"{name}_Isite{ilat:04d}_Jsite{jlat:04d}_l{iorb}{jorb}_s{ispin}_"
+            f"{'iw' if matsubara else 'realw'}{suffix}.vca")
+
+
+def read_splot(path: str):
+    """x and the complex function of a splot file (columns x, Im, Re)."""
+    a = np.loadtxt(path, ndmin=2)
+    return a[:, 0], a[:, 2] + 1j * a[:, 1]
 
 
 def gfm_elements(cfg: VcaConfig):
