@@ -78,6 +78,8 @@ def lib():
             "orc_custom_observable": (D, [P, dp, I]),
             "orc_sum_observable_kmesh": (D, [P, D, D, dp, I, I]),
             "orc_set_threads": (I, [I]),
+            "orc_lowest_pairs": (I, [P, I, I, dp, dp]),
+            "orc_neigen": (I, [P, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -347,6 +349,22 @@ class Oracle:
                 break
             out.append((isec.value, e.value))
             k += 1
+        return out
+
+    def lowest_pairs(self, isector: int, k: int):
+        """The k lowest eigenpairs of a sector on the LANC_METHOD="arpack"
+        path (dense below LANC_DIM_THRESHOLD): energies ascending and the
+        vectors as columns."""
+        D = self.dim(isector)
+        e = np.zeros(max(k, 1))
+        v = np.zeros((max(k, 1), D), dtype=np.complex128)
+        n = self.L.orc_lowest_pairs(self.h, isector, k, _dp(e), _dp(v))
+        return e[:n], v[:n].T.copy()
+
+    def neigen(self) -> np.ndarray:
+        """neigen_sector of every sector (LANC_METHOD="arpack")."""
+        out = np.zeros(self.Nsectors, dtype=np.int32)
+        self.L.orc_neigen(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
         return out
 
     def solve(self):

@@ -72,6 +72,10 @@ struct Oracle {
   // 434,448); it carries over to the next solve
   bool finiteT = false;
   int nstates_total = 1;
+  // LANC_METHOD="arpack": eigenpairs asked per sector, min(dim,
+  // LANC_NSTATES_SECTOR) at setup (VCA_SETUP.f90:312-314), adapted by every
+  // finite-T diagonalisation (VCA_DIAG.f90:411-437) and carried over
+  std::vector<int> neigen;
   // results
   std::vector<double> sector_e;
   std::vector<State> states;
@@ -815,10 +819,237 @@ void diagonalize_finite_t(Oracle& o, const std::vector<int>* mask) {
   o.zeta = zeta;
 }
 
+// ---------------------------------------------------------------------------
+// LANC_METHOD="arpack", the reference default: Neigen = min(dim,
+// neigen_sector(isector)) eigenpairs per sector (VCA_DIAG.f90:98-102) from
+// SciFortran sp_eigh (ARPACK, tol = LANC_TOLERANCE), dense eigh when
+// Neigen == dim or dim <= LANC_DIM_THRESHOLD (:109-111, :191-207).
+// ---------------------------------------------------------------------------
+// The k lowest eigenpairs of a sector, ascending.  Above the threshold:
+// Lanczos with full reorthogonalisation (classical Gram-Schmidt, twice) from
+// the deterministic start vector, extended until the k lowest Ritz pairs of
+// the tridiagonal have |b_{m+1} z_{m,j}| <= LANC_TOLERANCE * max(1,
+// |theta_j|), the Krylov space is exhausted or LANC_NITER steps are done.
+// One start vector reaches one vector of each eigenspace, so a degenerate
+// level inside a sector is found once on this path (fewer than k pairs may
+// come back); ARPACK finds further copies only through the rounding of its
+// restarts, which is not restated.  The dense path returns whole multiplets.
+int lowest_pairs(const Oracle& o, int isector, int k, std::vector<double>& e, std::vector<std::vector<cd>>& vecs) {
+  const vca_config& c = o.cfg;
+  SectorH s = build_sector_h(o, isector);
+  const int64_t D = s.dim;
+  e.clear();
+  vecs.clear();
+  k = (int)std::min<int64_t>(k, D);
+  if (k <= 0) return 0;
+  const bool lanc_solve = k != D && D > std::max(c.lanc_dim_threshold, 1);
+  if (!lanc_solve) {
+    std::vector<cd> H = dense_h(s), Z;
+    std::vector<double> w;
+    jacobi_eigh((int)D, H, w, Z);
+    for (int j = 0; j < k; j++) {
+      e.push_back(w[j]);
+      vecs.emplace_back(Z.begin() + (size_t)j * D, Z.begin() + (size_t)(j + 1) * D);
+    }
+    if (D == 1) vecs[0][0] = 1.0;
+    return k;
+  }
+  const int mmax = (int)std::min<int64_t>(D, std::max(c.lanc_niter, 2 * k));
+  std::vector<std::vector<cd>> V;
+  std::vector<double> a, b(1, 0.0);  // b[j] couples basis vectors j-1 and j
+  std::vector<cd> v(D), w(D);
+  for (int64_t i = 0; i < D; i++) v[i] = start_value(c.start_seed, isector, i);
+  {
+    const double n0 = vnorm(v);
+    for (auto& x : v) x /= n0;
+  }
+  std::vector<double> theta, Zt;
+  int m = 0;
+  auto ritz = [&]() {
+    theta = a;
+    std::vector<double> ee(m, 0.0), z0;
+    for (int q = 1; q < m; q++) ee[q] = b[q];
+    tql2(m, theta, ee, z0, &Zt);
+  };
+  for (int j = 0; j < mmax; j++) {
+    V.push_back(v);
+    hxv(s, v.data(), w.data());
+    if (j > 0)
+      for (int64_t i = 0; i < D; i++) w[i] -= b[j] * V[j - 1][i];
+    const double aj = vdot(v, w).real();
+    for (int64_t i = 0; i < D; i++) w[i] -= aj * v[i];
+    for (int pass = 0; pass < 2; pass++)
+      for (int q = 0; q <= j; q++) {
+        const cd cq = vdot(V[q], w);
+        for (int64_t i = 0; i < D; i++) w[i] -= cq * V[q][i];
+      }
+    const double bj1 = vnorm(w);
+    a.push_back(aj);
+    b.push_back(bj1);
+    m = j + 1;
+    const bool exhausted = bj1 <= c.gs_beta_tol * std::max(1.0, std::fabs(aj));
+    if (exhausted || m == mmax) break;
+    if (m >= k && m % 5 == 0) {
+      ritz();
+      bool conv = true;
+      for (int q = 0; q < k && conv; q++)
+        conv = std::fabs(bj1 * Zt[(m - 1) + (size_t)q * m]) <= c.lanc_tolerance * std::max(1.0, std::fabs(theta[q]));
+      if (conv) break;
+    }
+    for (int64_t i = 0; i < D; i++) v[i] = w[i] / bj1;
+  }
+  ritz();
+  const int nk = std::min(k, m);
+  for (int q = 0; q < nk; q++) {
+    std::vector<cd> x(D, 0.0);
+    for (int i = 0; i < m; i++) {
+      const double zi = Zt[i + (size_t)q * m];
+      for (int64_t r = 0; r < D; r++) x[r] += zi * V[i][r];
+    }
+    const double nx = vnorm(x);
+    for (auto& y : x) y /= nx;
+    e.push_back(theta[q]);
+    vecs.push_back(std::move(x));
+  }
+  return nk;
+}
+
+// T=0, LANC_METHOD="arpack": every sector's Neigen eigenvalues in ascending
+// order through the ground-state bookkeeping of VCA_DIAG.f90:224-236.
+void diagonalize_arpack_t0(Oracle& o, const std::vector<int>* mask) {
+  const double thr = o.cfg.gs_threshold;
+  double oldzero = 1000.0;
+  for (int isector = 1; isector <= o.Nsectors; isector++) {
+    if (mask && !(*mask)[isector - 1]) continue;
+    std::vector<double> e;
+    std::vector<std::vector<cd>> vecs;
+    lowest_pairs(o, isector, o.neigen[isector - 1], e, vecs);
+    if (!e.empty()) o.sector_e[isector - 1] = e[0];
+    for (size_t i = 0; i < e.size(); i++) {
+      const double en = e[i];
+      if (en < oldzero - 10.0 * thr) {
+        oldzero = en;
+        o.states.clear();
+        o.states.push_back({en, isector, std::move(vecs[i])});
+      } else if (std::fabs(en - oldzero) <= thr) {
+        oldzero = std::min(oldzero, en);
+        auto it = o.states.begin();
+        while (it != o.states.end() && !(en <= it->e)) ++it;
+        o.states.insert(it, State{en, isector, std::move(vecs[i])});
+      }
+    }
+  }
+  o.egs = INFINITY;
+  for (auto& st : o.states) o.egs = std::min(o.egs, st.e);
+  o.zeta = (double)o.states.size();  // VCA_DIAG.f90:363
+}
+
+// Finite T, LANC_METHOD="arpack": the annealing sweeps of VCA_DIAG.f90:78-256
+// with Neigen = min(dim, neigen_sector) states per sector added to the capped
+// list (es_add_state_c with size, VCA_EIGENSPACE.f90:136-159), then
+// vca_post_diag (:357-451): zeta over the whole list; neigen_sector(i) + 1
+// for sectors in the list, - 1 for the others, at most the sector's count in
+// the list + 1 and at least 1 (:411-437); then the cap grows or the list is
+// trimmed, as with one state per sector.  A sector's eigenpairs do not change
+// between sweeps: they are computed once per sector, again only when a sweep
+// asks for more.
+void diagonalize_arpack_finite_t(Oracle& o, const std::vector<int>* mask) {
+  const vca_config& c = o.cfg;
+  const double beta = c.beta, cutoff = c.cutoff;
+  std::vector<int> scan;
+  for (int isector = 1; isector <= o.Nsectors; isector++)
+    if (!mask || (*mask)[isector - 1]) scan.push_back(isector);
+  std::vector<std::vector<double>> E(o.Nsectors);
+  std::vector<std::vector<std::vector<cd>>> X(o.Nsectors);
+  std::vector<int> have(o.Nsectors, -1);  // eigenpairs asked of the sector so far
+  auto ensure = [&](const std::vector<int>& secs) {
+    std::vector<int> todo;
+    for (int isector : secs)
+      if (have[isector - 1] < o.neigen[isector - 1]) todo.push_back(isector);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t q = 0; q < (int64_t)todo.size(); q++) {
+      const int isector = todo[q];
+      lowest_pairs(o, isector, o.neigen[isector - 1], E[isector - 1], X[isector - 1]);
+      have[isector - 1] = o.neigen[isector - 1];
+    }
+  };
+  struct Entry {
+    int sector, idx;
+  };
+  std::vector<Entry> list;
+  auto en = [&](const Entry& x) { return E[x.sector - 1][x.idx]; };
+  double emin = DBL_MAX, emax = -DBL_MAX;
+  auto insert = [&](Entry x) {  // es_insert_state_c (:167-216): before the first c%e >= e
+    const double ev = en(x);
+    size_t pos = 0;
+    while (pos < list.size() && !(ev <= en(list[pos]))) pos++;
+    list.insert(list.begin() + pos, x);
+    if (ev > emax) emax = ev;
+    if (ev < emin) emin = ev;
+  };
+  auto pop = [&]() {  // es_pop_state without n (:230-312): the last entry
+    list.pop_back();
+    if (!list.empty()) {
+      emax = en(list.back());
+      emin = en(list.front());
+    }
+  };
+  bool converged = false;
+  int iter = 0;
+  double zeta = 0.0;
+  while (!converged && iter < c.lanc_niter_spectrum) {
+    iter++;
+    ensure(scan);
+    list.clear();
+    emin = DBL_MAX;
+    emax = -DBL_MAX;
+    for (int isector : scan) {
+      const int ne = std::min(o.neigen[isector - 1], (int)E[isector - 1].size());
+      for (int i = 0; i < ne; i++) {
+        const Entry x{isector, i};
+        if ((int)list.size() < o.nstates_total) insert(x);
+        else if (en(x) < en(list.back())) { pop(); insert(x); }
+      }
+    }
+    converged = std::exp(-beta * (emax - emin)) < cutoff;  // VCA_DIAG.f90:251-256
+    zeta = 0.0;
+    for (const Entry& x : list) zeta += std::exp(-beta * (en(x) - emin));
+    std::vector<int> count(o.Nsectors, 0);
+    for (const Entry& x : list) count[x.sector - 1]++;
+    for (int i = 0; i < o.Nsectors; i++) {
+      int& ne = o.neigen[i];
+      ne += count[i] > 0 ? 1 : -1;
+      if (ne > count[i]) ne = count[i] + 1;
+      if (ne <= 0) ne = 1;
+    }
+    if (std::exp(-beta * (emax - emin)) > cutoff) {
+      o.nstates_total += c.lanc_nstates_step;
+    } else {
+      double Ei = en(list.back());
+      while (std::exp(-beta * (Ei - emin)) <= cutoff) {
+        pop();
+        Ei = en(list.back());
+      }
+      o.nstates_total = std::max((int)list.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
+    }
+  }
+  for (int isector : scan)
+    if (!E[isector - 1].empty()) o.sector_e[isector - 1] = E[isector - 1][0];
+  o.states.clear();
+  for (const Entry& x : list) o.states.push_back({en(x), x.sector, X[x.sector - 1][x.idx]});
+  o.egs = emin;
+  o.zeta = zeta;
+}
+
 void diagonalize(Oracle& o, const std::vector<int>* mask) {
   const vca_config& c = o.cfg;
   o.sector_e.assign(o.Nsectors, INFINITY);
   o.states.clear();
+  if (c.lanc_method != VCA_LANC_LANCZOS) {  // "arpack", the reference default
+    if (o.finiteT) diagonalize_arpack_finite_t(o, mask);
+    else diagonalize_arpack_t0(o, mask);
+    return;
+  }
   if (o.finiteT) {
     diagonalize_finite_t(o, mask);
     return;
@@ -1516,6 +1747,14 @@ void* orc_create(const vca_config* cfg, const double* Hloc, const double* Hk, in
   o->nstates_total = c.lanc_nstates_total;
   if (o->finiteT && o->nstates_total % 2 != 0) o->nstates_total++;  // :172-175
   o->Nlso = c.Nlat * c.Nspin * c.Norb;
+  int nsec = c.lanc_nstates_sector;
+  if (o->finiteT && nsec % 2 != 0) nsec++;  // VCA_SETUP.f90:166-170
+  o->neigen.resize(o->Nsectors);
+  for (int isector = 1; isector <= o->Nsectors; isector++) {
+    const int Nsp = o->Ns;
+    const int64_t dim = binomial(Nsp, get_nup(isector, Nsp)) * binomial(Nsp, get_ndw(isector, Nsp));
+    o->neigen[isector - 1] = (int)std::min<int64_t>(dim, std::max(nsec, 1));
+  }
   const size_t nel = (size_t)c.Nlat * c.Nlat * c.Nspin * c.Nspin * c.Norb * c.Norb;
   copy_c(Hloc, nel, o->Hloc);
   o->Nk = Nk;
@@ -1763,6 +2002,29 @@ double orc_solve(void* h, double* egs_out, double* omega_int_out) {
   if (egs_out) *egs_out = o->egs;
   if (omega_int_out) *omega_int_out = o->omega_int;
   return o->sft;
+}
+// the k lowest eigenpairs of a sector in the arpack path (ascending);
+// vecs_out holds k vectors of the sector's dimension (complex, interleaved)
+int orc_lowest_pairs(void* h, int isector, int k, double* e_out, double* vecs_out) {
+  Oracle* o = (Oracle*)h;
+  std::vector<double> e;
+  std::vector<std::vector<cd>> v;
+  const int n = lowest_pairs(*o, isector, k, e, v);
+  for (int j = 0; j < n; j++) {
+    e_out[j] = e[j];
+    if (vecs_out)
+      for (size_t i = 0; i < v[j].size(); i++) {
+        vecs_out[2 * (j * v[j].size() + i)] = v[j][i].real();
+        vecs_out[2 * (j * v[j].size() + i) + 1] = v[j][i].imag();
+      }
+  }
+  return n;
+}
+// neigen_sector of every sector (1-based order)
+int orc_neigen(void* h, int* out) {
+  Oracle* o = (Oracle*)h;
+  for (int i = 0; i < o->Nsectors; i++) out[i] = o->neigen[i];
+  return o->Nsectors;
 }
 int orc_set_threads(int n) {
 #ifdef _OPENMP
