@@ -290,6 +290,24 @@ int vca_gfm_write(const char* path, int32_t formatted, int64_t nelem, const int3
 int vca_gfm_read(const char* path, int32_t formatted, int64_t nelem, int64_t* sizes, int32_t* nstates,
                  int32_t* nchan, int32_t* nexc, double* poles, double* weights);
 
+/*
+ * The state-list logic the solve runs on the host, without a context or a
+ * GPU.  E holds every sector's lowest energy (Nsectors entries, 1-based
+ * sector order), as the batched ground-state search returns them.
+ * T=0 (VCA_DIAG.f90:224-236): the kept states, each inserted before the
+ * first entry with e <= its energy (es_insert_state_c, VCA_EIGENSPACE.f90:
+ * 167-216); *n = their number, sectors/energies the first cap of them.
+ * Finite T with one state per sector (VCA_DIAG.f90:78-256, vca_post_diag
+ * :357-451): the annealed list from LANC_NSTATES_TOTAL = nstates_total, zeta
+ * (before the trim), E_min and the adjusted LANC_NSTATES_TOTAL; cfg gives
+ * BETA, CUTOFF, LANC_NSTATES_STEP and LANC_NITER_SPECTRUM.
+ */
+int vca_state_list_t0(const double* E, int32_t nsectors, double gs_threshold, int32_t* sectors, double* energies,
+                      int32_t cap, int32_t* n);
+int vca_state_list_finite_t(const double* E, int32_t nsectors, const vca_config* cfg, int32_t nstates_total,
+                            int32_t* sectors, int32_t cap, int32_t* n, double* zeta, double* emin,
+                            int32_t* nstates_total_out);
+
 /* Omega integrand f(w) = (1/Lk) sum_k ln|det(1+(Delta+Hloc-Hk)G'(iw))|
  * (VCA_OMEGA.f90:37-75) at nw real frequencies, from the last solve. */
 int vca_gpu_sum_kmesh(const double* w, int64_t nw, double* f_out);

@@ -80,6 +80,8 @@ def lib():
             "orc_set_threads": (I, [I]),
             "orc_lowest_pairs": (I, [P, I, I, dp, dp]),
             "orc_neigen": (I, [P, ip]),
+            "orc_state_list_t0": (I, [dp, I, D, ip, dp, I]),
+            "orc_state_list_finite_t": (I, [dp, I, ctypes.POINTER(VcaConfig), I, ip, I, dp, dp, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -372,6 +374,28 @@ class Oracle:
         oi = ctypes.c_double()
         sft = self.L.orc_solve(self.h, ctypes.byref(egs), ctypes.byref(oi))
         return sft, egs.value, oi.value
+
+
+def state_list_t0(E, gs_threshold: float):
+    """[(sector, energy)] the T=0 bookkeeping keeps for sector energies E."""
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    sec = np.zeros(len(E), dtype=np.int32)
+    en = np.zeros(len(E))
+    n = lib().orc_state_list_t0(_dp(E), len(E), gs_threshold, sec.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                _dp(en), len(E))
+    return list(zip(sec[:n].tolist(), en[:n].tolist()))
+
+
+def state_list_finite_t(E, cfg: VcaConfig, nstates_total: int):
+    """(sectors, zeta, emin, adjusted nstates_total) of the annealing sweeps."""
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    sec = np.zeros(max(len(E), 1), dtype=np.int32)
+    z, lo = ctypes.c_double(), ctypes.c_double()
+    nt = ctypes.c_int()
+    n = lib().orc_state_list_finite_t(_dp(E), len(E), ctypes.byref(cfg), nstates_total,
+                                      sec.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(sec),
+                                      ctypes.byref(z), ctypes.byref(lo), ctypes.byref(nt))
+    return sec[:n].tolist(), z.value, lo.value, nt.value
 
 
 def start_value(seed: int, isector: int, i: int) -> float:

@@ -748,16 +748,87 @@ double lowest_pair(const Oracle& o, int isector, std::vector<cd>& vec) {
   return e;
 }
 
+// The annealing sweeps on given sector energies (one state per sector):
+// E[isector-1] for the sectors in scan (sector order).  Each sweep empties
+// the list (es_free_espace, VCA_EIGENSPACE.f90:107-125), re-adds every
+// sector under the cap LANC_NSTATES_TOTAL (es_add_state_c with size,
+// :136-159), tests exp(-beta(emax-emin)) < cutoff (VCA_DIAG.f90:251-256),
+// then vca_post_diag (:357-363, :438-470): zeta over the whole list, and
+// either the cap grows by LANC_NSTATES_STEP or the states beyond the
+// cut-off are popped and the cap reset.
+void replay_finite_t(const std::vector<double>& E, const std::vector<int>& scan, const vca_config& c,
+                     int& nstates_total, std::vector<int>& list, double& zeta, double& emin) {
+  const double beta = c.beta, cutoff = c.cutoff;
+  list.clear();
+  double lo = DBL_MAX, hi = -DBL_MAX;
+  auto En = [&](size_t i) { return E[list[i] - 1]; };
+  auto insert = [&](int isector) {  // es_insert_state_c (:167-216): before the first c%e >= e
+    const double e = E[isector - 1];
+    size_t pos = 0;
+    while (pos < list.size() && !(e <= En(pos))) pos++;
+    list.insert(list.begin() + pos, isector);
+    if (e > hi) hi = e;
+    if (e < lo) lo = e;
+  };
+  auto pop = [&]() {  // es_pop_state without n (:230-312): the last entry
+    list.pop_back();
+    if (!list.empty()) { hi = En(list.size() - 1); lo = En(0); }
+  };
+  bool converged = false;
+  int iter = 0;
+  zeta = 0.0;
+  while (!converged && iter < c.lanc_niter_spectrum) {
+    iter++;
+    list.clear();
+    lo = DBL_MAX;
+    hi = -DBL_MAX;
+    for (int isector : scan) {
+      if ((int)list.size() < nstates_total) insert(isector);
+      else if (E[isector - 1] < En(list.size() - 1)) { pop(); insert(isector); }
+    }
+    converged = std::exp(-beta * (hi - lo)) < cutoff;
+    zeta = 0.0;
+    for (size_t i = 0; i < list.size(); i++) zeta += std::exp(-beta * (En(i) - lo));
+    if (std::exp(-beta * (hi - lo)) > cutoff) {
+      nstates_total += c.lanc_nstates_step;
+    } else {
+      double Ei = En(list.size() - 1);
+      while (std::exp(-beta * (Ei - lo)) <= cutoff) {
+        pop();
+        Ei = En(list.size() - 1);
+      }
+      nstates_total = std::max((int)list.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
+    }
+  }
+  emin = lo;
+}
+
+// T=0 bookkeeping on given sector energies (VCA_DIAG.f90:224-236): a new
+// lowest energy below oldzero - 10*gs_threshold empties the list, one within
+// gs_threshold of oldzero joins it (inserted before the first entry >= it).
+void replay_t0(const std::vector<double>& E, double thr, std::vector<std::pair<int, double>>& list) {
+  double oldzero = 1000.0;
+  list.clear();
+  for (int isector = 1; isector <= (int)E.size(); isector++) {
+    const double e = E[isector - 1];
+    if (e < oldzero - 10.0 * thr) {
+      oldzero = e;
+      list.assign(1, {isector, e});
+    } else if (std::fabs(e - oldzero) <= thr) {
+      oldzero = std::min(oldzero, e);
+      auto it = list.begin();
+      while (it != list.end() && !(e <= it->second)) ++it;
+      list.insert(it, {isector, e});
+    }
+  }
+}
+
 // Finite T (VCA_DIAG.f90:78-256 and vca_post_diag :357-363,:395-451) with
-// one state per sector: the annealing sweeps re-add every sector's lowest
-// state to a list capped at LANC_NSTATES_TOTAL (es_add_state_c with size,
-// VCA_EIGENSPACE.f90:136-159), test exp(-beta(emax-emin)) < cutoff, then
-// vca_post_diag computes zeta over the whole list, and either grows the cap
-// or trims the states beyond the cut-off and resets the cap.  Every sweep
-// finds the same eigenpairs, so they are computed once.
+// one state per sector: every sector's lowest eigenpair, then the annealing
+// sweeps of replay_finite_t on their energies.  Every sweep finds the same
+// eigenpairs, so they are computed once.
 void diagonalize_finite_t(Oracle& o, const std::vector<int>* mask) {
   const vca_config& c = o.cfg;
-  const double beta = c.beta, cutoff = c.cutoff;
   std::vector<State> all(o.Nsectors);
   std::vector<int> scan;
   for (int isector = 1; isector <= o.Nsectors; isector++)
@@ -770,49 +841,11 @@ void diagonalize_finite_t(Oracle& o, const std::vector<int>* mask) {
     st.e = lowest_pair(o, isector, st.vec);
   }
   for (int isector : scan) o.sector_e[isector - 1] = all[isector - 1].e;
-  // the list holds sector numbers in list order
+  std::vector<double> E(o.Nsectors, INFINITY);
+  for (int isector : scan) E[isector - 1] = all[isector - 1].e;
   std::vector<int> list;
-  double emin = DBL_MAX, emax = -DBL_MAX;
-  auto E = [&](size_t i) { return all[list[i] - 1].e; };
-  auto insert = [&](int isector) {  // es_insert_state_c (:167-216): before the first c%e >= e
-    const double e = all[isector - 1].e;
-    size_t pos = 0;
-    while (pos < list.size() && !(e <= E(pos))) pos++;
-    list.insert(list.begin() + pos, isector);
-    if (e > emax) emax = e;
-    if (e < emin) emin = e;
-  };
-  auto pop = [&]() {  // es_pop_state without n (:230-312): the last entry
-    list.pop_back();
-    if (!list.empty()) { emax = E(list.size() - 1); emin = E(0); }
-  };
-  bool converged = false;
-  int iter = 0;
-  double zeta = 0.0;
-  while (!converged && iter < c.lanc_niter_spectrum) {
-    iter++;
-    list.clear();  // es_free_espace (:107-125)
-    emin = DBL_MAX;
-    emax = -DBL_MAX;
-    for (int isector : scan) {
-      if ((int)list.size() < o.nstates_total) insert(isector);
-      else if (all[isector - 1].e < E(list.size() - 1)) { pop(); insert(isector); }
-    }
-    converged = std::exp(-beta * (emax - emin)) < cutoff;  // VCA_DIAG.f90:251-256
-    // vca_post_diag
-    zeta = 0.0;
-    for (size_t i = 0; i < list.size(); i++) zeta += std::exp(-beta * (E(i) - emin));
-    if (std::exp(-beta * (emax - emin)) > cutoff) {
-      o.nstates_total += c.lanc_nstates_step;
-    } else {
-      double Ei = E(list.size() - 1);
-      while (std::exp(-beta * (Ei - emin)) <= cutoff) {
-        pop();
-        Ei = E(list.size() - 1);
-      }
-      o.nstates_total = std::max((int)list.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
-    }
-  }
+  double zeta = 0.0, emin = 0.0;
+  replay_finite_t(E, scan, c, o.nstates_total, list, zeta, emin);
   o.states.clear();
   for (int isector : list) o.states.push_back(all[isector - 1]);
   o.egs = emin;
@@ -2019,6 +2052,29 @@ int orc_lowest_pairs(void* h, int isector, int k, double* e_out, double* vecs_ou
       }
   }
   return n;
+}
+// the state-list replays on given sector energies (1-based sector order)
+int orc_state_list_t0(const double* E, int nsec, double thr, int* sectors, double* energies, int cap) {
+  std::vector<std::pair<int, double>> list;
+  replay_t0(std::vector<double>(E, E + nsec), thr, list);
+  for (int i = 0; i < (int)list.size() && i < cap; i++) {
+    sectors[i] = list[i].first;
+    energies[i] = list[i].second;
+  }
+  return (int)list.size();
+}
+int orc_state_list_finite_t(const double* E, int nsec, const vca_config* cfg, int nstates_total, int* sectors,
+                            int cap, double* zeta, double* emin, int* nstates_total_out) {
+  std::vector<int> scan(nsec), list;
+  for (int i = 0; i < nsec; i++) scan[i] = i + 1;
+  int nt = nstates_total;
+  double z = 0.0, lo = 0.0;
+  replay_finite_t(std::vector<double>(E, E + nsec), scan, *cfg, nt, list, z, lo);
+  for (int i = 0; i < (int)list.size() && i < cap; i++) sectors[i] = list[i];
+  *zeta = z;
+  *emin = lo;
+  *nstates_total_out = nt;
+  return (int)list.size();
 }
 // neigen_sector of every sector (1-based order)
 int orc_neigen(void* h, int* out) {

@@ -1042,21 +1042,28 @@ int batched_sector_energies_f64(std::vector<double>& energy) {
 // the entries past the cut-off and resets the cap to max(size,step)+step.
 // Every sweep finds the same sector energies, so one pass computes them and
 // the host replays the sweeps; eigenvectors are computed for the states left.
-int diagonalize_finite_t() {
-  const vca_config& c = g->cfg;
-  std::vector<double> E(g->Nsectors, INFINITY);
-  RCHK(g->fx ? batched_sector_energies(E) : batched_sector_energies_f64(E));
-  g->sector_e = E;
-  struct Entry {
-    double e;
-    int sector;
-  };
-  std::vector<Entry> lst;
+// The finite-T state list from every sector's lowest energy E[isector-1]
+// (one state per sector): the annealing sweeps of VCA_DIAG.f90:78-256 replayed
+// on the host -- each sweep rebuilds the list capped at LANC_NSTATES_TOTAL
+// (es_add_state_c with size, VCA_EIGENSPACE.f90:136-159; insertion before the
+// first entry with e <= its energy, es_insert_state_c :167-216; the last entry
+// popped, es_pop_state :230-312), tests exp(-beta(emax-emin)) < CUTOFF, then
+// vca_post_diag (:357-451) sums zeta over the whole list and either grows the
+// cap by LANC_NSTATES_STEP or trims the states beyond the cut-off and resets
+// the cap to max(size, step) + step.  Every sweep finds the same energies, so
+// the search runs once.  Host only.
+struct ListEntry {
+  double e;
+  int sector;
+};
+void replay_finite_t(const std::vector<double>& E, const vca_config& c, int& nstates_total,
+                     std::vector<ListEntry>& lst, double& zeta, double& emin) {
+  const int nsec = (int)E.size();
   double lo = DBL_MAX, hi = -DBL_MAX;
   auto put = [&](int isector) {
     const double e = E[isector - 1];
-    auto at = std::find_if(lst.begin(), lst.end(), [&](const Entry& x) { return e <= x.e; });
-    lst.insert(at, Entry{e, isector});
+    auto at = std::find_if(lst.begin(), lst.end(), [&](const ListEntry& x) { return e <= x.e; });
+    lst.insert(at, ListEntry{e, isector});
     if (e > hi) hi = e;
     if (e < lo) lo = e;
   };
@@ -1065,28 +1072,60 @@ int diagonalize_finite_t() {
     if (!lst.empty()) { hi = lst.back().e; lo = lst.front().e; }
   };
   const double beta = c.beta;
-  double zeta = 0.0;
+  zeta = 0.0;
+  lst.clear();
   bool done = false;
   for (int sweep = 0; !done && sweep < c.lanc_niter_spectrum; sweep++) {
     lst.clear();
     lo = DBL_MAX;
     hi = -DBL_MAX;
-    for (int isector = 1; isector <= g->Nsectors; isector++) {
-      if ((int)lst.size() < g->nstates_total) put(isector);
+    for (int isector = 1; isector <= nsec; isector++) {
+      if ((int)lst.size() < nstates_total) put(isector);
       else if (E[isector - 1] < lst.back().e) { drop(); put(isector); }
     }
     const double spread = std::exp(-beta * (hi - lo));
     done = spread < c.cutoff;
     zeta = 0.0;
-    for (const Entry& x : lst) zeta += std::exp(-beta * (x.e - lo));
+    for (const ListEntry& x : lst) zeta += std::exp(-beta * (x.e - lo));
     if (spread > c.cutoff) {
-      g->nstates_total += c.lanc_nstates_step;
+      nstates_total += c.lanc_nstates_step;
     } else {
       while (std::exp(-beta * (lst.back().e - lo)) <= c.cutoff) drop();
-      g->nstates_total = std::max((int)lst.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
+      nstates_total = std::max((int)lst.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
     }
   }
-  for (const Entry& x : lst) {
+  emin = lo;
+}
+
+// The T=0 list from every sector's lowest energy: VCA_DIAG.f90:224-236 in
+// sector order (a new lowest energy below oldzero - 10*GS_THRESHOLD empties
+// the list, one within GS_THRESHOLD of oldzero joins it), each state
+// inserted before the first entry with e <= its energy.  Host only.
+void replay_t0(const std::vector<double>& E, double thr, std::vector<ListEntry>& lst) {
+  double oz = 1000.0;
+  lst.clear();
+  for (int isector = 1; isector <= (int)E.size(); isector++) {
+    const double e = E[isector - 1];
+    if (e < oz - 10.0 * thr) {
+      oz = e;
+      lst.assign(1, ListEntry{e, isector});
+    } else if (std::fabs(e - oz) <= thr) {
+      oz = std::min(oz, e);
+      auto at = std::find_if(lst.begin(), lst.end(), [&](const ListEntry& x) { return e <= x.e; });
+      lst.insert(at, ListEntry{e, isector});
+    }
+  }
+}
+
+int diagonalize_finite_t() {
+  const vca_config& c = g->cfg;
+  std::vector<double> E(g->Nsectors, INFINITY);
+  RCHK(g->fx ? batched_sector_energies(E) : batched_sector_energies_f64(E));
+  g->sector_e = E;
+  std::vector<ListEntry> lst;
+  double zeta = 0.0, lo = 0.0;
+  replay_finite_t(E, c, g->nstates_total, lst, zeta, lo);
+  for (const ListEntry& x : lst) {
     double e;
     void* vec = nullptr;
     RCHK(g->fx ? sector_gs_fx(x.sector, &e, &vec, g->states) : sector_gs(x.sector, &e, &vec, g->states));
@@ -1113,15 +1152,10 @@ int diagonalize() {
   std::vector<char> keep_sec(g->Nsectors + 1, 1);
   {
     RCHK(g->fx ? batched_sector_energies(eb) : batched_sector_energies_f64(eb));
-    double oz = 1000.0;
-    std::vector<int> lst;
-    for (int isector = 1; isector <= g->Nsectors; isector++) {  // replay VCA_DIAG.f90:224-236
-      const double e = eb[isector - 1];
-      if (e < oz - 10.0 * thr) { oz = e; lst.assign(1, isector); }
-      else if (std::fabs(e - oz) <= thr) { oz = std::min(oz, e); lst.push_back(isector); }
-    }
+    std::vector<ListEntry> lst;
+    replay_t0(eb, thr, lst);
     std::fill(keep_sec.begin(), keep_sec.end(), 0);
-    for (int q : lst) keep_sec[q] = 1;
+    for (const ListEntry& q : lst) keep_sec[q.sector] = 1;
   }
   for (int isector = 1; isector <= g->Nsectors; isector++) {
     double e;
@@ -2557,6 +2591,37 @@ int vca_gpu_read_gfprime(const char* file, const char* suffix, int32_t used, int
   g->gfm_chan0 = std::move(c0);
   g->gfm_exc0 = std::move(x0);
   g->gfm_loaded = true;
+  return VCA_OK;
+}
+
+int vca_state_list_t0(const double* E, int32_t nsectors, double gs_threshold, int32_t* sectors, double* energies,
+                      int32_t cap, int32_t* n) {
+  if (!E || nsectors < 0 || !n || cap < 0 || (cap > 0 && !sectors)) VFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<ListEntry> lst;
+  replay_t0(std::vector<double>(E, E + nsectors), gs_threshold, lst);
+  *n = (int32_t)lst.size();
+  for (int i = 0; i < (int)lst.size() && i < cap; i++) {
+    sectors[i] = lst[i].sector;
+    if (energies) energies[i] = lst[i].e;
+  }
+  return VCA_OK;
+}
+
+int vca_state_list_finite_t(const double* E, int32_t nsectors, const vca_config* cfg, int32_t nstates_total,
+                            int32_t* sectors, int32_t cap, int32_t* n, double* zeta, double* emin,
+                            int32_t* nstates_total_out) {
+  if (!E || nsectors < 0 || !cfg || !n || cap < 0 || (cap > 0 && !sectors)) VFAIL(VCA_ERR_ARG, "bad arguments");
+  if (!(cfg->cutoff > 0.0 && cfg->cutoff < 1.0) || !(cfg->beta > 0.0) || cfg->lanc_niter_spectrum < 1)
+    VFAIL(VCA_ERR_CONFIG, "CUTOFF in (0,1), BETA > 0 and LANC_NITER_SPECTRUM >= 1 are required");
+  std::vector<ListEntry> lst;
+  int nt = nstates_total;
+  double z = 0.0, lo = 0.0;
+  replay_finite_t(std::vector<double>(E, E + nsectors), *cfg, nt, lst, z, lo);
+  *n = (int32_t)lst.size();
+  for (int i = 0; i < (int)lst.size() && i < cap; i++) sectors[i] = lst[i].sector;
+  if (zeta) *zeta = z;
+  if (emin) *emin = lo;
+  if (nstates_total_out) *nstates_total_out = nt;
   return VCA_OK;
 }
 

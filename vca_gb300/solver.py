@@ -38,6 +38,7 @@ EXPORTS = [
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
     "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
+    "vca_state_list_t0", "vca_state_list_finite_t",
 ]
 
 
@@ -124,6 +125,10 @@ def load(path: Optional[str] = None):
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
         "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
+        "vca_state_list_t0": (ctypes.c_int, [dp, i32, ctypes.c_double, ctypes.POINTER(i32), dp, i32,
+                                             ctypes.POINTER(i32)]),
+        "vca_state_list_finite_t": (ctypes.c_int, [dp, i32, cfgp, i32, ctypes.POINTER(i32), i32,
+                                                   ctypes.POINTER(i32), dp, dp, ctypes.POINTER(i32)]),
         "vca_gpu_print_impSigma": (ctypes.c_int, []),
         "vca_gpu_print_impG": (ctypes.c_int, []),
         "vca_gpu_print_impG0": (ctypes.c_int, []),
@@ -474,6 +479,35 @@ class VcaSolver:
 
     def close(self):
         self.L.vca_gpu_finalize()
+
+
+# ---- state-list logic of the solve (host only, no GPU needed) -------------
+def state_list_t0(E, gs_threshold: float):
+    """[(sector, energy)] the T=0 bookkeeping keeps (VCA_DIAG.f90:224-236)
+    for every sector's lowest energy E (1-based sector order)."""
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    cap = max(len(E), 1)
+    sec = np.zeros(cap, dtype=np.int32)
+    en = np.zeros(cap)
+    n = ctypes.c_int32()
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    check(load().vca_state_list_t0(_dp(E), len(E), gs_threshold, sec.ctypes.data_as(i32p), _dp(en), cap,
+                                   ctypes.byref(n)))
+    return list(zip(sec[:n.value].tolist(), en[:n.value].tolist()))
+
+
+def state_list_finite_t(E, cfg: VcaConfig, nstates_total: int):
+    """(sectors in list order, zeta, E_min, adjusted LANC_NSTATES_TOTAL) of
+    the annealing sweeps (VCA_DIAG.f90:78-256, vca_post_diag :357-451)."""
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    cap = max(len(E), 1)
+    sec = np.zeros(cap, dtype=np.int32)
+    n, nt = ctypes.c_int32(), ctypes.c_int32()
+    z, lo = ctypes.c_double(), ctypes.c_double()
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    check(load().vca_state_list_finite_t(_dp(E), len(E), ctypes.byref(cfg), nstates_total, sec.ctypes.data_as(i32p),
+                                         cap, ctypes.byref(n), ctypes.byref(z), ctypes.byref(lo), ctypes.byref(nt)))
+    return sec[:n.value].tolist(), z.value, lo.value, nt.value
 
 
 # ---- GFmatrix restart files (host only, no GPU needed) --------------------
