@@ -304,6 +304,19 @@ int vca_gfm_read(const char* path, int32_t formatted, int64_t nelem, int64_t* si
  */
 int vca_state_list_t0(const double* E, int32_t nsectors, double gs_threshold, int32_t* sectors, double* energies,
                       int32_t cap, int32_t* n);
+/* More host logic of the solve, without a context or a GPU.
+ * vca_pair_kpoints: the k-points the Omega k-sum keeps for Hk (nel complex
+ * entries per k, Nk points): a point and its partner with H_k' = conj(H_k)
+ * (entry-wise to 1e-13 (1 + max|H|)) as one representative of weight 2,
+ * other points with weight 1; representatives ascending.
+ * vca_contour_rule: the nodes and weights on theta in [0, pi] of the fixed
+ * rule that replaces quad(integral_contour, 0, pi) (VCA_OMEGA.f90:172) at
+ * radius R: ngl Gauss-Legendre nodes per panel, panels graded from the angle
+ * of the Fermi pole xmu + i(2n+1)pi/beta nearest the arc. */
+int vca_pair_kpoints(const double* Hk, int64_t Nk, int64_t nel, int64_t* reps, double* weights, int64_t cap,
+                     int64_t* nrep);
+int vca_contour_rule(double R, double beta, double mu, int32_t ngl, double* theta, double* weights, int32_t cap,
+                     int32_t* n);
 int vca_state_list_finite_t(const double* E, int32_t nsectors, const vca_config* cfg, int32_t nstates_total,
                             int32_t* sectors, int32_t cap, int32_t* n, double* zeta, double* emin,
                             int32_t* nstates_total_out);

@@ -7,6 +7,10 @@ Energies are drawn in clusters around a few levels with offsets at and
 around the thresholds (GS_THRESHOLD, 10*GS_THRESHOLD, the CUTOFF spread),
 exact ties included.  The lists (sectors and order), zeta, E_min and the
 adjusted LANC_NSTATES_TOTAL must be identical, bit for bit.
+
+Also host logic of the Omega integral: the k-point pairing of the k-sum
+(vca_pair_kpoints) against a brute-force pairing and known counts, and the
+contour rule's nodes (vca_contour_rule) against the oracle's (1e-15).
 """
 import numpy as np
 import pytest
@@ -69,3 +73,74 @@ def test_replays_are_what_the_oracle_solve_keeps():
     sec, zeta, emin, nt = orc.state_list_finite_t(o.sector_energies(), cfg, 2)
     assert sec == [s for s, _ in o.states()] and nt == o.thermal()["nstates_total"]
     assert zeta == o.thermal()["zeta"] and emin == min(e for _, e in o.states())
+
+
+def _brute_pairs(Hk):
+    """Greedy pairing in k order by direct comparison (the reference sums
+    every k; pairing is this library's, so the check is the property: each
+    weight-2 representative has exactly one partner H_k' = conj(H_k))."""
+    Nk = Hk.shape[-1]
+    H = Hk.reshape(-1, Nk, order="F")
+    tol = 1e-13 * (1.0 + np.abs(np.concatenate([H.real.ravel(), H.imag.ravel()])).max())
+    used = np.zeros(Nk, bool)
+    reps, wts = [], []
+    for k in range(Nk):
+        if used[k]:
+            continue
+        used[k] = True
+        cand = [j for j in range(Nk) if not used[j]
+                and np.all(np.abs(H[:, j].real - H[:, k].real) <= tol)
+                and np.all(np.abs(H[:, j].imag + H[:, k].imag) <= tol)]
+        reps.append(k)
+        wts.append(2.0 if cand else 1.0)
+        if cand:
+            used[cand[0]] = True
+    return np.array(reps), np.array(wts)
+
+
+@pytest.mark.parametrize("make", [
+    lambda: clusters.square(nx=4, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=32, nky=32, ngfiter=20,
+                            omega_nodes=64),
+    lambda: clusters.chain1d(tprime=1.0, nlat=4, U=4.0, xmu=2.0, nk=64, ngfiter=20, omega_nodes=64),
+    lambda: clusters.bhz(mass=2.2, delta=0.1, nk1=12, ngfiter=20, omega_nodes=64),
+    lambda: clusters.square_bath(nb=4, nk1=8, ngfiter=20, omega_nodes=64),
+])
+def test_kpoint_pairs_match_brute_force(make):
+    from vca_gb300.solver import pair_kpoints
+    pt = make()
+    reps, w = pair_kpoints(pt.Hk)
+    assert w.sum() == pt.Nk and np.all(np.diff(reps) > 0)
+    if pt.Nk <= 256:
+        r2, w2 = _brute_pairs(pt.Hk)
+        # generic grids pair uniquely: the same representatives and weights
+        np.testing.assert_array_equal(reps, r2)
+        np.testing.assert_array_equal(w, w2)
+
+
+def test_kpoint_pairs_known_counts_and_random():
+    from vca_gb300.solver import pair_kpoints
+    pt = clusters.square(nx=4, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=32, nky=32, ngfiter=20, omega_nodes=64)
+    assert len(pair_kpoints(pt.Hk)[0]) == 514  # the benchmark grid: 514 of 1024 points
+    rng = np.random.default_rng(4)
+    H = rng.normal(size=(3, 3, 1, 1, 1, 1, 40)) + 1j * rng.normal(size=(3, 3, 1, 1, 1, 1, 40))
+    reps, w = pair_kpoints(H)
+    assert len(reps) == 40 and np.all(w == 1.0)  # no conjugate partners
+    H[..., 7] = np.conj(H[..., 30])
+    reps, w = pair_kpoints(H)
+    assert len(reps) == 39 and w[list(reps).index(7)] == 2.0 and 30 not in reps
+
+
+def test_contour_rule_matches_oracle():
+    from vca_gb300.solver import contour_rule
+    rng = np.random.default_rng(6)
+    for _ in range(200):
+        R = float(rng.uniform(1.0, 60.0))
+        beta = float(rng.choice([0.5, 5.0, 40.0, 400.0]))
+        mu = float(rng.uniform(-1.2, 1.2)) * R
+        ngl = int(rng.choice([2, 8, 24]))
+        th, w = contour_rule(R, beta, mu, ngl)
+        th2, w2 = orc.contour_rule(R, beta, mu, ngl)
+        assert len(th) == len(th2)
+        np.testing.assert_allclose(th, th2, rtol=0, atol=1e-15)
+        np.testing.assert_allclose(w, w2, rtol=0, atol=1e-15)
+        assert abs(w.sum() - np.pi) < 1e-12 and np.all(np.diff(th) > 0)

@@ -1993,7 +1993,14 @@ double omega_prime() {
 // per pair with weight 2.  Candidates are found through a random linear
 // signature of the matrix (sorted), then checked entry by entry; a point
 // without a partner keeps weight 1.
-int pair_kpoints(const double* Hk, int64_t Nk, size_t nel) {
+// k-points paired by H_k' = conj(H_k), entry-wise to 1e-13 (1 + max|H|):
+// each pair is summed once with weight 2 (the Omega integrand is equal at
+// the two points of a pair for the models that take this path), an unpaired
+// point with weight 1.  Candidates are found through a random real linear
+// signature of H_k and of conj(H_k), sorted; every match is verified entry by
+// entry.  reps in ascending order of k.  Host only.
+void pair_kpoints_host(const double* Hk, int64_t Nk, size_t nel, std::vector<int64_t>& reps,
+                       std::vector<double>& wts) {
   std::vector<double> cr(nel), ci(nel);
   uint64_t st = 0x9E3779B97F4A7C15ull;
   auto rnd = [&]() {
@@ -2023,10 +2030,11 @@ int pair_kpoints(const double* Hk, int64_t Nk, size_t nel) {
     csig[k] = b;
   }
   std::sort(sig.begin(), sig.end());
+  reps.clear();
+  wts.clear();
+  if (Nk == 0) return;
   const double stol = tol * wsum * 2.0 + 1e-12 * (std::fabs(sig.front().first) + std::fabs(sig.back().first));
   std::vector<char> used(Nk, 0);
-  std::vector<int64_t> reps;
-  std::vector<double> wts;
   auto conj_of = [&](int64_t j, int64_t k) {
     const double* a = Hk + 2 * nel * j;
     const double* b = Hk + 2 * nel * k;
@@ -2049,6 +2057,12 @@ int pair_kpoints(const double* Hk, int64_t Nk, size_t nel) {
       wts.push_back(1.0);
     }
   }
+}
+
+int pair_kpoints(const double* Hk, int64_t Nk, size_t nel) {
+  std::vector<int64_t> reps;
+  std::vector<double> wts;
+  pair_kpoints_host(Hk, Nk, nel, reps, wts);
   g->Nk_rep = (int64_t)reps.size();
   int64_t* d_rep;
   Arena tmp;
@@ -2591,6 +2605,35 @@ int vca_gpu_read_gfprime(const char* file, const char* suffix, int32_t used, int
   g->gfm_chan0 = std::move(c0);
   g->gfm_exc0 = std::move(x0);
   g->gfm_loaded = true;
+  return VCA_OK;
+}
+
+int vca_pair_kpoints(const double* Hk, int64_t Nk, int64_t nel, int64_t* reps, double* weights, int64_t cap,
+                     int64_t* nrep) {
+  if (!Hk || Nk < 0 || nel < 1 || !nrep || cap < 0 || (cap > 0 && (!reps || !weights)))
+    VFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<int64_t> r;
+  std::vector<double> w;
+  pair_kpoints_host(Hk, Nk, (size_t)nel, r, w);
+  *nrep = (int64_t)r.size();
+  for (int64_t i = 0; i < (int64_t)r.size() && i < cap; i++) {
+    reps[i] = r[i];
+    weights[i] = w[i];
+  }
+  return VCA_OK;
+}
+
+int vca_contour_rule(double R, double beta, double mu, int32_t ngl, double* theta, double* weights, int32_t cap,
+                     int32_t* n) {
+  if (!n || ngl < 2 || !(R > 0.0) || !(beta > 0.0) || cap < 0 || (cap > 0 && (!theta || !weights)))
+    VFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<double> th, wt;
+  contour_nodes_host(R, beta, mu, ngl, th, wt);
+  *n = (int32_t)th.size();
+  for (int i = 0; i < (int)th.size() && i < cap; i++) {
+    theta[i] = th[i];
+    weights[i] = wt[i];
+  }
   return VCA_OK;
 }
 

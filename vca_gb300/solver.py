@@ -38,7 +38,7 @@ EXPORTS = [
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
     "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
-    "vca_state_list_t0", "vca_state_list_finite_t",
+    "vca_state_list_t0", "vca_state_list_finite_t", "vca_pair_kpoints", "vca_contour_rule",
 ]
 
 
@@ -129,6 +129,9 @@ def load(path: Optional[str] = None):
                                              ctypes.POINTER(i32)]),
         "vca_state_list_finite_t": (ctypes.c_int, [dp, i32, cfgp, i32, ctypes.POINTER(i32), i32,
                                                    ctypes.POINTER(i32), dp, dp, ctypes.POINTER(i32)]),
+        "vca_pair_kpoints": (ctypes.c_int, [dp, i64, i64, ctypes.POINTER(i64), dp, i64, ctypes.POINTER(i64)]),
+        "vca_contour_rule": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, i32, dp, dp, i32,
+                                            ctypes.POINTER(i32)]),
         "vca_gpu_print_impSigma": (ctypes.c_int, []),
         "vca_gpu_print_impG": (ctypes.c_int, []),
         "vca_gpu_print_impG0": (ctypes.c_int, []),
@@ -508,6 +511,30 @@ def state_list_finite_t(E, cfg: VcaConfig, nstates_total: int):
     check(load().vca_state_list_finite_t(_dp(E), len(E), ctypes.byref(cfg), nstates_total, sec.ctypes.data_as(i32p),
                                          cap, ctypes.byref(n), ctypes.byref(z), ctypes.byref(lo), ctypes.byref(nt)))
     return sec[:n.value].tolist(), z.value, lo.value, nt.value
+
+
+def pair_kpoints(Hk):
+    """(representatives, weights) of the Omega k-sum for Hk of shape
+    (...,Nk): conjugate pairs H_k' = conj(H_k) summed once with weight 2."""
+    Hk = np.asfortranarray(Hk, dtype=np.complex128)
+    Nk = Hk.shape[-1]
+    nel = Hk.size // max(Nk, 1)
+    reps = np.zeros(max(Nk, 1), dtype=np.int64)
+    w = np.zeros(max(Nk, 1))
+    n = ctypes.c_int64()
+    check(load().vca_pair_kpoints(_dp(Hk), Nk, nel, reps.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _dp(w),
+                                  len(reps), ctypes.byref(n)))
+    return reps[:n.value], w[:n.value]
+
+
+def contour_rule(R: float, beta: float, mu: float, ngl: int):
+    """Nodes and weights on [0, pi] of the contour rule at radius R."""
+    n = ctypes.c_int32()
+    check(load().vca_contour_rule(R, beta, mu, ngl, None, None, 0, ctypes.byref(n)))
+    th = np.zeros(n.value)
+    w = np.zeros(n.value)
+    check(load().vca_contour_rule(R, beta, mu, ngl, _dp(th), _dp(w), n.value, ctypes.byref(n)))
+    return th, w
 
 
 # ---- GFmatrix restart files (host only, no GPU needed) --------------------
