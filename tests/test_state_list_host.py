@@ -144,3 +144,14 @@ def test_contour_rule_matches_oracle():
         np.testing.assert_allclose(th, th2, rtol=0, atol=1e-15)
         np.testing.assert_allclose(w, w2, rtol=0, atol=1e-15)
         assert abs(w.sum() - np.pi) < 1e-12 and np.all(np.diff(th) > 0)
+
+
+def test_hooks_reject_bad_arguments():
+    from vca_gb300.solver import VcaError
+    with pytest.raises(VcaError) as e:
+        state_list_finite_t(np.array([0.0, 1.0]), default_config(beta=1.0), 0)
+    assert e.value.code == -9
+    with pytest.raises(VcaError) as e:
+        state_list_finite_t(np.array([0.0]), default_config(beta=1.0, cutoff=1.0), 2)
+    assert e.value.code == -1
+    assert state_list_finite_t(np.zeros(0), default_config(beta=1.0), 2)[0] == []

@@ -2653,7 +2653,8 @@ int vca_state_list_t0(const double* E, int32_t nsectors, double gs_threshold, in
 int vca_state_list_finite_t(const double* E, int32_t nsectors, const vca_config* cfg, int32_t nstates_total,
                             int32_t* sectors, int32_t cap, int32_t* n, double* zeta, double* emin,
                             int32_t* nstates_total_out) {
-  if (!E || nsectors < 0 || !cfg || !n || cap < 0 || (cap > 0 && !sectors)) VFAIL(VCA_ERR_ARG, "bad arguments");
+  if (!E || nsectors < 0 || !cfg || !n || cap < 0 || (cap > 0 && !sectors) || nstates_total < 1)
+    VFAIL(VCA_ERR_ARG, "bad arguments");
   if (!(cfg->cutoff > 0.0 && cfg->cutoff < 1.0) || !(cfg->beta > 0.0) || cfg->lanc_niter_spectrum < 1)
     VFAIL(VCA_ERR_CONFIG, "CUTOFF in (0,1), BETA > 0 and LANC_NITER_SPECTRUM >= 1 are required");
   std::vector<ListEntry> lst;
