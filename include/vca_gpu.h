@@ -332,7 +332,7 @@ int vca_gpu_sum_kmesh_complex(const double* z, int64_t nz, double* f_out);
 /*
  * One custom observable of the last solve: init_custom_observables /
  * add_custom_observable / get_custom_observables (VCA_OBSERVABLES.f90:
- * 89-170) for a single item, whose value the reference prints and writes
+ * 76-165) for a single item, whose value the reference prints and writes
  * (write_custom_observables).  s is (Nlat,Nlat,Nspin,Nspin,Norb,Norb)
  * complex, the same at every k (kdep = 0, add_custom_observable_local), or
  * (...,Nk) (kdep = 1, add_custom_observable_kdep).  With the lattice

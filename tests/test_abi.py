@@ -82,3 +82,20 @@ def test_unterminated_file_suffix_rejected(lib):
     c.file_suffix = b"x" * 64
     assert lib.vca_gpu_init(ctypes.byref(c), None, None) == -1
     assert default_config(file_suffix="_a").file_suffix == b"_a"
+
+
+def test_module_names_of_the_reference(lib):
+    """The public names of module VCA (VCA.f90:1-38) exist at module level in
+    the Python mirror and raise VCA_ERR_STATE before vca_init_solver."""
+    names = ["vca_init_solver", "vca_solve", "vca_get_sft_potential", "vca_gf_cluster", "vca_get_sigma_matsubara",
+             "vca_get_sigma_realaxis", "vca_get_gimp_matsubara", "vca_get_gimp_realaxis", "vca_get_dens",
+             "vca_get_mag", "vca_get_docc", "init_custom_observables", "add_custom_observable",
+             "get_custom_observables", "clear_custom_observables", "vca_print_impSigma", "vca_print_impG",
+             "vca_print_impG0", "save_gfprime", "read_gfprime", "vca_get_cluster_dimension"]
+    for n in names:
+        assert callable(getattr(solver, n)), n
+    solver._solver = None
+    for n in ("vca_get_dens", "vca_get_sigma_matsubara", "vca_print_impG", "get_custom_observables"):
+        with pytest.raises(solver.VcaError) as e:
+            getattr(solver, n)()
+        assert e.value.code == -3

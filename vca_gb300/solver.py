@@ -391,7 +391,7 @@ class VcaSolver:
 
     # custom-observable registry with the reference's call sequence
     # (init_custom_observables, add_custom_observable, get_custom_observables,
-    # clear_custom_observables, VCA_OBSERVABLES.f90:81-189)
+    # clear_custom_observables, VCA_OBSERVABLES.f90:76-180)
     def init_custom_observables(self, n: int, nk: int):
         self._custom = {"asked": int(n), "nk": int(nk), "items": []}
 
@@ -469,15 +469,15 @@ class VcaSolver:
         return self.cfg.file_suffix.decode() if suffix is None else suffix
 
     def print_impSigma(self):
-        """vca_print_impSigma (VCA_IO.f90:112-136): splot files of Sigma."""
+        """vca_print_impSigma (VCA_IO.f90:112-138): splot files of Sigma."""
         check(self.L.vca_gpu_print_impSigma())
 
     def print_impG(self):
-        """vca_print_impG (VCA_IO.f90:143-170): splot files of G'."""
+        """vca_print_impG (VCA_IO.f90:146-173): splot files of G'."""
         check(self.L.vca_gpu_print_impG())
 
     def print_impG0(self):
-        """vca_print_impG0 (VCA_IO.f90:176-205): splot files of G0."""
+        """vca_print_impG0 (VCA_IO.f90:179-205): splot files of G0."""
         check(self.L.vca_gpu_print_impG0())
 
     def close(self):
@@ -640,13 +640,105 @@ def vca_solve(Hloc, Hk, bath_h=None, bath_v=None) -> float:
     return _solver.solve(Hloc, Hk, bath_h, bath_v)
 
 
-def vca_get_sft_potential() -> float:
+def _ctx() -> VcaSolver:
     if _solver is None:
         raise VcaError(-3, "vca_init_solver has not been called")
-    return _solver.get_sft_potential()
+    return _solver
+
+
+def vca_get_sft_potential() -> float:
+    """vca_get_sft_potential (VCA_IO/get_sft_potential.f90:1-4)."""
+    return _ctx().get_sft_potential()
 
 
 def vca_gf_cluster(z) -> np.ndarray:
-    if _solver is None:
-        raise VcaError(-3, "vca_init_solver has not been called")
-    return _solver.gf_cluster(z)
+    """vca_gf_cluster (VCA_IO/gf_cluster.f90): G'(z), shape (...,len(z))."""
+    return _ctx().gf_cluster(z)
+
+
+# the other public names of module VCA (VCA.f90:1-38)
+def vca_get_sigma_matsubara() -> np.ndarray:
+    """vca_get_sigma_matsubara (VCA_IO/get_sigma_matsubara.f90)."""
+    return _ctx().sigma_matsubara()
+
+
+def vca_get_sigma_realaxis() -> np.ndarray:
+    """vca_get_sigma_realaxis (VCA_IO/get_sigma_realaxis.f90)."""
+    return _ctx().sigma_realaxis()
+
+
+def vca_get_gimp_matsubara() -> np.ndarray:
+    """vca_get_gimp_matsubara (VCA_IO/get_gimp_matsubara.f90)."""
+    return _ctx().gimp_matsubara()
+
+
+def vca_get_gimp_realaxis() -> np.ndarray:
+    """vca_get_gimp_realaxis (VCA_IO/get_gimp_realaxis.f90)."""
+    return _ctx().gimp_realaxis()
+
+
+def vca_get_dens() -> np.ndarray:
+    """vca_get_dens (VCA_IO/get_dens.f90): (Nlat,Norb)."""
+    return _ctx().observables()["dens"]
+
+
+def vca_get_mag() -> np.ndarray:
+    """vca_get_mag (VCA_IO/get_mag.f90): (Nlat,Norb)."""
+    return _ctx().observables()["mag"]
+
+
+def vca_get_docc() -> np.ndarray:
+    """vca_get_docc (VCA_IO/get_docc.f90): (Nlat,Norb)."""
+    return _ctx().observables()["docc"]
+
+
+def init_custom_observables(N: int, Nk: int):
+    """init_custom_observables (VCA_OBSERVABLES.f90:76-87)."""
+    return _ctx().init_custom_observables(N, Nk)
+
+
+def add_custom_observable(name: str, sij):
+    """add_custom_observable, local or k-dependent (VCA_OBSERVABLES.f90:89-134)."""
+    return _ctx().add_custom_observable(name, sij)
+
+
+def get_custom_observables() -> dict:
+    """get_custom_observables (VCA_OBSERVABLES.f90:137-165): name -> value."""
+    return _ctx().get_custom_observables()
+
+
+def clear_custom_observables():
+    """clear_custom_observables (VCA_OBSERVABLES.f90:168-180)."""
+    return _ctx().clear_custom_observables()
+
+
+def vca_print_impSigma():
+    """vca_print_impSigma (VCA_IO.f90:112-138)."""
+    _ctx().print_impSigma()
+
+
+def vca_print_impG():
+    """vca_print_impG (VCA_IO.f90:146-173)."""
+    _ctx().print_impG()
+
+
+def vca_print_impG0():
+    """vca_print_impG0 (VCA_IO.f90:179-205)."""
+    _ctx().print_impG0()
+
+
+def save_gfprime(file: str = "gfprime", used: bool = False, use_formatted: bool = False):
+    """save_gfprime (VCA_AUX_FUNX.f90:601-645)."""
+    return _ctx().save_gfprime(file, used, use_formatted)
+
+
+def read_gfprime(file: str = "gfprime", used: bool = False, use_formatted: bool = False):
+    """read_gfprime (VCA_AUX_FUNX.f90:651-697)."""
+    _ctx().read_gfprime(file, used, use_formatted)
+
+
+def vca_get_cluster_dimension(with_bath: bool = False) -> int:
+    """vca_get_cluster_dimension (VCA_AUX_FUNX.f90:97-114): Nspin * levels."""
+    c = _ctx().cfg
+    ns = c.Nlat * c.Norb + (c.Nlat_bath * c.Norb_bath if with_bath else 0)
+    return c.Nspin * ns
