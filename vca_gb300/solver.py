@@ -16,6 +16,7 @@ from typing import Optional
 
 import numpy as np
 
+from . import search as _search
 from .config import VcaConfig, hloc_shape, bath_h_shape, bath_v_shape
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -735,6 +736,21 @@ def save_gfprime(file: str = "gfprime", used: bool = False, use_formatted: bool 
 def read_gfprime(file: str = "gfprime", used: bool = False, use_formatted: bool = False):
     """read_gfprime (VCA_AUX_FUNX.f90:651-697)."""
     _ctx().read_gfprime(file, used, use_formatted)
+
+
+# density searches (VCA_AUX_FUNX.f90:700-897); the SAVE state of the
+# reference's module lives in search_state
+search_state = _search.SearchState()
+
+
+def search_chemical_potential(var: float, ntmp: float, converged: bool):
+    """search_chemical_potential(var, ntmp, converged) -> (var, converged)."""
+    return _search.search_chemical_potential(search_state, var, ntmp, converged)
+
+
+def vca_search_variable(var: float, ntmp: float, converged: bool):
+    """vca_search_variable(var, ntmp, converged) -> (var, converged)."""
+    return _search.vca_search_variable(search_state, var, ntmp, converged)
 
 
 def vca_get_cluster_dimension(with_bath: bool = False) -> int:
