@@ -32,7 +32,7 @@ class SearchState:
     niter: int = 0
     file_suffix: str = ""
     write_files: bool = True
-    # SAVE variables of search_chemical_potential (VCA_AUX_FUNX.f90:796-803)
+    # SAVE variables of search_chemical_potential (VCA_AUX_FUNX.f90:798-804)
     count: int = 0
     totcount: int = 0
     nindex: int = 0
@@ -40,7 +40,7 @@ class SearchState:
     nth_magnitude_old: int = -2
     nth: float = 1e-2
     ireduce: bool = True
-    # SAVE variables of vca_search_variable (:713-720)
+    # SAVE variables of vca_search_variable (:714-721)
     v_count: int = 0
     v_totcount: int = 0
     chich: float = 0.0
@@ -67,7 +67,7 @@ def search_chemical_potential(st: SearchState, var: float, ntmp: float, converge
     The history nindex_old(3) of the reference is a local array without
     SAVE: only nindex_old(1) is assigned on every call, so entries 2 and 3
     hold whatever the stack held.  They are taken as 0 here, which leaves
-    the flip test of the commented-out form at :834, a step against the
+    the flip test of the commented-out form at :830, a step against the
     previous call's direction."""
     ndiff = ntmp - st.nread
     nratio = 0.5
