@@ -218,6 +218,14 @@ int vca_gpu_get_g0_realaxis(double* g0_out);
 int vca_gpu_print_impSigma(void);
 int vca_gpu_print_impG(void);
 int vca_gpu_print_impG0(void);
+/* vca_read_impSigma (VCA_IO.f90:208-239): Sigma on both grids from the
+ * impSigma splot files above (cfg.file_suffix, the config's Lmats/Lreal
+ * lines each); until the next solve the Sigma getters return it, as the
+ * reference's read fills impSmats / impSreal.  Needs vca_gpu_init only.
+ * vca_splot_read: one such file, n lines of x, Im, Re, into x (may be NULL)
+ * and y (complex); host only. */
+int vca_read_impSigma(void);
+int vca_splot_read(const char* path, int64_t n, double* x, double* y);
 
 /* Ground-state observables of the last solve, (Nlat,Norb) column-major:
  * density n_up + n_dw, its spin parts, double occupancy n_up n_dw and

@@ -80,3 +80,30 @@ def test_print_flags_print_at_the_end_of_a_solve(tmp_path, monkeypatch):
     _check(s, c, "impSigma", s.sigma_matsubara, True, "")
     _check(s, c, "impG0", s.g0_realaxis, False, "")
     s.close()
+
+
+def test_read_impsigma_gives_the_printed_sigma_back(tmp_path, monkeypatch):
+    """vca_read_impSigma (VCA_IO.f90:208-239): a fresh context reads the
+    files of another and its Sigma getters return them, bit-exact, until a
+    solve replaces them."""
+    monkeypatch.chdir(tmp_path)
+    pt = _point(file_suffix=b"_r")
+    c = pt.cfg
+    s = VcaSolver(c)
+    s.solve(pt.Hloc, pt.Hk)
+    sm, sr = s.sigma_matsubara(), s.sigma_realaxis()
+    s.print_impSigma()
+    s.close()
+    r = VcaSolver(c)
+    with pytest.raises(VcaError) as e:
+        r.sigma_matsubara()
+    assert e.value.code == -3
+    r.read_impSigma()
+    assert np.array_equal(r.sigma_matsubara(), sm) and np.array_equal(r.sigma_realaxis(), sr)
+    # the solve recomputes Sigma from its own chains
+    r.solve(pt.Hloc, pt.Hk)
+    assert np.abs(r.sigma_matsubara() - sm).max() < 1e-12
+    r.close()
+    with pytest.raises(VcaError) as e:
+        VcaSolver(_point(file_suffix=b"_none")).read_impSigma()
+    assert e.value.code == -10

@@ -164,6 +164,10 @@ struct Ctx {
   double t_ms[4] = {0, 0, 0, 0};  // set_hamiltonian, diagonalise, chains, Omega
   // GFmatrix read from a restart file (read_gfprime): replaces the solve's
   // tables for G'(z) and the channel getter until the next solve
+  // Sigma read back by vca_read_impSigma: the Sigma getters return it until
+  // the next solve, (Nlat,Nlat,Nspin,Nspin,Norb,Norb,L) complex per grid
+  bool sigma_loaded = false;
+  std::vector<double> sigma_mats, sigma_real;
   bool gfm_loaded = false;
   GfmTable gfm;                     // host copy, file order
   std::vector<int64_t> gfm_state0;  // per file element: its first entry in gfm.nchan
@@ -2131,6 +2135,9 @@ int solve_resident(const double* Hloc, const double* bath_h, const double* bath_
   if (!g->d_Hk) VFAIL(VCA_ERR_STATE, "no Hk resident: call vca_gpu_solve or vca_gpu_upload_hk first");
   g->solved = false;
   gfm_drop();  // vca_solve rebuilds impGmatrix
+  g->sigma_loaded = false;  // and impSmats / impSreal
+  g->sigma_mats.clear();
+  g->sigma_real.clear();
   double t0 = now_ms();
   RCHK(set_hamiltonian(Hloc, bath_h, bath_v));
   double t1 = now_ms();
@@ -2791,6 +2798,12 @@ static int gimp_grid(bool mats, double* g_out) {
 // build_sigma_normal (VCA_GF_NORMAL.f90:1045-1111), out in
 // (Nlat,Nlat,Nspin,Nspin,Norb,Norb,L) order
 static int sigma_grid(bool mats, bool want_g0, double* out) {
+  if (g && !want_g0 && g->sigma_loaded) {  // read by vca_read_impSigma
+    if (!out) VFAIL(VCA_ERR_ARG, "NULL output");
+    const std::vector<double>& v = mats ? g->sigma_mats : g->sigma_real;
+    std::copy(v.begin(), v.end(), out);
+    return VCA_OK;
+  }
   if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   if (!out) VFAIL(VCA_ERR_ARG, "NULL output");
   const vca_config& c = g->cfg;
@@ -2969,7 +2982,7 @@ static int print_after_solve() {
 }
 
 int vca_gpu_print_impSigma(void) {
-  if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
+  if (!g || !(g->solved || g->sigma_loaded)) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   return print_function(1);
 }
 int vca_gpu_print_impG(void) {
@@ -2979,6 +2992,74 @@ int vca_gpu_print_impG(void) {
 int vca_gpu_print_impG0(void) {
   if (!g || !g->solved) VFAIL(VCA_ERR_STATE, "no completed vca_gpu_solve");
   return print_function(2);
+}
+
+// One splot file of a complex function: n lines of x, Im y, Re y (blank- or
+// comma-separated, D or E exponents).  Host only.
+static int splot_read(const std::string& path, int64_t n, double* x, double* y) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) VFAIL(VCA_ERR_IO, "cannot open " + path + ": " + std::strerror(errno));
+  std::string text;
+  char buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, got);
+  std::fclose(f);
+  for (char& ch : text)
+    if (ch == 'd' || ch == 'D') ch = 'e';
+    else if (ch == ',') ch = ' ';
+  const char* p = text.c_str();
+  for (int64_t i = 0; i < n; i++) {
+    double v[3];
+    for (int k = 0; k < 3; k++) {
+      char* end = nullptr;
+      v[k] = std::strtod(p, &end);
+      if (end == p) VFAIL(VCA_ERR_IO, path + ": expected " + std::to_string(n) + " lines of x, Im, Re");
+      p = end;
+    }
+    if (x) x[i] = v[0];
+    y[2 * i] = v[2];
+    y[2 * i + 1] = v[1];
+  }
+  return VCA_OK;
+}
+
+int vca_splot_read(const char* path, int64_t n, double* x, double* y) {
+  if (!path || n < 0 || (n > 0 && !y)) VFAIL(VCA_ERR_ARG, "bad arguments");
+  return splot_read(path, n, x, y);
+}
+
+int vca_read_impSigma(void) {
+  if (!g || !g->basis.ptrs.size()) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  const vca_config& c = g->cfg;
+  const std::string sfx = cfg_suffix();
+  const size_t nel = hloc_len(c);
+  std::vector<double> sm(2 * nel * (size_t)std::max(c.Lmats, 0), 0.0), sr(2 * nel * (size_t)std::max(c.Lreal, 0), 0.0);
+  for (int m = 0; m < 2; m++) {
+    const bool mats = (m == 0);
+    const int L = mats ? c.Lmats : c.Lreal;
+    if (L <= 0) continue;
+    std::vector<double>& dst = mats ? sm : sr;
+    std::vector<double> y(2 * (size_t)L);
+    for (int is = 0; is < c.Nspin; is++)
+      for (int il = 0; il < c.Nlat; il++)
+        for (int jl = 0; jl < c.Nlat; jl++)
+          for (int io = 0; io < c.Norb; io++)
+            for (int jo = 0; jo < c.Norb; jo++) {
+              char tag[96];
+              std::snprintf(tag, sizeof tag, "_Isite%04d_Jsite%04d_l%d%d_s%d_%s", il + 1, jl + 1, io + 1, jo + 1,
+                            is + 1, mats ? "iw" : "realw");
+              RCHK(splot_read(std::string("impSigma") + tag + sfx + ".vca", L, nullptr, y.data()));
+              const int64_t off = idx_nnn(c, il, jl, is, is, io, jo);
+              for (int q = 0; q < L; q++) {
+                dst[2 * ((size_t)q * nel + off)] = y[2 * q];
+                dst[2 * ((size_t)q * nel + off) + 1] = y[2 * q + 1];
+              }
+            }
+  }
+  g->sigma_mats.swap(sm);
+  g->sigma_real.swap(sr);
+  g->sigma_loaded = true;
+  return VCA_OK;
 }
 
 int vca_gpu_get_sigma_matsubara(double* s_out) { return sigma_grid(true, false, s_out); }

@@ -40,6 +40,7 @@ EXPORTS = [
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
     "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
     "vca_state_list_t0", "vca_state_list_finite_t", "vca_pair_kpoints", "vca_contour_rule",
+    "vca_read_impSigma", "vca_splot_read",
 ]
 
 
@@ -134,6 +135,8 @@ def load(path: Optional[str] = None):
         "vca_contour_rule": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, i32, dp, dp, i32,
                                             ctypes.POINTER(i32)]),
         "vca_gpu_print_impSigma": (ctypes.c_int, []),
+        "vca_read_impSigma": (ctypes.c_int, []),
+        "vca_splot_read": (ctypes.c_int, [ctypes.c_char_p, i64, dp, dp]),
         "vca_gpu_print_impG": (ctypes.c_int, []),
         "vca_gpu_print_impG0": (ctypes.c_int, []),
         "vca_gpu_save_gfprime": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, i32, i32]),
@@ -473,6 +476,11 @@ class VcaSolver:
         """vca_print_impSigma (VCA_IO.f90:112-138): splot files of Sigma."""
         check(self.L.vca_gpu_print_impSigma())
 
+    def read_impSigma(self):
+        """vca_read_impSigma (VCA_IO.f90:208-239): Sigma from the impSigma
+        splot files; the Sigma getters return it until the next solve."""
+        check(self.L.vca_read_impSigma())
+
     def print_impG(self):
         """vca_print_impG (VCA_IO.f90:146-173): splot files of G'."""
         check(self.L.vca_gpu_print_impG())
@@ -552,10 +560,16 @@ def splot_name(name: str, ilat: int, jlat: int, iorb: int, jorb: int, ispin: int
             f"{'iw' if matsubara else 'realw'}{suffix}.vca")
 
 
-def read_splot(path: str):
-    """x and the complex function of a splot file (columns x, Im, Re)."""
-    a = np.loadtxt(path, ndmin=2)
-    return a[:, 0], a[:, 2] + 1j * a[:, 1]
+def read_splot(path: str, n: Optional[int] = None):
+    """x and the complex function of a splot file (columns x, Im, Re); n
+    lines (default: the file's line count)."""
+    if n is None:
+        with open(path) as f:
+            n = sum(1 for line in f if line.strip())
+    x = np.zeros(n)
+    y = np.zeros(n, dtype=np.complex128)
+    check(load().vca_splot_read(path.encode(), n, _dp(x), _dp(y)))
+    return x, y
 
 
 def gfm_elements(cfg: VcaConfig):
@@ -716,6 +730,11 @@ def clear_custom_observables():
 def vca_print_impSigma():
     """vca_print_impSigma (VCA_IO.f90:112-138)."""
     _ctx().print_impSigma()
+
+
+def vca_read_impSigma():
+    """vca_read_impSigma (VCA_IO.f90:208-239)."""
+    _ctx().read_impSigma()
 
 
 def vca_print_impG():
