@@ -17,6 +17,8 @@ from typing import Optional
 import numpy as np
 
 from . import search as _search
+from .reshape import (vca_lso2nnn_reshape, vca_nn2so_reshape, vca_nnn2lso_reshape,  # noqa: F401
+                      vca_rectangular_j2n_reshape, vca_rectangular_n2j_reshape, vca_so2nn_reshape)
 from .config import VcaConfig, hloc_shape, bath_h_shape, bath_v_shape
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
