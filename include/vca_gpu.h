@@ -91,8 +91,8 @@ typedef struct vca_config {
   int32_t vca_gf_symmetric;    /* VCA_GF_SYMMETRIC  2-channel off-diag GF */
   int32_t vca_sparse_H;        /* VCA_SPARSE_H  stored semantics (always) */
   int32_t vca_twin;            /* VCA_TWIN                                */
-  int32_t vca_sectors;         /* VCA_SECTORS   restrict sector scan      */
-  int32_t vca_sectors_shift;   /* VCA_SECTORS_SHIFT                       */
+  int32_t vca_sectors;         /* VCA_SECTORS   accepted; every sector is */
+  int32_t vca_sectors_shift;   /* VCA_SECTORS_SHIFT  scanned (a superset)  */
   int32_t verbose;             /* VERBOSE                                 */
   /* ---- no counterpart in the reference ---------------------------------- */
   int32_t omega_nodes;     /* Gauss-Legendre nodes on [0,inf) for Omega     */
