@@ -12,7 +12,10 @@ eigenpairs per sector, Neigen = min(dim, neigen_sector).
   <g|c^dag (z - E + H)^-1 c|g>];
 * finite T at U=0: with every sector's excited states in the list the
   Omega of the annealed list is the exact lattice grand potential; one state
-  per sector misses the in-sector excitations.
+  per sector misses the in-sector excitations;
+* finite T at U=4: with all 16 states of the two-site chain listed, zeta,
+  Omega' and G'_ii(z) equal the exact thermal Lehmann results (the Boltzmann
+  weights of the chains, pesoBZ = norm2 e^{-beta(E_i-E_gs)}/zeta).
 """
 import numpy as np
 import pytest
@@ -148,3 +151,41 @@ def test_finite_t_u0_is_the_lattice_value_with_excited_states():
     ne = o.neigen()
     for isec in range(1, o.Nsectors + 1):
         assert ne[isec - 1] == o.dim(isec) + 1
+
+
+def test_finite_t_gf_is_the_exact_thermal_average():
+    """Interacting two-site chain (U=4) at beta=1 in the arpack method: the
+    list holds all 16 cluster states, so G'_ii(z) must be the exact thermal
+    Lehmann sum (1/Z) sum_m e^{-beta E_m} [<m|c (z+E_m-H)^-1 c^dag|m> +
+    <m|c^dag (z-E_m+H)^-1 c|m>] over every eigenstate m of every sector,
+    evaluated here with dense resolvents, and Omega' = -T ln Z."""
+    beta = 1.0
+    pt = clusters.chain1d(tprime=1.0, nlat=2, U=4.0, xmu=1.3, nk=8, ngfiter=50, omega_nodes=64,
+                          lanc_nstates_total=2, beta=beta, bandwidth=4.0)
+    pt = _with(pt, lanc_method=LANC_ARPACK, lanc_niter_spectrum=20)
+    o = Oracle.from_point(pt)
+    o.solve()
+    assert len(o.states()) == 16
+    eig = {isec: np.linalg.eigh(o.dense_h(isec)) for isec in range(1, o.Nsectors + 1)}
+    e0 = min(w.min() for w, _ in eig.values())
+    Z = sum(np.exp(-beta * (w - e0)).sum() for w, _ in eig.values())
+    t = o.thermal()
+    assert abs(t["zeta"] - Z) < 1e-12 * Z
+    assert abs(t["omega_prime"] - (e0 - np.log(Z) / beta)) < 1e-12
+    zs = np.array([0.5j, 1.1 + 0.3j, -0.7 + 2.0j])
+    G = o.gf_cluster(zs)
+    for site in range(2):
+        ref = np.zeros(len(zs), dtype=np.complex128)
+        for isec, (w, V) in eig.items():
+            for m in range(len(w)):
+                pm = np.exp(-beta * (w[m] - e0)) / Z
+                for dag in (True, False):
+                    tgt, v = _apply(o, isec, V[:, m], site, dag)
+                    if tgt == 0 or not np.any(v):
+                        continue
+                    Ht = o.dense_h(tgt)
+                    I = np.eye(len(v))
+                    for q, z in enumerate(zs):
+                        A = (z + w[m]) * I - Ht if dag else (z - w[m]) * I + Ht
+                        ref[q] += pm * np.vdot(v, np.linalg.solve(A, v))
+        assert np.abs(G[site, site, 0, 0, 0, 0, :] - ref).max() < 1e-10, site
