@@ -13,9 +13,10 @@ eigenpairs per sector, Neigen = min(dim, neigen_sector).
 * finite T at U=0: with every sector's excited states in the list the
   Omega of the annealed list is the exact lattice grand potential; one state
   per sector misses the in-sector excitations;
-* finite T at U=4: with all 16 states of the two-site chain listed, zeta,
-  Omega' and G'_ii(z) equal the exact thermal Lehmann results (the Boltzmann
-  weights of the chains, pesoBZ = norm2 e^{-beta(E_i-E_gs)}/zeta).
+* finite T at U=4: with all states listed (two- and three-site chains), zeta,
+  Omega', G'_ii(z) and G'_ij(z) equal the exact thermal Lehmann results (the
+  Boltzmann weights of the chains, pesoBZ = norm2 e^{-beta(E_i-E_gs)}/zeta;
+  the mixed channels and their recombination, with four channels and two).
 """
 import numpy as np
 import pytest
@@ -189,3 +190,46 @@ def test_finite_t_gf_is_the_exact_thermal_average():
                         A = (z + w[m]) * I - Ht if dag else (z - w[m]) * I + Ht
                         ref[q] += pm * np.vdot(v, np.linalg.solve(A, v))
         assert np.abs(G[site, site, 0, 0, 0, 0, :] - ref).max() < 1e-10, site
+
+
+@pytest.mark.parametrize("symmetric", [0, 1])
+def test_finite_t_offdiagonal_gf_is_the_exact_thermal_average(symmetric):
+    """The same thermal cluster, off-diagonal elements: G'_ij(z) = (1/Z)
+    sum_m e^{-beta E_m} [<m|c_i (z+E_m-H)^-1 c_j^dag|m> + <m|c_j^dag
+    (z-E_m+H)^-1 c_i|m>], which the chains reach through the mixed channels
+    and the recombination 1/2[G^mix - (1 - i chan4)(G_ii + G_jj)]
+    (VCA_GF_NORMAL.f90:89-101) -- with four channels (VCA_GF_SYMMETRIC=F) and
+    with two (=T, a real model)."""
+    beta = 1.0
+    pt = clusters.chain1d(tprime=1.0, nlat=3, U=4.0, xmu=1.3, nk=8, ngfiter=80, omega_nodes=64,
+                          lanc_nstates_total=2, beta=beta, bandwidth=4.0)
+    pt = _with(pt, lanc_method=LANC_ARPACK, lanc_niter_spectrum=40, vca_gf_symmetric=symmetric)
+    o = Oracle.from_point(pt)
+    o.solve()
+    assert len(o.states()) == 64
+    eig = {isec: np.linalg.eigh(o.dense_h(isec)) for isec in range(1, o.Nsectors + 1)}
+    e0 = min(w.min() for w, _ in eig.values())
+    Z = sum(np.exp(-beta * (w - e0)).sum() for w, _ in eig.values())
+    zs = np.array([0.5j, 1.1 + 0.3j])
+    G = o.gf_cluster(zs)
+    for i, j in ((0, 1), (1, 0), (0, 2)):
+        ref = np.zeros(len(zs), dtype=np.complex128)
+        for isec, (w, V) in eig.items():
+            for m in range(len(w)):
+                pm = np.exp(-beta * (w[m] - e0)) / Z
+                if pm < 1e-300:
+                    continue
+                ti, vi = _apply(o, isec, V[:, m], i, True)
+                tj, vj = _apply(o, isec, V[:, m], j, True)
+                if ti and np.any(vi) and np.any(vj):
+                    Ht = o.dense_h(ti)
+                    for q, z in enumerate(zs):
+                        ref[q] += pm * np.vdot(vi, np.linalg.solve((z + w[m]) * np.eye(len(vi)) - Ht, vj))
+                ti, wi = _apply(o, isec, V[:, m], i, False)
+                tj, wj = _apply(o, isec, V[:, m], j, False)
+                if ti and np.any(wi) and np.any(wj):
+                    Ht = o.dense_h(ti)
+                    for q, z in enumerate(zs):
+                        ref[q] += pm * np.vdot(wj, np.linalg.solve((z - w[m]) * np.eye(len(wi)) + Ht, wi))
+        got = G[i, j, 0, 0, 0, 0, :]
+        assert np.abs(got - ref).max() < 1e-10, (i, j, got, ref)
