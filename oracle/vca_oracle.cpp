@@ -614,21 +614,30 @@ inline double start_value(uint64_t seed, int isector, int64_t i) {
   return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
 }
 
+// Sum of term(i) over [0, n): 64 contiguous chunks, each summed in index
+// order, the chunk sums added in chunk order -- the same bits for any thread
+// count and schedule (an OpenMP reduction combines thread partials in an
+// order that changes from run to run).
+template <class T, class F>
+T ordered_sum(int64_t n, F term) {
+  constexpr int kChunks = 64;
+  T part[kChunks];
+#pragma omp parallel for schedule(static)
+  for (int q = 0; q < kChunks; q++) {
+    T acc = T(0);
+    for (int64_t i = n * q / kChunks; i < n * (q + 1) / kChunks; i++) acc += term(i);
+    part[q] = acc;
+  }
+  T total = T(0);
+  for (int q = 0; q < kChunks; q++) total += part[q];
+  return total;
+}
+
 double vnorm(const std::vector<cd>& v) {
-  double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-  for (int64_t i = 0; i < (int64_t)v.size(); i++) s += std::norm(v[i]);
-  return std::sqrt(s);
+  return std::sqrt(ordered_sum<double>((int64_t)v.size(), [&](int64_t i) { return std::norm(v[i]); }));
 }
 cd vdot(const std::vector<cd>& a, const std::vector<cd>& b) {  // sum conj(a) b
-  double re = 0.0, im = 0.0;
-#pragma omp parallel for reduction(+ : re, im) schedule(static)
-  for (int64_t i = 0; i < (int64_t)a.size(); i++) {
-    cd p = std::conj(a[i]) * b[i];
-    re += p.real();
-    im += p.imag();
-  }
-  return cd(re, im);
+  return ordered_sum<cd>((int64_t)a.size(), [&](int64_t i) { return std::conj(a[i]) * b[i]; });
 }
 
 // One plain three-term Lanczos step in Paige's order (SciFortran
@@ -1481,8 +1490,8 @@ double sum_kmesh(const Oracle& o, double w) {
   delta_bath(o, cd(0.0, w), Dl);
   to_lso(o, o.Hloc.data(), Hl);
   const size_t nel = (size_t)o.cfg.Nlat * o.cfg.Nlat * o.cfg.Nspin * o.cfg.Nspin * o.cfg.Norb * o.cfg.Norb;
-  double out = 0.0;
-#pragma omp parallel for reduction(+ : out) schedule(static)
+  std::vector<double> perk(o.Nk);  // summed in k order below
+#pragma omp parallel for schedule(static)
   for (int64_t ik = 0; ik < o.Nk; ik++) {
     std::vector<cd> Hkl, M((size_t)N * N), T((size_t)N * N);
     to_lso(o, o.Hk.data() + ik * nel, Hkl);
@@ -1493,8 +1502,10 @@ double sum_kmesh(const Oracle& o, double w) {
         for (int k = 0; k < N; k++) s += M[i + (size_t)k * N] * G[k + (size_t)j * N];
         T[i + (size_t)j * N] = s;
       }
-    out += logabsdet_1pa(N, T);
+    perk[ik] = logabsdet_1pa(N, T);
   }
+  double out = 0.0;
+  for (int64_t ik = 0; ik < o.Nk; ik++) out += perk[ik];
   return out / (double)o.Nk;
 }
 
@@ -1591,8 +1602,8 @@ cd sum_kmesh_complex(const Oracle& o, cd z) {
   delta_bath(o, z, Dl);
   to_lso(o, o.Hloc.data(), Hl);
   const size_t nel = (size_t)o.cfg.Nlat * o.cfg.Nlat * o.cfg.Nspin * o.cfg.Nspin * o.cfg.Norb * o.cfg.Norb;
-  double re = 0.0, im = 0.0;
-#pragma omp parallel for reduction(+ : re, im) schedule(static)
+  std::vector<cd> perk(o.Nk);  // summed in k order below
+#pragma omp parallel for schedule(static)
   for (int64_t ik = 0; ik < o.Nk; ik++) {
     std::vector<cd> Hkl, M((size_t)N * N), T((size_t)N * N);
     to_lso(o, o.Hk.data() + ik * nel, Hkl);
@@ -1603,9 +1614,12 @@ cd sum_kmesh_complex(const Oracle& o, cd z) {
         for (int k = 0; k < N; k++) s += M[i + (size_t)k * N] * G[k + (size_t)j * N];
         T[i + (size_t)j * N] = s;
       }
-    const cd l = logdet_1pa(N, T);
-    re += l.real();
-    im += l.imag();
+    perk[ik] = logdet_1pa(N, T);
+  }
+  double re = 0.0, im = 0.0;
+  for (int64_t ik = 0; ik < o.Nk; ik++) {
+    re += perk[ik].real();
+    im += perk[ik].imag();
   }
   return cd(re, im) / (double)o.Nk;
 }
@@ -1693,8 +1707,8 @@ double sum_observable_kmesh(const Oracle& o, cd z, const std::vector<cd>& s, boo
   delta_bath(o, z, Dl);
   to_lso(o, o.Hloc.data(), Hl);
   const size_t nel = (size_t)o.cfg.Nlat * o.cfg.Nlat * o.cfg.Nspin * o.cfg.Nspin * o.cfg.Norb * o.cfg.Norb;
-  double out = 0.0;
-#pragma omp parallel for reduction(+ : out) schedule(static)
+  std::vector<double> perk(o.Nk);  // summed in k order below
+#pragma omp parallel for schedule(static)
   for (int64_t ik = 0; ik < o.Nk; ik++) {
     std::vector<cd> Hkl, Sl, A((size_t)N * N);
     to_lso(o, o.Hk.data() + ik * nel, Hkl);
@@ -1707,8 +1721,10 @@ double sum_observable_kmesh(const Oracle& o, cd z, const std::vector<cd>& s, boo
       ts += Sl[i + (size_t)i * N];
     }
     if (tail) tr -= ts / (z - 1.1);
-    out += tr.real();
+    perk[ik] = tr.real();
   }
+  double out = 0.0;
+  for (int64_t ik = 0; ik < o.Nk; ik++) out += perk[ik];
   return out / (double)o.Nk;
 }
 

@@ -399,3 +399,20 @@ def test_gf_bath_multiorbital_and_both_spins_match_dense_resolvent(make):
                         got = g[il, jl, sp - 1, sp - 1, io, jo]
                         ref = ge[io + il * c.Norb, jo + jl * c.Norb]
                         assert np.abs(got - ref).max() < 1e-9, (sp, il, jl, io, jo, got, ref)
+
+
+def test_oracle_is_deterministic_across_thread_counts():
+    """The oracle's sums run in a fixed order (contiguous chunks, k order), so
+    its results carry the same bits for any number of host threads."""
+    from oracle import oracle as orc
+    pt = SMALL["bath2+2"]()
+    out = []
+    n0 = orc.set_threads(0)  # 0 leaves the count as it is and returns it
+    for nt in (1, 5):
+        orc.set_threads(nt)
+        o = Oracle.from_point(pt)
+        sft, egs, oi = o.solve()
+        e, psi, it = o.lanczos_gs(32)
+        out.append((sft, egs, oi, e, it, psi.tobytes(), o.sum_kmesh_complex(0.7 + 0.2j)))
+    orc.set_threads(n0)
+    assert out[0] == out[1]
