@@ -92,7 +92,7 @@ def test_module_names_of_the_reference(lib):
              "vca_get_mag", "vca_get_docc", "init_custom_observables", "add_custom_observable",
              "get_custom_observables", "clear_custom_observables", "vca_print_impSigma", "vca_print_impG",
              "vca_print_impG0", "save_gfprime", "read_gfprime", "vca_get_cluster_dimension",
-             "search_chemical_potential", "vca_search_variable", "vca_read_impSigma"]
+             "search_chemical_potential", "vca_search_variable", "vca_read_impSigma", "observables_cluster"]
     for n in names:
         assert callable(getattr(solver, n)), n
     solver._solver = None

@@ -694,6 +694,12 @@ def vca_get_gimp_realaxis() -> np.ndarray:
     return _ctx().gimp_realaxis()
 
 
+def observables_cluster() -> dict:
+    """observables_cluster (VCA_OBSERVABLES.f90:70-74): dens, dens_up,
+    dens_dw, docc and mag of the last solve, each (Nlat,Norb)."""
+    return _ctx().observables()
+
+
 def vca_get_dens() -> np.ndarray:
     """vca_get_dens (VCA_IO/get_dens.f90): (Nlat,Norb)."""
     return _ctx().observables()["dens"]
