@@ -13,6 +13,11 @@ Contents:
                G'(i w) at t'=1 on 6 frequencies.
   small_models.npz  E_gs / Omega / G'(i w) of a spin-polarised 2x2 cluster,
                a 2x2+2 bath cluster and a BHZ 2x2 cluster (complex H).
+  mid_models.npz  larger sectors than the oracle runs inside the GPU tests:
+               the 3x3 AFM cluster (U=8, xmu=4, M=0.1, Nspin=2, sectors up to
+               15,876) at T=0 and at beta=10 (the finite-T list, zeta, Omega'
+               and the two parts of the Omega integral), and a 2x2 cluster
+               with 6 bath levels (sectors up to 63,504) at T=0.
 """
 import os
 import sys
@@ -77,7 +82,46 @@ def small_models():
     np.savez_compressed(os.path.join(OUT, "small_models.npz"), **out)
 
 
+def mid_points():
+    sq = clusters.square(nx=3, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=8, nky=8, ngfiter=100,
+                         omega_nodes=2048)
+    ft = clusters.square(nx=3, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=8, nky=8, ngfiter=80,
+                         omega_nodes=256)
+    c = ft.cfg.copy()
+    c.lanc_nstates_total, c.beta, c.bandwidth = 2, 10.0, 8.0
+    ft.cfg = c
+    bath = clusters.square_bath(nb=6, nk1=6, ngfiter=80, omega_nodes=1024)
+    return {"sq3x3": sq, "sq3x3_b10": ft, "bath6": bath}
+
+
+def mid_models():
+    out = {}
+    for name, pt in mid_points().items():
+        o = Oracle.from_point(pt)
+        a, b, c = o.solve()
+        check_energies(o)
+        out[name + "_sft"] = a
+        out[name + "_egs"] = b
+        out[name + "_omega_int"] = c
+        out[name + "_sector_e"] = o.sector_energies()
+        out[name + "_g"] = o.gf_cluster(1j * WG)
+        if pt.cfg.lanc_nstates_total != 1:
+            t = o.thermal()
+            out[name + "_states"] = np.array(sorted(s for s, _ in o.states()))
+            for key in ("zeta", "omega_prime", "max_exc", "sum_part", "contour_part"):
+                out[name + "_" + key] = t[key]
+            out[name + "_nmax"] = t["nmax"]
+    out["wg"] = WG
+    np.savez_compressed(os.path.join(OUT, "mid_models.npz"), **out)
+
+
 if __name__ == "__main__":
-    chain4()
-    small_models()
+    # optional arguments name the fixtures to write (chain4, small, mid); all by default
+    which = set(sys.argv[1:]) or {"chain4", "small", "mid"}
+    if "chain4" in which:
+        chain4()
+    if "small" in which:
+        small_models()
+    if "mid" in which:
+        mid_models()
     print("fixtures written to", OUT)

@@ -11,6 +11,7 @@ from vca_gb300 import clusters
 HERE = os.path.dirname(os.path.abspath(__file__))
 CH = np.load(os.path.join(HERE, "golden", "chain4.npz"))
 SM = np.load(os.path.join(HERE, "golden", "small_models.npz"))
+MM = np.load(os.path.join(HERE, "golden", "mid_models.npz"))
 
 
 def chain_point(tp):
@@ -24,6 +25,32 @@ def small_points():
         "bath": clusters.square_bath(nb=2, nk1=6, ngfiter=60, omega_nodes=1024),
         "bhz": clusters.bhz(mass=2.2, delta=0.1, nk1=4, ngfiter=60, omega_nodes=1024),
     }
+
+
+def mid_points():
+    """The points of mid_models.npz (as make_golden.mid_points)."""
+    sq = clusters.square(nx=3, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=8, nky=8, ngfiter=100,
+                         omega_nodes=2048)
+    ft = clusters.square(nx=3, ny=3, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=8, nky=8, ngfiter=80,
+                         omega_nodes=256)
+    c = ft.cfg.copy()
+    c.lanc_nstates_total, c.beta, c.bandwidth = 2, 10.0, 8.0
+    ft.cfg = c
+    bath = clusters.square_bath(nb=6, nk1=6, ngfiter=80, omega_nodes=1024)
+    return {"sq3x3": sq, "sq3x3_b10": ft, "bath6": bath}
+
+
+def _rel(a, b):
+    return abs(a - float(b)) / max(1.0, abs(float(b)))
+
+
+def test_oracle_reproduces_mid_fixture():
+    from oracle.oracle import Oracle
+    pt = mid_points()["sq3x3"]
+    o = Oracle.from_point(pt)
+    sft, egs, _ = o.solve()
+    assert _rel(sft, MM["sq3x3_sft"]) < 1e-12 and _rel(egs, MM["sq3x3_egs"]) < 1e-12
+    assert np.abs(o.gf_cluster(1j * MM["wg"]) - MM["sq3x3_g"]).max() < 1e-12
 
 
 @pytest.mark.parametrize("idx", [0, 10, 20])
@@ -65,3 +92,29 @@ def test_gpu_small_models_match_fixture(name):
     assert abs(om - SM[name + "_sft"]) <= 1e-10 * abs(SM[name + "_sft"])
     g = s.gf_cluster(1j * SM["wg"])
     assert np.abs(g - SM[name + "_g"]).max() < 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["sq3x3", "sq3x3_b10", "bath6"])
+def test_gpu_mid_models_match_fixture(name):
+    """Sectors larger than the oracle runs inside these tests: the 3x3 AFM
+    cluster (up to 15,876 states; fixed point) at T=0 and at beta=10, and
+    the 2x2 cluster with 6 bath levels (up to 63,504 states; FP64).  Every
+    listed sector's lowest level is simple (gaps >= 0.22), so G' is a parity
+    quantity too."""
+    from vca_gb300.solver import VcaSolver
+    pt = mid_points()[name]
+    s = VcaSolver(pt.cfg, pt.bath_h, pt.bath_v)
+    om = s.solve(pt.Hloc, pt.Hk, pt.bath_h, pt.bath_v)
+    egs, _ = s.energies()
+    assert _rel(egs, MM[name + "_egs"]) < 1e-10
+    assert _rel(om, MM[name + "_sft"]) < 1e-10, (om, float(MM[name + "_sft"]))
+    np.testing.assert_allclose(s.sector_energies(), MM[name + "_sector_e"], rtol=1e-10, atol=1e-10)
+    assert np.abs(s.gf_cluster(1j * MM["wg"]) - MM[name + "_g"]).max() < 1e-8
+    if name + "_states" in MM:
+        t = s.thermal()
+        assert sorted(x for x, _ in s.states()) == MM[name + "_states"].tolist()
+        for key in ("zeta", "omega_prime", "max_exc", "sum_part", "contour_part"):
+            assert _rel(t[key], MM[name + "_" + key]) < 1e-10, key
+        assert t["nmax"] == int(MM[name + "_nmax"])
+    s.close()
