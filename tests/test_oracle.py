@@ -416,3 +416,53 @@ def test_oracle_is_deterministic_across_thread_counts():
         out.append((sft, egs, oi, e, it, psi.tobytes(), o.sum_kmesh_complex(0.7 + 0.2j)))
     orc.set_threads(n0)
     assert out[0] == out[1]
+
+
+@pytest.mark.parametrize("hfmode", [0, 1])
+def test_local_term_three_orbitals_matches_the_reference_formula(hfmode):
+    """The diagonal of H (stored/H_cluster_local.f90) restated element by
+    element in numpy for 2 sites x 3 orbitals, both spins with different
+    orbital energies, Uloc per orbital, Ust, Jh and the HFMODE shifts."""
+    from vca_gb300.config import default_config
+    from vca_gb300.clusters import _zeros
+    rng = np.random.default_rng(17 + hfmode)
+    Nlat, Norb, Nspin = 2, 3, 2
+    U = [3.0, 2.5, 2.0]
+    Ust, Jh, xmu = 1.4, 0.35, 0.8
+    cfg = default_config(Nlat=Nlat, Norb=Norb, Nspin=Nspin, Uloc=U, Ust=Ust, Jh=Jh, xmu=xmu,
+                         hfmode=hfmode, lanc_method=1, lanc_nstates_total=1)
+    Hloc = _zeros(Nlat, Nlat, Nspin, Nspin, Norb, Norb)
+    eps = rng.normal(size=(Nlat, Nspin, Norb))
+    for il in range(Nlat):
+        for s in range(Nspin):
+            for io in range(Norb):
+                Hloc[il, il, s, s, io, io] = eps[il, s, io]
+    Hk = np.asfortranarray(Hloc[..., None].copy())
+    o = Oracle(cfg, Hloc, Hk)
+    checked = 0
+    for isec in range(1, o.Nsectors + 1):
+        nu, nd, du, dd = o.sector_info(isec)
+        if du * dd > 400:
+            continue
+        mu_, md_ = o.sector_map(isec, 1), o.sector_map(isec, 2)
+        ref = np.zeros(du * dd)
+        for i in range(du * dd):
+            wu, wd = int(mu_[i % du]), int(md_[i // du])
+            n = lambda w, il, io: float((w >> (io + il * Norb)) & 1)
+            h = 0.0
+            for il in range(Nlat):
+                for io in range(Norb):
+                    up, dw = n(wu, il, io), n(wd, il, io)
+                    h += eps[il, 0, io] * up + eps[il, 1, io] * dw - xmu * (up + dw) + U[io] * up * dw
+                    if hfmode:
+                        h += -0.5 * U[io] * (up + dw) + 0.25 * U[io]
+                    for jo in range(io + 1, Norb):
+                        uj, dj = n(wu, il, jo), n(wd, il, jo)
+                        h += Ust * (up * dj + uj * dw) + (Ust - Jh) * (up * uj + dw * dj)
+                        if hfmode:
+                            tot = up + dw + uj + dj
+                            h += -0.5 * Ust * tot + 0.25 * Ust - 0.5 * (Ust - Jh) * tot + 0.25 * (Ust - Jh)
+            ref[i] = h
+        np.testing.assert_allclose(o.diag_elements(isec), ref, rtol=0, atol=1e-13)
+        checked += 1
+    assert checked > 20
