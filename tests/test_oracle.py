@@ -466,3 +466,50 @@ def test_local_term_three_orbitals_matches_the_reference_formula(hfmode):
         np.testing.assert_allclose(o.diag_elements(isec), ref, rtol=0, atol=1e-13)
         checked += 1
     assert checked > 20
+
+
+@pytest.mark.parametrize("hfshift", [0, 1])
+def test_local_term_with_bath_levels_and_the_hartree_shift(hfshift):
+    """Bath levels in the diagonal (diag_hybr_bath.f90:6-10, HxV_local.f90:
+    80-88): bath_h(l,l,s,s,o,o) on the bit Nlat*Norb + l*Norb_bath + o
+    (getBathStride, VCA_SETUP.f90:341-349), minus xmu, with HFMODE and without
+    HFSHIFT shifted by -(Uloc(o)/2 + Ust(Norb-1)/2 + (Ust-Jh)(Norb-1)/2)
+    (vca_set_bath, VCA_BATH_SETUP.f90:127-134), Uloc indexed by the bath
+    orbital as the reference does."""
+    from vca_gb300.config import default_config
+    from vca_gb300.clusters import _zeros
+    rng = np.random.default_rng(5 + hfshift)
+    Nlat, Norb, Nspin, Nlb, Nob = 2, 1, 2, 3, 1
+    U, xmu = [3.0, 0.0, 0.0, 0.0, 0.0], 1.1
+    cfg = default_config(Nlat=Nlat, Norb=Norb, Nspin=Nspin, Nlat_bath=Nlb, Norb_bath=Nob, Uloc=U, xmu=xmu,
+                         hfmode=1, hfshift=hfshift, lanc_method=1, lanc_nstates_total=1)
+    Hloc = _zeros(Nlat, Nlat, Nspin, Nspin, Norb, Norb)
+    Hk = np.asfortranarray(Hloc[..., None].copy())
+    bh = _zeros(Nlb, Nlb, Nspin, Nspin, Nob, Nob)
+    A = rng.normal(size=(Nlb, Nlb))
+    for s in range(Nspin):
+        bh[:, :, s, s, 0, 0] = A + A.T + s * np.diag(rng.normal(size=Nlb))
+    bv = np.asfortranarray(rng.uniform(-0.5, 0.5, size=(Nlat, Nlb, Nspin, Nspin, Norb, Nob)).astype(complex))
+    for s1 in range(Nspin):
+        for s2 in range(Nspin):
+            if s1 != s2:
+                bv[:, :, s1, s2] = 0.0
+    o = Oracle(cfg, Hloc, Hk, bh, bv)
+    shift = 0.0 if hfshift else 0.5 * U[0]
+    for isec in range(1, o.Nsectors + 1):
+        nu, nd, du, dd = o.sector_info(isec)
+        mu_, md_ = o.sector_map(isec, 1), o.sector_map(isec, 2)
+        ref = np.zeros(du * dd)
+        for i in range(du * dd):
+            wu, wd = int(mu_[i % du]), int(md_[i // du])
+            h = 0.0
+            for il in range(Nlat):
+                up, dw = (wu >> il) & 1, (wd >> il) & 1
+                h += -xmu * (up + dw) + U[0] * up * dw - 0.5 * U[0] * (up + dw) + 0.25 * U[0]
+            for lb in range(Nlb):
+                b = Nlat * Norb + lb * Nob
+                up, dw = (wu >> b) & 1, (wd >> b) & 1
+                h += (bh[lb, lb, 0, 0, 0, 0].real - shift) * up + (bh[lb, lb, 1, 1, 0, 0].real - shift) * dw
+                h -= xmu * (up + dw)
+            ref[i] = h
+        np.testing.assert_allclose(o.diag_elements(isec), ref, rtol=0, atol=1e-13)
