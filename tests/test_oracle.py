@@ -513,3 +513,30 @@ def test_local_term_with_bath_levels_and_the_hartree_shift(hfshift):
                 h -= xmu * (up + dw)
             ref[i] = h
         np.testing.assert_allclose(o.diag_elements(isec), ref, rtol=0, atol=1e-13)
+
+
+def test_delta_bath_is_the_reference_formula():
+    """Delta(x) = V ((x + xmu) - h)^-1 V^dag in lso layout
+    (delta_bath_freq_main, VCA_BATH_FUNCTIONS.f90:127-150), written with the
+    reshapes of VCA_AUX_FUNX (the Python mirror's, themselves checked against
+    the reference's index loops) and numpy's inverse; the bath as
+    vca_set_bath leaves it, shifted under HFMODE without HFSHIFT."""
+    from vca_gb300.reshape import vca_nnn2lso_reshape, vca_rectangular_n2j_reshape
+    for hf in (0, 1):
+        pt = clusters.square_bath(nb=4, nk1=3, ngfiter=20, omega_nodes=64, seed=13)
+        c = pt.cfg.copy()
+        c.hfmode, c.hfshift = hf, 0
+        pt.cfg = c
+        o = Oracle.from_point(pt)
+        h = np.array(pt.bath_h, dtype=complex)
+        if hf:
+            for lb in range(c.Nlat_bath):
+                for ob in range(c.Norb_bath):
+                    for s in range(c.Nspin):
+                        h[lb, lb, s, s, ob, ob] -= (0.5 * c.Uloc[ob] + 0.5 * c.Ust * (c.Norb - 1)
+                                                    + 0.5 * (c.Ust - c.Jh) * (c.Norb - 1))
+        hl = vca_nnn2lso_reshape(h, c.Nlat_bath, c.Nspin, c.Norb_bath)
+        V = vca_rectangular_n2j_reshape(pt.bath_v, c.Nlat, c.Nlat_bath, c.Nspin, c.Nspin, c.Norb, c.Norb_bath)
+        for x in (0.4j, 1.5 + 0.2j, -3.0 + 1.0j):
+            ref = V @ np.linalg.inv((x + c.xmu) * np.eye(len(hl)) - hl) @ V.conj().T
+            np.testing.assert_allclose(o.delta_bath(x), ref, rtol=0, atol=1e-13)
