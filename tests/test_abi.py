@@ -102,24 +102,26 @@ def test_module_names_of_the_reference(lib):
         assert e.value.code == -3
 
 
-def test_config_layout_matches_the_c_header(tmp_path):
-    """sizeof(vca_config) and every field offset as a C compiler lays out
-    include/vca_gpu.h equal the Python mirror's ctypes layout; the header is
-    also plain C99."""
+@pytest.mark.parametrize("cname", ["vca_config", "vca_thermal"])
+def test_config_layout_matches_the_c_header(tmp_path, cname):
+    """sizeof and every field offset of the C-ABI structs as a C compiler lays
+    out include/vca_gpu.h equal the Python mirror's ctypes layouts; the
+    header is also plain C99."""
     import shutil
     import subprocess
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    names = [n for n, _ in VcaConfig._fields_]
+    S = VcaConfig if cname == "vca_config" else solver.VcaThermal
+    names = [n for n, _ in S._fields_]
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "vca_gpu.h"', "int main(void) {",
-           '  printf("%zu\\n", sizeof(vca_config));']
-    src += [f'  printf("%zu\\n", offsetof(vca_config, {n}));' for n in names]
+           f'  printf("%zu\\n", sizeof({cname}));']
+    src += [f'  printf("%zu\\n", offsetof({cname}, {n}));' for n in names]
     src += ["  return 0;", "}"]
     (tmp_path / "layout.c").write_text("\n".join(src) + "\n")
     exe = tmp_path / "layout"
     subprocess.check_call([cc, "-std=c99", "-Wall", "-I", os.path.join(ROOT, "include"), str(tmp_path / "layout.c"),
                            "-o", str(exe)])
     got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
-    assert got[0] == ctypes.sizeof(VcaConfig)
-    assert got[1:] == [getattr(VcaConfig, n).offset for n in names]
+    assert got[0] == ctypes.sizeof(S)
+    assert got[1:] == [getattr(S, n).offset for n in names]
