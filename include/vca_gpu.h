@@ -417,9 +417,10 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
  * allocator mid-run): the partial sums behind alpha live in a static 8 MiB
  * device array, so the call allocates nothing.  Batches whose partial sums
  * exceed 8 MiB are rejected with VCA_ERR_ARG.  The first call on a device
- * looks the array up (make it before any stream capture); all calls share
- * the array, so calls whose work overlaps on the GPU race.  No counterpart in
- * the reference. */
+ * looks the array up (make it before any stream capture); the address is
+ * kept until vca_gpu_finalize, so after a device reset finalize and init
+ * again.  All calls share the array, so calls whose work overlaps on the GPU
+ * race.  No counterpart in the reference. */
 int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void* d_hv, int32_t ncols,
                               double* d_alpha);
 
@@ -448,6 +449,13 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
 int vca_gpu_sector_row_order(int32_t isector, int64_t* order, int64_t cap);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);
+/* QL sweeps allowed per eigenvalue when the chains' tridiagonals are turned
+ * into poles and weights (default 60).
+ * A chain that needs more makes the call that asked for poles (the channel
+ * getter, the finite-T max_exc, save_gfprime) return VCA_ERR_NUMERIC instead
+ * of poles from an unfinished QL.  No counterpart in the reference (SciFortran's
+ * eigh stops the process); lowering it makes the failure path testable. */
+int vca_gpu_set_ql_max_iter(int32_t max_iter);
 /* CUDA events on the library stream: device time between start and stop. */
 int vca_gpu_timer_start(void);
 int vca_gpu_timer_stop(double* ms);

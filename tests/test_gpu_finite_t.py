@@ -2,11 +2,20 @@
 through the C-ABI against the CPU oracle.
 
 Compared: the annealed state list (the same sectors, energies 1e-10
-relative), zeta / Omega' / max_exc (1e-10 relative), nmax, the contour
-radius and node count (exact), the Matsubara and contour parts and the SFT
-potential (1e-10 relative), the complex integrand on the contour (1e-10),
-G'(z) (1e-8 absolute) and the Boltzmann-weighted observables (1e-10), plus
-the carry-over of the adapted LANC_NSTATES_TOTAL into the next solve.
+relative), zeta / Omega' (1e-10 relative), nmax, the contour radius and node
+count (exact), the Matsubara and contour parts and the SFT potential (1e-10
+relative), the complex integrand on the contour (1e-10), G'(z) (1e-8
+absolute) and the Boltzmann-weighted observables (1e-10), plus the
+carry-over of the adapted LANC_NSTATES_TOTAL into the next solve.
+
+max_exc is the largest Ritz value of chains run without reorthogonalisation
+from ground-state vectors that meet a 1e-11 residual, so it is set by
+rounding: the oracle alone moves it by 1.9e-7 relative across Lanczos start
+seeds on bhz_b10 (tests/test_oracle_finite_t.py measures this).  It enters
+Omega only through nmax = int(2(|max_exc| + bandwidth) beta / pi) and the
+radius R = 2 (nmax + 1) pi / beta, which are compared exactly; max_exc itself
+is compared at MAX_EXC_TOL, and every model keeps the nmax argument further
+than that tolerance from an integer, so that the exact comparison is sound.
 """
 import numpy as np
 import pytest
@@ -20,6 +29,7 @@ pytestmark = pytest.mark.gpu
 
 E_TOL = 1e-10
 G_TOL = 1e-8
+MAX_EXC_TOL = 1e-6
 
 
 def _ft(pt, beta, bandwidth, nstates=2, **kw):
@@ -75,6 +85,15 @@ def _rel(a, b):
     return abs(a - b) / max(1.0, abs(b))
 
 
+def _assert_nmax_away_from_edge(cfg, max_exc):
+    """nmax is compared exactly only where a max_exc error of MAX_EXC_TOL
+    cannot move the integer part of its argument."""
+    x = 2.0 * (abs(max_exc) + cfg.bandwidth) * cfg.beta / np.pi
+    dx = 2.0 * MAX_EXC_TOL * max(1.0, abs(max_exc)) * cfg.beta / np.pi
+    edge = min(x - np.floor(x), np.ceil(x) - x)
+    assert edge > 10 * dx, f"nmax argument {x} within {edge:.2e} of an integer: choose another model"
+
+
 @pytest.mark.parametrize("name", list(POINTS))
 def test_finite_t_solve_matches_oracle(name):
     pt = POINTS[name]()
@@ -91,8 +110,10 @@ def test_finite_t_solve_matches_oracle(name):
             assert _rel(e, er) < E_TOL
         t, tr = s.thermal(), o.thermal()
         assert t["finite_t"] == 1 and t["nstates_total"] == tr["nstates_total"]
-        for key in ("zeta", "omega_prime", "e_min", "max_exc", "sum_part", "contour_part"):
+        for key in ("zeta", "omega_prime", "e_min", "sum_part", "contour_part"):
             assert _rel(t[key], tr[key]) < E_TOL, (rep, key, t[key], tr[key])
+        assert _rel(t["max_exc"], tr["max_exc"]) < MAX_EXC_TOL, (rep, t["max_exc"], tr["max_exc"])
+        _assert_nmax_away_from_edge(pt.cfg, tr["max_exc"])
         assert t["nmax"] == tr["nmax"] and t["contour_points"] == tr["contour_points"]
         assert t["integration_R"] == tr["integration_R"]
         assert _rel(sft, sft_ref) < E_TOL, (rep, sft, sft_ref)

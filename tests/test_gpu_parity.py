@@ -180,6 +180,25 @@ def test_gf_channel_poles_match_oracle():
     assert np.abs(g - tot).max() < 1e-10
 
 
+def test_unconverged_ql_is_reported_not_returned():
+    """With the QL cap forced to one sweep per eigenvalue the 80-step chains
+    cannot converge: the pole request must fail with VCA_ERR_NUMERIC (-7)
+    rather than return poles of an unfinished QL.  Restoring the default cap
+    gives the poles back, equal to a fresh context's."""
+    pt = POINTS["square2x2_afm"]()
+    s = VcaSolver(pt.cfg)
+    s.solve(pt.Hloc, pt.Hk)
+    p0, w0 = s.gf_channel(1, 1, 1, 1, 1, 1, 1)
+    s.set_ql_max_iter(1)
+    with pytest.raises(VcaError) as ei:
+        s.gf_channel(1, 1, 1, 1, 1, 1, 1)
+    assert ei.value.code == -7 and "did not converge" in str(ei.value)
+    s.set_ql_max_iter(60)
+    p1, w1 = s.gf_channel(1, 1, 1, 1, 1, 1, 1)
+    np.testing.assert_array_equal(p1, p0)
+    np.testing.assert_array_equal(w1, w0)
+
+
 @pytest.mark.parametrize("name", list(POINTS))
 def test_sigma_and_g0_grids_match_oracle(name):
     """vca_get_sigma_matsubara/_realaxis and the G0 grids (build_sigma_normal)

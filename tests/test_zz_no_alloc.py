@@ -1,6 +1,6 @@
 """The allocation-free column H x v (vca_gpu_hxv_alpha_noalloc) through the
 C-ABI against the existing entry point (vca_gpu_hxv_timed, one repetition)
-on the same columns, two calls in a row: Y must equal the existing entry
+on the same columns, three calls in a row: Y must equal the existing entry
 point's Y (same kernels), and alpha[c] must equal <x_c, y_c> of the existing
 entry point's output -- exactly summed in the fixed-point path (1e-14
 relative after the conversion to double), 1e-13 relative in FP64.
@@ -21,11 +21,12 @@ NS = 9
 ISEC = 1 + 4 + 5 * (NS + 1)  # sector (5 up, 4 down) of the 3x3 cluster: 126 x 126
 
 
-def _solver(arith):
+def _solver(arith, variant=0):
     pt = clusters.square(nx=3, ny=3, U=8.0, xmu=4.0, maf=0.2, nspin=2, nkx=4, nky=4, ngfiter=40,
                          omega_nodes=64)
     cfg = pt.cfg.copy()
     cfg.arith = arith
+    cfg.hxv_variant = variant
     s = VcaSolver(cfg)
     s.set_hamiltonian(pt.Hloc)
     return s
@@ -51,11 +52,17 @@ def _rows(flat, D, m, fx):
     return flat.reshape(D, m)
 
 
-@pytest.mark.parametrize("m", [8, 40])
-@pytest.mark.parametrize("arith", [2, 1], ids=["fx", "fp64"])
-def test_noalloc_matches_existing_entry_point(arith, m):
+@pytest.mark.parametrize("arith,m,variant", [(2, 8, 0), (2, 40, 0), (2, 40, 1), (2, 40, 2),
+                                             (1, 8, 0), (1, 40, 0)],
+                         ids=["fx-m8", "fx-m40", "fx-m40-warp", "fx-m40-rowperm", "fp64-m8", "fp64-m40"])
+def test_noalloc_matches_existing_entry_point(arith, m, variant):
+    """hxv_variant 1 (warp kernel) and 2 (row-permuted kernel) size and fill
+    the partial-sum rows differently from the default staged kernel, so each
+    is compared with the existing entry point.  Free device memory and
+    torch's allocated bytes are recorded after a first call and must be
+    unchanged by the next ones: the entry point allocates nothing."""
     import torch
-    s = _solver(arith)
+    s = _solver(arith, variant)
     fx, F, G = s.arith_info()
     assert fx == (arith == 2)
     flat, D = _columns(s, m, seed=17 + m)
@@ -73,11 +80,19 @@ def test_noalloc_matches_existing_entry_point(arith, m):
     else:
         aref = (X * Yr).sum(axis=0)
         rtol = 1e-13
-    for call in range(2):
-        dY = torch.full_like(dX, 7)
-        dA = torch.full((m,), np.nan, dtype=torch.float64, device="cuda")
+    dY = torch.full_like(dX, 7)
+    dA = torch.full((m,), np.nan, dtype=torch.float64, device="cuda")
+    mem = None
+    for call in range(3):
+        dY.fill_(7)
+        dA.fill_(float("nan"))
+        torch.cuda.synchronize()
+        if call == 1:  # after the first call has looked up the scratch address
+            mem = (torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated())
         s.hxv_alpha_noalloc(ISEC, dX.data_ptr(), dY.data_ptr(), m, dA.data_ptr())
         s.synchronize()
+        if call >= 1:
+            assert (torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()) == mem
         np.testing.assert_array_equal(dY.cpu().numpy(), Yref)
         np.testing.assert_allclose(dA.cpu().numpy(), aref, rtol=rtol, atol=0.0)
 

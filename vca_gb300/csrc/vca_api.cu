@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <ctime>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -146,6 +147,7 @@ struct Ctx {
   double2* d_weights = nullptr;
   int* d_nexc = nullptr;
   bool poles_ready = false;
+  int ql_max_iter = 60;  // QL sweeps per eigenvalue before a chain is reported unconverged
   ChainStore cstore{};
   int nelem = 0;
   int* d_elem_ptr = nullptr;
@@ -1357,12 +1359,19 @@ int ensure_poles() {
   if (g->poles_ready || g->chains.empty()) return VCA_OK;
   Arena ar;
   double* work;
+  int* d_fail;
   const int nch = (int)g->chains.size();
   RCHK(ar.alloc(&work, (size_t)nch * 3 * g->ld));
-  launch_chain_poles(nch, g->cstore, work, g->d_poles, g->d_weights, g->d_nexc, g->st);
-  cudaError_t err = cudaStreamSynchronize(g->st);
+  RCHK(ar.alloc(&d_fail, 1));
+  CUCHK(cudaMemsetAsync(d_fail, 0, sizeof(int), g->st));
+  launch_chain_poles(nch, g->cstore, work, g->d_poles, g->d_weights, g->d_nexc, g->ql_max_iter, d_fail, g->st);
+  int nfail = 0;
+  cudaError_t err = cudaMemcpyAsync(&nfail, d_fail, sizeof(int), cudaMemcpyDeviceToHost, g->st);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(g->st);
   ar.release();
   CUCHK(err);
+  if (nfail > 0)
+    VFAIL(VCA_ERR_NUMERIC, "tridiagonal QL of " + std::to_string(nfail) + " Green's function chain(s) did not converge");
   g->poles_ready = true;
   return VCA_OK;
 }
@@ -2066,6 +2075,10 @@ static void gfm_drop() {
 // ===========================================================================
 // C-ABI
 // ===========================================================================
+// Forgets the cached device addresses of the allocation-free entry point's
+// static scratch (defined at the end of this file).
+static void noalloc_forget();
+
 extern "C" {
 
 void vca_config_defaults(vca_config* c) {
@@ -2125,6 +2138,7 @@ int vca_gpu_last_error(char* buf, int32_t len) {
 }
 
 int vca_gpu_finalize(void) {
+  noalloc_forget();
   if (!g) return VCA_OK;
   gfm_drop();
   g->work.release();
@@ -3001,6 +3015,14 @@ int vca_gpu_synchronize(void) {
   return VCA_OK;
 }
 
+int vca_gpu_set_ql_max_iter(int32_t max_iter) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (max_iter < 1) VFAIL(VCA_ERR_ARG, "max_iter must be >= 1");
+  g->ql_max_iter = max_iter;
+  g->poles_ready = false;  // the next pole request reruns the QL under the new cap
+  return VCA_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -3016,19 +3038,29 @@ int vca_gpu_synchronize(void) {
 //
 // The array's device address is looked up once per device, by the first call
 // made while that device is current; make that first call before any stream
-// capture.  Every call on a device shares the array and the array keeps the
-// last call's contents: each partial is overwritten before it is read, so
-// nothing needs clearing, but calls whose work overlaps on the GPU race.
+// capture.  The address is cached only as long as the CUDA context: a
+// vca_gpu_finalize forgets it, so a caller that resets the device (or makes a
+// new primary context) must finalize and init again before the next call.
+// Every call on a device shares the array and the array keeps the last call's
+// contents: each partial is overwritten before it is read, so nothing needs
+// clearing, but calls whose work overlaps on the GPU race.
 // ---------------------------------------------------------------------------
 #define VCA_NOALLOC_SCRATCH_BYTES (8u << 20)
 #define VCA_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) unsigned char g_noalloc_scratch[VCA_NOALLOC_SCRATCH_BYTES];
 static void* g_noalloc_addr[VCA_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+static void noalloc_forget() {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  for (auto& a : g_noalloc_addr) a = nullptr;
+}
 
 static int noalloc_scratch(void** out) {
   int dev = 0;
   CUCHK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= VCA_NOALLOC_MAX_DEVICES) VFAIL(VCA_ERR_CUDA, "device ordinal beyond the scratch table");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_addr[dev]) {
     void* p = nullptr;
     CUCHK(cudaGetSymbolAddress(&p, g_noalloc_scratch));

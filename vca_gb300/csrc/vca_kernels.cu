@@ -520,9 +520,11 @@ void launch_chain_store(int nch, const ChainMeta* meta, const double* A, const d
 // Chain tridiagonal -> poles and weights.  Implicit QL with Wilkinson shift
 // (EISPACK tql2; the reference calls SciFortran eigh(d,e,Ev=Z) at
 // VCA_GF_NORMAL.f90:1012) tracking only the first row of Z.  One thread per
-// chain, one warp per block; work = 3*ld doubles per chain.
+// chain, one warp per block; work = 3*ld doubles per chain.  A chain whose
+// QL needs more than max_iter sweeps for one eigenvalue is counted in *fail
+// (its poles are then not to be used: the host turns the count into an error).
 __global__ void k_chain_poles(int nch, ChainStore cs, double* work, double* poles, double2* weights,
-                              int* nexc) {
+                              int* nexc, int max_iter, int* fail) {
   const int ldab = cs.ld;
   for (int ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nch; ch += gridDim.x * blockDim.x) {
     const int n = cs.n[ch];
@@ -538,6 +540,7 @@ __global__ void k_chain_poles(int nch, ChainStore cs, double* work, double* pole
     }
     double f = 0.0, tst1 = 0.0;
     const double eps = 2.220446049250313e-16;
+    bool failed = false;
     for (int l = 0; l < n; l++) {
       int iter = 0;
       double h = fabs(d[l]) + fabs(e[l]);
@@ -546,7 +549,7 @@ __global__ void k_chain_poles(int nch, ChainStore cs, double* work, double* pole
       while (m < n - 1 && fabs(e[m]) > eps * tst1) m++;
       if (m > l) {
         do {
-          if (++iter > 60) break;
+          if (++iter > max_iter) { failed = true; break; }
           double g = d[l];
           double p = (d[l + 1] - g) / (2.0 * e[l]);
           double r = hypot(p, 1.0);
@@ -583,6 +586,7 @@ __global__ void k_chain_poles(int nch, ChainStore cs, double* work, double* pole
       d[l] += f;
       e[l] = 0.0;
     }
+    if (failed) atomicAdd(fail, 1);
     for (int ii = 1; ii < n; ii++) {  // ascending, as tql2
       int i = ii - 1, kk = i;
       double p = d[i];
@@ -607,10 +611,10 @@ __global__ void k_chain_poles(int nch, ChainStore cs, double* work, double* pole
   }
 }
 void launch_chain_poles(int nch, const ChainStore& cs, double* work, double* poles, double2* weights, int* nexc,
-                        cudaStream_t st) {
+                        int max_iter, int* fail, cudaStream_t st) {
   if (nch <= 0) return;
   COUNT_LAUNCH();
-  k_chain_poles<<<nblocks(nch, 32), 32, 0, st>>>(nch, cs, work, poles, weights, nexc);
+  k_chain_poles<<<nblocks(nch, 32), 32, 0, st>>>(nch, cs, work, poles, weights, nexc, max_iter, fail);
 }
 
 // ---------------------------------------------------------------------------

@@ -96,9 +96,10 @@ void launch_chain_store(int nch, const ChainMeta* meta, const double* A, const d
                         const double* norm2, const double2* wfac, const int* isign, double Ei, double boltz,
                         double zeta, const ChainStore& cs, int base, cudaStream_t st);
 // stored chains -> poles/weights (add_to_lanczos_gf_normal, VCA_GF_NORMAL.f90:970-1033);
-// work: 3*ld doubles per chain
+// work: 3*ld doubles per chain; *fail counts chains whose QL needed more
+// than max_iter sweeps for one eigenvalue
 void launch_chain_poles(int nch, const ChainStore& cs, double* work, double* poles, double2* weights, int* nexc,
-                        cudaStream_t st);
+                        int max_iter, int* fail, cudaStream_t st);
 
 // ---- chain initial vectors (VCA_GF_NORMAL.f90:179-197, :251-268, :608-646) -
 struct OpTerm {
