@@ -18,6 +18,18 @@ Contents:
                15,876) at T=0 and at beta=10 (the finite-T list, zeta, Omega'
                and the two parts of the Omega integral), and a 2x2 cluster
                with 6 bath levels (sectors up to 63,504) at T=0.
+  config_<name>.npz  one point of each full-size workload, at exactly the
+               sizes the benchmark and the batched form run (minutes to an
+               hour of oracle time each on a multi-core host):
+               c2_m00 / c2_m05: the 4x3 cluster (U=8, xmu=4, Nspin=2, 32x32 k,
+               200-step chains, 8192 nodes) at M = 0 and M = 0.1 (sweep
+               points 0 and 5 of linspace(0, 0.3, 16));
+               c3_p0: the first point of the 2x2 + 8 bath batch (24x24 k,
+               200-step chains, 4096 nodes);
+               c4_p0: the first point of the BHZ batch (48x48 k, 200-step
+               chains, 4096 nodes).
+               Each holds E_gs, the Omega integral, the SFT potential, every
+               sector energy and G'(i w) at the WG frequencies.
 """
 import os
 import sys
@@ -115,9 +127,39 @@ def mid_models():
     np.savez_compressed(os.path.join(OUT, "mid_models.npz"), **out)
 
 
+def config_points():
+    """The full-size points, built exactly as bench.py builds its workloads."""
+    ms = np.linspace(0.0, 0.3, 16)
+    c2 = {f"c2_m{i:02d}": clusters.square(nx=4, ny=3, U=8.0, xmu=4.0, maf=float(ms[i]), nspin=2, nkx=32,
+                                           nky=32, ngfiter=200, omega_nodes=8192) for i in (0, 5)}
+    return {
+        "c4_p0": clusters.batch_bhz(B=1)[0],
+        "c3_p0": clusters.batch_square_bath(B=1)[0],
+        **c2,
+    }
+
+
+def config_models(names=None):
+    for name, pt in config_points().items():
+        if names and name not in names:
+            continue
+        o = Oracle.from_point(pt)
+        a, b, c = o.solve()
+        out = {"sft": a, "egs": b, "omega_int": c, "sector_e": o.sector_energies(),
+               "g": o.gf_cluster(1j * WG), "wg": WG,
+               "states": np.array(sorted(s for s, _ in o.states()))}
+        np.savez_compressed(os.path.join(OUT, f"config_{name}.npz"), **out)
+        print(name, "written", flush=True)
+
+
 if __name__ == "__main__":
-    # optional arguments name the fixtures to write (chain4, small, mid); all by default
-    which = set(sys.argv[1:]) or {"chain4", "small", "mid"}
+    # optional arguments name the fixtures to write (chain4, small, mid, configs
+    # or one config point such as c3_p0); chain4, small and mid by default
+    args = set(sys.argv[1:])
+    if args & set(config_points()) or "configs" in args:
+        config_models(None if "configs" in args else args & set(config_points()))
+        sys.exit(0)
+    which = args or {"chain4", "small", "mid"}
     if "chain4" in which:
         chain4()
     if "small" in which:

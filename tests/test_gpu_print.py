@@ -105,5 +105,5 @@ def test_read_impsigma_gives_the_printed_sigma_back(tmp_path, monkeypatch):
     assert np.abs(r.sigma_matsubara() - sm).max() < 1e-12
     r.close()
     with pytest.raises(VcaError) as e:
-        VcaSolver(_point(file_suffix=b"_none")).read_impSigma()
+        VcaSolver(_point(file_suffix=b"_none").cfg).read_impSigma()
     assert e.value.code == -10
