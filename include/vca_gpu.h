@@ -460,6 +460,56 @@ int vca_gpu_set_ql_max_iter(int32_t max_iter);
 int vca_gpu_timer_start(void);
 int vca_gpu_timer_stop(double* ms);
 
+/* ---- the Omega surrogate (no counterpart in the reference) -------------- */
+/*
+ * A 4 -> 128 -> 128 -> 128 -> 1 SiLU network fitted on the GPU to Omega
+ * values and gradients that the solver produces (loss per sample
+ * (f - y)^2 + grad_weight * |grad f - dy|^2, averaged), with BF16 tensor-core
+ * GEMMs and FP32 master weights, trained by Adam.  It proposes candidates for
+ * the stationary-point search that the reference's drivers run with brent or
+ * fmin_bfgs (drivers/vca_hm_chain1d.f90:104-108, drivers/vca_bhz_2d.f90:
+ * 244-305); each accepted candidate is re-solved by vca_gpu_solve.  Inputs
+ * and targets are expected already scaled to O(1).  One global network, not
+ * thread-safe, like the solver context.
+ */
+typedef struct vca_mlp_config {
+  int32_t n_in;          /* network inputs, 1..4                              */
+  int32_t capacity;      /* most training samples / prediction points         */
+  uint64_t seed;         /* Glorot-uniform initial weights                    */
+  double lr;             /* Adam step size                                    */
+  double beta1, beta2, adam_eps;
+  double grad_weight;    /* weight of the gradient term of the loss           */
+  double weight_decay;   /* decoupled weight decay on the weights (not biases) */
+} vca_mlp_config;
+void vca_mlp_config_defaults(vca_mlp_config* cfg);
+int vca_mlp_init(const vca_mlp_config* cfg);
+int vca_mlp_finalize(void);
+/* Flat FP32 parameters: W1[128][n_in], b1[128], W2[128][128], b2[128],
+ * W3[128][128], b3[128], w4[128], b4 (W[out][in], row-major). */
+int64_t vca_mlp_param_count(void);
+int vca_mlp_get_params(float* out, int64_t n);
+int vca_mlp_set_params(const float* in, int64_t n); /* also resets Adam */
+/* Training set: x[n][n_in], y[n], dy[n][n_in] (dy NULL: zero targets, use
+ * grad_weight = 0 for a value-only fit). */
+int vca_mlp_set_data(int32_t n, const double* x, const double* y, const double* dy);
+/* Loss and its gradient with respect to every parameter at the current
+ * weights (no update): the check against the CPU restatement. */
+int vca_mlp_loss_grad(double* loss, float* grad, int64_t n);
+/* `steps` full-batch Adam steps (one step is a replayed CUDA graph); *loss =
+ * the loss at the final weights.  VCA_ERR_TIMEOUT if a bounded tensor-core
+ * wait ran out. */
+int vca_mlp_train(int32_t steps, double* loss);
+/* f[n] and, when df is not NULL, the input gradients df[n][n_in]. */
+int vca_mlp_predict(int32_t n, const double* x, double* f, double* df);
+/* Test hook of the tensor-core GEMM: C[M][128] (+)= A[M][K] B[128][K]^T with
+ * A, B row-major bf16 bit patterns, M a multiple of 128, K of 64. */
+int vca_umma_gemm_check(const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t K,
+                        int32_t accumulate);
+/* Test hook of the GEMM's bounded waits: a 128 x 64 GEMM whose load barrier
+ * expects bytes that never arrive.  Returns VCA_ERR_TIMEOUT after about a
+ * second, with the CUDA context still usable. */
+int vca_umma_timeout_check(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2072,6 +2072,11 @@ static void gfm_drop() {
 
 }  // namespace
 
+namespace vca {
+// error text of the last failed call of any entry point (vca_gpu_last_error)
+void set_api_error(const std::string& m) { g_err = m; }
+}  // namespace vca
+
 // ===========================================================================
 // C-ABI
 // ===========================================================================

@@ -44,6 +44,9 @@ EXPORTS = [
     "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
     "vca_state_list_t0", "vca_state_list_finite_t", "vca_pair_kpoints", "vca_contour_rule",
     "vca_read_impSigma", "vca_splot_read",
+    "vca_mlp_config_defaults", "vca_mlp_init", "vca_mlp_finalize", "vca_mlp_param_count",
+    "vca_mlp_get_params", "vca_mlp_set_params", "vca_mlp_set_data", "vca_mlp_loss_grad", "vca_mlp_train",
+    "vca_mlp_predict", "vca_umma_gemm_check", "vca_umma_timeout_check",
 ]
 
 
@@ -150,6 +153,23 @@ def load(path: Optional[str] = None):
         "vca_gfm_read": (ctypes.c_int, [ctypes.c_char_p, i32, i64, ctypes.POINTER(i64), ctypes.POINTER(i32),
                                         ctypes.POINTER(i32), ctypes.POINTER(i32), dp, dp]),
     }
+    fp = ctypes.POINTER(ctypes.c_float)
+    u16p = ctypes.POINTER(ctypes.c_uint16)
+    from .surrogate import MlpConfig
+    sig.update({
+        "vca_mlp_config_defaults": (None, [ctypes.POINTER(MlpConfig)]),
+        "vca_mlp_init": (ctypes.c_int, [ctypes.POINTER(MlpConfig)]),
+        "vca_mlp_finalize": (ctypes.c_int, []),
+        "vca_mlp_param_count": (i64, []),
+        "vca_mlp_get_params": (ctypes.c_int, [fp, i64]),
+        "vca_mlp_set_params": (ctypes.c_int, [fp, i64]),
+        "vca_mlp_set_data": (ctypes.c_int, [i32, dp, dp, dp]),
+        "vca_mlp_loss_grad": (ctypes.c_int, [dp, fp, i64]),
+        "vca_mlp_train": (ctypes.c_int, [i32, dp]),
+        "vca_mlp_predict": (ctypes.c_int, [i32, dp, dp, dp]),
+        "vca_umma_gemm_check": (ctypes.c_int, [u16p, u16p, fp, i32, i32, i32]),
+        "vca_umma_timeout_check": (ctypes.c_int, []),
+    })
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype = res
