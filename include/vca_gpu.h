@@ -110,7 +110,10 @@ typedef struct vca_config {
   int32_t lanc_niter_spectrum; /* LANC_NITER_SPECTRUM annealing sweeps        */
   int32_t contour_nodes;   /* Gauss-Legendre nodes per panel of the contour  */
                            /* rule replacing quad(integral_contour, 0, pi)   */
-  int32_t pad1;
+  int32_t sector_at_a_time; /* 1: the ground-state search diagonalises one   */
+                           /* sector after the other, as the reference's loop */
+                           /* (VCA_DIAG.f90:83-249); 0 (default): every      */
+                           /* sector in one batched search                   */
   double cutoff;           /* CUTOFF     spectrum cut-off exp(-beta dE)      */
   double bandwidth;        /* bandwidth  lattice bandwidth (a module variable */
                            /* the reference's drivers assign, default 0)     */
@@ -120,7 +123,9 @@ typedef struct vca_config {
   int32_t print_impg;      /* PRINT_IMPG   ... of G'  (VCA_INPUT_VARS.f90:137-139; */
   int32_t print_impg0;     /* PRINT_IMPG0  ... of G0   the reference's default is */
                            /* on, here off: see vca_gpu_print_impSigma)           */
-  int32_t pad2;
+  int32_t batch_loop;      /* 1: vca_gpu_solve_batch solves its points one      */
+                           /* after another (the plain path); 0 (default): the  */
+                           /* batched form at T=0 (FP64, every point per launch) */
   char file_suffix[64];    /* the reference's file_suffix, NUL-terminated: ends  */
                            /* the stem of every file name (VCA_IO.f90:126-128)   */
 } vca_config;
@@ -164,6 +169,15 @@ int vca_gpu_solve(const double* Hloc, const double* Hk, int64_t Nk,
  * drivers/vca_hm_chain1d.f90:88-111).  Point b uses Hloc + b*stride_hloc
  * complex elements, and bath_h/bath_v likewise (NULL = no bath); Hk is shared
  * by all points.  omega_out[b] receives the SFT potential of point b.
+ * At T=0 with B >= 2 (and batch_loop = 0) the points run in the batched
+ * form: in FP64, every (point, sector) ground-state search in one multi-task
+ * Lanczos, the kept eigenvectors in one second pass, every point's
+ * Green's-function chains in memory-bounded groups of (point, chain) tasks,
+ * then Omega per point; the points of one call are processed in waves that
+ * fit device memory.  Afterwards the context holds the last point's solve
+ * (re-run on the plain path; the call fails with VCA_ERR_NUMERIC if its two
+ * Omega values differ by more than 1e-10 relative).  Finite T, B = 1 or
+ * batch_loop = 1: one point after another through vca_gpu_solve's path.
  */
 int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc,
                         const double* Hk, int64_t Nk,

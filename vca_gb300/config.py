@@ -66,14 +66,14 @@ class VcaConfig(ctypes.Structure):
         ("lanc_nstates_step", ctypes.c_int32),
         ("lanc_niter_spectrum", ctypes.c_int32),
         ("contour_nodes", ctypes.c_int32),
-        ("pad1", ctypes.c_int32),
+        ("sector_at_a_time", ctypes.c_int32),
         ("cutoff", ctypes.c_double),
         ("bandwidth", ctypes.c_double),
         ("gs_beta_tol", ctypes.c_double),
         ("print_sigma", ctypes.c_int32),
         ("print_impg", ctypes.c_int32),
         ("print_impg0", ctypes.c_int32),
-        ("pad2", ctypes.c_int32),
+        ("batch_loop", ctypes.c_int32),
         ("file_suffix", ctypes.c_char * 64),
     ]
 
@@ -85,7 +85,7 @@ class VcaConfig(ctypes.Structure):
     def as_dict(self) -> dict:
         out = {}
         for name, _ in self._fields_:
-            if name in ("pad0", "pad1", "pad2"):
+            if name == "pad0":
                 continue
             v = getattr(self, name)
             out[name] = list(v) if name == "Uloc" else v

@@ -1083,7 +1083,20 @@ int diagonalize() {
   std::vector<double> eb;
   std::vector<char> keep_sec(g->Nsectors + 1, 1);
   {
-    RCHK(g->fx ? batched_sector_energies(eb) : batched_sector_energies_f64(eb));
+    if (c.sector_at_a_time) {  // the reference's loop, one sector per Lanczos run
+      eb.assign(g->Nsectors, INFINITY);
+      for (int isector = 1; isector <= g->Nsectors; isector++) {
+        double e;
+        void* vec = nullptr;
+        Arena tmp;
+        const int rc = g->fx ? sector_gs_fx(isector, &e, &vec, tmp) : sector_gs(isector, &e, &vec, tmp);
+        tmp.release();
+        if (rc) return rc;
+        eb[isector - 1] = e;
+      }
+    } else {
+      RCHK(g->fx ? batched_sector_energies(eb) : batched_sector_energies_f64(eb));
+    }
     std::vector<ListEntry> lst;
     replay_t0(eb, thr, lst);
     std::fill(keep_sec.begin(), keep_sec.end(), 0);
@@ -2070,6 +2083,479 @@ static void gfm_drop() {
   g->gfm_loaded = false;
 }
 
+// ===========================================================================
+// The batched form: B variational points in one pass.  The reference's
+// drivers call vca_solve once per point (drivers/vca_hm_chain1d.f90:88-95,
+// drivers/vca_bhz_2d.f90:244-305); here the points of a wave share every
+// launch.  The FP64 multi-task Lanczos of vca_multi.cu runs one task list per
+// stage, each task a (point, sector) or (point, chain) with that point's hop
+// tables:
+//   1. every point's one-body tables (set_hamiltonian, kept per point);
+//   2. every (point, sector) lowest energy in one search (as the plain
+//      path's batched search: same start vectors, recurrence and stopping);
+//   3. per point the T=0 list (VCA_DIAG.f90:224-236) on the host;
+//   4. the kept (point, sector) eigenvectors in one second pass;
+//   5. every point's Green's-function chains in memory-bounded groups of
+//      (point, chain) tasks (VCA_GF_NORMAL.f90:121-318,561-958);
+//   6. per point Omega from its chain store (VCA_OMEGA.f90:37-146).
+// T=0 only; the points share Hk.  The context is left as a solve of the last
+// point leaves it (that point is solved once more on the plain path, which
+// must agree with its batched Omega to 1e-10).
+// ===========================================================================
+struct PointTabs {
+  Arena ham;
+  std::vector<SpinSpace> sp[2];
+  std::vector<cd> Hloc, bath_h, bath_v;
+  bool real_model = true;
+};
+
+SectorView view_tabs(const PointTabs& P, int nup, int ndw) {
+  const SpinSpace& u = P.sp[0][nup];
+  const SpinSpace& d = P.sp[g->dwset][ndw];
+  SectorView v;
+  v.dimup = u.dim;
+  v.dimdw = d.dim;
+  v.wup = u.width;
+  v.wdw = d.width;
+  v.up_words = u.words;
+  v.dw_words = d.words;
+  v.up_cnt = u.cnt;
+  v.dw_cnt = d.cnt;
+  v.up_src = u.src;
+  v.dw_src = d.src;
+  v.up_amp = u.amp;
+  v.dw_amp = d.amp;
+  v.up_e1 = u.e1;
+  v.dw_e1 = d.e1;
+  return v;
+}
+
+struct TaskList {  // tasks packed back to back, cut into MS_TILE tiles
+  std::vector<MsSector> secs;
+  std::vector<int> tsec;
+  std::vector<int64_t> tstart;
+  int64_t tot = 0;
+  void add(const SectorView& sv, int64_t len, int isector, int ncomp) {
+    MsSector m{};
+    m.sv = sv;
+    m.off = tot;
+    m.D = len;
+    m.tile0 = (int)tsec.size();
+    m.isector = isector;
+    m.ncomp = ncomp;
+    for (int64_t s = 0; s < len; s += MS_TILE) {
+      tsec.push_back((int)secs.size());
+      tstart.push_back(s);
+    }
+    m.ntile = (int)tsec.size() - m.tile0;
+    secs.push_back(m);
+    tot += len;
+  }
+};
+
+struct MtRun {  // device state of one multi-task run
+  Arena ar;
+  MsGroup gp{};
+  Ms64Bufs b{};
+  double* n2 = nullptr;
+};
+
+int mt_alloc(MtRun& R, const TaskList& T, int ld, size_t es, bool psi) {
+  const int nsec = (int)T.secs.size(), ntiles = (int)T.tsec.size();
+  MsSector* d_secs;
+  int* d_tsec;
+  int64_t* d_tstart;
+  char *x0, *x1, *x2;
+  Ms64Bufs& b = R.b;
+  b.ld = ld;
+  Arena& ar = R.ar;
+  int rc = VCA_OK;
+  if ((rc = ar.alloc(&d_secs, nsec)) || (rc = ar.alloc(&d_tsec, ntiles)) || (rc = ar.alloc(&d_tstart, ntiles)) ||
+      (rc = ar.alloc(&x0, (size_t)T.tot * es)) || (rc = ar.alloc(&x1, (size_t)T.tot * es)) ||
+      (rc = ar.alloc(&x2, (size_t)T.tot * es)) || (rc = ar.alloc(&b.tpart, ntiles)) ||
+      (rc = ar.alloc(&b.meta, nsec)) || (rc = ar.alloc(&b.alpha, nsec)) || (rc = ar.alloc(&b.bnow, nsec)) ||
+      (rc = ar.alloc(&b.invb, nsec)) || (rc = ar.alloc(&b.A, (size_t)nsec * ld)) ||
+      (rc = ar.alloc(&b.Bt, (size_t)nsec * ld)) || (rc = ar.alloc(&b.theta, nsec)) ||
+      (rc = ar.alloc(&b.resid, nsec)) || (rc = ar.alloc(&b.state, nsec)) || (rc = ar.alloc(&b.mconv, nsec)) ||
+      (rc = ar.alloc(&b.undone, 1)) || (rc = ar.alloc(&R.n2, nsec)))
+    return rc;
+  if (!psi && (rc = ar.alloc(&b.svec, (size_t)nsec * 5 * ld))) return rc;
+  b.X = x0;
+  b.Xp = x1;
+  b.Y = x2;
+  CUCHK(cudaMemcpyAsync(d_secs, T.secs.data(), sizeof(MsSector) * nsec, cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_tsec, T.tsec.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_tstart, T.tstart.data(), sizeof(int64_t) * ntiles, cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemsetAsync(b.A, 0, sizeof(double) * nsec * ld, g->st));
+  CUCHK(cudaMemsetAsync(b.Bt, 0, sizeof(double) * nsec * ld, g->st));
+  CUCHK(cudaMemsetAsync(b.bnow, 0, sizeof(double) * nsec, g->st));
+  CUCHK(cudaMemsetAsync(b.state, 0, sizeof(int) * nsec, g->st));
+  R.gp = MsGroup{d_secs, d_tsec, d_tstart, nsec, ntiles};
+  return VCA_OK;
+}
+
+// one chain task of the batched form, with the bookkeeping its store needs
+struct BChain {
+  int point, state;  // point within the wave, its kept state
+  MtChain mc;
+  ChainRec rec;
+  int isign;
+  cd wfac;
+  int ncomp;
+  int tup, tdw;
+};
+
+int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_h, int64_t sbh, const double* bath_v,
+                      int64_t sbv, double* omega_out) {
+  const vca_config cfg0 = g->cfg;
+  vca_config& c = g->cfg;
+  c.arith = VCA_ARITH_FP64;  // the batched form runs the FP64 path
+  auto restore = [&]() { g->cfg = cfg0; };
+  auto hl = [&](int p) { return Hloc + 2 * (size_t)p * sh; };
+  auto bh = [&](int p) { return bath_h ? bath_h + 2 * (size_t)p * sbh : nullptr; };
+  auto bv = [&](int p) { return bath_v ? bath_v + 2 * (size_t)p * sbv : nullptr; };
+  const int Ns = g->Ns, nsecs = g->Nsectors;
+  int64_t sumD = 0;
+  for (int s = 1; s <= nsecs; s++) sumD += (int64_t)g->dimn[sec_nup(s)] * g->dimn[sec_ndw(s)];
+  const cd XI(0.0, 1.0);
+  const int L = c.Nlat * c.Norb;
+  int p0 = 0;
+  while (p0 < B) {
+    // ---- 1. tables of a wave of points ---------------------------------------
+    size_t freeb = 0, totb = 0;
+    if (cudaMemGetInfo(&freeb, &totb) != cudaSuccess) { restore(); VFAIL(VCA_ERR_CUDA, "cudaMemGetInfo failed"); }
+    const size_t per_point = 3 * (size_t)sumD * sizeof(double2) + ((size_t)8 << 20);
+    const int P = (int)std::max<int64_t>(1, std::min<int64_t>(B - p0, (int64_t)(0.35 * (double)freeb / per_point)));
+    const int p1 = p0 + P;
+    std::vector<PointTabs> tabs(P);
+    bool cplx = false;
+    for (int q = 0; q < P; q++) {
+      int rc = set_hamiltonian(hl(p0 + q), bh(p0 + q), bv(p0 + q));
+      if (rc) { restore(); return rc; }
+      PointTabs& T = tabs[q];
+      T.ham.ptrs.swap(g->ham.ptrs);  // the point keeps its tables; set_hamiltonian starts a new arena
+      T.sp[0] = g->sp[0];
+      T.sp[1] = g->sp[1];
+      T.Hloc = g->Hloc;
+      T.bath_h = g->bath_h;
+      T.bath_v = g->bath_v;
+      T.real_model = g->real_model;
+      if (q == 0) cplx = !g->real_model;
+      if (cplx != !g->real_model) {
+        for (auto& t : tabs) t.ham.release();
+        restore();
+        VFAIL(VCA_ERR_UNSUPPORTED, "a batch mixes real and complex Hamiltonians");
+      }
+    }
+    g->ham_set = false;  // g->sp points into the wave's tables until the final plain solve
+    const size_t es = cplx ? sizeof(double2) : sizeof(double);
+    auto cleanup = [&]() { for (auto& t : tabs) t.ham.release(); };
+    // ---- 2. every (point, sector) lowest energy ------------------------------
+    TaskList S;
+    int nmaxg = 1;
+    for (int q = 0; q < P; q++)
+      for (int s = 1; s <= nsecs; s++) {
+        const int nu = sec_nup(s), nd = sec_ndw(s);
+        const int64_t D = (int64_t)g->dimn[nu] * g->dimn[nd];
+        S.add(view_tabs(tabs[q], nu, nd), D, s, 1);
+        nmaxg = std::max(nmaxg, (int)std::min<int64_t>(D, std::min(c.lanc_niter, 512)));
+      }
+    const int ldg = nmaxg + 1;
+    std::vector<double> theta(S.secs.size());
+    std::vector<int> mconv(S.secs.size());
+    std::vector<double> svec_h;
+    {
+      MtRun R;
+      int rc = mt_alloc(R, S, ldg, es, false);
+      if (rc) { R.ar.release(); cleanup(); restore(); return rc; }
+      std::vector<ChainMeta> meta(S.secs.size());
+      for (size_t t = 0; t < S.secs.size(); t++)
+        meta[t] = ChainMeta{1, (int)t, (int)std::min<int64_t>(S.secs[t].D, std::min(c.lanc_niter, 512)), 1, 0};
+      cudaMemcpyAsync(R.b.meta, meta.data(), sizeof(ChainMeta) * meta.size(), cudaMemcpyHostToDevice, g->st);
+      m64_launch_start(R.gp, cplx, c.start_seed, R.b, g->st);
+      for (int k = 1; k <= nmaxg; k++) {
+        m64_launch_step(R.gp, cplx, g->md, k, c.gs_beta_tol, R.b, g->st);
+        if (k % std::max(1, c.gs_check_every) == 0 || k == nmaxg) {
+          cudaMemsetAsync(R.b.undone, 0, sizeof(int), g->st);
+          m64_launch_check(R.gp, R.b, c.gs_residual_tol, g->st);
+          int undone = 0;
+          cudaMemcpyAsync(&undone, R.b.undone, sizeof(int), cudaMemcpyDeviceToHost, g->st);
+          if (cudaStreamSynchronize(g->st) != cudaSuccess) { R.ar.release(); cleanup(); restore(); VFAIL(VCA_ERR_CUDA, "batched search failed"); }
+          if (undone == 0) break;
+        }
+      }
+      svec_h.resize(S.secs.size() * 5 * (size_t)ldg);
+      cudaMemcpyAsync(theta.data(), R.b.theta, sizeof(double) * theta.size(), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(mconv.data(), R.b.mconv, sizeof(int) * mconv.size(), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(svec_h.data(), R.b.svec, sizeof(double) * svec_h.size(), cudaMemcpyDeviceToHost, g->st);
+      cudaError_t e = cudaStreamSynchronize(g->st);
+      R.ar.release();
+      if (e != cudaSuccess) { cleanup(); restore(); VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e)); }
+    }
+    // ---- 3. T=0 lists -------------------------------------------------------
+    std::vector<std::vector<ListEntry>> lists(P);
+    for (int q = 0; q < P; q++) {
+      std::vector<double> E(theta.begin() + (size_t)q * nsecs, theta.begin() + (size_t)(q + 1) * nsecs);
+      replay_t0(E, c.gs_threshold, lists[q]);
+      if (lists[q].empty()) { cleanup(); restore(); VFAIL(VCA_ERR_NUMERIC, "no ground state found"); }
+    }
+    // ---- 4. eigenvectors of the kept (point, sector) tasks -------------------
+    TaskList V;
+    std::vector<int> vsrc;  // search task of each eigenvector task
+    for (int q = 0; q < P; q++)
+      for (const ListEntry& x : lists[q]) {
+        const int t = q * nsecs + (x.sector - 1);
+        V.add(S.secs[t].sv, S.secs[t].D, x.sector, 1);
+        vsrc.push_back(t);
+      }
+    MtRun RV;  // holds the ground-state vectors (psi) until the chains are done
+    char* psi = nullptr;
+    {
+      int rc = mt_alloc(RV, V, ldg, es, true);
+      if (!rc) rc = RV.ar.alloc(&psi, (size_t)V.tot * es);
+      double* d_svec = nullptr;
+      int* d_mc = nullptr;
+      if (!rc) rc = RV.ar.alloc(&d_svec, V.secs.size() * 5 * (size_t)ldg);
+      if (!rc) rc = RV.ar.alloc(&d_mc, V.secs.size());
+      if (rc) { RV.ar.release(); cleanup(); restore(); return rc; }
+      std::vector<double> sv(V.secs.size() * 5 * (size_t)ldg);
+      std::vector<int> mc(V.secs.size());
+      std::vector<ChainMeta> meta(V.secs.size());
+      int mmax = 1;
+      for (size_t v = 0; v < V.secs.size(); v++) {
+        std::copy(svec_h.begin() + vsrc[v] * 5 * (size_t)ldg, svec_h.begin() + (vsrc[v] + 1) * 5 * (size_t)ldg,
+                  sv.begin() + v * 5 * (size_t)ldg);
+        mc[v] = mconv[vsrc[v]];
+        if (mc[v] < 1) { RV.ar.release(); cleanup(); restore(); VFAIL(VCA_ERR_NUMERIC, "Lanczos start vector has zero norm"); }
+        meta[v] = ChainMeta{1, (int)v, mc[v], 1, 0};
+        mmax = std::max(mmax, mc[v]);
+      }
+      cudaMemcpyAsync(d_svec, sv.data(), sizeof(double) * sv.size(), cudaMemcpyHostToDevice, g->st);
+      cudaMemcpyAsync(d_mc, mc.data(), sizeof(int) * mc.size(), cudaMemcpyHostToDevice, g->st);
+      cudaMemcpyAsync(RV.b.meta, meta.data(), sizeof(ChainMeta) * meta.size(), cudaMemcpyHostToDevice, g->st);
+      cudaMemsetAsync(psi, 0, (size_t)V.tot * es, g->st);
+      m64_launch_start(RV.gp, cplx, c.start_seed, RV.b, g->st);
+      for (int k = 1; k <= mmax; k++) {  // psi = sum_k s_k x_k (sector_gs's second pass, every task at once)
+        m64_launch_psi(RV.gp, cplx, d_svec, 5 * ldg, d_mc, k, RV.b.X, psi, g->st);
+        if (k < mmax) m64_launch_step(RV.gp, cplx, g->md, k, c.gs_beta_tol, RV.b, g->st);
+      }
+      m64_launch_sqnorm(RV.gp, cplx, psi, RV.b.tpart, g->st);
+      mt_launch_norm(RV.gp, RV.b.tpart, RV.b.meta, RV.n2, RV.b.invb, g->st);
+      m64_launch_scale(RV.gp, cplx, RV.b.invb, psi, psi, g->st);
+      if (cudaStreamSynchronize(g->st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        RV.ar.release(); cleanup(); restore();
+        VFAIL(VCA_ERR_CUDA, "batched eigenvector pass failed");
+      }
+    }
+    // ---- 5. chains of every point --------------------------------------------
+    std::vector<std::vector<BChain>> pch(P);
+    {
+      int v = 0;
+      for (int q = 0; q < P; q++)
+        for (int k = 0; k < (int)lists[q].size(); k++, v++) {
+          const ListEntry& st = lists[q][k];
+          const int nup = sec_nup(st.sector), ndw = sec_ndw(st.sector);
+          const void* gsv = psi + (size_t)V.secs[v].off * es;
+          for (int is = 0; is < c.Nspin; is++)
+            for (int dag = 1; dag >= 0; dag--) {  // the particle batch, then the hole batch (build_gf's order)
+              const int tup = nup + (is == 0 ? (dag ? 1 : -1) : 0);
+              const int tdw = ndw + (is == 1 ? (dag ? 1 : -1) : 0);
+              if (tup < 0 || tup > Ns || tdw < 0 || tdw > Ns) continue;
+              auto add = [&](int e, int chan, int p, cd cp, int qq, cd cq, int nterm, cd wfac) {
+                BChain b{};
+                b.point = q;
+                b.state = k;
+                b.mc.gs = gsv;
+                b.mc.src_dimup = tabs[q].sp[0][nup].dim;
+                b.mc.spin = is;
+                b.mc.dag = dag;
+                b.mc.nterm = nterm;
+                b.mc.pos[0] = p;
+                b.mc.cre[0] = cp.real();
+                b.mc.cim[0] = cp.imag();
+                b.mc.pos[1] = qq;
+                b.mc.cre[1] = cq.real();
+                b.mc.cim[1] = cq.imag();
+                const bool imagcoef = (cp.imag() != 0.0) || (nterm > 1 && cq.imag() != 0.0);
+                b.ncomp = (!cplx && imagcoef) ? 2 : 1;
+                b.rec = ChainRec{e, k, chan, 0};
+                b.isign = dag ? 1 : -1;
+                b.wfac = wfac;
+                b.tup = tup;
+                b.tdw = tdw;
+                pch[q].push_back(b);
+              };
+              for (int io = 0; io < c.Norb; io++)
+                for (int il = 0; il < c.Nlat; il++) {
+                  const int p = io + il * c.Norb;
+                  add(elem_index(c, il, il, is, io, io), dag ? 1 : 2, p, 1.0, 0, 0.0, 1, 1.0);
+                  for (int jl = 0; jl < c.Nlat; jl++)
+                    for (int jo = 0; jo < c.Norb; jo++) {
+                      if (il == jl && io == jo) continue;
+                      const int qq = jo + jl * c.Norb;
+                      const int e = elem_index(c, il, jl, is, io, jo);
+                      add(e, dag ? 1 : 2, p, 1.0, qq, 1.0, 2, 1.0);
+                      if (!c.vca_gf_symmetric) {
+                        if (dag) add(e, 3, p, 1.0, qq, XI, 2, -XI);
+                        else add(e, 4, p, 1.0, qq, -XI, 2, -XI);
+                      }
+                    }
+                }
+            }
+        }
+    }
+    (void)L;
+    g->ld = std::max(1, c.lanc_ngfiter);
+    const int ld = g->ld;
+    // per-point chain stores
+    Arena stores;
+    std::vector<ChainStore> cs(P);
+    for (int q = 0; q < P; q++) {
+      const size_t n = std::max<size_t>(1, pch[q].size());
+      ChainStore& s = cs[q];
+      s.ld = ld;
+      int rc = VCA_OK;
+      if ((rc = stores.alloc(&s.A, n * ld)) || (rc = stores.alloc(&s.B, n * ld)) || (rc = stores.alloc(&s.n, n)) ||
+          (rc = stores.alloc(&s.pes, n)) || (rc = stores.alloc(&s.isign, n)) || (rc = stores.alloc(&s.wfac, n)) ||
+          (rc = stores.alloc(&s.Ei, n))) {
+        stores.release(); RV.ar.release(); cleanup(); restore();
+        return rc;
+      }
+      cudaMemsetAsync(s.n, 0, sizeof(int) * n, g->st);
+    }
+    {
+      // every chain task, point-major; groups bounded by memory
+      std::vector<std::pair<int, int>> all;  // (point, index in pch)
+      for (int q = 0; q < P; q++)
+        for (int i = 0; i < (int)pch[q].size(); i++) all.push_back({q, i});
+      size_t fb = 0;
+      cudaMemGetInfo(&fb, &totb);
+      const size_t gbudget = (size_t)(0.3 * (double)fb);
+      size_t a0 = 0;
+      while (a0 < all.size()) {
+        TaskList T;
+        std::vector<MtChain> mcs;
+        std::vector<ChainMeta> meta;
+        std::vector<int> isg;
+        std::vector<double2> wf;
+        size_t a1 = a0;
+        int nl_max = 1;
+        while (a1 < all.size()) {
+          const BChain& b = pch[all[a1].first][all[a1].second];
+          const SectorView tv = view_tabs(tabs[b.point], b.tup, b.tdw);
+          const int64_t Dsec = (int64_t)tv.dimup * tv.dimdw;
+          const int64_t len = b.ncomp * Dsec;
+          if (a1 > a0 && 3 * (size_t)(T.tot + len) * es > gbudget) break;
+          const int nl = (int)std::min<int64_t>(Dsec, c.lanc_ngfiter);
+          T.add(tv, len, 0, b.ncomp);
+          mcs.push_back(b.mc);
+          meta.push_back(ChainMeta{1, (int)meta.size(), nl, 1, 0});
+          isg.push_back(b.isign);
+          wf.push_back(make_double2(b.wfac.real(), b.wfac.imag()));
+          nl_max = std::max(nl_max, nl);
+          a1++;
+        }
+        MtRun R;
+        MtChain* d_mc = nullptr;
+        int* d_isg = nullptr;
+        double2* d_wf = nullptr;
+        int rc = mt_alloc(R, T, ld, es, true);
+        if (!rc) rc = R.ar.alloc(&d_mc, mcs.size());
+        if (!rc) rc = R.ar.alloc(&d_isg, isg.size());
+        if (!rc) rc = R.ar.alloc(&d_wf, wf.size());
+        if (rc) { R.ar.release(); stores.release(); RV.ar.release(); cleanup(); restore(); return rc; }
+        cudaMemcpyAsync(d_mc, mcs.data(), sizeof(MtChain) * mcs.size(), cudaMemcpyHostToDevice, g->st);
+        cudaMemcpyAsync(d_isg, isg.data(), sizeof(int) * isg.size(), cudaMemcpyHostToDevice, g->st);
+        cudaMemcpyAsync(d_wf, wf.data(), sizeof(double2) * wf.size(), cudaMemcpyHostToDevice, g->st);
+        cudaMemcpyAsync(R.b.meta, meta.data(), sizeof(ChainMeta) * meta.size(), cudaMemcpyHostToDevice, g->st);
+        // start vectors c^(dag)|gs>, normalised; norm^2 kept for the weights
+        mt_launch_chain_init(R.gp, cplx, d_mc, R.b.X, R.b.tpart, g->st);
+        mt_launch_norm(R.gp, R.b.tpart, R.b.meta, R.n2, R.b.invb, g->st);
+        m64_launch_scale(R.gp, cplx, R.b.invb, R.b.X, R.b.X, g->st);
+        for (int k = 1; k <= nl_max; k++) m64_launch_step(R.gp, cplx, g->md, k, c.gf_beta_tol, R.b, g->st);
+        // into the stores: runs of one (point, state)
+        size_t r0 = 0;
+        while (r0 < mcs.size()) {
+          const BChain& b0 = pch[all[a0 + r0].first][all[a0 + r0].second];
+          size_t r1 = r0;
+          while (r1 < mcs.size()) {
+            const BChain& b1 = pch[all[a0 + r1].first][all[a0 + r1].second];
+            if (b1.point != b0.point || b1.state != b0.state) break;
+            r1++;
+          }
+          const int q = b0.point;
+          const double Ei = lists[q][b0.state].e;
+          const double zeta = (double)lists[q].size();
+          launch_chain_store((int)(r1 - r0), R.b.meta + r0, R.b.A + r0 * ld, R.b.Bt + r0 * ld, ld, R.n2 + r0,
+                             d_wf + r0, d_isg + r0, Ei, 1.0, zeta, cs[q], all[a0 + r0].second, g->st);
+          r0 = r1;
+        }
+        cudaError_t e = cudaStreamSynchronize(g->st);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        R.ar.release();
+        if (e != cudaSuccess) { stores.release(); RV.ar.release(); cleanup(); restore(); VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e)); }
+        a0 = a1;
+      }
+    }
+    RV.ar.release();  // the ground-state vectors are no longer needed
+    // ---- 6. Omega per point --------------------------------------------------
+    for (int q = 0; q < P; q++) {
+      g->Hloc = tabs[q].Hloc;
+      g->bath_h = tabs[q].bath_h;
+      g->bath_v = tabs[q].bath_v;
+      g->real_model = tabs[q].real_model;
+      g->gs.clear();
+      for (const ListEntry& x : lists[q]) g->gs.push_back(GState{x.sector, x.e, nullptr});
+      g->egs = INFINITY;
+      for (auto& s : g->gs) g->egs = std::min(g->egs, s.e);
+      g->zeta = (double)g->gs.size();
+      g->chains.clear();
+      for (const BChain& b : pch[q]) {
+        ChainRec r = b.rec;
+        const int64_t Dsec = (int64_t)g->dimn[b.tup] * g->dimn[b.tdw];
+        r.nlanc = (int)std::min<int64_t>(Dsec, c.lanc_ngfiter);
+        g->chains.push_back(r);
+      }
+      g->cstore = cs[q];
+      g->poles_ready = false;
+      g->nelem = c.Nlat * c.Nlat * c.Nspin * c.Norb * c.Norb;
+      std::vector<std::vector<int>> lst(g->nelem);
+      for (int ch = 0; ch < (int)g->chains.size(); ch++) lst[g->chains[ch].elem].push_back(ch);
+      std::vector<int> ptr(g->nelem + 1, 0), flat;
+      for (int e = 0; e < g->nelem; e++) {
+        ptr[e + 1] = ptr[e] + (int)lst[e].size();
+        flat.insert(flat.end(), lst[e].begin(), lst[e].end());
+      }
+      Arena csr;
+      int rc = csr.alloc(&g->d_elem_ptr, ptr.size());
+      if (!rc) rc = csr.alloc(&g->d_elem_chain, std::max<size_t>(1, flat.size()));
+      if (!rc) {
+        cudaMemcpyAsync(g->d_elem_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, g->st);
+        if (!flat.empty())
+          cudaMemcpyAsync(g->d_elem_chain, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, g->st);
+        double oi = 0.0;
+        rc = omega_integral(&oi);
+        if (!rc) omega_out[p0 + q] = g->egs - oi;  // VCA_MAIN.f90:183-197 at T=0
+      }
+      csr.release();
+      g->d_elem_ptr = g->d_elem_chain = nullptr;
+      g->cstore = ChainStore{};
+      g->chains.clear();
+      if (rc) { stores.release(); cleanup(); restore(); return rc; }
+    }
+    stores.release();
+    cleanup();
+    p0 = p1;
+  }
+  restore();
+  // the context as a loop of vca_solve leaves it: the last point, plain path
+  double last = 0.0;
+  RCHK(solve_resident(hl(B - 1), bh(B - 1), bv(B - 1), &last));
+  if (std::fabs(last - omega_out[B - 1]) > 1e-10 * std::max(1.0, std::fabs(last)))
+    VFAIL(VCA_ERR_NUMERIC, "batched and plain Omega of the last point disagree");
+  return VCA_OK;
+}
+
 }  // namespace
 
 namespace vca {
@@ -2250,6 +2736,10 @@ int vca_gpu_solve_batch(int32_t B, const double* Hloc, int64_t stride_hloc, cons
   if (B < 0 || !omega_out) VFAIL(VCA_ERR_ARG, "bad batch arguments");
   if (B == 0) return VCA_OK;
   RCHK(upload_hk(Hk, Nk));  // shared by every point: uploaded (and its k-pairs found) once
+  if (B >= 2 && !g->finiteT && !g->cfg.batch_loop) {
+    RCHK(solve_batch_fused(B, Hloc, stride_hloc, bath_h, stride_bath_h, bath_v, stride_bath_v, omega_out));
+    return print_after_solve();
+  }
   for (int b = 0; b < B; b++) {
     RCHK(solve_resident(Hloc + 2 * (size_t)b * stride_hloc,
                         bath_h ? bath_h + 2 * (size_t)b * stride_bath_h : nullptr,

@@ -4,6 +4,7 @@
 #include "vca_kernels.cuh"
 #include "vca_fx.cuh"
 #include "vca_tri.cuh"
+#include "vca_multi.cuh"
 
 #include <cmath>
 #include <atomic>
@@ -663,6 +664,78 @@ __global__ void k_chain_init(SectorView tgt, int src_dimup, const void* gsv, int
     }
   }
 }
+// The same gather for chain tasks of the batched form: one packed vector per
+// task (its point's target sector), [re; im] halves for a complex chain on a
+// real H; per-tile |x|^2 partials in a fixed order for the norm.
+template <typename T>
+__global__ void k_mt_chain_init(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
+                                const MtChain* chs, T* X, double* tpart) {
+  __shared__ double red[256];
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    const MsSector& S = secs[s];
+    const SectorView& tgt = S.sv;
+    const MtChain c = chs[s];
+    const int64_t Dsec = (int64_t)tgt.dimup * tgt.dimdw;
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    double acc = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const int comp = (i >= Dsec) ? 1 : 0;
+      const int64_t ii = i - (comp ? Dsec : 0);
+      const int idw = (int)(ii / tgt.dimup);
+      const int iup = (int)(ii - (int64_t)idw * tgt.dimup);
+      const unsigned w = (unsigned)(c.spin == 0 ? tgt.up_words[iup] : tgt.dw_words[idw]);
+      double vr = 0.0, vi = 0.0;
+      for (int q = 0; q < c.nterm; q++) {
+        const int pos = c.pos[q];
+        const bool occ = (w >> pos) & 1u;
+        if (c.dag ? !occ : occ) continue;
+        const unsigned ws = w ^ (1u << pos);
+        const double sg = parity(ws & ((1u << pos) - 1u));
+        const int rs = rank_word(ws);
+        const int64_t si = (c.spin == 0) ? ((int64_t)rs + (int64_t)idw * c.src_dimup)
+                                         : ((int64_t)iup + (int64_t)rs * c.src_dimup);
+        double gr, gi = 0.0;
+        if (sizeof(T) == sizeof(double2)) {
+          const double2 gv = ((const double2*)c.gs)[si];
+          gr = gv.x;
+          gi = gv.y;
+        } else {
+          gr = ((const double*)c.gs)[si];
+        }
+        const double ar = c.cre[q] * sg, ai = c.cim[q] * sg;
+        vr += ar * gr - ai * gi;
+        vi += ar * gi + ai * gr;
+      }
+      if (sizeof(T) == sizeof(double2)) {
+        ((double2*)X)[S.off + i] = make_double2(vr, vi);
+        acc += vr * vr + vi * vi;
+      } else {
+        const double v = comp ? vi : vr;
+        ((double*)X)[S.off + i] = v;
+        acc += v * v;
+      }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) tpart[t] = red[0];
+    __syncthreads();
+  }
+}
+void mt_launch_chain_init(const MsGroup& gp, bool cplx, const MtChain* d_ch, void* X, double* tpart,
+                          cudaStream_t st) {
+  COUNT_LAUNCH();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  if (cplx)
+    k_mt_chain_init<double2><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, d_ch, (double2*)X, tpart);
+  else
+    k_mt_chain_init<double><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, d_ch, (double*)X, tpart);
+}
+
 void launch_chain_init(const SectorView& tgt, int src_dimup, const void* gs, bool gs_cplx,
                        int nchain, const ChainInit* d_ci, int m, bool cols_cplx, void* X,
                        cudaStream_t st) {

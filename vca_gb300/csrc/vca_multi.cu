@@ -472,16 +472,20 @@ __global__ void __launch_bounds__(256) k_m64_hxv(const MsSector* secs, const int
     if (meta[s].active) {
       const MsSector& S = secs[s];
       const SectorView& sv = S.sv;
-      const T* x = X + S.off;
+      const int64_t Dsec = (int64_t)sv.dimup * sv.dimdw;
       const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
       const double b = use_b ? bnow[s] : 0.0;
       for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        const int idw = (int)(i / sv.dimup);
-        const int iup = (int)(i - (int64_t)idw * sv.dimup);
+        // a [re; im] task (ncomp 2) applies the real H to each half
+        const int64_t cb = (i >= Dsec) ? Dsec : 0;
+        const T* x = X + S.off + cb;
+        const int64_t ii = i - cb;
+        const int idw = (int)(ii / sv.dimup);
+        const int iup = (int)(ii - (int64_t)idw * sv.dimup);
         const double dre = sv.up_e1[iup].x + sv.dw_e1[idw].x +
                            mixed_diag(md, (unsigned)sv.up_words[iup], (unsigned)sv.dw_words[idw]);
         const double dim_ = sv.up_e1[iup].y + sv.dw_e1[idw].y;
-        const T xi = x[i];
+        const T xi = x[ii];
         T y = m64_diag(dre, dim_, xi);
         const int nu = sv.up_cnt[iup], nd = sv.dw_cnt[idw];
         const int64_t colbase = (int64_t)idw * sv.dimup;
@@ -606,6 +610,88 @@ void m64_launch_check(const MsGroup& gp, Ms64Bufs& b, double tol, cudaStream_t s
   const int blocks = std::max(1, (gp.nsec * 32 + threads - 1) / threads);
   k_ms_check<<<blocks, threads, 0, st>>>(gp.nsec, b.meta, b.A, b.Bt, b.ld, b.bnow, b.svec, b.theta, b.resid,
                                          b.state, b.mconv, tol, b.undone);
+}
+
+// ---- multi-task helpers of the batched form --------------------------------
+__global__ void k_mt_norm(int nsec, const MsSector* secs, const double* tpart, ChainMeta* meta, double* n2,
+                          double* invn) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nsec; s += nw) {
+    const double v = m64_sum_tiles(tpart, secs[s].tile0, secs[s].ntile);
+    if (lane == 0) {
+      n2[s] = v;
+      if (v > 0.0) {
+        invn[s] = 1.0 / sqrt(v);
+      } else {
+        invn[s] = 0.0;
+        meta[s].active = 0;
+        meta[s].len = 0;
+      }
+    }
+  }
+}
+template <typename T>
+__global__ void k_m64_psi(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
+                          const double* svec, int ld5, const int* mconv, int k, const T* X, T* psi) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int s = tsec[t];
+    if (k > mconv[s]) continue;
+    const MsSector& S = secs[s];
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    const double w = svec[(int64_t)s * ld5 + (k - 1)];
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      T p = psi[S.off + i];
+      p = m64_axpy(p, -w, X[S.off + i]);
+      psi[S.off + i] = p;
+    }
+  }
+}
+template <typename T>
+__global__ void k_m64_sqnorm(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles, const T* X,
+                             double* tpart) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const MsSector& S = secs[tsec[t]];
+    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
+    double acc = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc += m64_re(X[S.off + i], X[S.off + i]);
+    m64_block_store(acc, tpart, t);
+  }
+}
+
+void mt_launch_norm(const MsGroup& gp, const double* tpart, ChainMeta* meta, double* n2, double* invn,
+                    cudaStream_t st) {
+  count_launch_external();
+  k_mt_norm<<<(gp.nsec * 32 + 127) / 128, 128, 0, st>>>(gp.nsec, gp.secs, tpart, meta, n2, invn);
+}
+void m64_launch_scale(const MsGroup& gp, bool cplx, const double* f, const void* Xi, void* Xo, cudaStream_t st) {
+  count_launch_external();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  if (cplx)
+    k_m64_scale<double2><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, f, (const double2*)Xi,
+                                            (double2*)Xo);
+  else
+    k_m64_scale<double><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, f, (const double*)Xi,
+                                           (double*)Xo);
+}
+void m64_launch_psi(const MsGroup& gp, bool cplx, const double* svec, int ld5, const int* mconv, int k,
+                    const void* X, void* psi, cudaStream_t st) {
+  count_launch_external();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  if (cplx)
+    k_m64_psi<double2><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, svec, ld5, mconv, k,
+                                          (const double2*)X, (double2*)psi);
+  else
+    k_m64_psi<double><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, svec, ld5, mconv, k,
+                                         (const double*)X, (double*)psi);
+}
+void m64_launch_sqnorm(const MsGroup& gp, bool cplx, const void* X, double* tpart, cudaStream_t st) {
+  count_launch_external();
+  const int nb = std::min(gp.ntiles, 152 * 8);
+  if (cplx)
+    k_m64_sqnorm<double2><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, (const double2*)X, tpart);
+  else
+    k_m64_sqnorm<double><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, (const double*)X, tpart);
 }
 
 }  // namespace vca

@@ -16,7 +16,8 @@ struct MsSector {
   int64_t D;
   int tile0, ntile;
   int isector;   // 1-based sector number (start-vector seed)
-  int pad;
+  int ncomp;     // FP64 tasks: 2 when the task's vector is [re; im] of a complex
+                 // chain on a real H (length 2 * DimUp * DimDw), else 0 or 1
 };
 
 struct MsGroup {   // device tables of one group of sectors
@@ -54,5 +55,35 @@ void m64_launch_start(const MsGroup& gp, bool cplx, uint64_t seed, Ms64Bufs& b, 
 void m64_launch_step(const MsGroup& gp, bool cplx, const MixedDiag& md, int k, double tol, Ms64Bufs& b,
                      cudaStream_t st);
 void m64_launch_check(const MsGroup& gp, Ms64Bufs& b, double tol, cudaStream_t st);
+
+// ---- multi-task Lanczos over many variational points (the batched form) --
+// The FP64 step kernels above run any list of tasks: (point, sector) ground-
+// state searches, their eigenvector passes, and (point, chain) Green's-
+// function chains; a task's SectorView carries its point's hop tables.
+//
+// A chain task's start vector is an operator applied to its point's ground
+// state: sum_q coef_q c^(dag)_{pos_q, spin}|gs> (VCA_GF_NORMAL.f90:121-318,
+// 561-958), gathered per target element with the reference's one-word signs.
+struct MtChain {
+  const void* gs;   // source ground state: double (real H) or double2 (complex H)
+  int src_dimup;    // DimUp of the ground state's sector
+  int spin, dag, nterm;
+  int pos[2];
+  double cre[2], cim[2];
+};
+// X = start vectors of the chain tasks, tpart = per-tile |x|^2 partials
+void mt_launch_chain_init(const MsGroup& gp, bool cplx, const MtChain* d_ch, void* X, double* tpart,
+                          cudaStream_t st);
+// per task: n2 = |x|^2 (fixed-order sum of the tile partials), invn = 1/|x|
+// (0 and the task retired when the vector vanishes)
+void mt_launch_norm(const MsGroup& gp, const double* tpart, ChainMeta* meta, double* n2, double* invn,
+                    cudaStream_t st);
+// Xo = f[task] Xi
+void m64_launch_scale(const MsGroup& gp, bool cplx, const double* f, const void* Xi, void* Xo, cudaStream_t st);
+// psi += svec[task * ld5 + k - 1] X for the tasks with k <= mconv[task]
+void m64_launch_psi(const MsGroup& gp, bool cplx, const double* svec, int ld5, const int* mconv, int k,
+                    const void* X, void* psi, cudaStream_t st);
+// per-tile |x|^2 partials
+void m64_launch_sqnorm(const MsGroup& gp, bool cplx, const void* X, double* tpart, cudaStream_t st);
 
 }  // namespace vca
