@@ -120,9 +120,12 @@ def _square_hopping(nx, ny, nspin, t, H, spin_block=None):
 def square(nx: int = 4, ny: int = 3, U: float = 8.0, xmu: float = 4.0, t: float = 1.0,
            tprime: Optional[float] = None, maf: float = 0.0, nspin: int = 2, nkx: int = 32,
            nky: int = 32, ngfiter: int = 200, omega_nodes: int = 8192, mu_shift: float = 0.0,
-           **cfgkw) -> SolvePoint:
+           cdw: float = 0.0, **cfgkw) -> SolvePoint:
     """Square Hubbard cluster with an antiferromagnetic Weiss field M on the
-    cluster only: Hloc(i,i,s,s) += M*(-1)^(x+y)*(+1 up / -1 down)."""
+    cluster only: Hloc(i,i,s,s) += M*(-1)^(x+y)*(+1 up / -1 down), and
+    optionally a staggered charge field cdw*(-1)^(x+y) on both spins (the
+    surrogate's fourth input on a one-orbital cluster, where a uniform
+    orbital energy would only repeat mu')."""
     nlat = nx * ny
     tp = t if tprime is None else tprime
     cfg = lanczos_cfg(Nlat=nlat, Norb=1, Nspin=nspin, Uloc=[U], hfmode=0, xmu=xmu,
@@ -135,6 +138,7 @@ def square(nx: int = 4, ny: int = 3, U: float = 8.0, xmu: float = 4.0, t: float 
             for s in range(nspin):
                 sz = 1.0 if s == 0 else -1.0
                 H[i, i, s, s, 0, 0] += -mu_shift + (maf * (-1) ** (x + y) * sz if nspin == 2 else 0.0)
+                H[i, i, s, s, 0, 0] += cdw * (-1) ** (x + y)
     nk = nkx * nky
     Hk = _zeros(nlat, nlat, nspin, nspin, 1, 1, nk)
     base = _zeros(nlat, nlat, nspin, nspin, 1, 1)
@@ -156,7 +160,7 @@ def square(nx: int = 4, ny: int = 3, U: float = 8.0, xmu: float = 4.0, t: float 
                     Hk[i1, i2, s, s, 0, 0, ik] += -t * np.exp(-1j * kyN)
             ik += 1
     return SolvePoint(cfg, H, Hk, label=f"square{nx}x{ny} M={maf:.4f}",
-                      params={"maf": maf, "tprime": tp, "mu_shift": mu_shift})
+                      params={"maf": maf, "tprime": tp, "mu_shift": mu_shift, "cdw": cdw})
 
 
 # ---------------------------------------------------------------------------
