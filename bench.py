@@ -314,8 +314,8 @@ def run_gpu(args):
         s.close()
         out["hxv_single_4x4"] = hxv_single_4x4()
         out["finite_t"] = finite_t_sample(cpu=(world == 1 and not args.no_cpu))
-        out["c3_bath_plain"] = batch_sample("c3")
-        out["c4_bhz_plain"] = batch_sample("c4")
+        out["batched_c3"] = batched_block("c3", args.batch_c3, 4, 2)
+        out["batched_c4"] = batched_block("c4", args.batch_c4, 8, 2)
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample, _ = cpu_sample(pts[0], os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -367,39 +367,66 @@ def finite_t_sample(reps: int = 3, cpu: bool = True) -> dict:
     return out
 
 
-def batch_sample(which: str) -> dict:
-    """Omega evals/s of the plain path (one point after another through
-    vca_gpu_solve_batch, H_k uploaded once) on the first points of the C3
-    batch (2x2 cluster + 8 bath levels, 24x24 k, 200-step chains, 4096-node
-    rule) or the C4 batch (BHZ 2x2, Norb=2, Nspin=2, 48x48 k, 200-step
-    chains, 4096-node rule), after one warm-up point."""
+def batch_points(which: str, B: int):
+    """The first B points of the C3 batch (2x2 cluster + 8 bath levels, U=4,
+    24x24 k, 200-step chains, 4096-node rule) or of the C4 batch (BHZ 2x2,
+    Norb=2, Nspin=2, 48x48 k, 200-step chains, 4096-node rule), Hk shared."""
     import numpy as np
     from vca_gb300 import clusters
-    from vca_gb300.solver import VcaSolver
     if which == "c3":
-        pts = clusters.batch_square_bath(B=5)
+        pts = clusters.batch_square_bath(B=B)
         desc = "C3: 2x2 Hubbard + 8 bath levels, U=4, 24x24 k, 200-step chains, 4096 nodes"
     else:
         rng = np.random.Generator(np.random.PCG64(20261203 + 4))
-        prm = rng.uniform([1.5, -0.2], [2.5, 0.2], size=(17, 2))
+        prm = rng.uniform([1.5, -0.2], [2.5, 0.2], size=(B, 2))
         base = clusters.bhz(mass=2.0, delta=0.0)  # H_k (48x48) is the same for every point
         pts = [clusters.bhz(mass=p[0], delta=p[1], nk1=1) for p in prm]
         for p in pts:
             p.Hk = base.Hk
         desc = "C4: BHZ 2x2, Norb=2, Nspin=2, 48x48 k, 200-step chains, 4096 nodes"
-    cfg = pts[0].cfg
+    return pts, desc
+
+
+def _solve_points(pts, batch_loop: int, sector_at_a_time: int = 0):
+    import numpy as np
+    from vca_gb300.solver import VcaSolver
+    cfg = pts[0].cfg.copy()
+    cfg.batch_loop, cfg.sector_at_a_time = batch_loop, sector_at_a_time
     s = VcaSolver(cfg, pts[0].bath_h, pts[0].bath_v)
-    s.solve(pts[0].Hloc, pts[0].Hk, pts[0].bath_h, pts[0].bath_v)
-    rest = pts[1:]
-    Hl = np.stack([p.Hloc for p in rest], axis=-1)
-    bh = np.stack([p.bath_h for p in rest], axis=-1) if rest[0].bath_h is not None else None
-    bv = np.stack([p.bath_v for p in rest], axis=-1) if rest[0].bath_v is not None else None
+    s.solve(pts[0].Hloc, pts[0].Hk, pts[0].bath_h, pts[0].bath_v)  # warm-up (Hk upload, node rule)
+    Hl = np.stack([p.Hloc for p in pts], axis=-1)
+    bh = np.stack([p.bath_h for p in pts], axis=-1) if pts[0].bath_h is not None else None
+    bv = np.stack([p.bath_v for p in pts], axis=-1) if pts[0].bath_v is not None else None
+    s.synchronize()
     t0 = time.perf_counter()
-    om = s.solve_batch(Hl, rest[0].Hk, bh, bv)
+    om = s.solve_batch(Hl, pts[0].Hk, bh, bv)
     dt = time.perf_counter() - t0
     s.close()
-    return {"workload": desc, "points": len(rest), "value": len(rest) / dt, "unit": "Omega evals/s",
-            "ms_per_eval": round(1e3 * dt / len(rest), 1), "omega_first": float(om[0])}
+    return om, dt
+
+
+def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
+    """Omega evals/s of the batched form (vca_gpu_solve_batch, B points in
+    one call) against the plain path on the same points: one point after
+    another through the per-point path (every sector of a point in one
+    batched search), and the reference's loop structure (one sector per
+    Lanczos run).  Host arrays in, Omega out; wall time of the call."""
+    pts, desc = batch_points(which, B)
+    om_b, t_b = _solve_points(pts, 0)
+    om_l, t_l = _solve_points(pts[:n_loop], 1)
+    om_s, t_s = _solve_points(pts[:n_sat], 1, 1)
+    d_loop = max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(om_b[:n_loop], om_l))
+    d_sat = max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(om_b[:n_sat], om_s))
+    v_b, v_l, v_s = B / t_b, n_loop / t_l, n_sat / t_s
+    return {"workload": desc, "unit": "Omega evals/s",
+            "batched": {"points": B, "value": round(v_b, 4), "ms_per_eval": round(1e3 * t_b / B, 2)},
+            "plain_per_point": {"points": n_loop, "value": round(v_l, 4), "ms_per_eval": round(1e3 * t_l / n_loop, 2),
+                                "what": "one point after another, every sector of a point in one batched search"},
+            "plain_sector_at_a_time": {"points": n_sat, "value": round(v_s, 4),
+                                       "ms_per_eval": round(1e3 * t_s / n_sat, 2),
+                                       "what": "one point and one sector at a time (the reference's loops)"},
+            "ratio_vs_sector_at_a_time": round(v_b / v_s, 2), "ratio_vs_per_point": round(v_b / v_l, 2),
+            "max_rel_dOmega_vs_plain": max(d_loop, d_sat)}
 
 
 def hxv_single_4x4(reps: int = 10) -> dict:
@@ -489,6 +516,9 @@ def main():
     ap.add_argument("--profile-hxv1", action="store_true",
                     help="profiling mode: single-vector H x v on sector (8,8) of the 4x4 cluster")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--batch-c3", type=int, default=32, help="points of the C3 batch timed in the batched block")
+    ap.add_argument("--batch-c4", type=int, default=256, help="points of the C4 batch timed in the batched block")
+    ap.add_argument("--batched-only", action="store_true", help="only the batched block (C3 and C4)")
     ap.add_argument("--hxv-variant", type=int, default=2,
                     help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
     args = ap.parse_args()
@@ -500,6 +530,12 @@ def main():
         from vca_gb300 import build as vbuild
         vbuild.build()
         print(json.dumps(hxv_single_4x4(args.reps)))
+        return 0
+    if args.batched_only:
+        from vca_gb300 import build as vbuild
+        vbuild.build()
+        print(json.dumps({"batched_c3": batched_block("c3", args.batch_c3, 4, 2),
+                          "batched_c4": batched_block("c4", args.batch_c4, 8, 2)}))
         return 0
     if args.impl == "reference":
         return run_reference(args)

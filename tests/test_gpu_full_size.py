@@ -14,7 +14,16 @@ through identities that hold at any size:
   relative);
 * the fixed-point and the FP64 arithmetic give the same Omega (1e-10
   relative).
+
+It is also checked directly against the oracle at points of the benchmark's
+M sweep (M = 0.1 and M = 0, sweep points 5 and 0), from the fixtures
+tests/golden/config_c2_m05.npz / config_c2_m00.npz that
+tests/golden/make_golden.py writes (tens of minutes of oracle time each):
+E_gs, the Omega integral and Omega at 1e-10 relative, every sector energy at
+1e-10, the ground-state sectors, G'(i w) at 1e-8 absolute -- for the default
+(fixed-point) arithmetic and for FP64.
 """
+import os
 import numpy as np
 import pytest
 
@@ -22,6 +31,8 @@ from vca_gb300 import clusters
 from vca_gb300.solver import VcaSolver
 
 pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def bench_point(maf, arith=0):
@@ -73,3 +84,24 @@ def test_full_size_fixed_point_matches_fp64():
         assert s.arith_info()[0] == (1 if arith == 2 else 0)
         s.close()
     assert abs(vals[0] - vals[1]) < 1e-10 * abs(vals[1]), vals
+
+
+@pytest.mark.parametrize("idx", [5, 0])
+@pytest.mark.parametrize("arith", [0, 1], ids=["default", "fp64"])
+def test_full_size_points_match_the_oracle(idx, arith):
+    path = os.path.join(GOLD, f"config_c2_m{idx:02d}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"{os.path.basename(path)} not generated")
+    fx = np.load(path)
+    m = float(np.linspace(0.0, 0.3, 16)[idx])
+    pt = bench_point(m, arith)
+    s = VcaSolver(pt.cfg)
+    om = s.solve(pt.Hloc, pt.Hk)
+    egs, oi = s.energies()
+    rel = lambda a, b: abs(a - b) / max(1.0, abs(b))  # noqa: E731
+    assert rel(om, float(fx["sft"])) < 1e-10, (om, float(fx["sft"]))
+    assert rel(egs, float(fx["egs"])) < 1e-10 and rel(oi, float(fx["omega_int"])) < 1e-10
+    assert sorted(x[0] for x in s.states()) == sorted(int(v) for v in fx["states"])
+    np.testing.assert_allclose(s.sector_energies(), fx["sector_e"], rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(s.gf_cluster(1j * fx["wg"]), fx["g"], rtol=0, atol=1e-8)
+    s.close()

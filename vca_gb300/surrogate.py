@@ -122,3 +122,155 @@ def umma_gemm_check(A_bits: np.ndarray, B_bits: np.ndarray, C: Optional[np.ndarr
     _check(_lib().vca_umma_gemm_check(A_bits.ctypes.data_as(u16), B_bits.ctypes.data_as(u16), _fp(out), M, K,
                                       1 if accumulate else 0))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Stationary-point searches of Omega over a box of variational parameters
+# ---------------------------------------------------------------------------
+class CountingSolver:
+    """Wraps a plain solve p -> Omega and counts the calls (the cost the
+    searches are compared on)."""
+
+    def __init__(self, solve):
+        self.solve = solve
+        self.calls = 0
+        self.log = []
+
+    def __call__(self, p):
+        self.calls += 1
+        v = float(self.solve(np.asarray(p, dtype=np.float64)))
+        self.log.append((np.array(p, dtype=np.float64), v))
+        return v
+
+
+def newton_fd_search(f, p0, lo, hi, h_frac=1e-3, tol=1e-7, maxit=25):
+    """The plain search: Newton's method on grad Omega = 0 with the gradient
+    and Hessian from central differences of plain solves (1 + 2d + 2d(d-1)
+    calls per iteration).  It finds saddle points as well as minima, which
+    the drivers' minimisers (brent, fmin_bfgs) do not.  Stops when the
+    Newton step is below tol of the box half-width in every coordinate."""
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    d = len(lo)
+    hw = 0.5 * (hi - lo)
+    h = h_frac * hw
+    p = np.array(p0, dtype=np.float64)
+    E = np.eye(d)
+    it = 0
+    for it in range(1, maxit + 1):
+        f0 = f(p)
+        fp = np.array([f(p + h[i] * E[i]) for i in range(d)])
+        fm = np.array([f(p - h[i] * E[i]) for i in range(d)])
+        g = (fp - fm) / (2 * h)
+        H = np.diag((fp - 2 * f0 + fm) / h ** 2)
+        for i in range(d):
+            for j in range(i + 1, d):
+                a = f(p + h[i] * E[i] + h[j] * E[j])
+                b = f(p + h[i] * E[i] - h[j] * E[j])
+                c = f(p - h[i] * E[i] + h[j] * E[j])
+                e = f(p - h[i] * E[i] - h[j] * E[j])
+                H[i, j] = H[j, i] = (a - b - c + e) / (4 * h[i] * h[j])
+        step = -np.linalg.solve(H, g)
+        s = np.max(np.abs(step) / hw)
+        if s > 0.5:  # damp long steps
+            step *= 0.5 / s
+        p = np.clip(p + step, lo, hi)
+        if np.max(np.abs(step) / hw) < tol:
+            break
+    return p, f(p), it
+
+
+class BoxSurrogate:
+    """The network on a box of variational parameters: inputs scaled to
+    [-1, 1]^d, Omega shifted and scaled to unit spread by the first fit."""
+
+    def __init__(self, lo, hi, seed=20261203, capacity=1024, **net_kw):
+        self.lo, self.hi = np.asarray(lo, float), np.asarray(hi, float)
+        self.d = len(self.lo)
+        net_kw.setdefault("grad_weight", 0.0)  # values only: no gradient targets
+        self.net = SurrogateNet(n_in=self.d, capacity=capacity, seed=seed, **net_kw)
+        self.mu = self.sd = None
+
+    def close(self):
+        self.net.close()
+
+    def x(self, P):
+        return 2.0 * (np.atleast_2d(P) - self.lo) / (self.hi - self.lo) - 1.0
+
+    def p(self, X):
+        return self.lo + 0.5 * (np.atleast_2d(X) + 1.0) * (self.hi - self.lo)
+
+    def fit(self, P, Om, steps=3000):
+        Om = np.asarray(Om, float)
+        if self.mu is None:
+            self.mu, self.sd = float(np.mean(Om)), float(max(np.std(Om), 1e-12))
+        self.net.set_data(self.x(P), (Om - self.mu) / self.sd, None)
+        return self.net.train(steps)
+
+    def predict(self, P):
+        f, df = self.net.predict(self.x(P))
+        return self.mu + self.sd * f, df * self.sd * 2.0 / (self.hi - self.lo)
+
+    def stationary(self, p_start, h=0.02, iters=40):
+        """Newton on the network's input gradient (exact, from its tangent
+        rows); its Hessian by central differences of that gradient, all 2d
+        points in one prediction call."""
+        x = self.x(p_start)[0]
+        d = self.d
+        for _ in range(iters):
+            pts = np.vstack([x] + [x + h * e for e in np.eye(d)] + [x - h * e for e in np.eye(d)])
+            _, g = self.net.predict(pts)
+            H = (g[1:1 + d] - g[1 + d:]).T / (2 * h)
+            H = 0.5 * (H + H.T)
+            step = -np.linalg.lstsq(H, g[0], rcond=None)[0]
+            s = np.max(np.abs(step))
+            if s > 0.25:
+                step *= 0.25 / s
+            x = np.clip(x + step, -1.0, 1.0)
+            if s < 1e-6:
+                break
+        return self.p(x)[0]
+
+
+def surrogate_search(f, lo, hi, p0, n_design=12, stencil=0.05, rounds=3, steps=3000, tol=2e-3, seed=20261203,
+                     **net_kw):
+    """Surrogate-guided stationary-point search.  The network is fitted to a
+    space-filling design of plain solves (a Latin hypercube plus p0), its own
+    stationary point (Newton on the network from p0) is proposed and re-solved
+    by the plain path, a small axial stencil of plain solves around the
+    proposal is added, and the network is refitted; the rounds stop when two
+    proposals agree to tol of the box half-width.  Returns the last verified
+    point, its plain Omega, and per round the surrogate's error there."""
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    d = len(lo)
+    rng = np.random.default_rng(seed)
+    u = (np.argsort(rng.random((n_design, d)), axis=0) + rng.random((n_design, d))) / n_design
+    P = [np.asarray(p0, float)] + [lo + ui * (hi - lo) for ui in u]
+    Om = [f(p) for p in P]
+    S = BoxSurrogate(lo, hi, seed=seed, **net_kw)
+    history = []
+    prev = None
+    p_star, om_star = P[0], Om[0]
+    try:
+        for r in range(rounds):
+            S.fit(np.array(P), np.array(Om), steps=steps)
+            cand = S.stationary(p0 if prev is None else prev)
+            pred = float(S.predict(cand[None])[0][0])
+            om_c = f(cand)  # every accepted point is re-solved by the plain path
+            history.append({"point": cand.tolist(), "omega": om_c, "surrogate": pred,
+                            "surrogate_error": abs(pred - om_c)})
+            P.append(cand)
+            Om.append(om_c)
+            p_star, om_star = cand, om_c
+            if prev is not None and np.max(np.abs(cand - prev) / (0.5 * (hi - lo))) < tol:
+                break
+            if r + 1 < rounds:
+                hw = stencil * 0.5 * (hi - lo)
+                for i in range(d):
+                    for sgn in (1.0, -1.0):
+                        q = np.clip(cand + sgn * hw[i] * np.eye(d)[i], lo, hi)
+                        P.append(q)
+                        Om.append(f(q))
+            prev = cand
+    finally:
+        S.close()
+    return p_star, om_star, history
