@@ -32,6 +32,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Omega evals/sec (plain GPU path, |dOmega|<=1e-10 vs FP64 oracle)"
+# the arithmetic the timed path runs: the 4x3 Hubbard Hamiltonian is real with
+# one hopping magnitude, so the Lanczos vectors are int64 fixed point (2^-59)
+# with exact int128 dot products, the scalars and Omega FP64
+DTYPE = "fx64 vectors (Q59, int128 dots) / f64 scalars and Omega"
+DTYPE_REF = "f64"
 UNIT = "Omega evals/s"
 WORKLOAD = ("square4x3 Hubbard U=8 Nspin=2, M_AF sweep 16 pts [0,0.3], 32x32 k-grid, "
             "200-step GF chains (chan4), 8192-node Omega rule")
@@ -125,6 +130,8 @@ def build_points():
 # CPU timing of the oracle on a bounded sample of one Omega evaluation
 # ---------------------------------------------------------------------------
 def cpu_sample(pt, threads: int):
+    """(estimated Omega evals/s, description, estimated seconds per eval,
+    measured seconds of the sample)."""
     import numpy as np
     from oracle import oracle as orc
     from oracle.oracle import Oracle
@@ -133,6 +140,7 @@ def cpu_sample(pt, threads: int):
     Ns = o.Ns
     big = 1 + 6 + 6 * (Ns + 1)         # sector (6,6), dim 853,776
     tgt = 1 + 6 + 7 * (Ns + 1)         # GF target sector (7,6), dim 731,808
+    t_all = time.perf_counter()
     t0 = time.perf_counter()
     e, psi, iters = o.lanczos_gs(big)
     t_gs = time.perf_counter() - t0
@@ -159,28 +167,38 @@ def cpu_sample(pt, threads: int):
               f"[{iters} its, {t_gs:.2f}s] scaled by total/largest sector dim; {nch} of {chains} "
               f"200-step chains on sector (7,6) [{t_chain:.2f}s each]; {nn} of 8192 Omega nodes "
               f"[{t_node * 1e3:.1f}ms each]; one eval estimated at {total:.0f}s")
-    return 1.0 / total, sample, total
+    return 1.0 / total, sample, total, time.perf_counter() - t_all
 
 
 def run_reference(args):
+    """The reference arm: the oracle port (the Fortran reference does not
+    build here) on all host threads.  One step is one bounded sample of an
+    Omega evaluation at the benchmark configuration (the largest sector's
+    ground-state Lanczos, 2 of the 1104 chains, 8 of the 8192 Omega nodes);
+    ms_per_step is that sample's measured wall time, and value the Omega
+    evals/s the sample implies (its parts scaled to a whole evaluation)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     pts = build_points()
-    vals = []
+    vals, walls = [], []
+    sample = ""
+    est = 0.0
     for s in range(args.warmup + args.steps):
-        v, sample, tot = cpu_sample(pts[s % len(pts)], threads)
+        v, sample, est, wall = cpu_sample(pts[s % len(pts)], threads)
         if s >= args.warmup:
             vals.append(v)
+            walls.append(wall)
     value = sum(vals) / len(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host threads"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(walls) / len(walls),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_REF,
+        "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host threads",
+                                        "step": "one bounded sample of an Omega evaluation"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "estimated_seconds_per_eval": round(est, 1)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -295,7 +313,7 @@ def run_gpu(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPE, "data": "synthetic",
         "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (chain column batches 2.3 GB per buffer)",
                    "stage_ms_last_warmup": [round(x, 1) for x in stage_ms]},
@@ -307,6 +325,8 @@ def run_gpu(args):
     if roof is not None:
         out["roofline"] = roof
     if rank == 0:
+        out["accuracy"] = accuracy_check(pts, cfg0)
+    if rank == 0:
         # single-vector H x v on the half-filled 4x4 sector (the largest
         # sector of the 4x4 cluster), the vector size the roofline target
         # of this path is stated for; measured after the solves (it replaces
@@ -317,7 +337,7 @@ def run_gpu(args):
         out["batched_c3"] = batched_block("c3", args.batch_c3, 4, 2)
         out["batched_c4"] = batched_block("c4", args.batch_c4, 8, 2)
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, sample, _ = cpu_sample(pts[0], os.cpu_count() or 1)
+        v, sample, _, _ = cpu_sample(pts[0], os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                                "sample": sample}
     if rank == 0:
@@ -327,6 +347,29 @@ def run_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def accuracy_check(pts, cfg0, idx: int = 5) -> dict:
+    """Omega of sweep point idx (M = 0.1) in the timed arithmetic and in FP64,
+    and against the oracle's value at exactly this configuration
+    (tests/golden/config_c2_m05.npz, written by tests/golden/make_golden.py)."""
+    import numpy as np
+    from vca_gb300.solver import VcaSolver
+    p = pts[idx]
+    vals = {}
+    for name, arith in (("timed", cfg0.arith), ("fp64", 1)):
+        cfg = cfg0.copy()
+        cfg.arith = arith
+        s = VcaSolver(cfg)
+        vals[name] = s.solve(p.Hloc, p.Hk)
+        s.close()
+    rel = lambda a, b: abs(a - b) / max(1.0, abs(b))  # noqa: E731
+    out = {"point": f"M = {p.params['maf']:.4f}", "omega": vals["timed"],
+           "omega_fx_vs_fp64": rel(vals["timed"], vals["fp64"])}
+    gold = os.path.join(ROOT, "tests", "golden", f"config_c2_m{idx:02d}.npz")
+    if os.path.exists(gold):
+        out["omega_vs_oracle_fixture"] = rel(vals["timed"], float(np.load(gold)["sft"]))
+    return out
 
 
 def finite_t_point():
@@ -401,8 +444,9 @@ def _solve_points(pts, batch_loop: int, sector_at_a_time: int = 0):
     t0 = time.perf_counter()
     om = s.solve_batch(Hl, pts[0].Hk, bh, bv)
     dt = time.perf_counter() - t0
+    stages = s.timings(batched=not batch_loop)
     s.close()
-    return om, dt
+    return om, dt, stages
 
 
 def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
@@ -412,14 +456,16 @@ def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
     batched search), and the reference's loop structure (one sector per
     Lanczos run).  Host arrays in, Omega out; wall time of the call."""
     pts, desc = batch_points(which, B)
-    om_b, t_b = _solve_points(pts, 0)
-    om_l, t_l = _solve_points(pts[:n_loop], 1)
-    om_s, t_s = _solve_points(pts[:n_sat], 1, 1)
+    om_b, t_b, st_b = _solve_points(pts, 0)
+    om_l, t_l, _ = _solve_points(pts[:n_loop], 1)
+    om_s, t_s, _ = _solve_points(pts[:n_sat], 1, 1)
     d_loop = max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(om_b[:n_loop], om_l))
     d_sat = max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(om_b[:n_sat], om_s))
     v_b, v_l, v_s = B / t_b, n_loop / t_l, n_sat / t_s
     return {"workload": desc, "unit": "Omega evals/s",
-            "batched": {"points": B, "value": round(v_b, 4), "ms_per_eval": round(1e3 * t_b / B, 2)},
+            "batched": {"points": B, "value": round(v_b, 4), "ms_per_eval": round(1e3 * t_b / B, 2),
+                        "stage_ms": dict(zip(["tables", "search", "eigenvectors", "chains", "omega",
+                                              "closing_plain_solve"], [round(x, 1) for x in st_b]))},
             "plain_per_point": {"points": n_loop, "value": round(v_l, 4), "ms_per_eval": round(1e3 * t_l / n_loop, 2),
                                 "what": "one point after another, every sector of a point in one batched search"},
             "plain_sector_at_a_time": {"points": n_sat, "value": round(v_s, 4),

@@ -447,7 +447,10 @@ int vca_gpu_solve_resident(const double* Hloc, const double* bath_h, const doubl
 /* Kernel launches issued by the library since it was loaded. */
 int64_t vca_gpu_kernel_launches(void);
 /* Wall-clock milliseconds of the last solve's stages: [0] one-body tables,
- * [1] sector diagonalisation, [2] Green's function chains, [3] Omega. */
+ * [1] sector diagonalisation, [2] Green's function chains, [3] Omega; with
+ * n >= 10 also the last batched-form vca_gpu_solve_batch's stages over all
+ * its points: [4] tables, [5] ground-state search, [6] eigenvectors,
+ * [7] chains, [8] Omega, [9] the closing plain solve of the last point. */
 int vca_gpu_get_timings(double* ms, int32_t n);
 /* Arithmetic of the loaded Hamiltonian: *fx = 1 when the fixed-point path is
  * active, with vector scale 2^-F and H v scale 2^-G.  In that case the device
@@ -503,9 +506,12 @@ int vca_mlp_finalize(void);
 int64_t vca_mlp_param_count(void);
 int vca_mlp_get_params(float* out, int64_t n);
 int vca_mlp_set_params(const float* in, int64_t n); /* also resets Adam */
-/* Training set: x[n][n_in], y[n], dy[n][n_in] (dy NULL: zero targets, use
- * grad_weight = 0 for a value-only fit). */
-int vca_mlp_set_data(int32_t n, const double* x, const double* y, const double* dy);
+/* Training set: x[n][n_in], y[n], dy[n][n_in] and per-sample weights gw[n]
+ * of the gradient term (the loss of sample j uses grad_weight * gw[j]; gw
+ * NULL: all 1; dy NULL: zero targets -- give samples without gradient data
+ * gw = 0). */
+int vca_mlp_set_data(int32_t n, const double* x, const double* y, const double* dy,
+                     const double* gw);
 /* Loss and its gradient with respect to every parameter at the current
  * weights (no update): the check against the CPU restatement. */
 int vca_mlp_loss_grad(double* loss, float* grad, int64_t n);

@@ -99,10 +99,12 @@ def forward(p: np.ndarray, x: np.ndarray, bf16: bool = False, tangents: bool = T
     return f, g, cache
 
 
-def loss_grad(p: np.ndarray, x: np.ndarray, y: np.ndarray, dy: np.ndarray, lam: float, bf16: bool = False):
-    """Mean over samples of (f - y)^2 + lam |df/dx - dy|^2, and its gradient
-    with respect to the flat parameters (reverse pass written out)."""
+def loss_grad(p: np.ndarray, x: np.ndarray, y: np.ndarray, dy: np.ndarray, lam, bf16: bool = False):
+    """Mean over samples of (f - y)^2 + lam_j |df/dx - dy|^2, and its gradient
+    with respect to the flat parameters (reverse pass written out); lam is a
+    scalar or one weight per sample."""
     n, nin = x.shape
+    lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (n,))
     r = bf16_round if bf16 else (lambda a: a)
     f, g, c = forward(p, x, bf16=bf16)
     P = c["P"]
@@ -110,7 +112,7 @@ def loss_grad(p: np.ndarray, x: np.ndarray, y: np.ndarray, dy: np.ndarray, lam: 
     resd = g - dy
     loss = float(np.mean(res ** 2 + lam * np.sum(resd ** 2, axis=1)))
     e = 2.0 * res / n                                    # dL/df
-    ed = (2.0 * lam * resd / n).T                        # dL/d(df/dx_d), [nin][n]
+    ed = (2.0 * lam[:, None] * resd / n).T               # dL/d(df/dx_d), [nin][n]
     # head: f = w4 . a3 + b4, g_d = w4 . (s'(z3) zd3_d)
     s3 = c["a3"]
     gw4 = e @ s3 + np.einsum("dn,dno->o", ed, c["s1_3"][None] * c["zd3"])

@@ -68,17 +68,20 @@ def _blocks(nin):
     return o
 
 
-@pytest.mark.parametrize("S,lam", [(37, 0.7), (200, 1.0), (130, 0.0)])
-def test_loss_and_gradients_match_oracle(S, lam):
+@pytest.mark.parametrize("S,lam,mixed", [(37, 0.7, False), (200, 1.0, False), (130, 0.0, False), (61, 1.3, True)])
+def test_loss_and_gradients_match_oracle(S, lam, mixed):
     nin = 4
     rng = np.random.default_rng(S)
     x = rng.uniform(-1, 1, (S, nin))
     y = np.sin(x @ np.array([1.0, -0.5, 0.3, 0.8]))
     dy = np.cos(x)
+    gw = np.where(rng.random(S) < 0.5, 0.0, rng.uniform(0.5, 2.0, S)) if mixed else None
     net = _net(nin, grad_weight=lam)
     p = mlp.init_params(nin, seed=S).astype(np.float32)
     net.set_params(p)
-    net.set_data(x, y, dy)
+    net.set_data(x, y, dy, gw)
+    if mixed:
+        lam = lam * gw.astype(np.float32).astype(np.float64)
     loss, g = net.loss_grad()
     p64 = p.astype(np.float64)
     xs = x.astype(np.float32).astype(np.float64)  # the GPU holds x, y, dy in FP32

@@ -165,6 +165,9 @@ struct Ctx {
   std::vector<cd> hk_const;       // lso: value of Hk when equal at every k
   std::vector<char> hk_varying;   // lso: 1 when Hk differs between k-points
   double t_ms[4] = {0, 0, 0, 0};  // set_hamiltonian, diagonalise, chains, Omega
+  // the last vca_gpu_solve_batch in the batched form: tables, search,
+  // eigenvectors, chains, Omega, the closing plain solve (wall ms, all waves)
+  double bt_ms[6] = {0, 0, 0, 0, 0, 0};
   // GFmatrix read from a restart file (read_gfprime): replaces the solve's
   // tables for G'(z) and the channel getter until the next solve
   // Sigma read back by vca_read_impSigma: the Sigma getters return it until
@@ -2219,6 +2222,14 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
   for (int s = 1; s <= nsecs; s++) sumD += (int64_t)g->dimn[sec_nup(s)] * g->dimn[sec_ndw(s)];
   const cd XI(0.0, 1.0);
   const int L = c.Nlat * c.Norb;
+  for (double& t : g->bt_ms) t = 0.0;
+  double tmark = now_ms();
+  auto lap = [&](int stage) {
+    cudaStreamSynchronize(g->st);
+    const double t = now_ms();
+    g->bt_ms[stage] += t - tmark;
+    tmark = t;
+  };
   int p0 = 0;
   while (p0 < B) {
     // ---- 1. tables of a wave of points ---------------------------------------
@@ -2250,6 +2261,7 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
     g->ham_set = false;  // g->sp points into the wave's tables until the final plain solve
     const size_t es = cplx ? sizeof(double2) : sizeof(double);
     auto cleanup = [&]() { for (auto& t : tabs) t.ham.release(); };
+    lap(0);
     // ---- 2. every (point, sector) lowest energy ------------------------------
     TaskList S;
     int nmaxg = 1;
@@ -2292,6 +2304,7 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
       R.ar.release();
       if (e != cudaSuccess) { cleanup(); restore(); VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e)); }
     }
+    lap(1);
     // ---- 3. T=0 lists -------------------------------------------------------
     std::vector<std::vector<ListEntry>> lists(P);
     for (int q = 0; q < P; q++) {
@@ -2347,6 +2360,7 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
         VFAIL(VCA_ERR_CUDA, "batched eigenvector pass failed");
       }
     }
+    lap(2);
     // ---- 5. chains of every point --------------------------------------------
     std::vector<std::vector<BChain>> pch(P);
     {
@@ -2498,6 +2512,7 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
       }
     }
     RV.ar.release();  // the ground-state vectors are no longer needed
+    lap(3);
     // ---- 6. Omega per point --------------------------------------------------
     for (int q = 0; q < P; q++) {
       g->Hloc = tabs[q].Hloc;
@@ -2545,12 +2560,14 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
     }
     stores.release();
     cleanup();
+    lap(4);
     p0 = p1;
   }
   restore();
   // the context as a loop of vca_solve leaves it: the last point, plain path
   double last = 0.0;
   RCHK(solve_resident(hl(B - 1), bh(B - 1), bv(B - 1), &last));
+  lap(5);
   if (std::fabs(last - omega_out[B - 1]) > 1e-10 * std::max(1.0, std::fabs(last)))
     VFAIL(VCA_ERR_NUMERIC, "batched and plain Omega of the last point disagree");
   return VCA_OK;
@@ -3462,6 +3479,7 @@ int vca_gpu_get_timings(double* ms, int32_t n) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   if (!ms) VFAIL(VCA_ERR_ARG, "NULL output");
   for (int i = 0; i < n && i < 4; i++) ms[i] = g->t_ms[i];
+  for (int i = 4; i < n && i < 10; i++) ms[i] = g->bt_ms[i - 4];
   return VCA_OK;
 }
 

@@ -84,6 +84,7 @@ struct Mlp {
   float *P = nullptr, *G = nullptr, *Mo = nullptr, *Ve = nullptr;
   bf16 *W2t = nullptr, *W2Tt = nullptr, *W3t = nullptr, *W3Tt = nullptr;
   float *X = nullptr, *Y = nullptr, *DY = nullptr;  // training set
+  float* GW = nullptr;                              // per-sample weight of the gradient term
   float *Xq = nullptr;                              // prediction points
   bf16 *A1 = nullptr, *A1T = nullptr, *A2 = nullptr, *A2T = nullptr, *GZ = nullptr, *GZT = nullptr;
   float *Z2 = nullptr, *Z3 = nullptr, *GA = nullptr;
@@ -179,8 +180,8 @@ __global__ void k_mlp_head(const float* P, Offs of, const float* Z3, int S, int 
 }
 
 // per-sample loss and the seeds dL/df, dL/d(df/dx_d)
-__global__ void k_mlp_loss(const float* F, const float* Y, const float* DY, int S, int Spad, int nin, int nch,
-                           float lam, float* E, float* Lj) {
+__global__ void k_mlp_loss(const float* F, const float* Y, const float* DY, const float* GW, int S, int Spad,
+                           int nin, int nch, float lam0, float* E, float* Lj) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= Spad) return;
   if (j >= S) {
@@ -188,6 +189,7 @@ __global__ void k_mlp_loss(const float* F, const float* Y, const float* DY, int 
     return;
   }
   const float inv = 1.0f / (float)S;
+  const float lam = lam0 * GW[j];
   const float r0 = F[j] - Y[j];
   float L = r0 * r0;
   E[j] = 2.0f * r0 * inv;
@@ -373,7 +375,7 @@ void launch_loss_grad() {
   cudaStream_t st = m->st;
   launch_forward(m->X, S, nch);
   count_launch_external();
-  k_mlp_loss<<<nblk(Spad, 128), 128, 0, st>>>(m->F, m->Y, m->DY, S, Spad, m->nin, nch, (float)m->cfg.grad_weight,
+  k_mlp_loss<<<nblk(Spad, 128), 128, 0, st>>>(m->F, m->Y, m->DY, m->GW, S, Spad, m->nin, nch, (float)m->cfg.grad_weight,
                                               m->E, m->Lj);
   count_launch_external();
   k_mlp_head_bwd<<<nb, 256, 0, st>>>(m->P, m->of, m->Z3, m->E, S, Spad, nch, m->GZ, m->GZT, m->T4, m->GZB3);
@@ -485,7 +487,7 @@ int vca_mlp_init(const vca_mlp_config* cfg) {
       (rc = malloc_n(&m->Ve, np)) || (rc = malloc_n(&m->W2t, MW * MW)) || (rc = malloc_n(&m->W2Tt, MW * MW)) ||
       (rc = malloc_n(&m->W3t, MW * MW)) || (rc = malloc_n(&m->W3Tt, MW * MW)) ||
       (rc = malloc_n(&m->X, (size_t)m->cap * m->nin)) || (rc = malloc_n(&m->Y, m->cap)) ||
-      (rc = malloc_n(&m->DY, (size_t)m->cap * m->nin)) || (rc = malloc_n(&m->Xq, (size_t)m->cap * m->nin)) ||
+      (rc = malloc_n(&m->DY, (size_t)m->cap * m->nin)) || (rc = malloc_n(&m->GW, m->cap)) || (rc = malloc_n(&m->Xq, (size_t)m->cap * m->nin)) ||
       (rc = malloc_n(&m->A1, R * MW)) || (rc = malloc_n(&m->A1T, R * MW)) || (rc = malloc_n(&m->A2, R * MW)) ||
       (rc = malloc_n(&m->A2T, R * MW)) || (rc = malloc_n(&m->GZ, R * MW)) || (rc = malloc_n(&m->GZT, R * MW)) ||
       (rc = malloc_n(&m->Z2, R * MW)) || (rc = malloc_n(&m->Z3, R * MW)) || (rc = malloc_n(&m->GA, R * MW)) ||
@@ -540,13 +542,18 @@ int vca_mlp_set_params(const float* in, int64_t n) {
   return VCA_OK;
 }
 
-int vca_mlp_set_data(int32_t n, const double* x, const double* y, const double* dy) {
+int vca_mlp_set_data(int32_t n, const double* x, const double* y, const double* dy, const double* gw) {
   if (!m) MFAIL(VCA_ERR_STATE, "vca_mlp_init has not been called");
   if (n < 1 || n > m->cap) MFAIL(VCA_ERR_ARG, "sample count outside 1..capacity");
   if (!x || !y) MFAIL(VCA_ERR_ARG, "x and y are required");
   const int nin = m->nin;
-  std::vector<float> fx((size_t)n * nin), fy(n), fd((size_t)n * nin, 0.0f);
+  std::vector<float> fx((size_t)n * nin), fy(n), fd((size_t)n * nin, 0.0f), fw(n, 1.0f);
   for (size_t i = 0; i < fx.size(); i++) fx[i] = (float)x[i];
+  if (gw)
+    for (int i = 0; i < n; i++) {
+      if (!(gw[i] >= 0.0) || !std::isfinite(gw[i])) MFAIL(VCA_ERR_NUMERIC, "gradient weights must be finite and >= 0");
+      fw[i] = (float)gw[i];
+    }
   for (int i = 0; i < n; i++) fy[i] = (float)y[i];
   if (dy)
     for (size_t i = 0; i < fd.size(); i++) fd[i] = (float)dy[i];
@@ -557,6 +564,7 @@ int vca_mlp_set_data(int32_t n, const double* x, const double* y, const double* 
   MCU(cudaMemcpyAsync(m->X, fx.data(), fx.size() * sizeof(float), cudaMemcpyHostToDevice, m->st));
   MCU(cudaMemcpyAsync(m->Y, fy.data(), fy.size() * sizeof(float), cudaMemcpyHostToDevice, m->st));
   MCU(cudaMemcpyAsync(m->DY, fd.data(), fd.size() * sizeof(float), cudaMemcpyHostToDevice, m->st));
+  MCU(cudaMemcpyAsync(m->GW, fw.data(), fw.size() * sizeof(float), cudaMemcpyHostToDevice, m->st));
   MCU(cudaStreamSynchronize(m->st));
   if (n != m->S) drop_graph();
   m->S = n;

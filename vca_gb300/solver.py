@@ -163,7 +163,7 @@ def load(path: Optional[str] = None):
         "vca_mlp_param_count": (i64, []),
         "vca_mlp_get_params": (ctypes.c_int, [fp, i64]),
         "vca_mlp_set_params": (ctypes.c_int, [fp, i64]),
-        "vca_mlp_set_data": (ctypes.c_int, [i32, dp, dp, dp]),
+        "vca_mlp_set_data": (ctypes.c_int, [i32, dp, dp, dp, dp]),
         "vca_mlp_loss_grad": (ctypes.c_int, [dp, fp, i64]),
         "vca_mlp_train": (ctypes.c_int, [i32, dp]),
         "vca_mlp_predict": (ctypes.c_int, [i32, dp, dp, dp]),
@@ -264,10 +264,13 @@ class VcaSolver:
         check(self.L.vca_gpu_solve_resident(_dp(Hloc), _dp(bath_h), _dp(bath_v), ctypes.byref(out)))
         return out.value
 
-    def timings(self):
-        out = np.zeros(4)
-        check(self.L.vca_gpu_get_timings(_dp(out), 4))
-        return out
+    def timings(self, batched: bool = False):
+        """Stage wall times (ms) of the last solve, or with batched=True of
+        the last batched-form solve_batch (tables, search, eigenvectors,
+        chains, Omega, closing plain solve)."""
+        out = np.zeros(10)
+        check(self.L.vca_gpu_get_timings(_dp(out), 10))
+        return out[4:] if batched else out[:4]
 
     def arith_info(self):
         fx, F, G = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -85,11 +85,13 @@ class SurrogateNet:
         p = np.ascontiguousarray(p, dtype=np.float32)
         _check(self.L.vca_mlp_set_params(_fp(p), p.size))
 
-    def set_data(self, x, y, dy=None):
+    def set_data(self, x, y, dy=None, gw=None):
+        """gw[j]: weight of sample j's gradient term (None: 1 for every sample)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.ascontiguousarray(y, dtype=np.float64)
         dy = None if dy is None else np.ascontiguousarray(dy, dtype=np.float64)
-        _check(self.L.vca_mlp_set_data(len(y), _dp(x), _dp(y), _dp(dy)))
+        gw = None if gw is None else np.ascontiguousarray(gw, dtype=np.float64)
+        _check(self.L.vca_mlp_set_data(len(y), _dp(x), _dp(y), _dp(dy), _dp(gw)))
 
     def loss_grad(self):
         loss = ctypes.c_double()
@@ -179,14 +181,43 @@ def newton_fd_search(f, p0, lo, hi, h_frac=1e-3, tol=1e-7, maxit=25):
     return p, f(p), it
 
 
+def coordinate_brent_search(f, p0, lo, hi, kinds, xtol=1e-5, tol=1e-5, maxcycles=30):
+    """The drivers' tool applied per variable: Brent's method on one
+    parameter at a time (brent, drivers/vca_hm_chain1d.f90:104-108),
+    minimising Omega along the variables of kind "min" and maximising it
+    along those of kind "max", cycled until no parameter moves by more than
+    tol of its box half-width."""
+    import scipy.optimize
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    p = np.array(p0, dtype=np.float64)
+    hw = 0.5 * (hi - lo)
+    cyc = 0
+    for cyc in range(1, maxcycles + 1):
+        moved = 0.0
+        for i, kind in enumerate(kinds):
+            sg = 1.0 if kind == "min" else -1.0
+
+            def g(t, i=i, sg=sg):
+                q = p.copy()
+                q[i] = t
+                return sg * f(q)
+            r = scipy.optimize.minimize_scalar(g, bounds=(lo[i], hi[i]), method="bounded",
+                                               options={"xatol": xtol * hw[i]})
+            moved = max(moved, abs(r.x - p[i]) / hw[i])
+            p[i] = r.x
+        if moved < tol:
+            break
+    return p, f(p), cyc
+
+
 class BoxSurrogate:
     """The network on a box of variational parameters: inputs scaled to
-    [-1, 1]^d, Omega shifted and scaled to unit spread by the first fit."""
+    [-1, 1]^d, Omega shifted and scaled to unit spread by the first fit, and
+    its gradients scaled alike."""
 
     def __init__(self, lo, hi, seed=20261203, capacity=1024, **net_kw):
         self.lo, self.hi = np.asarray(lo, float), np.asarray(hi, float)
         self.d = len(self.lo)
-        net_kw.setdefault("grad_weight", 0.0)  # values only: no gradient targets
         self.net = SurrogateNet(n_in=self.d, capacity=capacity, seed=seed, **net_kw)
         self.mu = self.sd = None
 
@@ -199,29 +230,40 @@ class BoxSurrogate:
     def p(self, X):
         return self.lo + 0.5 * (np.atleast_2d(X) + 1.0) * (self.hi - self.lo)
 
-    def fit(self, P, Om, steps=3000):
+    def fit(self, P, Om, dOm=None, steps=3000):
+        """dOm[j]: the gradient at P[j] in parameter units, or a row of NaN
+        where none was measured (that sample's gradient term is off)."""
         Om = np.asarray(Om, float)
         if self.mu is None:
             self.mu, self.sd = float(np.mean(Om)), float(max(np.std(Om), 1e-12))
-        self.net.set_data(self.x(P), (Om - self.mu) / self.sd, None)
+        dy = gw = None
+        if dOm is not None:
+            dOm = np.asarray(dOm, float)
+            have = np.all(np.isfinite(dOm), axis=1)
+            dy = np.where(have[:, None], np.nan_to_num(dOm) * 0.5 * (self.hi - self.lo) / self.sd, 0.0)
+            gw = have.astype(float)
+        self.net.set_data(self.x(P), (Om - self.mu) / self.sd, dy, gw)
         return self.net.train(steps)
 
     def predict(self, P):
         f, df = self.net.predict(self.x(P))
         return self.mu + self.sd * f, df * self.sd * 2.0 / (self.hi - self.lo)
 
-    def stationary(self, p_start, h=0.02, iters=40):
-        """Newton on the network's input gradient (exact, from its tangent
-        rows); its Hessian by central differences of that gradient, all 2d
-        points in one prediction call."""
-        x = self.x(p_start)[0]
+    def hessian_x(self, x, h=0.02):
+        """The network's Hessian in scaled inputs: central differences of its
+        exact input gradient (tangent rows), 2d points in one prediction."""
         d = self.d
+        pts = np.vstack([x] + [x + h * e for e in np.eye(d)] + [x - h * e for e in np.eye(d)])
+        _, g = self.net.predict(pts)
+        H = (g[1:1 + d] - g[1 + d:]).T / (2 * h)
+        return g[0], 0.5 * (H + H.T)
+
+    def stationary(self, p_start, iters=40):
+        """Newton on the network's input gradient from p_start."""
+        x = self.x(p_start)[0]
         for _ in range(iters):
-            pts = np.vstack([x] + [x + h * e for e in np.eye(d)] + [x - h * e for e in np.eye(d)])
-            _, g = self.net.predict(pts)
-            H = (g[1:1 + d] - g[1 + d:]).T / (2 * h)
-            H = 0.5 * (H + H.T)
-            step = -np.linalg.lstsq(H, g[0], rcond=None)[0]
+            g, H = self.hessian_x(x)
+            step = -np.linalg.lstsq(H, g, rcond=None)[0]
             s = np.max(np.abs(step))
             if s > 0.25:
                 step *= 0.25 / s
@@ -231,46 +273,53 @@ class BoxSurrogate:
         return self.p(x)[0]
 
 
-def surrogate_search(f, lo, hi, p0, n_design=12, stencil=0.05, rounds=3, steps=3000, tol=2e-3, seed=20261203,
-                     **net_kw):
-    """Surrogate-guided stationary-point search.  The network is fitted to a
-    space-filling design of plain solves (a Latin hypercube plus p0), its own
-    stationary point (Newton on the network from p0) is proposed and re-solved
-    by the plain path, a small axial stencil of plain solves around the
-    proposal is added, and the network is refitted; the rounds stop when two
-    proposals agree to tol of the box half-width.  Returns the last verified
-    point, its plain Omega, and per round the surrogate's error there."""
+def surrogate_search(f, lo, hi, p0, n_design=6, h_frac=1e-3, rounds=8, steps=3000, omega_tol=1e-7,
+                     seed=20261203, grad_weight=1.0, **net_kw):
+    """Surrogate-guided stationary-point search.
+
+    The network is fitted to a space-filling design of plain solves (p0 and a
+    Latin hypercube of n_design points, values only).  Each round proposes
+    the network's stationary point (Newton on the network from the last
+    proposal), re-solves it by the plain path together with its gradient
+    from d forward differences of plain solves, adds that value and gradient
+    to the training set (the Sobolev term), and refits.  The plain solver is
+    the judge: the search stops when the measured gradient g at a proposal,
+    through the network's curvature H there, puts it within
+    |1/2 g^T H^-1 g| < omega_tol of the stationary value.  Returns the last
+    verified point, its plain Omega, and per round the surrogate's error."""
     lo, hi = np.asarray(lo, float), np.asarray(hi, float)
     d = len(lo)
+    hw = 0.5 * (hi - lo)
     rng = np.random.default_rng(seed)
     u = (np.argsort(rng.random((n_design, d)), axis=0) + rng.random((n_design, d))) / n_design
     P = [np.asarray(p0, float)] + [lo + ui * (hi - lo) for ui in u]
-    Om = [f(p) for p in P]
-    S = BoxSurrogate(lo, hi, seed=seed, **net_kw)
+    Om = [f(q) for q in P]
+    G = [np.full(d, np.nan) for _ in P]
+    S = BoxSurrogate(lo, hi, seed=seed, grad_weight=grad_weight, **net_kw)
     history = []
-    prev = None
-    p_star, om_star = P[0], Om[0]
+    cand, om_c = P[0], Om[0]
     try:
         for r in range(rounds):
-            S.fit(np.array(P), np.array(Om), steps=steps)
-            cand = S.stationary(p0 if prev is None else prev)
-            pred = float(S.predict(cand[None])[0][0])
+            S.fit(np.array(P), np.array(Om), np.array(G), steps=steps)
+            cand = S.stationary(cand)
+            pred, pgrad = S.predict(cand[None])
             om_c = f(cand)  # every accepted point is re-solved by the plain path
-            history.append({"point": cand.tolist(), "omega": om_c, "surrogate": pred,
-                            "surrogate_error": abs(pred - om_c)})
+            h = h_frac * hw
+            g = np.array([(f(np.clip(cand + h[i] * np.eye(d)[i], lo, hi)) - om_c) / h[i] for i in range(d)])
+            _, Hx = S.hessian_x(S.x(cand)[0])
+            gx = g * hw  # gradient in the scaled inputs
+            try:
+                est = abs(0.5 * gx @ np.linalg.solve(Hx * S.sd, gx))
+            except np.linalg.LinAlgError:
+                est = np.inf
+            history.append({"point": cand.tolist(), "omega": om_c, "surrogate": float(pred[0]),
+                            "surrogate_error": abs(float(pred[0]) - om_c),
+                            "gradient": g.tolist(), "omega_gap_estimate": float(est)})
             P.append(cand)
             Om.append(om_c)
-            p_star, om_star = cand, om_c
-            if prev is not None and np.max(np.abs(cand - prev) / (0.5 * (hi - lo))) < tol:
+            G.append(g)
+            if est < omega_tol:
                 break
-            if r + 1 < rounds:
-                hw = stencil * 0.5 * (hi - lo)
-                for i in range(d):
-                    for sgn in (1.0, -1.0):
-                        q = np.clip(cand + sgn * hw[i] * np.eye(d)[i], lo, hi)
-                        P.append(q)
-                        Om.append(f(q))
-            prev = cand
     finally:
         S.close()
-    return p_star, om_star, history
+    return cand, om_c, history
