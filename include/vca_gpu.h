@@ -65,7 +65,10 @@ typedef struct vca_config {
   int32_t Nlat;      /* NLAT       cluster sites                            */
   int32_t Nlat_bath; /* NLAT_BATH  bath "site" levels                       */
   int32_t Norb_bath; /* NORB_BATH  bath "orb" levels                        */
-  int32_t pad0;
+  int32_t no_sector_screen; /* no counterpart: 1 makes the batched form of      */
+                           /* vca_gpu_solve_batch search every (point, sector); */
+                           /* 0 (default) skips sectors whose one-body lower    */
+                           /* bound proves them above the T=0 window            */
   double Uloc[5];    /* ULOC       on-site interaction per orbital          */
   double Ust;        /* UST        inter-orbital opposite-spin interaction  */
   double Jh;         /* JH         Hund coupling (Ust-Jh parallel spins)    */
@@ -450,7 +453,8 @@ int64_t vca_gpu_kernel_launches(void);
  * [1] sector diagonalisation, [2] Green's function chains, [3] Omega; with
  * n >= 10 also the last batched-form vca_gpu_solve_batch's stages over all
  * its points: [4] tables, [5] ground-state search, [6] eigenvectors,
- * [7] chains, [8] Omega, [9] the closing plain solve of the last point. */
+ * [7] chains, [8] Omega, [9] the closing plain solve of the last point;
+ * with n >= 11, [10] the (point, sector) searches its screening skipped. */
 int vca_gpu_get_timings(double* ms, int32_t n);
 /* Arithmetic of the loaded Hamiltonian: *fx = 1 when the fixed-point path is
  * active, with vector scale 2^-F and H v scale 2^-G.  In that case the device
@@ -466,6 +470,11 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
 int vca_gpu_sector_row_order(int32_t isector, int64_t* order, int64_t cap);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);
+/* Lower bound of every sector's lowest energy for the loaded Hamiltonian
+ * (out[isector-1]): the one-body part's ground energy in that sector, valid
+ * when U, Ust and Ust - Jh are non-negative (VCA_ERR_UNSUPPORTED otherwise).
+ * The batched form skips sectors with it; no counterpart in the reference. */
+int vca_gpu_sector_bounds(double* out, int32_t n);
 /* QL sweeps allowed per eigenvalue when the chains' tridiagonals are turned
  * into poles and weights (default 60).
  * A chain that needs more makes the call that asked for poles (the channel

@@ -124,3 +124,30 @@ def test_batched_full_configs_against_the_oracle(which):
     for p, o in zip(pts[1:], om[1:]):
         r = VcaSolver(p.cfg, p.bath_h, p.bath_v)
         assert _rel(o, r.solve(p.Hloc, pts[0].Hk, p.bath_h, p.bath_v)) < E_TOL
+
+
+@pytest.mark.parametrize("name", ["bath2x2+4", "bhz", "square2x2_afm", "chain4"])
+def test_sector_bounds_are_below_every_sector_energy(name):
+    """The one-body lower bound the batched form screens sectors with is at
+    most each sector's lowest energy (plain solve, every sector searched)."""
+    pt = _small(name)[1]
+    s = VcaSolver(pt.cfg, pt.bath_h, pt.bath_v)
+    s.solve(pt.Hloc, pt.Hk, pt.bath_h, pt.bath_v)
+    e = s.sector_energies()
+    b = s.sector_bounds()
+    assert np.all(b <= e + 1e-9 * np.maximum(1.0, np.abs(e))), (b - e).max()
+
+
+def test_screened_and_full_batched_searches_agree():
+    """Screening skips (point, sector) searches; Omega is unchanged."""
+    pts = clusters.batch_square_bath(B=3, nk1=6, ngfiter=60, omega_nodes=256)
+    Hl, bh, bv = _stack(pts)
+    vals, skipped = [], []
+    for flag in (0, 1):
+        cfg = pts[0].cfg.copy()
+        cfg.no_sector_screen = flag
+        s = VcaSolver(cfg, pts[0].bath_h, pts[0].bath_v)
+        vals.append(s.solve_batch(Hl, pts[0].Hk, bh, bv))
+        skipped.append(s.timings(batched=True)[6])
+    np.testing.assert_allclose(vals[0], vals[1], rtol=E_TOL, atol=0)
+    assert skipped[0] > 0 and skipped[1] == 0, skipped

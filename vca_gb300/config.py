@@ -26,7 +26,7 @@ class VcaConfig(ctypes.Structure):
         ("Nlat", ctypes.c_int32),
         ("Nlat_bath", ctypes.c_int32),
         ("Norb_bath", ctypes.c_int32),
-        ("pad0", ctypes.c_int32),
+        ("no_sector_screen", ctypes.c_int32),
         ("Uloc", ctypes.c_double * 5),
         ("Ust", ctypes.c_double),
         ("Jh", ctypes.c_double),
@@ -85,8 +85,6 @@ class VcaConfig(ctypes.Structure):
     def as_dict(self) -> dict:
         out = {}
         for name, _ in self._fields_:
-            if name == "pad0":
-                continue
             v = getattr(self, name)
             out[name] = list(v) if name == "Uloc" else v
         return out

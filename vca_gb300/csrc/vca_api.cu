@@ -129,6 +129,7 @@ struct Ctx {
   };
   std::vector<PermTabs> fx_ptab[2];  // tables in perm order
   std::vector<HopPair> host_pairs;
+  size_t host_pairs_set0 = 0;  // pairs of the up set (the rest are the down set's)
   std::vector<double> host_eps_abs;  // per spin set: bound of |one-body energy|
   // finite temperature (LANC_NSTATES_TOTAL != 1, VCA_SETUP.f90:157-175); the
   // list cap is adjusted by every finite-T diagonalisation and carries over
@@ -168,6 +169,7 @@ struct Ctx {
   // the last vca_gpu_solve_batch in the batched form: tables, search,
   // eigenvectors, chains, Omega, the closing plain solve (wall ms, all waves)
   double bt_ms[6] = {0, 0, 0, 0, 0, 0};
+  int64_t bt_skipped = 0;  // (point, sector) searches the last batched solve skipped by their bound
   // GFmatrix read from a restart file (read_gfprime): replaces the solve's
   // tables for G'(z) and the channel getter until the next solve
   // Sigma read back by vca_read_impSigma: the Sigma getters return it until
@@ -376,6 +378,7 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
     if ((int)pairs.size() > VCA_MAX_PAIRS) VFAIL(VCA_ERR_UNSUPPORTED, "too many one-body pairs");
     if (set == 0) { g->host_pairs.clear(); g->host_eps_abs.clear(); }
     g->host_pairs.insert(g->host_pairs.end(), pairs.begin(), pairs.end());
+    if (set == 0) g->host_pairs_set0 = g->host_pairs.size();
     RCHK(g->ham.alloc(&g->d_pairs[set], pairs.size()));
     if (!pairs.empty())
       CUCHK(cudaMemcpyAsync(g->d_pairs[set], pairs.data(), pairs.size() * sizeof(HopPair),
@@ -2105,6 +2108,110 @@ static void gfm_drop() {
 // point leaves it (that point is solved once more on the plain path, which
 // must agree with its batched Omega to 1e-10).
 // ===========================================================================
+// Eigenvalues of a complex Hermitian n x n matrix (column-major), ascending:
+// cyclic Jacobi on the real symmetric 2n x 2n embedding [[Re, -Im], [Im, Re]],
+// whose spectrum is each eigenvalue twice.
+void herm_eigvals(int n, const std::vector<cd>& h, std::vector<double>& w) {
+  const int m = 2 * n;
+  std::vector<double> a((size_t)m * m);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      const cd z = h[i + (size_t)j * n];
+      a[i + (size_t)j * m] = z.real();
+      a[(i + n) + (size_t)(j + n) * m] = z.real();
+      a[(i + n) + (size_t)j * m] = z.imag();
+      a[i + (size_t)(j + n) * m] = -z.imag();
+    }
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < m; i++)
+      for (int j = 0; j < m; j++) {
+        tot += a[i + (size_t)j * m] * a[i + (size_t)j * m];
+        if (i != j) off += a[i + (size_t)j * m] * a[i + (size_t)j * m];
+      }
+    if (off <= 1e-30 * tot || off == 0.0) break;
+    for (int p = 0; p < m; p++)
+      for (int q = p + 1; q < m; q++) {
+        const double apq = a[p + (size_t)q * m];
+        if (apq == 0.0) continue;
+        const double app = a[p + (size_t)p * m], aqq = a[q + (size_t)q * m];
+        const double th = 0.5 * (aqq - app) / apq;
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < m; k++) {  // columns p, q
+          const double akp = a[k + (size_t)p * m], akq = a[k + (size_t)q * m];
+          a[k + (size_t)p * m] = c * akp - sn * akq;
+          a[k + (size_t)q * m] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < m; k++) {  // rows p, q
+          const double apk = a[p + (size_t)k * m], aqk = a[q + (size_t)k * m];
+          a[p + (size_t)k * m] = c * apk - sn * aqk;
+          a[q + (size_t)k * m] = sn * apk + c * aqk;
+        }
+      }
+  }
+  std::vector<double> d(m);
+  for (int i = 0; i < m; i++) d[i] = a[i + (size_t)i * m];
+  std::sort(d.begin(), d.end());
+  w.resize(n);
+  for (int i = 0; i < n; i++) w[i] = d[2 * i];
+}
+
+// Lower bounds on the lowest energy of every sector of the loaded
+// Hamiltonian, or an empty vector when none is available.  With every
+// interaction coefficient non-negative (U, Ust, Ust - Jh), H = H1 + Hint
+// with Hint >= 0, so E_min(n_up, n_dw) >= the ground energy of the one-body
+// part H1 in that sector: the sum of the n_up lowest levels of the up
+// one-body matrix (hops, level energies with -xmu and the HFMODE shifts) and
+// the n_dw lowest of the down one, plus the HFMODE constant.
+std::vector<double> sector_lower_bounds() {
+  const vca_config& c = g->cfg;
+  std::vector<double> out;
+  for (int o = 0; o < c.Norb; o++)
+    if (c.Uloc[o] < 0.0) return out;
+  if (c.Norb > 1 && (c.Ust < 0.0 || c.Ust - c.Jh < 0.0)) return out;
+  const int Ns = g->Ns, LC = c.Nlat * c.Norb;
+  const int nsets = (c.Nspin == 2) ? 2 : 1;
+  std::vector<double> lev[2];
+  for (int set = 0; set < nsets; set++) {
+    const int sidx = (set == 0) ? 0 : c.Nspin - 1;
+    std::vector<cd> h((size_t)Ns * Ns, cd(0.0, 0.0));
+    for (int il = 0; il < c.Nlat; il++)
+      for (int io = 0; io < c.Norb; io++) {
+        double e = g->Hloc[idx_nnn(c, il, il, sidx, sidx, io, io)].real() - c.xmu;
+        if (c.hfmode) {
+          e += -0.5 * c.Uloc[io];
+          if (c.Norb > 1) e += -0.5 * (2.0 * c.Ust - c.Jh) * (c.Norb - 1);
+        }
+        const int l = io + il * c.Norb;
+        h[l + (size_t)l * Ns] = e;
+      }
+    if (g->has_bath)
+      for (int lb = 0; lb < c.Nlat_bath; lb++)
+        for (int ob = 0; ob < c.Norb_bath; ob++) {
+          const int l = LC + lb * c.Norb_bath + ob;
+          h[l + (size_t)l * Ns] = g->bath_h[idx_bh(c, lb, lb, sidx, sidx, ob, ob)].real() - c.xmu;
+        }
+    // the hopping pairs of this spin set: set 0 owns [0, set0), set 1 the rest
+    const size_t q0 = (set == 0) ? 0 : g->host_pairs_set0;
+    const size_t q1 = (set == 0) ? g->host_pairs_set0 : g->host_pairs.size();
+    for (size_t q = q0; q < q1; q++) {
+      const HopPair& hp = g->host_pairs[q];
+      h[hp.i + (size_t)hp.j * Ns] += cd(hp.re, hp.im);  // c^dag_i c_j
+    }
+    herm_eigvals(Ns, h, lev[set]);
+  }
+  if (nsets == 1) lev[1] = lev[0];
+  std::vector<double> cum[2];
+  for (int set = 0; set < 2; set++) {
+    cum[set].assign(Ns + 1, 0.0);
+    for (int k = 0; k < Ns; k++) cum[set][k + 1] = cum[set][k] + lev[set][k];
+  }
+  out.assign(g->Nsectors, 0.0);
+  for (int s = 1; s <= g->Nsectors; s++) out[s - 1] = cum[0][sec_nup(s)] + cum[1][sec_ndw(s)] + g->md.c0;
+  return out;
+}
+
 struct PointTabs {
   Arena ham;
   std::vector<SpinSpace> sp[2];
@@ -2239,10 +2346,12 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
     const int P = (int)std::max<int64_t>(1, std::min<int64_t>(B - p0, (int64_t)(0.35 * (double)freeb / per_point)));
     const int p1 = p0 + P;
     std::vector<PointTabs> tabs(P);
+    std::vector<std::vector<double>> bnd(P);  // per point: lower bound of every sector's energy
     bool cplx = false;
     for (int q = 0; q < P; q++) {
       int rc = set_hamiltonian(hl(p0 + q), bh(p0 + q), bv(p0 + q));
       if (rc) { restore(); return rc; }
+      if (!c.no_sector_screen) bnd[q] = sector_lower_bounds();
       PointTabs& T = tabs[q];
       T.ham.ptrs.swap(g->ham.ptrs);  // the point keeps its tables; set_hamiltonian starts a new arena
       T.sp[0] = g->sp[0];
@@ -2262,24 +2371,33 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
     const size_t es = cplx ? sizeof(double2) : sizeof(double);
     auto cleanup = [&]() { for (auto& t : tabs) t.ham.release(); };
     lap(0);
-    // ---- 2. every (point, sector) lowest energy ------------------------------
-    TaskList S;
-    int nmaxg = 1;
-    for (int q = 0; q < P; q++)
-      for (int s = 1; s <= nsecs; s++) {
-        const int nu = sec_nup(s), nd = sec_ndw(s);
+    // ---- 2. the (point, sector) lowest energies ------------------------------
+    // Screened in two runs when a lower bound exists (sector_lower_bounds):
+    // first each point's two lowest-bound sectors, whose Ritz values give an
+    // upper bound E_up on its ground energy, then only the sectors whose
+    // bound lies below E_up + 20 GS_THRESHOLD.  A skipped sector's lowest
+    // level is above every level within 20 GS_THRESHOLD of the ground state,
+    // so the T=0 list (VCA_DIAG.f90:224-236) is the one of a full scan.
+    const int LDS = std::min(c.lanc_niter, 512) + 1;  // svec rows kept per (point, sector)
+    std::vector<double> theta((size_t)P * nsecs, INFINITY);
+    std::vector<int> mconv((size_t)P * nsecs, 0);
+    std::vector<double> svec_h((size_t)P * nsecs * LDS, 0.0);
+    std::vector<char> done((size_t)P * nsecs, 0);
+    auto run_search = [&](const std::vector<int>& which /* q * nsecs + (s - 1) */) -> int {
+      if (which.empty()) return VCA_OK;
+      TaskList S;
+      int nmaxg = 1;
+      for (int t : which) {
+        const int q = t / nsecs, sct = t % nsecs + 1;
+        const int nu = sec_nup(sct), nd = sec_ndw(sct);
         const int64_t D = (int64_t)g->dimn[nu] * g->dimn[nd];
-        S.add(view_tabs(tabs[q], nu, nd), D, s, 1);
+        S.add(view_tabs(tabs[q], nu, nd), D, sct, 1);
         nmaxg = std::max(nmaxg, (int)std::min<int64_t>(D, std::min(c.lanc_niter, 512)));
       }
-    const int ldg = nmaxg + 1;
-    std::vector<double> theta(S.secs.size());
-    std::vector<int> mconv(S.secs.size());
-    std::vector<double> svec_h;
-    {
+      const int ldg = nmaxg + 1;
       MtRun R;
       int rc = mt_alloc(R, S, ldg, es, false);
-      if (rc) { R.ar.release(); cleanup(); restore(); return rc; }
+      if (rc) { R.ar.release(); return rc; }
       std::vector<ChainMeta> meta(S.secs.size());
       for (size_t t = 0; t < S.secs.size(); t++)
         meta[t] = ChainMeta{1, (int)t, (int)std::min<int64_t>(S.secs[t].D, std::min(c.lanc_niter, 512)), 1, 0};
@@ -2292,56 +2410,99 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
           m64_launch_check(R.gp, R.b, c.gs_residual_tol, g->st);
           int undone = 0;
           cudaMemcpyAsync(&undone, R.b.undone, sizeof(int), cudaMemcpyDeviceToHost, g->st);
-          if (cudaStreamSynchronize(g->st) != cudaSuccess) { R.ar.release(); cleanup(); restore(); VFAIL(VCA_ERR_CUDA, "batched search failed"); }
+          if (cudaStreamSynchronize(g->st) != cudaSuccess) { R.ar.release(); VFAIL(VCA_ERR_CUDA, "batched search failed"); }
           if (undone == 0) break;
         }
       }
-      svec_h.resize(S.secs.size() * 5 * (size_t)ldg);
-      cudaMemcpyAsync(theta.data(), R.b.theta, sizeof(double) * theta.size(), cudaMemcpyDeviceToHost, g->st);
-      cudaMemcpyAsync(mconv.data(), R.b.mconv, sizeof(int) * mconv.size(), cudaMemcpyDeviceToHost, g->st);
-      cudaMemcpyAsync(svec_h.data(), R.b.svec, sizeof(double) * svec_h.size(), cudaMemcpyDeviceToHost, g->st);
+      std::vector<double> th(S.secs.size()), sv(S.secs.size() * 5 * (size_t)ldg);
+      std::vector<int> mc(S.secs.size());
+      cudaMemcpyAsync(th.data(), R.b.theta, sizeof(double) * th.size(), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(mc.data(), R.b.mconv, sizeof(int) * mc.size(), cudaMemcpyDeviceToHost, g->st);
+      cudaMemcpyAsync(sv.data(), R.b.svec, sizeof(double) * sv.size(), cudaMemcpyDeviceToHost, g->st);
       cudaError_t e = cudaStreamSynchronize(g->st);
       R.ar.release();
-      if (e != cudaSuccess) { cleanup(); restore(); VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e)); }
+      if (e != cudaSuccess) VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e));
+      for (size_t i = 0; i < which.size(); i++) {
+        const int t = which[i];
+        theta[t] = th[i];
+        mconv[t] = mc[i];
+        done[t] = 1;
+        const int n = std::min(mc[i], LDS);
+        std::copy(sv.begin() + i * 5 * (size_t)ldg, sv.begin() + i * 5 * (size_t)ldg + n,
+                  svec_h.begin() + (size_t)t * LDS);
+      }
+      return VCA_OK;
+    };
+    {
+      std::vector<int> stageA, stageB;
+      bool screened = true;
+      for (int q = 0; q < P; q++) screened = screened && !bnd[q].empty();
+      for (int q = 0; q < P; q++) {
+        if (!screened) {
+          for (int s2 = 0; s2 < nsecs; s2++) stageA.push_back(q * nsecs + s2);
+          continue;
+        }
+        std::vector<int> ord(nsecs);
+        for (int s2 = 0; s2 < nsecs; s2++) ord[s2] = s2;
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) { return bnd[q][a] < bnd[q][b]; });
+        for (int r = 0; r < std::min(2, nsecs); r++) stageA.push_back(q * nsecs + ord[r]);
+      }
+      int rc = run_search(stageA);
+      if (rc) { cleanup(); restore(); return rc; }
+      if (screened) {
+        for (int q = 0; q < P; q++) {
+          double eup = INFINITY;
+          for (int s2 = 0; s2 < nsecs; s2++)
+            if (done[(size_t)q * nsecs + s2]) eup = std::min(eup, theta[(size_t)q * nsecs + s2]);
+          const double cut = eup + 20.0 * c.gs_threshold + 1e-9 * std::max(1.0, std::fabs(eup));
+          for (int s2 = 0; s2 < nsecs; s2++)
+            if (!done[(size_t)q * nsecs + s2] && !(bnd[q][s2] > cut)) stageB.push_back(q * nsecs + s2);
+        }
+        rc = run_search(stageB);
+        if (rc) { cleanup(); restore(); return rc; }
+      }
+      g->bt_skipped = 0;
+      for (char d : done) g->bt_skipped += d ? 0 : 1;
     }
-    lap(1);
     // ---- 3. T=0 lists -------------------------------------------------------
     std::vector<std::vector<ListEntry>> lists(P);
     for (int q = 0; q < P; q++) {
       std::vector<double> E(theta.begin() + (size_t)q * nsecs, theta.begin() + (size_t)(q + 1) * nsecs);
-      replay_t0(E, c.gs_threshold, lists[q]);
+      replay_t0(E, c.gs_threshold, lists[q]);  // skipped sectors are +inf: never listed
       if (lists[q].empty()) { cleanup(); restore(); VFAIL(VCA_ERR_NUMERIC, "no ground state found"); }
     }
     // ---- 4. eigenvectors of the kept (point, sector) tasks -------------------
     TaskList V;
-    std::vector<int> vsrc;  // search task of each eigenvector task
+    std::vector<int> vsrc;  // (point, sector) index of each eigenvector task
     for (int q = 0; q < P; q++)
       for (const ListEntry& x : lists[q]) {
         const int t = q * nsecs + (x.sector - 1);
-        V.add(S.secs[t].sv, S.secs[t].D, x.sector, 1);
+        const int nu = sec_nup(x.sector), nd = sec_ndw(x.sector);
+        V.add(view_tabs(tabs[q], nu, nd), (int64_t)g->dimn[nu] * g->dimn[nd], x.sector, 1);
         vsrc.push_back(t);
       }
     MtRun RV;  // holds the ground-state vectors (psi) until the chains are done
     char* psi = nullptr;
     {
-      int rc = mt_alloc(RV, V, ldg, es, true);
+      int mmax = 1;
+      for (size_t v = 0; v < V.secs.size(); v++) mmax = std::max(mmax, mconv[vsrc[v]]);
+      const int ldv = mmax + 1;
+      int rc = mt_alloc(RV, V, ldv, es, true);
       if (!rc) rc = RV.ar.alloc(&psi, (size_t)V.tot * es);
       double* d_svec = nullptr;
       int* d_mc = nullptr;
-      if (!rc) rc = RV.ar.alloc(&d_svec, V.secs.size() * 5 * (size_t)ldg);
+      if (!rc) rc = RV.ar.alloc(&d_svec, V.secs.size() * 5 * (size_t)ldv);
       if (!rc) rc = RV.ar.alloc(&d_mc, V.secs.size());
       if (rc) { RV.ar.release(); cleanup(); restore(); return rc; }
-      std::vector<double> sv(V.secs.size() * 5 * (size_t)ldg);
+      std::vector<double> sv(V.secs.size() * 5 * (size_t)ldv, 0.0);
       std::vector<int> mc(V.secs.size());
       std::vector<ChainMeta> meta(V.secs.size());
-      int mmax = 1;
       for (size_t v = 0; v < V.secs.size(); v++) {
-        std::copy(svec_h.begin() + vsrc[v] * 5 * (size_t)ldg, svec_h.begin() + (vsrc[v] + 1) * 5 * (size_t)ldg,
-                  sv.begin() + v * 5 * (size_t)ldg);
         mc[v] = mconv[vsrc[v]];
+        std::copy(svec_h.begin() + (size_t)vsrc[v] * LDS, svec_h.begin() + (size_t)vsrc[v] * LDS + std::min(mc[v], LDS),
+                  sv.begin() + v * 5 * (size_t)ldv);
         if (mc[v] < 1) { RV.ar.release(); cleanup(); restore(); VFAIL(VCA_ERR_NUMERIC, "Lanczos start vector has zero norm"); }
         meta[v] = ChainMeta{1, (int)v, mc[v], 1, 0};
-        mmax = std::max(mmax, mc[v]);
       }
       cudaMemcpyAsync(d_svec, sv.data(), sizeof(double) * sv.size(), cudaMemcpyHostToDevice, g->st);
       cudaMemcpyAsync(d_mc, mc.data(), sizeof(int) * mc.size(), cudaMemcpyHostToDevice, g->st);
@@ -2349,7 +2510,7 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
       cudaMemsetAsync(psi, 0, (size_t)V.tot * es, g->st);
       m64_launch_start(RV.gp, cplx, c.start_seed, RV.b, g->st);
       for (int k = 1; k <= mmax; k++) {  // psi = sum_k s_k x_k (sector_gs's second pass, every task at once)
-        m64_launch_psi(RV.gp, cplx, d_svec, 5 * ldg, d_mc, k, RV.b.X, psi, g->st);
+        m64_launch_psi(RV.gp, cplx, d_svec, 5 * ldv, d_mc, k, RV.b.X, psi, g->st);
         if (k < mmax) m64_launch_step(RV.gp, cplx, g->md, k, c.gs_beta_tol, RV.b, g->st);
       }
       m64_launch_sqnorm(RV.gp, cplx, psi, RV.b.tpart, g->st);
@@ -3480,6 +3641,7 @@ int vca_gpu_get_timings(double* ms, int32_t n) {
   if (!ms) VFAIL(VCA_ERR_ARG, "NULL output");
   for (int i = 0; i < n && i < 4; i++) ms[i] = g->t_ms[i];
   for (int i = 4; i < n && i < 10; i++) ms[i] = g->bt_ms[i - 4];
+  if (n > 10) ms[10] = (double)g->bt_skipped;
   return VCA_OK;
 }
 
@@ -3525,6 +3687,15 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G) {
 int vca_gpu_synchronize(void) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+int vca_gpu_sector_bounds(double* out, int32_t n) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian or a solve)");
+  if (!out || n < g->Nsectors) VFAIL(VCA_ERR_ARG, "output too small");
+  const std::vector<double> b = sector_lower_bounds();
+  if (b.empty()) VFAIL(VCA_ERR_UNSUPPORTED, "no bound: an interaction coefficient is negative");
+  for (int i = 0; i < g->Nsectors; i++) out[i] = b[i];
   return VCA_OK;
 }
 
