@@ -470,6 +470,12 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
 int vca_gpu_sector_row_order(int32_t isector, int64_t* order, int64_t cap);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);
+/* The T=0 Omega integrand ln|det(1 + M_k G'(iw))| (VCA_OMEGA.f90:66-67) is
+ * evaluated as ln|det(G'^-1 + M_k)| + ln|det G'| at nodes w <= 10, with G'^-1
+ * and ln|det G'| formed once per node, which saves the M_k G' product at
+ * every k (on = 1, the default); on = 0 keeps the product form everywhere.
+ * No counterpart in the reference; a switch for tests and measurements. */
+int vca_gpu_set_omega_inverse_form(int32_t on);
 /* Lower bound of every sector's lowest energy for the loaded Hamiltonian
  * (out[isector-1]): the one-body part's ground energy in that sector, valid
  * when U, Ust and Ust - Jh are non-negative (VCA_ERR_UNSUPPORTED otherwise).

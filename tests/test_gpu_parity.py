@@ -268,3 +268,20 @@ def test_chan2_solve_matches_oracle(name):
     p, w = s.gf_channel(1, 2, 1, 1, 1, 1, 1)
     assert len(p) > 0
     assert len(s.gf_channel(1, 2, 1, 1, 1, 1, 3)[0]) == 0  # no third channel
+
+
+@pytest.mark.parametrize("name", ["bhz_small", "bath2x2+4", "square2x2_afm"])
+def test_omega_inverse_form_equals_product_form(name):
+    """The T=0 integrand as ln|det(G'^-1 + M_k)| + ln|det G'| below w = 10
+    (the default) and as ln|det(1 + M_k G')| at every node give the same
+    Omega and the same integrand."""
+    pt = POINTS[name]()
+    vals, f = [], []
+    w = np.array([0.01, 0.3, 2.0, 9.0, 40.0])
+    for on in (True, False):
+        s = VcaSolver(pt.cfg, pt.bath_h, pt.bath_v)
+        s.set_omega_inverse_form(on)
+        vals.append(s.solve(pt.Hloc, pt.Hk, pt.bath_h, pt.bath_v))
+        f.append(s.sum_kmesh(w))
+    assert abs(vals[0] - vals[1]) < 1e-12 * max(1.0, abs(vals[1])), vals
+    np.testing.assert_allclose(f[0], f[1], rtol=1e-12, atol=1e-13)

@@ -149,6 +149,7 @@ struct Ctx {
   int* d_nexc = nullptr;
   bool poles_ready = false;
   int ql_max_iter = 60;  // QL sweeps per eigenvalue before a chain is reported unconverged
+  bool omega_inverse_form = true;  // T=0 k-sum through G'^-1 + M at nodes with w <= 10
   ChainStore cstore{};
   int nelem = 0;
   int* d_elem_ptr = nullptr;
@@ -1603,8 +1604,19 @@ int ksum_device(int n, const double2* d_z, bool want_im, Arena& ar, double** f_r
     launch_m_from_hk(nks, NN, P, hks, M, g->st);
     hks = M;
   }
+  KsumInverse ki;
+  if (!want_im && g->omega_inverse_form) {  // T=0 integrand: the inverse form below omega_c
+    double2* Ginv;
+    double* ldG;
+    if ((rc = ar.alloc(&Ginv, (size_t)n * NN)) || (rc = ar.alloc(&ldG, (size_t)n * nblk))) return rc;
+    launch_ginv_blocks(n, N, nblk, nb, Glso, Ginv, ldG, g->st);
+    ki.z = d_z;
+    ki.Ginv = Ginv;
+    ki.ldG = ldG;
+    ki.omega_c = 10.0;
+  }
   launch_omega_ksum2(n, N, nblk, nb, P, Glso, nks, hks, pairs ? g->d_kw : nullptr, d_rowptr, d_cols, fpart,
-                     fpart_im, kchunks, pre_m, g->st);
+                     fpart_im, kchunks, pre_m, ki, g->st);
   launch_reduce_rows(n, kchunks, fpart, 1.0 / (double)Nk, *f_re, g->st);
   if (want_im) launch_reduce_rows(n, kchunks, fpart_im, 1.0 / (double)Nk, *f_im, g->st);
   CUCHK(cudaGetLastError());
@@ -2464,6 +2476,7 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
       g->bt_skipped = 0;
       for (char d : done) g->bt_skipped += d ? 0 : 1;
     }
+    lap(1);
     // ---- 3. T=0 lists -------------------------------------------------------
     std::vector<std::vector<ListEntry>> lists(P);
     for (int q = 0; q < P; q++) {
@@ -3687,6 +3700,12 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G) {
 int vca_gpu_synchronize(void) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+int vca_gpu_set_omega_inverse_form(int32_t on) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  g->omega_inverse_form = on != 0;
   return VCA_OK;
 }
 

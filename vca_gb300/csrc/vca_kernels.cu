@@ -1221,6 +1221,115 @@ __device__ __forceinline__ void ksum_block_product(const KGroup& kg, double2* Aw
   __syncwarp(kg.mask);
 }
 
+// Aw = G^-1 - 1 + M for the block at offset off (Gs holds G^-1 here):
+// ksum_block_logdet adds the 1 back, so it returns ln|det(G^-1 + M)|.
+template <int G>
+__device__ __forceinline__ void ksum_block_inverse_plus_m(const KGroup& kg, double2* Aw, int nb, int off, int N,
+                                                          const double2* Ps, const double2* Gs, const double2* H,
+                                                          const int* rowptr, const int* cols, bool pre_m) {
+  const int nbb = nb * nb;
+  for (int e = kg.gl; e < nbb; e += G) {
+    const int i = e % nb, j = e / nb;
+    double2 a = Gs[(off + i) + (off + j) * N];
+    if (i == j) a.x -= 1.0;
+    Aw[e] = a;
+  }
+  __syncwarp(kg.mask);
+  for (int i = kg.gl; i < nb; i += G) {  // one lane per row: M's entries of row off + i
+    const int gi = off + i;
+    for (int q = rowptr[gi]; q < rowptr[gi + 1]; q++) {
+      const int gl = cols[q];
+      const int il = gi + gl * N;
+      double mr, mi;
+      if (pre_m) {
+        mr = H[il].x;
+        mi = H[il].y;
+      } else {
+        mr = Ps[il].x - H[il].x;
+        mi = Ps[il].y - H[il].y;
+      }
+      double2& t = Aw[i + (gl - off) * nb];
+      t.x += mr;
+      t.y += mi;
+    }
+  }
+  __syncwarp(kg.mask);
+}
+
+// G^-1 and ln|det G| of every diagonal block of n lso matrices (one warp per
+// (node, block), Gauss-Jordan with partial pivoting in shared memory, nb <= 32)
+__global__ void k_ginv_blocks(int n, int N, int nblk, int nb, const double2* Glso, double2* Ginv, double* ldG) {
+  extern __shared__ double2 gj[];  // per warp: nb x 2nb, column-major with 32-row columns
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double2* M = gj + (size_t)wib * 64 * 32;
+  const int task = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (task >= n * nblk) return;
+  const int w = task / nblk, b = task % nblk, off = b * nb;
+  const double2* Gw = Glso + (int64_t)w * N * N;
+  for (int j = 0; j < 2 * nb; j++)
+    if (lane < nb)
+      M[j * 32 + lane] = (j < nb) ? Gw[(off + lane) + (off + j) * N] : make_double2(lane == j - nb ? 1.0 : 0.0, 0.0);
+  __syncwarp();
+  double logabs = 0.0;
+  for (int k = 0; k < nb; k++) {
+    double mag = -1.0;
+    int arg = k;
+    if (lane >= k && lane < nb) {
+      const double2 a = M[k * 32 + lane];
+      mag = a.x * a.x + a.y * a.y;
+      arg = lane;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double om = __shfl_xor_sync(0xffffffffu, mag, o);
+      const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+      if (om > mag || (om == mag && oa < arg)) { mag = om; arg = oa; }
+    }
+    if (arg != k)  // swap rows k and arg, lanes over the 2nb columns
+      for (int j = lane; j < 2 * nb; j += 32) {
+        const double2 t = M[j * 32 + k];
+        M[j * 32 + k] = M[j * 32 + arg];
+        M[j * 32 + arg] = t;
+      }
+    __syncwarp();
+    const double2 piv = M[k * 32 + k];
+    const double pm = piv.x * piv.x + piv.y * piv.y;
+    logabs += 0.5 * log(pm);
+    const double ir = piv.x / pm, ii = -piv.y / pm;
+    for (int j = lane; j < 2 * nb; j += 32) {  // scale row k
+      const double2 a = M[j * 32 + k];
+      M[j * 32 + k] = make_double2(a.x * ir - a.y * ii, a.x * ii + a.y * ir);
+    }
+    __syncwarp();
+    if (lane < nb && lane != k) {  // eliminate column k from row `lane`
+      const double2 f = M[k * 32 + lane];
+      for (int j = 0; j < 2 * nb; j++) {
+        const double2 u = M[j * 32 + k];
+        double2& t = M[j * 32 + lane];
+        t.x -= f.x * u.x - f.y * u.y;
+        t.y -= f.x * u.y + f.y * u.x;
+      }
+    }
+    __syncwarp();
+  }
+  double2* Gi = Ginv + (int64_t)w * N * N;
+  for (int j = 0; j < nb; j++)
+    if (lane < nb) Gi[(off + lane) + (off + j) * N] = M[(nb + j) * 32 + lane];
+  if (lane == 0) ldG[(int64_t)w * nblk + b] = logabs;
+}
+void launch_ginv_blocks(int n, int N, int nblk, int nb, const double2* Glso, double2* Ginv, double* ldG,
+                        cudaStream_t st) {
+  COUNT_LAUNCH();
+  const int warps = 4;
+  const size_t shm = sizeof(double2) * warps * 64 * 32;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_ginv_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    attr = true;
+  }
+  const int tasks = n * nblk;
+  k_ginv_blocks<<<(tasks + warps - 1) / warps, 32 * warps, shm, st>>>(n, N, nblk, nb, Glso, Ginv, ldG);
+}
+
 // ln|det(1 + A)| of the block in Aw (destroyed); with PH, *ph gains the sum
 // of the pivots' arguments (plus pi per row swap).  Both are valid on the
 // group's first lane only.
@@ -1351,7 +1460,9 @@ template <bool CPLX, int G>
 __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, const double2* P,
                                                      const double2* Glso, int64_t Nk, const double2* Hk,
                                                      const double* kw, const int* rowptr, const int* cols,
-                                                     double* fpart, double* fpart_im, int kchunks, int pre_m) {
+                                                     double* fpart, double* fpart_im, int kchunks, int pre_m,
+                                                     const double2* zn, const double2* Ginv, const double* ldG,
+                                                     double omega_c) {
   extern __shared__ double2 shm[];
   constexpr int TPW = 32 / G;
   const int w = blockIdx.y;
@@ -1367,8 +1478,12 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
   kg.base = grp * G;
   kg.mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (grp * G));
   double2* Aw = shm + 2 * NN + ((int64_t)warp * TPW + grp) * nb * nb;
+  // inverse form at this node: ln|det(1 + M G)| = ln|det(G^-1 + M)| + ln|det G|
+  // (no product per k); kept below omega_c, where the two logs are O(1)
+  const bool inv = !CPLX && Ginv != nullptr && zn[w].y <= omega_c;
+  const double2* Gsrc = inv ? Ginv : Glso;
   for (int t = threadIdx.x; t < NN; t += blockDim.x) {
-    Gs[t] = Glso[(int64_t)w * NN + t];
+    Gs[t] = Gsrc[(int64_t)w * NN + t];
     Ps[t] = P[(int64_t)w * NN + t];
   }
   __syncthreads();
@@ -1381,8 +1496,14 @@ __global__ void __launch_bounds__(128) k_omega_ksum2(int N, int nblk, int nb, co
     const int b0 = CPLX ? 0 : (int)(task % nblk), b1 = CPLX ? nblk : b0 + 1;
     double ld = 0.0, ph = 0.0;
     for (int b = b0; b < b1; b++) {
-      ksum_block_product<G>(kg, Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, pre_m != 0);
-      ld += ksum_block_logdet<G, CPLX>(kg, Aw, nb, &ph);
+      if (inv) {
+        ksum_block_inverse_plus_m<G>(kg, Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, pre_m != 0);
+        const double l = ksum_block_logdet<G, CPLX>(kg, Aw, nb, &ph);
+        ld += (kg.gl == 0) ? l + ldG[(int64_t)w * nblk + b] : 0.0;
+      } else {
+        ksum_block_product<G>(kg, Aw, nb, b * nb, N, Ps, Gs, H, rowptr, cols, pre_m != 0);
+        ld += ksum_block_logdet<G, CPLX>(kg, Aw, nb, &ph);
+      }
     }
     if (kg.gl == 0) {
       acc += kw ? kw[k] * ld : ld;
@@ -1424,7 +1545,7 @@ void launch_m_from_hk(int64_t Nk, int NN, const double2* Hl, const double2* Hk, 
 template <bool CPLX, int G>
 static void ksum2_launch(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                          const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                         double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
+                         double* fpart_im, int kchunks, bool pre_m, const KsumInverse& ki, cudaStream_t st) {
   const int threads = 128;
   const size_t shm = sizeof(double2) * (2 * (size_t)N * N + (size_t)(threads / G) * nb * nb);
   static bool attr = false;
@@ -1433,28 +1554,34 @@ static void ksum2_launch(int nw, int N, int nblk, int nb, const double2* P, cons
     attr = true;
   }
   k_omega_ksum2<CPLX, G><<<dim3(kchunks, nw, 1), threads, shm, st>>>(N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols,
-                                                                     fpart, fpart_im, kchunks, pre_m ? 1 : 0);
+                                                                     fpart, fpart_im, kchunks, pre_m ? 1 : 0, ki.z,
+                                                                     ki.Ginv, ki.ldG, ki.omega_c);
 }
 template <bool CPLX>
 static void ksum2_dispatch(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                            const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                           double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
+                           double* fpart_im, int kchunks, bool pre_m, const KsumInverse& ki, cudaStream_t st) {
   // 8 lanes per task up to 12 x 12 blocks, 16 up to 16 x 16, else a warp
   if (nb <= 12)
-    ksum2_launch<CPLX, 8>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+    ksum2_launch<CPLX, 8>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, ki,
+                          st);
   else if (nb <= 16)
-    ksum2_launch<CPLX, 16>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+    ksum2_launch<CPLX, 16>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, ki,
+                           st);
   else
-    ksum2_launch<CPLX, 32>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+    ksum2_launch<CPLX, 32>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, ki,
+                           st);
 }
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                        double* fpart_im, int kchunks, bool pre_m, cudaStream_t st) {
+                        double* fpart_im, int kchunks, bool pre_m, const KsumInverse& ki, cudaStream_t st) {
   COUNT_LAUNCH();
   if (fpart_im)
-    ksum2_dispatch<true>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, st);
+    ksum2_dispatch<true>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, fpart_im, kchunks, pre_m, ki,
+                         st);
   else
-    ksum2_dispatch<false>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, nullptr, kchunks, pre_m, st);
+    ksum2_dispatch<false>(nw, N, nblk, nb, P, Glso, Nk, Hk, kw, rowptr, cols, fpart, nullptr, kchunks, pre_m, ki,
+                          st);
 }
 
 // ---------------------------------------------------------------------------

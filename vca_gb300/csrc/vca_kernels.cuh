@@ -147,9 +147,20 @@ void launch_gf_assemble(const ClusterDims& cd, int nz, const double2* Graw, doub
 // updates.  With fpart_im (sum_kmesh_complex, :78-114) also the k-sum of the
 // principal argument of det over all blocks of each k.
 // pre_m: Hk holds M_k = P - H_k already (P the same at every node)
+// The inverse form of the k-sum at nodes with Im z <= omega_c (T=0 real
+// integrand only): Ginv / ldG from launch_ginv_blocks; Ginv = NULL: off.
+struct KsumInverse {
+  const double2* z = nullptr;      // the nodes
+  const double2* Ginv = nullptr;   // per node, the inverse of each diagonal block of G' (lso)
+  const double* ldG = nullptr;     // per node and block, ln|det G'_block|
+  double omega_c = 0.0;
+};
 void launch_omega_ksum2(int nw, int N, int nblk, int nb, const double2* P, const double2* Glso, int64_t Nk,
                         const double2* Hk, const double* kw, const int* rowptr, const int* cols, double* fpart,
-                        double* fpart_im, int kchunks, bool pre_m, cudaStream_t st);
+                        double* fpart_im, int kchunks, bool pre_m, const KsumInverse& ki, cudaStream_t st);
+// G'^-1 and ln|det G'| of each diagonal block (nblk blocks of nb <= 32) of n lso matrices
+void launch_ginv_blocks(int n, int N, int nblk, int nb, const double2* Glso, double2* Ginv, double* ldG,
+                        cudaStream_t st);
 // M[k] = Hl - Hk[k] for Nk lso matrices of NN elements
 void launch_m_from_hk(int64_t Nk, int NN, const double2* Hl, const double2* Hk, double2* M, cudaStream_t st);
 // Sigma(z) (want_g0 = false) or G0(z) on nz frequencies from G' (lso) and

@@ -37,7 +37,8 @@ EXPORTS = [
     "vca_gpu_get_g0_realaxis", "vca_gpu_get_dens", "vca_gpu_get_dens_up", "vca_gpu_get_dens_dw",
     "vca_gpu_get_docc", "vca_gpu_get_mag",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
-    "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_set_ql_max_iter", "vca_gpu_sector_bounds", "vca_gpu_timer_start",
+    "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_set_ql_max_iter", "vca_gpu_sector_bounds",
+    "vca_gpu_set_omega_inverse_form", "vca_gpu_timer_start",
     "vca_gpu_timer_stop",
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
@@ -132,6 +133,7 @@ def load(path: Optional[str] = None):
         "vca_gpu_synchronize": (ctypes.c_int, []),
         "vca_gpu_set_ql_max_iter": (ctypes.c_int, [i32]),
         "vca_gpu_sector_bounds": (ctypes.c_int, [dp, i32]),
+        "vca_gpu_set_omega_inverse_form": (ctypes.c_int, [i32]),
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
         "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
@@ -295,6 +297,10 @@ class VcaSolver:
         out = np.zeros(n)
         check(self.L.vca_gpu_sector_bounds(_dp(out), n))
         return out
+
+    def set_omega_inverse_form(self, on: bool):
+        """T=0 k-sum through G'^-1 + M_k below w = 10 (default on)."""
+        check(self.L.vca_gpu_set_omega_inverse_form(1 if on else 0))
 
     def set_ql_max_iter(self, n: int):
         """QL sweeps per eigenvalue allowed when chains become poles (default 60)."""
