@@ -472,6 +472,8 @@ def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
                         "stage_ms": dict(zip(["tables", "search", "eigenvectors", "chains", "omega",
                                               "closing_plain_solve"], [round(x, 1) for x in st_b[:6]])),
                         "sector_searches_skipped_by_bound": int(st_b[6]),
+                        "chain_tile_shape": {"rows_per_tile": int(st_b[7]), "row_lanes_per_block": int(st_b[8]),
+                                             "chosen_by": "autotuner"},
                         "sector_searches_total": B * _nsectors(pts[0].cfg)},
             "plain_per_point": {"points": n_loop, "value": round(v_l, 4), "ms_per_eval": round(1e3 * t_l / n_loop, 2),
                                 "what": "one point after another, every sector of a point in one batched search"},

@@ -454,7 +454,9 @@ int64_t vca_gpu_kernel_launches(void);
  * n >= 10 also the last batched-form vca_gpu_solve_batch's stages over all
  * its points: [4] tables, [5] ground-state search, [6] eigenvectors,
  * [7] chains, [8] Omega, [9] the closing plain solve of the last point;
- * with n >= 11, [10] the (point, sector) searches its screening skipped. */
+ * with n >= 11, [10] the (point, sector) searches its screening skipped;
+ * with n >= 13, [11] rows per tile and [12] row lanes per block of its
+ * chains' (autotuned) tile shape. */
 int vca_gpu_get_timings(double* ms, int32_t n);
 /* Arithmetic of the loaded Hamiltonian: *fx = 1 when the fixed-point path is
  * active, with vector scale 2^-F and H v scale 2^-G.  In that case the device
@@ -470,6 +472,14 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G);
 int vca_gpu_sector_row_order(int32_t isector, int64_t* order, int64_t cap);
 /* Wait for all work on the library stream. */
 int vca_gpu_synchronize(void);
+/* The batched form's Green's-function chains run as column tasks whose tile
+ * shape (rows per tile, row lanes per block) is tuned at first use for each
+ * problem class: every candidate's H x v is timed on the call's own first
+ * tasks and the fastest kept for the life of the process (on = 1, default).
+ * on = 0 runs the fixed shape (64 rows, 8 lanes).  The shape changes only
+ * the summation order of the chains' dot products.  No counterpart in the
+ * reference. */
+int vca_gpu_set_autotune(int32_t on);
 /* The T=0 Omega integrand ln|det(1 + M_k G'(iw))| (VCA_OMEGA.f90:66-67) is
  * evaluated as ln|det(G'^-1 + M_k)| + ln|det G'| at nodes w <= 10, with G'^-1
  * and ln|det G'| formed once per node, which saves the M_k G' product at

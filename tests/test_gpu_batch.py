@@ -151,3 +151,19 @@ def test_screened_and_full_batched_searches_agree():
         skipped.append(s.timings(batched=True)[6])
     np.testing.assert_allclose(vals[0], vals[1], rtol=E_TOL, atol=0)
     assert skipped[0] > 0 and skipped[1] == 0, skipped
+
+
+def test_autotuned_and_fixed_chain_shapes_agree():
+    """The chains' tile shape the autotuner picks changes only the order of
+    the dot products' sums: Omega agrees with the fixed shape to 1e-12."""
+    pts = _small("bhz")
+    Hl, bh, bv = _stack(pts)
+    vals, shapes = [], []
+    for on in (True, False):
+        s = VcaSolver(pts[0].cfg)
+        s.set_autotune(on)
+        vals.append(s.solve_batch(Hl, pts[0].Hk))
+        shapes.append(tuple(s.timings(batched=True)[7:9]))
+    np.testing.assert_allclose(vals[0], vals[1], rtol=1e-12, atol=0)
+    assert shapes[1] == (64, 8)
+    assert shapes[0][0] in (32, 64, 128, 256) and shapes[0][1] in (4, 8, 16)

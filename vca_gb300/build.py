@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "libvca_gpu.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["vca_kernels.cu", "vca_fx.cu", "vca_multi.cu", "vca_api.cu", "vca_umma.cu", "vca_mlp.cu",
+SOURCES = ["vca_kernels.cu", "vca_fx.cu", "vca_multi.cu", "vca_batch.cu", "vca_api.cu", "vca_umma.cu", "vca_mlp.cu",
            "vca_gfmatrix.cpp", "vca_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

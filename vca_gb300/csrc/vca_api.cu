@@ -21,6 +21,7 @@
 #include "../../include/vca_gpu.h"
 #include "vca_fx.cuh"
 #include "vca_multi.cuh"
+#include "vca_batch.cuh"
 #include "vca_kernels.cuh"
 #include "vca_gfmatrix.h"
 #include "vca_host.h"
@@ -171,6 +172,8 @@ struct Ctx {
   // eigenvectors, chains, Omega, the closing plain solve (wall ms, all waves)
   double bt_ms[6] = {0, 0, 0, 0, 0, 0};
   int64_t bt_skipped = 0;  // (point, sector) searches the last batched solve skipped by their bound
+  int bt_shape[2] = {MC_ROWS, 8};  // the chains' tile shape it ran: rows per tile, row lanes per block
+  bool autotune = true;      // tune that shape on first use per problem class
   // GFmatrix read from a restart file (read_gfprime): replaces the solve's
   // tables for G'(z) and the channel getter until the next solve
   // Sigma read back by vca_read_impSigma: the Sigma getters return it until
@@ -2327,6 +2330,173 @@ struct BChain {
   int tup, tdw;
 };
 
+// Host tables of one group of column tasks (chains grouped by point, state,
+// spin and particle/hole; rows cut into tiles of R rows)
+struct McTaskRef {
+  int point, c0, c1;  // chains [c0, c1) of that point's list
+  int64_t D;
+  int m;
+};
+struct McHost {
+  std::vector<McTask> tasks;
+  std::vector<int> tile_task, col_chain, col_part, isg, ch_point, ch_index;
+  std::vector<int64_t> tile_row0, tile_row1;
+  std::vector<McChain> chains;
+  std::vector<ChainMeta> meta;
+  std::vector<double2> wf;
+  int64_t xoff = 0, part = 0;
+  int nl_max = 1;
+};
+void mc_build(const std::vector<McTaskRef>& refs, size_t t0, size_t t1,
+              const std::vector<std::vector<BChain>>& pch, const std::vector<PointTabs>& tabs, int R, int ngfiter,
+              McHost& h) {
+  for (size_t ti = t0; ti < t1; ti++) {
+    const McTaskRef& r = refs[ti];
+    const BChain& b0 = pch[r.point][r.c0];
+    McTask tk{};
+    tk.sv = view_tabs(tabs[r.point], b0.tup, b0.tdw);
+    tk.D = r.D;
+    tk.m = r.m;
+    tk.col0 = (int)h.col_chain.size();
+    tk.xoff = h.xoff;
+    tk.tile0 = (int)h.tile_task.size();
+    for (int64_t rr = 0; rr < r.D; rr += R) {
+      h.tile_task.push_back((int)h.tasks.size());
+      h.tile_row0.push_back(rr);
+      h.tile_row1.push_back(std::min<int64_t>(rr + R, r.D));
+    }
+    tk.ntile = (int)h.tile_task.size() - tk.tile0;
+    tk.part0 = h.part;
+    h.part += (int64_t)tk.ntile * tk.m;
+    h.xoff += r.D * r.m;
+    const int nl = (int)std::min<int64_t>(r.D, ngfiter);
+    h.nl_max = std::max(h.nl_max, nl);
+    int col = 0;
+    for (int ci = r.c0; ci < r.c1; ci++) {
+      const BChain& b = pch[r.point][ci];
+      McChain mc{};
+      mc.task = (int)h.tasks.size();
+      mc.col0 = col;
+      mc.ncol = b.ncomp;
+      mc.op = b.mc;
+      for (int qq = 0; qq < b.ncomp; qq++) {
+        h.col_chain.push_back((int)h.chains.size());
+        h.col_part.push_back(qq);
+      }
+      col += b.ncomp;
+      h.meta.push_back(ChainMeta{b.ncomp, 0, nl, 1, 0});
+      h.isg.push_back(b.isign);
+      h.wf.push_back(make_double2(b.wfac.real(), b.wfac.imag()));
+      h.ch_point.push_back(r.point);
+      h.ch_index.push_back(ci);
+      h.chains.push_back(mc);
+    }
+    h.tasks.push_back(tk);
+  }
+}
+
+// device copy of a group's tables; McGroup points into `ar`
+int mc_upload(const McHost& h, int by, Arena& ar, McGroup& gp, ChainMeta** d_meta) {
+  McTask* d_tasks;
+  int *d_tt, *d_cc, *d_cp;
+  int64_t *d_r0, *d_r1;
+  McChain* d_ch;
+  const int nch = (int)h.chains.size();
+  RCHK(ar.alloc(&d_tasks, h.tasks.size()));
+  RCHK(ar.alloc(&d_tt, h.tile_task.size()));
+  RCHK(ar.alloc(&d_r0, h.tile_row0.size()));
+  RCHK(ar.alloc(&d_r1, h.tile_row1.size()));
+  RCHK(ar.alloc(&d_cc, h.col_chain.size()));
+  RCHK(ar.alloc(&d_cp, h.col_part.size()));
+  RCHK(ar.alloc(&d_ch, nch));
+  RCHK(ar.alloc(d_meta, nch));
+  CUCHK(cudaMemcpyAsync(d_tasks, h.tasks.data(), sizeof(McTask) * h.tasks.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_tt, h.tile_task.data(), sizeof(int) * h.tile_task.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_r0, h.tile_row0.data(), sizeof(int64_t) * h.tile_row0.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_r1, h.tile_row1.data(), sizeof(int64_t) * h.tile_row1.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_cc, h.col_chain.data(), sizeof(int) * h.col_chain.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_cp, h.col_part.data(), sizeof(int) * h.col_part.size(), cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(d_ch, h.chains.data(), sizeof(McChain) * nch, cudaMemcpyHostToDevice, g->st));
+  CUCHK(cudaMemcpyAsync(*d_meta, h.meta.data(), sizeof(ChainMeta) * nch, cudaMemcpyHostToDevice, g->st));
+  gp = McGroup{d_tasks, d_tt, d_r0, d_r1, d_cc, d_cp, d_ch, (int)h.tasks.size(), (int)h.tile_task.size(),
+               (int)h.col_chain.size(), nch, by};
+  return VCA_OK;
+}
+
+// Autotuner of the chains' tile shape: rows per tile R and row lanes per
+// block by.  Each candidate runs the chain step's H x v (the dominant
+// kernel) three times on the group's first tasks (up to 2^24 elements),
+// timed by CUDA events; the fastest shape is kept per (real/complex,
+// log2 mean dimension, log2 mean width) for the life of the process.  The
+// shape changes the summation order of the chain's dot products (at the
+// 1e-16 level), not what is summed.
+struct McShape { int R = MC_ROWS, by = 8; double ms = 0.0; bool tuned = false; };
+McShape mc_autotune(const std::vector<McTaskRef>& refs, size_t t0, size_t t1,
+                    const std::vector<std::vector<BChain>>& pch, const std::vector<PointTabs>& tabs, bool cplx,
+                    size_t es) {
+  static std::vector<std::pair<long, McShape>> cache;
+  McShape best;
+  if (!g->autotune) return best;
+  double sd = 0.0, sm = 0.0;
+  size_t n = 0, t1s = t0;
+  int64_t elems = 0;
+  while (t1s < t1 && (t1s == t0 || elems + refs[t1s].D * refs[t1s].m <= ((int64_t)1 << 24))) {
+    elems += refs[t1s].D * refs[t1s].m;
+    sd += (double)refs[t1s].D;
+    sm += refs[t1s].m;
+    n++;
+    t1s++;
+  }
+  const long key = (cplx ? 1L : 0L) | ((long)std::ilogb(std::max(1.0, sd / n)) << 1) |
+                   ((long)std::ilogb(std::max(1.0, sm / n)) << 8);
+  for (auto& kv : cache)
+    if (kv.first == key) return kv.second;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  best.ms = INFINITY;
+  for (int R : {32, 64, 128, 256}) {
+    McHost h;
+    mc_build(refs, t0, t1s, pch, tabs, R, g->cfg.lanc_ngfiter, h);
+    Arena ar;
+    McGroup gp;
+    ChainMeta* d_meta;
+    double *d_tp, *d_bn;
+    char *x0, *x1, *x2;
+    const int nch = (int)h.chains.size();
+    if (mc_upload(h, 8, ar, gp, &d_meta) || ar.alloc(&d_tp, (size_t)h.part) || ar.alloc(&d_bn, nch) ||
+        ar.alloc(&x0, (size_t)h.xoff * es) || ar.alloc(&x1, (size_t)h.xoff * es) || ar.alloc(&x2, (size_t)h.xoff * es)) {
+      ar.release();
+      continue;
+    }
+    cudaMemsetAsync(x0, 0, (size_t)h.xoff * es, g->st);
+    cudaMemsetAsync(x1, 0, (size_t)h.xoff * es, g->st);
+    cudaMemsetAsync(d_bn, 0, sizeof(double) * nch, g->st);
+    for (int by : {4, 8, 16}) {
+      gp.by = by;
+      mc_launch_hxv(gp, cplx, g->md, d_meta, d_bn, 1, x0, x1, x2, d_tp, g->st);  // warm-up
+      cudaEventRecord(e0, g->st);
+      for (int r = 0; r < 3; r++) mc_launch_hxv(gp, cplx, g->md, d_meta, d_bn, 1, x0, x1, x2, d_tp, g->st);
+      cudaEventRecord(e1, g->st);
+      float ms = 0.0f;
+      if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+          ms < best.ms) {
+        best.R = R;
+        best.by = by;
+        best.ms = ms;
+      }
+    }
+    ar.release();
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGetLastError();
+  if (!std::isfinite(best.ms)) return McShape{};
+  best.tuned = true;
+  cache.push_back({key, best});
+  return best;
+}
+
 int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_h, int64_t sbh, const double* bath_v,
                       int64_t sbv, double* omega_out) {
   const vca_config cfg0 = g->cfg;
@@ -2612,77 +2782,109 @@ int solve_batch_fused(int B, const double* Hloc, int64_t sh, const double* bath_
       cudaMemsetAsync(s.n, 0, sizeof(int) * n, g->st);
     }
     {
-      // every chain task, point-major; groups bounded by memory
-      std::vector<std::pair<int, int>> all;  // (point, index in pch)
-      for (int q = 0; q < P; q++)
-        for (int i = 0; i < (int)pch[q].size(); i++) all.push_back({q, i});
+      // column tasks: the chains of one (point, state, spin, particle/hole)
+      // share a target sector and run as one task of m columns; tasks are
+      // grouped point-major under a memory budget
+      std::vector<McTaskRef> trefs;
+      for (int q = 0; q < P; q++) {
+        int i = 0;
+        const int n = (int)pch[q].size();
+        while (i < n) {
+          const BChain& b0 = pch[q][i];
+          int j = i, m = 0;
+          while (j < n && pch[q][j].state == b0.state && pch[q][j].mc.spin == b0.mc.spin &&
+                 pch[q][j].mc.dag == b0.mc.dag) {
+            m += pch[q][j].ncomp;
+            j++;
+          }
+          trefs.push_back({q, i, j, (int64_t)g->dimn[b0.tup] * g->dimn[b0.tdw], m});
+          i = j;
+        }
+      }
       size_t fb = 0;
       cudaMemGetInfo(&fb, &totb);
       const size_t gbudget = (size_t)(0.3 * (double)fb);
-      size_t a0 = 0;
-      while (a0 < all.size()) {
-        TaskList T;
-        std::vector<MtChain> mcs;
-        std::vector<ChainMeta> meta;
-        std::vector<int> isg;
-        std::vector<double2> wf;
-        size_t a1 = a0;
-        int nl_max = 1;
-        while (a1 < all.size()) {
-          const BChain& b = pch[all[a1].first][all[a1].second];
-          const SectorView tv = view_tabs(tabs[b.point], b.tup, b.tdw);
-          const int64_t Dsec = (int64_t)tv.dimup * tv.dimdw;
-          const int64_t len = b.ncomp * Dsec;
-          if (a1 > a0 && 3 * (size_t)(T.tot + len) * es > gbudget) break;
-          const int nl = (int)std::min<int64_t>(Dsec, c.lanc_ngfiter);
-          T.add(tv, len, 0, b.ncomp);
-          mcs.push_back(b.mc);
-          meta.push_back(ChainMeta{1, (int)meta.size(), nl, 1, 0});
-          isg.push_back(b.isign);
-          wf.push_back(make_double2(b.wfac.real(), b.wfac.imag()));
-          nl_max = std::max(nl_max, nl);
-          a1++;
+      size_t t0i = 0;
+      while (t0i < trefs.size()) {
+        size_t t1i = t0i;
+        int64_t tot = 0;
+        while (t1i < trefs.size()) {
+          const int64_t add = trefs[t1i].D * trefs[t1i].m;
+          if (t1i > t0i && 3 * (size_t)(tot + add) * es > gbudget) break;
+          tot += add;
+          t1i++;
         }
-        MtRun R;
-        MtChain* d_mc = nullptr;
-        int* d_isg = nullptr;
-        double2* d_wf = nullptr;
-        int rc = mt_alloc(R, T, ld, es, true);
-        if (!rc) rc = R.ar.alloc(&d_mc, mcs.size());
-        if (!rc) rc = R.ar.alloc(&d_isg, isg.size());
-        if (!rc) rc = R.ar.alloc(&d_wf, wf.size());
-        if (rc) { R.ar.release(); stores.release(); RV.ar.release(); cleanup(); restore(); return rc; }
-        cudaMemcpyAsync(d_mc, mcs.data(), sizeof(MtChain) * mcs.size(), cudaMemcpyHostToDevice, g->st);
-        cudaMemcpyAsync(d_isg, isg.data(), sizeof(int) * isg.size(), cudaMemcpyHostToDevice, g->st);
-        cudaMemcpyAsync(d_wf, wf.data(), sizeof(double2) * wf.size(), cudaMemcpyHostToDevice, g->st);
-        cudaMemcpyAsync(R.b.meta, meta.data(), sizeof(ChainMeta) * meta.size(), cudaMemcpyHostToDevice, g->st);
+        const McShape shape = mc_autotune(trefs, t0i, t1i, pch, tabs, cplx, es);
+        g->bt_shape[0] = shape.R;
+        g->bt_shape[1] = shape.by;
+        McHost h;
+        mc_build(trefs, t0i, t1i, pch, tabs, shape.R, c.lanc_ngfiter, h);
+        const int nch = (int)h.chains.size();
+        const int nl_max = h.nl_max;
+        const int64_t xoff = h.xoff, part = h.part;
+        const std::vector<int>& ch_point = h.ch_point;
+        const std::vector<int>& ch_index = h.ch_index;
+        Arena ar;
+        McGroup gp;
+        ChainMeta* d_meta;
+        int* d_isg;
+        double *d_tp, *d_al, *d_b2, *d_bn, *d_ib, *d_A, *d_B, *d_n2, *d_in;
+        double2* d_wf;
+        char *x0, *x1, *x2;
+        int rc = mc_upload(h, shape.by, ar, gp, &d_meta);
+        if (!rc)
+          (void)((rc = ar.alloc(&d_tp, (size_t)part)) || (rc = ar.alloc(&d_al, nch)) || (rc = ar.alloc(&d_b2, nch)) ||
+                 (rc = ar.alloc(&d_bn, nch)) || (rc = ar.alloc(&d_ib, nch)) ||
+                 (rc = ar.alloc(&d_A, (size_t)nch * ld)) || (rc = ar.alloc(&d_B, (size_t)nch * ld)) ||
+                 (rc = ar.alloc(&d_n2, nch)) || (rc = ar.alloc(&d_in, nch)) || (rc = ar.alloc(&d_isg, nch)) ||
+                 (rc = ar.alloc(&d_wf, nch)) || (rc = ar.alloc(&x0, (size_t)xoff * es)) ||
+                 (rc = ar.alloc(&x1, (size_t)xoff * es)) || (rc = ar.alloc(&x2, (size_t)xoff * es)));
+        if (rc) {
+          ar.release(); stores.release(); RV.ar.release(); cleanup(); restore();
+          return rc;
+        }
+        cudaMemcpyAsync(d_isg, h.isg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, g->st);
+        cudaMemcpyAsync(d_wf, h.wf.data(), sizeof(double2) * nch, cudaMemcpyHostToDevice, g->st);
+        cudaMemsetAsync(d_A, 0, sizeof(double) * nch * ld, g->st);
+        cudaMemsetAsync(d_B, 0, sizeof(double) * nch * ld, g->st);
+        cudaMemsetAsync(d_bn, 0, sizeof(double) * nch, g->st);
+        void *X = x0, *Xp = x1, *Y = x2;
         // start vectors c^(dag)|gs>, normalised; norm^2 kept for the weights
-        mt_launch_chain_init(R.gp, cplx, d_mc, R.b.X, R.b.tpart, g->st);
-        mt_launch_norm(R.gp, R.b.tpart, R.b.meta, R.n2, R.b.invb, g->st);
-        m64_launch_scale(R.gp, cplx, R.b.invb, R.b.X, R.b.X, g->st);
-        for (int k = 1; k <= nl_max; k++) m64_launch_step(R.gp, cplx, g->md, k, c.gf_beta_tol, R.b, g->st);
+        mc_launch_chain_init(gp, cplx, X, d_tp, g->st);
+        mc_launch_reduce(gp, d_tp, d_n2, g->st);
+        launch_chain_norm_init(nch, d_meta, d_n2, d_in, g->st);
+        mc_launch_scale(gp, cplx, d_meta, d_in, X, X, g->st);
+        for (int k = 1; k <= nl_max; k++) {
+          mc_launch_hxv(gp, cplx, g->md, d_meta, d_bn, k > 1 ? 1 : 0, X, Xp, Y, d_tp, g->st);
+          mc_launch_reduce(gp, d_tp, d_al, g->st);
+          mc_launch_update(gp, cplx, d_meta, d_al, X, Y, d_tp, g->st);
+          mc_launch_reduce(gp, d_tp, d_b2, g->st);
+          launch_lanczos_record(nch, d_meta, k, d_al, d_b2, d_A, d_B, ld, c.gf_beta_tol, d_ib, d_bn, g->st);
+          mc_launch_scale(gp, cplx, d_meta, d_ib, Y, Y, g->st);
+          void* t = Xp;  // (X, Xp, Y) <- (Y, X, Xp)
+          Xp = X;
+          X = Y;
+          Y = t;
+        }
         // into the stores: runs of one (point, state)
-        size_t r0 = 0;
-        while (r0 < mcs.size()) {
-          const BChain& b0 = pch[all[a0 + r0].first][all[a0 + r0].second];
-          size_t r1 = r0;
-          while (r1 < mcs.size()) {
-            const BChain& b1 = pch[all[a0 + r1].first][all[a0 + r1].second];
-            if (b1.point != b0.point || b1.state != b0.state) break;
+        int r0 = 0;
+        while (r0 < nch) {
+          int r1 = r0;
+          while (r1 < nch && ch_point[r1] == ch_point[r0] &&
+                 pch[ch_point[r1]][ch_index[r1]].state == pch[ch_point[r0]][ch_index[r0]].state)
             r1++;
-          }
-          const int q = b0.point;
-          const double Ei = lists[q][b0.state].e;
-          const double zeta = (double)lists[q].size();
-          launch_chain_store((int)(r1 - r0), R.b.meta + r0, R.b.A + r0 * ld, R.b.Bt + r0 * ld, ld, R.n2 + r0,
-                             d_wf + r0, d_isg + r0, Ei, 1.0, zeta, cs[q], all[a0 + r0].second, g->st);
+          const int q = ch_point[r0];
+          const BChain& b0 = pch[q][ch_index[r0]];
+          launch_chain_store(r1 - r0, d_meta + r0, d_A + (size_t)r0 * ld, d_B + (size_t)r0 * ld, ld, d_n2 + r0,
+                             d_wf + r0, d_isg + r0, lists[q][b0.state].e, 1.0, (double)lists[q].size(), cs[q],
+                             ch_index[r0], g->st);
           r0 = r1;
         }
         cudaError_t e = cudaStreamSynchronize(g->st);
         if (e == cudaSuccess) e = cudaGetLastError();
-        R.ar.release();
+        ar.release();
         if (e != cudaSuccess) { stores.release(); RV.ar.release(); cleanup(); restore(); VFAIL(VCA_ERR_CUDA, cudaGetErrorString(e)); }
-        a0 = a1;
+        t0i = t1i;
       }
     }
     RV.ar.release();  // the ground-state vectors are no longer needed
@@ -3655,6 +3857,7 @@ int vca_gpu_get_timings(double* ms, int32_t n) {
   for (int i = 0; i < n && i < 4; i++) ms[i] = g->t_ms[i];
   for (int i = 4; i < n && i < 10; i++) ms[i] = g->bt_ms[i - 4];
   if (n > 10) ms[10] = (double)g->bt_skipped;
+  if (n > 12) { ms[11] = g->bt_shape[0]; ms[12] = g->bt_shape[1]; }
   return VCA_OK;
 }
 
@@ -3700,6 +3903,12 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G) {
 int vca_gpu_synchronize(void) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+int vca_gpu_set_autotune(int32_t on) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  g->autotune = on != 0;
   return VCA_OK;
 }
 

@@ -5,6 +5,7 @@
 #include "vca_fx.cuh"
 #include "vca_tri.cuh"
 #include "vca_multi.cuh"
+#include "vca_batch.cuh"
 
 #include <cmath>
 #include <atomic>
@@ -664,76 +665,76 @@ __global__ void k_chain_init(SectorView tgt, int src_dimup, const void* gsv, int
     }
   }
 }
-// The same gather for chain tasks of the batched form: one packed vector per
-// task (its point's target sector), [re; im] halves for a complex chain on a
-// real H; per-tile |x|^2 partials in a fixed order for the norm.
+// The gather for the column tasks of the batched chains (vca_batch.cuh):
+// column c of a task is part re/im of its chain's start vector.
 template <typename T>
-__global__ void k_mt_chain_init(const MsSector* secs, const int* tsec, const int64_t* tstart, int ntiles,
-                                const MtChain* chs, T* X, double* tpart) {
-  __shared__ double red[256];
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int s = tsec[t];
-    const MsSector& S = secs[s];
-    const SectorView& tgt = S.sv;
-    const MtChain c = chs[s];
-    const int64_t Dsec = (int64_t)tgt.dimup * tgt.dimdw;
-    const int64_t i0 = tstart[t], i1 = min(i0 + (int64_t)MS_TILE, S.D);
-    double acc = 0.0;
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      const int comp = (i >= Dsec) ? 1 : 0;
-      const int64_t ii = i - (comp ? Dsec : 0);
-      const int idw = (int)(ii / tgt.dimup);
-      const int iup = (int)(ii - (int64_t)idw * tgt.dimup);
-      const unsigned w = (unsigned)(c.spin == 0 ? tgt.up_words[iup] : tgt.dw_words[idw]);
-      double vr = 0.0, vi = 0.0;
-      for (int q = 0; q < c.nterm; q++) {
-        const int pos = c.pos[q];
-        const bool occ = (w >> pos) & 1u;
-        if (c.dag ? !occ : occ) continue;
-        const unsigned ws = w ^ (1u << pos);
-        const double sg = parity(ws & ((1u << pos) - 1u));
-        const int rs = rank_word(ws);
-        const int64_t si = (c.spin == 0) ? ((int64_t)rs + (int64_t)idw * c.src_dimup)
-                                         : ((int64_t)iup + (int64_t)rs * c.src_dimup);
-        double gr, gi = 0.0;
-        if (sizeof(T) == sizeof(double2)) {
-          const double2 gv = ((const double2*)c.gs)[si];
-          gr = gv.x;
-          gi = gv.y;
-        } else {
-          gr = ((const double*)c.gs)[si];
+__global__ void __launch_bounds__(512) k_mc_chain_init(McGroup gp, T* X, double* tpart) {
+  __shared__ double red[MC_BY_MAX][33];
+  for (int tile = blockIdx.x; tile < gp.ntiles; tile += gridDim.x) {
+    const McTask tk = gp.tasks[gp.tile_task[tile]];
+    const SectorView& tgt = tk.sv;
+    const int64_t r0 = gp.tile_row0[tile], r1 = gp.tile_row1[tile];
+    for (int cb = 0; cb < tk.m; cb += 32) {
+      const int c = cb + threadIdx.x;
+      const bool ok = c < tk.m;
+      double acc = 0.0;
+      if (ok) {
+        const int ch = gp.col_chain[tk.col0 + c];
+        const int part = gp.col_part[tk.col0 + c];
+        const MtChain op = gp.chains[ch].op;
+        for (int64_t i = r0 + threadIdx.y; i < r1; i += blockDim.y) {
+          const int idw = (int)(i / tgt.dimup);
+          const int iup = (int)(i - (int64_t)idw * tgt.dimup);
+          const unsigned w = (unsigned)(op.spin == 0 ? tgt.up_words[iup] : tgt.dw_words[idw]);
+          double vr = 0.0, vi = 0.0;
+          for (int q = 0; q < op.nterm; q++) {
+            const int pos = op.pos[q];
+            const bool occ = (w >> pos) & 1u;
+            if (op.dag ? !occ : occ) continue;
+            const unsigned ws = w ^ (1u << pos);
+            const double sg = parity(ws & ((1u << pos) - 1u));
+            const int rs = rank_word(ws);
+            const int64_t si = (op.spin == 0) ? ((int64_t)rs + (int64_t)idw * op.src_dimup)
+                                              : ((int64_t)iup + (int64_t)rs * op.src_dimup);
+            double gr, gi = 0.0;
+            if (sizeof(T) == sizeof(double2)) {
+              const double2 gv = ((const double2*)op.gs)[si];
+              gr = gv.x;
+              gi = gv.y;
+            } else {
+              gr = ((const double*)op.gs)[si];
+            }
+            const double ar = op.cre[q] * sg, ai = op.cim[q] * sg;
+            vr += ar * gr - ai * gi;
+            vi += ar * gi + ai * gr;
+          }
+          const int64_t e = tk.xoff + i * tk.m + c;
+          if (sizeof(T) == sizeof(double2)) {
+            ((double2*)X)[e] = make_double2(vr, vi);
+            acc += vr * vr + vi * vi;
+          } else {
+            const double v = part ? vi : vr;
+            ((double*)X)[e] = v;
+            acc += v * v;
+          }
         }
-        const double ar = c.cre[q] * sg, ai = c.cim[q] * sg;
-        vr += ar * gr - ai * gi;
-        vi += ar * gi + ai * gr;
       }
-      if (sizeof(T) == sizeof(double2)) {
-        ((double2*)X)[S.off + i] = make_double2(vr, vi);
-        acc += vr * vr + vi * vi;
-      } else {
-        const double v = comp ? vi : vr;
-        ((double*)X)[S.off + i] = v;
-        acc += v * v;
+      red[threadIdx.y][threadIdx.x] = acc;
+      __syncthreads();
+      if (threadIdx.y == 0 && ok) {
+        double sum = 0.0;
+        for (int y = 0; y < (int)blockDim.y; y++) sum += red[y][threadIdx.x];
+        tpart[tk.part0 + (int64_t)(tile - tk.tile0) * tk.m + c] = sum;
       }
-    }
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-      if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
       __syncthreads();
     }
-    if (threadIdx.x == 0) tpart[t] = red[0];
-    __syncthreads();
   }
 }
-void mt_launch_chain_init(const MsGroup& gp, bool cplx, const MtChain* d_ch, void* X, double* tpart,
-                          cudaStream_t st) {
+void mc_launch_chain_init(const McGroup& gp, bool cplx, void* X, double* tpart, cudaStream_t st) {
   COUNT_LAUNCH();
-  const int nb = std::min(gp.ntiles, 152 * 8);
-  if (cplx)
-    k_mt_chain_init<double2><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, d_ch, (double2*)X, tpart);
-  else
-    k_mt_chain_init<double><<<nb, 256, 0, st>>>(gp.secs, gp.tsec, gp.tstart, gp.ntiles, d_ch, (double*)X, tpart);
+  const int nb = gp.ntiles < 152 * 8 ? gp.ntiles : 152 * 8;
+  if (cplx) k_mc_chain_init<double2><<<nb, dim3(32, gp.by), 0, st>>>(gp, (double2*)X, tpart);
+  else k_mc_chain_init<double><<<nb, dim3(32, gp.by), 0, st>>>(gp, (double*)X, tpart);
 }
 
 void launch_chain_init(const SectorView& tgt, int src_dimup, const void* gs, bool gs_cplx,

@@ -57,11 +57,12 @@ void m64_launch_step(const MsGroup& gp, bool cplx, const MixedDiag& md, int k, d
 void m64_launch_check(const MsGroup& gp, Ms64Bufs& b, double tol, cudaStream_t st);
 
 // ---- multi-task Lanczos over many variational points (the batched form) --
-// The FP64 step kernels above run any list of tasks: (point, sector) ground-
-// state searches, their eigenvector passes, and (point, chain) Green's-
-// function chains; a task's SectorView carries its point's hop tables.
+// The FP64 step kernels above run any list of tasks: the (point, sector)
+// ground-state searches and their eigenvector passes; a task's SectorView
+// carries its point's hop tables.  (The chains run as column batches,
+// vca_batch.cuh.)
 //
-// A chain task's start vector is an operator applied to its point's ground
+// A chain's start vector is an operator applied to its point's ground
 // state: sum_q coef_q c^(dag)_{pos_q, spin}|gs> (VCA_GF_NORMAL.f90:121-318,
 // 561-958), gathered per target element with the reference's one-word signs.
 struct MtChain {
@@ -71,9 +72,6 @@ struct MtChain {
   int pos[2];
   double cre[2], cim[2];
 };
-// X = start vectors of the chain tasks, tpart = per-tile |x|^2 partials
-void mt_launch_chain_init(const MsGroup& gp, bool cplx, const MtChain* d_ch, void* X, double* tpart,
-                          cudaStream_t st);
 // per task: n2 = |x|^2 (fixed-order sum of the tile partials), invn = 1/|x|
 // (0 and the task retired when the vector vanishes)
 void mt_launch_norm(const MsGroup& gp, const double* tpart, ChainMeta* meta, double* n2, double* invn,

@@ -38,7 +38,7 @@ EXPORTS = [
     "vca_gpu_get_docc", "vca_gpu_get_mag",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_set_ql_max_iter", "vca_gpu_sector_bounds",
-    "vca_gpu_set_omega_inverse_form", "vca_gpu_timer_start",
+    "vca_gpu_set_omega_inverse_form", "vca_gpu_set_autotune", "vca_gpu_timer_start",
     "vca_gpu_timer_stop",
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
@@ -134,6 +134,7 @@ def load(path: Optional[str] = None):
         "vca_gpu_set_ql_max_iter": (ctypes.c_int, [i32]),
         "vca_gpu_sector_bounds": (ctypes.c_int, [dp, i32]),
         "vca_gpu_set_omega_inverse_form": (ctypes.c_int, [i32]),
+        "vca_gpu_set_autotune": (ctypes.c_int, [i32]),
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
         "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
@@ -271,8 +272,8 @@ class VcaSolver:
         """Stage wall times (ms) of the last solve, or with batched=True of
         the last batched-form solve_batch (tables, search, eigenvectors,
         chains, Omega, closing plain solve)."""
-        out = np.zeros(11)
-        check(self.L.vca_gpu_get_timings(_dp(out), 11))
+        out = np.zeros(13)
+        check(self.L.vca_gpu_get_timings(_dp(out), 13))
         return out[4:] if batched else out[:4]
 
     def arith_info(self):
@@ -297,6 +298,10 @@ class VcaSolver:
         out = np.zeros(n)
         check(self.L.vca_gpu_sector_bounds(_dp(out), n))
         return out
+
+    def set_autotune(self, on: bool):
+        """Tune the batched chains' tile shape at first use (default on)."""
+        check(self.L.vca_gpu_set_autotune(1 if on else 0))
 
     def set_omega_inverse_form(self, on: bool):
         """T=0 k-sum through G'^-1 + M_k below w = 10 (default on)."""
