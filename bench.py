@@ -336,6 +336,7 @@ def run_gpu(args):
         out["finite_t"] = finite_t_sample(cpu=(world == 1 and not args.no_cpu))
         out["batched_c3"] = batched_block("c3", args.batch_c3, 4, 2)
         out["batched_c4"] = batched_block("c4", args.batch_c4, 8, 2)
+        out["surrogate_search"] = search_block()
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample, _, _ = cpu_sample(pts[0], os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
@@ -484,6 +485,51 @@ def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
             "max_rel_dOmega_vs_plain": max(d_loop, d_sat)}
 
 
+def search_block() -> dict:
+    """Stationary-point searches of Omega over (t', M_AF, staggered charge
+    field) of the 2x2 Hubbard cluster (U=8, half filling, 8x8 k, 100-step
+    chains, 512 nodes): the plain Newton search (central differences of
+    plain solves), the drivers' one-parameter Brent cycled over the
+    parameters, and the surrogate-guided search (the network trained on the
+    GPU on solver values and forward-difference gradients); every Omega is a
+    plain FP64 solve, counted."""
+    import numpy as np
+    from vca_gb300 import clusters
+    from vca_gb300.solver import VcaSolver
+    from vca_gb300.surrogate import CountingSolver, coordinate_brent_search, newton_fd_search, surrogate_search
+    lo, hi = clusters.SEARCH_LO, clusters.SEARCH_HI
+    p0 = 0.5 * (lo + hi)
+    pt = clusters.search_point(p0)
+    s = VcaSolver(pt.cfg)
+    s.upload_hk(pt.Hk)
+
+    def solve(p):
+        return s.solve_resident(clusters.search_point(p).Hloc)
+    out = {"workload": "2x2 Hubbard U=8 half filling, Nspin=2, 8x8 k, 100-step chains, 512 nodes; "
+                       "box t' in [1.1,1.7], M_AF in [0.2,0.55], charge field in [-0.2,0.2]"}
+    f = CountingSolver(solve)
+    t0 = time.perf_counter()
+    p_n, om_n, it = newton_fd_search(f, p0, lo, hi)
+    out["plain_newton"] = {"calls": f.calls, "iterations": it, "omega": om_n, "point": p_n.tolist(),
+                           "s": round(time.perf_counter() - t0, 2)}
+    f = CountingSolver(solve)
+    t0 = time.perf_counter()
+    p_b, om_b, cyc = coordinate_brent_search(f, p0, lo, hi, ["min", "min", "max"])
+    out["plain_coordinate_brent"] = {"calls": f.calls, "cycles": cyc, "dOmega": om_b - om_n,
+                                     "s": round(time.perf_counter() - t0, 2)}
+    f = CountingSolver(solve)
+    t0 = time.perf_counter()
+    p_s, om_s, hist = surrogate_search(f, lo, hi, p0, n_design=10, steps=4000)
+    out["surrogate"] = {"calls": f.calls, "omega": om_s, "dOmega_vs_newton": om_s - om_n, "point": p_s.tolist(),
+                        "s": round(time.perf_counter() - t0, 2),
+                        "rounds": [{"dOmega": h["omega"] - om_n, "surrogate_error": h["surrogate_error"],
+                                    "omega_gap_estimate": h["omega_gap_estimate"]} for h in hist]}
+    out["calls_ratio_vs_newton"] = round(out["plain_newton"]["calls"] / f.calls, 2)
+    out["calls_ratio_vs_coordinate_brent"] = round(out["plain_coordinate_brent"]["calls"] / f.calls, 2)
+    s.close()
+    return out
+
+
 def hxv_single_4x4(reps: int = 10) -> dict:
     """One H x v of a unit vector on sector (8,8) of the 4x4 Hubbard cluster
     (D = 12870^2 = 165,636,900), CUDA events on the library stream;
@@ -590,7 +636,8 @@ def main():
         from vca_gb300 import build as vbuild
         vbuild.build()
         print(json.dumps({"batched_c3": batched_block("c3", args.batch_c3, 4, 2),
-                          "batched_c4": batched_block("c4", args.batch_c4, 8, 2)}))
+                          "batched_c4": batched_block("c4", args.batch_c4, 8, 2),
+                          "surrogate_search": search_block()}))
         return 0
     if args.impl == "reference":
         return run_reference(args)

@@ -277,3 +277,23 @@ def batch_bhz(B: int = 1024, seed: int = SEED, **kw):
     rng = np.random.Generator(np.random.PCG64(seed + 4))
     pts = rng.uniform([1.5, -0.2], [2.5, 0.2], size=(B, 2))
     return [bhz(mass=p[0], delta=p[1], **kw) for p in pts]
+
+
+# ---------------------------------------------------------------------------
+# The stationary-point search problem of the surrogate: a 2x2 cluster stands
+# in for the 4x4 one (whose single solve takes minutes), same inputs
+# ---------------------------------------------------------------------------
+SEARCH_PARAMS = ("tprime", "maf", "cdw")
+SEARCH_LO = np.array([1.1, 0.2, -0.2])
+SEARCH_HI = np.array([1.7, 0.55, 0.2])
+
+
+def search_point(p, nkx: int = 8, ngfiter: int = 100, omega_nodes: int = 512) -> SolvePoint:
+    """2x2 Hubbard cluster at half filling (U = 8, xmu = 4, Nspin = 2) with
+    variational (t', M_AF, staggered charge field), 8x8 k-grid.  Omega has an
+    interior stationary point in the box SEARCH_LO..SEARCH_HI near
+    (1.35, 0.33, 0): a minimum in t' and M_AF, a maximum in the charge field.
+    (A cluster mu' would enter Omega linearly here, with slope -<N> = -4, so
+    it has no stationary point and is not searched.)"""
+    return square(nx=2, ny=2, U=8.0, xmu=4.0, tprime=float(p[0]), maf=float(p[1]), cdw=float(p[2]), nspin=2,
+                  nkx=nkx, nky=nkx, ngfiter=ngfiter, omega_nodes=omega_nodes)

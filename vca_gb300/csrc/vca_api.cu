@@ -2424,12 +2424,12 @@ int mc_upload(const McHost& h, int by, Arena& ar, McGroup& gp, ChainMeta** d_met
 }
 
 // Autotuner of the chains' tile shape: rows per tile R and row lanes per
-// block by.  Each candidate runs the chain step's H x v (the dominant
-// kernel) three times on the group's first tasks (up to 2^24 elements),
-// timed by CUDA events; the fastest shape is kept per (real/complex,
-// log2 mean dimension, log2 mean width) for the life of the process.  The
-// shape changes the summation order of the chain's dot products (at the
-// 1e-16 level), not what is summed.
+// block by.  Each candidate runs one whole chain step (H x v, the two
+// reductions, the update and the scaling) three times on the group's first
+// tasks (up to 2^24 elements), timed by CUDA events; the fastest shape is
+// kept per (real/complex, log2 mean dimension, log2 mean width) for the life
+// of the process.  The shape changes the summation order of the chain's dot
+// products (at the 1e-16 level), not what is summed.
 struct McShape { int R = MC_ROWS, by = 8; double ms = 0.0; bool tuned = false; };
 McShape mc_autotune(const std::vector<McTaskRef>& refs, size_t t0, size_t t1,
                     const std::vector<std::vector<BChain>>& pch, const std::vector<PointTabs>& tabs, bool cplx,
@@ -2455,28 +2455,37 @@ McShape mc_autotune(const std::vector<McTaskRef>& refs, size_t t0, size_t t1,
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   best.ms = INFINITY;
-  for (int R : {32, 64, 128, 256}) {
+  for (int R : {64, 256, 1024}) {
     McHost h;
     mc_build(refs, t0, t1s, pch, tabs, R, g->cfg.lanc_ngfiter, h);
     Arena ar;
     McGroup gp;
     ChainMeta* d_meta;
-    double *d_tp, *d_bn;
+    double *d_tp, *d_bn, *d_al;
     char *x0, *x1, *x2;
     const int nch = (int)h.chains.size();
     if (mc_upload(h, 8, ar, gp, &d_meta) || ar.alloc(&d_tp, (size_t)h.part) || ar.alloc(&d_bn, nch) ||
-        ar.alloc(&x0, (size_t)h.xoff * es) || ar.alloc(&x1, (size_t)h.xoff * es) || ar.alloc(&x2, (size_t)h.xoff * es)) {
+        ar.alloc(&d_al, nch) || ar.alloc(&x0, (size_t)h.xoff * es) || ar.alloc(&x1, (size_t)h.xoff * es) ||
+        ar.alloc(&x2, (size_t)h.xoff * es)) {
       ar.release();
       continue;
     }
     cudaMemsetAsync(x0, 0, (size_t)h.xoff * es, g->st);
     cudaMemsetAsync(x1, 0, (size_t)h.xoff * es, g->st);
     cudaMemsetAsync(d_bn, 0, sizeof(double) * nch, g->st);
+    cudaMemsetAsync(d_al, 0, sizeof(double) * nch, g->st);
+    auto step = [&]() {
+      mc_launch_hxv(gp, cplx, g->md, d_meta, d_bn, 1, x0, x1, x2, d_tp, g->st);
+      mc_launch_reduce(gp, d_tp, d_al, g->st);
+      mc_launch_update(gp, cplx, d_meta, d_bn, x0, x2, d_tp, g->st);
+      mc_launch_reduce(gp, d_tp, d_al, g->st);
+      mc_launch_scale(gp, cplx, d_meta, d_bn, x2, x2, g->st);
+    };
     for (int by : {4, 8, 16}) {
       gp.by = by;
-      mc_launch_hxv(gp, cplx, g->md, d_meta, d_bn, 1, x0, x1, x2, d_tp, g->st);  // warm-up
+      step();  // warm-up
       cudaEventRecord(e0, g->st);
-      for (int r = 0; r < 3; r++) mc_launch_hxv(gp, cplx, g->md, d_meta, d_bn, 1, x0, x1, x2, d_tp, g->st);
+      for (int r = 0; r < 3; r++) step();
       cudaEventRecord(e1, g->st);
       float ms = 0.0f;
       if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(512) k_mc_hxv(McGroup gp, MixedDiag md, const 
         acc += bre(xi, y);
       }
       if (ok && !meta[ch].active) acc = 0.0;
-      tile_col_store(acc, tpart, tk.part0 + (int64_t)(tile - tk.tile0) * tk.m + c, ok);
+      tile_col_store(acc, tpart, tk.part0 + (int64_t)c * tk.ntile + (tile - tk.tile0), ok);
     }
   }
 }
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(512) k_mc_update(McGroup gp, const ChainMeta* 
           Y[e] = y;
           acc += bre(y, y);
         }
-      tile_col_store(acc, tpart, tk.part0 + (int64_t)(tile - tk.tile0) * tk.m + c, ok);
+      tile_col_store(acc, tpart, tk.part0 + (int64_t)c * tk.ntile + (tile - tk.tile0), ok);
     }
   }
 }
@@ -147,7 +147,8 @@ __global__ void k_mc_reduce(McGroup gp, const double* tpart, double* out) {
     double s = 0.0;
     for (int q = 0; q < cc.ncol; q++) {
       const int c = cc.col0 + q;
-      for (int t = lane; t < tk.ntile; t += 32) s += tpart[tk.part0 + (int64_t)t * tk.m + c];
+      const double* pc = tpart + tk.part0 + (int64_t)c * tk.ntile;  // the column's tiles, contiguous
+      for (int t = lane; t < tk.ntile; t += 32) s += pc[t];
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);

@@ -27,7 +27,7 @@ struct McTask {
   int col0;       // first column of the task (global column numbering)
   int64_t xoff;   // element offset of the task's block
   int tile0, ntile;
-  int64_t part0;  // partial (tile, c) at part0 + (tile - tile0) * m + c
+  int64_t part0;  // partial (tile, c) at part0 + c * ntile + (tile - tile0): a column's tiles contiguous
 };
 
 struct McChain {  // one chain: columns col0 .. col0 + ncol - 1 of task `task`

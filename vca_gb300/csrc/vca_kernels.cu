@@ -724,7 +724,7 @@ __global__ void __launch_bounds__(512) k_mc_chain_init(McGroup gp, T* X, double*
       if (threadIdx.y == 0 && ok) {
         double sum = 0.0;
         for (int y = 0; y < (int)blockDim.y; y++) sum += red[y][threadIdx.x];
-        tpart[tk.part0 + (int64_t)(tile - tk.tile0) * tk.m + c] = sum;
+        tpart[tk.part0 + (int64_t)c * tk.ntile + (tile - tk.tile0)] = sum;
       }
       __syncthreads();
     }
