@@ -334,8 +334,8 @@ def run_gpu(args):
         s.close()
         out["hxv_single_4x4"] = hxv_single_4x4()
         out["finite_t"] = finite_t_sample(cpu=(world == 1 and not args.no_cpu))
-        out["batched_c3"] = batched_block("c3", args.batch_c3, 4, 2)
-        out["batched_c4"] = batched_block("c4", args.batch_c4, 8, 2)
+        out["batched_c3"] = batched_block("c3", args.batch_c3, 8, 3)
+        out["batched_c4"] = batched_block("c4", args.batch_c4, 8, 3)
         out["surrogate_search"] = search_block()
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample, _, _ = cpu_sample(pts[0], os.cpu_count() or 1)
@@ -462,11 +462,15 @@ def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
     batched search), and the reference's loop structure (one sector per
     Lanczos run).  Host arrays in, Omega out; wall time of the call."""
     pts, desc = batch_points(which, B)
+    # the plain paths run on points spread evenly over the batch (the points'
+    # ground states, and so their chains, differ from point to point)
+    il = [round(i * (B - 1) / max(1, n_loop - 1)) for i in range(n_loop)]
+    isat = [round(i * (B - 1) / max(1, n_sat - 1)) for i in range(n_sat)]
     om_b, t_b, st_b = _solve_points(pts, 0)
-    om_l, t_l, _ = _solve_points(pts[:n_loop], 1)
-    om_s, t_s, _ = _solve_points(pts[:n_sat], 1, 1)
-    d_loop = max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(om_b[:n_loop], om_l))
-    d_sat = max(abs(a - b) / max(1.0, abs(b)) for a, b in zip(om_b[:n_sat], om_s))
+    om_l, t_l, _ = _solve_points([pts[i] for i in il], 1)
+    om_s, t_s, _ = _solve_points([pts[i] for i in isat], 1, 1)
+    d_loop = max(abs(om_b[i] - b) / max(1.0, abs(b)) for i, b in zip(il, om_l))
+    d_sat = max(abs(om_b[i] - b) / max(1.0, abs(b)) for i, b in zip(isat, om_s))
     v_b, v_l, v_s = B / t_b, n_loop / t_l, n_sat / t_s
     return {"workload": desc, "unit": "Omega evals/s",
             "batched": {"points": B, "value": round(v_b, 4), "ms_per_eval": round(1e3 * t_b / B, 2),
@@ -476,9 +480,9 @@ def batched_block(which: str, B: int, n_loop: int, n_sat: int) -> dict:
                         "chain_tile_shape": {"rows_per_tile": int(st_b[7]), "row_lanes_per_block": int(st_b[8]),
                                              "chosen_by": "autotuner"},
                         "sector_searches_total": B * _nsectors(pts[0].cfg)},
-            "plain_per_point": {"points": n_loop, "value": round(v_l, 4), "ms_per_eval": round(1e3 * t_l / n_loop, 2),
+            "plain_per_point": {"points": il, "value": round(v_l, 4), "ms_per_eval": round(1e3 * t_l / n_loop, 2),
                                 "what": "one point after another, every sector of a point in one batched search"},
-            "plain_sector_at_a_time": {"points": n_sat, "value": round(v_s, 4),
+            "plain_sector_at_a_time": {"points": isat, "value": round(v_s, 4),
                                        "ms_per_eval": round(1e3 * t_s / n_sat, 2),
                                        "what": "one point and one sector at a time (the reference's loops)"},
             "ratio_vs_sector_at_a_time": round(v_b / v_s, 2), "ratio_vs_per_point": round(v_b / v_l, 2),
@@ -635,8 +639,8 @@ def main():
     if args.batched_only:
         from vca_gb300 import build as vbuild
         vbuild.build()
-        print(json.dumps({"batched_c3": batched_block("c3", args.batch_c3, 4, 2),
-                          "batched_c4": batched_block("c4", args.batch_c4, 8, 2),
+        print(json.dumps({"batched_c3": batched_block("c3", args.batch_c3, 8, 3),
+                          "batched_c4": batched_block("c4", args.batch_c4, 8, 3),
                           "surrogate_search": search_block()}))
         return 0
     if args.impl == "reference":
