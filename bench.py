@@ -588,6 +588,33 @@ def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
     return 0
 
 
+def profile_batch(which: str, points: int, autotune: bool) -> int:
+    """Batched form on the first points of the C3 or C4 batch (FP64), then one
+    plain solve of the first point (for ncu captures of the batched kernels)."""
+    import numpy as np
+    from vca_gb300 import build as vbuild
+    vbuild.build()
+    from vca_gb300.solver import VcaSolver
+    pts, _ = batch_points(which, points)
+    Hl = np.stack([p.Hloc for p in pts], axis=-1)
+    bh = np.stack([p.bath_h for p in pts], axis=-1) if pts[0].bath_h is not None else None
+    bv = np.stack([p.bath_v for p in pts], axis=-1) if pts[0].bath_v is not None else None
+    cfg = pts[0].cfg.copy()
+    cfg.arith = 1
+    s = VcaSolver(cfg, pts[0].bath_h, pts[0].bath_v)
+    s.set_autotune(autotune)
+    t0 = time.perf_counter()
+    om = s.solve_batch(Hl, pts[0].Hk, bh, bv)
+    tb = time.perf_counter() - t0
+    stages = s.timings(batched=True).tolist()
+    t0 = time.perf_counter()
+    o1 = s.solve(pts[0].Hloc, pts[0].Hk, pts[0].bath_h, pts[0].bath_v)
+    print(json.dumps({"batched_s": tb, "batched_stage_ms": stages, "plain_s": time.perf_counter() - t0,
+                      "plain_stage_ms": s.timings().tolist(), "omega0": [float(om[0]), o1]}))
+    s.close()
+    return 0
+
+
 def profile_solve() -> int:
     """One warm-up and one timed plain solve of a reduced 4x3 point."""
     from vca_gb300 import build as vbuild, clusters
@@ -624,6 +651,10 @@ def main():
     ap.add_argument("--batch-c3", type=int, default=32, help="points of the C3 batch timed in the batched block")
     ap.add_argument("--batch-c4", type=int, default=256, help="points of the C4 batch timed in the batched block")
     ap.add_argument("--batched-only", action="store_true", help="only the batched block (C3 and C4)")
+    ap.add_argument("--profile-batch", choices=["c3", "c4"], default=None,
+                    help="profiling mode: batched form on --points points of the C3/C4 batch, then a plain solve")
+    ap.add_argument("--points", type=int, default=4)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--hxv-variant", type=int, default=2,
                     help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
     args = ap.parse_args()
@@ -636,6 +667,8 @@ def main():
         vbuild.build()
         print(json.dumps(hxv_single_4x4(args.reps)))
         return 0
+    if args.profile_batch:
+        return profile_batch(args.profile_batch, args.points, not args.no_autotune)
     if args.batched_only:
         from vca_gb300 import build as vbuild
         vbuild.build()
