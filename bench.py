@@ -615,6 +615,30 @@ def profile_batch(which: str, points: int, autotune: bool) -> int:
     return 0
 
 
+def profile_mlp(steps: int) -> int:
+    """Surrogate training on 200 samples of a smooth 4-input function with
+    its gradient (1000 GEMM rows), `steps` Adam steps, then one prediction
+    (for ncu captures of the tensor-core GEMM k_umma_gemm)."""
+    import numpy as np
+    from vca_gb300 import build as vbuild
+    vbuild.build()
+    from vca_gb300.surrogate import SurrogateNet
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, (200, 4))
+    w = np.array([0.7, -0.4, 0.2, 0.5])
+    y = np.sin(x @ w) + 0.3 * (x ** 2).sum(axis=1)
+    dy = np.cos(x @ w)[:, None] * w[None, :] + 0.6 * x
+    net = SurrogateNet(n_in=4, capacity=1024, grad_weight=1.0)
+    net.set_data(x, y, dy)
+    t0 = time.perf_counter()
+    loss = net.train(steps)
+    dt = time.perf_counter() - t0
+    f, df = net.predict(rng.uniform(-1, 1, (1000, 4)))
+    print(json.dumps({"steps": steps, "train_s": dt, "ms_per_step": 1e3 * dt / max(1, steps), "loss": loss}))
+    net.close()
+    return 0
+
+
 def profile_solve() -> int:
     """One warm-up and one timed plain solve of a reduced 4x3 point."""
     from vca_gb300 import build as vbuild, clusters
@@ -654,6 +678,8 @@ def main():
     ap.add_argument("--profile-batch", choices=["c3", "c4"], default=None,
                     help="profiling mode: batched form on --points points of the C3/C4 batch, then a plain solve")
     ap.add_argument("--points", type=int, default=4)
+    ap.add_argument("--profile-mlp", type=int, default=0, metavar="STEPS",
+                    help="profiling mode: STEPS Adam steps of the surrogate on 200 samples with gradients")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--hxv-variant", type=int, default=2,
                     help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
@@ -667,6 +693,8 @@ def main():
         vbuild.build()
         print(json.dumps(hxv_single_4x4(args.reps)))
         return 0
+    if args.profile_mlp:
+        return profile_mlp(args.profile_mlp)
     if args.profile_batch:
         return profile_batch(args.profile_batch, args.points, not args.no_autotune)
     if args.batched_only:
