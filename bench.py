@@ -615,6 +615,24 @@ def profile_batch(which: str, points: int, autotune: bool) -> int:
     return 0
 
 
+def cpu_full_eval(threads: int) -> int:
+    """One complete Omega evaluation of the benchmark workload (sweep point 5,
+    M = 0.1) by the CPU oracle on `threads` host threads, timed, and checked
+    against the committed oracle fixture of that point."""
+    import numpy as np
+    from oracle import oracle as orc
+    from oracle.oracle import Oracle
+    pts = build_points()
+    n = orc.set_threads(threads)
+    t0 = time.perf_counter()
+    om = Oracle.from_point(pts[5]).solve()[0]
+    dt = time.perf_counter() - t0
+    fx = float(np.load(os.path.join(ROOT, "tests", "golden", "config_c2_m05.npz"))["sft"])
+    print(json.dumps({"workload": WORKLOAD, "point": "M = 0.1", "cores": n, "seconds": dt,
+                      "omega": om, "omega_vs_fixture": abs(om - fx) / abs(fx)}))
+    return 0
+
+
 def profile_mlp(steps: int) -> int:
     """Surrogate training on 200 samples of a smooth 4-input function with
     its gradient (1000 GEMM rows), `steps` Adam steps, then one prediction
@@ -681,6 +699,8 @@ def main():
     ap.add_argument("--profile-mlp", type=int, default=0, metavar="STEPS",
                     help="profiling mode: STEPS Adam steps of the surrogate on 200 samples with gradients")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--cpu-full-eval", action="store_true",
+                    help="one complete oracle Omega evaluation of the benchmark workload on all host threads")
     ap.add_argument("--hxv-variant", type=int, default=2,
                     help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
     args = ap.parse_args()
@@ -693,6 +713,8 @@ def main():
         vbuild.build()
         print(json.dumps(hxv_single_4x4(args.reps)))
         return 0
+    if args.cpu_full_eval:
+        return cpu_full_eval(os.cpu_count() or 1)
     if args.profile_mlp:
         return profile_mlp(args.profile_mlp)
     if args.profile_batch:
