@@ -131,30 +131,29 @@ def build_points():
 # ---------------------------------------------------------------------------
 def cpu_sample(pt, threads: int):
     """(estimated Omega evals/s, description, estimated seconds per eval,
-    measured seconds of the sample)."""
+    measured seconds of the sample).  Each stage is sampled in the parallel
+    form the oracle's full evaluation runs it in: sectors diagonalised one per
+    thread (the `threads` largest, scaled by total/sampled dimension), chains
+    one per thread (`threads` 200-step chains on the GF target sector, scaled
+    by chains/threads), and the frequency rule's k-sums parallel over k (8 of
+    the nodes, scaled by the node count)."""
     import numpy as np
     from oracle import oracle as orc
     from oracle.oracle import Oracle
     orc.set_threads(threads)
     o = Oracle.from_point(pt)
     Ns = o.Ns
-    big = 1 + 6 + 6 * (Ns + 1)         # sector (6,6), dim 853,776
     tgt = 1 + 6 + 7 * (Ns + 1)         # GF target sector (7,6), dim 731,808
     t_all = time.perf_counter()
+    dims = np.array([o.dim(s) for s in range(1, o.Nsectors + 1)], dtype=np.float64)
+    big = np.argsort(-dims, kind="stable")[:threads]
+    mask = np.zeros(o.Nsectors, dtype=np.int32)
+    mask[big] = 1
     t0 = time.perf_counter()
-    e, psi, iters = o.lanczos_gs(big)
+    o.diagonalize(mask)
     t_gs = time.perf_counter() - t0
-    dims = [o.dim(s) for s in range(1, o.Nsectors + 1)]
-    gs_total = t_gs * sum(dims) / dims[big - 1]
-    d = o.dim(tgt)
-    rng = np.random.default_rng(1)
-    v = rng.normal(size=d) + 0j
-    v /= np.linalg.norm(v)
-    nch = 2
-    t0 = time.perf_counter()
-    for _ in range(nch):
-        o.lanczos_tridiag(tgt, v, 200)
-    t_chain = (time.perf_counter() - t0) / nch
+    gs_total = t_gs * dims.sum() / dims[big].sum()
+    t_chain = o.chain_sample(tgt, threads, 200)
     L = pt.cfg.Nlat * pt.cfg.Norb
     chains = pt.cfg.Nspin * (2 * L + 4 * L * (L - 1))
     nn = 8
@@ -162,10 +161,11 @@ def cpu_sample(pt, threads: int):
     for w in np.linspace(0.1, 5.0, nn):
         o.sum_kmesh(float(w))
     t_node = (time.perf_counter() - t0) / nn
-    total = gs_total + chains * t_chain + pt.cfg.omega_nodes * t_node
-    sample = (f"oracle (C++/OpenMP restatement) timed on: GS Lanczos of sector (6,6) "
-              f"[{iters} its, {t_gs:.2f}s] scaled by total/largest sector dim; {nch} of {chains} "
-              f"200-step chains on sector (7,6) [{t_chain:.2f}s each]; {nn} of 8192 Omega nodes "
+    total = gs_total + chains / threads * t_chain + pt.cfg.omega_nodes * t_node
+    sample = (f"oracle (C++/OpenMP restatement) on {threads} threads, each stage in the evaluation's own "
+              f"parallel form: the {len(big)} largest of {o.Nsectors} sectors diagonalised one per thread "
+              f"[{t_gs:.2f}s] scaled by total/sampled dimension; {threads} of {chains} 200-step chains on "
+              f"sector (7,6), one per thread [{t_chain:.2f}s]; {nn} of {pt.cfg.omega_nodes} Omega nodes "
               f"[{t_node * 1e3:.1f}ms each]; one eval estimated at {total:.0f}s")
     return 1.0 / total, sample, total, time.perf_counter() - t_all
 
@@ -173,8 +173,9 @@ def cpu_sample(pt, threads: int):
 def run_reference(args):
     """The reference arm: the oracle port (the Fortran reference does not
     build here) on all host threads.  One step is one bounded sample of an
-    Omega evaluation at the benchmark configuration (the largest sector's
-    ground-state Lanczos, 2 of the 1104 chains, 8 of the 8192 Omega nodes);
+    Omega evaluation at the benchmark configuration, each stage in the
+    evaluation's own parallel form (the largest sectors' ground states one per
+    thread, one chain per thread, 8 of the 8192 Omega nodes; cpu_sample);
     ms_per_step is that sample's measured wall time, and value the Omega
     evals/s the sample implies (its parts scaled to a whole evaluation)."""
     rank, world, _ = dist_env()
@@ -537,31 +538,49 @@ def search_block() -> dict:
 def hxv_single_4x4(reps: int = 10) -> dict:
     """One H x v of a unit vector on sector (8,8) of the 4x4 Hubbard cluster
     (D = 12870^2 = 165,636,900), CUDA events on the library stream;
-    algorithmic bytes 16*D (read v, write Hv)."""
+    algorithmic bytes 16*D (read v, write Hv).  The paired-column form (the
+    library's) and the one-column form (hxv_variant 1) on the same vector;
+    their outputs must agree bit for bit."""
     import torch
     from vca_gb300 import clusters
     from vca_gb300.solver import VcaSolver
     pt = clusters.square(nx=4, ny=4, U=8.0, xmu=4.0, maf=0.0, nspin=1, nkx=4, nky=4, ngfiter=10,
                          omega_nodes=64)
-    s4 = VcaSolver(pt.cfg)
-    s4.set_hamiltonian(pt.Hloc)
     isec = 1 + 8 + 8 * 17
-    _, _, du, dd = s4.sector_info(isec)
-    D = du * dd
-    fx, F, _ = s4.arith_info()
-    x = torch.randn(D, dtype=torch.float64, device="cuda")
-    x /= torch.linalg.vector_norm(x)
-    if fx:
-        x = torch.round(x * 2.0 ** F).to(torch.int64)
-    y = torch.empty_like(x)
-    ms = s4.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, 1, reps)
     peak, kind = measured_peaks()
-    gbs = 16.0 * D / (ms / 1e3) / 1e9
-    del x, y
-    s4.close()
-    return {"sector": [8, 8], "D": D, "arith": "fx" if fx else "f64", "launch_ms": round(ms, 4),
-            "kernels": "k_hxv1_up + k_hxv1_dw", "achieved_GBps": round(gbs, 1), "peak": peak,
-            "frac": round(gbs / peak, 4), "peak_kind": kind}
+    out = {"sector": [8, 8], "peak": peak, "peak_kind": kind}
+    x = y = y0 = None
+    for variant, name, kernels in ((0, "paired", "k_hxv1_up2 + k_hxv1_dw2"), (1, "one_column", "k_hxv1_up + k_hxv1_dw")):
+        cfg = pt.cfg.copy()
+        cfg.hxv_variant = variant
+        s4 = VcaSolver(cfg)
+        s4.set_hamiltonian(pt.Hloc)
+        _, _, du, dd = s4.sector_info(isec)
+        D = du * dd
+        fx, F, _ = s4.arith_info()
+        if x is None:
+            g = torch.Generator(device="cuda").manual_seed(4)
+            x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+            x /= torch.linalg.vector_norm(x)
+            if fx:
+                x = torch.round(x * 2.0 ** F).to(torch.int64)
+            y = torch.empty_like(x)
+        ms = s4.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, 1, reps)
+        s4.close()
+        gbs = 16.0 * D / (ms / 1e3) / 1e9
+        out["D"] = D
+        out["arith"] = "fx" if fx else "f64"
+        out[name] = {"kernels": kernels, "launch_ms": round(ms, 4), "achieved_GBps": round(gbs, 1),
+                     "frac": round(gbs / peak, 4)}
+        if y0 is None:
+            y0 = y.clone()
+        else:
+            out["bit_identical"] = bool(torch.equal(y0, y))
+    # headline fields: the library's form
+    out.update({"launch_ms": out["paired"]["launch_ms"], "kernels": out["paired"]["kernels"],
+                "achieved_GBps": out["paired"]["achieved_GBps"], "frac": out["paired"]["frac"]})
+    del x, y, y0
+    return out
 
 
 def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
@@ -617,19 +636,23 @@ def profile_batch(which: str, points: int, autotune: bool) -> int:
 
 def cpu_full_eval(threads: int) -> int:
     """One complete Omega evaluation of the benchmark workload (sweep point 5,
-    M = 0.1) by the CPU oracle on `threads` host threads, timed, and checked
-    against the committed oracle fixture of that point."""
+    M = 0.1) by the CPU oracle on `threads` host threads, timed by stage and
+    checked against the committed oracle fixture of that point, beside the
+    reference arm's bounded-sample estimate for the same point."""
     import numpy as np
     from oracle import oracle as orc
     from oracle.oracle import Oracle
     pts = build_points()
     n = orc.set_threads(threads)
     t0 = time.perf_counter()
-    om = Oracle.from_point(pts[5]).solve()[0]
+    om, _, _, stages = Oracle.from_point(pts[5]).solve_timed()
     dt = time.perf_counter() - t0
     fx = float(np.load(os.path.join(ROOT, "tests", "golden", "config_c2_m05.npz"))["sft"])
+    _, sample, est, wall = cpu_sample(pts[5], threads)
     print(json.dumps({"workload": WORKLOAD, "point": "M = 0.1", "cores": n, "seconds": dt,
-                      "omega": om, "omega_vs_fixture": abs(om - fx) / abs(fx)}))
+                      "stage_seconds": {"diagonalize": stages[0], "chains": stages[1], "omega": stages[2]},
+                      "omega": om, "omega_vs_fixture": abs(om - fx) / abs(fx),
+                      "sample_estimate_s": est, "sample_wall_s": wall, "sample": sample}))
     return 0
 
 

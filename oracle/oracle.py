@@ -70,6 +70,8 @@ def lib():
             "orc_gauss_legendre01": (I, [I, dp, dp]),
             "orc_frequency_integration": (D, [P]),
             "orc_solve": (D, [P, dp, dp]),
+            "orc_solve_timed": (D, [P, dp, dp, dp]),
+            "orc_chain_sample": (D, [P, I, I, I]),
             "orc_sum_kmesh_complex": (D, [P, D, D, dp]),
             "orc_contour_rule": (I, [D, D, D, I, dp, dp, I]),
             "orc_contour_integrand": (D, [P, D, D]),
@@ -374,6 +376,20 @@ class Oracle:
         oi = ctypes.c_double()
         sft = self.L.orc_solve(self.h, ctypes.byref(egs), ctypes.byref(oi))
         return sft, egs.value, oi.value
+
+    def solve_timed(self):
+        """solve() plus the wall seconds of its stages (diagonalisation,
+        chains, frequency integration)."""
+        egs = ctypes.c_double()
+        oi = ctypes.c_double()
+        st = np.zeros(3)
+        sft = self.L.orc_solve_timed(self.h, ctypes.byref(egs), ctypes.byref(oi), _dp(st))
+        return sft, egs.value, oi.value, st.tolist()
+
+    def chain_sample(self, isector: int, nchains: int, nlanc: int) -> float:
+        """Wall seconds of nchains chains of nlanc steps on sector isector run
+        as the chain stage runs them (one per thread)."""
+        return self.L.orc_chain_sample(self.h, isector, nchains, nlanc)
 
 
 def state_list_t0(E, gs_threshold: float):

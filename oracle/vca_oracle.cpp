@@ -1904,6 +1904,29 @@ int orc_lanczos_tridiag(void* h, int isector, const double* v1, int nlanc, doubl
   for (int i = 0; i < nlanc; i++) { a[i] = al[i]; b[i] = bl[i]; }
   return 0;
 }
+// Timing sample of the chain stage in its own parallel form (build_gf: one
+// chain per thread, dynamic schedule, the H x v inside serial): nchains
+// chains of nlanc steps on sector isector, each building the sector's
+// tables and starting from its own seeded unit vector, as run_chain does.
+// Returns the wall seconds.
+double orc_chain_sample(void* h, int isector, int nchains, int nlanc) {
+  Oracle* o = (Oracle*)h;
+  const double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int q = 0; q < nchains; q++) {
+    SectorH J = build_sector_h(*o, isector);
+    std::vector<cd> v(J.dim);
+    double n2 = 0.0;
+    for (int64_t i = 0; i < J.dim; i++) {
+      v[i] = cd(start_value(1000 + q, isector, i), 0.0);
+      n2 += std::norm(v[i]);
+    }
+    for (auto& x : v) x /= std::sqrt(n2);
+    std::vector<double> al, bl;
+    lanczos_tridiag(J, v, (int)std::min<int64_t>(J.dim, nlanc), o->cfg.gf_beta_tol, al, bl);
+  }
+  return omp_get_wtime() - t0;
+}
 int orc_tql2(int n, const double* d, const double* e, double* w, double* z0) {
   std::vector<double> dd(d, d + n), ee(e, e + n), zz;
   int r = tql2(n, dd, ee, zz, nullptr);
@@ -2041,16 +2064,26 @@ int orc_thermal(void* h, double* d7, int* i4) {
 }
 
 // Full vca_solve (VCA_MAIN.f90:124-215): returns the SFT potential
-// Omega' - Omega_int; egs_out receives E_min (E_gs at T=0).
-double orc_solve(void* h, double* egs_out, double* omega_int_out) {
+// Omega' - Omega_int; egs_out receives E_min (E_gs at T=0); stage_s (if
+// given) the wall seconds of its stages: diagonalisation, chains, frequency
+// integration (+ Omega').
+double orc_solve_timed(void* h, double* egs_out, double* omega_int_out, double* stage_s) {
   Oracle* o = (Oracle*)h;
+  const double t0 = omp_get_wtime();
   diagonalize(*o, nullptr);
+  const double t1 = omp_get_wtime();
   build_gf(*o);
+  const double t2 = omp_get_wtime();
   o->omega_int = o->finiteT ? frequency_integration_finite_t(*o) : frequency_integration(*o);
   o->sft = omega_prime(*o) - o->omega_int;
+  const double t3 = omp_get_wtime();
+  if (stage_s) stage_s[0] = t1 - t0, stage_s[1] = t2 - t1, stage_s[2] = t3 - t2;
   if (egs_out) *egs_out = o->egs;
   if (omega_int_out) *omega_int_out = o->omega_int;
   return o->sft;
+}
+double orc_solve(void* h, double* egs_out, double* omega_int_out) {
+  return orc_solve_timed(h, egs_out, omega_int_out, nullptr);
 }
 // the k lowest eigenpairs of a sector in the arpack path (ascending);
 // vecs_out holds k vectors of the sector's dimension (complex, interleaved)

@@ -129,6 +129,11 @@ struct Ctx {
     i64* e1 = nullptr;
   };
   std::vector<PermTabs> fx_ptab[2];  // tables in perm order
+  // bank schedules of the paired-column single-vector kernel (spin spaces
+  // that can be the up role of a sector >= FX1_MIN_DIM), else nullptr
+  std::vector<unsigned*> fx_sched[2];
+  std::vector<int*> fx_wround[2];
+  std::vector<int*> fx_wgrp[2];
   std::vector<HopPair> host_pairs;
   size_t host_pairs_set0 = 0;  // pairs of the up set (the rest are the down set's)
   std::vector<double> host_eps_abs;  // per spin set: bound of |one-body energy|
@@ -284,6 +289,10 @@ FxView fx_view_pair(int sa, int na, int sb, int nb) {
   f.up_pnpos = pt.npos;
   f.up_pword = pt.word;
   f.up_pe1 = pt.e1;
+  // hxv_variant 1 keeps the one-column single-vector form (the comparison arm)
+  f.up_sched = g->cfg.hxv_variant == 1 ? nullptr : g->fx_sched[sa][na];
+  f.up_wround = g->cfg.hxv_variant == 1 ? nullptr : g->fx_wround[sa][na];
+  f.up_wgrp = g->cfg.hxv_variant == 1 ? nullptr : g->fx_wgrp[sa][na];
   return f;
 }
 FxView fx_view_of(int nup, int ndw) { return fx_view_pair(0, nup, g->dwset, ndw); }
@@ -502,6 +511,11 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
         g->fx_npos[set].assign(g->Ns + 1, nullptr);
         g->fx_perm[set].assign(g->Ns + 1, nullptr);
         g->fx_ptab[set].assign(g->Ns + 1, Ctx::PermTabs{});
+        g->fx_sched[set].assign(g->Ns + 1, nullptr);
+        g->fx_wround[set].assign(g->Ns + 1, nullptr);
+        g->fx_wgrp[set].assign(g->Ns + 1, nullptr);
+        int64_t partner = 0;  // largest spin space the other role can take
+        for (int n = 0; n <= g->Ns; n++) partner = std::max<int64_t>(partner, g->sp[nsets - 1 - set][n].dim);
         for (int n = 0; n <= g->Ns; n++) {
           SpinSpace& S = g->sp[set][n];
           RCHK(g->ham.alloc(&g->fx_hop[set][n], (size_t)S.width * S.dim));
@@ -536,6 +550,27 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
           launch_fx_perm_tables(S.dim, S.width, g->fx_perm[set][n], pt.pinv, g->fx_hop[set][n], S.cnt,
                                 g->fx_npos[set][n], S.words, g->fx_e1[set][n], pt.hop, pt.rhop, pt.cnt, pt.npos,
                                 pt.word, pt.e1, g->st);
+          if (S.dim > 0 && fx_pair_fits(S.dim) && (int64_t)S.dim * partner >= FX1_MIN_DIM) {
+            std::vector<int> cnt(S.dim);
+            std::vector<unsigned> hop((size_t)S.width * S.dim), sched;
+            std::vector<int> wround, wgrp;
+            CUCHK(cudaMemcpyAsync(cnt.data(), S.cnt, sizeof(int) * S.dim, cudaMemcpyDeviceToHost, g->st));
+            CUCHK(cudaMemcpyAsync(hop.data(), g->fx_hop[set][n], sizeof(unsigned) * hop.size(),
+                                  cudaMemcpyDeviceToHost, g->st));
+            CUCHK(cudaStreamSynchronize(g->st));
+            if (fx_pair_schedule(S.dim, S.width, fb.K, cnt.data(), hop.data(), sched, wround, wgrp) < 0)
+              VFAIL(VCA_ERR_NUMERIC, "hop schedule of the paired-column form left hops unplaced");
+            RCHK(g->ham.alloc(&g->fx_sched[set][n], std::max<size_t>(1, sched.size())));
+            RCHK(g->ham.alloc(&g->fx_wround[set][n], wround.size()));
+            CUCHK(cudaMemcpyAsync(g->fx_sched[set][n], sched.data(), sizeof(unsigned) * sched.size(),
+                                  cudaMemcpyHostToDevice, g->st));
+            CUCHK(cudaMemcpyAsync(g->fx_wround[set][n], wround.data(), sizeof(int) * wround.size(),
+                                  cudaMemcpyHostToDevice, g->st));
+            RCHK(g->ham.alloc(&g->fx_wgrp[set][n], std::max<size_t>(1, wgrp.size())));
+            CUCHK(cudaMemcpyAsync(g->fx_wgrp[set][n], wgrp.data(), sizeof(int) * wgrp.size(),
+                                  cudaMemcpyHostToDevice, g->st));
+            CUCHK(cudaStreamSynchronize(g->st));  // host vectors go out of scope
+          }
         }
       }
       if (nsets == 1) {
@@ -545,6 +580,9 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
         g->fx_npos[1] = g->fx_npos[0];
         g->fx_perm[1] = g->fx_perm[0];
         g->fx_ptab[1] = g->fx_ptab[0];
+        g->fx_sched[1] = g->fx_sched[0];
+        g->fx_wround[1] = g->fx_wround[0];
+        g->fx_wgrp[1] = g->fx_wgrp[0];
       }
       CUCHK(cudaGetLastError());
       g->fxs = fs;

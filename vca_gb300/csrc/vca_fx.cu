@@ -252,7 +252,303 @@ __global__ void __launch_bounds__(256) k_hxv1_dw(SectorView sv, FxView fv, int c
   }
 }
 
-#define FX1_MIN_DIM (1 << 22)
+// Paired-column up part (+ diagonal): one CTA stages columns idw0 = 2*bx and
+// idw0 + 1 interleaved, one 16-byte unit (X[iup, idw0], X[iup, idw0+1]) per
+// up configuration (then FX1_ZERO_UNITS zero units), and walks the bank
+// schedule (fx_pair_schedule).  A warp's rounds come in groups of one
+// amplitude class and one sign, so a round is one 16-byte shared-memory read
+// and a plain 64-bit add per column: no per-hop class or sign logic.  Each
+// schedule word (the unit's byte offset) serves both columns, the 8 lanes of
+// a quarter warp read distinct units, and the schedule is read from L2 once
+// per two columns.  The int128 sum and its single rounding are those of the
+// one-column form, bit for bit.
+#define FX1_UP2_THREADS 1024
+template <int K>
+__global__ void __launch_bounds__(FX1_UP2_THREADS, 1) k_hxv1_up2(SectorView sv, FxView fv, const i64* __restrict__ X,
+                                                             i64* __restrict__ Y) {
+  extern __shared__ __align__(16) unsigned char x1p_smem[];
+  longlong2* xs = (longlong2*)x1p_smem;
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int idw0 = 2 * blockIdx.x;
+  const bool two = idw0 + 1 < DD;
+  const long long* c0 = (const long long*)X + (int64_t)idw0 * DU;
+  const long long* c1 = c0 + DU;
+  constexpr int U = 8;  // loads in flight per thread and column
+  for (int t0 = threadIdx.x; t0 < DU; t0 += U * FX1_UP2_THREADS) {
+    long long a[U], b[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int t = t0 + u * FX1_UP2_THREADS;
+      a[u] = t < DU ? __ldcs(c0 + t) : 0ll;
+      b[u] = (two && t < DU) ? __ldcs(c1 + t) : 0ll;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int t = t0 + u * FX1_UP2_THREADS;
+      if (t < DU) xs[t] = make_longlong2(a[u], b[u]);
+    }
+  }
+  if (threadIdx.x < FX1_ZERO_UNITS) xs[DU + threadIdx.x] = make_longlong2(0ll, 0ll);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int nw = (DU + 31) >> 5;
+  const i64 e1d0 = fv.dw_e1[idw0], e1d1 = two ? fv.dw_e1[idw0 + 1] : 0;
+  const unsigned wd0 = (unsigned)sv.dw_words[idw0], wd1 = two ? (unsigned)sv.dw_words[idw0 + 1] : 0u;
+  for (int w = threadIdx.x >> 5; w < nw; w += FX1_UP2_THREADS / 32) {
+    const int iup = w * 32 + lane;
+    const bool row = iup < DU;
+    const i64 eu = row ? fv.up_e1[iup] : 0;  // the epilogue's tables, ahead of the rounds
+    const unsigned wu = row ? (unsigned)sv.up_words[iup] : 0u;
+    u64 A[K], B[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) A[k] = B[k] = 0;
+    const unsigned* sp = fv.up_sched + (size_t)fv.up_wround[w] * 32 + lane;
+    const int* gr = fv.up_wgrp + w * 2 * K;
+#pragma unroll
+    for (int g = 0; g < 2 * K; g++) {
+      const int Rg = gr[g];
+      u64 a = 0, b = 0;
+      int r = 0;
+      for (; r + 8 <= Rg; r += 8) {  // 8 schedule loads in flight, then 8 unit reads
+        unsigned o[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) o[u] = __ldg(sp + (r + u) * 32);
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+          const longlong2 v0 = *(const longlong2*)(x1p_smem + o[u]);
+          const longlong2 v1 = *(const longlong2*)(x1p_smem + o[u + 1]);
+          a += (u64)v0.x + (u64)v1.x;
+          b += (u64)v0.y + (u64)v1.y;
+        }
+      }
+      if (r + 4 <= Rg) {
+        unsigned o[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) o[u] = __ldg(sp + (r + u) * 32);
+#pragma unroll
+        for (int u = 0; u < 4; u += 2) {
+          const longlong2 v0 = *(const longlong2*)(x1p_smem + o[u]);
+          const longlong2 v1 = *(const longlong2*)(x1p_smem + o[u + 1]);
+          a += (u64)v0.x + (u64)v1.x;
+          b += (u64)v0.y + (u64)v1.y;
+        }
+        r += 4;
+      }
+      if (r < Rg) {  // 1..3 rounds left: their loads together
+        const unsigned o0 = __ldg(sp + r * 32);
+        const unsigned o1 = r + 1 < Rg ? __ldg(sp + (r + 1) * 32) : 16u * (unsigned)DU;
+        const unsigned o2 = r + 2 < Rg ? __ldg(sp + (r + 2) * 32) : 16u * (unsigned)DU;
+        const longlong2 v0 = *(const longlong2*)(x1p_smem + o0);
+        a += (u64)v0.x;
+        b += (u64)v0.y;
+        if (r + 1 < Rg) {
+          const longlong2 v1 = *(const longlong2*)(x1p_smem + o1);
+          a += (u64)v1.x;
+          b += (u64)v1.y;
+        }
+        if (r + 2 < Rg) {
+          const longlong2 v2 = *(const longlong2*)(x1p_smem + o2);
+          a += (u64)v2.x;
+          b += (u64)v2.y;
+        }
+      }
+      sp += Rg * 32;
+      if (g & 1) {
+        A[g >> 1] -= a;
+        B[g >> 1] -= b;
+      } else {
+        A[g >> 1] += a;
+        B[g >> 1] += b;
+      }
+    }
+    if (!row) continue;
+    const longlong2 xi = xs[iup];
+    i128 p0 = (i128)(eu + e1d0 + mixed_fx(fv, wu, wd0)) * xi.x;
+#pragma unroll
+    for (int k = 0; k < K; k++) p0 += (i128)fv.afx[k] * (i64)A[k];
+    __stcs((long long*)Y + (int64_t)idw0 * DU + iup, (long long)rshift_round(p0, fv.shift));
+    if (two) {
+      i128 p1 = (i128)(eu + e1d1 + mixed_fx(fv, wu, wd1)) * xi.y;
+#pragma unroll
+      for (int k = 0; k < K; k++) p1 += (i128)fv.afx[k] * (i64)B[k];
+      __stcs((long long*)Y + (int64_t)(idw0 + 1) * DU + iup, (long long)rshift_round(p1, fv.shift));
+    }
+  }
+}
+
+// Down part on row pairs (DimUp even): as k_hxv1_dw, each thread two
+// adjacent rows of one chunk, every neighbour row pair one 16-byte L2 read;
+// chunks of FX1_DW2_ROWS-row multiples (one pair per thread).
+#define FX1_DW2_ROWS 512
+template <int K>
+__global__ void __launch_bounds__(FX1_DW2_ROWS / 2) k_hxv1_dw2(SectorView sv, FxView fv, int chunk_rows,
+                                                          const i64* __restrict__ X, i64* __restrict__ Y) {
+  extern __shared__ __align__(16) unsigned char x1d_smem[];
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int ck = blockIdx.x / DD;
+  const int idw = blockIdx.x - ck * DD;
+  const int64_t DU2 = DU / 2;
+  int64_t* doff = (int64_t*)x1d_smem;  // neighbour column offsets in row pairs
+  unsigned char* dcl = (unsigned char*)(doff + sv.wdw);
+  const int nd = sv.dw_cnt[idw], ndp = fv.dw_npos[idw];
+  for (int h = threadIdx.x; h < nd; h += blockDim.x) {
+    const unsigned hw = fv.dw_hop[idw + h * DD];
+    doff[h] = ((int64_t)(hw & 0xFFFFFFu) - idw) * DU2;
+    dcl[h] = (unsigned char)((hw >> 24) & 3u);
+  }
+  __syncthreads();
+  const int64_t base2 = (int64_t)idw * DU2;
+  const int q0 = ck * (chunk_rows / 2), q1 = (int)min((int64_t)DU2, (int64_t)(ck + 1) * (chunk_rows / 2));
+  const longlong2* Xb = (const longlong2*)X + base2;
+  longlong2* Yb = (longlong2*)Y + base2;
+  for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+    const longlong2 y = __ldcs(Yb + q);
+    u64 A[K], B[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) A[k] = B[k] = 0;
+    int h = 0;
+#pragma unroll 4
+    for (; h < ndp; h++) {
+      const longlong2 v = __ldcg(Xb + q + doff[h]);
+      const int cls = (K == 1) ? 0 : (int)dcl[h];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) A[k] += (u64)v.x, B[k] += (u64)v.y;
+    }
+#pragma unroll 4
+    for (; h < nd; h++) {
+      const longlong2 v = __ldcg(Xb + q + doff[h]);
+      const int cls = (K == 1) ? 0 : (int)dcl[h];
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) A[k] -= (u64)v.x, B[k] -= (u64)v.y;
+    }
+    i128 pa = 0, pb = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) pa += (i128)fv.afx[k] * (i64)A[k], pb += (i128)fv.afx[k] * (i64)B[k];
+    __stcs(Yb + q, make_longlong2((long long)((i64)y.x + rshift_round(pa, fv.shift)),
+                                  (long long)((i64)y.y + rshift_round(pb, fv.shift))));
+  }
+}
+
+// ---- host: the bank schedule of k_hxv1_up2 ----
+namespace {
+struct QuarterMatch {  // lanes of one quarter warp against the 8 bank groups of 16-byte units
+  const std::vector<unsigned>* rem;
+  int unit_lane[8], lane_unit[8];
+  bool seen[8];
+  bool augment(int j) {
+    for (unsigned src : rem[j]) {
+      const int u = (int)(src & 7u);
+      if (seen[u]) continue;
+      seen[u] = true;
+      if (unit_lane[u] < 0 || augment(unit_lane[u])) {
+        unit_lane[u] = j;
+        lane_unit[j] = u;
+        return true;
+      }
+    }
+    return false;
+  }
+};
+}  // namespace
+
+int64_t fx_pair_schedule(int dim, int width, int K, const int* cnt, const unsigned* hop,
+                         std::vector<unsigned>& sched, std::vector<int>& wround, std::vector<int>& wgrp) {
+  const int nw = (dim + 31) / 32, NG = 2 * K;
+  auto group = [&](unsigned hw) { return 2 * (int)((hw >> 24) & 3u) + (int)(hw >> 31); };
+  wround.assign(nw + 1, 0);
+  wgrp.assign((size_t)nw * NG, 0);
+  for (int w = 0; w < nw; w++) {
+    for (int l = 0; l < 32 && w * 32 + l < dim; l++) {
+      const int r = w * 32 + l;
+      int c[2 * VCA_FX_KMAX] = {0};
+      for (int h = 0; h < cnt[r] && h < width; h++) {
+        const int gg = group(hop[(size_t)h * dim + r]);
+        if (gg >= NG) return -1;
+        c[gg]++;
+      }
+      for (int gg = 0; gg < NG; gg++) wgrp[(size_t)w * NG + gg] = std::max(wgrp[(size_t)w * NG + gg], c[gg]);
+    }
+    int R = 0;
+    for (int gg = 0; gg < NG; gg++) R += wgrp[(size_t)w * NG + gg];
+    wround[w + 1] = wround[w] + R;
+  }
+  sched.assign((size_t)wround[nw] * 32, 0u);
+  int64_t conflicts = 0;
+  std::vector<unsigned> rem[8];
+  for (int w = 0; w < nw; w++) {
+    for (int q = 0; q < 4; q++) {
+      int rd0 = wround[w];
+      for (int gg = 0; gg < NG; gg++) {
+        const int R = wgrp[(size_t)w * NG + gg];
+        for (int j = 0; j < 8; j++) {
+          rem[j].clear();
+          const int r = w * 32 + q * 8 + j;
+          if (r < dim)
+            for (int h = 0; h < cnt[r] && h < width; h++) {
+              const unsigned hw = hop[(size_t)h * dim + r];
+              if (group(hw) == gg) rem[j].push_back(hw & 0xFFFFFFu);
+            }
+        }
+        for (int rd = 0; rd < R; rd++) {
+          int ord[8];
+          for (int j = 0; j < 8; j++) ord[j] = j;
+          std::stable_sort(ord, ord + 8, [&](int a, int b) { return rem[a].size() > rem[b].size(); });
+          QuarterMatch qm;
+          qm.rem = rem;
+          for (int u = 0; u < 8; u++) qm.unit_lane[u] = qm.lane_unit[u] = -1;
+          for (int t = 0; t < 8; t++) {
+            const int j = ord[t];
+            if (rem[j].empty()) break;
+            for (int u = 0; u < 8; u++) qm.seen[u] = false;
+            qm.augment(j);
+          }
+          int load[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          unsigned src[8];
+          bool real[8];
+          for (int j = 0; j < 8; j++) {
+            real[j] = false;
+            if (qm.lane_unit[j] < 0) continue;
+            for (size_t i = 0; i < rem[j].size(); i++)
+              if ((int)(rem[j][i] & 7u) == qm.lane_unit[j]) {
+                src[j] = rem[j][i];
+                rem[j].erase(rem[j].begin() + (std::ptrdiff_t)i);
+                break;
+              }
+            real[j] = true;
+            load[qm.lane_unit[j]]++;
+          }
+          bool conflict = false;
+          for (int j = 0; j < 8; j++) {  // lanes that must take a hop in every remaining round
+            if (real[j] || (int)rem[j].size() < R - rd) continue;
+            size_t best = 0;
+            for (size_t i = 1; i < rem[j].size(); i++)
+              if (load[rem[j][i] & 7u] < load[rem[j][best] & 7u]) best = i;
+            src[j] = rem[j][best];
+            rem[j].erase(rem[j].begin() + (std::ptrdiff_t)best);
+            real[j] = true;
+            conflict = conflict || load[src[j] & 7u] > 0;
+            load[src[j] & 7u]++;
+          }
+          conflicts += conflict ? 1 : 0;
+          // lanes without a hop read a zero unit in a bank group no real lane uses
+          // (there is one whenever such a lane exists: at most 7 real lanes)
+          int freeg = 0;
+          while (freeg < 7 && load[freeg] > 0) freeg++;
+          const unsigned zero_unit = (unsigned)dim + (unsigned)((freeg - dim % 8 + 8) % 8);
+          unsigned* out = sched.data() + (size_t)(rd0 + rd) * 32 + q * 8;
+          for (int j = 0; j < 8; j++) out[j] = 16u * (real[j] ? src[j] : zero_unit);
+        }
+        for (int j = 0; j < 8; j++)
+          if (!rem[j].empty()) return -1;
+        rd0 += R;
+      }
+    }
+  }
+  return conflicts;
+}
+
 static bool hxv1_ok(const SectorView& sv, const FxView& fv, int m) {
   return m == 1 && fv.up_npos && fv.dw_npos && (int64_t)sv.dimup * sv.dimdw >= FX1_MIN_DIM &&
          (size_t)sv.dimup * sizeof(i64) <= 200 * 1024;
@@ -263,11 +559,25 @@ static void launch_hxv1_k(const SectorView& sv, const FxView& fv, const i64* X, 
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_hxv1_up<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_hxv1_up2<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, FX1_SMEM_MAX);
     attr = true;
   }
   count_launch_external();
   count_launch_external();
-  k_hxv1_up<K><<<sv.dimdw, 1024, (size_t)sv.dimup * sizeof(i64), st>>>(sv, fv, X, Y);
+  const bool paired = fv.up_sched && fv.up_wround && fv.up_wgrp && fx_pair_fits(sv.dimup);
+  if (paired)
+    k_hxv1_up2<K><<<(sv.dimdw + 1) / 2, FX1_UP2_THREADS, (size_t)(sv.dimup + FX1_ZERO_UNITS) * 16, st>>>(sv, fv, X,
+                                                                                                     Y);
+  else
+    k_hxv1_up<K><<<sv.dimdw, 1024, (size_t)sv.dimup * sizeof(i64), st>>>(sv, fv, X, Y);
+  if (paired && sv.dimup % 2 == 0) {  // row pairs: 16-byte streams of the neighbour columns
+    const int64_t fit = FX1_CHUNK_BYTES / ((int64_t)sv.dimdw * sizeof(i64));
+    int rows = (int)std::max<int64_t>(FX1_DW2_ROWS, fit / FX1_DW2_ROWS * FX1_DW2_ROWS);
+    rows = std::min(rows, (sv.dimup + FX1_DW2_ROWS - 1) / FX1_DW2_ROWS * FX1_DW2_ROWS);
+    const int nck = (sv.dimup + rows - 1) / rows;
+    k_hxv1_dw2<K><<<nck * sv.dimdw, FX1_DW2_ROWS / 2, (size_t)sv.wdw * 9 + 16, st>>>(sv, fv, rows, X, Y);
+    return;
+  }
   int rows = (int)std::max<int64_t>(256, FX1_CHUNK_BYTES / ((int64_t)sv.dimdw * sizeof(i64)));
   rows = std::min(rows, sv.dimup);
   const int nck = (sv.dimup + rows - 1) / rows;

@@ -16,6 +16,8 @@
 // fixed-point coefficients.
 #pragma once
 
+#include <vector>
+
 #include "vca_common.cuh"
 #include "vca_kernels.cuh"
 
@@ -55,6 +57,13 @@ struct FxView {
   const int* up_pnpos;
   const int* up_pword;
   const i64* up_pe1;
+  // bank schedule of the paired-column single-vector kernel (fx_pair_schedule):
+  // shared-memory byte offsets, warp w's round r, lane l at
+  // up_sched[(up_wround[w] + r)*32 + l], rounds in groups of one class and
+  // sign (up_wgrp[w*2K + g] rounds in group g); nullptr: the one-column form runs
+  const unsigned* up_sched;
+  const int* up_wround;
+  const int* up_wgrp;
   int K;
   i64 afx[VCA_FX_KMAX];        // class amplitudes, scale 2^-A
   int norb;
@@ -111,6 +120,31 @@ void launch_fx_codes(int dim, int width, const double2* amp, const double* class
                      signed char* code, cudaStream_t st);
 // FP64 one-body table -> fixed point
 void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st);
+// Bank schedule of the paired-column staged up kernel.  Rows are taken in
+// warps of 32, and a warp's hops in groups g = 2*class + (amplitude < 0);
+// group g of warp w gets wgrp[w*2K + g] rounds (the most hops of that group
+// in any of its rows), the groups' rounds follow one another from round
+// wround[w], and each round holds one word per lane: the byte offset in the
+// kernel's shared memory of the 16-byte unit the lane reads (a hop's source
+// unit, or for a lane without a hop in that round a zero unit).  Within every
+// quarter warp (8 lanes: one 128-byte shared-memory wavefront of 16-byte
+// reads) a round's sources are chosen by bipartite matching (lanes by
+// remaining hops, most first, against the bank groups src mod 8) so that
+// they fall in distinct groups, and the zero unit read by idle lanes lies in
+// a group no real lane of that round uses.  hop: the packed hop words
+// [width*dim] (host copy); cnt: hop counts [dim].  The fixed-point hop sums
+// are exact, so the order of a row's hops changes no result.  Returns the
+// number of quarter-warp rounds that could not be made conflict free, or -1
+// if a hop was left unplaced.
+int64_t fx_pair_schedule(int dim, int width, int K, const int* cnt, const unsigned* hop,
+                         std::vector<unsigned>& sched, std::vector<int>& wround, std::vector<int>& wgrp);
+// the paired-column form's shared memory: dim + FX1_ZERO_UNITS 16-byte units
+// (the last ones zero, one per bank group)
+#define FX1_ZERO_UNITS 8
+#define FX1_SMEM_MAX (227 * 1024)
+// single vectors of sectors from this dimension on take the staged two-kernel form
+#define FX1_MIN_DIM (1 << 22)
+inline bool fx_pair_fits(int dim) { return (size_t)(dim + FX1_ZERO_UNITS) * 16 <= FX1_SMEM_MAX; }
 // Y = H X (FX) on a slab-major column batch, any m (the small-batch form)
 void launch_hxv_fx(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, cudaStream_t st);
 // per-column exact dot: out_col[c] = (sum X*Y) * 2^-(sx+sy) (double)
