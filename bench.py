@@ -583,6 +583,78 @@ def hxv_single_4x4(reps: int = 10) -> dict:
     return out
 
 
+def hxv_cols_4x4(ncols: int, reps: int) -> dict:
+    """Column-batch H x v on a Green's-function target sector of the 4x4
+    cluster (sector (9,8): 11440 x 12870 = 147,232,800), `ncols` slab-major
+    int64 columns, CUDA events on the library stream: the slab-pair form
+    (the library's) against the warp form (hxv_variant 1), same input;
+    algorithmic bytes 16 per element and column."""
+    import torch
+    from vca_gb300 import clusters
+    from vca_gb300.solver import VcaSolver
+    pt = clusters.square(nx=4, ny=4, U=8.0, xmu=4.0, maf=0.15, nspin=2, nkx=2, nky=2, ngfiter=10,
+                         omega_nodes=64)
+    isec = 1 + 9 + 8 * 17
+    peak, kind = measured_peaks()
+    out = {"sector": [9, 8], "ncols": ncols, "peak": peak, "peak_kind": kind}
+    x = y = y0 = None
+    for variant, name in ((0, "slab_pair"), (1, "warp")):
+        cfg = pt.cfg.copy()
+        cfg.hxv_variant = variant
+        s = VcaSolver(cfg)
+        s.set_hamiltonian(pt.Hloc)
+        _, _, du, dd = s.sector_info(isec)
+        D = du * dd
+        if x is None:
+            fx, F, _ = s.arith_info()
+            g = torch.Generator(device="cuda").manual_seed(5)
+            x = torch.randn(D * ncols, dtype=torch.float64, device="cuda", generator=g)
+            x = x.mul_(2.0 ** F / (D ** 0.5 * 4.0)).round_().to(torch.int64)
+            y = torch.empty_like(x)
+        ms = s.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, ncols, reps)
+        s.close()
+        gbs = 16.0 * D * ncols / (ms / 1e3) / 1e9
+        out["D"] = D
+        out[name] = {"launch_ms": round(ms, 3), "ms_per_column": round(ms / ncols, 4),
+                     "achieved_GBps": round(gbs, 1), "frac": round(gbs / peak, 4)}
+        if y0 is None:
+            y0 = y.clone()
+        else:
+            out["bit_identical"] = bool(torch.equal(y0, y))
+    del x, y, y0
+    return out
+
+
+def c5_solve(steps: int) -> dict:
+    """One plain vca_solve of the 4x4 Hubbard cluster (Ns = 16, 289 sectors,
+    largest 12870^2): U = 8, half filling, t' = 1, M_AF = 0.15, Nspin = 2,
+    16x16 k-grid, `steps`-step chains (the reference's channel set: 1984
+    chains), 8192-node Omega rule; wall time and the library's stage times."""
+    import numpy as np
+    from vca_gb300 import clusters
+    from vca_gb300.solver import VcaSolver
+    pt = clusters.square(nx=4, ny=4, U=8.0, xmu=4.0, t=1.0, tprime=1.0, maf=0.15, nspin=2, nkx=16, nky=16,
+                         ngfiter=steps, omega_nodes=8192)
+    s = VcaSolver(pt.cfg)
+    t0 = time.perf_counter()
+    om = s.solve(pt.Hloc, pt.Hk)
+    dt = time.perf_counter() - t0
+    st = s.timings()
+    out = {"workload": "C5: 4x4 Hubbard U=8, half filling, t'=1, M_AF=0.15, Nspin=2, 16x16 k, "
+                       f"{steps}-step chains (chan4), 8192-node Omega rule",
+           "omega": om, "seconds": round(dt, 2),
+           "stage_s": {"hamiltonian": round(st[0] / 1e3, 3), "diagonalize": round(st[1] / 1e3, 3),
+                       "chains": round(st[2] / 1e3, 3), "omega": round(st[3] / 1e3, 3)},
+           "arith": "fx" if s.arith_info()[0] else "f64"}
+    cs, cl, nb = s.chain_timings()
+    out["chain_stage"] = {"start_vectors_s": round(cs / 1e3, 3), "lanczos_steps_s": round(cl / 1e3, 3),
+                          "column_batches": nb}
+    out["egs"] = s.energies()[0]
+    out["states"] = [list(x) for x in s.states()]
+    s.close()
+    return out
+
+
 def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
     """Batched H x v only (for ncu captures of the H x v kernel)."""
     import torch
@@ -722,6 +794,11 @@ def main():
     ap.add_argument("--profile-mlp", type=int, default=0, metavar="STEPS",
                     help="profiling mode: STEPS Adam steps of the surrogate on 200 samples with gradients")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--profile-hxv-c5", type=int, default=0, metavar="NCOLS",
+                    help="time a NCOLS-column H x v on a chain sector of the 4x4 cluster, both forms")
+    ap.add_argument("--c5-solve", action="store_true",
+                    help="one plain solve of the 4x4 cluster (C5), timed by stage")
+    ap.add_argument("--c5-steps", type=int, default=200, help="chain steps of --c5-solve")
     ap.add_argument("--cpu-full-eval", action="store_true",
                     help="one complete oracle Omega evaluation of the benchmark workload on all host threads")
     ap.add_argument("--hxv-variant", type=int, default=2,
@@ -735,6 +812,16 @@ def main():
         from vca_gb300 import build as vbuild
         vbuild.build()
         print(json.dumps(hxv_single_4x4(args.reps)))
+        return 0
+    if args.profile_hxv_c5:
+        from vca_gb300 import build as vbuild
+        vbuild.build()
+        print(json.dumps(hxv_cols_4x4(args.profile_hxv_c5, args.reps)))
+        return 0
+    if args.c5_solve:
+        from vca_gb300 import build as vbuild
+        vbuild.build()
+        print(json.dumps(c5_solve(args.c5_steps)))
         return 0
     if args.cpu_full_eval:
         return cpu_full_eval(os.cpu_count() or 1)

@@ -456,7 +456,9 @@ int64_t vca_gpu_kernel_launches(void);
  * [7] chains, [8] Omega, [9] the closing plain solve of the last point;
  * with n >= 11, [10] the (point, sector) searches its screening skipped;
  * with n >= 13, [11] rows per tile and [12] row lanes per block of its
- * chains' (autotuned) tile shape. */
+ * chains' (autotuned) tile shape; with n >= 16, the last solve's chain
+ * stage split into [13] start vectors and [14] Lanczos steps (ms) and
+ * [15] its column batches. */
 int vca_gpu_get_timings(double* ms, int32_t n);
 /* Arithmetic of the loaded Hamiltonian: *fx = 1 when the fixed-point path is
  * active, with vector scale 2^-F and H v scale 2^-G.  In that case the device

@@ -81,3 +81,42 @@ def test_paired_column_form_matches_one_column_form(ty, nup, ndw, oracle_check):
         ref = o.hxv(isec, X.astype(np.float64) * 2.0 ** -F).real
         got = Yp.astype(np.float64) * 2.0 ** -G
         assert np.abs(got - ref).max() / max(1.0, np.abs(ref).max()) < 1e-13
+
+
+def _slabs(X):
+    D, m = X.shape
+    return np.ascontiguousarray(X.reshape(D, m // 8, 8).transpose(1, 0, 2)).reshape(-1)
+
+
+@pytest.mark.parametrize("ty,nup,ndw,m", [(1.0, 7, 7, 16), (0.7, 7, 6, 24)])
+def test_slab_pair_form_matches_warp_form(ty, nup, ndw, m):
+    """Column batches of a sector whose up block of one slab does not fit
+    shared memory (2x7 cluster, DimUp 3432): the slab-pair form (16-byte
+    column pairs through the bank schedule, chunked down streams, separate
+    exact alpha partials) against the warp form (hxv_variant 1), Y and
+    alpha = <x, Hx> bit for bit."""
+    import torch
+    pt = _point(ty)
+    isec = 1 + nup + ndw * (NS + 1)
+    out = {}
+    for variant in (0, 1):
+        cfg = pt.cfg.copy()
+        cfg.hxv_variant = variant
+        s = VcaSolver(cfg)
+        s.set_hamiltonian(pt.Hloc)
+        _, _, du, dd = s.sector_info(isec)
+        fx, F, G = s.arith_info()
+        assert fx
+        D = du * dd
+        x = np.random.default_rng(40 + m).normal(size=(D, m))
+        x /= np.linalg.norm(x, axis=0, keepdims=True)
+        dX = torch.from_numpy(_slabs(np.rint(x * 2.0 ** F).astype(np.int64))).cuda()
+        dY = torch.zeros_like(dX)
+        dA = torch.zeros(m, dtype=torch.float64, device="cuda")
+        s.hxv_alpha_noalloc(isec, dX.data_ptr(), dY.data_ptr(), m, dA.data_ptr())
+        torch.cuda.synchronize()
+        out[variant] = (dY.cpu().numpy(), dA.cpu().numpy())
+        del dX, dY, dA
+        s.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])

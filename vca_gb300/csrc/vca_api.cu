@@ -173,6 +173,7 @@ struct Ctx {
   std::vector<cd> hk_const;       // lso: value of Hk when equal at every k
   std::vector<char> hk_varying;   // lso: 1 when Hk differs between k-points
   double t_ms[4] = {0, 0, 0, 0};  // set_hamiltonian, diagonalise, chains, Omega
+  double chain_ms[3] = {0, 0, 0};  // chain stage: start vectors, Lanczos steps (ms), batches
   // the last vca_gpu_solve_batch in the batched form: tables, search,
   // eigenvectors, chains, Omega, the closing plain solve (wall ms, all waves)
   double bt_ms[6] = {0, 0, 0, 0, 0, 0};
@@ -1213,6 +1214,8 @@ double state_weight(const GState& S) {
   return x < 200.0 ? std::exp(-x) : 0.0;
 }
 
+double now_ms();
+
 int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs) {
   const vca_config& c = g->cfg;
   const GState& S = g->gs[state];
@@ -1289,6 +1292,9 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
     cudaMemcpyAsync(d_isign, isg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, g->st);
     cudaMemcpyAsync(d_wfac, wf.data(), sizeof(double2) * nch, cudaMemcpyHostToDevice, g->st);
     ColBatch cb{D, m, cplx, nch, bb.col2ch, bb.meta};
+    CUCHK(cudaStreamSynchronize(g->st));
+    const double tb0 = now_ms();
+    double tb1 = tb0;
     // start vectors: gather from the ground state, normalise per chain
     if (g->fx) {
       const FxScales& fs = g->fxs;
@@ -1299,6 +1305,8 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
       launch_chain_sum(cb, norm2c, norm2, g->st);
       launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
       launch_fx_rescale(cb, invn, fs.F, fs.F, (i64*)bb.b[0], (i64*)bb.b[0], bb.scr, g->st);
+      CUCHK(cudaStreamSynchronize(g->st));
+      tb1 = now_ms();
       for (int k = 1; k <= nlanc; k++)
         if ((rc = lanczos_step_fx(hv, fv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
     } else {
@@ -1307,6 +1315,8 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
       launch_chain_sum(cb, norm2c, norm2, g->st);
       launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
       launch_col_scale(cb, invn, bb.b[0], bb.b[0], g->st);
+      CUCHK(cudaStreamSynchronize(g->st));
+      tb1 = now_ms();
       for (int k = 1; k <= nlanc; k++)
         if ((rc = lanczos_step(tv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
     }
@@ -1316,6 +1326,9 @@ int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs
                        g->cstore, base, g->st);
     CUCHK(cudaGetLastError());
     CUCHK(cudaStreamSynchronize(g->st));
+    g->chain_ms[0] += tb1 - tb0;
+    g->chain_ms[1] += now_ms() - tb1;
+    g->chain_ms[2] += 1.0;
     for (int q = 0; q < nch; q++) {
       g->chains.push_back(specs[q0 + q].rec);
       g->chains.back().nlanc = nlanc;
@@ -1337,6 +1350,7 @@ int build_gf() {
   const vca_config& c = g->cfg;
   g->gf.release();
   g->chains.clear();
+  for (double& t : g->chain_ms) t = 0.0;
   g->ld = std::max(1, c.lanc_ngfiter);
   const int nmax = count_chains();
   RCHK(g->gf.alloc(&g->d_poles, (size_t)nmax * g->ld));
@@ -3905,6 +3919,7 @@ int vca_gpu_get_timings(double* ms, int32_t n) {
   for (int i = 4; i < n && i < 10; i++) ms[i] = g->bt_ms[i - 4];
   if (n > 10) ms[10] = (double)g->bt_skipped;
   if (n > 12) { ms[11] = g->bt_shape[0]; ms[12] = g->bt_shape[1]; }
+  for (int i = 13; i < n && i < 16; i++) ms[i] = g->chain_ms[i - 13];
   return VCA_OK;
 }
 

@@ -252,6 +252,76 @@ __global__ void __launch_bounds__(256) k_hxv1_dw(SectorView sv, FxView fv, int c
   }
 }
 
+// The rounds of warp-row w of the bank schedule (fx_pair_schedule) over the
+// staged 16-byte units at smem: A[k], B[k] = signed class-k hop sums of the
+// lane's row in the units' first and second words.  Every round of the warp
+// is one 16-byte read per lane; 8 schedule words are loaded ahead.
+template <int K>
+__device__ __forceinline__ void up2_rounds(const FxView& fv, int w, int lane, int DU,
+                                           const unsigned char* __restrict__ x1p_smem, u64 (&A)[K], u64 (&B)[K]) {
+#pragma unroll
+  for (int k = 0; k < K; k++) A[k] = B[k] = 0;
+  const unsigned* sp = fv.up_sched + (size_t)fv.up_wround[w] * 32 + lane;
+  const int* gr = fv.up_wgrp + w * 2 * K;
+#pragma unroll
+  for (int g = 0; g < 2 * K; g++) {
+    const int Rg = gr[g];
+    u64 a = 0, b = 0;
+    int r = 0;
+    for (; r + 8 <= Rg; r += 8) {  // 8 schedule loads in flight, then 8 unit reads
+      unsigned o[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) o[u] = __ldg(sp + (r + u) * 32);
+#pragma unroll
+      for (int u = 0; u < 8; u += 2) {
+        const longlong2 v0 = *(const longlong2*)(x1p_smem + o[u]);
+        const longlong2 v1 = *(const longlong2*)(x1p_smem + o[u + 1]);
+        a += (u64)v0.x + (u64)v1.x;
+        b += (u64)v0.y + (u64)v1.y;
+      }
+    }
+    if (r + 4 <= Rg) {
+      unsigned o[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) o[u] = __ldg(sp + (r + u) * 32);
+#pragma unroll
+      for (int u = 0; u < 4; u += 2) {
+        const longlong2 v0 = *(const longlong2*)(x1p_smem + o[u]);
+        const longlong2 v1 = *(const longlong2*)(x1p_smem + o[u + 1]);
+        a += (u64)v0.x + (u64)v1.x;
+        b += (u64)v0.y + (u64)v1.y;
+      }
+      r += 4;
+    }
+    if (r < Rg) {  // 1..3 rounds left: their loads together
+      const unsigned o0 = __ldg(sp + r * 32);
+      const unsigned o1 = r + 1 < Rg ? __ldg(sp + (r + 1) * 32) : 16u * (unsigned)DU;
+      const unsigned o2 = r + 2 < Rg ? __ldg(sp + (r + 2) * 32) : 16u * (unsigned)DU;
+      const longlong2 v0 = *(const longlong2*)(x1p_smem + o0);
+      a += (u64)v0.x;
+      b += (u64)v0.y;
+      if (r + 1 < Rg) {
+        const longlong2 v1 = *(const longlong2*)(x1p_smem + o1);
+        a += (u64)v1.x;
+        b += (u64)v1.y;
+      }
+      if (r + 2 < Rg) {
+        const longlong2 v2 = *(const longlong2*)(x1p_smem + o2);
+        a += (u64)v2.x;
+        b += (u64)v2.y;
+      }
+    }
+    sp += Rg * 32;
+    if (g & 1) {
+      A[g >> 1] -= a;
+      B[g >> 1] -= b;
+    } else {
+      A[g >> 1] += a;
+      B[g >> 1] += b;
+    }
+  }
+}
+
 // Paired-column up part (+ diagonal): one CTA stages columns idw0 = 2*bx and
 // idw0 + 1 interleaved, one 16-byte unit (X[iup, idw0], X[iup, idw0+1]) per
 // up configuration (then FX1_ZERO_UNITS zero units), and walks the bank
@@ -300,67 +370,7 @@ __global__ void __launch_bounds__(FX1_UP2_THREADS, 1) k_hxv1_up2(SectorView sv, 
     const i64 eu = row ? fv.up_e1[iup] : 0;  // the epilogue's tables, ahead of the rounds
     const unsigned wu = row ? (unsigned)sv.up_words[iup] : 0u;
     u64 A[K], B[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) A[k] = B[k] = 0;
-    const unsigned* sp = fv.up_sched + (size_t)fv.up_wround[w] * 32 + lane;
-    const int* gr = fv.up_wgrp + w * 2 * K;
-#pragma unroll
-    for (int g = 0; g < 2 * K; g++) {
-      const int Rg = gr[g];
-      u64 a = 0, b = 0;
-      int r = 0;
-      for (; r + 8 <= Rg; r += 8) {  // 8 schedule loads in flight, then 8 unit reads
-        unsigned o[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) o[u] = __ldg(sp + (r + u) * 32);
-#pragma unroll
-        for (int u = 0; u < 8; u += 2) {
-          const longlong2 v0 = *(const longlong2*)(x1p_smem + o[u]);
-          const longlong2 v1 = *(const longlong2*)(x1p_smem + o[u + 1]);
-          a += (u64)v0.x + (u64)v1.x;
-          b += (u64)v0.y + (u64)v1.y;
-        }
-      }
-      if (r + 4 <= Rg) {
-        unsigned o[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) o[u] = __ldg(sp + (r + u) * 32);
-#pragma unroll
-        for (int u = 0; u < 4; u += 2) {
-          const longlong2 v0 = *(const longlong2*)(x1p_smem + o[u]);
-          const longlong2 v1 = *(const longlong2*)(x1p_smem + o[u + 1]);
-          a += (u64)v0.x + (u64)v1.x;
-          b += (u64)v0.y + (u64)v1.y;
-        }
-        r += 4;
-      }
-      if (r < Rg) {  // 1..3 rounds left: their loads together
-        const unsigned o0 = __ldg(sp + r * 32);
-        const unsigned o1 = r + 1 < Rg ? __ldg(sp + (r + 1) * 32) : 16u * (unsigned)DU;
-        const unsigned o2 = r + 2 < Rg ? __ldg(sp + (r + 2) * 32) : 16u * (unsigned)DU;
-        const longlong2 v0 = *(const longlong2*)(x1p_smem + o0);
-        a += (u64)v0.x;
-        b += (u64)v0.y;
-        if (r + 1 < Rg) {
-          const longlong2 v1 = *(const longlong2*)(x1p_smem + o1);
-          a += (u64)v1.x;
-          b += (u64)v1.y;
-        }
-        if (r + 2 < Rg) {
-          const longlong2 v2 = *(const longlong2*)(x1p_smem + o2);
-          a += (u64)v2.x;
-          b += (u64)v2.y;
-        }
-      }
-      sp += Rg * 32;
-      if (g & 1) {
-        A[g >> 1] -= a;
-        B[g >> 1] -= b;
-      } else {
-        A[g >> 1] += a;
-        B[g >> 1] += b;
-      }
-    }
+    up2_rounds<K>(fv, w, lane, DU, x1p_smem, A, B);
     if (!row) continue;
     const longlong2 xi = xs[iup];
     i128 p0 = (i128)(eu + e1d0 + mixed_fx(fv, wu, wd0)) * xi.x;
@@ -1641,8 +1651,161 @@ static void launch_hxv_fx_s_k(const SectorView& sv, const FxView& fv, int m, con
   k_hxv_fx_s<K><<<sv.dimdw * ns, FXS_THREADS, hxv_fx_s_smem(sv, K), st>>>(sv, fv, m, X, Y, apart);
 }
 
+// ---------------------------------------------------------------------------
+// Column batches of large sectors whose up block of one slab does not fit
+// shared memory: the paired-column forms on 16-byte column pairs of the
+// slabs.  Slab s holds columns 8s..8s+7 as rows of 64 bytes, so the four
+// 16-byte pairs of a row are four interleaved single-vector problems that
+// share the row's diagonal and the up role's bank schedule.
+//  * up part (+ diagonal): one CTA per (down configuration, slab, pair),
+//    pairs fastest so the four CTAs of one 64-byte row block run together
+//    and read its lines once from DRAM; the block's DimUp units are staged
+//    and the schedule walked as in k_hxv1_up2.
+//  * down part: one CTA per (chunk of FXS_DW_ROWS rows, slab, group of
+//    FXS_DW_GRP down configurations), chunk-major so the chunk's rows of
+//    every down configuration (FXS_DW_ROWS * DimDw * 64 bytes) stay in L2;
+//    four lanes per row, one pair each: a warp reads 512 contiguous bytes
+//    of each neighbour block.
+// Both halves round their own int128 sums, as the single-vector form does.
+// ---------------------------------------------------------------------------
+#define FXS_DW_ROWS 64
+#define FXS_DW_GRP 8
+template <int K>
+__global__ void __launch_bounds__(FX1_UP2_THREADS, 1) k_hxv_slab_up2(SectorView sv, FxView fv, int nslab,
+                                                                 const i64* __restrict__ X, i64* __restrict__ Y) {
+  extern __shared__ __align__(16) unsigned char x1p_smem[];
+  longlong2* xs = (longlong2*)x1p_smem;
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int pr = blockIdx.x & 3;
+  const int rest = blockIdx.x >> 2;
+  const int sl = rest % nslab, idw = rest / nslab;
+  if (idw >= DD) return;
+  const int64_t base = ((int64_t)sl * DU * DD + (int64_t)idw * DU) * 4 + pr;  // 16-byte units
+  const longlong2* X2 = (const longlong2*)X + base;
+  longlong2* Y2 = (longlong2*)Y + base;
+  constexpr int U = 8;
+  for (int t0 = threadIdx.x; t0 < DU; t0 += U * FX1_UP2_THREADS) {
+    longlong2 a[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int t = t0 + u * FX1_UP2_THREADS;
+      a[u] = t < DU ? __ldcg(X2 + (int64_t)t * 4) : make_longlong2(0ll, 0ll);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int t = t0 + u * FX1_UP2_THREADS;
+      if (t < DU) xs[t] = a[u];
+    }
+  }
+  if (threadIdx.x < FX1_ZERO_UNITS) xs[DU + threadIdx.x] = make_longlong2(0ll, 0ll);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int nw = (DU + 31) >> 5;
+  const i64 e1d = fv.dw_e1[idw];
+  const unsigned wd = (unsigned)sv.dw_words[idw];
+  for (int w = threadIdx.x >> 5; w < nw; w += FX1_UP2_THREADS / 32) {
+    const int iup = w * 32 + lane;
+    const bool row = iup < DU;
+    const i64 eu = row ? fv.up_e1[iup] : 0;
+    const unsigned wu = row ? (unsigned)sv.up_words[iup] : 0u;
+    u64 A[K], B[K];
+    up2_rounds<K>(fv, w, lane, DU, x1p_smem, A, B);
+    if (!row) continue;
+    const longlong2 xi = xs[iup];
+    const i64 d = eu + e1d + mixed_fx(fv, wu, wd);
+    i128 p0 = (i128)d * xi.x, p1 = (i128)d * xi.y;
+#pragma unroll
+    for (int k = 0; k < K; k++) p0 += (i128)fv.afx[k] * (i64)A[k], p1 += (i128)fv.afx[k] * (i64)B[k];
+    __stcg(Y2 + (int64_t)iup * 4, make_longlong2((long long)rshift_round(p0, fv.shift),
+                                                 (long long)rshift_round(p1, fv.shift)));
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(FXS_DW_ROWS * 4) k_hxv_slab_dw2(SectorView sv, FxView fv, int nslab,
+                                                              const i64* __restrict__ X, i64* __restrict__ Y) {
+  const int DU = sv.dimup, DD = sv.dimdw;
+  const int ngrp = (DD + FXS_DW_GRP - 1) / FXS_DW_GRP;
+  const int grp = blockIdx.x % ngrp;
+  const int t2 = blockIdx.x / ngrp;
+  const int sl = t2 % nslab, ck = t2 / nslab;
+  const int pr = threadIdx.x & 3;
+  const int iup = ck * FXS_DW_ROWS + (threadIdx.x >> 2);
+  if (iup >= DU) return;
+  const int64_t D = (int64_t)DU * DD;
+  const longlong2* X2 = (const longlong2*)X + ((int64_t)sl * D + iup) * 4 + pr;
+  longlong2* Y2 = (longlong2*)Y + ((int64_t)sl * D + iup) * 4 + pr;
+  const int64_t bstride = (int64_t)DU * 4;  // one down configuration, in 16-byte units
+  for (int j = 0; j < FXS_DW_GRP; j++) {
+    const int idw = grp * FXS_DW_GRP + j;
+    if (idw >= DD) break;
+    const int nd = sv.dw_cnt[idw], ndp = fv.dw_npos[idw];
+    const int64_t own = (int64_t)idw * bstride;
+    const longlong2 y = __ldcg(Y2 + own);
+    u64 A[K], B[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) A[k] = B[k] = 0;
+    int h = 0;
+#pragma unroll 4
+    for (; h < ndp; h++) {
+      const unsigned hw = __ldg(fv.dw_hop + idw + (int64_t)h * DD);
+      const longlong2 v = __ldcg(X2 + (int64_t)(hw & 0xFFFFFFu) * bstride);
+      const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) A[k] += (u64)v.x, B[k] += (u64)v.y;
+    }
+#pragma unroll 4
+    for (; h < nd; h++) {
+      const unsigned hw = __ldg(fv.dw_hop + idw + (int64_t)h * DD);
+      const longlong2 v = __ldcg(X2 + (int64_t)(hw & 0xFFFFFFu) * bstride);
+      const int cls = (K == 1) ? 0 : (int)((hw >> 24) & 3u);
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (k == cls) A[k] -= (u64)v.x, B[k] -= (u64)v.y;
+    }
+    i128 pa = 0, pb = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) pa += (i128)fv.afx[k] * (i64)A[k], pb += (i128)fv.afx[k] * (i64)B[k];
+    __stcg(Y2 + own, make_longlong2((long long)((i64)y.x + rshift_round(pa, fv.shift)),
+                                    (long long)((i64)y.y + rshift_round(pb, fv.shift))));
+  }
+}
+
+#define FXS_DOT_ROWS (152 * 4)  // alpha partial rows of the slab-pair form
+static bool hxv_fx_slab2_ok(const SectorView& sv, const FxView& fv, int m, bool warp_only) {
+  return !warp_only && !fv.rows_permuted && fv.up_sched && fv.up_wround && fv.up_wgrp && fv.dw_npos &&
+         fx_pair_fits(sv.dimup) && m >= FX_SLAB && m % FX_SLAB == 0 &&
+         (int64_t)sv.dimup * sv.dimdw >= FX1_MIN_DIM;
+}
+
+template <int K>
+static void launch_hxv_slab_k(const SectorView& sv, const FxView& fv, int m, const i64* X, i64* Y, i64* apart,
+                              cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_hxv_slab_up2<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, FX1_SMEM_MAX);
+    attr = true;
+  }
+  const int nslab = m / FX_SLAB;
+  const int DU = sv.dimup, DD = sv.dimdw;
+  count_launch_external();
+  count_launch_external();
+  k_hxv_slab_up2<K><<<DD * nslab * 4, FX1_UP2_THREADS, (size_t)(DU + FX1_ZERO_UNITS) * 16, st>>>(sv, fv, nslab, X, Y);
+  const int nck = (DU + FXS_DW_ROWS - 1) / FXS_DW_ROWS, ngrp = (DD + FXS_DW_GRP - 1) / FXS_DW_GRP;
+  k_hxv_slab_dw2<K><<<nck * nslab * ngrp, FXS_DW_ROWS * 4, 0, st>>>(sv, fv, nslab, X, Y);
+  if (apart) {  // exact int128 <X, Y> partials, FXS_DOT_ROWS rows of m
+    count_launch_external();
+    dim3 blk;
+    int ns;
+    slab_shape(m, blk, ns);
+    k_fx_dot<<<dim3(FXS_DOT_ROWS, ns, 1), blk, sizeof(i128) * 256, st>>>((int64_t)DU * DD, m, X, Y, apart);
+  }
+}
+
 int hxv_fx_cols_rows(const SectorView& sv, const FxView& fv, int m, bool warp_only) {
   if (fv.rows_permuted || hxv_fx_s_ok(sv, fv, m, warp_only)) return sv.dimdw;
+  if (hxv_fx_slab2_ok(sv, fv, m, warp_only)) return FXS_DOT_ROWS;
   return hxv_fx_w_rowblocks((int64_t)sv.dimup * sv.dimdw);
 }
 
@@ -1659,6 +1822,15 @@ void launch_hxv_fx_cols(const SectorView& sv, const FxView& fv, int m, const i64
       case 2: launch_hxv_fx_s_k<2>(sv, fv, m, X, Y, apart, st); break;
       case 3: launch_hxv_fx_s_k<3>(sv, fv, m, X, Y, apart, st); break;
       default: launch_hxv_fx_s_k<4>(sv, fv, m, X, Y, apart, st); break;
+    }
+    return;
+  }
+  if (hxv_fx_slab2_ok(sv, fv, m, warp_only)) {
+    switch (fv.K) {
+      case 1: launch_hxv_slab_k<1>(sv, fv, m, X, Y, apart, st); break;
+      case 2: launch_hxv_slab_k<2>(sv, fv, m, X, Y, apart, st); break;
+      case 3: launch_hxv_slab_k<3>(sv, fv, m, X, Y, apart, st); break;
+      default: launch_hxv_slab_k<4>(sv, fv, m, X, Y, apart, st); break;
     }
     return;
   }

@@ -276,6 +276,13 @@ class VcaSolver:
         check(self.L.vca_gpu_get_timings(_dp(out), 13))
         return out[4:] if batched else out[:4]
 
+    def chain_timings(self):
+        """The last solve's chain stage: (start-vector ms, Lanczos-step ms,
+        column batches)."""
+        out = np.zeros(16)
+        check(self.L.vca_gpu_get_timings(_dp(out), 16))
+        return float(out[13]), float(out[14]), int(out[15])
+
     def arith_info(self):
         fx, F, G = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         check(self.L.vca_gpu_arith_info(ctypes.byref(fx), ctypes.byref(F), ctypes.byref(G)))
