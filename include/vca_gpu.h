@@ -345,6 +345,16 @@ int vca_contour_rule(double R, double beta, double mu, int32_t ngl, double* thet
 int vca_state_list_finite_t(const double* E, int32_t nsectors, const vca_config* cfg, int32_t nstates_total,
                             int32_t* sectors, int32_t cap, int32_t* n, double* zeta, double* emin,
                             int32_t* nstates_total_out);
+/* The host eigensolvers of the "arpack" diagonalisation, without a context
+ * or a GPU.  vca_tridiag_eig: the symmetric tridiagonal matrix with diagonal
+ * d[0..n-1] and off-diagonal e[0..n-2] (implicit QL, Wilkinson shifts);
+ * vca_herm_eig: the Hermitian n x n matrix A (row-major, complex
+ * interleaved; cyclic Jacobi).  Eigenvalues ascending in w; eigenvectors as
+ * the columns of Z (column-major; complex interleaved for vca_herm_eig), or
+ * Z = NULL.  They stand in for SciFortran's sp_eigh/eigh (VCA_DIAG.f90:
+ * 153-170) on the Ritz problem and below LANC_DIM_THRESHOLD. */
+int vca_tridiag_eig(int32_t n, const double* d, const double* e, double* w, double* Z);
+int vca_herm_eig(int32_t n, const double* A, double* w, double* Z);
 
 /* Omega integrand f(w) = (1/Lk) sum_k ln|det(1+(Delta+Hloc-Hk)G'(iw))|
  * (VCA_OMEGA.f90:37-75) at nw real frequencies, from the last solve. */
@@ -449,6 +459,14 @@ int vca_gpu_solve_resident(const double* Hloc, const double* bath_h, const doubl
                            double* omega_out);
 /* Kernel launches issued by the library since it was loaded. */
 int64_t vca_gpu_kernel_launches(void);
+/* The k lowest eigenpairs of sector isector of the loaded Hamiltonian as the
+ * "arpack" diagonalisation finds them (LANC_METHOD="arpack", VCA_DIAG.f90:
+ * 153-170): dense below LANC_DIM_THRESHOLD (or k >= dim), else a Lanczos
+ * with full reorthogonalisation to LANC_TOLERANCE.  *n = pairs found
+ * (<= min(k, dim)); energies ascending; vecs (NULL or n*dim complex
+ * interleaved doubles, vector j at j*dim) unit-norm FP64.  No counterpart
+ * in the reference (its sp_eigh call). */
+int vca_gpu_sector_pairs(int32_t isector, int32_t k, double* energies, double* vecs, int32_t* n);
 /* Wall-clock milliseconds of the last solve's stages: [0] one-body tables,
  * [1] sector diagonalisation, [2] Green's function chains, [3] Omega; with
  * n >= 10 also the last batched-form vca_gpu_solve_batch's stages over all

@@ -1,0 +1,156 @@
+"""LANC_METHOD="arpack" (the reference default; VCA_DIAG.f90:98-111,153-170,
+220-236) on the GPU at T=0.
+
+* sector eigenpairs: dense below LANC_DIM_THRESHOLD (whole multiplets), a
+  Lanczos with full reorthogonalisation above it, against numpy's dense
+  eigh of the oracle's H (eigenvalues 1e-10, simple levels' vectors up to a
+  phase 1e-9);
+* the 2x2 plaquette at U = 8, xmu = 0.95, whose N = 3 ground level is a
+  doublet in each of the sectors (2,1) and (1,2): all four states kept
+  (zeta = 4), Omega equal to the oracle's arpack restatement (1e-10) and
+  0.077 away from the one-state-per-sector result;
+* the same against the oracle on the Lanczos path: a complex BHZ point
+  (FP64) and a real 2x3 cluster (fixed-point vectors), threshold lowered so
+  the sectors near the ground state go through the reorthogonalised
+  Lanczos.
+"""
+import numpy as np
+import pytest
+
+from vca_gb300 import clusters
+from vca_gb300.config import LANC_ARPACK, LANC_LANCZOS
+from vca_gb300.solver import VcaSolver
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _with(pt, **kw):
+    cfg = pt.cfg.copy()
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    pt.cfg = cfg
+    return pt
+
+
+def _solve(pt):
+    s = VcaSolver(pt.cfg)
+    om = s.solve(pt.Hloc, pt.Hk, pt.bath_h, pt.bath_v)
+    out = (om, sorted(s.states()), s.thermal())
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("threshold", [4, 256])
+def test_sector_pairs_match_dense_eigh(threshold):
+    pt = _with(clusters.bhz(mass=2.2, delta=0.1, nk1=4, ngfiter=60, omega_nodes=256),
+               lanc_method=LANC_ARPACK, lanc_dim_threshold=threshold)
+    o = Oracle.from_point(pt)
+    s = VcaSolver(pt.cfg)
+    s.set_hamiltonian(pt.Hloc)
+    checked = 0
+    lo, hi = (100, 900) if threshold == 4 else (20, 256)
+    for isec in range(1, o.Nsectors + 1):
+        D = o.dim(isec)
+        if not lo <= D <= hi:
+            continue
+        e, V = s.sector_pairs(isec, 6)
+        w, Z = np.linalg.eigh(o.dense_h(isec))
+        assert len(e) == 6
+        np.testing.assert_allclose(e, w[:6], rtol=0, atol=1e-10 * max(1.0, abs(w[0])))
+        np.testing.assert_allclose(np.linalg.norm(V, axis=0), 1.0, atol=1e-12)
+        for j in range(6):
+            gaps = np.abs(w - w[j])
+            gaps[j] = np.inf
+            if gaps.min() > 1e-6:  # a simple level: the vector up to a phase
+                assert abs(abs(np.vdot(Z[:, j], V[:, j])) - 1.0) < 1e-9
+        checked += 1
+        if checked == 3:
+            break
+    s.close()
+    assert checked == 3
+
+
+def _plaquette(method):
+    pt = clusters.square(nx=2, ny=2, U=8.0, xmu=0.95, maf=0.0, nspin=1, nkx=4, nky=4, ngfiter=100,
+                         omega_nodes=256)
+    return _with(pt, lanc_method=method)
+
+
+def test_t0_plaquette_keeps_both_doublets():
+    om, states, th = _solve(_plaquette(LANC_ARPACK))
+    assert [sec for sec, _ in states] == [8, 8, 12, 12]
+    assert th["zeta"] == 4.0
+    o = Oracle.from_point(_plaquette(LANC_ARPACK))
+    ref, _, _ = o.solve()
+    assert abs(om - ref) <= 1e-10 * max(1.0, abs(ref)), (om, ref)
+    om1, states1, th1 = _solve(_plaquette(LANC_LANCZOS))
+    assert [sec for sec, _ in states1] == [8, 12] and th1["zeta"] == 2.0
+    assert abs(om - om1) > 0.05
+
+
+@pytest.mark.parametrize("case", ["bhz-f64", "square2x3-fx"])
+def test_t0_lanczos_path_matches_oracle(case):
+    if case == "bhz-f64":
+        pt = clusters.bhz(mass=2.2, delta=0.1, nk1=4, ngfiter=60, omega_nodes=256)
+    else:
+        pt = clusters.square(nx=3, ny=2, U=6.0, xmu=3.0, maf=0.1, nspin=2, nkx=4, nky=4, ngfiter=60,
+                             omega_nodes=256)
+    pt = _with(pt, lanc_method=LANC_ARPACK, lanc_dim_threshold=8)
+    om, states, th = _solve(pt)
+    o = Oracle.from_point(pt)
+    ref, egs, _ = o.solve()
+    ost = sorted(o.states())
+    assert [sec for sec, _ in states] == [sec for sec, _ in ost]
+    np.testing.assert_allclose([e for _, e in states], [e for _, e in ost], rtol=0, atol=1e-10)
+    assert th["zeta"] == float(len(ost))
+    assert abs(om - ref) <= 1e-10 * max(1.0, abs(ref)), (om, ref)
+
+
+def _lattice_omega(pt, beta, mu):
+    from vca_gb300.clusters import nnn2lso
+    Hk = nnn2lso(pt.Hk)
+    tot = 0.0
+    for k in range(pt.Nk):
+        e = np.linalg.eigvalsh(Hk[:, :, k]) - mu
+        tot -= np.sum(np.logaddexp(0.0, -beta * e)) / beta
+    return (3 - pt.cfg.Nspin) * tot / pt.Nk
+
+
+def test_finite_t_u0_is_the_lattice_value_with_excited_states():
+    """U = 0 two-site chain at beta = 3: with every sector's excited states
+    in the list (16 states) Omega is the exact lattice grand potential; one
+    state per sector (LANC_METHOD="lanczos") misses the in-sector
+    excitations."""
+    beta = 3.0
+    res = {}
+    for method in (LANC_ARPACK, LANC_LANCZOS):
+        pt = clusters.chain1d(tprime=1.0, nlat=2, U=0.0, xmu=0.0, nk=32, ngfiter=50, omega_nodes=64,
+                              lanc_nstates_total=2, beta=beta, bandwidth=4.0)
+        res[method] = _solve(_with(pt, lanc_method=method))
+        exact = _lattice_omega(pt, beta, 0.0)
+    om, states, th = res[LANC_ARPACK]
+    assert len(states) == 16 and th["finite_t"] == 1
+    assert abs(om - exact) < 1e-10, (om, exact)
+    om1, states1, _ = res[LANC_LANCZOS]
+    assert len(states1) == 9 and abs(om1 - exact) > 1e-4
+
+
+@pytest.mark.parametrize("nlat,U,xmu,beta", [(2, 4.0, 1.3, 1.0), (3, 4.0, 2.0, 2.0)])
+def test_finite_t_matches_oracle(nlat, U, xmu, beta):
+    """Interacting chains in the arpack method at finite T: the annealed
+    list (states, zeta, the adapted LANC_NSTATES_TOTAL) and Omega against
+    the oracle's restatement of the same sweeps."""
+    pt = clusters.chain1d(tprime=1.0, nlat=nlat, U=U, xmu=xmu, nk=8, ngfiter=50, omega_nodes=64,
+                          lanc_nstates_total=2, beta=beta, bandwidth=4.0)
+    pt = _with(pt, lanc_method=LANC_ARPACK, lanc_niter_spectrum=20)
+    om, states, th = _solve(pt)
+    o = Oracle.from_point(pt)
+    ref, _, _ = o.solve()
+    ost = sorted(o.states())
+    assert [sec for sec, _ in states] == [sec for sec, _ in ost]
+    np.testing.assert_allclose([e for _, e in states], [e for _, e in ost], rtol=0, atol=1e-10)
+    ot = o.thermal()
+    assert abs(th["zeta"] - ot["zeta"]) <= 1e-12 * ot["zeta"]
+    assert th["nstates_total"] == ot["nstates_total"]
+    assert abs(om - ref) <= 1e-10 * max(1.0, abs(ref)), (om, ref)

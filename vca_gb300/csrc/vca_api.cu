@@ -141,6 +141,9 @@ struct Ctx {
   // list cap is adjusted by every finite-T diagonalisation and carries over
   bool finiteT = false;
   int nstates_total = 1;
+  // "arpack" at finite T: eigenpairs asked of each sector, adapted by every
+  // solve's sweeps (neigen_sector, VCA_DIAG.f90:98-102, vca_post_diag :411-437)
+  std::vector<int> neigen;
   // results
   bool solved = false;
   std::vector<double> sector_e;
@@ -1119,11 +1122,327 @@ int diagonalize_finite_t() {
   return VCA_OK;
 }
 
+// ---------------------------------------------------------------------------
+// LANC_METHOD="arpack" (the reference default; VCA_DIAG.f90:98-111,153-170):
+// the k = min(dim, LANC_NSTATES_SECTOR) lowest eigenpairs of a sector.  Above
+// LANC_DIM_THRESHOLD (and k < dim): a Lanczos with full reorthogonalisation
+// (classical Gram-Schmidt twice per step) from the ground-state search's
+// start vector, stopped when the k lowest Ritz pairs have
+// |beta_{m+1} z_{m,q}| <= LANC_TOLERANCE max(1, |theta_q|) (tested every 5
+// steps) or the Krylov space is exhausted; the Ritz vectors are V z_q.  At
+// or below the threshold the dense H (H x v on the unit vectors) is
+// diagonalised on the host, which returns whole degenerate multiplets as
+// the reference's dense path does.  Vectors come back unit-norm in the
+// solve's state storage: int64 at 2^-F on the fixed-point path, else FP64
+// real or complex.
+// ---------------------------------------------------------------------------
+int sector_pairs(int isector, int k, std::vector<double>& e, std::vector<void*>& vecs, Arena& keep,
+                 bool fp64_out = false) {
+  const vca_config& c = g->cfg;
+  const int nup = sec_nup(isector), ndw = sec_ndw(isector);
+  SectorView sv = view_of(nup, ndw);
+  const int64_t D = (int64_t)sv.dimup * sv.dimdw;
+  const bool cplx = !g->real_model;
+  const size_t es = cplx ? sizeof(double2) : sizeof(double);
+  e.clear();
+  vecs.clear();
+  k = (int)std::min<int64_t>(k, D);
+  if (k <= 0) return VCA_OK;
+  auto emit = [&](const void* x) -> int {  // x: unit-norm FP64 vector on the device
+    if (g->fx && !fp64_out) {
+      i64* X;
+      RCHK(keep.alloc(&X, (size_t)D));
+      launch_fx_from_double(D, (const double*)x, g->fxs.F, X, g->st);
+      vecs.push_back(X);
+    } else {
+      char* X;
+      RCHK(keep.alloc(&X, (size_t)D * es));
+      CUCHK(cudaMemcpyAsync(X, x, (size_t)D * es, cudaMemcpyDeviceToDevice, g->st));
+      vecs.push_back(X);
+    }
+    return VCA_OK;
+  };
+  auto hxv1 = [&](const void* x, void* y, int m) {
+    if (cplx) launch_hxv_cplx(sv, g->md, m, (const double2*)x, (double2*)y, g->st);
+    else launch_hxv_real(sv, g->md, m, (const double*)x, (double*)y, g->st);
+  };
+  Arena ar;
+  int rc = VCA_OK;
+  const bool lanc_solve = k != D && D > std::max(c.lanc_dim_threshold, 1);
+  if (!lanc_solve) {  // dense: H column by column, Jacobi on the host
+    char *X, *Y;
+    if ((rc = ar.alloc(&X, (size_t)D * D * es)) || (rc = ar.alloc(&Y, (size_t)D * D * es))) {
+      ar.release();
+      return rc;
+    }
+    std::vector<double> h((size_t)D * D * (es / sizeof(double)), 0.0);
+    for (int64_t i = 0; i < D; i++) h[(size_t)(i * D + i) * (es / sizeof(double))] = 1.0;
+    CUCHK(cudaMemcpyAsync(X, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, g->st));
+    hxv1(X, Y, (int)D);  // Y[i*D + col] = H[i][col]
+    CUCHK(cudaMemcpyAsync(h.data(), Y, h.size() * sizeof(double), cudaMemcpyDeviceToHost, g->st));
+    CUCHK(cudaStreamSynchronize(g->st));
+    std::vector<double> A(2 * (size_t)D * D, 0.0), w, Z;
+    for (size_t t = 0; t < (size_t)D * D; t++) {
+      A[2 * t] = cplx ? h[2 * t] : h[t];
+      A[2 * t + 1] = cplx ? h[2 * t + 1] : 0.0;
+    }
+    if (!herm_eig((int)D, A.data(), w, Z)) { ar.release(); VFAIL(VCA_ERR_NUMERIC, "dense sector eigensolver did not converge"); }
+    std::vector<double> xh((size_t)D * (es / sizeof(double)));
+    for (int j = 0; j < k; j++) {
+      for (int64_t i = 0; i < D; i++) {
+        const double re = Z[2 * (i + (size_t)j * D)], im = Z[2 * (i + (size_t)j * D) + 1];
+        if (cplx) { xh[2 * i] = re; xh[2 * i + 1] = im; }
+        else xh[i] = re;  // a real symmetric H: Jacobi's rotations are real up to signs
+      }
+      CUCHK(cudaMemcpyAsync(X, xh.data(), xh.size() * sizeof(double), cudaMemcpyHostToDevice, g->st));
+      if ((rc = emit(X))) { ar.release(); return rc; }
+      CUCHK(cudaStreamSynchronize(g->st));
+      e.push_back(w[j]);
+    }
+    ar.release();
+    return VCA_OK;
+  }
+  const int mmax = (int)std::min<int64_t>(D, std::max(c.lanc_niter, 2 * k));
+  char *V, *w, *partial, *cq;
+  double* dz;
+  if ((rc = ar.alloc(&V, (size_t)mmax * D * es))) {
+    ar.release();
+    VFAIL(VCA_ERR_ALLOC, "the arpack path stores " + std::to_string(mmax) + " Lanczos vectors of sector " +
+                             std::to_string(isector) + " (" + std::to_string((size_t)mmax * D * es) +
+                             " bytes); use lanc_method=lanczos");
+  }
+  if ((rc = ar.alloc(&w, (size_t)D * es)) || (rc = ar.alloc(&partial, (size_t)ap_partial_len(mmax) * es)) ||
+      (rc = ar.alloc(&cq, (size_t)mmax * es)) || (rc = ar.alloc(&dz, (size_t)mmax))) {
+    ar.release();
+    return rc;
+  }
+  auto vec = [&](int j) { return V + (size_t)j * D * es; };
+  auto dotr = [&](const void* x, const void* y, double* out) -> int {  // Re <x, y>
+    launch_ap_proj(D, 1, cplx, x, y, partial, cq, g->st);
+    CUCHK(cudaMemcpyAsync(out, cq, sizeof(double), cudaMemcpyDeviceToHost, g->st));
+    CUCHK(cudaStreamSynchronize(g->st));
+    return VCA_OK;
+  };
+  launch_start_vector(D, c.start_seed, isector, (double*)w, g->st);
+  if (cplx) launch_real_to_cplx(D, (const double*)w, (double2*)vec(0), g->st);
+  else CUCHK(cudaMemcpyAsync(vec(0), w, (size_t)D * es, cudaMemcpyDeviceToDevice, g->st));
+  double n2 = 0.0;
+  if ((rc = dotr(vec(0), vec(0), &n2))) { ar.release(); return rc; }
+  if (!(n2 > 0.0)) { ar.release(); VFAIL(VCA_ERR_NUMERIC, "Lanczos start vector has zero norm"); }
+  launch_ap_axpby(D, cplx, 0.0, -1.0 / std::sqrt(n2), vec(0), vec(0), g->st);
+  std::vector<double> a, b(1, 0.0), theta, Zt;
+  int m = 0;
+  for (int j = 0; j < mmax; j++) {
+    hxv1(vec(j), w, 1);
+    if (j > 0) launch_ap_axpby(D, cplx, 1.0, b[j], vec(j - 1), w, g->st);
+    double aj = 0.0;
+    if ((rc = dotr(vec(j), w, &aj))) { ar.release(); return rc; }
+    launch_ap_axpby(D, cplx, 1.0, aj, vec(j), w, g->st);
+    for (int pass = 0; pass < 2; pass++) {
+      launch_ap_proj(D, j + 1, cplx, V, w, partial, cq, g->st);
+      launch_ap_orth(D, j + 1, cplx, V, cq, w, g->st);
+    }
+    double bb2 = 0.0;
+    if ((rc = dotr(w, w, &bb2))) { ar.release(); return rc; }
+    const double bj1 = std::sqrt(std::max(bb2, 0.0));
+    a.push_back(aj);
+    b.push_back(bj1);
+    m = j + 1;
+    const bool exhausted = bj1 <= c.gs_beta_tol * std::max(1.0, std::fabs(aj));
+    if (exhausted || m == mmax) break;
+    if (m >= k && m % 5 == 0) {
+      if (!tridiag_eig(m, a.data(), b.data() + 1, theta, Zt)) { ar.release(); VFAIL(VCA_ERR_NUMERIC, "Ritz QL did not converge"); }
+      bool conv = true;
+      for (int q = 0; q < k && conv; q++)
+        conv = std::fabs(bj1 * Zt[(m - 1) + (size_t)q * m]) <= c.lanc_tolerance * std::max(1.0, std::fabs(theta[q]));
+      if (conv) break;
+    }
+    launch_ap_axpby(D, cplx, 0.0, -1.0 / bj1, w, vec(j + 1), g->st);
+  }
+  if (!tridiag_eig(m, a.data(), b.data() + 1, theta, Zt)) { ar.release(); VFAIL(VCA_ERR_NUMERIC, "Ritz QL did not converge"); }
+  const int nk = std::min(k, m);
+  for (int q = 0; q < nk; q++) {
+    CUCHK(cudaMemcpyAsync(dz, Zt.data() + (size_t)q * m, sizeof(double) * m, cudaMemcpyHostToDevice, g->st));
+    launch_ap_combine(D, m, cplx, V, dz, w, g->st);
+    double nx = 0.0;
+    if ((rc = dotr(w, w, &nx))) { ar.release(); return rc; }
+    launch_ap_axpby(D, cplx, 0.0, -1.0 / std::sqrt(nx), w, w, g->st);
+    if ((rc = emit(w))) { ar.release(); return rc; }
+    CUCHK(cudaStreamSynchronize(g->st));
+    e.push_back(theta[q]);
+  }
+  ar.release();
+  return VCA_OK;
+}
+
+// T=0, LANC_METHOD="arpack": every sector's eigenpairs through the
+// ground-state bookkeeping of VCA_DIAG.f90:224-236 (a level below the running
+// zero by more than 10 GS_THRESHOLD restarts the list, one within
+// GS_THRESHOLD joins it, inserted before the first entry with e <= its
+// energy), sector by sector and, inside a sector, in ascending order.  Only
+// sectors whose lowest level (the batched search) lies within 11
+// GS_THRESHOLD of the minimum need their pairs: the minimum restarts the list
+// below every level above that window whenever it comes, and after it no
+// such level joins, so the list is the one of a scan of all pairs of all
+// sectors.
+int diagonalize_arpack_t0() {
+  const vca_config& c = g->cfg;
+  const double thr = c.gs_threshold;
+  std::vector<double> eb;
+  RCHK(g->fx ? batched_sector_energies(eb) : batched_sector_energies_f64(eb));
+  double emin = INFINITY;
+  for (double x : eb) emin = std::min(emin, x);
+  std::vector<std::vector<double>> E(g->Nsectors);
+  std::vector<std::vector<void*>> X(g->Nsectors);
+  Arena keep;
+  for (int isector = 1; isector <= g->Nsectors; isector++) {
+    const int64_t D = (int64_t)g->dimn[sec_nup(isector)] * g->dimn[sec_ndw(isector)];
+    if (eb[isector - 1] <= emin + 11.0 * thr) {
+      const int k = (int)std::min<int64_t>(D, std::max(1, c.lanc_nstates_sector));
+      const int rc = sector_pairs(isector, k, E[isector - 1], X[isector - 1], keep);
+      if (rc) { keep.release(); return rc; }
+    }
+    if (E[isector - 1].empty()) {  // outside the window: its lowest level stands for the sector
+      E[isector - 1].assign(1, eb[isector - 1]);
+      X[isector - 1].assign(1, nullptr);
+    }
+    g->sector_e[isector - 1] = E[isector - 1][0];
+  }
+  struct Entry {
+    double e;
+    int sector, idx;
+  };
+  std::vector<Entry> list;
+  double oldzero = 1000.0;
+  for (int isector = 1; isector <= g->Nsectors; isector++)
+    for (int i = 0; i < (int)E[isector - 1].size(); i++) {
+      const double en = E[isector - 1][i];
+      if (en < oldzero - 10.0 * thr) {
+        oldzero = en;
+        list.assign(1, Entry{en, isector, i});
+      } else if (std::fabs(en - oldzero) <= thr) {
+        oldzero = std::min(oldzero, en);
+        auto it = list.begin();
+        while (it != list.end() && !(en <= it->e)) ++it;
+        list.insert(it, Entry{en, isector, i});
+      }
+    }
+  g->states.release();
+  g->gs.clear();
+  for (const Entry& x : list) {
+    void* v = X[x.sector - 1][x.idx];
+    if (!v) { keep.release(); VFAIL(VCA_ERR_NUMERIC, "a level outside the screened window entered the state list"); }
+    g->gs.push_back(GState{x.sector, x.e, v});
+  }
+  g->states.ptrs = keep.ptrs;
+  g->egs = INFINITY;
+  for (auto& st : g->gs) g->egs = std::min(g->egs, st.e);
+  g->zeta = (double)g->gs.size();  // VCA_DIAG.f90:363
+  return VCA_OK;
+}
+
+// Finite T, LANC_METHOD="arpack": the annealing sweeps of VCA_DIAG.f90:
+// 78-256 with Neigen = min(dim, neigen_sector) eigenpairs of every sector in
+// the capped list (es_add_state_c with size, VCA_EIGENSPACE.f90:136-159),
+// then vca_post_diag (:357-451): zeta over the whole list; neigen_sector + 1
+// for sectors in the list and - 1 for the others, at most the sector's count
+// in the list + 1 and at least 1 (:411-437); the cap grows by
+// LANC_NSTATES_STEP, or the list is trimmed at the cut-off and the cap reset
+// to max(size, step) + step.  A sector's pairs are computed again only when a
+// sweep asks for more of them.
+int diagonalize_arpack_finite_t() {
+  const vca_config& c = g->cfg;
+  const int ns = g->Nsectors;
+  auto dim = [&](int isector) { return (int64_t)g->dimn[sec_nup(isector)] * g->dimn[sec_ndw(isector)]; };
+  if ((int)g->neigen.size() != ns) {
+    g->neigen.resize(ns);
+    for (int i = 0; i < ns; i++) g->neigen[i] = (int)std::min<int64_t>(dim(i + 1), std::max(1, c.lanc_nstates_sector));
+  }
+  std::vector<std::vector<double>> E(ns);
+  std::vector<std::vector<void*>> X(ns);
+  std::vector<int> have(ns, -1);
+  Arena keep;
+  struct Entry {
+    int sector, idx;
+  };
+  std::vector<Entry> list;
+  auto en = [&](const Entry& x) { return E[x.sector - 1][x.idx]; };
+  double emin = DBL_MAX, emax = -DBL_MAX, zeta = 0.0;
+  auto insert = [&](Entry x) {  // es_insert_state_c (:167-216): before the first entry with e >= its energy
+    const double ev = en(x);
+    size_t pos = 0;
+    while (pos < list.size() && !(ev <= en(list[pos]))) pos++;
+    list.insert(list.begin() + pos, x);
+    if (ev > emax) emax = ev;
+    if (ev < emin) emin = ev;
+  };
+  auto pop = [&]() {  // es_pop_state (:230-312): the last entry
+    list.pop_back();
+    if (!list.empty()) {
+      emax = en(list.back());
+      emin = en(list.front());
+    }
+  };
+  bool converged = false;
+  for (int iter = 0; !converged && iter < c.lanc_niter_spectrum; iter++) {
+    for (int isector = 1; isector <= ns; isector++)
+      if (have[isector - 1] < g->neigen[isector - 1]) {
+        std::vector<void*> v;
+        const int rc = sector_pairs(isector, g->neigen[isector - 1], E[isector - 1], v, keep);
+        if (rc) { keep.release(); return rc; }
+        X[isector - 1] = v;
+        have[isector - 1] = g->neigen[isector - 1];
+      }
+    list.clear();
+    emin = DBL_MAX;
+    emax = -DBL_MAX;
+    for (int isector = 1; isector <= ns; isector++) {
+      const int ne = std::min(g->neigen[isector - 1], (int)E[isector - 1].size());
+      for (int i = 0; i < ne; i++) {
+        const Entry x{isector, i};
+        if ((int)list.size() < g->nstates_total) insert(x);
+        else if (en(x) < en(list.back())) { pop(); insert(x); }
+      }
+    }
+    converged = std::exp(-c.beta * (emax - emin)) < c.cutoff;  // VCA_DIAG.f90:251-256
+    zeta = 0.0;
+    for (const Entry& x : list) zeta += std::exp(-c.beta * (en(x) - emin));
+    std::vector<int> count(ns, 0);
+    for (const Entry& x : list) count[x.sector - 1]++;
+    for (int i = 0; i < ns; i++) {
+      int& ne = g->neigen[i];
+      ne += count[i] > 0 ? 1 : -1;
+      if (ne > count[i]) ne = count[i] + 1;
+      if (ne <= 0) ne = 1;
+    }
+    if (std::exp(-c.beta * (emax - emin)) > c.cutoff) {
+      g->nstates_total += c.lanc_nstates_step;
+    } else {
+      double Ei = en(list.back());
+      while (std::exp(-c.beta * (Ei - emin)) <= c.cutoff) {
+        pop();
+        Ei = en(list.back());
+      }
+      g->nstates_total = std::max((int)list.size(), c.lanc_nstates_step) + c.lanc_nstates_step;
+    }
+  }
+  for (int isector = 1; isector <= ns; isector++)
+    if (!E[isector - 1].empty()) g->sector_e[isector - 1] = E[isector - 1][0];
+  g->states.release();
+  g->gs.clear();
+  for (const Entry& x : list) g->gs.push_back(GState{x.sector, en(x), X[x.sector - 1][x.idx]});
+  g->states.ptrs = keep.ptrs;
+  g->egs = emin;
+  g->zeta = zeta;
+  return VCA_OK;
+}
+
 int diagonalize() {
   const vca_config& c = g->cfg;
   g->states.release();
   g->gs.clear();
   g->sector_e.assign(g->Nsectors, INFINITY);
+  if (c.lanc_method != VCA_LANC_LANCZOS) return g->finiteT ? diagonalize_arpack_finite_t() : diagonalize_arpack_t0();
   if (g->finiteT) return diagonalize_finite_t();
   double oldzero = 1000.0;
   const double thr = c.gs_threshold;
@@ -3911,6 +4230,32 @@ int vca_gpu_solve_resident(const double* Hloc, const double* bath_h, const doubl
 }
 
 int64_t vca_gpu_kernel_launches(void) { return (int64_t)launch_count(); }
+
+int vca_gpu_sector_pairs(int32_t isector, int32_t k, double* energies, double* vecs, int32_t* n) {
+  if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
+  if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
+  if (k < 1 || !energies || !n) VFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<double> e;
+  std::vector<void*> v;
+  Arena keep;
+  int rc = sector_pairs(isector, k, e, v, keep, true);
+  if (rc) { keep.release(); return rc; }
+  const int64_t D = (int64_t)g->dimn[sec_nup(isector)] * g->dimn[sec_ndw(isector)];
+  *n = (int32_t)e.size();
+  for (size_t j = 0; j < e.size(); j++) {
+    energies[j] = e[j];
+    if (!vecs) continue;
+    std::vector<double> h((size_t)D * (g->real_model ? 1 : 2));
+    cudaMemcpy(h.data(), v[j], h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    for (int64_t i = 0; i < D; i++) {
+      vecs[2 * (j * D + i)] = g->real_model ? h[i] : h[2 * i];
+      vecs[2 * (j * D + i) + 1] = g->real_model ? 0.0 : h[2 * i + 1];
+    }
+  }
+  keep.release();
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
 
 int vca_gpu_get_timings(double* ms, int32_t n) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <complex>
 #include <cstring>
 
 #include "vca_gfmatrix.h"
@@ -222,9 +223,161 @@ void contour_nodes_host(double R, double beta, double mu, int ngl, std::vector<d
   }
 }
 
+// Implicit QL with Wilkinson shifts on a symmetric tridiagonal matrix.  Each
+// sweep deflates at the first negligible off-diagonal element below l, then
+// chases the bulge from m back up to l with Givens rotations, accumulating
+// them in the columns of Z.
+bool tridiag_eig(int n, const double* d_in, const double* e_in, std::vector<double>& w, std::vector<double>& Z) {
+  std::vector<double> d(d_in, d_in + n), e(n, 0.0);
+  for (int i = 0; i + 1 < n; i++) e[i] = e_in[i];
+  Z.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) Z[i + (size_t)i * n] = 1.0;
+  for (int l = 0; l < n; l++) {
+    for (int iter = 0;; iter++) {
+      int m = l;
+      for (; m + 1 < n; m++) {
+        const double scale = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) <= DBL_EPSILON * scale) break;
+      }
+      if (m == l) break;
+      if (iter == 60) return false;
+      // shift: the eigenvalue of the leading 2x2 block nearer d[l]
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? r : -r));
+      double s = 1.0, c = 1.0, p = 0.0;
+      int i = m - 1;
+      bool early = false;
+      for (; i >= l; i--) {
+        const double f = s * e[i], b = c * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {  // the bulge vanished: split here
+          d[i + 1] -= p;
+          e[m] = 0.0;
+          early = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+        double* zi = Z.data() + (size_t)i * n;
+        double* zj = Z.data() + (size_t)(i + 1) * n;
+        for (int k = 0; k < n; k++) {
+          const double t = zj[k];
+          zj[k] = s * zi[k] + c * t;
+          zi[k] = c * zi[k] - s * t;
+        }
+      }
+      if (early) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return d[a] < d[b]; });
+  w.resize(n);
+  std::vector<double> Zs((size_t)n * n);
+  for (int j = 0; j < n; j++) {
+    w[j] = d[ord[j]];
+    std::memcpy(Zs.data() + (size_t)j * n, Z.data() + (size_t)ord[j] * n, sizeof(double) * n);
+  }
+  Z.swap(Zs);
+  return true;
+}
+
+// Cyclic Jacobi for a Hermitian matrix: for each pair (p, q) the phase of
+// a_pq is moved into column q (making a_pq real and positive), then a real
+// rotation zeroes it; the same unitary is accumulated in Z.
+bool herm_eig(int n, const double* A_in, std::vector<double>& w, std::vector<double>& Z) {
+  typedef std::complex<double> cdd;
+  std::vector<cdd> a((size_t)n * n), z((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) a[i + (size_t)j * n] = cdd(A_in[2 * ((size_t)i * n + j)], A_in[2 * ((size_t)i * n + j) + 1]);
+  for (int i = 0; i < n; i++) z[i + (size_t)i * n] = 1.0;
+  auto A = [&](int i, int j) -> cdd& { return a[i + (size_t)j * n]; };
+  bool ok = false;
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        const double v = std::norm(A(i, j));
+        tot += v;
+        if (i != j) off += v;
+      }
+    if (off <= 1e-30 * tot || off == 0.0) { ok = true; break; }
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double r = std::abs(A(p, q));
+        if (r == 0.0) continue;
+        const cdd ph = std::conj(A(p, q)) / r;  // column q times ph, row q times conj(ph)
+        for (int k = 0; k < n; k++) A(k, q) *= ph;
+        for (int k = 0; k < n; k++) A(q, k) *= std::conj(ph);
+        for (int k = 0; k < n; k++) z[k + (size_t)q * n] *= ph;
+        const double app = A(p, p).real(), aqq = A(q, q).real(), apq = A(p, q).real();
+        const double th = 0.5 * (aqq - app) / apq;
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < n; k++) {
+          const cdd akp = A(k, p), akq = A(k, q);
+          A(k, p) = c * akp - sn * akq;
+          A(k, q) = sn * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {
+          const cdd apk = A(p, k), aqk = A(q, k);
+          A(p, k) = c * apk - sn * aqk;
+          A(q, k) = sn * apk + c * aqk;
+        }
+        A(p, q) = A(q, p) = 0.0;
+        for (int k = 0; k < n; k++) {
+          const cdd zkp = z[k + (size_t)p * n], zkq = z[k + (size_t)q * n];
+          z[k + (size_t)p * n] = c * zkp - sn * zkq;
+          z[k + (size_t)q * n] = sn * zkp + c * zkq;
+        }
+      }
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A(x, x).real() < A(y, y).real(); });
+  w.resize(n);
+  Z.assign(2 * (size_t)n * n, 0.0);
+  for (int j = 0; j < n; j++) {
+    w[j] = A(ord[j], ord[j]).real();
+    for (int k = 0; k < n; k++) {
+      Z[2 * (k + (size_t)j * n)] = z[k + (size_t)ord[j] * n].real();
+      Z[2 * (k + (size_t)j * n) + 1] = z[k + (size_t)ord[j] * n].imag();
+    }
+  }
+  return ok;
+}
+
 }  // namespace vca
 
 using namespace vca;
+
+int vca_tridiag_eig(int32_t n, const double* d, const double* e, double* w, double* Z) {
+  if (n < 1 || !d || !w || (n > 1 && !e)) HFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<double> ww, zz;
+  if (!tridiag_eig(n, d, e, ww, zz)) HFAIL(VCA_ERR_NUMERIC, "tridiagonal QL did not converge");
+  std::memcpy(w, ww.data(), sizeof(double) * n);
+  if (Z) std::memcpy(Z, zz.data(), sizeof(double) * zz.size());
+  return VCA_OK;
+}
+
+int vca_herm_eig(int32_t n, const double* A, double* w, double* Z) {
+  if (n < 1 || !A || !w) HFAIL(VCA_ERR_ARG, "bad arguments");
+  std::vector<double> ww, zz;
+  if (!herm_eig(n, A, ww, zz)) HFAIL(VCA_ERR_NUMERIC, "Jacobi rotations did not converge");
+  std::memcpy(w, ww.data(), sizeof(double) * n);
+  if (Z) std::memcpy(Z, zz.data(), sizeof(double) * zz.size());
+  return VCA_OK;
+}
 
 extern "C" {
 

@@ -30,6 +30,18 @@ void gauss_legendre01_host(int n, std::vector<double>& x, std::vector<double>& w
 void contour_nodes_host(double R, double beta, double mu, int ngl, std::vector<double>& th,
                         std::vector<double>& wt);
 
+// Symmetric tridiagonal eigenproblem (diagonal d[0..n-1], off-diagonal
+// e[i] coupling i and i+1, i < n-1) by implicit QL iterations with
+// Wilkinson shifts: eigenvalues ascending in w, eigenvectors as columns of
+// Z (column-major n x n).  Returns false if an eigenvalue needed more than
+// 60 iterations.
+bool tridiag_eig(int n, const double* d, const double* e, std::vector<double>& w, std::vector<double>& Z);
+// Hermitian dense eigenproblem (A row-major n x n, complex interleaved) by
+// cyclic complex Jacobi rotations: eigenvalues ascending in w, eigenvectors
+// as columns of Z (column-major n x n, complex interleaved).  Returns false
+// if 100 sweeps did not bring the off-diagonal norm to 1e-15 of the total.
+bool herm_eig(int n, const double* A, std::vector<double>& w, std::vector<double>& Z);
+
 // sets the text vca_gpu_last_error returns and hands the code back
 int set_error(int code, const std::string& msg);
 

@@ -1871,4 +1871,148 @@ void launch_gather_blocks(int64_t nrep, int64_t nel, const int64_t* idx, const d
   k_gather_blocks<<<nblocks(nrep * nel, 256), 256, 0, st>>>(nrep, nel, idx, src, dst);
 }
 
+// ---------------------------------------------------------------------------
+// Lanczos with full reorthogonalisation ("arpack" diagonalisation): the
+// stored basis V (nq vectors of n elements, vector q at V + q*n), real
+// (double) or complex (double2) elements.  Every reduction is fixed-order:
+// block partials in a fixed tree, then one warp per output over the blocks.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double ap_cdot(double v, double w) { return v * w; }
+__device__ __forceinline__ double2 ap_cdot(double2 v, double2 w) {  // conj(v) * w
+  return make_double2(v.x * w.x + v.y * w.y, v.x * w.y - v.y * w.x);
+}
+__device__ __forceinline__ double ap_add(double a, double b) { return a + b; }
+__device__ __forceinline__ double2 ap_add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double ap_zero(double) { return 0.0; }
+__device__ __forceinline__ double2 ap_zero(double2) { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ double ap_fms(double w, double c, double v) { return fma(-c, v, w); }
+__device__ __forceinline__ double2 ap_fms(double2 w, double2 c, double2 v) {  // w - c v
+  return make_double2(w.x - (c.x * v.x - c.y * v.y), w.y - (c.x * v.y + c.y * v.x));
+}
+__device__ __forceinline__ double ap_shfl(double v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
+__device__ __forceinline__ double2 ap_shfl(double2 v, int off) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, off), __shfl_xor_sync(0xffffffffu, v.y, off));
+}
+
+__device__ __forceinline__ double ap_scalar(double, double v) { return v; }
+__device__ __forceinline__ double2 ap_scalar(double2, double v) { return make_double2(v, 0.0); }
+// a = 0 ignores y (a fresh buffer may hold NaN bit patterns)
+__device__ __forceinline__ double ap_lin(double a, double y, double s, double x) {
+  return fma(-s, x, a == 0.0 ? 0.0 : a * y);
+}
+__device__ __forceinline__ double2 ap_lin(double a, double2 y, double s, double2 x) {
+  return make_double2(fma(-s, x.x, a == 0.0 ? 0.0 : a * y.x), fma(-s, x.y, a == 0.0 ? 0.0 : a * y.y));
+}
+
+// partial[q*nblk + b] = sum over block b's rows of conj(V_q[i]) w[i]
+template <typename T>
+__global__ void __launch_bounds__(256) k_ap_proj(int64_t n, const T* __restrict__ V, const T* __restrict__ w,
+                                                 T* partial) {
+  __shared__ T red[256];
+  const int q = blockIdx.y, nblk = gridDim.x;
+  const int64_t chunk = (n + nblk - 1) / nblk;
+  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+  const T* vq = V + (int64_t)q * n;
+  T s = ap_zero(T());
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = ap_add(s, ap_cdot(vq[i], w[i]));
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] = ap_add(red[threadIdx.x], red[threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(int64_t)q * nblk + blockIdx.x] = red[0];
+}
+
+// c[q] = sum_b partial[q*nblk + b], one warp per q
+template <typename T>
+__global__ void k_ap_sum(int nq, int nblk, const T* partial, T* c) {
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= nq) return;
+  T s = ap_zero(T());
+  for (int b = lane; b < nblk; b += 32) s = ap_add(s, partial[(int64_t)q * nblk + b]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s = ap_add(s, ap_shfl(s, off));
+  if (lane == 0) c[q] = s;
+}
+
+// w[i] -= sum_q c[q] V_q[i]  (q ascending)
+template <typename T>
+__global__ void __launch_bounds__(256) k_ap_orth(int64_t n, int nq, const T* __restrict__ V, const T* __restrict__ c,
+                                                 T* __restrict__ w) {
+  extern __shared__ __align__(16) unsigned char ap_smem[];
+  T* cs = (T*)ap_smem;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) cs[q] = c[q];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T x = w[i];
+    for (int q = 0; q < nq; q++) x = ap_fms(x, cs[q], V[(int64_t)q * n + i]);
+    w[i] = x;
+  }
+}
+
+// x[i] = sum_q z[q] V_q[i] (real coefficients, q ascending)
+template <typename T>
+__global__ void __launch_bounds__(256) k_ap_combine(int64_t n, int nq, const T* __restrict__ V,
+                                                    const double* __restrict__ z, T* __restrict__ x) {
+  extern __shared__ __align__(16) unsigned char ap_smem[];
+  double* zs = (double*)ap_smem;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) zs[q] = z[q];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T acc = ap_zero(T());
+    for (int q = 0; q < nq; q++) acc = ap_fms(acc, ap_scalar(T(), -zs[q]), V[(int64_t)q * n + i]);
+    x[i] = acc;
+  }
+}
+
+// y = a*y - s*x (real scalars: y -= s x with a = 1, y = x/b with a = 0)
+template <typename T>
+__global__ void k_ap_axpby(int64_t n, double a, double s, const T* __restrict__ x, T* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = ap_lin(a, y[i], s, x[i]);
+}
+
+#define AP_NBLK 304
+void launch_ap_proj(int64_t n, int nq, bool cplx, const void* V, const void* w, void* partial, void* c,
+                    cudaStream_t st) {
+  COUNT_LAUNCH();
+  COUNT_LAUNCH();
+  const dim3 grd(AP_NBLK, nq, 1);
+  if (cplx) {
+    k_ap_proj<double2><<<grd, 256, 0, st>>>(n, (const double2*)V, (const double2*)w, (double2*)partial);
+    k_ap_sum<double2><<<(nq * 32 + 127) / 128, 128, 0, st>>>(nq, AP_NBLK, (const double2*)partial, (double2*)c);
+  } else {
+    k_ap_proj<double><<<grd, 256, 0, st>>>(n, (const double*)V, (const double*)w, (double*)partial);
+    k_ap_sum<double><<<(nq * 32 + 127) / 128, 128, 0, st>>>(nq, AP_NBLK, (const double*)partial, (double*)c);
+  }
+}
+int ap_partial_len(int nq) { return AP_NBLK * nq; }
+void launch_ap_orth(int64_t n, int nq, bool cplx, const void* V, const void* c, void* w, cudaStream_t st) {
+  COUNT_LAUNCH();
+  if (cplx)
+    k_ap_orth<double2><<<nblocks(n, 256), 256, sizeof(double2) * nq, st>>>(n, nq, (const double2*)V,
+                                                                         (const double2*)c, (double2*)w);
+  else
+    k_ap_orth<double><<<nblocks(n, 256), 256, sizeof(double) * nq, st>>>(n, nq, (const double*)V, (const double*)c,
+                                                                       (double*)w);
+}
+void launch_ap_combine(int64_t n, int nq, bool cplx, const void* V, const double* z, void* x, cudaStream_t st) {
+  COUNT_LAUNCH();
+  if (cplx)
+    k_ap_combine<double2><<<nblocks(n, 256), 256, sizeof(double) * nq, st>>>(n, nq, (const double2*)V, z,
+                                                                           (double2*)x);
+  else
+    k_ap_combine<double><<<nblocks(n, 256), 256, sizeof(double) * nq, st>>>(n, nq, (const double*)V, z,
+                                                                          (double*)x);
+}
+void launch_ap_axpby(int64_t n, bool cplx, double a, double s, const void* x, void* y, cudaStream_t st) {
+  COUNT_LAUNCH();
+  if (cplx)
+    k_ap_axpby<double2><<<nblocks(n, 256), 256, 0, st>>>(n, a, s, (const double2*)x, (double2*)y);
+  else
+    k_ap_axpby<double><<<nblocks(n, 256), 256, 0, st>>>(n, a, s, (const double*)x, (double*)y);
+}
+
 }  // namespace vca

@@ -209,4 +209,17 @@ void launch_omega_nodes(int n, double scale, const double* s, const double* w, d
 void launch_wsum(int n, const double* a, const double* b, double* out, cudaStream_t st);
 void launch_real_to_cplx(int64_t n, const double* in, double2* out, cudaStream_t st);
 
+// ---- Lanczos with full reorthogonalisation ("arpack" diagonalisation) ----
+// V: nq stored vectors of n elements (double, or double2 when cplx).
+// c[q] = <V_q, w> (conj(V_q) . w; partial needs ap_partial_len(nq) elements)
+void launch_ap_proj(int64_t n, int nq, bool cplx, const void* V, const void* w, void* partial, void* c,
+                    cudaStream_t st);
+int ap_partial_len(int nq);
+// w -= sum_q c[q] V_q
+void launch_ap_orth(int64_t n, int nq, bool cplx, const void* V, const void* c, void* w, cudaStream_t st);
+// x = sum_q z[q] V_q (z real, on the device)
+void launch_ap_combine(int64_t n, int nq, bool cplx, const void* V, const double* z, void* x, cudaStream_t st);
+// y = a*y - s*x
+void launch_ap_axpby(int64_t n, bool cplx, double a, double s, const void* x, void* y, cudaStream_t st);
+
 }  // namespace vca

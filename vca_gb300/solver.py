@@ -44,6 +44,7 @@ EXPORTS = [
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
     "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
     "vca_state_list_t0", "vca_state_list_finite_t", "vca_pair_kpoints", "vca_contour_rule",
+    "vca_tridiag_eig", "vca_herm_eig", "vca_gpu_sector_pairs",
     "vca_read_impSigma", "vca_splot_read",
     "vca_mlp_config_defaults", "vca_mlp_init", "vca_mlp_finalize", "vca_mlp_param_count",
     "vca_mlp_get_params", "vca_mlp_set_params", "vca_mlp_set_data", "vca_mlp_loss_grad", "vca_mlp_train",
@@ -143,6 +144,9 @@ def load(path: Optional[str] = None):
         "vca_state_list_finite_t": (ctypes.c_int, [dp, i32, cfgp, i32, ctypes.POINTER(i32), i32,
                                                    ctypes.POINTER(i32), dp, dp, ctypes.POINTER(i32)]),
         "vca_pair_kpoints": (ctypes.c_int, [dp, i64, i64, ctypes.POINTER(i64), dp, i64, ctypes.POINTER(i64)]),
+        "vca_tridiag_eig": (ctypes.c_int, [i32, dp, dp, dp, dp]),
+        "vca_gpu_sector_pairs": (ctypes.c_int, [i32, i32, dp, dp, ctypes.POINTER(i32)]),
+        "vca_herm_eig": (ctypes.c_int, [i32, dp, dp, dp]),
         "vca_contour_rule": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, i32, dp, dp, i32,
                                             ctypes.POINTER(i32)]),
         "vca_gpu_print_impSigma": (ctypes.c_int, []),
@@ -275,6 +279,18 @@ class VcaSolver:
         out = np.zeros(13)
         check(self.L.vca_gpu_get_timings(_dp(out), 13))
         return out[4:] if batched else out[:4]
+
+    def sector_pairs(self, isector: int, k: int):
+        """(energies, vectors as columns) of the k lowest eigenpairs of a
+        sector as the "arpack" diagonalisation finds them."""
+        _, _, du, dd = self.sector_info(isector)
+        D = du * dd
+        e = np.zeros(k)
+        v = np.zeros(2 * k * D)
+        n = ctypes.c_int32()
+        check(self.L.vca_gpu_sector_pairs(isector, k, _dp(e), _dp(v), ctypes.byref(n)))
+        nn = n.value
+        return e[:nn], v.view(np.complex128).reshape(k, D)[:nn].T
 
     def chain_timings(self):
         """The last solve's chain stage: (start-vector ms, Lanczos-step ms,
@@ -563,6 +579,29 @@ def state_list_t0(E, gs_threshold: float):
     check(load().vca_state_list_t0(_dp(E), len(E), gs_threshold, sec.ctypes.data_as(i32p), _dp(en), cap,
                                    ctypes.byref(n)))
     return list(zip(sec[:n.value].tolist(), en[:n.value].tolist()))
+
+
+def tridiag_eig(d, e):
+    """Eigenvalues (ascending) and eigenvectors (columns) of the symmetric
+    tridiagonal matrix with diagonal d and off-diagonal e (host QL)."""
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    n = len(d)
+    e = np.ascontiguousarray(np.r_[e, 0.0][:max(n - 1, 1)], dtype=np.float64)
+    w = np.zeros(n)
+    Z = np.zeros(n * n)
+    check(load().vca_tridiag_eig(n, _dp(d), _dp(e), _dp(w), _dp(Z)))
+    return w, Z.reshape(n, n).T
+
+
+def herm_eig(A):
+    """Eigenvalues (ascending) and eigenvectors (columns) of the Hermitian
+    matrix A (host Jacobi)."""
+    A = np.ascontiguousarray(A, dtype=np.complex128)
+    n = A.shape[0]
+    w = np.zeros(n)
+    Z = np.zeros(2 * n * n)
+    check(load().vca_herm_eig(n, _dp(A.view(np.float64)), _dp(w), _dp(Z)))
+    return w, Z.view(np.complex128).reshape(n, n).T
 
 
 def state_list_finite_t(E, cfg: VcaConfig, nstates_total: int):
