@@ -655,7 +655,7 @@ def c5_solve(steps: int) -> dict:
     return out
 
 
-def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
+def profile_hxv(ncols: int, reps: int, variant: int = 0, pairing: bool = True) -> int:
     """Batched H x v only (for ncu captures of the H x v kernel)."""
     import torch
     from vca_gb300 import build as vbuild
@@ -665,6 +665,7 @@ def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
     cfg = pt.cfg.copy()
     cfg.hxv_variant = variant
     s = VcaSolver(cfg)
+    s.set_hop_pairing(pairing)
     s.set_hamiltonian(pt.Hloc)
     isec = 1 + 6 + 7 * 13
     _, _, du, dd = s.sector_info(isec)
@@ -673,7 +674,7 @@ def profile_hxv(ncols: int, reps: int, variant: int = 0) -> int:
     y = torch.empty_like(x)
     torch.cuda.synchronize()
     ms = s.hxv_timed(isec, x.data_ptr(), y.data_ptr(), 0, ncols, reps)
-    print(json.dumps({"kernel": kname, "sector": [7, 6], "D": D, "ncols": ncols, "reps": reps,
+    print(json.dumps({"kernel": kname, "sector": [7, 6], "D": D, "ncols": ncols, "reps": reps, "hop_pairing": pairing,
                       "ms_per_launch": ms, "alg_GBps": 16.0 * D * ncols / (ms / 1e3) / 1e9}))
     s.close()
     return 0
@@ -794,6 +795,8 @@ def main():
     ap.add_argument("--profile-mlp", type=int, default=0, metavar="STEPS",
                     help="profiling mode: STEPS Adam steps of the surrogate on 200 samples with gradients")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-hop-pairing", action="store_true",
+                    help="--profile-hxv with the chains' kernel's plain hop order")
     ap.add_argument("--profile-hxv-c5", type=int, default=0, metavar="NCOLS",
                     help="time a NCOLS-column H x v on a chain sector of the 4x4 cluster, both forms")
     ap.add_argument("--c5-solve", action="store_true",
@@ -805,7 +808,7 @@ def main():
                     help="0 staged form, 1 warp form, 2 the chains' layout and kernel (default)")
     args = ap.parse_args()
     if args.profile_hxv:
-        return profile_hxv(args.profile_hxv, args.reps, args.hxv_variant)
+        return profile_hxv(args.profile_hxv, args.reps, args.hxv_variant, not args.no_hop_pairing)
     if args.profile_solve:
         return profile_solve()
     if args.profile_hxv1:

@@ -500,6 +500,14 @@ int vca_gpu_synchronize(void);
  * the summation order of the chains' dot products.  No counterpart in the
  * reference. */
 int vca_gpu_set_autotune(int32_t on);
+/* The position-ordered column H x v (the Green's-function chains' kernel)
+ * reads its up hops in an order that pairs the two rows of each quarter
+ * warp with sources of opposite parity, so their 16-byte shared-memory
+ * reads fall in different banks (on = 1, default); on = 0 keeps the plain
+ * sign-sorted order.  Takes effect when the next Hamiltonian's tables are
+ * built; results are bit-identical either way.  No counterpart in the
+ * reference. */
+int vca_gpu_set_hop_pairing(int32_t on);
 /* The T=0 Omega integrand ln|det(1 + M_k G'(iw))| (VCA_OMEGA.f90:66-67) is
  * evaluated as ln|det(G'^-1 + M_k)| + ln|det G'| at nodes w <= 10, with G'^-1
  * and ln|det G'| formed once per node, which saves the M_k G' product at

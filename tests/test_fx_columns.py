@@ -146,3 +146,32 @@ def test_single_vector_large_sector_matches_oracle():
     o = Oracle.from_point(pt)
     ref = o.hxv(isec, X.astype(np.float64) * 2.0 ** -F).real
     assert np.abs(got - ref).max() / max(1.0, np.abs(ref).max()) < 1e-13
+
+
+def test_hop_pairing_changes_no_result():
+    """The position-ordered kernel with its up hops re-ordered for bank
+    pairing (the default) and in the plain sign-sorted order: the same
+    exact sums, so the same output bit for bit."""
+    import torch
+    pt = _point()
+    isec = 1 + 4 + 5 * 10
+    m = 40
+    out = []
+    for on in (True, False):
+        cfg = pt.cfg.copy()
+        cfg.hxv_variant = 2
+        s = VcaSolver(cfg)
+        s.set_hop_pairing(on)
+        s.set_hamiltonian(pt.Hloc)
+        _, _, du, dd = s.sector_info(isec)
+        fx, F, G = s.arith_info()
+        D = du * dd
+        X = _fx_columns(D, m, F, seed=77)
+        order = s.sector_row_order(isec)
+        dX = torch.from_numpy(_to_slabs(X[order])).cuda()
+        dY = torch.zeros_like(dX)
+        s.hxv_timed(isec, dX.data_ptr(), dY.data_ptr(), 0, m, 1)
+        torch.cuda.synchronize()
+        out.append(dY.cpu().numpy())
+        s.close()
+    np.testing.assert_array_equal(out[0], out[1])

@@ -8,7 +8,9 @@
 * the 2x2 plaquette at U = 8, xmu = 0.95, whose N = 3 ground level is a
   doublet in each of the sectors (2,1) and (1,2): all four states kept
   (zeta = 4), Omega equal to the oracle's arpack restatement (1e-10) and
-  0.077 away from the one-state-per-sector result;
+  away from the one-state-per-sector result (which of each doublet's
+  members one Lanczos run keeps depends on the method: 0.015 away on the
+  GPU's Lanczos, 0.077 on the oracle's dense path);
 * the same against the oracle on the Lanczos path: a complex BHZ point
   (FP64) and a real 2x3 cluster (fixed-point vectors), threshold lowered so
   the sectors near the ground state go through the reorthogonalised
@@ -86,7 +88,7 @@ def test_t0_plaquette_keeps_both_doublets():
     assert abs(om - ref) <= 1e-10 * max(1.0, abs(ref)), (om, ref)
     om1, states1, th1 = _solve(_plaquette(LANC_LANCZOS))
     assert [sec for sec, _ in states1] == [8, 12] and th1["zeta"] == 2.0
-    assert abs(om - om1) > 0.05
+    assert abs(om - om1) > 1e-3
 
 
 @pytest.mark.parametrize("case", ["bhz-f64", "square2x3-fx"])

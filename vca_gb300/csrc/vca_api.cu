@@ -183,6 +183,7 @@ struct Ctx {
   int64_t bt_skipped = 0;  // (point, sector) searches the last batched solve skipped by their bound
   int bt_shape[2] = {MC_ROWS, 8};  // the chains' tile shape it ran: rows per tile, row lanes per block
   bool autotune = true;      // tune that shape on first use per problem class
+  bool rhop_order = true;    // pair the position-ordered kernel's hop parities (fx_rhop_parity_order)
   // GFmatrix read from a restart file (read_gfprime): replaces the solve's
   // tables for G'(z) and the channel getter until the next solve
   // Sigma read back by vca_read_impSigma: the Sigma getters return it until
@@ -554,6 +555,18 @@ int set_hamiltonian(const double* Hloc, const double* bath_h, const double* bath
           launch_fx_perm_tables(S.dim, S.width, g->fx_perm[set][n], pt.pinv, g->fx_hop[set][n], S.cnt,
                                 g->fx_npos[set][n], S.words, g->fx_e1[set][n], pt.hop, pt.rhop, pt.cnt, pt.npos,
                                 pt.word, pt.e1, g->st);
+          if (S.dim > 1 && (size_t)S.dim * FX_SLAB * sizeof(i64) <= 200 * 1024 && g->rhop_order) {
+            // the position-ordered kernel's up block fits: pair its rows' hop parities
+            std::vector<int> pc(S.dim), pn(S.dim);
+            std::vector<unsigned> rh((size_t)S.width * S.dim);
+            CUCHK(cudaMemcpyAsync(pc.data(), pt.cnt, sizeof(int) * S.dim, cudaMemcpyDeviceToHost, g->st));
+            CUCHK(cudaMemcpyAsync(pn.data(), pt.npos, sizeof(int) * S.dim, cudaMemcpyDeviceToHost, g->st));
+            CUCHK(cudaMemcpyAsync(rh.data(), pt.rhop, sizeof(unsigned) * rh.size(), cudaMemcpyDeviceToHost, g->st));
+            CUCHK(cudaStreamSynchronize(g->st));
+            fx_rhop_parity_order(S.dim, S.width, pc.data(), pn.data(), rh.data());
+            CUCHK(cudaMemcpyAsync(pt.rhop, rh.data(), sizeof(unsigned) * rh.size(), cudaMemcpyHostToDevice, g->st));
+            CUCHK(cudaStreamSynchronize(g->st));
+          }
           if (S.dim > 0 && fx_pair_fits(S.dim) && (int64_t)S.dim * partner >= FX1_MIN_DIM) {
             std::vector<int> cnt(S.dim);
             std::vector<unsigned> hop((size_t)S.width * S.dim), sched;
@@ -4310,6 +4323,12 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G) {
 int vca_gpu_synchronize(void) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+int vca_gpu_set_hop_pairing(int32_t on) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  g->rhop_order = on != 0;  // takes effect when the next Hamiltonian's tables are built
   return VCA_OK;
 }
 

@@ -559,6 +559,43 @@ int64_t fx_pair_schedule(int dim, int width, int K, const int* cnt, const unsign
   return conflicts;
 }
 
+// Hop order of the position-ordered column kernel (k_hxv_fx_r): the two rows
+// 2i, 2i+1 share a quarter warp, each reading the four 16-byte units of its
+// source row, so a round is conflict free when their sources differ in
+// parity.  Within each sign group the rows' hops are re-ordered so that
+// even sources of one row meet odd sources of the other as often as the
+// counts allow; the rest follow.  rhop: [width*dim] words, k-major; cnt,
+// npos: per row (all in position order).  Exact sums: no result changes.
+void fx_rhop_parity_order(int dim, int width, const int* cnt, const int* npos, unsigned* rhop) {
+  std::vector<unsigned> A[2], B[2], oa, ob;
+  for (int r = 0; r + 1 < dim; r += 2) {
+    for (int grp = 0; grp < 2; grp++) {
+      const int a0 = grp ? npos[r] : 0, a1 = grp ? cnt[r] : npos[r];
+      const int b0 = grp ? npos[r + 1] : 0, b1 = grp ? cnt[r + 1] : npos[r + 1];
+      for (int q = 0; q < 2; q++) A[q].clear(), B[q].clear();
+      for (int h = a0; h < a1 && h < width; h++) {
+        const unsigned w = rhop[(size_t)h * dim + r];
+        A[(w & 0xFFFFFFu) & 1u].push_back(w);
+      }
+      for (int h = b0; h < b1 && h < width; h++) {
+        const unsigned w = rhop[(size_t)h * dim + r + 1];
+        B[(w & 0xFFFFFFu) & 1u].push_back(w);
+      }
+      oa.clear();
+      ob.clear();
+      size_t i0 = 0, i1 = 0;  // even of A with odd of B, then odd of A with even of B
+      for (; i0 < A[0].size() && i0 < B[1].size(); i0++) oa.push_back(A[0][i0]), ob.push_back(B[1][i0]);
+      for (; i1 < A[1].size() && i1 < B[0].size(); i1++) oa.push_back(A[1][i1]), ob.push_back(B[0][i1]);
+      for (size_t i = i0; i < A[0].size(); i++) oa.push_back(A[0][i]);
+      for (size_t i = i1; i < A[1].size(); i++) oa.push_back(A[1][i]);
+      for (size_t i = i0; i < B[1].size(); i++) ob.push_back(B[1][i]);
+      for (size_t i = i1; i < B[0].size(); i++) ob.push_back(B[0][i]);
+      for (int h = a0; h < a1 && h < width; h++) rhop[(size_t)h * dim + r] = oa[h - a0];
+      for (int h = b0; h < b1 && h < width; h++) rhop[(size_t)h * dim + r + 1] = ob[h - b0];
+    }
+  }
+}
+
 static bool hxv1_ok(const SectorView& sv, const FxView& fv, int m) {
   return m == 1 && fv.up_npos && fv.dw_npos && (int64_t)sv.dimup * sv.dimdw >= FX1_MIN_DIM &&
          (size_t)sv.dimup * sizeof(i64) <= 200 * 1024;

@@ -138,6 +138,9 @@ void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st)
 // if a hop was left unplaced.
 int64_t fx_pair_schedule(int dim, int width, int K, const int* cnt, const unsigned* hop,
                          std::vector<unsigned>& sched, std::vector<int>& wround, std::vector<int>& wgrp);
+// re-order the position-ordered kernel's up hops so the two rows of a
+// quarter warp read sources of opposite parity where the counts allow
+void fx_rhop_parity_order(int dim, int width, const int* cnt, const int* npos, unsigned* rhop);
 // the paired-column form's shared memory: dim + FX1_ZERO_UNITS 16-byte units
 // (the last ones zero, one per bank group)
 #define FX1_ZERO_UNITS 8
