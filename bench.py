@@ -753,6 +753,33 @@ def profile_mlp(steps: int) -> int:
     return 0
 
 
+def chain_streams_ab(reps: int) -> dict:
+    """The benchmark solve (point M = 0.1) with the chains' column groups one
+    after another (1 stream) and two at a time (2 streams): seconds per
+    solve, the chain stage, and whether Omega agrees bit for bit."""
+    from vca_gb300.solver import VcaSolver
+    pt = build_points()[5]
+    out = {"workload": WORKLOAD, "point": "M = 0.1", "reps": reps}
+    oms = []
+    for n in (1, 2, 1, 2):
+        cfg = pt.cfg.copy()
+        cfg.hxv_variant = 2
+        s = VcaSolver(cfg)
+        s.set_chain_streams(n)
+        s.upload_hk(pt.Hk)
+        s.solve_resident(pt.Hloc)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            om = s.solve_resident(pt.Hloc)
+        dt = (time.perf_counter() - t0) / reps
+        st = s.timings()
+        s.close()
+        oms.append(om)
+        out.setdefault(f"streams_{n}", []).append({"s_per_solve": round(dt, 4), "chains_s": round(st[2] / 1e3, 4)})
+    out["omega_bit_identical"] = len(set(oms)) == 1
+    return out
+
+
 def profile_solve() -> int:
     """One warm-up and one timed plain solve of a reduced 4x3 point."""
     from vca_gb300 import build as vbuild, clusters
@@ -799,6 +826,8 @@ def main():
                     help="--profile-hxv with the chains' kernel's plain hop order")
     ap.add_argument("--profile-hxv-c5", type=int, default=0, metavar="NCOLS",
                     help="time a NCOLS-column H x v on a chain sector of the 4x4 cluster, both forms")
+    ap.add_argument("--chain-streams-ab", action="store_true",
+                    help="the benchmark solve with one and with two chain streams, --reps solves each")
     ap.add_argument("--c5-solve", action="store_true",
                     help="one plain solve of the 4x4 cluster (C5), timed by stage")
     ap.add_argument("--c5-steps", type=int, default=200, help="chain steps of --c5-solve")
@@ -815,6 +844,11 @@ def main():
         from vca_gb300 import build as vbuild
         vbuild.build()
         print(json.dumps(hxv_single_4x4(args.reps)))
+        return 0
+    if args.chain_streams_ab:
+        from vca_gb300 import build as vbuild
+        vbuild.build()
+        print(json.dumps(chain_streams_ab(args.reps)))
         return 0
     if args.profile_hxv_c5:
         from vca_gb300 import build as vbuild

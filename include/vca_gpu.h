@@ -508,6 +508,14 @@ int vca_gpu_set_autotune(int32_t on);
  * built; results are bit-identical either way.  No counterpart in the
  * reference. */
 int vca_gpu_set_hop_pairing(int32_t on);
+/* The Green's-function chains run as column groups; n = 1 (default) runs
+ * one group after another, n = 2 keeps two groups in flight on two
+ * streams with their Lanczos steps interleaved, so that one group's H x v
+ * could overlap the other's element passes (each group then gets a quarter
+ * of the free memory instead of half).  On the 4x3 benchmark solve two
+ * streams are 1 % slower: the chains' H x v fills every SM.  Results are
+ * bit-identical either way.  No counterpart in the reference. */
+int vca_gpu_set_chain_streams(int32_t n);
 /* The T=0 Omega integrand ln|det(1 + M_k G'(iw))| (VCA_OMEGA.f90:66-67) is
  * evaluated as ln|det(G'^-1 + M_k)| + ln|det G'| at nodes w <= 10, with G'^-1
  * and ln|det G'| formed once per node, which saves the M_k G' product at

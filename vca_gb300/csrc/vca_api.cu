@@ -184,6 +184,8 @@ struct Ctx {
   int bt_shape[2] = {MC_ROWS, 8};  // the chains' tile shape it ran: rows per tile, row lanes per block
   bool autotune = true;      // tune that shape on first use per problem class
   bool rhop_order = true;    // pair the position-ordered kernel's hop parities (fx_rhop_parity_order)
+  int chain_streams = 1;     // chain column groups in flight at a time (their own streams)
+  cudaStream_t st2 = nullptr;  // the second group's stream
   // GFmatrix read from a restart file (read_gfprime): replaces the solve's
   // tables for G'(z) and the channel getter until the next solve
   // Sigma read back by vca_read_impSigma: the Sigma getters return it until
@@ -630,8 +632,9 @@ struct BatchBufs {
   int64_t wpart_rows;
 };
 
-int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k, double tol, int ldab) {
-  cudaStream_t st = g->st;
+int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k, double tol, int ldab,
+                 cudaStream_t stream = nullptr) {
+  cudaStream_t st = stream ? stream : g->st;
   void* X = bb.b[0];
   void* Xp = bb.b[1];
   void* Y = bb.b[2];
@@ -658,8 +661,8 @@ int lanczos_step(const SectorView& sv, const ColBatch& cb, BatchBufs& bb, int k,
 // One Lanczos step in fixed point: X (2^-F) -> W = H X - a X - b Xp (2^-G)
 // -> X_next = W / beta (2^-F).  Buffers rotate as (X, Xp, YW) <- (new, X, YW).
 int lanczos_step_fx(const SectorView& sv, const FxView& fv, const ColBatch& cb, BatchBufs& bb, int k,
-                    double tol, int ldab) {
-  cudaStream_t st = g->st;
+                    double tol, int ldab, cudaStream_t stream = nullptr) {
+  cudaStream_t st = stream ? stream : g->st;
   const FxScales& fs = g->fxs;
   i64* X = (i64*)bb.b[0];
   i64* Xp = (i64*)bb.b[1];
@@ -1548,125 +1551,200 @@ double state_weight(const GState& S) {
 
 double now_ms();
 
-int run_chain_batch(int state, int spin, bool dag, std::vector<ChainSpec>& specs) {
+// One column batch of Green's-function chains: the chains of one (state,
+// spin, particle|hole) target sector whose columns fit, on its own stream.
+struct ChainGroup {
+  int state = 0, spin = 0;
+  bool dag = false;
+  std::vector<ChainSpec>* specs = nullptr;
+  size_t q0 = 0, q1 = 0;
+  int tup = 0, tdw = 0, m = 0, nch = 0, nlanc = 0;
+  int64_t D = 0;
+  bool swap = false;
+  SectorView tv{}, hv{};
+  FxView hf{};
+  Arena ar;
+  BatchBufs bb{};
+  double *norm2c = nullptr, *norm2 = nullptr, *invn = nullptr;
+  ChainInit* d_ci = nullptr;
+  int* d_isign = nullptr;
+  double2* d_wfac = nullptr;
+  ColBatch cb{};
+  cudaStream_t st = nullptr;
+};
+
+// Cut the chains of one (state, spin, particle|hole) list into column groups
+// whose three column buffers fit 1/npar of half the free device memory (npar
+// groups run at a time).
+int chain_groups(int state, int spin, bool dag, std::vector<ChainSpec>& specs, int npar,
+                 std::vector<ChainGroup>& out) {
   const vca_config& c = g->cfg;
   const GState& S = g->gs[state];
   const int nup = sec_nup(S.sector), ndw = sec_ndw(S.sector);
   const int tup = nup + (spin == 0 ? (dag ? 1 : -1) : 0);
   const int tdw = ndw + (spin == 1 ? (dag ? 1 : -1) : 0);
   if (tup < 0 || tup > g->Ns || tdw < 0 || tdw > g->Ns) return VCA_OK;  // no target sector
-  SectorView tv = view_of(tup, tdw);
+  const SectorView tv = view_of(tup, tdw);
   const int64_t D = (int64_t)tv.dimup * tv.dimdw;
   const bool cplx = !g->real_model;
-  const int nlanc = (int)std::min<int64_t>(D, c.lanc_ngfiter);
   const size_t es = cplx ? sizeof(double2) : sizeof(double);
-  // memory budget: three column buffers per batch
   size_t freeb = 0, totb = 0;
   CUCHK(cudaMemGetInfo(&freeb, &totb));
-  const size_t budget = (size_t)(0.5 * (double)freeb);
+  const size_t budget = (size_t)(0.5 * (double)freeb / std::max(1, npar));
   int64_t maxcols = (int64_t)(budget / (3 * (size_t)D * es + 1));
   if (g->fx && maxcols > FX_SLAB) maxcols = maxcols / FX_SLAB * FX_SLAB;  // room for the pad columns
   if (maxcols < 2) VFAIL(VCA_ERR_ALLOC, "not enough device memory for one Green's function chain");
   size_t q0 = 0;
   while (q0 < specs.size()) {
-    // group of chains whose columns fit
     size_t q1 = q0;
     int m = 0;
     while (q1 < specs.size() && m + specs[q1].ncol <= maxcols) { m += specs[q1].ncol; q1++; }
-    const int nch = (int)(q1 - q0);
-    Arena ar;
-    BatchBufs bb;
-    int rc = alloc_batch(ar, D, m, cplx, nch, g->ld, bb);
-    // fixed-point batches hold the smaller spin block first (see view_pair),
-    // its rows in hop-count order where the position-ordered H x v applies
-    const bool swap = g->fx && tv.dimup > tv.dimdw;
-    const SectorView hv = swap ? view_pair(g->dwset, tdw, 0, tup) : tv;
-    FxView hf{};
-    if (g->fx) {
-      hf = swap ? fx_view_pair(g->dwset, tdw, 0, tup) : fx_view_of(tup, tdw);
-      hf.rows_permuted = (g->cfg.hxv_variant != 1 && hxv_fx_r_ok(hv, hf, m)) ? 1 : 0;
-    }
-    if (!rc && g->fx) {
-      const int rbw = hxv_fx_cols_rows(hv, hf, m, g->cfg.hxv_variant == 1);
-      rc = ar.alloc(&bb.wpart, 2 * (size_t)rbw * m);
-      bb.wpart_rows = rbw;
-    }
-    double *norm2c, *norm2, *invn;
-    ChainInit* d_ci;
-    int* d_isign;
-    double2* d_wfac;
-    if (!rc) rc = ar.alloc(&norm2c, m);
-    if (!rc) rc = ar.alloc(&norm2, nch);
-    if (!rc) rc = ar.alloc(&invn, nch);
-    if (!rc) rc = ar.alloc(&d_ci, nch);
-    if (!rc) rc = ar.alloc(&d_isign, nch);
-    if (!rc) rc = ar.alloc(&d_wfac, nch);
-    if (rc) { ar.release(); return rc; }
-    std::vector<ChainMeta> meta(nch);
-    std::vector<int> col2ch(m);
-    std::vector<ChainInit> ci(nch);
-    std::vector<int> isg(nch);
-    std::vector<double2> wf(nch);
-    int col = 0;
-    for (int q = 0; q < nch; q++) {
-      ChainSpec& sp = specs[q0 + q];
-      sp.ci.col0 = col;
-      ci[q] = sp.ci;
-      meta[q] = ChainMeta{sp.ncol, col, nlanc, 1, 0};
-      for (int t = 0; t < sp.ncol; t++) col2ch[col + t] = q;
-      col += sp.ncol;
-      isg[q] = sp.isign;
-      wf[q] = make_double2(sp.wfac.real(), sp.wfac.imag());
-    }
-    cudaMemcpyAsync(bb.meta, meta.data(), sizeof(ChainMeta) * nch, cudaMemcpyHostToDevice, g->st);
-    cudaMemcpyAsync(bb.col2ch, col2ch.data(), sizeof(int) * m, cudaMemcpyHostToDevice, g->st);
-    cudaMemcpyAsync(d_ci, ci.data(), sizeof(ChainInit) * nch, cudaMemcpyHostToDevice, g->st);
-    cudaMemcpyAsync(d_isign, isg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, g->st);
-    cudaMemcpyAsync(d_wfac, wf.data(), sizeof(double2) * nch, cudaMemcpyHostToDevice, g->st);
-    ColBatch cb{D, m, cplx, nch, bb.col2ch, bb.meta};
-    CUCHK(cudaStreamSynchronize(g->st));
+    ChainGroup G;
+    G.state = state;
+    G.spin = spin;
+    G.dag = dag;
+    G.specs = &specs;
+    G.q0 = q0;
+    G.q1 = q1;
+    G.tup = tup;
+    G.tdw = tdw;
+    G.m = m;
+    G.nch = (int)(q1 - q0);
+    G.D = D;
+    G.nlanc = (int)std::min<int64_t>(D, c.lanc_ngfiter);
+    G.tv = tv;
+    out.push_back(G);
+    q0 = q1;
+  }
+  return VCA_OK;
+}
+
+// allocations, tables and the normalised start vectors of a group, on G.st
+int chain_group_prepare(ChainGroup& G) {
+  const GState& S = g->gs[G.state];
+  const int nup = sec_nup(S.sector);
+  const bool cplx = !g->real_model;
+  const int m = G.m, nch = G.nch;
+  int rc = alloc_batch(G.ar, G.D, m, cplx, nch, g->ld, G.bb);
+  BatchBufs& bb = G.bb;
+  // fixed-point batches hold the smaller spin block first (see view_pair),
+  // its rows in hop-count order where the position-ordered H x v applies
+  G.swap = g->fx && G.tv.dimup > G.tv.dimdw;
+  G.hv = G.swap ? view_pair(g->dwset, G.tdw, 0, G.tup) : G.tv;
+  if (g->fx) {
+    G.hf = G.swap ? fx_view_pair(g->dwset, G.tdw, 0, G.tup) : fx_view_of(G.tup, G.tdw);
+    G.hf.rows_permuted = (g->cfg.hxv_variant != 1 && hxv_fx_r_ok(G.hv, G.hf, m)) ? 1 : 0;
+  }
+  if (!rc && g->fx) {
+    const int rbw = hxv_fx_cols_rows(G.hv, G.hf, m, g->cfg.hxv_variant == 1);
+    rc = G.ar.alloc(&bb.wpart, 2 * (size_t)rbw * m);
+    bb.wpart_rows = rbw;
+  }
+  if (!rc) rc = G.ar.alloc(&G.norm2c, m);
+  if (!rc) rc = G.ar.alloc(&G.norm2, nch);
+  if (!rc) rc = G.ar.alloc(&G.invn, nch);
+  if (!rc) rc = G.ar.alloc(&G.d_ci, nch);
+  if (!rc) rc = G.ar.alloc(&G.d_isign, nch);
+  if (!rc) rc = G.ar.alloc(&G.d_wfac, nch);
+  if (rc) return rc;
+  std::vector<ChainMeta> meta(nch);
+  std::vector<int> col2ch(m);
+  std::vector<ChainInit> ci(nch);
+  std::vector<int> isg(nch);
+  std::vector<double2> wf(nch);
+  int col = 0;
+  for (int q = 0; q < nch; q++) {
+    ChainSpec& sp = (*G.specs)[G.q0 + q];
+    sp.ci.col0 = col;
+    ci[q] = sp.ci;
+    meta[q] = ChainMeta{sp.ncol, col, G.nlanc, 1, 0};
+    for (int t = 0; t < sp.ncol; t++) col2ch[col + t] = q;
+    col += sp.ncol;
+    isg[q] = sp.isign;
+    wf[q] = make_double2(sp.wfac.real(), sp.wfac.imag());
+  }
+  cudaStream_t st = G.st;
+  CUCHK(cudaMemcpyAsync(bb.meta, meta.data(), sizeof(ChainMeta) * nch, cudaMemcpyHostToDevice, st));
+  CUCHK(cudaMemcpyAsync(bb.col2ch, col2ch.data(), sizeof(int) * m, cudaMemcpyHostToDevice, st));
+  CUCHK(cudaMemcpyAsync(G.d_ci, ci.data(), sizeof(ChainInit) * nch, cudaMemcpyHostToDevice, st));
+  CUCHK(cudaMemcpyAsync(G.d_isign, isg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
+  CUCHK(cudaMemcpyAsync(G.d_wfac, wf.data(), sizeof(double2) * nch, cudaMemcpyHostToDevice, st));
+  G.cb = ColBatch{G.D, m, cplx, nch, bb.col2ch, bb.meta};
+  const ColBatch& cb = G.cb;
+  // start vectors: gather from the ground state, normalise per chain
+  if (g->fx) {
+    const FxScales& fs = g->fxs;
+    launch_chain_init_fx(G.tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, G.d_ci, m, G.swap,
+                         G.hf.rows_permuted ? G.hf.up_pinv : nullptr, (i64*)bb.b[0], st);
+    launch_fx_dot(cb, (i64*)bb.b[0], (i64*)bb.b[0], fs.F, fs.F, (i64*)bb.partial, bb.nblk, G.norm2c, st);
+    launch_chain_sum(cb, G.norm2c, G.norm2, st);
+    launch_chain_norm_init(nch, bb.meta, G.norm2, G.invn, st);
+    launch_fx_rescale(cb, G.invn, fs.F, fs.F, (i64*)bb.b[0], (i64*)bb.b[0], bb.scr, st);
+  } else {
+    launch_chain_init(G.tv, g->sp[0][nup].dim, S.vec, cplx, nch, G.d_ci, m, cplx, bb.b[0], st);
+    launch_col_dot(cb, bb.b[0], bb.b[0], bb.partial, bb.nblk, G.norm2c, st);
+    launch_chain_sum(cb, G.norm2c, G.norm2, st);
+    launch_chain_norm_init(nch, bb.meta, G.norm2, G.invn, st);
+    launch_col_scale(cb, G.invn, bb.b[0], bb.b[0], st);
+  }
+  CUCHK(cudaGetLastError());
+  return VCA_OK;
+}
+
+int chain_group_step(ChainGroup& G, int k) {
+  const vca_config& c = g->cfg;
+  if (g->fx) return lanczos_step_fx(G.hv, G.hf, G.cb, G.bb, k, c.gf_beta_tol, g->ld, G.st);
+  return lanczos_step(G.tv, G.cb, G.bb, k, c.gf_beta_tol, g->ld, G.st);
+}
+
+// poles and weights into the global chain table, after every earlier group
+int chain_group_finish(ChainGroup& G) {
+  const GState& S = g->gs[G.state];
+  const int base = (int)g->chains.size();
+  launch_chain_store(G.nch, G.bb.meta, G.bb.A, G.bb.Bt, g->ld, G.norm2, G.d_wfac, G.d_isign, S.e, state_weight(S),
+                     g->zeta, g->cstore, base, G.st);
+  CUCHK(cudaGetLastError());
+  CUCHK(cudaStreamSynchronize(G.st));
+  for (int q = 0; q < G.nch; q++) {
+    g->chains.push_back((*G.specs)[G.q0 + q].rec);
+    g->chains.back().nlanc = G.nlanc;
+  }
+  G.ar.release();
+  return VCA_OK;
+}
+
+// The groups npar at a time, each on its own stream, their steps
+// interleaved so one group's H x v overlaps the other's element passes;
+// every group computes exactly what it computes alone.
+int run_chain_groups(std::vector<ChainGroup>& groups, int npar) {
+  CUCHK(cudaStreamSynchronize(g->st));  // ground states and the chain store are in place
+  cudaStream_t streams[2] = {g->st, g->st2};
+  for (size_t i = 0; i < groups.size(); i += (size_t)npar) {
+    const size_t j1 = std::min(groups.size(), i + (size_t)npar);
+    auto release = [&]() { for (size_t j = i; j < j1; j++) groups[j].ar.release(); };
     const double tb0 = now_ms();
-    double tb1 = tb0;
-    // start vectors: gather from the ground state, normalise per chain
-    if (g->fx) {
-      const FxScales& fs = g->fxs;
-      const FxView& fv = hf;
-      launch_chain_init_fx(tv, g->sp[0][nup].dim, (const i64*)S.vec, nch, d_ci, m, swap,
-                           fv.rows_permuted ? fv.up_pinv : nullptr, (i64*)bb.b[0], g->st);
-      launch_fx_dot(cb, (i64*)bb.b[0], (i64*)bb.b[0], fs.F, fs.F, (i64*)bb.partial, bb.nblk, norm2c, g->st);
-      launch_chain_sum(cb, norm2c, norm2, g->st);
-      launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
-      launch_fx_rescale(cb, invn, fs.F, fs.F, (i64*)bb.b[0], (i64*)bb.b[0], bb.scr, g->st);
-      CUCHK(cudaStreamSynchronize(g->st));
-      tb1 = now_ms();
-      for (int k = 1; k <= nlanc; k++)
-        if ((rc = lanczos_step_fx(hv, fv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
-    } else {
-      launch_chain_init(tv, g->sp[0][nup].dim, S.vec, cplx, nch, d_ci, m, cplx, bb.b[0], g->st);
-      launch_col_dot(cb, bb.b[0], bb.b[0], bb.partial, bb.nblk, norm2c, g->st);
-      launch_chain_sum(cb, norm2c, norm2, g->st);
-      launch_chain_norm_init(nch, bb.meta, norm2, invn, g->st);
-      launch_col_scale(cb, invn, bb.b[0], bb.b[0], g->st);
-      CUCHK(cudaStreamSynchronize(g->st));
-      tb1 = now_ms();
-      for (int k = 1; k <= nlanc; k++)
-        if ((rc = lanczos_step(tv, cb, bb, k, c.gf_beta_tol, g->ld))) { ar.release(); return rc; }
+    int kmax = 0;
+    for (size_t j = i; j < j1; j++) {
+      groups[j].st = streams[(j - i) % 2];
+      const int rc = chain_group_prepare(groups[j]);
+      if (rc) { release(); return rc; }
+      kmax = std::max(kmax, groups[j].nlanc);
     }
-    // poles and weights into the global chain table
-    const int base = (int)g->chains.size();
-    launch_chain_store(nch, bb.meta, bb.A, bb.Bt, g->ld, norm2, d_wfac, d_isign, S.e, state_weight(S), g->zeta,
-                       g->cstore, base, g->st);
-    CUCHK(cudaGetLastError());
-    CUCHK(cudaStreamSynchronize(g->st));
+    for (size_t j = i; j < j1; j++) CUCHK(cudaStreamSynchronize(groups[j].st));
+    const double tb1 = now_ms();
+    for (int k = 1; k <= kmax; k++)
+      for (size_t j = i; j < j1; j++)
+        if (k <= groups[j].nlanc) {
+          const int rc = chain_group_step(groups[j], k);
+          if (rc) { release(); return rc; }
+        }
+    for (size_t j = i; j < j1; j++) {
+      const int rc = chain_group_finish(groups[j]);
+      if (rc) { release(); return rc; }
+    }
     g->chain_ms[0] += tb1 - tb0;
     g->chain_ms[1] += now_ms() - tb1;
-    g->chain_ms[2] += 1.0;
-    for (int q = 0; q < nch; q++) {
-      g->chains.push_back(specs[q0 + q].rec);
-      g->chains.back().nlanc = nlanc;
-    }
-    ar.release();
-    q0 = q1;
+    g->chain_ms[2] += (double)(j1 - i);
   }
   return VCA_OK;
 }
@@ -1702,9 +1780,16 @@ int build_gf() {
   CUCHK(cudaMemsetAsync(cs.n, 0, sizeof(int) * nmax, g->st));
   const bool cplx = !g->real_model;
   const cd XI(0.0, 1.0);
+  const int npar = std::max(1, std::min(2, g->chain_streams));
+  std::vector<std::vector<ChainSpec>> speclists;
+  speclists.reserve(2 * g->gs.size() * (size_t)c.Nspin);  // the groups point into them
+  std::vector<ChainGroup> groups;
   for (int k = 0; k < (int)g->gs.size(); k++)
     for (int is = 0; is < c.Nspin; is++) {
-      std::vector<ChainSpec> part, hole;
+      speclists.emplace_back();
+      std::vector<ChainSpec>& part = speclists.back();
+      speclists.emplace_back();
+      std::vector<ChainSpec>& hole = speclists.back();
       auto add = [&](std::vector<ChainSpec>& v, int dag, int e, int chan, int p, cd cp, int q, cd cq,
                      int nterm, cd wfac) {
         ChainSpec s{};
@@ -1740,9 +1825,10 @@ int build_gf() {
               }
             }
         }
-      RCHK(run_chain_batch(k, is, true, part));
-      RCHK(run_chain_batch(k, is, false, hole));
+      RCHK(chain_groups(k, is, true, part, npar, groups));
+      RCHK(chain_groups(k, is, false, hole, npar, groups));
     }
+  RCHK(run_chain_groups(groups, npar));
   // element -> chains CSR
   g->nelem = c.Nlat * c.Nlat * c.Nspin * c.Norb * c.Norb;
   std::vector<std::vector<int>> lists(g->nelem);
@@ -3426,6 +3512,7 @@ int vca_gpu_finalize(void) {
   g->ham.release();
   g->basis.release();
   if (g->st) cudaStreamDestroy(g->st);
+  if (g->st2) cudaStreamDestroy(g->st2);
   delete g;
   g = nullptr;
   return VCA_OK;
@@ -3485,6 +3572,7 @@ int vca_gpu_init(const vca_config* cfg, const double* bath_h, const double* bath
   }
   // a blocking stream: the synchronous getters on the legacy stream order after it
   CUCHK(cudaStreamCreate(&g->st));
+  CUCHK(cudaStreamCreate(&g->st2));
   set_binomials(Ns, g->st);
   g->dimn.resize(Ns + 1);
   g->words.resize(Ns + 1);
@@ -4323,6 +4411,13 @@ int vca_gpu_arith_info(int32_t* fx, int32_t* F, int32_t* G) {
 int vca_gpu_synchronize(void) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   CUCHK(cudaStreamSynchronize(g->st));
+  return VCA_OK;
+}
+
+int vca_gpu_set_chain_streams(int32_t n) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (n < 1 || n > 2) VFAIL(VCA_ERR_ARG, "1 or 2 chain streams");
+  g->chain_streams = n;
   return VCA_OK;
 }
 
