@@ -516,6 +516,14 @@ int vca_gpu_set_hop_pairing(int32_t on);
  * streams are 1 % slower: the chains' H x v fills every SM.  Results are
  * bit-identical either way.  No counterpart in the reference. */
 int vca_gpu_set_chain_streams(int32_t n);
+/* Test hook of the bounded waits in the chains' column H x v: its own-block
+ * bulk copy (cp.async.bulk, mbarrier completion) is awaited for at most one
+ * second; with bytes > 0 the barrier expects that many bytes more than are
+ * copied, so the wait runs out (no fault), the kernel returns early, and
+ * the call that ran it (vca_gpu_solve, vca_gpu_hxv_timed) returns
+ * VCA_ERR_TIMEOUT.  bytes = 0 (default) restores normal operation.  No
+ * counterpart in the reference. */
+int vca_gpu_set_stage_extra_tx(int32_t bytes);
 /* The T=0 Omega integrand ln|det(1 + M_k G'(iw))| (VCA_OMEGA.f90:66-67) is
  * evaluated as ln|det(G'^-1 + M_k)| + ln|det G'| at nodes w <= 10, with G'^-1
  * and ln|det G'| formed once per node, which saves the M_k G' product at

@@ -2445,6 +2445,8 @@ int solve_resident(const double* Hloc, const double* bath_h, const double* bath_
   RCHK(diagonalize());
   double t2 = now_ms();
   RCHK(build_gf());
+  if (g->fx && fx_take_wait_failures() != 0)
+    VFAIL(VCA_ERR_TIMEOUT, "a bounded wait for a bulk copy in the column H x v ran out");
   double t3 = now_ms();
   RCHK(g->finiteT ? omega_integral_finite_t(&g->omega_int) : omega_integral(&g->omega_int));
   double t4 = now_ms();
@@ -4222,6 +4224,7 @@ static int hxv_cols(int32_t isector, const void* d_v, void* d_hv, int32_t is_com
   const int nup = sec_nup(isector), ndw = sec_ndw(isector);
   SectorView sv = view_of(nup, ndw);
   const int m = (is_complex && g->real_model) ? 2 * ncols : ncols;
+  if ((((uintptr_t)d_v) | ((uintptr_t)d_hv)) & 15u) VFAIL(VCA_ERR_ARG, "device vectors must be 16-byte aligned");
   if (g->fx) {  // slab-major fixed-point columns (scale 2^-F, unit norm)
     if (m >= FX_SLAB && m % FX_SLAB)
       VFAIL(VCA_ERR_ARG, "fixed-point column batches of 8 or more columns need a multiple of 8 columns");
@@ -4314,7 +4317,16 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
   cudaEventDestroy(e1);
   CUCHK(cudaStreamSynchronize(g->st));
   ar.release();
+  if (g->fx && fx_take_wait_failures() != 0)
+    VFAIL(VCA_ERR_TIMEOUT, "a bounded wait for a bulk copy in the column H x v ran out");
   *ms_per_call = ms / reps;
+  return VCA_OK;
+}
+
+int vca_gpu_set_stage_extra_tx(int32_t bytes) {
+  if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
+  if (bytes < 0 || bytes > (1 << 16) || bytes % 16) VFAIL(VCA_ERR_ARG, "0..65536 bytes, a multiple of 16");
+  if (fx_set_stage_extra_tx(bytes) != 0) VFAIL(VCA_ERR_CUDA, "cannot set the test hook");
   return VCA_OK;
 }
 

@@ -1493,6 +1493,45 @@ __global__ void __launch_bounds__(512, 2) k_hxv_fx_s(SectorView sv, FxView fv, i
 // Only the own-block copy needs a barrier; shared memory is one block
 // (DimUp*64 bytes), so four CTAs share an SM on the 4x3 chain sectors.
 #define FXR_THREADS 256
+
+// ---- bulk copy of the own block (cp.async.bulk, mbarrier completion) ----
+// A bounded wait that runs out adds 1 to g_fx_wait_fail, which the solve and
+// the timed H x v turn into VCA_ERR_TIMEOUT; g_fx_stage_extra_tx (a test
+// hook, 0 otherwise) raises the bytes the barrier expects above those
+// copied, so that the wait runs out without any fault.
+__device__ int g_fx_wait_fail = 0;
+__device__ int g_fx_stage_extra_tx = 0;
+#define FXB_WAIT_NS 1000000000ull
+__device__ __forceinline__ uint64_t fxb_time() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool fxb_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ bool fxb_wait_bounded(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = fxb_time();
+  while (!fxb_try_wait(bar, parity))
+    if (fxb_time() - t0 > FXB_WAIT_NS) return false;
+  return true;
+}
+// thread 0: init the barrier, expect the bytes, start the copy
+__device__ __forceinline__ void fxb_start(uint32_t bar, uint32_t dst, const void* src, uint32_t bytes) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1u) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const uint32_t expect = bytes + (uint32_t)g_fx_stage_extra_tx;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(expect) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
 template <int K, bool SH63, bool APART>
 __global__ void __launch_bounds__(FXR_THREADS, 4) k_hxv_fx_r(SectorView sv, FxView fv, int m,
                                                               const i64* __restrict__ X, i64* __restrict__ Y,
@@ -1502,7 +1541,8 @@ __global__ void __launch_bounds__(FXR_THREADS, 4) k_hxv_fx_r(SectorView sv, FxVi
   const int DU = sv.dimup, DD = sv.dimdw;
   const int64_t D = (int64_t)DU * DD;
   longlong2* xs2 = (longlong2*)fxr_smem;                // [DU][4] own block, position order
-  int* doff = (int*)(xs2 + (size_t)DU * 4);            // down hops: offsets in 16-byte units
+  unsigned long long* sbar = (unsigned long long*)(xs2 + (size_t)DU * 4);  // its copy's mbarrier (16-byte slot)
+  int* doff = (int*)(sbar + 2);                        // down hops: offsets in 16-byte units
   unsigned char* dcl = (unsigned char*)(doff + sv.wdw);
   const int cs = blockIdx.x / DD;
   const int idw = blockIdx.x - cs * DD;
@@ -1512,13 +1552,29 @@ __global__ void __launch_bounds__(FXR_THREADS, 4) k_hxv_fx_r(SectorView sv, FxVi
   longlong2* yown = (longlong2*)Y + (int64_t)cs * D * (W / 2) + rowbase * 4;
   const int nd = sv.dw_cnt[idw];
   const int ndp = fv.dw_npos[idw];
+  // the own block (DU x 64 contiguous bytes) by one bulk copy, the down-hop
+  // table meanwhile; thread 0 waits (bounded) and the CTA follows its verdict
+  __shared__ int stage_ok;
+  const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(sbar);
+  if (threadIdx.x == 0)
+    fxb_start(bar_s, (uint32_t)__cvta_generic_to_shared(xs2), own, (uint32_t)DU * 64u);
   for (int h = threadIdx.x; h < nd; h += blockDim.x) {
     const unsigned hw = fv.dw_hop[idw + h * DD];
     doff[h] = ((int)(hw & 0xFFFFFFu) - idw) * DU * 4;  // neighbour block relative to own (|.| < D*4 < 2^31)
     dcl[h] = (unsigned char)((hw >> 24) & 3u);
   }
-  for (int t = threadIdx.x; t < DU * 4; t += blockDim.x) xs2[t] = __ldcg(own + t);
+  if (threadIdx.x == 0) {
+    const bool ok = fxb_wait_bounded(bar_s, 0);
+    if (!ok) {
+      atomicAdd(&g_fx_wait_fail, 1);
+      fxb_wait_bounded(bar_s, 0);  // the copy's bytes in flight, again bounded
+    }
+    stage_ok = ok ? 1 : 0;
+  }
   __syncthreads();
+  if (!stage_ok) return;  // uniform: no later barrier is reached by part of the CTA
+  for (int it = 0; it < (1 << 16) && !fxb_try_wait(bar_s, 0); it++) {
+  }  // the phase is complete: this thread's acquire of the copied bytes
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int u = lane & 3, rsub = lane >> 2;
   const i64 e1d = fv.dw_e1[idw];
@@ -1631,7 +1687,20 @@ __global__ void __launch_bounds__(FXR_THREADS, 4) k_hxv_fx_r(SectorView sv, FxVi
 
 #define FXR_SMEM_MAX (200 * 1024)
 static size_t hxv_fx_r_smem(const SectorView& sv) {
-  return (size_t)sv.dimup * FX_SLAB * sizeof(i64) + (size_t)sv.wdw * 5 + 16;
+  return (size_t)sv.dimup * FX_SLAB * sizeof(i64) + 16 + (size_t)sv.wdw * 5 + 16;
+}
+
+int fx_take_wait_failures() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_fx_wait_fail, sizeof(int)) != cudaSuccess) return -1;
+  if (v) {
+    const int z = 0;
+    cudaMemcpyToSymbol(g_fx_wait_fail, &z, sizeof(int));
+  }
+  return v;
+}
+int fx_set_stage_extra_tx(int bytes) {
+  return cudaMemcpyToSymbol(g_fx_stage_extra_tx, &bytes, sizeof(int)) == cudaSuccess ? 0 : -1;
 }
 
 bool hxv_fx_r_ok(const SectorView& sv, const FxView& fv, int m) {

@@ -138,6 +138,12 @@ void launch_fx_e1(int dim, const double2* e1, int A, i64* e1fx, cudaStream_t st)
 // if a hop was left unplaced.
 int64_t fx_pair_schedule(int dim, int width, int K, const int* cnt, const unsigned* hop,
                          std::vector<unsigned>& sched, std::vector<int>& wround, std::vector<int>& wgrp);
+// bounded waits of the position-ordered kernel's bulk copies that ran out
+// since the last call (the count is reset), -1 if it cannot be read
+int fx_take_wait_failures();
+// test hook: bytes the position-ordered kernel's copy barrier expects beyond
+// those it copies (0: none), so that its bounded wait runs out
+int fx_set_stage_extra_tx(int bytes);
 // re-order the position-ordered kernel's up hops so the two rows of a
 // quarter warp read sources of opposite parity where the counts allow
 void fx_rhop_parity_order(int dim, int width, const int* cnt, const int* npos, unsigned* rhop);

@@ -38,7 +38,7 @@ EXPORTS = [
     "vca_gpu_get_docc", "vca_gpu_get_mag",
     "vca_gpu_hxv_timed", "vca_gpu_hxv_alpha_noalloc", "vca_gpu_sector_row_order", "vca_gpu_upload_hk", "vca_gpu_solve_resident", "vca_gpu_kernel_launches",
     "vca_gpu_get_timings", "vca_gpu_synchronize", "vca_gpu_set_ql_max_iter", "vca_gpu_sector_bounds",
-    "vca_gpu_set_omega_inverse_form", "vca_gpu_set_autotune", "vca_gpu_set_hop_pairing", "vca_gpu_set_chain_streams",
+    "vca_gpu_set_omega_inverse_form", "vca_gpu_set_autotune", "vca_gpu_set_hop_pairing", "vca_gpu_set_chain_streams", "vca_gpu_set_stage_extra_tx",
     "vca_gpu_timer_start",
     "vca_gpu_timer_stop",
     "vca_gpu_arith_info", "vca_gpu_sum_kmesh_complex", "vca_gpu_get_thermal", "vca_gpu_custom_observable",
@@ -139,6 +139,7 @@ def load(path: Optional[str] = None):
         "vca_gpu_set_autotune": (ctypes.c_int, [i32]),
         "vca_gpu_set_hop_pairing": (ctypes.c_int, [i32]),
         "vca_gpu_set_chain_streams": (ctypes.c_int, [i32]),
+        "vca_gpu_set_stage_extra_tx": (ctypes.c_int, [i32]),
         "vca_gpu_timer_start": (ctypes.c_int, []),
         "vca_gpu_timer_stop": (ctypes.c_int, [dp]),
         "vca_gpu_arith_info": (ctypes.c_int, [ctypes.POINTER(i32)] * 3),
@@ -328,6 +329,10 @@ class VcaSolver:
     def set_autotune(self, on: bool):
         """Tune the batched chains' tile shape at first use (default on)."""
         check(self.L.vca_gpu_set_autotune(1 if on else 0))
+
+    def set_stage_extra_tx(self, nbytes: int):
+        """Test hook: make the chains' H x v bulk-copy wait run out (0 = off)."""
+        check(self.L.vca_gpu_set_stage_extra_tx(int(nbytes)))
 
     def set_chain_streams(self, n: int):
         """Chain column groups in flight at a time (1 or 2, default 1)."""
