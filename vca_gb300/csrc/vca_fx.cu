@@ -48,6 +48,12 @@ __device__ __forceinline__ i64 rshift_round63(i128 p, int s) {
   return (i64)((lo >> s) | (hi << (64 - s)));
 }
 
+// either form by a uniform flag (sh63: 1 <= s <= 63, the two-word form)
+__device__ __forceinline__ i64 rshift_round_u(i128 p, int s, bool sh63) {
+  if (sh63) return rshift_round63(p, s);
+  return rshift_round(p, s);
+}
+
 __device__ __forceinline__ double i128_to_double(i128 v, int scale_exp) {
   const bool neg = v < 0;
   unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
@@ -362,6 +368,7 @@ __global__ void __launch_bounds__(FX1_UP2_THREADS, 1) k_hxv1_up2(SectorView sv, 
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int nw = (DU + 31) >> 5;
+  const bool sh63 = fv.shift >= 1 && fv.shift <= 63;
   const i64 e1d0 = fv.dw_e1[idw0], e1d1 = two ? fv.dw_e1[idw0 + 1] : 0;
   const unsigned wd0 = (unsigned)sv.dw_words[idw0], wd1 = two ? (unsigned)sv.dw_words[idw0 + 1] : 0u;
   for (int w = threadIdx.x >> 5; w < nw; w += FX1_UP2_THREADS / 32) {
@@ -376,12 +383,12 @@ __global__ void __launch_bounds__(FX1_UP2_THREADS, 1) k_hxv1_up2(SectorView sv, 
     i128 p0 = (i128)(eu + e1d0 + mixed_fx(fv, wu, wd0)) * xi.x;
 #pragma unroll
     for (int k = 0; k < K; k++) p0 += (i128)fv.afx[k] * (i64)A[k];
-    __stcs((long long*)Y + (int64_t)idw0 * DU + iup, (long long)rshift_round(p0, fv.shift));
+    __stcs((long long*)Y + (int64_t)idw0 * DU + iup, (long long)rshift_round_u(p0, fv.shift, sh63));
     if (two) {
       i128 p1 = (i128)(eu + e1d1 + mixed_fx(fv, wu, wd1)) * xi.y;
 #pragma unroll
       for (int k = 0; k < K; k++) p1 += (i128)fv.afx[k] * (i64)B[k];
-      __stcs((long long*)Y + (int64_t)(idw0 + 1) * DU + iup, (long long)rshift_round(p1, fv.shift));
+      __stcs((long long*)Y + (int64_t)(idw0 + 1) * DU + iup, (long long)rshift_round_u(p1, fv.shift, sh63));
     }
   }
 }
@@ -436,8 +443,9 @@ __global__ void __launch_bounds__(FX1_DW2_ROWS / 2) k_hxv1_dw2(SectorView sv, Fx
     i128 pa = 0, pb = 0;
 #pragma unroll
     for (int k = 0; k < K; k++) pa += (i128)fv.afx[k] * (i64)A[k], pb += (i128)fv.afx[k] * (i64)B[k];
-    __stcs(Yb + q, make_longlong2((long long)((i64)y.x + rshift_round(pa, fv.shift)),
-                                  (long long)((i64)y.y + rshift_round(pb, fv.shift))));
+    const bool sh63 = fv.shift >= 1 && fv.shift <= 63;
+    __stcs(Yb + q, make_longlong2((long long)((i64)y.x + rshift_round_u(pa, fv.shift, sh63)),
+                                  (long long)((i64)y.y + rshift_round_u(pb, fv.shift, sh63))));
   }
 }
 
@@ -1822,8 +1830,9 @@ __global__ void __launch_bounds__(FX1_UP2_THREADS, 1) k_hxv_slab_up2(SectorView 
     i128 p0 = (i128)d * xi.x, p1 = (i128)d * xi.y;
 #pragma unroll
     for (int k = 0; k < K; k++) p0 += (i128)fv.afx[k] * (i64)A[k], p1 += (i128)fv.afx[k] * (i64)B[k];
-    __stcg(Y2 + (int64_t)iup * 4, make_longlong2((long long)rshift_round(p0, fv.shift),
-                                                 (long long)rshift_round(p1, fv.shift)));
+    const bool sh63 = fv.shift >= 1 && fv.shift <= 63;
+    __stcg(Y2 + (int64_t)iup * 4, make_longlong2((long long)rshift_round_u(p0, fv.shift, sh63),
+                                                 (long long)rshift_round_u(p1, fv.shift, sh63)));
   }
 }
 
@@ -1873,8 +1882,9 @@ __global__ void __launch_bounds__(FXS_DW_ROWS * 4) k_hxv_slab_dw2(SectorView sv,
     i128 pa = 0, pb = 0;
 #pragma unroll
     for (int k = 0; k < K; k++) pa += (i128)fv.afx[k] * (i64)A[k], pb += (i128)fv.afx[k] * (i64)B[k];
-    __stcg(Y2 + own, make_longlong2((long long)((i64)y.x + rshift_round(pa, fv.shift)),
-                                    (long long)((i64)y.y + rshift_round(pb, fv.shift))));
+    const bool sh63 = fv.shift >= 1 && fv.shift <= 63;
+    __stcg(Y2 + own, make_longlong2((long long)((i64)y.x + rshift_round_u(pa, fv.shift, sh63)),
+                                    (long long)((i64)y.y + rshift_round_u(pb, fv.shift, sh63))));
   }
 }
 
