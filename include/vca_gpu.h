@@ -354,6 +354,21 @@ int vca_state_list_finite_t(const double* E, int32_t nsectors, const vca_config*
  * Z = NULL.  They stand in for SciFortran's sp_eigh/eigh (VCA_DIAG.f90:
  * 153-170) on the Ritz problem and below LANC_DIM_THRESHOLD. */
 int vca_tridiag_eig(int32_t n, const double* d, const double* e, double* w, double* Z);
+/* The host-side hop orders of the fixed-point H x v, without a context or a
+ * GPU.  vca_hop_schedule: the bank schedule of the paired-column kernel for
+ * one spin space of dim configurations (hop words src | class << 24 |
+ * sign << 31, width per row, k-major [h*dim + row]; cnt per row): warp w's
+ * rounds start at wround[w] (nwarps + 1 entries) in groups of one class and
+ * sign with wgrp[w*2K + g] rounds each; sched holds 32 words per round, the
+ * byte offset (16 per unit) of the 16-byte unit each lane reads, units >= dim
+ * being the zero units of idle lanes; *nrounds = total rounds, *conflicts =
+ * quarter-warp rounds left with a bank conflict.  vca_hop_parity_order: the
+ * chains' kernel's up hops (the same word layout, sign sorted, npos
+ * positive ones per row) re-ordered in place so that rows 2i and 2i+1 read
+ * sources of opposite parity where the counts allow. */
+int vca_hop_schedule(int32_t dim, int32_t width, int32_t K, const int32_t* cnt, const uint32_t* hop, uint32_t* sched,
+                     int64_t sched_cap, int32_t* wround, int32_t* wgrp, int64_t* nrounds, int64_t* conflicts);
+int vca_hop_parity_order(int32_t dim, int32_t width, const int32_t* cnt, const int32_t* npos, uint32_t* rhop);
 int vca_herm_eig(int32_t n, const double* A, double* w, double* Z);
 
 /* Omega integrand f(w) = (1/Lk) sum_k ln|det(1+(Delta+Hloc-Hk)G'(iw))|

@@ -4426,6 +4426,29 @@ int vca_gpu_synchronize(void) {
   return VCA_OK;
 }
 
+int vca_hop_schedule(int32_t dim, int32_t width, int32_t K, const int32_t* cnt, const uint32_t* hop, uint32_t* sched,
+                     int64_t sched_cap, int32_t* wround, int32_t* wgrp, int64_t* nrounds, int64_t* conflicts) {
+  if (dim < 1 || width < 0 || K < 1 || K > VCA_FX_KMAX || !cnt || (width > 0 && !hop) || !wround || !wgrp ||
+      !nrounds || sched_cap < 0 || (sched_cap > 0 && !sched))
+    return set_error(VCA_ERR_ARG, "bad arguments");
+  std::vector<unsigned> sc;
+  std::vector<int> wr, wg;
+  const int64_t nc = fx_pair_schedule(dim, width, K, cnt, hop, sc, wr, wg);
+  if (nc < 0) return set_error(VCA_ERR_NUMERIC, "a hop was left unplaced");
+  *nrounds = wr.back();
+  if (conflicts) *conflicts = nc;
+  std::memcpy(wround, wr.data(), sizeof(int) * wr.size());
+  std::memcpy(wgrp, wg.data(), sizeof(int) * wg.size());
+  std::memcpy(sched, sc.data(), sizeof(unsigned) * std::min<size_t>(sc.size(), (size_t)sched_cap));
+  return VCA_OK;
+}
+
+int vca_hop_parity_order(int32_t dim, int32_t width, const int32_t* cnt, const int32_t* npos, uint32_t* rhop) {
+  if (dim < 1 || width < 0 || !cnt || !npos || (width > 0 && !rhop)) return set_error(VCA_ERR_ARG, "bad arguments");
+  fx_rhop_parity_order(dim, width, cnt, npos, rhop);
+  return VCA_OK;
+}
+
 int vca_gpu_set_chain_streams(int32_t n) {
   if (!g) VFAIL(VCA_ERR_STATE, "vca_gpu_init has not been called");
   if (n < 1 || n > 2) VFAIL(VCA_ERR_ARG, "1 or 2 chain streams");

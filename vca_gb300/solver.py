@@ -45,7 +45,7 @@ EXPORTS = [
     "vca_gpu_save_gfprime", "vca_gpu_read_gfprime", "vca_gfm_write", "vca_gfm_read",
     "vca_gpu_print_impSigma", "vca_gpu_print_impG", "vca_gpu_print_impG0",
     "vca_state_list_t0", "vca_state_list_finite_t", "vca_pair_kpoints", "vca_contour_rule",
-    "vca_tridiag_eig", "vca_herm_eig", "vca_gpu_sector_pairs",
+    "vca_tridiag_eig", "vca_herm_eig", "vca_gpu_sector_pairs", "vca_hop_schedule", "vca_hop_parity_order",
     "vca_read_impSigma", "vca_splot_read",
     "vca_mlp_config_defaults", "vca_mlp_init", "vca_mlp_finalize", "vca_mlp_param_count",
     "vca_mlp_get_params", "vca_mlp_set_params", "vca_mlp_set_data", "vca_mlp_loss_grad", "vca_mlp_train",
@@ -149,6 +149,9 @@ def load(path: Optional[str] = None):
                                                    ctypes.POINTER(i32), dp, dp, ctypes.POINTER(i32)]),
         "vca_pair_kpoints": (ctypes.c_int, [dp, i64, i64, ctypes.POINTER(i64), dp, i64, ctypes.POINTER(i64)]),
         "vca_tridiag_eig": (ctypes.c_int, [i32, dp, dp, dp, dp]),
+        "vca_hop_schedule": (ctypes.c_int, [i32, i32, i32, vp, vp, vp, i64, vp, vp, ctypes.POINTER(i64),
+                                            ctypes.POINTER(i64)]),
+        "vca_hop_parity_order": (ctypes.c_int, [i32, i32, vp, vp, vp]),
         "vca_gpu_sector_pairs": (ctypes.c_int, [i32, i32, dp, dp, ctypes.POINTER(i32)]),
         "vca_herm_eig": (ctypes.c_int, [i32, dp, dp, dp]),
         "vca_contour_rule": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, i32, dp, dp, i32,
@@ -608,6 +611,38 @@ def tridiag_eig(d, e):
     Z = np.zeros(n * n)
     check(load().vca_tridiag_eig(n, _dp(d), _dp(e), _dp(w), _dp(Z)))
     return w, Z.reshape(n, n).T
+
+
+def hop_schedule(cnt, hop, K: int = 1):
+    """(sched words [rounds, 32], wround, wgrp [nwarps, 2K], conflicts): the
+    paired-column kernel's bank schedule of one spin space (host)."""
+    cnt = np.ascontiguousarray(cnt, dtype=np.int32)
+    hop = np.ascontiguousarray(hop, dtype=np.uint32)  # [width, dim]
+    dim = len(cnt)
+    width = hop.shape[0]
+    nw = (dim + 31) // 32
+    wround = np.zeros(nw + 1, dtype=np.int32)
+    wgrp = np.zeros(nw * 2 * K, dtype=np.int32)
+    cap = int(nw * 2 * max(1, width) * 32)
+    sched = np.zeros(cap, dtype=np.uint32)
+    nr, nc = ctypes.c_int64(), ctypes.c_int64()
+    vp_ = ctypes.c_void_p
+    check(load().vca_hop_schedule(dim, width, K, vp_(cnt.ctypes.data), vp_(hop.ctypes.data), vp_(sched.ctypes.data),
+                                  cap, vp_(wround.ctypes.data), vp_(wgrp.ctypes.data), ctypes.byref(nr),
+                                  ctypes.byref(nc)))
+    return sched[:nr.value * 32].reshape(nr.value, 32), wround, wgrp.reshape(nw, 2 * K), nc.value
+
+
+def hop_parity_order(cnt, npos, rhop):
+    """The chains' kernel's up hops re-ordered for bank pairing (host); rhop
+    [width, dim] is modified in place and returned."""
+    cnt = np.ascontiguousarray(cnt, dtype=np.int32)
+    npos = np.ascontiguousarray(npos, dtype=np.int32)
+    assert rhop.dtype == np.uint32 and rhop.flags["C_CONTIGUOUS"]
+    vp_ = ctypes.c_void_p
+    check(load().vca_hop_parity_order(len(cnt), rhop.shape[0], vp_(cnt.ctypes.data), vp_(npos.ctypes.data),
+                                      vp_(rhop.ctypes.data)))
+    return rhop
 
 
 def herm_eig(A):
