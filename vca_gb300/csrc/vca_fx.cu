@@ -1561,7 +1561,7 @@ __global__ void __launch_bounds__(FXR_THREADS, 4) k_hxv_fx_r(SectorView sv, FxVi
   const int nd = sv.dw_cnt[idw];
   const int ndp = fv.dw_npos[idw];
   // the own block (DU x 64 contiguous bytes) by one bulk copy, the down-hop
-  // table meanwhile; thread 0 waits (bounded) and the CTA follows its verdict
+  // table meanwhile; thread 0 waits (bounded) and the CTA follows its outcome
   __shared__ int stage_ok;
   const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(sbar);
   if (threadIdx.x == 0)

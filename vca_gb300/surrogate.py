@@ -5,8 +5,8 @@ the stationary-point search.
 The reference searches with scalar minimisers around ``vca_solve``
 (``brent`` in drivers/vca_hm_chain1d.f90:104-108, ``fmin_bfgs``/``fmin`` in
 drivers/vca_bhz_2d.f90:244-305); here the network proposes, and every
-accepted point is re-solved by the plain solver, which is both judge and
-fallback.
+accepted point is re-solved by the plain solver, which both decides and
+stands in.
 
 ``SurrogateNet`` drives the C-ABI ``vca_mlp_*`` entry points (CUDA kernels in
 vca_gb300/csrc/vca_mlp.cu, tensor-core GEMMs in vca_umma.cu); it scales the
@@ -282,8 +282,8 @@ def surrogate_search(f, lo, hi, p0, n_design=6, h_frac=1e-3, rounds=8, steps=300
     the network's stationary point (Newton on the network from the last
     proposal), re-solves it by the plain path together with its gradient
     from d forward differences of plain solves, adds that value and gradient
-    to the training set (the Sobolev term), and refits.  The plain solver is
-    the judge: the search stops when the measured gradient g at a proposal,
+    to the training set (the Sobolev term), and refits.  The plain solver
+    decides: the search stops when the measured gradient g at a proposal,
     through the network's curvature H there, puts it within
     |1/2 g^T H^-1 g| < omega_tol of the stationary value.  Returns the last
     verified point, its plain Omega, and per round the surrogate's error."""
