@@ -540,3 +540,23 @@ def test_delta_bath_is_the_reference_formula():
         for x in (0.4j, 1.5 + 0.2j, -3.0 + 1.0j):
             ref = V @ np.linalg.inv((x + c.xmu) * np.eye(len(hl)) - hl) @ V.conj().T
             np.testing.assert_allclose(o.delta_bath(x), ref, rtol=0, atol=1e-13)
+
+
+def test_timed_solve_and_chain_sample():
+    """The oracle entries behind the CPU baseline: solve_timed gives the
+    solve's Omega with non-negative stage times that sum to at most the
+    wall time, and chain_sample runs one chain per thread on a sector."""
+    import time
+    from vca_gb300 import clusters
+    from oracle.oracle import Oracle
+    pt = clusters.square(nx=2, ny=2, U=8.0, xmu=4.0, maf=0.1, nspin=2, nkx=4, nky=4, ngfiter=40, omega_nodes=64)
+    ref = Oracle.from_point(pt).solve()[0]
+    t0 = time.perf_counter()
+    om, _, _, st = Oracle.from_point(pt).solve_timed()
+    wall = time.perf_counter() - t0
+    assert om == ref
+    assert len(st) == 3 and min(st) >= 0.0 and sum(st) <= wall + 1e-3
+    o = Oracle.from_point(pt)
+    isec = 1 + 2 + 2 * 5  # sector (2,2): 36 states
+    dt = o.chain_sample(isec, 4, 20)
+    assert 0.0 <= dt < 10.0
