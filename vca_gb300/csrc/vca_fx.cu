@@ -793,19 +793,32 @@ __global__ void __launch_bounds__(256) k_fx_apply8(int64_t rows, int m, const in
     }
   }
   if (!wr[0] && !wr[1]) return;
+  const bool s63a = sv[0] >= 1 && sv[0] <= 63, s63b = sv[1] >= 1 && sv[1] <= 63;
   const int64_t sb = (int64_t)blockIdx.y * rows * (FX_SLAB / 2) + tx;
   const longlong2* I2 = (const longlong2*)Xi + sb;
   longlong2* O2 = (longlong2*)Xo + sb;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.y + ty; i < rows; i += (int64_t)gridDim.x * blockDim.y) {
-    const longlong2 v = I2[i * 4];
-    const i64 o0 = rshift_round((i128)mu[0] * v.x, sv[0]);
-    const i64 o1 = rshift_round((i128)mu[1] * v.y, sv[1]);
-    if (wr[0] && wr[1]) {
-      O2[i * 4] = make_longlong2(o0, o1);
-    } else {
-      i64* o = (i64*)(O2 + i * 4);
-      if (wr[0]) o[0] = o0;
-      if (wr[1]) o[1] = o1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.y;
+  constexpr int U = 4;  // rows in flight per thread
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.y + ty; i0 < rows; i0 += U * stride) {
+    longlong2 v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int64_t i = i0 + u * stride;
+      v[u] = i < rows ? I2[i * 4] : make_longlong2(0ll, 0ll);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int64_t i = i0 + u * stride;
+      if (i >= rows) break;
+      const i64 o0 = s63a ? rshift_round63((i128)mu[0] * v[u].x, sv[0]) : rshift_round((i128)mu[0] * v[u].x, sv[0]);
+      const i64 o1 = s63b ? rshift_round63((i128)mu[1] * v[u].y, sv[1]) : rshift_round((i128)mu[1] * v[u].y, sv[1]);
+      if (wr[0] && wr[1]) {
+        O2[i * 4] = make_longlong2(o0, o1);
+      } else {
+        i64* o = (i64*)(O2 + i * 4);
+        if (wr[0]) o[0] = o0;
+        if (wr[1]) o[1] = o1;
+      }
     }
   }
 }
