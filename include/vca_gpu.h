@@ -465,6 +465,9 @@ int vca_gpu_hxv_timed(int32_t isector, const void* d_v, void* d_hv, int32_t is_c
  * race.  No counterpart in the reference. */
 int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void* d_hv, int32_t ncols,
                               double* d_alpha);
+/* (Device vectors passed to the H x v entry points must be 16-byte aligned,
+ * as cudaMalloc and torch allocations are; others are rejected with
+ * VCA_ERR_ARG.) */
 
 /* ---- residency and diagnostics (no counterpart in the reference) -------- */
 /* Upload Hk (as in vca_gpu_solve) and keep it resident on the device. */

@@ -4543,6 +4543,7 @@ extern "C" int vca_gpu_hxv_alpha_noalloc(int32_t isector, const void* d_v, void*
   if (!g || !g->ham_set) VFAIL(VCA_ERR_STATE, "no Hamiltonian loaded (vca_gpu_set_hamiltonian)");
   if (isector < 1 || isector > g->Nsectors) VFAIL(VCA_ERR_ARG, "sector out of range");
   if (ncols < 1 || !d_v || !d_hv || !d_alpha) VFAIL(VCA_ERR_ARG, "bad arguments");
+  if ((((uintptr_t)d_v) | ((uintptr_t)d_hv)) & 15u) VFAIL(VCA_ERR_ARG, "device vectors must be 16-byte aligned");
   if (!g->real_model) VFAIL(VCA_ERR_UNSUPPORTED, "real columns need a real Hamiltonian");
   const int nup = sec_nup(isector), ndw = sec_ndw(isector);
   const SectorView sv = view_of(nup, ndw);
